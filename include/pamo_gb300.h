@@ -1,0 +1,98 @@
+/*
+ * pamo_gb300 — C ABI of the GB300-native PaMO stage-2 simplifier (parallel QEM edge collapse with LBVH
+ * self-intersection rollback).
+ *
+ * Every pointer argument named points/triangles/verts/tris/verts_* is a DEVICE pointer on the context's
+ * GPU unless stated otherwise; sizes are element counts (points = rows of 3 float32, triangles = rows of 3
+ * int32). Every call returns a pamo_status; the message of the last failure is pamo_ctx_last_error().
+ * A context is not thread-safe: use one context per host thread / stream.
+ */
+#ifndef PAMO_GB300_H
+#define PAMO_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct pamo_ctx pamo_ctx;
+typedef void* pamo_stream; /* a cudaStream_t; NULL is the legacy default stream */
+
+typedef enum pamo_status {
+    PAMO_OK = 0,
+    PAMO_ERR_INVALID_ARG = 1, /* bad size, null pointer or out-of-range vertex index */
+    PAMO_ERR_OOM = 2,         /* device allocation failed */
+    PAMO_ERR_CAPACITY = 3,    /* an internal list overflowed (reported, never clipped silently) */
+    PAMO_ERR_ITER_LIMIT = 4,  /* a bounded device loop or traversal ran out of room */
+    PAMO_ERR_CUDA = 5,        /* a CUDA runtime call failed */
+    PAMO_ERR_STATE = 6        /* call order: e.g. outputs requested before a round ran */
+} pamo_status;
+
+const char* pamo_status_string(int status);
+
+/* Create a context on CUDA device `device`. Replaces the default construction of the reference's
+ * pybind class CUDSP_Free (simp_cuda/src/pybind.cpp:16-19, 189-193). */
+int pamo_ctx_create(pamo_ctx** out, int device);
+
+/* Release every device buffer of the context (simp_cuda/src/pybind.cpp:21-49). */
+int pamo_ctx_destroy(pamo_ctx* ctx);
+
+/* Message of the last failed call on this context ("" when none). */
+const char* pamo_ctx_last_error(const pamo_ctx* ctx);
+
+/*
+ * One simplification round: CUDSP_Free.forward(points, triangles, verts_undo, n_verts_undo, scale,
+ * threshold, is_stuck, init) (simp_cuda/src/pybind.cpp:52-72 -> CUSimp_Free::forward,
+ * simp_cuda/src/cusimp_free.cu:891-1048). Inputs are only read. State that the reference keeps between
+ * calls (stale edge costs, the invalid-vertex table, the previous compaction map, the undo list) is kept
+ * in the context with the same semantics. Synchronises `stream` before returning.
+ */
+int pamo_forward_round(pamo_ctx* ctx, const float* points, const int32_t* triangles, const int32_t* verts_undo,
+                       int32_t n_verts_undo, int32_t n_points, int32_t n_triangles, float scale, float threshold,
+                       int32_t is_stuck, int32_t init, pamo_stream stream);
+
+/* Shapes of the five outputs of the last round: verts [n_points,3], tris [n_triangles,3],
+ * verts_occ [n_points,1], verts_map [n_points,1], verts_undo [n_verts_undo] (simp_cuda/src/pybind.cpp:74-102). */
+int pamo_round_sizes(const pamo_ctx* ctx, int32_t* n_points, int32_t* n_triangles, int32_t* n_verts_undo);
+
+/* Copy the last round's outputs into caller-owned device buffers (any may be NULL to skip it). Removed
+ * faces are (-1, -1, -1); verts_map is the exclusive scan of verts_occ. */
+int pamo_round_outputs(pamo_ctx* ctx, float* verts, int32_t* tris, int32_t* verts_occ, int32_t* verts_map,
+                       int32_t* verts_undo, pamo_stream stream);
+
+/* Diagnostics of the last round, written to out[0..n): n_edges, n_win, n_collapsed, n_considered,
+ * n_query, passes, n_vertices_undo, status bits, candidate pairs, fp64 pairs, undo per pass [8]. */
+int pamo_round_stats(const pamo_ctx* ctx, int64_t* out, int32_t n);
+
+/*
+ * The whole stage-2 loop of PaMO.run(points, triangles, ratio, tolerance, threshold, iter, min_verts) with
+ * stage 1 and stage 3 off (simp_cuda/pamo/__init__.py:95-163): centring by the mean of the face centroids,
+ * rounds with compaction on the device, stuck/tolerance termination. Results stay in the context; fetch
+ * them with pamo_simplify_result. Returns the output sizes and the number of rounds run.
+ */
+int pamo_simplify_device(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                         int32_t n_triangles, double ratio, int32_t tolerance, float threshold, int32_t iter,
+                         int64_t min_verts, int32_t* out_n_points, int32_t* out_n_triangles, int32_t* out_rounds,
+                         pamo_stream stream);
+
+/* Copy the result of pamo_simplify_device (centring undone, as the reference's run() returns it). */
+int pamo_simplify_result(pamo_ctx* ctx, float* verts, int32_t* tris, pamo_stream stream);
+
+/* Face count after each round of the last pamo_simplify_device call (host array of `capacity`). */
+int pamo_simplify_round_faces(const pamo_ctx* ctx, int32_t* faces_per_round, int32_t capacity);
+
+/* Phase timers: when enabled, CUDA events on the call's stream bracket each phase of every round
+ * (0 load/shuffle, 1 adjacency, 2 quadrics, 3 edge cost, 4 selection+collapse, 5 cleanup+query marks,
+ * 6 LBVH build, 7 LBVH query + pair tests, 8 undo, 9 compaction, 10 centring). Enabling resets them.
+ * No reference counterpart (the reference only prints wall-clock times, simp_cuda/pamo/__init__.py:121,160). */
+int pamo_profile_enable(pamo_ctx* ctx, int32_t enable);
+
+/* Accumulated milliseconds and launch counts per phase; returns the number of phases. */
+int pamo_profile_read(const pamo_ctx* ctx, double* ms, int64_t* counts, int32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PAMO_GB300_H */

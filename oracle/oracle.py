@@ -1,0 +1,135 @@
+"""ctypes wrapper of the CPU oracle (oracle/pamo_oracle.cpp).
+
+Test infrastructure only: used as the checker by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline; the product path never imports it.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import build as _build
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        L = ctypes.CDLL(_build.build())
+        P, I, F, D, LL = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_double, ctypes.c_longlong
+        L.oracle_create.restype = P
+        L.oracle_destroy.argtypes = [P]
+        L.oracle_set_threads.argtypes = [P, I]
+        L.oracle_forward.argtypes = [P, P, P, P, I, I, I, F, F, I, I]
+        L.oracle_counts.argtypes = [P, P]
+        L.oracle_outputs.argtypes = [P, P, P, P, P, P]
+        L.oracle_collapsed.argtypes = [P, P]
+        L.oracle_edge_costs.argtypes = [P, P]
+        L.oracle_edges.argtypes = [P, P]
+        L.oracle_shuffle_perm.argtypes = [LL, P]
+        L.oracle_pair_intersects.argtypes = [P, P, P, F]
+        L.oracle_tris_mean.argtypes = [P, P, I, P]
+        L.oracle_run.argtypes = [P, P, P, I, I, D, I, F, I, LL, P, P]
+        L.oracle_run_result.argtypes = [P, P, P, P]
+        _LIB = L
+    return _LIB
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def shuffle_perm(m: int) -> np.ndarray:
+    out = np.zeros(m, np.int32)
+    lib().oracle_shuffle_perm(m, _p(out))
+    return out
+
+
+def pair_intersects(points: np.ndarray, cur, qry, eps: float = 1e-3) -> bool:
+    pts = np.ascontiguousarray(points, np.float32)
+    c = np.ascontiguousarray(cur, np.int32)
+    q = np.ascontiguousarray(qry, np.int32)
+    return bool(lib().oracle_pair_intersects(_p(pts), _p(c), _p(q), eps))
+
+
+def tris_mean(points: np.ndarray, tris: np.ndarray) -> np.ndarray:
+    out = np.zeros(3, np.float32)
+    p = np.ascontiguousarray(points, np.float32)
+    t = np.ascontiguousarray(tris, np.int32)
+    lib().oracle_tris_mean(_p(p), _p(t), len(t), _p(out))
+    return out
+
+
+class Oracle:
+    """Stateful CPU restatement of one reference CUSimp_Free (simp_cuda/src/cusimp_free.cu:891-1048)."""
+
+    COUNT_KEYS = ["n_pts", "n_tris", "n_vertices_undo", "n_edges", "n_win", "n_collapsed", "n_considered", "passes",
+                  "n_intersect_pairs", "status"]
+
+    def __init__(self, threads: int = 1):
+        self._h = ctypes.c_void_p(lib().oracle_create())
+        lib().oracle_set_threads(self._h, threads)
+
+    def __del__(self):
+        try:
+            if self._h:
+                lib().oracle_destroy(self._h)
+        except Exception:
+            pass
+
+    def forward(self, points, triangles, verts_undo, n_verts_undo, scale, threshold, is_stuck, init):
+        pts = np.ascontiguousarray(points, np.float32)
+        tri = np.ascontiguousarray(triangles, np.int32)
+        und = np.ascontiguousarray(verts_undo, np.int32)
+        if und.size == 0:
+            und = np.zeros(1, np.int32)
+        lib().oracle_forward(self._h, _p(pts), _p(tri), _p(und), int(n_verts_undo), len(pts), len(tri), float(scale),
+                             float(threshold), int(bool(is_stuck)), int(bool(init)))
+        c = self.counts()
+        nP, nT, nU = c["n_pts"], c["n_tris"], c["n_vertices_undo"]
+        verts = np.zeros((nP, 3), np.float32)
+        tris = np.zeros((nT, 3), np.int32)
+        occ = np.zeros((nP, 1), np.int32)
+        vmap = np.zeros((nP, 1), np.int32)
+        undo = np.zeros(max(nU, 1), np.int32)
+        lib().oracle_outputs(self._h, _p(verts), _p(tris), _p(occ), _p(vmap), _p(undo))
+        return verts, tris, occ, vmap, undo[:nU]
+
+    def counts(self) -> dict:
+        c = np.zeros(10, np.int64)
+        lib().oracle_counts(self._h, _p(c))
+        return {k: int(v) for k, v in zip(self.COUNT_KEYS, c)}
+
+    def collapsed(self) -> np.ndarray:
+        n = self.counts()["n_collapsed"]
+        out = np.zeros(max(n, 1), np.int32)
+        lib().oracle_collapsed(self._h, _p(out))
+        return out[:n]
+
+    def edges(self) -> np.ndarray:
+        n = self.counts()["n_edges"]
+        out = np.zeros((max(n, 1), 2), np.int32)
+        lib().oracle_edges(self._h, _p(out))
+        return out[:n]
+
+    def edge_costs(self) -> np.ndarray:
+        n = self.counts()["n_edges"]
+        out = np.zeros(max(n, 1), np.uint32)
+        lib().oracle_edge_costs(self._h, _p(out))
+        return out[:n]
+
+    def run(self, points, triangles, ratio, tolerance=4, threshold=1e-3, iters=1000000, min_verts=10000000000):
+        """The stage-2 loop of PaMO.run: returns (verts, faces, faces_per_round)."""
+        pts = np.ascontiguousarray(points, np.float32)
+        tri = np.ascontiguousarray(triangles, np.int32)
+        onp, ont = ctypes.c_int(), ctypes.c_int()
+        rounds = lib().oracle_run(self._h, _p(pts), _p(tri), len(pts), len(tri), float(ratio), int(tolerance),
+                                  float(threshold), int(iters), int(min_verts), ctypes.byref(onp), ctypes.byref(ont))
+        V = np.zeros((onp.value, 3), np.float32)
+        F = np.zeros((ont.value, 3), np.int32)
+        fpr = np.zeros(max(rounds, 1), np.int32)
+        lib().oracle_run_result(self._h, _p(V), _p(F), _p(fpr))
+        return V, F, fpr[:rounds]

@@ -1,0 +1,96 @@
+"""ctypes binding of the C ABI in include/pamo_gb300.h (the in-tree libpamo_gb300.so).
+
+There is no fallback: when the library is missing or cannot be loaded every entry point raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import _build
+
+PAMO_OK = 0
+STATUS_NAMES = {
+    0: "ok",
+    1: "invalid argument",
+    2: "out of device memory",
+    3: "capacity exceeded",
+    4: "iteration limit",
+    5: "CUDA error",
+    6: "invalid call order",
+}
+
+# every exported symbol of include/pamo_gb300.h with (restype, argtypes)
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_F32 = ctypes.c_float
+_F64 = ctypes.c_double
+_PI32 = ctypes.POINTER(ctypes.c_int32)
+_PI64 = ctypes.POINTER(ctypes.c_int64)
+
+SIGNATURES = {
+    "pamo_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "pamo_ctx_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int]),
+    "pamo_ctx_destroy": (ctypes.c_int, [_P]),
+    "pamo_ctx_last_error": (ctypes.c_char_p, [_P]),
+    "pamo_forward_round": (ctypes.c_int, [_P, _P, _P, _P, _I32, _I32, _I32, _F32, _F32, _I32, _I32, _P]),
+    "pamo_round_sizes": (ctypes.c_int, [_P, _PI32, _PI32, _PI32]),
+    "pamo_round_outputs": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
+    "pamo_round_stats": (ctypes.c_int, [_P, _PI64, _I32]),
+    "pamo_simplify_device": (
+        ctypes.c_int,
+        [_P, _P, _P, _I32, _I32, _F64, _I32, _F32, _I32, _I64, _PI32, _PI32, _PI32, _P],
+    ),
+    "pamo_simplify_result": (ctypes.c_int, [_P, _P, _P, _P]),
+    "pamo_simplify_round_faces": (ctypes.c_int, [_P, _PI32, _I32]),
+    "pamo_profile_enable": (ctypes.c_int, [_P, _I32]),
+    "pamo_profile_read": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _PI64, _I32]),
+}
+
+PHASES = ["load", "adjacency", "quadrics", "edge_cost", "collapse", "marks", "bvh_build", "bvh_query", "undo",
+          "compact", "center"]
+
+_LIB = None
+
+
+class PamoError(RuntimeError):
+    """A pamo_* call returned a non-zero status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"pamo: {STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def lib_path() -> str:
+    return _build.lib_path()
+
+
+def load() -> ctypes.CDLL:
+    """Load libpamo_gb300.so (raises when it has not been built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"pamo_gb300 CUDA library not found at {path}; build it with "
+            "`python -c 'import pamo_gb300._build as b; b.build()'` (requires nvcc)"
+        )
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(status: int, ctx=None) -> None:
+    if status != PAMO_OK:
+        msg = ""
+        if ctx is not None:
+            raw = load().pamo_ctx_last_error(ctx)
+            msg = raw.decode() if raw else ""
+        raise PamoError(status, msg)

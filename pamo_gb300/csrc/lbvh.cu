@@ -1,0 +1,423 @@
+// LBVH over live faces: AABBs and scene bounds, 30-bit Morton codes of box centroids, an in-house stable
+// LSD radix sort (8-bit digits, warp-match ranking), Karras (2012) topology with an index tie-break for
+// equal codes, bottom-up boxes, and a per-face query that walks the tree with a stack in shared memory and
+// runs the reference's pair test on every overlapping leaf.
+//
+// The tree only filters candidates: a (query f, hit g) pair is tested iff both faces are live, f != g and
+// their closed boxes overlap (simp_cuda/src/bvh/query.cuh:8-133, aabb.cuh:154-162), which is the candidate
+// set of the reference's global LBVH query.
+#include <cstdint>
+#include "lbvh.cuh"
+#include "scan.cuh"
+#include "tritri.cuh"
+
+namespace pamo {
+
+namespace {
+
+constexpr int kSortTiles = 4 * kNumSM;
+constexpr int kSortThreads = 256;
+constexpr int kQueryThreads = 128;
+constexpr int kStackDepth = 64;
+
+__device__ __forceinline__ unsigned f2ord(float f) {
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__device__ __forceinline__ unsigned expand10(unsigned v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__device__ __forceinline__ bool boxes_overlap(float4 alo, float4 ahi, float4 blo, float4 bhi) {
+    if (ahi.x < blo.x || bhi.x < alo.x) return false;
+    if (ahi.y < blo.y || bhi.y < alo.y) return false;
+    if (ahi.z < blo.z || bhi.z < alo.z) return false;
+    return true;
+}
+
+// ---------------------------------------------------------------- boxes + scene bounds
+__global__ void __launch_bounds__(256) k_boxes(const int4* __restrict__ tri, const float4* __restrict__ pos,
+                                                const RoundCounters* rc, float4* box_lo, float4* box_hi, int* live,
+                                                unsigned* scene) {
+    const int n = rc->n_tris;
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int f = gtid(); f < n; f += gstride()) {
+        int4 t = tri[f];
+        int is_live = (t.x != -1);
+        live[f] = is_live;
+        if (!is_live) continue;
+        float4 a = pos[t.x], b = pos[t.y], c = pos[t.z];
+        float4 lo = make_float4(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)), 0.f);
+        float4 hi = make_float4(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)), 0.f);
+        box_lo[f] = lo;
+        box_hi[f] = hi;
+        mn[0] = fminf(mn[0], lo.x); mn[1] = fminf(mn[1], lo.y); mn[2] = fminf(mn[2], lo.z);
+        mx[0] = fmaxf(mx[0], hi.x); mx[1] = fmaxf(mx[1], hi.y); mx[2] = fmaxf(mx[2], hi.z);
+    }
+    if (gtid() == 0) live[n] = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+            mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            if (mn[d] <= mx[d]) {
+                atomicMin(&scene[d], f2ord(mn[d]));
+                atomicMax(&scene[3 + d], f2ord(mx[d]));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- Morton codes of live faces
+__global__ void __launch_bounds__(256) k_morton(const RoundCounters* rc, const int* live_scan, const float4* box_lo,
+                                                 const float4* box_hi, const unsigned* scene, unsigned* keys, int* vals) {
+    const int n = rc->n_tris;
+    float lo[3], ext[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = ord2f(scene[d]);
+        float hi = ord2f(scene[3 + d]);
+        ext[d] = hi - lo[d];
+    }
+    for (int f = gtid(); f < n; f += gstride()) {
+        int i = live_scan[f];
+        if (live_scan[f + 1] == i) continue;
+        float4 a = box_lo[f], b = box_hi[f];
+        float c[3] = {(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f};
+        unsigned q[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            float t = ext[d] > 0.f ? (c[d] - lo[d]) / ext[d] : 0.f;
+            t = fminf(fmaxf(t * 1024.0f, 0.0f), 1023.0f);
+            q[d] = (unsigned)t;
+        }
+        keys[i] = expand10(q[0]) * 4u + expand10(q[1]) * 2u + expand10(q[2]);
+        vals[i] = f;
+    }
+}
+
+// ---------------------------------------------------------------- stable LSD radix sort
+__device__ __forceinline__ void sort_chunk(int n, int& lo, int& hi) {
+    long long chunk = ((long long)n + kSortTiles - 1) / kSortTiles;
+    chunk = (chunk + kSortThreads - 1) / kSortThreads * kSortThreads;
+    long long a = chunk * blockIdx.x, b = a + chunk;
+    lo = (int)(a < n ? a : n);
+    hi = (int)(b < n ? b : n);
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_rs_hist(const unsigned* __restrict__ keys, const int* d_n, int shift,
+                                                          int* hist) {
+    __shared__ int h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int lo, hi;
+    sort_chunk(*d_n, lo, hi);
+    for (int i = lo + threadIdx.x; i < hi; i += kSortThreads) atomicAdd(&h[(keys[i] >> shift) & 0xFF], 1);
+    __syncthreads();
+    hist[threadIdx.x * kSortTiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Each tile of 256 keys is ranked stably: lanes of a warp with the same digit find each other with
+// __match_any_sync, warps are ordered through per-warp digit counts in shared memory.
+__global__ void __launch_bounds__(kSortThreads) k_rs_scatter(const unsigned* __restrict__ kin, const int* __restrict__ vin,
+                                                             unsigned* kout, int* vout, const int* d_n, int shift,
+                                                             const int* hist) {
+    constexpr int W = kSortThreads / 32;
+    __shared__ int base[256];
+    __shared__ int wcnt[W][256];
+    __shared__ int tot[256];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    base[threadIdx.x] = hist[threadIdx.x * kSortTiles + blockIdx.x];
+    for (int w = 0; w < W; ++w) wcnt[w][threadIdx.x] = 0;
+    __syncthreads();
+    int lo, hi;
+    sort_chunk(*d_n, lo, hi);
+    for (int t0 = lo; t0 < hi; t0 += kSortThreads) {
+        const int i = t0 + threadIdx.x;
+        const bool valid = i < hi;
+        unsigned key = valid ? kin[i] : 0u;
+        int val = valid ? vin[i] : 0;
+        const int dig = valid ? (int)((key >> shift) & 0xFF) : 256;
+        const unsigned peers = __match_any_sync(0xffffffffu, dig);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && rank == 0) wcnt[warp][dig] = __popc(peers);
+        __syncthreads();
+        {
+            int run = 0;
+            for (int w = 0; w < W; ++w) {
+                int c = wcnt[w][threadIdx.x];
+                wcnt[w][threadIdx.x] = run;
+                run += c;
+            }
+            tot[threadIdx.x] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            const int dst = base[dig] + wcnt[warp][dig] + rank;
+            kout[dst] = key;
+            vout[dst] = val;
+        }
+        __syncthreads();
+        base[threadIdx.x] += tot[threadIdx.x];
+        for (int w = 0; w < W; ++w) wcnt[w][threadIdx.x] = 0;
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- Karras topology
+__device__ __forceinline__ int delta(const unsigned* k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    unsigned a = k[i], b = k[j];
+    if (a != b) return __clz(a ^ b);
+    return 32 + __clz((unsigned)(i ^ j));
+}
+
+__global__ void __launch_bounds__(256) k_leaves(const RoundCounters* rc, const int* vals, const float4* box_lo,
+                                                 const float4* box_hi, float4* llo, float4* lhi, int* visit, int* lparent) {
+    const int n = rc->n_live;
+    for (int i = gtid(); i < n; i += gstride()) {
+        int f = vals[i];
+        llo[i] = box_lo[f];
+        lhi[i] = box_hi[f];
+        if (i < n - 1) visit[i] = 0;
+        if (n == 1) lparent[0] = -1;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_karras(const RoundCounters* rc, const unsigned* keys, int2* child, int* iparent,
+                                                 int* lparent) {
+    const int n = rc->n_live;
+    for (int i = gtid(); i < n - 1; i += gstride()) {
+        const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+        const int dmin = delta(keys, n, i, i - d);
+        int lmax = 2;
+        while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+        int l = 0;
+        for (int t = lmax >> 1; t >= 1; t >>= 1)
+            if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+        const int j = i + l * d;
+        const int dnode = delta(keys, n, i, j);
+        int s = 0;
+        int t = l;
+        do {
+            t = (t + 1) >> 1;
+            if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+        } while (t > 1);
+        const int gamma = i + s * d + (d < 0 ? -1 : 0);
+        const int lo = min(i, j), hi = max(i, j);
+        int left, right;
+        if (lo == gamma) {
+            left = ~gamma;
+            lparent[gamma] = i;
+        } else {
+            left = gamma;
+            iparent[gamma] = i;
+        }
+        if (hi == gamma + 1) {
+            right = ~(gamma + 1);
+            lparent[gamma + 1] = i;
+        } else {
+            right = gamma + 1;
+            iparent[gamma + 1] = i;
+        }
+        child[i] = make_int2(left, right);
+        if (i == 0) iparent[0] = -1;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_bottom_up(RoundCounters* rc, const int2* child, const int* iparent,
+                                                    const int* lparent, const float4* llo, const float4* lhi,
+                                                    float4* nlo, float4* nhi, int* visit) {
+    const int n = rc->n_live;
+    for (int i = gtid(); i < n; i += gstride()) {
+        int p = lparent[i];
+        int guard = 0;
+        while (p >= 0) {
+            __threadfence();
+            if (atomicAdd(&visit[p], 1) == 0) break;
+            const int2 c = child[p];
+            float4 alo, ahi, blo, bhi;
+            if (c.x < 0) { alo = __ldcg(&llo[~c.x]); ahi = __ldcg(&lhi[~c.x]); }
+            else { alo = __ldcg(&nlo[c.x]); ahi = __ldcg(&nhi[c.x]); }
+            if (c.y < 0) { blo = __ldcg(&llo[~c.y]); bhi = __ldcg(&lhi[~c.y]); }
+            else { blo = __ldcg(&nlo[c.y]); bhi = __ldcg(&nhi[c.y]); }
+            __stcg(&nlo[p], make_float4(fminf(alo.x, blo.x), fminf(alo.y, blo.y), fminf(alo.z, blo.z), 0.f));
+            __stcg(&nhi[p], make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y), fmaxf(ahi.z, bhi.z), 0.f));
+            p = iparent[p];
+            if (++guard > 4096) {
+                atomicOr(&rc->status, kErrIterLimit);
+                break;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- localized query
+__global__ void __launch_bounds__(kQueryThreads) k_query(const int2* __restrict__ child, const float4* __restrict__ nlo,
+                                                          const float4* __restrict__ nhi, const float4* __restrict__ llo,
+                                                          const float4* __restrict__ lhi, const int* __restrict__ leaf_face,
+                                                          const float4* __restrict__ box_lo, const float4* __restrict__ box_hi,
+                                                          const int4* __restrict__ tri, const float4* __restrict__ pos,
+                                                          const int* __restrict__ qlist, unsigned char* hit,
+                                                          RoundCounters* rc, float eps) {
+    __shared__ int stack[kStackDepth][kQueryThreads];
+    const int nq = rc->n_query;
+    const int nl = rc->n_live;
+    unsigned long long pairs = 0;
+    unsigned exact = 0;
+    for (int qi = gtid(); qi < nq; qi += gstride()) {
+        const int f = qlist[qi];
+        const int4 qt = tri[f];
+        if (qt.x == -1 || nl < 2) continue;
+        const float4 q0 = pos[qt.x], q1 = pos[qt.y], q2 = pos[qt.z];
+        const float4 qlo = box_lo[f], qhi = box_hi[f];
+        bool found = false;
+        int sp = 0;
+        int node = 0;
+        int guard = 0;
+        while (true) {
+            if (++guard > (1 << 22)) {
+                atomicOr(&rc->status, kErrIterLimit);
+                break;
+            }
+            const int2 c = child[node];
+            int next[2];
+            int nn = 0;
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                const int x = side == 0 ? c.x : c.y;
+                if (x < 0) {
+                    const int li = ~x;
+                    if (!boxes_overlap(qlo, qhi, llo[li], lhi[li])) continue;
+                    const int g = leaf_face[li];
+                    if (g == f) continue;
+                    const int4 gt = tri[g];
+                    const float4 g0 = pos[gt.x], g1 = pos[gt.y], g2 = pos[gt.z];
+                    ++pairs;
+                    if (pair_intersects(g0, g1, g2, gt, q0, q1, q2, qt, eps, exact) ||
+                        pair_intersects(q0, q1, q2, qt, g0, g1, g2, gt, eps, exact)) {
+                        found = true;
+                        break;
+                    }
+                } else {
+                    if (boxes_overlap(qlo, qhi, nlo[x], nhi[x])) next[nn++] = x;
+                }
+            }
+            if (found) break;
+            if (nn == 2) {
+                if (sp >= kStackDepth) {
+                    atomicOr(&rc->status, kErrStackOverflow);
+                    break;
+                }
+                stack[sp++][threadIdx.x] = next[1];
+                node = next[0];
+            } else if (nn == 1) {
+                node = next[0];
+            } else {
+                if (sp == 0) break;
+                node = stack[--sp][threadIdx.x];
+            }
+        }
+        if (found) hit[f] = 1;
+    }
+    // diagnostics: warp-aggregated counters
+    for (int o = 16; o > 0; o >>= 1) {
+        pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+        exact += __shfl_xor_sync(0xffffffffu, exact, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (pairs) atomicAdd(&rc->n_pairs, pairs);
+        if (exact) atomicAdd(&rc->n_exact, (unsigned long long)exact);
+    }
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+
+size_t bvh_bytes(int cap) {
+    size_t c = (size_t)cap + 1;
+    size_t b = 0;
+    b += 2 * align256(16 * c);              // box_lo / hi
+    b += align256(4 * (c + 1));             // live_scan
+    b += 2 * align256(4 * c);               // keys
+    b += 2 * align256(4 * c);               // vals
+    b += align256(4 * (256 * (size_t)kSortTiles + 1));
+    b += align256(8 * c);                   // child
+    b += 2 * align256(4 * c);               // iparent, lparent
+    b += 4 * align256(16 * c);              // nlo nhi llo lhi
+    b += align256(4 * c);                   // visit
+    b += align256(4 * 8);                   // scene
+    b += align256(4 * scan_scratch_ints());
+    return b;
+}
+
+void bvh_carve(BvhBuffers& b, int cap, char* base) {
+    size_t c = (size_t)cap + 1;
+    char* p = base;
+    auto take = [&](size_t bytes) {
+        char* r = p;
+        p += align256(bytes);
+        return r;
+    };
+    b.cap = cap;
+    b.box_lo = (float4*)take(16 * c);
+    b.box_hi = (float4*)take(16 * c);
+    b.live_scan = (int*)take(4 * (c + 1));
+    b.keys[0] = (unsigned*)take(4 * c);
+    b.keys[1] = (unsigned*)take(4 * c);
+    b.vals[0] = (int*)take(4 * c);
+    b.vals[1] = (int*)take(4 * c);
+    b.hist = (int*)take(4 * (256 * (size_t)kSortTiles + 1));
+    b.child = (int2*)take(8 * c);
+    b.iparent = (int*)take(4 * c);
+    b.lparent = (int*)take(4 * c);
+    b.nlo = (float4*)take(16 * c);
+    b.nhi = (float4*)take(16 * c);
+    b.llo = (float4*)take(16 * c);
+    b.lhi = (float4*)take(16 * c);
+    b.visit = (int*)take(4 * c);
+    b.scene = (unsigned*)take(4 * 8);
+    b.scan_scratch = (int*)take(4 * scan_scratch_ints());
+}
+
+void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s) {
+    cudaMemsetAsync(b.scene, 0xFF, 3 * sizeof(unsigned), s);
+    cudaMemsetAsync(b.scene + 3, 0x00, 3 * sizeof(unsigned), s);
+    const int gF = grid_for(n_tris_bound, 256);
+    k_boxes<<<gF, 256, 0, s>>>(tri, pos, rc, b.box_lo, b.box_hi, b.live_scan, b.scene);
+    exclusive_scan(b.live_scan, b.live_scan, &rc->n_tris, 1, &rc->n_live, b.scan_scratch, s);
+    k_morton<<<gF, 256, 0, s>>>(rc, b.live_scan, b.box_lo, b.box_hi, b.scene, b.keys[0], b.vals[0]);
+    for (int pass = 0; pass < 4; ++pass) {
+        const int in = pass & 1, out = in ^ 1;
+        k_rs_hist<<<kSortTiles, kSortThreads, 0, s>>>(b.keys[in], &rc->n_live, 8 * pass, b.hist);
+        exclusive_scan(b.hist, b.hist, nullptr, 256 * kSortTiles, nullptr, b.scan_scratch, s);
+        k_rs_scatter<<<kSortTiles, kSortThreads, 0, s>>>(b.keys[in], b.vals[in], b.keys[out], b.vals[out], &rc->n_live,
+                                                         8 * pass, b.hist);
+    }
+    k_leaves<<<gF, 256, 0, s>>>(rc, b.vals[0], b.box_lo, b.box_hi, b.llo, b.lhi, b.visit, b.lparent);
+    k_karras<<<gF, 256, 0, s>>>(rc, b.keys[0], b.child, b.iparent, b.lparent);
+    k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit);
+}
+
+void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, unsigned char* hit,
+               RoundCounters* rc, int n_query_bound, float eps, cudaStream_t s) {
+    const int g = grid_for(n_query_bound, kQueryThreads, 16);
+    k_query<<<g, kQueryThreads, 0, s>>>(b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], b.box_lo, b.box_hi, tri, pos,
+                                        qlist, hit, rc, eps);
+}
+
+}  // namespace pamo

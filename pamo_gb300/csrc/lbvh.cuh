@@ -1,0 +1,41 @@
+// Morton-code LBVH over the live faces and the localized self-intersection query of one collapse round.
+#pragma once
+#include <cstddef>
+#include <cuda_runtime.h>
+#include "pamo_common.cuh"
+
+namespace pamo {
+
+struct BvhBuffers {
+    int cap = 0;                       // face capacity
+    float4* box_lo = nullptr;          // per face AABB (by face id)
+    float4* box_hi = nullptr;
+    int* live_scan = nullptr;          // exclusive scan of live flags [cap + 1]
+    unsigned* keys[2] = {nullptr, nullptr};  // Morton codes, sort ping-pong
+    int* vals[2] = {nullptr, nullptr};       // face ids, sort ping-pong
+    int* hist = nullptr;               // radix histograms [256 * kSortTiles + 1]
+    int2* child = nullptr;             // internal node children; v < 0 encodes leaf ~v
+    int* iparent = nullptr;            // parent of internal node
+    int* lparent = nullptr;            // parent of leaf
+    float4* nlo = nullptr;             // internal node boxes
+    float4* nhi = nullptr;
+    float4* llo = nullptr;             // leaf boxes in sorted order
+    float4* lhi = nullptr;
+    int* visit = nullptr;              // bottom-up arrival counters
+    unsigned* scene = nullptr;         // scene bounds as order-preserving uints (6)
+    int* scan_scratch = nullptr;
+};
+
+size_t bvh_bytes(int cap);
+void bvh_carve(BvhBuffers& b, int cap, char* base);
+
+// Builds the LBVH over faces with tri[f].x != -1 (count from rc->n_tris); writes rc->n_live.
+void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s);
+
+// For every face in the query list that is still live: hit[f] = 1 iff some live face g != f with an
+// overlapping closed AABB makes the reference's pair test true in either order. Query faces are taken
+// from qlist[0 .. rc->n_query).
+void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, unsigned char* hit,
+               RoundCounters* rc, int n_query_bound, float eps, cudaStream_t s);
+
+}  // namespace pamo

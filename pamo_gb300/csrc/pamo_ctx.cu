@@ -1,0 +1,626 @@
+// Host driver of the PaMO stage-2 GB300 path and its C ABI (include/pamo_gb300.h).
+//
+// The context owns every device buffer (grow-only) and the state the reference keeps between forward()
+// calls: the edge-cost buffer whose stale entries are read back in stuck rounds, the invalid-vertex table,
+// the previous call's compaction map and the undo-vertex list (simp_cuda/src/cusimp_free.h:184-280). The
+// reference's capacity policy (new capacity = n + n/5, fresh buffers read as zero) is kept for these
+// buffers because it decides when their contents are reset.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pamo_gb300.h"
+#include "lbvh.cuh"
+#include "pamo_common.cuh"
+#include "scan.cuh"
+#include "simp_round.cuh"
+
+using namespace pamo;
+
+namespace {
+
+constexpr float kCostRange = 10.0f;
+constexpr int kMaxExtraPasses = 5;  // cusimp_free.cu:1039
+constexpr float kTriEps = 1e-3f;    // cusimp_free.cu:893
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;  // elements
+};
+
+inline uint32_t collapse_threshold(float threshold) {  // cusimp_free.cu:923, saturating
+    float t = threshold > 0.0f ? threshold : 0.0f;  // clamp of cusimp_free.cu:34 (NaN -> upper bound)
+    t = (t < kCostRange) ? t : kCostRange;
+    if (threshold != threshold) t = kCostRange;
+    const float f = t / kCostRange * 4294967296.0f;
+    if (!(f > 0.0f)) return 0u;
+    if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)f;
+}
+
+}  // namespace
+
+// Phase timers (CUDA events on the context's stream), enabled with pamo_profile_enable.
+enum Phase { kPhLoad, kPhAdj, kPhQuad, kPhCost, kPhCollapse, kPhMarks, kPhBvh, kPhQuery, kPhUndo, kPhCompact, kPhCenter,
+             kNumPhases };
+
+struct Profiler {
+    bool on = false;
+    cudaEvent_t ev[2 * kNumPhases] = {};
+    bool pending[kNumPhases] = {};
+    double ms[kNumPhases] = {};
+    long long count[kNumPhases] = {};
+    bool ready = false;
+    void create() {
+        if (ready) return;
+        for (auto& e : ev) cudaEventCreate(&e);
+        ready = true;
+    }
+    void destroy() {
+        if (!ready) return;
+        for (auto& e : ev) cudaEventDestroy(e);
+        ready = false;
+    }
+    void begin(int p, cudaStream_t s) {
+        if (!on) return;
+        cudaEventRecord(ev[2 * p], s);
+    }
+    void end(int p, cudaStream_t s) {
+        if (!on) return;
+        cudaEventRecord(ev[2 * p + 1], s);
+        pending[p] = true;
+    }
+    // called after a stream synchronisation
+    void collect() {
+        if (!on) return;
+        for (int p = 0; p < kNumPhases; ++p)
+            if (pending[p]) {
+                float t = 0.f;
+                cudaEventElapsedTime(&t, ev[2 * p], ev[2 * p + 1]);
+                ms[p] += t;
+                count[p] += 1;
+                pending[p] = false;
+            }
+    }
+};
+
+struct pamo_ctx {
+    int device = 0;
+    Profiler prof;
+    std::string err;
+    cudaStream_t stream = nullptr;
+
+    // ---- capacities ----
+    size_t cap_v = 0;    // physical per-vertex capacity
+    size_t cap_f = 0;    // physical per-face capacity
+    size_t cap_ec = 0;   // physical edge-cost length
+    size_t logical_pts = 0;  // reference's allocated_pts
+
+    // ---- persistent reference state ----
+    DevBuf<uint32_t> edge_cost;
+    DevBuf<unsigned char> invalid;
+    DevBuf<int> pts_map, undo_list, tmp_undo;
+    int* d_ecap = nullptr;  // reference's allocated_edge_cost, kept on the device
+
+    // ---- per-vertex working buffers ----
+    DevBuf<float4> pos, orig_pos, pos_in, pos_out;
+    DevBuf<int> occ, valence, cursor;
+    DevBuf<Quadric> quad;
+    DevBuf<unsigned long long> vmin;
+    DevBuf<int> undo_in;
+
+    // ---- per-face ----
+    DevBuf<int4> tri, orig_tri, tri_in, tri_out;
+    DevBuf<int> ecount, qflag, qlist, fflags, nt, shuffle_flags;
+    DevBuf<unsigned long long> fkey;
+    DevBuf<unsigned char> hit;
+    BvhBuffers bvh;
+    char* bvh_mem = nullptr;
+    size_t bvh_cap = 0;
+
+    // ---- per-edge ----
+    DevBuf<int2> edges;
+    DevBuf<int> win, collapsed, uflag;
+
+    // ---- small ----
+    RoundCounters* rc = nullptr;
+    RoundCounters* h_rc = nullptr;  // pinned
+    int* scan_scratch = nullptr;
+    float* d_scale = nullptr;
+    float* d_center = nullptr;  // [16]
+    DevBuf<float> face_mean;
+    float* h_pinned_f = nullptr;
+
+    // ---- results of the last round / run ----
+    bool have_round = false;
+    int out_np = 0, out_nt = 0, out_nu = 0;
+    RoundCounters last{};
+    bool have_run = false;
+    int run_np = 0, run_nt = 0;
+    std::vector<int> faces_per_round;
+
+    int fail(int code, const char* fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+
+    int check(cudaError_t e, const char* what) {
+        if (e == cudaSuccess) return PAMO_OK;
+        return fail(e == cudaErrorMemoryAllocation ? PAMO_ERR_OOM : PAMO_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    }
+
+    template <typename T>
+    int grow(DevBuf<T>& b, size_t n, bool keep = false, bool zero = false) {
+        if (b.n >= n && b.p) return PAMO_OK;
+        T* p = nullptr;
+        cudaError_t e = cudaMalloc((void**)&p, n * sizeof(T));
+        if (e != cudaSuccess) return check(e, "cudaMalloc");
+        if (zero) cudaMemsetAsync(p, 0, n * sizeof(T), stream);
+        if (keep && b.p && b.n) cudaMemcpyAsync(p, b.p, b.n * sizeof(T), cudaMemcpyDeviceToDevice, stream);
+        if (b.p) {
+            cudaStreamSynchronize(stream);
+            cudaFree(b.p);
+        }
+        b.p = p;
+        b.n = n;
+        return PAMO_OK;
+    }
+
+    int init() {
+        int r;
+        if ((r = check(cudaSetDevice(device), "cudaSetDevice"))) return r;
+        if ((r = check(cudaMalloc((void**)&rc, sizeof(RoundCounters)), "cudaMalloc"))) return r;
+        if ((r = check(cudaMallocHost((void**)&h_rc, sizeof(RoundCounters)), "cudaMallocHost"))) return r;
+        if ((r = check(cudaMallocHost((void**)&h_pinned_f, 64 * sizeof(float)), "cudaMallocHost"))) return r;
+        if ((r = check(cudaMalloc((void**)&scan_scratch, scan_scratch_ints() * sizeof(int)), "cudaMalloc"))) return r;
+        if ((r = check(cudaMalloc((void**)&d_ecap, sizeof(int)), "cudaMalloc"))) return r;
+        if ((r = check(cudaMalloc((void**)&d_scale, sizeof(float)), "cudaMalloc"))) return r;
+        if ((r = check(cudaMalloc((void**)&d_center, 16 * sizeof(float)), "cudaMalloc"))) return r;
+        cudaMemset(d_ecap, 0, sizeof(int));
+        return PAMO_OK;
+    }
+
+    void release() {
+        cudaSetDevice(device);
+        cudaDeviceSynchronize();
+        auto fr = [](auto& b) {
+            if (b.p) cudaFree(b.p);
+            b.p = nullptr;
+            b.n = 0;
+        };
+        fr(edge_cost); fr(invalid); fr(pts_map); fr(undo_list); fr(tmp_undo);
+        fr(pos); fr(orig_pos); fr(pos_in); fr(pos_out); fr(occ); fr(valence); fr(cursor); fr(quad); fr(vmin); fr(undo_in);
+        fr(tri); fr(orig_tri); fr(tri_in); fr(tri_out); fr(ecount); fr(qflag); fr(qlist); fr(fflags); fr(nt);
+        fr(shuffle_flags); fr(fkey); fr(hit); fr(edges); fr(win); fr(collapsed); fr(uflag); fr(face_mean);
+        if (bvh_mem) cudaFree(bvh_mem);
+        bvh_mem = nullptr;
+        prof.destroy();
+        if (rc) cudaFree(rc);
+        if (h_rc) cudaFreeHost(h_rc);
+        if (h_pinned_f) cudaFreeHost(h_pinned_f);
+        if (scan_scratch) cudaFree(scan_scratch);
+        if (d_ecap) cudaFree(d_ecap);
+        if (d_scale) cudaFree(d_scale);
+        if (d_center) cudaFree(d_center);
+        rc = nullptr;
+    }
+
+    // Reference allocation semantics for the per-vertex state (cusimp_free.cu:47-85): when n exceeds the
+    // capacity the buffers are replaced by fresh (zero) ones of n + n/5 + 1 entries.
+    int ensure_pts_state(size_t n) {
+        if (n <= logical_pts && pts_map.p) return PAMO_OK;
+        logical_pts = n + n / 5;
+        const size_t len = logical_pts + 1;
+        int r;
+        auto fresh = [&](auto& b) {
+            if (b.p) {
+                cudaStreamSynchronize(stream);
+                cudaFree(b.p);
+                b.p = nullptr;
+                b.n = 0;
+            }
+            return grow(b, len, false, true);
+        };
+        if ((r = fresh(invalid))) return r;
+        if ((r = fresh(pts_map))) return r;
+        if ((r = fresh(undo_list))) return r;
+        if ((r = fresh(tmp_undo))) return r;
+        return PAMO_OK;
+    }
+
+    int ensure_vertex_buffers(size_t n) {
+        const size_t c = n + 2;
+        if (c <= cap_v && pos.p) return PAMO_OK;
+        const size_t nc = c + c / 5;
+        int r;
+        if ((r = grow(pos, nc)) || (r = grow(orig_pos, nc)) || (r = grow(pos_out, nc)) || (r = grow(occ, nc + 1)) ||
+            (r = grow(valence, nc + 1)) || (r = grow(cursor, nc)) || (r = grow(quad, nc)) || (r = grow(vmin, nc)) ||
+            (r = grow(pos_in, nc)))
+            return r;
+        cap_v = nc;
+        return PAMO_OK;
+    }
+
+    int ensure_face_buffers(size_t n) {
+        const size_t c = n + 2;
+        if (c <= cap_f && tri.p) return PAMO_OK;
+        const size_t nc = c + c / 5;
+        int r;
+        if ((r = grow(tri, nc)) || (r = grow(orig_tri, nc)) || (r = grow(tri_in, nc)) || (r = grow(tri_out, nc)) ||
+            (r = grow(ecount, nc + 1)) || (r = grow(qflag, nc + 1)) || (r = grow(qlist, nc)) || (r = grow(fflags, nc + 1)) ||
+            (r = grow(nt, 3 * nc)) || (r = grow(shuffle_flags, 2 * nc + 40)) || (r = grow(fkey, nc)) || (r = grow(hit, nc)) ||
+            (r = grow(edges, 2 * nc)) || (r = grow(win, 2 * nc + 1)) || (r = grow(collapsed, 2 * nc)) ||
+            (r = grow(uflag, 2 * nc + 1)) || (r = grow(face_mean, 3 * nc)))
+            return r;
+        // edge costs keep their stale contents when the physical buffer grows
+        if ((r = grow(edge_cost, 2 * nc + 2 * nc / 5 + 2, true, true))) return r;
+        if (bvh_cap < nc) {
+            if (bvh_mem) {
+                cudaStreamSynchronize(stream);
+                cudaFree(bvh_mem);
+                bvh_mem = nullptr;
+            }
+            cudaError_t e = cudaMalloc((void**)&bvh_mem, bvh_bytes((int)nc));
+            if (e != cudaSuccess) return check(e, "cudaMalloc(bvh)");
+            bvh_carve(bvh, (int)nc, bvh_mem);
+            bvh_cap = nc;
+        }
+        cap_f = nc;
+        return PAMO_OK;
+    }
+
+    // Host copy of the counters (synchronises the stream).
+    int read_counters() {
+        int r;
+        if ((r = check(cudaGetLastError(), "kernel launch"))) return r;
+        cudaMemcpyAsync(h_rc, rc, sizeof(RoundCounters), cudaMemcpyDeviceToHost, stream);
+        r = check(cudaStreamSynchronize(stream), "round");
+        prof.collect();
+        return r;
+    }
+
+    int status_to_error(int bits) {
+        if (bits & kErrBadIndex) return fail(PAMO_ERR_INVALID_ARG, "a triangle references a vertex outside [0, n_points)");
+        if (bits & kErrStackOverflow) return fail(PAMO_ERR_ITER_LIMIT, "BVH traversal stack overflow");
+        if (bits & kErrIterLimit) return fail(PAMO_ERR_ITER_LIMIT, "a bounded device loop hit its iteration limit");
+        if (bits & kErrCapacity) return fail(PAMO_ERR_CAPACITY, "the undo-vertex list overflowed its capacity");
+        return PAMO_OK;
+    }
+
+    // One forward() round. Points come either as AoS float [n,3] (pts3) or float4 (pts4); faces as AoS int
+    // [m,3] (tris3, validated) or int4 (tris4). `shuffle` applies the reference's init shuffle.
+    int round(const float* pts3, const float4* pts4, const int* tris3, const int4* tris4, const int* verts_undo, int nU,
+              int nP, int nT, float threshold, int is_stuck, int init, bool operator_mode) {
+        cudaStream_t s = stream;
+        int r;
+        if ((r = ensure_vertex_buffers(nP)) || (r = ensure_face_buffers(nT))) return r;
+        if (is_stuck && nU > 0) {
+            if (!pts_map.p) return fail(PAMO_ERR_STATE, "a stuck round needs a previous round on this context");
+            if ((size_t)nU > undo_list.n) return fail(PAMO_ERR_CAPACITY, "verts_undo longer than the undo list");
+        }
+
+        // counters; a stuck round starts its undo list with the carried-over entries
+        std::memset(h_rc, 0, sizeof(RoundCounters));
+        h_rc->n_pts = nP;
+        h_rc->n_tris = nT;
+        if (is_stuck) {
+            h_rc->first_undo = nU;
+            h_rc->n_vertices_undo = nU;
+        }
+        cudaMemcpyAsync(rc, h_rc, sizeof(RoundCounters), cudaMemcpyHostToDevice, s);
+
+        // undo-list bookkeeping with the previous call's map (cusimp_free.cu:895-918)
+        launch_undo_bookkeeping(verts_undo, nU, is_stuck, tmp_undo.p, undo_list.p, pts_map.p, (int)pts_map.n, invalid.p,
+                                (int)invalid.n, s);
+        if ((r = ensure_pts_state(nP))) return r;
+
+        const uint32_t collapse_t = collapse_threshold(threshold);
+
+        // inputs
+        prof.begin(kPhLoad, s);
+        if (pts3) launch_load_points(pts3, nP, pos.p, orig_pos.p, occ.p, s);
+        else launch_load_points4(pts4, nP, pos.p, orig_pos.p, occ.p, s);
+        int4* tri_src = init ? tri_in.p : tri.p;
+        if (tris3) launch_load_tris(tris3, nT, nP, tri_src, rc, s);
+        else if (tri_src != tris4) launch_load_tris4(tris4, nT, tri_src, s);
+        if (init) {
+            Feistel fb = make_feistel((unsigned long long)nT);
+            if (nT > 0) launch_shuffle_tris(fb, shuffle_flags.p, scan_scratch, tri_src, tri.p, nT, s);
+        }
+        launch_copy_tris(tri.p, orig_tri.p, nT, s);
+        prof.end(kPhLoad, s);
+
+        // adjacency
+        prof.begin(kPhAdj, s);
+        cudaMemsetAsync(valence.p, 0, (nP + 1) * sizeof(int), s);
+        cudaMemsetAsync(cursor.p, 0, (nP + 1) * sizeof(int), s);
+        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, s);
+        exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
+        exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s);
+        launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, s);
+        launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
+        const int* nt_off = valence.p;
+        const int eb = 2 * nT;
+        prof.end(kPhAdj, s);
+
+        // cost and selection
+        prof.begin(kPhQuad, s);
+        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, pos.p, quad.p, s);
+        prof.end(kPhQuad, s);
+        launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
+        cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
+        prof.begin(kPhCost, s);
+        launch_edge_cost(rc, eb, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, invalid.p, edge_cost.p, vmin.p, d_scale,
+                         threshold, is_stuck, s);
+        prof.end(kPhCost, s);
+        prof.begin(kPhCollapse, s);
+        launch_face_keys(rc, nT, tri.p, vmin.p, fkey.p, s);
+        launch_collapse(rc, eb, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p,
+                        orig_pos.p, occ.p, win.p, s);
+        exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s);
+        launch_compact_winners(rc, eb, win.p, collapsed.p, s);
+        prof.end(kPhCollapse, s);
+        prof.begin(kPhMarks, s);
+        launch_remove_invalid(rc, nT, tri.p, s);
+        launch_line_edges(rc, eb, edges.p, nt_off, nt.p, tri.p, pos.p, occ.p, nullptr, (int)collapsed.n, collapsed.p, s);
+
+        // faces whose intersections decide the undo: rings of the considered collapsed edges
+        cudaMemsetAsync(qflag.p, 0, (nT + 1) * sizeof(int), s);
+        launch_mark_query(rc, eb, collapsed.p, edges.p, nt_off, nt.p, qflag.p, s);
+        exclusive_scan(qflag.p, qflag.p, &rc->n_tris, 1, &rc->n_query, scan_scratch, s);
+        launch_compact_flags(qflag.p, nT, &rc->n_tris, qlist.p, s);
+        prof.end(kPhMarks, s);
+
+        // self-intersection check and undo passes (cusimp_free.cu:1014-1040)
+        const int list_cap = (int)undo_list.n;
+        auto check_pass = [&]() {
+            cudaMemsetAsync(hit.p, 0, nT + 1, s);
+            prof.begin(kPhBvh, s);
+            bvh_build(bvh, tri.p, pos.p, rc, nT, s);
+            prof.end(kPhBvh, s);
+            prof.begin(kPhQuery, s);
+            bvh_query(bvh, tri.p, pos.p, qlist.p, hit.p, rc, nT, kTriEps, s);
+            prof.end(kPhQuery, s);
+            launch_undo_check(rc, eb, collapsed.p, edges.p, nt_off, nt.p, hit.p, uflag.p, s);
+            exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s);
+            launch_after_check(rc, s);
+        };
+        check_pass();
+        if ((r = read_counters())) return r;
+        int extra = 0;
+        while (h_rc->n_undo != 0) {
+            ++extra;
+            launch_undo_apply(rc, eb, collapsed.p, uflag.p, edges.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p, orig_pos.p,
+                              occ.p, tmp_undo.p, undo_list.p, pts_map.p, list_cap, s);
+            check_pass();
+            if ((r = read_counters())) return r;
+            if (extra == kMaxExtraPasses) break;
+        }
+
+        // compaction map (cusimp_free.cu:1042-1045)
+        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
+        (void)operator_mode;
+        if ((r = read_counters())) return r;
+        if ((r = status_to_error(h_rc->status))) return r;
+        if ((size_t)h_rc->n_vertices_undo > undo_list.n)
+            return fail(PAMO_ERR_CAPACITY, "undo-vertex list longer than its capacity");
+        last = *h_rc;
+        return PAMO_OK;
+    }
+};
+
+// =====================================================================================================
+extern "C" {
+
+const char* pamo_status_string(int status) {
+    switch (status) {
+        case PAMO_OK: return "ok";
+        case PAMO_ERR_INVALID_ARG: return "invalid argument";
+        case PAMO_ERR_OOM: return "out of device memory";
+        case PAMO_ERR_CAPACITY: return "capacity exceeded";
+        case PAMO_ERR_ITER_LIMIT: return "iteration limit";
+        case PAMO_ERR_CUDA: return "CUDA error";
+        case PAMO_ERR_STATE: return "invalid call order";
+        default: return "unknown status";
+    }
+}
+
+int pamo_ctx_create(pamo_ctx** out, int device) {
+    if (!out) return PAMO_ERR_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return PAMO_ERR_INVALID_ARG;
+    pamo_ctx* c = new pamo_ctx();
+    c->device = device;
+    int r = c->init();
+    if (r) {
+        c->release();
+        delete c;
+        return r;
+    }
+    *out = c;
+    return PAMO_OK;
+}
+
+int pamo_ctx_destroy(pamo_ctx* ctx) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    ctx->release();
+    delete ctx;
+    return PAMO_OK;
+}
+
+const char* pamo_ctx_last_error(const pamo_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int pamo_forward_round(pamo_ctx* ctx, const float* points, const int32_t* triangles, const int32_t* verts_undo,
+                       int32_t n_verts_undo, int32_t n_points, int32_t n_triangles, float scale, float threshold,
+                       int32_t is_stuck, int32_t init, pamo_stream stream) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (n_points < 1 || n_triangles < 1 || !points || !triangles || n_verts_undo < 0 || (n_verts_undo > 0 && !verts_undo))
+        return ctx->fail(PAMO_ERR_INVALID_ARG, "invalid sizes or null pointers");
+    cudaSetDevice(ctx->device);
+    ctx->stream = (cudaStream_t)stream;
+    ctx->have_round = false;
+    ctx->h_pinned_f[0] = scale;
+    cudaMemcpyAsync(ctx->d_scale, ctx->h_pinned_f, sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    int r = ctx->round(points, nullptr, triangles, nullptr, verts_undo, n_verts_undo, n_points, n_triangles, threshold,
+                       is_stuck, init, true);
+    if (r) return r;
+    ctx->have_round = true;
+    ctx->out_np = n_points;
+    ctx->out_nt = n_triangles;
+    ctx->out_nu = ctx->last.n_vertices_undo;
+    return PAMO_OK;
+}
+
+int pamo_round_sizes(const pamo_ctx* ctx, int32_t* n_points, int32_t* n_triangles, int32_t* n_verts_undo) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    if (!ctx->have_round) return PAMO_ERR_STATE;
+    if (n_points) *n_points = ctx->out_np;
+    if (n_triangles) *n_triangles = ctx->out_nt;
+    if (n_verts_undo) *n_verts_undo = ctx->out_nu;
+    return PAMO_OK;
+}
+
+int pamo_round_outputs(pamo_ctx* ctx, float* verts, int32_t* tris, int32_t* verts_occ, int32_t* verts_map,
+                       int32_t* verts_undo, pamo_stream stream) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    if (!ctx->have_round) return ctx->fail(PAMO_ERR_STATE, "no round has run");
+    if (!verts || !tris) return ctx->fail(PAMO_ERR_INVALID_ARG, "verts and tris are required");
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    launch_export_round(ctx->rc, ctx->out_np, ctx->out_nt, ctx->pos.p, ctx->tri.p, ctx->occ.p, ctx->pts_map.p,
+                        ctx->undo_list.p, verts, tris, verts_occ, verts_map, verts_undo, ctx->out_nu, s);
+    return ctx->check(cudaGetLastError(), "export");
+}
+
+int pamo_round_stats(const pamo_ctx* ctx, int64_t* out, int32_t n) {
+    if (!ctx || !out) return PAMO_ERR_INVALID_ARG;
+    const RoundCounters& c = ctx->last;
+    int64_t v[18] = {c.n_edges, c.n_win, c.n_collapsed, c.n_considered, c.n_query, c.passes, c.n_vertices_undo,
+                     c.status, (int64_t)c.n_pairs, (int64_t)c.n_exact};
+    for (int i = 0; i < 8; ++i) v[10 + i] = c.undo_per_pass[i];
+    for (int i = 0; i < n && i < 18; ++i) out[i] = v[i];
+    return PAMO_OK;
+}
+
+int pamo_simplify_device(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                         int32_t n_triangles, double ratio, int32_t tolerance, float threshold, int32_t iter,
+                         int64_t min_verts, int32_t* out_n_points, int32_t* out_n_triangles, int32_t* out_rounds,
+                         pamo_stream stream) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (n_points < 1 || n_triangles < 1 || !points || !triangles)
+        return ctx->fail(PAMO_ERR_INVALID_ARG, "invalid sizes or null pointers");
+    cudaSetDevice(ctx->device);
+    ctx->stream = (cudaStream_t)stream;
+    cudaStream_t s = ctx->stream;
+    ctx->have_run = false;
+    ctx->faces_per_round.clear();
+    int r;
+    if ((r = ctx->ensure_vertex_buffers(n_points)) || (r = ctx->ensure_face_buffers(n_triangles))) return r;
+
+    // target_faces = max(int(ratio * F), min_verts) (pamo/__init__.py:97)
+    const long long target = std::max((long long)(ratio * (double)n_triangles), (long long)min_verts);
+
+    // centring and scale on the device, with numpy's float32 summation order
+    ctx->prof.begin(kPhCenter, s);
+    launch_center(points, triangles, n_points, n_triangles, ctx->face_mean.p, ctx->d_center, ctx->d_scale,
+                  ctx->pos_in.p, s);
+    ctx->prof.end(kPhCenter, s);
+
+    int np = n_points, nf = n_triangles;
+    int nu = 0;
+    int count = 0, stuck = 0, init = 1, rounds = 0;
+    for (int it = 0; it < iter; ++it) {
+        const int nf_prev = nf;
+        if (nu > 0) cudaMemcpyAsync(ctx->undo_in.p, ctx->undo_list.p, nu * sizeof(int), cudaMemcpyDeviceToDevice, s);
+        if (init) r = ctx->round(nullptr, ctx->pos_in.p, triangles, nullptr, ctx->undo_in.p, nu, np, nf, threshold, stuck,
+                                 init, false);
+        else r = ctx->round(nullptr, ctx->pos_in.p, nullptr, ctx->tri_in.p, ctx->undo_in.p, nu, np, nf, threshold, stuck,
+                            init, false);
+        if (r) return r;
+        ++rounds;
+        init = 0;
+        nu = ctx->last.n_vertices_undo;
+        if ((r = ctx->grow(ctx->undo_in, (size_t)nu + 1))) return r;
+        // compaction (pamo/__init__.py:136-140)
+        ctx->prof.begin(kPhCompact, s);
+        launch_live_flags(ctx->rc, nf, ctx->tri.p, ctx->fflags.p, s);
+        exclusive_scan(ctx->fflags.p, ctx->fflags.p, &ctx->rc->n_tris, 1, nullptr, ctx->scan_scratch, s);
+        launch_compact_mesh(ctx->rc, np, nf, ctx->pos.p, ctx->occ.p, ctx->pts_map.p, ctx->tri.p, ctx->fflags.p,
+                            ctx->pos_out.p, ctx->tri_out.p, s);
+        ctx->prof.end(kPhCompact, s);
+        if ((r = ctx->read_counters())) return r;
+        np = ctx->h_rc->n_pts_out;
+        nf = ctx->h_rc->n_tris_out;
+        std::swap(ctx->pos_in, ctx->pos_out);
+        std::swap(ctx->tri_in, ctx->tri_out);
+        ctx->faces_per_round.push_back(nf);
+        if (nf <= target || nf <= 10) break;
+        if (nf == nf_prev) {
+            count++;
+        } else {
+            count = 0;
+            stuck = 0;
+        }
+        if (count >= 2) stuck = 1;
+        if (count == tolerance) break;
+    }
+    ctx->run_np = np;
+    ctx->run_nt = nf;
+    ctx->have_run = true;
+    if (out_n_points) *out_n_points = np;
+    if (out_n_triangles) *out_n_triangles = nf;
+    if (out_rounds) *out_rounds = rounds;
+    return PAMO_OK;
+}
+
+int pamo_simplify_result(pamo_ctx* ctx, float* verts, int32_t* tris, pamo_stream stream) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    if (!ctx->have_run) return ctx->fail(PAMO_ERR_STATE, "no simplification has run");
+    if (!verts || !tris) return ctx->fail(PAMO_ERR_INVALID_ARG, "verts and tris are required");
+    cudaSetDevice(ctx->device);
+    launch_export_mesh(ctx->run_np, ctx->run_nt, ctx->pos_in.p, ctx->tri_in.p, ctx->d_center, verts, tris,
+                       (cudaStream_t)stream);
+    return ctx->check(cudaGetLastError(), "export");
+}
+
+int pamo_profile_enable(pamo_ctx* ctx, int32_t enable) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (enable) ctx->prof.create();
+    ctx->prof.on = enable != 0;
+    for (int p = 0; p < kNumPhases; ++p) {
+        ctx->prof.ms[p] = 0.0;
+        ctx->prof.count[p] = 0;
+        ctx->prof.pending[p] = false;
+    }
+    return PAMO_OK;
+}
+
+int pamo_profile_read(const pamo_ctx* ctx, double* ms, int64_t* counts, int32_t n) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    for (int p = 0; p < n && p < kNumPhases; ++p) {
+        if (ms) ms[p] = ctx->prof.ms[p];
+        if (counts) counts[p] = ctx->prof.count[p];
+    }
+    return kNumPhases;
+}
+
+int pamo_simplify_round_faces(const pamo_ctx* ctx, int32_t* faces_per_round, int32_t capacity) {
+    if (!ctx || !faces_per_round) return PAMO_ERR_INVALID_ARG;
+    for (int i = 0; i < capacity && i < (int)ctx->faces_per_round.size(); ++i) faces_per_round[i] = ctx->faces_per_round[i];
+    return PAMO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,860 @@
+// Kernels of one PaMO stage-2 collapse round on GB300.
+//
+// Reference round: CUSimp_Free::forward (simp_cuda/src/cusimp_free.cu:891-1048). Differences in form, not in
+// result:
+//   * vertex->face lists are filled with atomics and then sorted per vertex, so every float sum over a ring
+//     runs in ascending face order and the round is deterministic;
+//   * the per-face minimum key of propagate_edge_cost_kernel (:587-610) is computed as the minimum over the
+//     face's three vertices of a per-vertex minimum (two 64-bit atomicMin per edge instead of one per ring
+//     face); both are the minimum over all edges touching the face;
+//   * winners are listed in ascending edge order through a scan instead of an atomic counter;
+//   * the undo check marks intersecting faces in a flag array and tests ring membership in O(ring) instead
+//     of scanning the whole intersection list per collapsed edge (:776-827).
+#include <cstdint>
+#include "scan.cuh"
+#include "simp_round.cuh"
+
+namespace pamo {
+
+namespace {
+
+constexpr int kT = 256;
+constexpr float kCostRange = 10.0f;            // cusimp_free.cu:15
+constexpr float kU32MaxF = 4294967296.0f;      // (float)UINT32_MAX
+
+// ------------------------------------------------------------------ set-up
+__global__ void k_undo_stuck(const int* __restrict__ verts_undo, int n, int* tmp_undo, int* undo_list,
+                             const int* __restrict__ pts_map, int map_len) {
+    for (int a = gtid(); a < n; a += gstride()) {
+        const int x = verts_undo[a];
+        tmp_undo[a] = x;
+        undo_list[a] = (x >= 0 && x < map_len) ? pts_map[x] : 0;  // rearrange_index_of_undo_vertices, :869-878
+    }
+}
+
+__global__ void k_invalid_mark(const int* __restrict__ verts_undo, int n, unsigned char* invalid, int len) {
+    for (int a = gtid(); a < n; a += gstride()) {
+        const int x = verts_undo[a];
+        if (x >= 0 && x < len) invalid[x] = 1;  // compute_invalid_vertices_table, :880-889
+    }
+}
+
+__global__ void k_load_points(const float* __restrict__ pts, int n, float4* pos, float4* orig, int* occ) {
+    for (int v = gtid(); v < n; v += gstride()) {
+        const float4 p = make_float4(pts[3 * v], pts[3 * v + 1], pts[3 * v + 2], 0.f);
+        pos[v] = p;
+        orig[v] = p;
+        occ[v] = 1;
+    }
+    if (gtid() == 0) occ[n] = 0;
+}
+
+__global__ void k_load_points4(const float4* __restrict__ pts, int n, float4* pos, float4* orig, int* occ) {
+    for (int v = gtid(); v < n; v += gstride()) {
+        const float4 p = pts[v];
+        pos[v] = p;
+        orig[v] = p;
+        occ[v] = 1;
+    }
+    if (gtid() == 0) occ[n] = 0;
+}
+
+__global__ void k_load_tris(const int* __restrict__ tris, int n, int n_pts, int4* tri, RoundCounters* rc) {
+    for (int f = gtid(); f < n; f += gstride()) {
+        const int a = tris[3 * f], b = tris[3 * f + 1], c = tris[3 * f + 2];
+        const bool dead = (a == -1 && b == -1 && c == -1);
+        const bool ok = dead || (a >= 0 && a < n_pts && b >= 0 && b < n_pts && c >= 0 && c < n_pts);
+        if (!ok) atomicOr(&rc->status, kErrBadIndex);
+        tri[f] = ok ? make_int4(a, b, c, 0) : make_int4(-1, -1, -1, 0);
+    }
+}
+
+__global__ void k_copy4(const int4* __restrict__ src, int4* dst, int n) {
+    for (int f = gtid(); f < n; f += gstride()) dst[f] = src[f];
+}
+
+__device__ __forceinline__ unsigned long long feistel(const Feistel& fb, unsigned long long idx) {
+    uint32_t s0 = (uint32_t)(idx >> fb.rbits), s1 = (uint32_t)(idx & fb.rmask);
+#pragma unroll 4
+    for (int r = 0; r < 24; ++r) {
+        const unsigned long long prod = 0xD2B74407B1CE6E93ull * (unsigned long long)s0;
+        const uint32_t hi = (uint32_t)(prod >> 32);
+        uint32_t lo = (uint32_t)prod;
+        lo = (lo << (fb.rbits - fb.lbits)) | (s1 >> fb.lbits);
+        s0 = ((hi ^ fb.key[r]) ^ s1) & fb.lmask;
+        s1 = lo & fb.rmask;
+    }
+    return ((unsigned long long)s0 << fb.rbits) | (unsigned long long)s1;
+}
+
+__global__ void k_shuffle_flags(Feistel fb, int* flags) {
+    const long long n = (long long)fb.n;
+    for (long long i = gtid(); i < n; i += gstride()) flags[i] = feistel(fb, (unsigned long long)i) < fb.m ? 1 : 0;
+    if (gtid() == 0) flags[n] = 0;
+}
+
+__global__ void k_shuffle_gather(Feistel fb, const int* __restrict__ scan, const int4* __restrict__ src, int4* dst) {
+    const long long n = (long long)fb.n;
+    for (long long i = gtid(); i < n; i += gstride()) {
+        const unsigned long long g = feistel(fb, (unsigned long long)i);
+        if (g < fb.m) dst[scan[i]] = src[g];
+    }
+}
+
+// ------------------------------------------------------------------ adjacency
+__global__ void __launch_bounds__(kT) k_face_counts(const int4* __restrict__ tri, const RoundCounters* rc, int* valence,
+                                                    int* ecount) {
+    const int n = rc->n_tris;
+    for (int f = gtid(); f < n; f += gstride()) {
+        const int4 t = tri[f];
+        if (face_killed(t)) {
+            ecount[f] = 0;
+            continue;
+        }
+        atomicAdd(&valence[t.x], 1);
+        atomicAdd(&valence[t.y], 1);
+        atomicAdd(&valence[t.z], 1);
+        ecount[f] = (t.x > t.y) + (t.y > t.z) + (t.z > t.x);  // count_edge_kernel, :306-316
+    }
+    if (gtid() == 0) ecount[n] = 0;
+}
+
+__global__ void __launch_bounds__(kT) k_fill_adjacency(const int4* __restrict__ tri, const RoundCounters* rc,
+                                                       const int* __restrict__ nt_off, int* cursor, int* nt,
+                                                       const int* __restrict__ edge_off, int2* edges) {
+    const int n = rc->n_tris;
+    for (int f = gtid(); f < n; f += gstride()) {
+        const int4 t = tri[f];
+        if (face_killed(t)) continue;
+        nt[nt_off[t.x] + atomicAdd(&cursor[t.x], 1)] = f;
+        nt[nt_off[t.y] + atomicAdd(&cursor[t.y], 1)] = f;
+        nt[nt_off[t.z] + atomicAdd(&cursor[t.z], 1)] = f;
+        int e = edge_off[f];  // create_edge_kernel, :318-335
+        if (t.x > t.y) edges[e++] = make_int2(t.y, t.x);
+        if (t.y > t.z) edges[e++] = make_int2(t.z, t.y);
+        if (t.z > t.x) edges[e++] = make_int2(t.x, t.z);
+    }
+}
+
+__global__ void __launch_bounds__(kT) k_sort_adjacency(const RoundCounters* rc, const int* __restrict__ nt_off, int* nt) {
+    const int n = rc->n_pts;
+    for (int v = gtid(); v < n; v += gstride()) {
+        const int a = nt_off[v], b = nt_off[v + 1];
+        for (int i = a + 1; i < b; ++i) {
+            const int x = nt[i];
+            int j = i - 1;
+            while (j >= a && nt[j] > x) {
+                nt[j + 1] = nt[j];
+                --j;
+            }
+            nt[j + 1] = x;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ quadrics (compute_vert_Q_kernel, :337-366)
+__device__ __forceinline__ void face_plane(const float4* __restrict__ pos, int4 t, float p[4]) {
+    const V3 v0 = v3(pos[t.x]), v1 = v3(pos[t.y]), v2 = v3(pos[t.z]);
+    V3 n = vcross(vsub(v1, v0), vsub(v2, v0));
+    n = vdiv(n, vnorm(n));
+    p[0] = n.x;
+    p[1] = n.y;
+    p[2] = n.z;
+    p[3] = -vdot(n, v0);
+}
+
+__global__ void __launch_bounds__(kT) k_quadrics(const RoundCounters* rc, const int* __restrict__ nt_off,
+                                                 const int* __restrict__ nt, const int4* __restrict__ tri,
+                                                 const float4* __restrict__ pos, Quadric* q) {
+    const int n = rc->n_pts;
+    for (int v = gtid(); v < n; v += gstride()) {
+        float m00 = 0.f, m01 = 0.f, m02 = 0.f, m03 = 0.f, m11 = 0.f, m12 = 0.f, m13 = 0.f, m22 = 0.f, m23 = 0.f, m33 = 0.f;
+        const int b = nt_off[v + 1];
+        for (int s = nt_off[v]; s < b; ++s) {
+            float p[4];
+            face_plane(pos, tri[nt[s]], p);
+            m00 += p[0] * p[0]; m01 += p[0] * p[1]; m02 += p[0] * p[2]; m03 += p[0] * p[3];
+            m11 += p[1] * p[1]; m12 += p[1] * p[2]; m13 += p[1] * p[3];
+            m22 += p[2] * p[2]; m23 += p[2] * p[3];
+            m33 += p[3] * p[3];
+        }
+        Quadric Q;
+        Q.a = make_float4(m00, m01, m02, m03);
+        Q.b = make_float4(m11, m12, m13, m22);
+        Q.c = make_float4(m23, m33, 0.f, 0.f);
+        q[v] = Q;
+    }
+}
+
+// ------------------------------------------------------------------ edge cost (compute_edge_cost_kernel, :382-585)
+__device__ __forceinline__ int next_after(int4 t, int v) {
+    if (t.x == v) return t.y;
+    if (t.y == v) return t.z;
+    if (t.z == v) return t.x;
+    return -1;
+}
+
+__device__ __forceinline__ float tri_area(V3 p0, V3 p1, V3 p2) {
+    const float a = vnorm(vsub(p0, p1)), b = vnorm(vsub(p1, p2)), c = vnorm(vsub(p2, p0));
+    const float s = (a + b + c) / 2;
+    return sqrtf(s * (s - a) * (s - b) * (s - c));
+}
+
+__device__ __forceinline__ void ring_len(int w, const int* __restrict__ nt_off, const int* __restrict__ nt,
+                                         const int4* __restrict__ tri, const float4* __restrict__ pos, float& len, int& cnt) {
+    const int b = nt_off[w + 1];
+    for (int s = nt_off[w]; s < b; ++s) {
+        const int4 t = tri[nt[s]];
+        if (t.x > t.y) { len += vnorm(vsub(v3(pos[t.x]), v3(pos[t.y]))); cnt++; }
+        if (t.y > t.z) { len += vnorm(vsub(v3(pos[t.y]), v3(pos[t.z]))); cnt++; }
+        if (t.z > t.x) { len += vnorm(vsub(v3(pos[t.z]), v3(pos[t.x]))); cnt++; }
+    }
+}
+
+// normal-flip test and skinny term over the ring of w with w moved to vm (faces holding `other` skipped)
+__device__ __forceinline__ bool ring_skinny(int w, int other, V3 vm, const int* __restrict__ nt_off,
+                                            const int* __restrict__ nt, const int4* __restrict__ tri,
+                                            const float4* __restrict__ pos, float& qa, int& ntri) {
+    const float k4s3 = 4.0f * sqrtf(3.0f);
+    const int b = nt_off[w + 1];
+    for (int s = nt_off[w]; s < b; ++s) {
+        const int4 t = tri[nt[s]];
+        if (t.x == other || t.y == other || t.z == other) continue;
+        const V3 o0 = v3(pos[t.x]), o1 = v3(pos[t.y]), o2 = v3(pos[t.z]);
+        const V3 n0 = (t.x == w) ? vm : o0, n1 = (t.y == w) ? vm : o1, n2 = (t.z == w) ? vm : o2;
+        V3 on = vcross(vsub(o1, o0), vsub(o2, o0));
+        on = vdiv(on, vnorm(on));
+        V3 nn = vcross(vsub(n1, n0), vsub(n2, n0));
+        nn = vdiv(nn, vnorm(nn));
+        if (vdot(on, nn) < 0) return false;
+        const float l01 = vnorm(vsub(n0, n1)), l12 = vnorm(vsub(n1, n2)), l20 = vnorm(vsub(n2, n0));
+        // the reference's operator precedence: only the first squared length divides (pow(x, 2) == x * x)
+        const float e = k4s3 * tri_area(n0, n1, n2) / (l01 * l01) + l12 * l12 + l20 * l20 + 0.0000001f;
+        qa += 1.0f - rclamp(e, 0.0f, 1.0f);
+        ntri++;
+    }
+    return true;
+}
+
+__device__ __forceinline__ uint32_t f2u_sat(float f) {
+    return __float2uint_rz(f);  // round toward zero, saturating like the reference's uint32_t(float) on the GPU
+}
+
+// returns false when the reference leaves the stale cost in place
+__device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restrict__ nt_off, const int* __restrict__ nt,
+                                                const int4* __restrict__ tri, const float4* __restrict__ pos,
+                                                const Quadric* __restrict__ q, float scale, float tres, uint32_t& out) {
+    // link condition
+    int dup = 0;
+    const int ua = nt_off[u], ub = nt_off[u + 1], va = nt_off[v], vb = nt_off[v + 1];
+    for (int a = ua; a < ub; ++a) {
+        const int iu = next_after(tri[nt[a]], u);
+        for (int b = va; b < vb; ++b) {
+            const int iv = next_after(tri[nt[b]], v);
+            if (iu == iv) dup++;
+            if (dup > 2) {
+                out = 0xFFFFFFFFu;
+                return true;
+            }
+        }
+    }
+    if (dup != 2) return false;
+    float len = 0.0f;
+    int cnt = 0;
+    ring_len(u, nt_off, nt, tri, pos, len, cnt);
+    ring_len(v, nt_off, nt, tri, pos, len, cnt);
+    const V3 v0 = v3(pos[u]), v1 = v3(pos[v]);
+    len = len / (float)cnt / scale * tres;
+    len = len + vnorm(vsub(v0, v1)) / scale * tres;
+    const V3 vm = vdiv(vadd(v0, v1), 2.0f);
+    float qa = 0.0f;
+    int ntri = 0;
+    if (!ring_skinny(u, v, vm, nt_off, nt, tri, pos, qa, ntri) || !ring_skinny(v, u, vm, nt_off, nt, tri, pos, qa, ntri)) {
+        out = 0xFFFFFFFFu;
+        return true;
+    }
+    qa = 5.0f * qa;  // SKINNY_TRIANGLE_PENALTY
+    const Quadric Qu = q[u], Qv = q[v];
+    const float m00 = Qu.a.x + Qv.a.x, m01 = Qu.a.y + Qv.a.y, m02 = Qu.a.z + Qv.a.z, m03 = Qu.a.w + Qv.a.w;
+    const float m11 = Qu.b.x + Qv.b.x, m12 = Qu.b.y + Qv.b.y, m13 = Qu.b.z + Qv.b.z, m22 = Qu.b.w + Qv.b.w;
+    const float m23 = Qu.c.x + Qv.c.x, m33 = Qu.c.y + Qv.c.y;
+    const float x = vm.x, y = vm.y, z = vm.z, w = 1.0f;
+    // Mat4x4::vTMv (cusimp_free.h:145-152) on the symmetric matrix
+    const float c0 = m00 * x + m01 * y + m02 * z + m03 * w;
+    const float c1 = m01 * x + m11 * y + m12 * z + m13 * w;
+    const float c2 = m02 * x + m12 * y + m22 * z + m23 * w;
+    const float c3 = m03 * x + m13 * y + m23 * z + m33 * w;
+    const float qem = c0 * x + c1 * y + c2 * z + c3 * w;
+    const float cost = qem / (scale * scale);
+    const float tot = cost + len + qa / (float)ntri * tres;
+    out = f2u_sat(rclamp(tot, 0.0f, kCostRange) / kCostRange * kU32MaxF);
+    return true;
+}
+
+__global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const int2* __restrict__ edges,
+                                                  const int* __restrict__ nt_off, const int* __restrict__ nt,
+                                                  const int4* __restrict__ tri, const float4* __restrict__ pos,
+                                                  const Quadric* __restrict__ q, const unsigned char* __restrict__ invalid,
+                                                  uint32_t* cost, unsigned long long* vmin, const float* d_scale,
+                                                  float tres, int is_stuck) {
+    const int n = rc->n_edges;
+    const float scale = *d_scale;
+    for (int e = gtid(); e < n; e += gstride()) {
+        const int2 ed = edges[e];
+        const int u = ed.x, v = ed.y;
+        uint32_t c = 0;
+        bool write;
+        if (invalid[u] && invalid[v]) {
+            c = 0xFFFFFFFFu;
+            write = true;
+        } else if (is_stuck) {
+            write = false;
+        } else {
+            write = edge_cost_value(u, v, nt_off, nt, tri, pos, q, scale, tres, c);
+        }
+        if (write) cost[e] = c;
+        else c = cost[e];  // stale value of an earlier round
+        const unsigned long long key = ((unsigned long long)c << 32) | (unsigned)e;
+        atomicMin(&vmin[u], key);
+        atomicMin(&vmin[v], key);
+    }
+}
+
+__global__ void k_edge_cost_capacity(RoundCounters* rc, int* d_cap) {
+    const int n = rc->n_edges;
+    int grow = 0;
+    if (n > *d_cap) {
+        *d_cap = n + n / 5;
+        grow = 1;
+    }
+    rc->pad[0] = grow;
+}
+
+__global__ void k_edge_cost_zero(const RoundCounters* rc, uint32_t* cost, int len) {
+    if (!rc->pad[0]) return;
+    for (int i = gtid(); i < len; i += gstride()) cost[i] = 0u;
+}
+
+__global__ void __launch_bounds__(kT) k_face_keys(const RoundCounters* rc, const int4* __restrict__ tri,
+                                                  const unsigned long long* __restrict__ vmin, unsigned long long* fkey) {
+    const int n = rc->n_tris;
+    for (int f = gtid(); f < n; f += gstride()) {
+        const int4 t = tri[f];
+        if (face_killed(t)) continue;
+        unsigned long long k = vmin[t.x];
+        k = min(k, vmin[t.y]);
+        k = min(k, vmin[t.z]);
+        fkey[f] = k;
+    }
+}
+
+// ------------------------------------------------------------------ collapse (collapse_edge_kernel, :639-774)
+__device__ __forceinline__ bool is_skinny(V3 p, V3 q, V3 r) {  // :617-637
+    const V3 pq = vsub(q, p), pr = vsub(r, p), qr = vsub(r, q);
+    const float lpq = sqrtf(vdot(pq, pq)), lpr = sqrtf(vdot(pr, pr)), lqr = sqrtf(vdot(qr, qr));
+    const float maxl = fmaxf(lpq, fmaxf(lpr, lqr));
+    const V3 c = {pq.y * pr.z - pq.z * pr.y, pq.z * pr.x - pq.x * pr.z, pq.x * pr.y - pq.y * pr.x};
+    const float thr = (float)(1e-6 * (double)maxl * (double)maxl);
+    const float area = 0.5f * sqrtf(c.x * c.x + c.y * c.y + c.z * c.z);
+    return area < thr;
+}
+
+__device__ __forceinline__ void rewire(int u, int v, const int* __restrict__ nt_off, const int* __restrict__ nt, int4* tri) {
+    for (int s = nt_off[u]; s < nt_off[u + 1]; ++s) {
+        const int f = nt[s];
+        const int4 t = tri[f];
+        if (t.x == v || t.y == v || t.z == v) tri[f] = make_int4(-1, -1, -1, 0);
+    }
+    for (int s = nt_off[v]; s < nt_off[v + 1]; ++s) {
+        const int f = nt[s];
+        int4 t = tri[f];
+        if (t.x == u || t.y == u || t.z == u) t = make_int4(-1, -1, -1, 0);
+        else if (t.x == v) t.x = u;
+        else if (t.y == v) t.y = u;
+        else if (t.z == v) t.z = u;
+        tri[f] = t;
+    }
+}
+
+__device__ __forceinline__ bool ring_has_skinny(int w, const int* __restrict__ nt_off, const int* __restrict__ nt,
+                                                const int4* tri, const float4* pos) {
+    for (int s = nt_off[w]; s < nt_off[w + 1]; ++s) {
+        const int4 t = tri[nt[s]];
+        if (t.x == -1) continue;
+        if (is_skinny(v3(pos[t.x]), v3(pos[t.y]), v3(pos[t.z]))) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void restore_ring(int w, const int* __restrict__ nt_off, const int* __restrict__ nt, int4* tri,
+                                             const int4* __restrict__ orig_tri) {
+    for (int s = nt_off[w]; s < nt_off[w + 1]; ++s) {
+        const int f = nt[s];
+        tri[f] = orig_tri[f];
+    }
+}
+
+__global__ void __launch_bounds__(kT) k_collapse(RoundCounters* rc, const int2* __restrict__ edges,
+                                                 const uint32_t* __restrict__ cost, uint32_t collapse_t,
+                                                 const unsigned long long* __restrict__ fkey, const int* __restrict__ nt_off,
+                                                 const int* __restrict__ nt, int4* tri, const int4* __restrict__ orig_tri,
+                                                 float4* pos, const float4* __restrict__ orig_pos, int* occ, int* win) {
+    const int n = rc->n_edges;
+    if (gtid() == 0) win[n] = 0;
+    for (int e = gtid(); e < n; e += gstride()) {
+        int w = 0;
+        const uint32_t c = cost[e];
+        if (c <= collapse_t) {
+            const int2 ed = edges[e];
+            const int u = ed.x, v = ed.y;
+            const unsigned long long key = ((unsigned long long)c << 32) | (unsigned)e;
+            bool ok = true;
+            for (int s = nt_off[u]; s < nt_off[u + 1] && ok; ++s) ok = (fkey[nt[s]] == key);
+            for (int s = nt_off[v]; s < nt_off[v + 1] && ok; ++s) ok = (fkey[nt[s]] == key);
+            if (ok) {
+                w = 1;
+                const V3 v0 = v3(pos[u]), v1 = v3(pos[v]);
+                const V3 vm = vdiv(vadd(v0, v1), 2.0f);
+                pos[u] = make_float4(vm.x, vm.y, vm.z, 0.f);
+                pos[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+                occ[v] = 0;
+                rewire(u, v, nt_off, nt, tri);
+                bool sk = ring_has_skinny(u, nt_off, nt, tri, pos);
+                if (!sk) sk = ring_has_skinny(v, nt_off, nt, tri, pos);
+                if (sk) {
+                    occ[v] = 1;
+                    pos[u] = orig_pos[u];
+                    pos[v] = orig_pos[v];
+                    restore_ring(u, nt_off, nt, tri, orig_tri);
+                    restore_ring(v, nt_off, nt, tri, orig_tri);
+                }
+            }
+        }
+        win[e] = w;
+    }
+}
+
+__global__ void k_compact_winners(const RoundCounters* rc, const int* __restrict__ scan, int* collapsed) {
+    const int n = rc->n_edges;
+    for (int e = gtid(); e < n; e += gstride())
+        if (scan[e + 1] != scan[e]) collapsed[scan[e]] = e;
+}
+
+__global__ void __launch_bounds__(kT) k_remove_invalid(const RoundCounters* rc, int4* tri) {  // :218-232
+    const int n = rc->n_tris;
+    for (int f = gtid(); f < n; f += gstride()) {
+        const int4 t = tri[f];
+        if (face_killed(t)) continue;
+        if (t.x == t.y || t.y == t.z || t.z == t.x) tri[f] = make_int4(-1, -1, -1, 0);
+    }
+}
+
+__global__ void __launch_bounds__(kT) k_line_detect(RoundCounters* rc, const int2* __restrict__ edges, const float4* pos) {
+    const int n = rc->n_edges;
+    int found = 0;
+    for (int e = gtid(); e < n; e += gstride()) {
+        const int2 ed = edges[e];
+        const float4 p = pos[ed.x], q = pos[ed.y];
+        if (p.x == q.x && p.y == q.y && p.z == q.z) found = 1;
+    }
+    if (__any_sync(0xffffffffu, found) && (threadIdx.x & 31) == 0) atomicAdd(&rc->n_line, 1);
+}
+
+// remove_line_edge_collapse (:234-274), applied in edge order by one thread when any coincident edge exists;
+// then the collapsed-list bookkeeping of forward() (:1004-1016).
+__global__ void k_line_apply(RoundCounters* rc, const int2* __restrict__ edges, const int* __restrict__ nt_off,
+                             const int* __restrict__ nt, int4* tri, float4* pos, int* occ, int* collapsed, int cap) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int h = rc->n_win;
+    int k = h;
+    if (rc->n_line > 0) {
+        const int n = rc->n_edges;
+        for (int e = 0; e < n; ++e) {
+            const int2 ed = edges[e];
+            const float4 p = pos[ed.x], q = pos[ed.y];
+            if (!(p.x == q.x && p.y == q.y && p.z == q.z)) continue;
+            if (k >= cap) {
+                atomicOr(&rc->status, kErrCapacity);
+                break;
+            }
+            collapsed[k++] = e;
+            pos[ed.y] = make_float4(0.f, 0.f, 0.f, 0.f);
+            occ[ed.y] = 0;
+            rewire(ed.x, ed.y, nt_off, nt, tri);
+        }
+    }
+    rc->n_collapsed = k;
+    const int roundup = ((h + 511) / 512) * 512;
+    rc->n_considered = (h == 0) ? 0 : (k < roundup ? k : roundup);
+}
+
+// ------------------------------------------------------------------ rollback
+__global__ void k_mark_query(const RoundCounters* rc, const int* __restrict__ collapsed, const int2* __restrict__ edges,
+                             const int* __restrict__ nt_off, const int* __restrict__ nt, int* qflag) {
+    const int n = rc->n_considered;
+    for (int c = gtid(); c < n; c += gstride()) {
+        const int2 ed = edges[collapsed[c]];
+        for (int s = nt_off[ed.x]; s < nt_off[ed.x + 1]; ++s) qflag[nt[s]] = 1;
+        for (int s = nt_off[ed.y]; s < nt_off[ed.y + 1]; ++s) qflag[nt[s]] = 1;
+    }
+}
+
+__global__ void k_compact_flags(const int* __restrict__ scan, const int* d_n, int* out) {
+    const int n = *d_n;
+    for (int i = gtid(); i < n; i += gstride())
+        if (scan[i + 1] != scan[i]) out[scan[i]] = i;
+}
+
+__global__ void k_undo_check(RoundCounters* rc, const int* __restrict__ collapsed, const int2* __restrict__ edges,
+                             const int* __restrict__ nt_off, const int* __restrict__ nt, const unsigned char* __restrict__ hit,
+                             int* uflag) {
+    const int n = rc->n_considered;
+    if (gtid() == 0) uflag[n] = 0;
+    for (int c = gtid(); c < n; c += gstride()) {
+        const int2 ed = edges[collapsed[c]];
+        int f = 0;
+        for (int s = nt_off[ed.x]; s < nt_off[ed.x + 1] && !f; ++s) f = hit[nt[s]];
+        for (int s = nt_off[ed.y]; s < nt_off[ed.y + 1] && !f; ++s) f = hit[nt[s]];
+        uflag[c] = f ? 1 : 0;
+    }
+}
+
+__global__ void k_after_check(RoundCounters* rc) {
+    const int nu = rc->n_undo;
+    if (rc->passes < 8) rc->undo_per_pass[rc->passes] = nu;
+    rc->passes += 1;
+    rc->n_vertices_undo += 2 * nu;
+}
+
+// undo_collapse_kernel (:829-867) + rearrange_index_of_undo_vertices (:869-878). The map is the compaction
+// map of the previous call, as in the reference.
+__global__ void k_undo_apply(RoundCounters* rc, const int* __restrict__ collapsed, const int* __restrict__ uscan,
+                             const int2* __restrict__ edges, const int* __restrict__ nt_off, const int* __restrict__ nt,
+                             int4* tri, const int4* __restrict__ orig_tri, float4* pos, const float4* __restrict__ orig_pos,
+                             int* occ, int* tmp_undo, int* undo_list, const int* __restrict__ pts_map, int map_len,
+                             int list_cap) {
+    const int n = rc->n_considered;
+    const int first = rc->first_undo;
+    for (int c = gtid(); c < n; c += gstride()) {
+        if (uscan[c + 1] == uscan[c]) continue;
+        const int a = uscan[c];
+        const int2 ed = edges[collapsed[c]];
+        const int u = ed.x, v = ed.y;
+        occ[v] = 1;
+        pos[u] = orig_pos[u];
+        pos[v] = orig_pos[v];
+        restore_ring(u, nt_off, nt, tri, orig_tri);
+        restore_ring(v, nt_off, nt, tri, orig_tri);
+        if (first + 2 * a + 1 < list_cap) {
+            tmp_undo[2 * a] = u;
+            tmp_undo[2 * a + 1] = v;
+            undo_list[first + 2 * a] = (u < map_len) ? pts_map[u] : 0;
+            undo_list[first + 2 * a + 1] = (v < map_len) ? pts_map[v] : 0;
+        } else {
+            atomicOr(&rc->status, kErrCapacity);
+        }
+    }
+}
+
+__global__ void k_after_apply(RoundCounters* rc) { rc->first_undo += 2 * rc->n_undo; }
+
+// ------------------------------------------------------------------ outputs
+__global__ void k_live_flags(const RoundCounters* rc, const int4* __restrict__ tri, int* flags) {
+    const int n = rc->n_tris;
+    for (int f = gtid(); f < n; f += gstride()) flags[f] = (tri[f].x >= 0) ? 1 : 0;
+    if (gtid() == 0) flags[n] = 0;
+}
+
+__global__ void k_compact_mesh(RoundCounters* rc, const float4* __restrict__ pos, const int* __restrict__ occ,
+                               const int* __restrict__ pts_map, const int4* __restrict__ tri, const int* __restrict__ fscan,
+                               float4* out_pos, int4* out_tri) {
+    const int np = rc->n_pts, nf = rc->n_tris;
+    for (int v = gtid(); v < np; v += gstride())
+        if (occ[v]) out_pos[pts_map[v]] = pos[v];
+    for (int f = gtid(); f < nf; f += gstride()) {
+        if (fscan[f + 1] == fscan[f]) continue;
+        const int4 t = tri[f];
+        out_tri[fscan[f]] = make_int4(pts_map[t.x], pts_map[t.y], pts_map[t.z], 0);
+    }
+    if (gtid() == 0) {
+        rc->n_pts_out = pts_map[np];
+        rc->n_tris_out = fscan[nf];
+    }
+}
+
+__global__ void k_export_round(int np, int nf, const float4* __restrict__ pos, const int4* __restrict__ tri,
+                               const int* __restrict__ occ, const int* __restrict__ pts_map, const int* __restrict__ undo,
+                               float* verts, int* tris, int* vocc, int* vmap, int* vundo, int nu) {
+    for (int v = gtid(); v < np; v += gstride()) {
+        const float4 p = pos[v];
+        verts[3 * v] = p.x;
+        verts[3 * v + 1] = p.y;
+        verts[3 * v + 2] = p.z;
+        if (vocc) vocc[v] = occ[v];
+        if (vmap) vmap[v] = pts_map[v];
+    }
+    for (int f = gtid(); f < nf; f += gstride()) {
+        const int4 t = tri[f];
+        tris[3 * f] = t.x;
+        tris[3 * f + 1] = t.y;
+        tris[3 * f + 2] = t.z;
+    }
+    if (vundo)
+        for (int a = gtid(); a < nu; a += gstride()) vundo[a] = undo[a];
+}
+
+__global__ void k_export_mesh(int np, int nf, const float4* __restrict__ pos, const int4* __restrict__ tri,
+                              const float* __restrict__ add, float* verts, int* tris) {
+    const float ax = add ? add[0] : 0.f, ay = add ? add[1] : 0.f, az = add ? add[2] : 0.f;
+    for (int v = gtid(); v < np; v += gstride()) {
+        const float4 p = pos[v];
+        verts[3 * v] = p.x + ax;
+        verts[3 * v + 1] = p.y + ay;
+        verts[3 * v + 2] = p.z + az;
+    }
+    for (int f = gtid(); f < nf; f += gstride()) {
+        const int4 t = tri[f];
+        tris[3 * f] = t.x;
+        tris[3 * f + 1] = t.y;
+        tris[3 * f + 2] = t.z;
+    }
+}
+
+// ------------------------------------------------------------------ centring (pamo/__init__.py:60-72, 117, 126)
+// numpy float32 semantics: per-face ((a + b) + c) / 3, then a sequential float32 sum over faces / F.
+__global__ void k_face_means(const float* __restrict__ pts, const int* __restrict__ tris, int nf, float* fm) {
+    for (int f = gtid(); f < nf; f += gstride()) {
+        const int a = tris[3 * f], b = tris[3 * f + 1], c = tris[3 * f + 2];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) fm[3 * f + d] = ((pts[3 * a + d] + pts[3 * b + d]) + pts[3 * c + d]) / 3.0f;
+    }
+}
+
+__global__ void k_sequential_sum(const float* __restrict__ fm, int nf, float* center) {
+    const int d = threadIdx.x;
+    if (d >= 3) return;
+    float s = 0.0f;
+    int f = 0;
+    for (; f + 8 <= nf; f += 8) {
+        float x[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) x[k] = fm[3 * (f + k) + d];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) s += x[k];
+    }
+    for (; f < nf; ++f) s += fm[3 * f + d];
+    center[d] = s / (float)nf;
+}
+
+__global__ void k_center_points(const float* __restrict__ pts, int np, const float* __restrict__ center, float4* out,
+                                unsigned* ext) {
+    const float cx = center[0], cy = center[1], cz = center[2];
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int v = gtid(); v < np; v += gstride()) {
+        const float x = pts[3 * v] - cx, y = pts[3 * v + 1] - cy, z = pts[3 * v + 2] - cz;
+        out[v] = make_float4(x, y, z, 0.f);
+        mn[0] = fminf(mn[0], x); mn[1] = fminf(mn[1], y); mn[2] = fminf(mn[2], z);
+        mx[0] = fmaxf(mx[0], x); mx[1] = fmaxf(mx[1], y); mx[2] = fmaxf(mx[2], z);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+            mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+        }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            unsigned a = __float_as_uint(mn[d]), b = __float_as_uint(mx[d]);
+            a = (a & 0x80000000u) ? ~a : (a | 0x80000000u);
+            b = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+            atomicMin(&ext[d], a);
+            atomicMax(&ext[3 + d], b);
+        }
+    }
+}
+
+__device__ __forceinline__ float ord_dec(unsigned u) { return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u); }
+
+// scale = max(max(ex, ey), ez) of the centred points (pamo/__init__.py:126)
+__global__ void k_extents(const unsigned* ext, float* scale) {
+    if (threadIdx.x != 0) return;
+    const float ex = ord_dec(ext[3]) - ord_dec(ext[0]);
+    const float ey = ord_dec(ext[4]) - ord_dec(ext[1]);
+    const float ez = ord_dec(ext[5]) - ord_dec(ext[2]);
+    const float m = (ey > ex) ? ey : ex;
+    *scale = (ez > m) ? ez : m;
+}
+
+}  // namespace
+
+// ================================================================== host launchers
+Feistel make_feistel(unsigned long long m) {
+    Feistel fb{};
+    unsigned long long bits;
+    if (m <= 16) {
+        bits = 4;
+    } else {
+        bits = 0;
+        unsigned long long t = m - 1;
+        while (t) {
+            ++bits;
+            t >>= 1;
+        }
+    }
+    fb.lbits = (uint32_t)(bits / 2);
+    fb.rbits = (uint32_t)(bits - bits / 2);
+    fb.lmask = (uint32_t)((1ull << fb.lbits) - 1);
+    fb.rmask = (uint32_t)((1ull << fb.rbits) - 1);
+    unsigned long long x = 1;  // minstd_rand, default seed
+    for (int r = 0; r < 24; ++r) {
+        x = (x * 48271ull) % 2147483647ull;
+        fb.key[r] = (uint32_t)x;
+    }
+    fb.n = 1ull << bits;
+    fb.m = m;
+    return fb;
+}
+
+void launch_undo_bookkeeping(const int* verts_undo, int n_verts_undo, int is_stuck, int* tmp_undo, int* undo_list,
+                             const int* pts_map, int pts_map_len, unsigned char* invalid, int invalid_len, cudaStream_t s) {
+    if (is_stuck) {
+        if (n_verts_undo > 0)
+            k_undo_stuck<<<grid_for(n_verts_undo, kT), kT, 0, s>>>(verts_undo, n_verts_undo, tmp_undo, undo_list, pts_map,
+                                                                   pts_map_len);
+    } else if (n_verts_undo != 0) {
+        cudaMemsetAsync(invalid, 0, invalid_len, s);
+    }
+    if (n_verts_undo > 0)
+        k_invalid_mark<<<grid_for(n_verts_undo, kT), kT, 0, s>>>(verts_undo, n_verts_undo, invalid, invalid_len);
+}
+
+void launch_load_points(const float* pts, int n, float4* pos, float4* orig_pos, int* occ, cudaStream_t s) {
+    k_load_points<<<grid_for(n, kT), kT, 0, s>>>(pts, n, pos, orig_pos, occ);
+}
+void launch_load_points4(const float4* pts, int n, float4* pos, float4* orig_pos, int* occ, cudaStream_t s) {
+    k_load_points4<<<grid_for(n, kT), kT, 0, s>>>(pts, n, pos, orig_pos, occ);
+}
+void launch_load_tris(const int* tris, int n, int n_pts, int4* tri, RoundCounters* rc, cudaStream_t s) {
+    k_load_tris<<<grid_for(n, kT), kT, 0, s>>>(tris, n, n_pts, tri, rc);
+}
+void launch_load_tris4(const int4* tris, int n, int4* tri, cudaStream_t s) {
+    k_copy4<<<grid_for(n, kT), kT, 0, s>>>(tris, tri, n);
+}
+void launch_copy_tris(const int4* src, int4* dst, int n, cudaStream_t s) {
+    k_copy4<<<grid_for(n, kT), kT, 0, s>>>(src, dst, n);
+}
+void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4* src, int4* dst, int n, cudaStream_t s) {
+    (void)n;
+    const int g = grid_for((long long)fb.n, kT);
+    k_shuffle_flags<<<g, kT, 0, s>>>(fb, flags);
+    exclusive_scan(flags, flags, nullptr, (int)fb.n + 1, nullptr, scan_scratch, s);
+    k_shuffle_gather<<<g, kT, 0, s>>>(fb, flags, src, dst);
+}
+
+void launch_face_counts(const int4* tri, const RoundCounters* rc, int n_tris_bound, int* valence, int* ecount,
+                        cudaStream_t s) {
+    k_face_counts<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, valence, ecount);
+}
+void launch_fill_adjacency(const int4* tri, const RoundCounters* rc, int n_tris_bound, const int* nt_off, int* cursor,
+                           int* nt, const int* edge_off, int2* edges, cudaStream_t s) {
+    k_fill_adjacency<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, nt_off, cursor, nt, edge_off, edges);
+}
+void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* nt_off, int* nt, cudaStream_t s) {
+    k_sort_adjacency<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt);
+}
+void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
+                     const float4* pos, Quadric* q, cudaStream_t s) {
+    k_quadrics<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, pos, q);
+}
+void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s) {
+    k_edge_cost_capacity<<<1, 1, 0, s>>>(rc, d_cap);
+    k_edge_cost_zero<<<grid_for(phys_len, kT), kT, 0, s>>>(rc, edge_cost, phys_len);
+}
+void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int2* edges, const int* nt_off, const int* nt,
+                      const int4* tri, const float4* pos, const Quadric* q, const unsigned char* invalid,
+                      uint32_t* cost, unsigned long long* vmin, const float* d_scale, float tres, int is_stuck,
+                      cudaStream_t s) {
+    k_edge_cost<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, edges, nt_off, nt, tri, pos, q, invalid, cost, vmin, d_scale,
+                                                           tres, is_stuck);
+}
+void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
+                      unsigned long long* fkey, cudaStream_t s) {
+    k_face_keys<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(rc, tri, vmin, fkey);
+}
+void launch_collapse(RoundCounters* rc, int n_edges_bound, const int2* edges, const uint32_t* cost, uint32_t collapse_t,
+                     const unsigned long long* fkey, const int* nt_off, const int* nt, int4* tri, const int4* orig_tri,
+                     float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s) {
+    k_collapse<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, edges, cost, collapse_t, fkey, nt_off, nt, tri, orig_tri,
+                                                          pos, orig_pos, occ, win);
+}
+void launch_compact_winners(const RoundCounters* rc, int n_edges_bound, const int* win_scan, int* collapsed,
+                            cudaStream_t s) {
+    k_compact_winners<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, win_scan, collapsed);
+}
+void launch_remove_invalid(const RoundCounters* rc, int n_tris_bound, int4* tri, cudaStream_t s) {
+    k_remove_invalid<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(rc, tri);
+}
+void launch_line_edges(RoundCounters* rc, int n_edges_bound, const int2* edges, const int* nt_off, const int* nt,
+                       int4* tri, float4* pos, int* occ, int* line_buf, int line_cap, int* collapsed, cudaStream_t s) {
+    (void)line_buf;
+    k_line_detect<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, edges, pos);
+    k_line_apply<<<1, 32, 0, s>>>(rc, edges, nt_off, nt, tri, pos, occ, collapsed, line_cap);
+}
+void launch_mark_query(const RoundCounters* rc, int n_edges_bound, const int* collapsed, const int2* edges,
+                       const int* nt_off, const int* nt, int* qflag, cudaStream_t s) {
+    k_mark_query<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, collapsed, edges, nt_off, nt, qflag);
+}
+void launch_compact_flags(const int* scan, int n_bound, const int* d_n, int* out_list, cudaStream_t s) {
+    k_compact_flags<<<grid_for(n_bound, kT), kT, 0, s>>>(scan, d_n, out_list);
+}
+void launch_undo_check(RoundCounters* rc, int n_edges_bound, const int* collapsed, const int2* edges, const int* nt_off,
+                       const int* nt, const unsigned char* hit, int* uflag, cudaStream_t s) {
+    k_undo_check<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, collapsed, edges, nt_off, nt, hit, uflag);
+}
+void launch_undo_apply(RoundCounters* rc, int n_edges_bound, const int* collapsed, const int* uscan, const int2* edges,
+                       const int* nt_off, const int* nt, int4* tri, const int4* orig_tri, float4* pos,
+                       const float4* orig_pos, int* occ, int* tmp_undo, int* undo_list, const int* pts_map,
+                       int list_cap, cudaStream_t s) {
+    k_undo_apply<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, collapsed, uscan, edges, nt_off, nt, tri, orig_tri, pos,
+                                                            orig_pos, occ, tmp_undo, undo_list, pts_map, list_cap, list_cap);
+    k_after_apply<<<1, 1, 0, s>>>(rc);
+}
+void launch_after_check(RoundCounters* rc, cudaStream_t s) { k_after_check<<<1, 1, 0, s>>>(rc); }
+
+void launch_live_flags(const RoundCounters* rc, int n_tris_bound, const int4* tri, int* flags, cudaStream_t s) {
+    k_live_flags<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(rc, tri, flags);
+}
+void launch_compact_mesh(RoundCounters* rc, int n_pts_bound, int n_tris_bound, const float4* pos, const int* occ,
+                         const int* pts_map, const int4* tri, const int* face_scan, float4* out_pos, int4* out_tri,
+                         cudaStream_t s) {
+    const int n = n_pts_bound > n_tris_bound ? n_pts_bound : n_tris_bound;
+    k_compact_mesh<<<grid_for(n, kT), kT, 0, s>>>(rc, pos, occ, pts_map, tri, face_scan, out_pos, out_tri);
+}
+void launch_export_round(const RoundCounters* rc, int n_pts, int n_tris, const float4* pos, const int4* tri,
+                         const int* occ, const int* pts_map, const int* undo_list, float* verts, int* tris,
+                         int* verts_occ, int* verts_map, int* verts_undo, int n_undo, cudaStream_t s) {
+    (void)rc;
+    const int n = n_pts > n_tris ? n_pts : n_tris;
+    k_export_round<<<grid_for(n, kT), kT, 0, s>>>(n_pts, n_tris, pos, tri, occ, pts_map, undo_list, verts, tris, verts_occ,
+                                                  verts_map, verts_undo, n_undo);
+}
+void launch_export_mesh(int n_pts, int n_tris, const float4* pos, const int4* tri, const float* add, float* verts,
+                        int* tris, cudaStream_t s) {
+    const int n = n_pts > n_tris ? n_pts : n_tris;
+    k_export_mesh<<<grid_for(n, kT), kT, 0, s>>>(n_pts, n_tris, pos, tri, add, verts, tris);
+}
+
+void launch_center(const float* pts, const int* tris, int n_pts, int n_tris, float* face_mean, float* center,
+                   float* d_scale, float4* pos_out, cudaStream_t s) {
+    // center[0..2] = tris_mean; center[4..9] scratch (order-preserving extents)
+    k_face_means<<<grid_for(n_tris, kT), kT, 0, s>>>(pts, tris, n_tris, face_mean);
+    k_sequential_sum<<<1, 32, 0, s>>>(face_mean, n_tris, center);
+    unsigned* ext = (unsigned*)(center + 4);
+    cudaMemsetAsync(ext, 0xFF, 3 * sizeof(unsigned), s);
+    cudaMemsetAsync(ext + 3, 0x00, 3 * sizeof(unsigned), s);
+    k_center_points<<<grid_for(n_pts, kT), kT, 0, s>>>(pts, n_pts, center, pos_out, ext);
+    k_extents<<<1, 32, 0, s>>>(ext, d_scale);
+}
+
+}  // namespace pamo

@@ -1,0 +1,81 @@
+// Kernels of one stage-2 collapse round (host launchers). Every count is read from RoundCounters in device
+// memory; the *_bound arguments only size the grids.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "pamo_common.cuh"
+
+namespace pamo {
+
+struct Feistel {  // thrust::shuffle's bijection parameters for m elements
+    uint32_t key[24];
+    uint32_t lbits, rbits, lmask, rmask;
+    unsigned long long n;  // 2^bits
+    unsigned long long m;
+};
+Feistel make_feistel(unsigned long long m);
+
+// ---- set-up of a round ----
+void launch_undo_bookkeeping(const int* verts_undo, int n_verts_undo, int is_stuck, int* tmp_undo, int* undo_list,
+                             const int* pts_map, int pts_map_len, unsigned char* invalid, int invalid_len, cudaStream_t s);
+void launch_load_points(const float* pts, int n, float4* pos, float4* orig_pos, int* occ, cudaStream_t s);
+void launch_load_points4(const float4* pts, int n, float4* pos, float4* orig_pos, int* occ, cudaStream_t s);
+void launch_load_tris(const int* tris, int n, int n_pts, int4* tri, RoundCounters* rc, cudaStream_t s);
+void launch_load_tris4(const int4* tris, int n, int4* tri, cudaStream_t s);
+void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4* tmp, int4* tri, int n, cudaStream_t s);
+void launch_copy_tris(const int4* src, int4* dst, int n, cudaStream_t s);
+
+// ---- adjacency ----
+void launch_face_counts(const int4* tri, const RoundCounters* rc, int n_tris_bound, int* valence, int* ecount,
+                        cudaStream_t s);
+void launch_fill_adjacency(const int4* tri, const RoundCounters* rc, int n_tris_bound, const int* nt_off, int* cursor,
+                           int* nt, const int* edge_off, int2* edges, cudaStream_t s);
+void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* nt_off, int* nt, cudaStream_t s);
+
+// ---- cost, selection, collapse ----
+void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
+                     const float4* pos, Quadric* q, cudaStream_t s);
+void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s);
+void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int2* edges, const int* nt_off, const int* nt,
+                      const int4* tri, const float4* pos, const Quadric* q, const unsigned char* invalid,
+                      uint32_t* cost, unsigned long long* vmin, const float* d_scale, float tres, int is_stuck,
+                      cudaStream_t s);
+void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
+                      unsigned long long* fkey, cudaStream_t s);
+void launch_collapse(RoundCounters* rc, int n_edges_bound, const int2* edges, const uint32_t* cost, uint32_t collapse_t,
+                     const unsigned long long* fkey, const int* nt_off, const int* nt, int4* tri, const int4* orig_tri,
+                     float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s);
+void launch_compact_winners(const RoundCounters* rc, int n_edges_bound, const int* win_scan, int* collapsed,
+                            cudaStream_t s);
+void launch_remove_invalid(const RoundCounters* rc, int n_tris_bound, int4* tri, cudaStream_t s);
+void launch_line_edges(RoundCounters* rc, int n_edges_bound, const int2* edges, const int* nt_off, const int* nt,
+                       int4* tri, float4* pos, int* occ, int* line_buf, int line_cap, int* collapsed, cudaStream_t s);
+
+// ---- self-intersection rollback ----
+void launch_mark_query(const RoundCounters* rc, int n_edges_bound, const int* collapsed, const int2* edges,
+                       const int* nt_off, const int* nt, int* qflag, cudaStream_t s);
+void launch_compact_flags(const int* scan, int n_bound, const int* d_n, int* out_list, cudaStream_t s);
+void launch_undo_check(RoundCounters* rc, int n_edges_bound, const int* collapsed, const int2* edges, const int* nt_off,
+                       const int* nt, const unsigned char* hit, int* uflag, cudaStream_t s);
+void launch_undo_apply(RoundCounters* rc, int n_edges_bound, const int* collapsed, const int* uscan, const int2* edges,
+                       const int* nt_off, const int* nt, int4* tri, const int4* orig_tri, float4* pos,
+                       const float4* orig_pos, int* occ, int* tmp_undo, int* undo_list, const int* pts_map,
+                       int list_cap, cudaStream_t s);
+
+// ---- outputs ----
+void launch_live_flags(const RoundCounters* rc, int n_tris_bound, const int4* tri, int* flags, cudaStream_t s);
+void launch_compact_mesh(RoundCounters* rc, int n_pts_bound, int n_tris_bound, const float4* pos, const int* occ,
+                         const int* pts_map, const int4* tri, const int* face_scan, float4* out_pos, int4* out_tri,
+                         cudaStream_t s);
+void launch_export_round(const RoundCounters* rc, int n_pts, int n_tris, const float4* pos, const int4* tri,
+                         const int* occ, const int* pts_map, const int* undo_list, float* verts, int* tris,
+                         int* verts_occ, int* verts_map, int* verts_undo, int n_undo, cudaStream_t s);
+void launch_export_mesh(int n_pts, int n_tris, const float4* pos, const int4* tri, const float* add, float* verts,
+                        int* tris, cudaStream_t s);
+
+// ---- whole-loop helpers ----
+void launch_center(const float* pts, const int* tris, int n_pts, int n_tris, float* face_mean, float* center,
+                   float* d_scale, float4* pos_out, cudaStream_t s);
+void launch_after_check(RoundCounters* rc, cudaStream_t s);
+
+}  // namespace pamo

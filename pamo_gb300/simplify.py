@@ -1,0 +1,214 @@
+"""Python face of the GB300 PaMO path, mirroring the reference's operator and API.
+
+* ``CUDSP_Free`` — the reference's pybind operator ``pamo._C.CUDSP_Free`` (simp_cuda/src/pybind.cpp:16-103,
+  189-193): one collapse round per ``forward`` call, five output tensors, state carried between calls.
+* ``PaMO`` — the reference's ``pamo.PaMO`` (simp_cuda/pamo/__init__.py:18-178) with the same constructor,
+  ``run`` signature and return convention (NumPy vertices and faces). The stage-2 round loop runs on the
+  device through ``pamo_simplify_device``; stage 3 (safe projection) runs when enabled.
+
+Both call the CUDA library through its C ABI (include/pamo_gb300.h); there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native
+
+__all__ = ["Context", "CUDSP_Free", "PaMO", "simplify"]
+
+
+def _ptr(t: torch.Tensor) -> ctypes.c_void_p:
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(device: torch.device) -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+class Context:
+    """Owns one ``pamo_ctx`` (device buffers and the state kept between rounds) on one CUDA device."""
+
+    def __init__(self, device=None):
+        lib = _native.load()
+        if device is None:
+            device = torch.cuda.current_device()
+        dev = torch.device("cuda", device) if isinstance(device, int) else torch.device(device)
+        if dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
+        h = ctypes.c_void_p()
+        _native.check(lib.pamo_ctx_create(ctypes.byref(h), self.device.index))
+        self._h = h
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("pamo context is closed")
+        return self._h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            _native.load().pamo_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def profile(self, enable: bool = True) -> None:
+        """Enable (and reset) or disable the per-phase CUDA-event timers."""
+        _native.check(_native.load().pamo_profile_enable(self.handle, int(enable)), self.handle)
+
+    def profile_read(self) -> dict:
+        n = len(_native.PHASES)
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_int64 * n)()
+        _native.load().pamo_profile_read(self.handle, ms, cnt, n)
+        return {p: (float(ms[i]), int(cnt[i])) for i, p in enumerate(_native.PHASES)}
+
+    def stats(self) -> dict:
+        out = (ctypes.c_int64 * 18)()
+        _native.check(_native.load().pamo_round_stats(self.handle, out, 18), self.handle)
+        keys = ["n_edges", "n_win", "n_collapsed", "n_considered", "n_query", "passes", "n_vertices_undo", "status",
+                "n_pairs", "n_exact"]
+        d = {k: int(out[i]) for i, k in enumerate(keys)}
+        d["undo_per_pass"] = [int(out[10 + i]) for i in range(8)]
+        return d
+
+
+def _check_input(t: torch.Tensor, name: str, dtype: torch.dtype) -> None:
+    # AT_ASSERTM / TORCH_INTERNAL_ASSERT checks of simp_cuda/src/pybind.cpp:8-14, 54-63
+    if not t.is_cuda:
+        raise RuntimeError(f"{name} must be a CUDA tensor")
+    if not t.is_contiguous():
+        raise RuntimeError(f"{name} must be contiguous")
+    if t.dtype != dtype:
+        raise RuntimeError(f"{name} type must match the pamo class")
+
+
+class CUDSP_Free:
+    """One PaMO stage-2 round per ``forward`` call (drop-in for ``pamo._C.CUDSP_Free``)."""
+
+    def __init__(self):
+        self._ctx: Context | None = None
+
+    def _context(self, device: torch.device) -> Context:
+        if self._ctx is None or self._ctx.device != device:
+            self._ctx = Context(device)
+        return self._ctx
+
+    def forward(self, points, triangles, verts_undo, n_verts_undo, scale, threshold, is_stuck, init):
+        _check_input(points, "points", torch.float32)
+        _check_input(triangles, "triangles", torch.int32)
+        _check_input(verts_undo, "verts_undo", torch.int32)
+        dev = points.device
+        ctx = self._context(dev)
+        lib = _native.load()
+        n_pts, n_tris = int(points.shape[0]), int(triangles.shape[0])
+        with torch.cuda.device(dev):
+            st = _stream(dev)
+            _native.check(
+                lib.pamo_forward_round(ctx.handle, _ptr(points), _ptr(triangles), _ptr(verts_undo), int(n_verts_undo),
+                                       n_pts, n_tris, float(scale), float(threshold), int(bool(is_stuck)),
+                                       int(bool(init)), st),
+                ctx.handle,
+            )
+            np_, nt_, nu_ = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+            _native.check(lib.pamo_round_sizes(ctx.handle, ctypes.byref(np_), ctypes.byref(nt_), ctypes.byref(nu_)),
+                          ctx.handle)
+            verts = torch.empty((np_.value, 3), dtype=torch.float32, device=dev)
+            tris = torch.empty((nt_.value, 3), dtype=torch.int32, device=dev)
+            occ = torch.empty((np_.value, 1), dtype=torch.int32, device=dev)
+            vmap = torch.empty((np_.value, 1), dtype=torch.int32, device=dev)
+            undo = torch.empty((nu_.value,), dtype=torch.int32, device=dev)
+            _native.check(
+                lib.pamo_round_outputs(ctx.handle, _ptr(verts), _ptr(tris), _ptr(occ), _ptr(vmap),
+                                       _ptr(undo) if nu_.value else None, st),
+                ctx.handle,
+            )
+        return verts, tris, occ, vmap, undo
+
+    def stats(self) -> dict:
+        if self._ctx is None:
+            raise RuntimeError("no round has run")
+        return self._ctx.stats()
+
+
+def _mesh_arrays(mesh):
+    if isinstance(mesh, (tuple, list)) and len(mesh) == 2:
+        return np.asarray(mesh[0]), np.asarray(mesh[1])
+    return np.asarray(mesh.vertices), np.asarray(mesh.faces)
+
+
+def simplify(points: torch.Tensor, triangles: torch.Tensor, ratio: float, tolerance: int = 4, threshold: float = 1e-3,
+             iter: int = 1000000, min_verts: int = 10000000000, ctx: Context | None = None):
+    """Stage-2 loop of ``PaMO.run`` on the device. Returns (verts float32 [N,3], faces int32 [M,3], rounds) as CUDA
+    tensors, with the centring undone as ``run`` does."""
+    _check_input(points, "points", torch.float32)
+    _check_input(triangles, "triangles", torch.int32)
+    dev = points.device
+    if ctx is None:
+        ctx = Context(dev)
+    lib = _native.load()
+    with torch.cuda.device(dev):
+        st = _stream(dev)
+        onp, ont, rounds = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _native.check(
+            lib.pamo_simplify_device(ctx.handle, _ptr(points), _ptr(triangles), int(points.shape[0]),
+                                     int(triangles.shape[0]), float(ratio), int(tolerance), float(threshold), int(iter),
+                                     int(min_verts), ctypes.byref(onp), ctypes.byref(ont), ctypes.byref(rounds), st),
+            ctx.handle,
+        )
+        verts = torch.empty((onp.value, 3), dtype=torch.float32, device=dev)
+        faces = torch.empty((ont.value, 3), dtype=torch.int32, device=dev)
+        _native.check(lib.pamo_simplify_result(ctx.handle, _ptr(verts), _ptr(faces), st), ctx.handle)
+    return verts, faces, rounds.value
+
+
+def round_faces(ctx: Context, rounds: int):
+    buf = (ctypes.c_int32 * max(1, rounds))()
+    _native.check(_native.load().pamo_simplify_round_faces(ctx.handle, buf, rounds), ctx.handle)
+    return [int(buf[i]) for i in range(rounds)]
+
+
+class PaMO(torch.nn.Module):
+    """Drop-in for ``pamo.PaMO`` (simp_cuda/pamo/__init__.py:18-178).
+
+    ``input_mesh`` is any object with ``vertices`` and ``faces`` (a trimesh, or a ``(V, F)`` pair). Stage 1
+    (SDF remeshing) is not part of this build: ``use_stage1=True`` raises ``NotImplementedError``.
+    """
+
+    def __init__(self, input_mesh, use_stage1: bool = True, use_stage3: bool = True):
+        super().__init__()
+        if use_stage1:
+            raise NotImplementedError("stage 1 (SDF + dual marching cubes remeshing) is not provided; pass use_stage1=False")
+        self.use_stage1 = use_stage1
+        self.use_stage3 = use_stage3
+        V, F = _mesh_arrays(input_mesh)
+        self.bbox = np.stack([V.min(axis=0), V.max(axis=0)])
+        self.gt_mesh = (np.array(V, copy=True), np.array(F, copy=True))
+        self.target_faces = None
+        self._ctx: Context | None = None
+        self.last_rounds = 0
+        if use_stage3:
+            from . import safe_project  # noqa: F401  (raises if stage 3 is unavailable)
+
+    def run(self, points, triangles, ratio, tolerance=4, threshold=1e-3, iter=1000000, min_verts=10000000000):
+        self.target_faces = max(int(ratio * len(triangles)), min_verts)
+        if self._ctx is None or self._ctx.device != points.device:
+            self._ctx = Context(points.device)
+        verts, faces, rounds = simplify(points, triangles, ratio, tolerance, threshold, iter, min_verts, ctx=self._ctx)
+        self.last_rounds = rounds
+        verts_np = verts.cpu().numpy()
+        faces_np = faces.cpu().numpy()
+        if self.use_stage3:
+            from . import safe_project
+
+            verts_np, faces_np = safe_project.process(self.gt_mesh[0], self.gt_mesh[1], verts_np, faces_np, 5)
+        return verts_np, faces_np

@@ -1,0 +1,34 @@
+"""Small test meshes shared by the tests."""
+
+import numpy as np
+
+from pamo_gb300 import synth
+
+
+def octahedron():
+    v = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]], np.float32)
+    f = np.array([[0, 2, 4], [2, 1, 4], [1, 3, 4], [3, 0, 4], [2, 0, 5], [1, 2, 5], [3, 1, 5], [0, 3, 5]], np.int32)
+    return v, f
+
+
+def sphere(n, L=4, sigma=0.03, seed=1):
+    return synth.star_mesh(n, L, lambda l: sigma, seed)
+
+
+def open_patch(n=12, seed=3):
+    """A bumpy open grid (has boundary edges)."""
+    rng = np.random.default_rng(seed)
+    xs, ys = np.meshgrid(np.linspace(0, 1, n + 1), np.linspace(0, 1, n + 1), indexing="ij")
+    z = 0.05 * np.sin(3 * xs) * np.cos(2 * ys) + 0.002 * rng.standard_normal(xs.shape)
+    v = np.stack([xs, ys, z], -1).reshape(-1, 3).astype(np.float32)
+    idx = np.arange((n + 1) * (n + 1)).reshape(n + 1, n + 1)
+    a, b, c, d = idx[:-1, :-1].ravel(), idx[1:, :-1].ravel(), idx[1:, 1:].ravel(), idx[:-1, 1:].ravel()
+    f = np.concatenate([np.stack([a, b, c], 1), np.stack([a, c, d], 1)]).astype(np.int32)
+    return v, f
+
+
+def euler(f):
+    e = np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]]), axis=1)
+    ne = len(np.unique(e, axis=0))
+    nv = len(np.unique(f))
+    return nv - ne + len(f)

@@ -1,0 +1,121 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle, round by round and over the whole loop.
+
+Integer outputs (faces, occupancy, maps, undo lists, collapse sets) must be bit-exact; positions are
+compared exactly too because both sides evaluate the same float32 operations in the same order.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as orc
+from tests import meshes
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases():
+    return {
+        "octahedron": meshes.octahedron(),
+        "sphere4": meshes.sphere(4),
+        "sphere8": meshes.sphere(8, L=5, sigma=0.05, seed=3),
+        "open_patch": meshes.open_patch(),
+    }
+
+
+def _compact(verts, tris, occ, vmap):
+    v = verts[occ[:, 0].astype(bool)]
+    f = tris[tris[:, 0] >= 0]
+    return v, vmap[:, 0][f].astype(np.int32)
+
+
+def _chain(v, f, rounds, gpu: bool):
+    import pamo_gb300
+
+    op = pamo_gb300.CUDSP_Free() if gpu else orc.Oracle()
+    scale = float(np.max(v.max(0) - v.min(0)))
+    undo = np.zeros(0, np.int32)
+    outs = []
+    count, stuck, nprev = 0, False, len(f)
+    for r in range(rounds):
+        if gpu:
+            res = op.forward(torch.from_numpy(v).cuda(), torch.from_numpy(f).cuda(), torch.from_numpy(undo).cuda(),
+                             len(undo), scale, 1e-3, stuck, r == 0)
+            res = [t.cpu().numpy() for t in res]
+        else:
+            res = op.forward(v, f, undo, len(undo), scale, 1e-3, stuck, r == 0)
+        outs.append(res)
+        verts, tris, occ, vmap, undo = res
+        v, f = _compact(verts, tris, occ, vmap)
+        if len(f) == nprev:
+            count += 1
+        else:
+            count, stuck = 0, False
+        if count >= 2:
+            stuck = True
+        nprev = len(f)
+        if len(f) <= 10:
+            break
+    return outs
+
+
+@pytest.mark.parametrize("name", ["octahedron", "sphere4", "sphere8", "open_patch"])
+def test_rounds_match_oracle(name):
+    v, f = _cases()[name]
+    g = _chain(v, f, 12, gpu=True)
+    c = _chain(v, f, 12, gpu=False)
+    assert len(g) == len(c)
+    for r, (a, b) in enumerate(zip(g, c)):
+        for k, (x, y) in enumerate(zip(a, b)):
+            assert x.shape == y.shape, (name, r, k)
+            assert np.array_equal(x, y), (name, r, k)
+
+
+def test_plain_small_first_rounds_match_oracle():
+    from pamo_gb300 import synth
+
+    v, f = synth.config_mesh("plain_small", seed=0)
+    g = _chain(v, f, 6, gpu=True)
+    c = _chain(v, f, 6, gpu=False)
+    for r, (a, b) in enumerate(zip(g, c)):
+        for k, (x, y) in enumerate(zip(a, b)):
+            assert np.array_equal(x, y), (r, k)
+
+
+@pytest.mark.parametrize("name,ratio", [("sphere8", 0.05), ("plain_small", 0.01)])
+def test_run_matches_oracle(name, ratio):
+    import pamo_gb300
+    from pamo_gb300 import synth
+
+    v, f = synth.config_mesh("plain_small", seed=0) if name == "plain_small" else _cases()[name]
+    pamo = pamo_gb300.PaMO((v, f), use_stage1=False, use_stage3=False)
+    V, F = pamo.run(torch.from_numpy(v).cuda(), torch.from_numpy(f).cuda(), ratio=ratio, min_verts=0)
+    V0, F0, fpr = orc.Oracle().run(v, f, ratio, min_verts=0)
+    assert pamo.last_rounds == len(fpr)
+    assert np.array_equal(F, F0)
+    assert np.array_equal(V, V0)
+
+
+def test_bad_index_is_an_error():
+    import pamo_gb300
+
+    v, f = meshes.octahedron()
+    f = f.copy()
+    f[3, 1] = 99
+    op = pamo_gb300.CUDSP_Free()
+    with pytest.raises(pamo_gb300.PamoError):
+        op.forward(torch.from_numpy(v).cuda(), torch.from_numpy(f).cuda(), torch.zeros(0, dtype=torch.int32).cuda(), 0,
+                   2.0, 1e-3, False, True)
+
+
+def test_operator_input_checks():
+    import pamo_gb300
+
+    v, f = meshes.octahedron()
+    op = pamo_gb300.CUDSP_Free()
+    with pytest.raises(RuntimeError):
+        op.forward(torch.from_numpy(v), torch.from_numpy(f).cuda(), torch.zeros(0, dtype=torch.int32).cuda(), 0, 2.0,
+                   1e-3, False, True)
+    with pytest.raises(RuntimeError):
+        op.forward(torch.from_numpy(v).double().cuda(), torch.from_numpy(f).cuda(),
+                   torch.zeros(0, dtype=torch.int32).cuda(), 0, 2.0, 1e-3, False, True)
