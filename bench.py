@@ -1,0 +1,351 @@
+"""Benchmark of the GB300 PaMO stage-2 path (parallel QEM collapse with LBVH self-intersection rollback).
+
+One step = one whole simplification job (the stage-2 loop of PaMO.run) of the configured synthetic
+mesh, with its inputs already resident in HBM. Prints one JSON line (rank 0).
+
+    python bench.py [--steps K] [--warmup W] [--config plain_large|plain_small] [--impl gb300|reference]
+
+Multi-GPU: a mesh does not shard (every round needs a whole-mesh independent set and intersection check),
+so N GPUs run N independent replicas of the job ("replicas only"); value = N * input faces / slowest rank.
+
+--impl reference times the CPU restatement of the reference's algorithm (oracle/, OpenMP on every host
+core) on a bounded sample of the same workload; the reference's own stage-2 code is CUDA-only.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    # name: (mesh, ratio, description)
+    "plain_large": ("plain_large", 0.001,
+                    "level-9 icosphere 2621442 V / 5242880 F, SH l<=16 sigma 0.05/l, seed 0; ratio 0.001, threshold 1e-3, "
+                    "tolerance 4, min_verts 0"),
+    "plain_small": ("plain_small", 0.01,
+                    "level-5 icosphere 10242 V / 20480 F, SH l<=6 sigma 0.03, seed 0; ratio 0.01, threshold 1e-3, "
+                    "tolerance 4, min_verts 0"),
+}
+THRESHOLD, TOLERANCE = 1e-3, 4
+L2_FLUSH_BYTES = 512 << 20
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def compulsory_bytes(phase: str, t: dict) -> tuple[float, str]:
+    """Algorithmic (compulsory) bytes of one phase over the whole run: each array the phase needs is read or
+    written once. Returns (bytes, unit description)."""
+    V, F, E = t["vertices"], t["faces"], t["edges"]
+    if phase == "bvh_query":
+        # BVH read once (internal node: children 8 + box 32; leaf: box 32 + face id 4) + faces 16 + positions 16
+        # (live faces ~ F) + query list 4 + hit flag 1 per query test
+        return 92.0 * t["live_indexed"] + 16.0 * V + 5.0 * t["query_tests"], \
+            "92 B per indexed face per check + 16 B per vertex per round + 5 B per query test"
+    if phase == "edge_cost":
+        # edges 8 + cost 4 per edge; positions 16 + quadric 48 + vmin 8 r/w per vertex; faces 16 + CSR 12 per face
+        return 12.0 * E + 80.0 * V + 28.0 * F, "12 B/edge + 80 B/vertex + 28 B/face"
+    if phase == "bvh_build":
+        return 200.0 * t["live_indexed"], "200 B per indexed face per check (boxes, keys, 4 sort passes, nodes)"
+    if phase == "adjacency":
+        return 8.0 * V + 60.0 * F, "8 B/vertex + 60 B/face (faces, CSR, edges)"
+    if phase == "collapse":
+        return 28.0 * E + 24.0 * F, "28 B/edge + 24 B/face"
+    return 32.0 * V + 32.0 * F, "32 B/vertex + 32 B/face"
+
+
+def cpu_sample(v, f, ratio, gpu_faces_per_round, budget_s=15.0, threads=None):
+    """Times the oracle (OpenMP) on the first rounds of the same job until budget_s, then projects the whole
+    job with the face counts per round of the GPU run (time per face-round is taken as constant)."""
+    from oracle import oracle as orc
+
+    threads = threads or os.cpu_count() or 1
+    o = orc.Oracle(threads=threads)
+    mean = orc.tris_mean(v, f)
+    verts = (v - mean).astype(np.float32)
+    scale = float(np.max(verts.max(0) - verts.min(0)))
+    faces = f
+    undo = np.zeros(0, np.int32)
+    t0 = time.perf_counter()
+    face_rounds = 0
+    rounds = 0
+    while True:
+        out = o.forward(verts, faces, undo, len(undo), scale, THRESHOLD, False, rounds == 0)
+        face_rounds += len(faces)
+        rounds += 1
+        vv, tt, occ, vmap, undo = out
+        verts = vv[occ[:, 0].astype(bool)]
+        faces = vmap[:, 0][tt[tt[:, 0] >= 0]].astype(np.int32)
+        if time.perf_counter() - t0 > budget_s or len(faces) <= 10:
+            break
+    dt = time.perf_counter() - t0
+    rate = face_rounds / dt
+    total_face_rounds = int(len(f) + sum(gpu_faces_per_round[:-1])) if gpu_faces_per_round else face_rounds
+    projected = total_face_rounds / rate
+    return {
+        "value": len(f) / projected,
+        "unit": "input faces/s",
+        "cores": threads,
+        "kind": "port",
+        "sample": f"oracle (OpenMP, {threads} threads) ran the first {rounds} rounds ({face_rounds} face-rounds) in "
+                  f"{dt:.1f} s; whole job projected from the per-round face counts of the GPU run "
+                  f"({total_face_rounds} face-rounds)",
+        "projected_job_s": projected,
+    }
+
+
+def run_reference(args):
+    """CPU reference arm: the oracle restatement of the reference's algorithm on all host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from pamo_gb300 import synth
+
+    mesh, ratio, desc = CONFIGS[args.config]
+    v, f = synth.config_mesh(mesh, seed=0)
+    threads = os.cpu_count() or 1
+    budget = 8.0 if args.config == "plain_large" else 2.0
+    # face counts per round of the whole job (identical on the GPU path and the oracle), for the projection
+    fpr = []
+    rec = os.path.join(ROOT, "profiles", f"faces_per_round_{args.config}.json")
+    if os.path.exists(rec):
+        fpr = json.load(open(rec))["faces_per_round"]
+    vals = []
+    for i in range(args.warmup + args.steps):
+        s = cpu_sample(v, f, ratio, fpr, budget_s=budget, threads=threads)
+        if i >= args.warmup:
+            vals.append(s)
+    value = float(np.median([s["value"] for s in vals]))
+    line = {
+        "impl": "reference", "metric": "input faces/s to 0.1% ratio", "value": value, "unit": "input faces/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * len(f) / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{args.config}: {desc}", "stage3": False},
+        "cpu_baseline": {k: vals[-1][k] for k in ("unit", "cores", "kind", "sample")} | {"value": value},
+        "e2e": {"value": value, "unit": "input faces/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--config", default="plain_large", choices=sorted(CONFIGS))
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+
+    import pamo_gb300
+    from pamo_gb300 import synth
+    from pamo_gb300 import api as simp
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    mesh, ratio, desc = CONFIGS[args.config]
+    v, f = synth.config_mesh(mesh, seed=0)
+    F0 = len(f)
+    pts = torch.from_numpy(v).to(dev)
+    tri = torch.from_numpy(f).to(dev)
+    ctx = pamo_gb300.Context(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            dist.barrier()
+
+    def job():
+        return pamo_gb300.simplify(pts, tri, ratio, TOLERANCE, THRESHOLD, 1000000, 0, ctx=ctx)
+
+    for _ in range(args.warmup):
+        out = job()
+    out_faces = out[1].shape[0]
+    rounds = out[2]
+
+    # ---- timed region: K jobs, L2 flushed between them, CUDA events on the launching stream ----
+    stream = torch.cuda.current_stream(dev)
+    step_ms = []
+    launches0 = simp.launch_count()
+    barrier()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            job()
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+    barrier()
+    launches = simp.launch_count() - launches0
+    ms = float(np.mean(step_ms))
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * F0 / (ms / 1000.0)
+
+    # ---- end to end through the public API from pinned host buffers ----
+    v_host = torch.from_numpy(v).pin_memory()
+    f_host = torch.from_numpy(f).pin_memory()
+    model = pamo_gb300.PaMO((v, f), use_stage1=False, use_stage3=False)
+    e2e_s = []
+    d2h = 0
+    for i in range(args.steps + 1):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        V, Fo = model.run(v_host.to(dev, non_blocking=True), f_host.to(dev, non_blocking=True), ratio=ratio,
+                          tolerance=TOLERANCE, threshold=THRESHOLD, min_verts=0)
+        torch.cuda.synchronize(dev)
+        if i > 0:
+            e2e_s.append(time.perf_counter() - t0)
+        d2h = V.nbytes + Fo.nbytes
+    e2e = F0 / float(np.mean(e2e_s))
+    if world > 1:
+        t = torch.tensor([float(np.mean(e2e_s))], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e = world * F0 / float(t.item())
+
+    # ---- phase profile of one more job (not part of the timed steps) ----
+    ctx.profile(True)
+    job()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    totals = ctx.run_totals()
+    fpr = simp.round_faces(ctx, rounds)
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dom]
+    peak, peak_kind = load_peaks()
+    run_bytes, unit_desc = compulsory_bytes(dom, totals)
+    per_launch_bytes = run_bytes / max(1, dom_n)
+    achieved = per_launch_bytes / (dom_ms / max(1, dom_n) / 1000.0) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        try:
+            traffic = json.load(open(tfile)).get(args.config, {}).get(dom)
+        except Exception:
+            traffic = None
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return 0
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_sample(v, f, ratio, fpr, budget_s=12.0 if args.config == "plain_large" else 3.0)
+        cpu.pop("projected_job_s", None)
+
+    line = {
+        "metric": "input faces/s to 0.1% ratio", "value": value, "unit": "input faces/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{args.config}: {desc}", "stage3": False, "parallelism": f"replicas{world}",
+                   "l2": "512 MiB buffer written between timed steps", "output_faces": out_faces, "rounds": rounds},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": dom, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": per_launch_bytes, "launches": dom_n,
+                     "avg_launch_ms": dom_ms / max(1, dom_n), "bytes_model": unit_desc},
+        "phases_ms": {k: round(ms_, 3) for k, (ms_, _) in prof.items()},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": "input faces/s", "h2d_bytes_per_step": int(v.nbytes + f.nbytes),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -82,6 +82,16 @@ int pamo_simplify_result(pamo_ctx* ctx, float* verts, int32_t* tris, pamo_stream
 /* Face count after each round of the last pamo_simplify_device call (host array of `capacity`). */
 int pamo_simplify_round_faces(const pamo_ctx* ctx, int32_t* faces_per_round, int32_t capacity);
 
+/* Totals over the rounds of the last pamo_simplify_device call, written to out[0..n): vertices, faces,
+ * edges, winners, query-face tests (query faces x checks), candidate pairs, pairs that took the fp64 path,
+ * intersection checks, live faces indexed by the LBVH (x checks), collapsed edges. Returns 10. No reference
+ * counterpart (diagnostics). */
+int pamo_run_totals(const pamo_ctx* ctx, int64_t* out, int32_t n);
+
+/* Number of kernels this library has launched since it was loaded (all contexts). No reference
+ * counterpart (launch accounting for benchmarks). */
+int64_t pamo_launch_count(void);
+
 /* Phase timers: when enabled, CUDA events on the call's stream bracket each phase of every round
  * (0 load/shuffle, 1 adjacency, 2 quadrics, 3 edge cost, 4 selection+collapse, 5 cleanup+query marks,
  * 6 LBVH build, 7 LBVH query + pair tests, 8 undo, 9 compaction, 10 centring). Enabling resets them.

@@ -45,9 +45,14 @@ SIGNATURES = {
     ),
     "pamo_simplify_result": (ctypes.c_int, [_P, _P, _P, _P]),
     "pamo_simplify_round_faces": (ctypes.c_int, [_P, _PI32, _I32]),
+    "pamo_run_totals": (ctypes.c_int, [_P, _PI64, _I32]),
+    "pamo_launch_count": (ctypes.c_int64, []),
     "pamo_profile_enable": (ctypes.c_int, [_P, _I32]),
     "pamo_profile_read": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _PI64, _I32]),
 }
+
+RUN_TOTALS = ["vertices", "faces", "edges", "winners", "query_tests", "pairs", "exact_pairs", "checks", "live_indexed",
+              "collapsed"]
 
 PHASES = ["load", "adjacency", "quadrics", "edge_cost", "collapse", "marks", "bvh_build", "bvh_query", "undo",
           "compact", "center"]

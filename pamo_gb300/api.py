@@ -72,6 +72,12 @@ class Context:
         _native.load().pamo_profile_read(self.handle, ms, cnt, n)
         return {p: (float(ms[i]), int(cnt[i])) for i, p in enumerate(_native.PHASES)}
 
+    def run_totals(self) -> dict:
+        n = len(_native.RUN_TOTALS)
+        out = (ctypes.c_int64 * n)()
+        _native.load().pamo_run_totals(self.handle, out, n)
+        return {k: int(out[i]) for i, k in enumerate(_native.RUN_TOTALS)}
+
     def stats(self) -> dict:
         out = (ctypes.c_int64 * 18)()
         _native.check(_native.load().pamo_round_stats(self.handle, out, 18), self.handle)
@@ -169,6 +175,11 @@ def simplify(points: torch.Tensor, triangles: torch.Tensor, ratio: float, tolera
         faces = torch.empty((ont.value, 3), dtype=torch.int32, device=dev)
         _native.check(lib.pamo_simplify_result(ctx.handle, _ptr(verts), _ptr(faces), st), ctx.handle)
     return verts, faces, rounds.value
+
+
+def launch_count() -> int:
+    """Kernels launched by the CUDA library since it was loaded."""
+    return int(_native.load().pamo_launch_count())
 
 
 def round_faces(ctx: Context, rounds: int):

@@ -266,16 +266,32 @@ __global__ void __launch_bounds__(256) k_bottom_up(RoundCounters* rc, const int2
 }
 
 // ---------------------------------------------------------------- localized query
+// Pass 1 (k_query): one thread per query face walks the tree with its stack in shared memory. Every
+// overlapping leaf g is a candidate pair; a pair of two query faces is taken only by the lower face index
+// (and then flags both faces). Pairs the float certificates decide are done; the rest are appended to
+// the exact list for pass 2. Pass 2 (k_query_exact) evaluates the fp64 decision, one pair per thread.
+__device__ __forceinline__ int warp_append(int* counter) {
+    const unsigned am = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(am) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(am));
+    base = __shfl_sync(am, base, leader);
+    return base + __popc(am & ((1u << lane) - 1u));
+}
+
 __global__ void __launch_bounds__(kQueryThreads) k_query(const int2* __restrict__ child, const float4* __restrict__ nlo,
                                                           const float4* __restrict__ nhi, const float4* __restrict__ llo,
                                                           const float4* __restrict__ lhi, const int* __restrict__ leaf_face,
                                                           const float4* __restrict__ box_lo, const float4* __restrict__ box_hi,
                                                           const int4* __restrict__ tri, const float4* __restrict__ pos,
-                                                          const int* __restrict__ qlist, unsigned char* hit,
+                                                          const int* __restrict__ qlist, const int* __restrict__ qscan,
+                                                          unsigned char* hit, int2* exact_list, int exact_cap,
                                                           RoundCounters* rc, float eps) {
     __shared__ int stack[kStackDepth][kQueryThreads];
     const int nq = rc->n_query;
     const int nl = rc->n_live;
+    int* n_list = &rc->pad[1];
     unsigned long long pairs = 0;
     unsigned exact = 0;
     for (int qi = gtid(); qi < nq; qi += gstride()) {
@@ -284,7 +300,6 @@ __global__ void __launch_bounds__(kQueryThreads) k_query(const int2* __restrict_
         if (qt.x == -1 || nl < 2) continue;
         const float4 q0 = pos[qt.x], q1 = pos[qt.y], q2 = pos[qt.z];
         const float4 qlo = box_lo[f], qhi = box_hi[f];
-        bool found = false;
         int sp = 0;
         int node = 0;
         int guard = 0;
@@ -304,19 +319,29 @@ __global__ void __launch_bounds__(kQueryThreads) k_query(const int2* __restrict_
                     if (!boxes_overlap(qlo, qhi, llo[li], lhi[li])) continue;
                     const int g = leaf_face[li];
                     if (g == f) continue;
+                    if (g < f && qscan[g + 1] != qscan[g]) continue;  // the lower query face owns the pair
                     const int4 gt = tri[g];
                     const float4 g0 = pos[gt.x], g1 = pos[gt.y], g2 = pos[gt.z];
                     ++pairs;
-                    if (pair_intersects(g0, g1, g2, gt, q0, q1, q2, qt, eps, exact) ||
-                        pair_intersects(q0, q1, q2, qt, g0, g1, g2, gt, eps, exact)) {
-                        found = true;
-                        break;
+                    PairGeom ga, gb;
+                    pair_geom(g0, g1, g2, gt, q0, q1, q2, qt, ga);  // reference order: hit is "current"
+                    pair_geom(q0, q1, q2, qt, g0, g1, g2, gt, gb);  // the order seen from g's own query
+                    const int mask = (pair_certainly_disjoint(ga) ? 0 : 1) | (pair_certainly_disjoint(gb) ? 0 : 2);
+                    if (mask) {
+                        exact += __popc(mask);
+                        const int at = warp_append(n_list);
+                        if (at < exact_cap) {
+                            exact_list[at] = make_int2(f, g | (mask << 30));
+                        } else if (((mask & 1) && pair_decide_exact(g0, g1, g2, gt, q0, q1, q2, qt, eps)) ||
+                                   ((mask & 2) && pair_decide_exact(q0, q1, q2, qt, g0, g1, g2, gt, eps))) {
+                            hit[f] = 1;
+                            hit[g] = 1;
+                        }
                     }
                 } else {
                     if (boxes_overlap(qlo, qhi, nlo[x], nhi[x])) next[nn++] = x;
                 }
             }
-            if (found) break;
             if (nn == 2) {
                 if (sp >= kStackDepth) {
                     atomicOr(&rc->status, kErrStackOverflow);
@@ -331,9 +356,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_query(const int2* __restrict_
                 node = stack[--sp][threadIdx.x];
             }
         }
-        if (found) hit[f] = 1;
     }
-    // diagnostics: warp-aggregated counters
     for (int o = 16; o > 0; o >>= 1) {
         pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
         exact += __shfl_xor_sync(0xffffffffu, exact, o);
@@ -341,6 +364,27 @@ __global__ void __launch_bounds__(kQueryThreads) k_query(const int2* __restrict_
     if ((threadIdx.x & 31) == 0) {
         if (pairs) atomicAdd(&rc->n_pairs, pairs);
         if (exact) atomicAdd(&rc->n_exact, (unsigned long long)exact);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_query_exact(const int4* __restrict__ tri, const float4* __restrict__ pos,
+                                                     const int2* __restrict__ exact_list, int exact_cap,
+                                                     unsigned char* hit, const RoundCounters* rc, float eps) {
+    const int n = min(rc->pad[1], exact_cap);
+    for (int i = gtid(); i < n; i += gstride()) {
+        const int2 e = exact_list[i];
+        const int f = e.x, g = e.y & 0x3fffffff, mask = (unsigned)e.y >> 30;
+        if (hit[f] && hit[g]) continue;
+        const int4 qt = tri[f], gt = tri[g];
+        const float4 q0 = pos[qt.x], q1 = pos[qt.y], q2 = pos[qt.z];
+        const float4 g0 = pos[gt.x], g1 = pos[gt.y], g2 = pos[gt.z];
+        bool r = false;
+        if (mask & 1) r = pair_decide_exact(g0, g1, g2, gt, q0, q1, q2, qt, eps);
+        if (!r && (mask & 2)) r = pair_decide_exact(q0, q1, q2, qt, g0, g1, g2, gt, eps);
+        if (r) {
+            hit[f] = 1;
+            hit[g] = 1;
+        }
     }
 }
 
@@ -398,26 +442,32 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
     cudaMemsetAsync(b.scene, 0xFF, 3 * sizeof(unsigned), s);
     cudaMemsetAsync(b.scene + 3, 0x00, 3 * sizeof(unsigned), s);
     const int gF = grid_for(n_tris_bound, 256);
-    k_boxes<<<gF, 256, 0, s>>>(tri, pos, rc, b.box_lo, b.box_hi, b.live_scan, b.scene);
+    k_boxes<<<gF, 256, 0, s>>>(tri, pos, rc, b.box_lo, b.box_hi, b.live_scan, b.scene); note_launch();
     exclusive_scan(b.live_scan, b.live_scan, &rc->n_tris, 1, &rc->n_live, b.scan_scratch, s);
-    k_morton<<<gF, 256, 0, s>>>(rc, b.live_scan, b.box_lo, b.box_hi, b.scene, b.keys[0], b.vals[0]);
+    k_morton<<<gF, 256, 0, s>>>(rc, b.live_scan, b.box_lo, b.box_hi, b.scene, b.keys[0], b.vals[0]); note_launch();
     for (int pass = 0; pass < 4; ++pass) {
         const int in = pass & 1, out = in ^ 1;
-        k_rs_hist<<<kSortTiles, kSortThreads, 0, s>>>(b.keys[in], &rc->n_live, 8 * pass, b.hist);
+        k_rs_hist<<<kSortTiles, kSortThreads, 0, s>>>(b.keys[in], &rc->n_live, 8 * pass, b.hist); note_launch();
         exclusive_scan(b.hist, b.hist, nullptr, 256 * kSortTiles, nullptr, b.scan_scratch, s);
         k_rs_scatter<<<kSortTiles, kSortThreads, 0, s>>>(b.keys[in], b.vals[in], b.keys[out], b.vals[out], &rc->n_live,
-                                                         8 * pass, b.hist);
+                                                         8 * pass, b.hist); note_launch();
     }
-    k_leaves<<<gF, 256, 0, s>>>(rc, b.vals[0], b.box_lo, b.box_hi, b.llo, b.lhi, b.visit, b.lparent);
-    k_karras<<<gF, 256, 0, s>>>(rc, b.keys[0], b.child, b.iparent, b.lparent);
-    k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit);
+    k_leaves<<<gF, 256, 0, s>>>(rc, b.vals[0], b.box_lo, b.box_hi, b.llo, b.lhi, b.visit, b.lparent); note_launch();
+    k_karras<<<gF, 256, 0, s>>>(rc, b.keys[0], b.child, b.iparent, b.lparent); note_launch();
+    k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit); note_launch();
 }
 
-void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, unsigned char* hit,
-               RoundCounters* rc, int n_query_bound, float eps, cudaStream_t s) {
+void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, const int* qscan,
+               unsigned char* hit, int2* exact_list, int exact_cap, RoundCounters* rc, int n_query_bound, float eps,
+               cudaStream_t s) {
+    cudaMemsetAsync(&rc->pad[1], 0, sizeof(int), s);
     const int g = grid_for(n_query_bound, kQueryThreads, 16);
     k_query<<<g, kQueryThreads, 0, s>>>(b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], b.box_lo, b.box_hi, tri, pos,
-                                        qlist, hit, rc, eps);
+                                        qlist, qscan, hit, exact_list, exact_cap, rc, eps);
+    note_launch();
+    k_query_exact<<<grid_for((long long)n_query_bound * 4, 128, 16), 128, 0, s>>>(tri, pos, exact_list, exact_cap, hit, rc,
+                                                                                  eps);
+    note_launch();
 }
 
 }  // namespace pamo

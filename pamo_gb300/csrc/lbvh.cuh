@@ -34,8 +34,11 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
 
 // For every face in the query list that is still live: hit[f] = 1 iff some live face g != f with an
 // overlapping closed AABB makes the reference's pair test true in either order. Query faces are taken
-// from qlist[0 .. rc->n_query).
-void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, unsigned char* hit,
-               RoundCounters* rc, int n_query_bound, float eps, cudaStream_t s);
+// from qlist[0 .. rc->n_query); qscan is the exclusive scan of the query flags (membership test). Pairs the
+// float certificates cannot decide go through exact_list (capacity exact_cap; beyond it they are decided
+// in place).
+void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, const int* qscan,
+               unsigned char* hit, int2* exact_list, int exact_cap, RoundCounters* rc, int n_query_bound, float eps,
+               cudaStream_t s);
 
 }  // namespace pamo

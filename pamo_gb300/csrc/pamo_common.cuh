@@ -84,6 +84,10 @@ __device__ __forceinline__ T ldg(const T* p) {
 __device__ __forceinline__ int gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
 __device__ __forceinline__ int gstride() { return gridDim.x * blockDim.x; }
 
+// Host-side count of kernels this library has launched (for launch accounting in benchmarks).
+void note_launch();
+long long launches_so_far();
+
 inline int grid_for(long long n, int threads, int per_sm = 8) {
     long long g = (n + threads - 1) / threads;
     long long cap = (long long)kNumSM * per_sm;

@@ -117,6 +117,7 @@ struct pamo_ctx {
     DevBuf<int4> tri, orig_tri, tri_in, tri_out;
     DevBuf<int> ecount, qflag, qlist, fflags, nt, shuffle_flags;
     DevBuf<unsigned long long> fkey;
+    DevBuf<float4> flen, fnrm;  // per-face edge lengths and unit normal
     DevBuf<unsigned char> hit;
     BvhBuffers bvh;
     char* bvh_mem = nullptr;
@@ -125,6 +126,7 @@ struct pamo_ctx {
     // ---- per-edge ----
     DevBuf<int2> edges;
     DevBuf<int> win, collapsed, uflag;
+    DevBuf<int2> exact_list;  // candidate pairs left to the fp64 decision
 
     // ---- small ----
     RoundCounters* rc = nullptr;
@@ -142,6 +144,8 @@ struct pamo_ctx {
     bool have_run = false;
     int run_np = 0, run_nt = 0;
     std::vector<int> faces_per_round;
+    // totals over the rounds of the last pamo_simplify_device call
+    long long tot[10] = {};
 
     int fail(int code, const char* fmt, ...) {
         char buf[512];
@@ -200,7 +204,7 @@ struct pamo_ctx {
         fr(edge_cost); fr(invalid); fr(pts_map); fr(undo_list); fr(tmp_undo);
         fr(pos); fr(orig_pos); fr(pos_in); fr(pos_out); fr(occ); fr(valence); fr(cursor); fr(quad); fr(vmin); fr(undo_in);
         fr(tri); fr(orig_tri); fr(tri_in); fr(tri_out); fr(ecount); fr(qflag); fr(qlist); fr(fflags); fr(nt);
-        fr(shuffle_flags); fr(fkey); fr(hit); fr(edges); fr(win); fr(collapsed); fr(uflag); fr(face_mean);
+        fr(shuffle_flags); fr(fkey); fr(flen); fr(fnrm); fr(hit); fr(edges); fr(win); fr(collapsed); fr(uflag); fr(face_mean); fr(exact_list);
         if (bvh_mem) cudaFree(bvh_mem);
         bvh_mem = nullptr;
         prof.destroy();
@@ -258,8 +262,10 @@ struct pamo_ctx {
         if ((r = grow(tri, nc)) || (r = grow(orig_tri, nc)) || (r = grow(tri_in, nc)) || (r = grow(tri_out, nc)) ||
             (r = grow(ecount, nc + 1)) || (r = grow(qflag, nc + 1)) || (r = grow(qlist, nc)) || (r = grow(fflags, nc + 1)) ||
             (r = grow(nt, 3 * nc)) || (r = grow(shuffle_flags, 2 * nc + 40)) || (r = grow(fkey, nc)) || (r = grow(hit, nc)) ||
+            (r = grow(flen, nc)) || (r = grow(fnrm, nc)) ||
             (r = grow(edges, 2 * nc)) || (r = grow(win, 2 * nc + 1)) || (r = grow(collapsed, 2 * nc)) ||
-            (r = grow(uflag, 2 * nc + 1)) || (r = grow(face_mean, 3 * nc)))
+            (r = grow(uflag, 2 * nc + 1)) || (r = grow(face_mean, 3 * nc)) ||
+            (r = grow(exact_list, std::max<size_t>(1 << 20, 8 * nc))))
             return r;
         // edge costs keep their stale contents when the physical buffer grows
         if ((r = grow(edge_cost, 2 * nc + 2 * nc / 5 + 2, true, true))) return r;
@@ -354,13 +360,14 @@ struct pamo_ctx {
 
         // cost and selection
         prof.begin(kPhQuad, s);
-        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, pos.p, quad.p, s);
+        launch_face_geom(rc, nT, tri.p, pos.p, flen.p, fnrm.p, s);
+        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, pos.p, fnrm.p, quad.p, s);
         prof.end(kPhQuad, s);
         launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
         cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
         prof.begin(kPhCost, s);
-        launch_edge_cost(rc, eb, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, invalid.p, edge_cost.p, vmin.p, d_scale,
-                         threshold, is_stuck, s);
+        launch_edge_cost(rc, eb, edges.p, nt_off, nt.p, tri.p, pos.p, flen.p, fnrm.p, quad.p, invalid.p, edge_cost.p,
+                         vmin.p, d_scale, threshold, is_stuck, s);
         prof.end(kPhCost, s);
         prof.begin(kPhCollapse, s);
         launch_face_keys(rc, nT, tri.p, vmin.p, fkey.p, s);
@@ -388,7 +395,7 @@ struct pamo_ctx {
             bvh_build(bvh, tri.p, pos.p, rc, nT, s);
             prof.end(kPhBvh, s);
             prof.begin(kPhQuery, s);
-            bvh_query(bvh, tri.p, pos.p, qlist.p, hit.p, rc, nT, kTriEps, s);
+            bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, (int)exact_list.n, rc, nT, kTriEps, s);
             prof.end(kPhQuery, s);
             launch_undo_check(rc, eb, collapsed.p, edges.p, nt_off, nt.p, hit.p, uflag.p, s);
             exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s);
@@ -526,6 +533,7 @@ int pamo_simplify_device(pamo_ctx* ctx, const float* points, const int32_t* tria
     cudaStream_t s = ctx->stream;
     ctx->have_run = false;
     ctx->faces_per_round.clear();
+    for (auto& t : ctx->tot) t = 0;
     int r;
     if ((r = ctx->ensure_vertex_buffers(n_points)) || (r = ctx->ensure_face_buffers(n_triangles))) return r;
 
@@ -551,6 +559,13 @@ int pamo_simplify_device(pamo_ctx* ctx, const float* points, const int32_t* tria
         if (r) return r;
         ++rounds;
         init = 0;
+        {
+            const RoundCounters& c = ctx->last;
+            long long* t = ctx->tot;
+            t[0] += c.n_pts; t[1] += c.n_tris; t[2] += c.n_edges; t[3] += c.n_win;
+            t[4] += (long long)c.n_query * c.passes; t[5] += (long long)c.n_pairs; t[6] += (long long)c.n_exact;
+            t[7] += c.passes; t[8] += (long long)c.n_live * c.passes; t[9] += c.n_collapsed;
+        }
         nu = ctx->last.n_vertices_undo;
         if ((r = ctx->grow(ctx->undo_in, (size_t)nu + 1))) return r;
         // compaction (pamo/__init__.py:136-140)
@@ -616,6 +631,14 @@ int pamo_profile_read(const pamo_ctx* ctx, double* ms, int64_t* counts, int32_t 
     }
     return kNumPhases;
 }
+
+int pamo_run_totals(const pamo_ctx* ctx, int64_t* out, int32_t n) {
+    if (!ctx || !out) return PAMO_ERR_INVALID_ARG;
+    for (int i = 0; i < n && i < 10; ++i) out[i] = ctx->tot[i];
+    return 10;
+}
+
+int64_t pamo_launch_count(void) { return launches_so_far(); }
 
 int pamo_simplify_round_faces(const pamo_ctx* ctx, int32_t* faces_per_round, int32_t capacity) {
     if (!ctx || !faces_per_round) return PAMO_ERR_INVALID_ARG;

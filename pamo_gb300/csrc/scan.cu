@@ -4,7 +4,13 @@
 #include "pamo_common.cuh"
 #include "scan.cuh"
 
+#include <atomic>
+
 namespace pamo {
+
+static std::atomic<long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 
 namespace {
 constexpr int kThreads = 512;
@@ -72,9 +78,9 @@ __global__ void __launch_bounds__(kThreads) k_tile_scan(const int* in, int* out,
 }  // namespace
 
 void exclusive_scan(const int* in, int* out, const int* d_n, int n_add, int* d_total, int* scratch, cudaStream_t s) {
-    k_tile_sums<<<kScanTiles, kThreads, 0, s>>>(in, d_n, n_add, scratch);
-    k_scan_tiles<<<1, 1024, 0, s>>>(scratch, d_total);
-    k_tile_scan<<<kScanTiles, kThreads, 0, s>>>(in, out, d_n, n_add, scratch);
+    k_tile_sums<<<kScanTiles, kThreads, 0, s>>>(in, d_n, n_add, scratch); note_launch();
+    k_scan_tiles<<<1, 1024, 0, s>>>(scratch, d_total); note_launch();
+    k_tile_scan<<<kScanTiles, kThreads, 0, s>>>(in, out, d_n, n_add, scratch); note_launch();
 }
 
 }  // namespace pamo

@@ -152,27 +152,39 @@ __global__ void __launch_bounds__(kT) k_sort_adjacency(const RoundCounters* rc, 
     }
 }
 
-// ------------------------------------------------------------------ quadrics (compute_vert_Q_kernel, :337-366)
-__device__ __forceinline__ void face_plane(const float4* __restrict__ pos, int4 t, float p[4]) {
-    const V3 v0 = v3(pos[t.x]), v1 = v3(pos[t.y]), v2 = v3(pos[t.z]);
-    V3 n = vcross(vsub(v1, v0), vsub(v2, v0));
-    n = vdiv(n, vnorm(n));
-    p[0] = n.x;
-    p[1] = n.y;
-    p[2] = n.z;
-    p[3] = -vdot(n, v0);
+// ------------------------------------------------------------------ per-face geometry
+// Values several kernels of the round need for every face, computed once with the reference's formulas
+// (so they are bit-identical to recomputing them in place): the unit normal of tri2plane / the edge-cost
+// flip test, (v1 - v0) x (v2 - v0) / |.| (cusimp_free.cu:337-346, 520-521), and the three edge lengths
+// |p_i - p_j|, |p_j - p_k|, |p_k - p_i| of the ring-length sum and the skinny term (:449-484, 368-380).
+__global__ void __launch_bounds__(kT) k_face_geom(const RoundCounters* rc, const int4* __restrict__ tri,
+                                                  const float4* __restrict__ pos, float4* flen, float4* fnrm) {
+    const int n = rc->n_tris;
+    for (int f = gtid(); f < n; f += gstride()) {
+        const int4 t = tri[f];
+        if (face_killed(t)) continue;
+        const V3 v0 = v3(pos[t.x]), v1 = v3(pos[t.y]), v2 = v3(pos[t.z]);
+        V3 nrm = vcross(vsub(v1, v0), vsub(v2, v0));
+        nrm = vdiv(nrm, vnorm(nrm));
+        fnrm[f] = make_float4(nrm.x, nrm.y, nrm.z, 0.f);
+        flen[f] = make_float4(vnorm(vsub(v0, v1)), vnorm(vsub(v1, v2)), vnorm(vsub(v2, v0)), 0.f);
+    }
 }
 
+// ------------------------------------------------------------------ quadrics (compute_vert_Q_kernel, :337-366)
 __global__ void __launch_bounds__(kT) k_quadrics(const RoundCounters* rc, const int* __restrict__ nt_off,
                                                  const int* __restrict__ nt, const int4* __restrict__ tri,
-                                                 const float4* __restrict__ pos, Quadric* q) {
+                                                 const float4* __restrict__ pos, const float4* __restrict__ fnrm,
+                                                 Quadric* q) {
     const int n = rc->n_pts;
     for (int v = gtid(); v < n; v += gstride()) {
         float m00 = 0.f, m01 = 0.f, m02 = 0.f, m03 = 0.f, m11 = 0.f, m12 = 0.f, m13 = 0.f, m22 = 0.f, m23 = 0.f, m33 = 0.f;
         const int b = nt_off[v + 1];
         for (int s = nt_off[v]; s < b; ++s) {
-            float p[4];
-            face_plane(pos, tri[nt[s]], p);
+            const int f = nt[s];
+            const float4 nn = fnrm[f];
+            const V3 nrm = {nn.x, nn.y, nn.z};
+            const float p[4] = {nrm.x, nrm.y, nrm.z, -vdot(nrm, v3(pos[tri[f].x]))};
             m00 += p[0] * p[0]; m01 += p[0] * p[1]; m02 += p[0] * p[2]; m03 += p[0] * p[3];
             m11 += p[1] * p[1]; m12 += p[1] * p[2]; m13 += p[1] * p[3];
             m22 += p[2] * p[2]; m23 += p[2] * p[3];
@@ -201,35 +213,55 @@ __device__ __forceinline__ float tri_area(V3 p0, V3 p1, V3 p2) {
 }
 
 __device__ __forceinline__ void ring_len(int w, const int* __restrict__ nt_off, const int* __restrict__ nt,
-                                         const int4* __restrict__ tri, const float4* __restrict__ pos, float& len, int& cnt) {
+                                         const int4* __restrict__ tri, const float4* __restrict__ flen, float& len, int& cnt) {
     const int b = nt_off[w + 1];
     for (int s = nt_off[w]; s < b; ++s) {
-        const int4 t = tri[nt[s]];
-        if (t.x > t.y) { len += vnorm(vsub(v3(pos[t.x]), v3(pos[t.y]))); cnt++; }
-        if (t.y > t.z) { len += vnorm(vsub(v3(pos[t.y]), v3(pos[t.z]))); cnt++; }
-        if (t.z > t.x) { len += vnorm(vsub(v3(pos[t.z]), v3(pos[t.x]))); cnt++; }
+        const int f = nt[s];
+        const int4 t = tri[f];
+        const float4 L = flen[f];
+        if (t.x > t.y) { len += L.x; cnt++; }
+        if (t.y > t.z) { len += L.y; cnt++; }
+        if (t.z > t.x) { len += L.z; cnt++; }
     }
 }
 
-// normal-flip test and skinny term over the ring of w with w moved to vm (faces holding `other` skipped)
+// normal-flip test and skinny term over the ring of w with w moved to vm (faces holding `other` skipped).
+// The flip sign dot(n_old, n_new / |n_new|) < 0 is taken from the unnormalised n_new when a float bound
+// proves it (|dot| > 1e-5 |n_old|_1 |n_new|_1, far above the ~1e-6 relative rounding of the normalised
+// form); otherwise the normalised form is evaluated exactly as the reference does.
 __device__ __forceinline__ bool ring_skinny(int w, int other, V3 vm, const int* __restrict__ nt_off,
                                             const int* __restrict__ nt, const int4* __restrict__ tri,
-                                            const float4* __restrict__ pos, float& qa, int& ntri) {
+                                            const float4* __restrict__ pos, const float4* __restrict__ flen,
+                                            const float4* __restrict__ fnrm, float& qa, int& ntri) {
     const float k4s3 = 4.0f * sqrtf(3.0f);
     const int b = nt_off[w + 1];
     for (int s = nt_off[w]; s < b; ++s) {
-        const int4 t = tri[nt[s]];
+        const int f = nt[s];
+        const int4 t = tri[f];
         if (t.x == other || t.y == other || t.z == other) continue;
-        const V3 o0 = v3(pos[t.x]), o1 = v3(pos[t.y]), o2 = v3(pos[t.z]);
-        const V3 n0 = (t.x == w) ? vm : o0, n1 = (t.y == w) ? vm : o1, n2 = (t.z == w) ? vm : o2;
-        V3 on = vcross(vsub(o1, o0), vsub(o2, o0));
-        on = vdiv(on, vnorm(on));
-        V3 nn = vcross(vsub(n1, n0), vsub(n2, n0));
-        nn = vdiv(nn, vnorm(nn));
-        if (vdot(on, nn) < 0) return false;
-        const float l01 = vnorm(vsub(n0, n1)), l12 = vnorm(vsub(n1, n2)), l20 = vnorm(vsub(n2, n0));
+        const float4 on4 = fnrm[f];
+        const V3 on = {on4.x, on4.y, on4.z};
+        const V3 n0 = (t.x == w) ? vm : v3(pos[t.x]);
+        const V3 n1 = (t.y == w) ? vm : v3(pos[t.y]);
+        const V3 n2 = (t.z == w) ? vm : v3(pos[t.z]);
+        const V3 nu = vcross(vsub(n1, n0), vsub(n2, n0));
+        const float du = vdot(on, nu);
+        const float bound = 1e-5f * (fabsf(on.x) + fabsf(on.y) + fabsf(on.z)) * (fabsf(nu.x) + fabsf(nu.y) + fabsf(nu.z));
+        if (du < -bound) return false;
+        if (!(du > bound)) {
+            const V3 nn = vdiv(nu, vnorm(nu));
+            if (vdot(on, nn) < 0) return false;
+        }
+        const float4 L = flen[f];
+        // lengths |n0 - n1|, |n1 - n2|, |n2 - n0|: an edge without w keeps the face's own edge length
+        const bool wx = t.x == w, wy = t.y == w, wz = t.z == w;
+        const float l01 = (!wx && !wy) ? L.x : vnorm(vsub(n0, n1));
+        const float l12 = (!wy && !wz) ? L.y : vnorm(vsub(n1, n2));
+        const float l20 = (!wz && !wx) ? L.z : vnorm(vsub(n2, n0));
+        const float sh = (l01 + l12 + l20) / 2;  // triangle_area (Heron), :368-375
+        const float area = sqrtf(sh * (sh - l01) * (sh - l12) * (sh - l20));
         // the reference's operator precedence: only the first squared length divides (pow(x, 2) == x * x)
-        const float e = k4s3 * tri_area(n0, n1, n2) / (l01 * l01) + l12 * l12 + l20 * l20 + 0.0000001f;
+        const float e = k4s3 * area / (l01 * l01) + l12 * l12 + l20 * l20 + 0.0000001f;
         qa += 1.0f - rclamp(e, 0.0f, 1.0f);
         ntri++;
     }
@@ -243,6 +275,7 @@ __device__ __forceinline__ uint32_t f2u_sat(float f) {
 // returns false when the reference leaves the stale cost in place
 __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restrict__ nt_off, const int* __restrict__ nt,
                                                 const int4* __restrict__ tri, const float4* __restrict__ pos,
+                                                const float4* __restrict__ flen, const float4* __restrict__ fnrm,
                                                 const Quadric* __restrict__ q, float scale, float tres, uint32_t& out) {
     // link condition
     int dup = 0;
@@ -261,15 +294,16 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
     if (dup != 2) return false;
     float len = 0.0f;
     int cnt = 0;
-    ring_len(u, nt_off, nt, tri, pos, len, cnt);
-    ring_len(v, nt_off, nt, tri, pos, len, cnt);
+    ring_len(u, nt_off, nt, tri, flen, len, cnt);
+    ring_len(v, nt_off, nt, tri, flen, len, cnt);
     const V3 v0 = v3(pos[u]), v1 = v3(pos[v]);
     len = len / (float)cnt / scale * tres;
     len = len + vnorm(vsub(v0, v1)) / scale * tres;
     const V3 vm = vdiv(vadd(v0, v1), 2.0f);
     float qa = 0.0f;
     int ntri = 0;
-    if (!ring_skinny(u, v, vm, nt_off, nt, tri, pos, qa, ntri) || !ring_skinny(v, u, vm, nt_off, nt, tri, pos, qa, ntri)) {
+    if (!ring_skinny(u, v, vm, nt_off, nt, tri, pos, flen, fnrm, qa, ntri) ||
+        !ring_skinny(v, u, vm, nt_off, nt, tri, pos, flen, fnrm, qa, ntri)) {
         out = 0xFFFFFFFFu;
         return true;
     }
@@ -294,6 +328,7 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
 __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const int2* __restrict__ edges,
                                                   const int* __restrict__ nt_off, const int* __restrict__ nt,
                                                   const int4* __restrict__ tri, const float4* __restrict__ pos,
+                                                  const float4* __restrict__ flen, const float4* __restrict__ fnrm,
                                                   const Quadric* __restrict__ q, const unsigned char* __restrict__ invalid,
                                                   uint32_t* cost, unsigned long long* vmin, const float* d_scale,
                                                   float tres, int is_stuck) {
@@ -310,7 +345,7 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
         } else if (is_stuck) {
             write = false;
         } else {
-            write = edge_cost_value(u, v, nt_off, nt, tri, pos, q, scale, tres, c);
+            write = edge_cost_value(u, v, nt_off, nt, tri, pos, flen, fnrm, q, scale, tres, c);
         }
         if (write) cost[e] = c;
         else c = cost[e];  // stale value of an earlier round
@@ -622,28 +657,54 @@ __global__ void k_export_mesh(int np, int nf, const float4* __restrict__ pos, co
 
 // ------------------------------------------------------------------ centring (pamo/__init__.py:60-72, 117, 126)
 // numpy float32 semantics: per-face ((a + b) + c) / 3, then a sequential float32 sum over faces / F.
+// Face means are written per coordinate (SoA) so that the sequential pass can stage them through shared
+// memory with coalesced loads; three lanes of one warp then run the three dependent add chains while the
+// other warps fetch the next tile.
 __global__ void k_face_means(const float* __restrict__ pts, const int* __restrict__ tris, int nf, float* fm) {
     for (int f = gtid(); f < nf; f += gstride()) {
         const int a = tris[3 * f], b = tris[3 * f + 1], c = tris[3 * f + 2];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) fm[3 * f + d] = ((pts[3 * a + d] + pts[3 * b + d]) + pts[3 * c + d]) / 3.0f;
+        for (int d = 0; d < 3; ++d) fm[(size_t)d * nf + f] = ((pts[3 * a + d] + pts[3 * b + d]) + pts[3 * c + d]) / 3.0f;
     }
 }
 
-__global__ void k_sequential_sum(const float* __restrict__ fm, int nf, float* center) {
-    const int d = threadIdx.x;
-    if (d >= 3) return;
+constexpr int kSumTile = 2048;
+
+__global__ void __launch_bounds__(1024) k_sequential_sum(const float* __restrict__ fm, int nf, float* center) {
+    __shared__ float buf[2][3][kSumTile];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ntiles = (nf + kSumTile - 1) / kSumTile;
+    auto load = [&](int t, int slot, int first_thread, int nthreads) {
+        const int base = t * kSumTile;
+        const int len = min(kSumTile, nf - base);
+        for (int i = (int)threadIdx.x - first_thread; i < 3 * kSumTile; i += nthreads) {
+            const int d = i / kSumTile, k = i - d * kSumTile;
+            if (k < len) buf[slot][d][k] = fm[(size_t)d * nf + base + k];
+        }
+    };
+    if (ntiles > 0) load(0, 0, 0, blockDim.x);
+    __syncthreads();
     float s = 0.0f;
-    int f = 0;
-    for (; f + 8 <= nf; f += 8) {
-        float x[8];
+    for (int t = 0; t < ntiles; ++t) {
+        const int cur = t & 1;
+        if (warp != 0) {
+            if (t + 1 < ntiles) load(t + 1, cur ^ 1, 32, blockDim.x - 32);
+        } else if (lane < 3) {
+            const int len = min(kSumTile, nf - t * kSumTile);
+            const float* x = buf[cur][lane];
+            int k = 0;
+            for (; k + 8 <= len; k += 8) {
+                float v[8];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) x[k] = fm[3 * (f + k) + d];
+                for (int j = 0; j < 8; ++j) v[j] = x[k + j];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) s += x[k];
+                for (int j = 0; j < 8; ++j) s += v[j];
+            }
+            for (; k < len; ++k) s += x[k];
+        }
+        __syncthreads();
     }
-    for (; f < nf; ++f) s += fm[3 * f + d];
-    center[d] = s / (float)nf;
+    if (warp == 0 && lane < 3) center[lane] = s / (float)nf;
 }
 
 __global__ void k_center_points(const float* __restrict__ pts, int np, const float* __restrict__ center, float4* out,
@@ -721,115 +782,122 @@ void launch_undo_bookkeeping(const int* verts_undo, int n_verts_undo, int is_stu
     if (is_stuck) {
         if (n_verts_undo > 0)
             k_undo_stuck<<<grid_for(n_verts_undo, kT), kT, 0, s>>>(verts_undo, n_verts_undo, tmp_undo, undo_list, pts_map,
-                                                                   pts_map_len);
+                                                                   pts_map_len); note_launch();
     } else if (n_verts_undo != 0) {
         cudaMemsetAsync(invalid, 0, invalid_len, s);
     }
     if (n_verts_undo > 0)
-        k_invalid_mark<<<grid_for(n_verts_undo, kT), kT, 0, s>>>(verts_undo, n_verts_undo, invalid, invalid_len);
+        k_invalid_mark<<<grid_for(n_verts_undo, kT), kT, 0, s>>>(verts_undo, n_verts_undo, invalid, invalid_len); note_launch();
 }
 
 void launch_load_points(const float* pts, int n, float4* pos, float4* orig_pos, int* occ, cudaStream_t s) {
-    k_load_points<<<grid_for(n, kT), kT, 0, s>>>(pts, n, pos, orig_pos, occ);
+    k_load_points<<<grid_for(n, kT), kT, 0, s>>>(pts, n, pos, orig_pos, occ); note_launch();
 }
 void launch_load_points4(const float4* pts, int n, float4* pos, float4* orig_pos, int* occ, cudaStream_t s) {
-    k_load_points4<<<grid_for(n, kT), kT, 0, s>>>(pts, n, pos, orig_pos, occ);
+    k_load_points4<<<grid_for(n, kT), kT, 0, s>>>(pts, n, pos, orig_pos, occ); note_launch();
 }
 void launch_load_tris(const int* tris, int n, int n_pts, int4* tri, RoundCounters* rc, cudaStream_t s) {
-    k_load_tris<<<grid_for(n, kT), kT, 0, s>>>(tris, n, n_pts, tri, rc);
+    k_load_tris<<<grid_for(n, kT), kT, 0, s>>>(tris, n, n_pts, tri, rc); note_launch();
 }
 void launch_load_tris4(const int4* tris, int n, int4* tri, cudaStream_t s) {
-    k_copy4<<<grid_for(n, kT), kT, 0, s>>>(tris, tri, n);
+    k_copy4<<<grid_for(n, kT), kT, 0, s>>>(tris, tri, n); note_launch();
 }
 void launch_copy_tris(const int4* src, int4* dst, int n, cudaStream_t s) {
-    k_copy4<<<grid_for(n, kT), kT, 0, s>>>(src, dst, n);
+    k_copy4<<<grid_for(n, kT), kT, 0, s>>>(src, dst, n); note_launch();
 }
 void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4* src, int4* dst, int n, cudaStream_t s) {
     (void)n;
     const int g = grid_for((long long)fb.n, kT);
-    k_shuffle_flags<<<g, kT, 0, s>>>(fb, flags);
+    k_shuffle_flags<<<g, kT, 0, s>>>(fb, flags); note_launch();
     exclusive_scan(flags, flags, nullptr, (int)fb.n + 1, nullptr, scan_scratch, s);
-    k_shuffle_gather<<<g, kT, 0, s>>>(fb, flags, src, dst);
+    k_shuffle_gather<<<g, kT, 0, s>>>(fb, flags, src, dst); note_launch();
 }
 
 void launch_face_counts(const int4* tri, const RoundCounters* rc, int n_tris_bound, int* valence, int* ecount,
                         cudaStream_t s) {
-    k_face_counts<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, valence, ecount);
+    k_face_counts<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, valence, ecount); note_launch();
 }
 void launch_fill_adjacency(const int4* tri, const RoundCounters* rc, int n_tris_bound, const int* nt_off, int* cursor,
                            int* nt, const int* edge_off, int2* edges, cudaStream_t s) {
-    k_fill_adjacency<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, nt_off, cursor, nt, edge_off, edges);
+    k_fill_adjacency<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, nt_off, cursor, nt, edge_off, edges); note_launch();
 }
 void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* nt_off, int* nt, cudaStream_t s) {
-    k_sort_adjacency<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt);
+    k_sort_adjacency<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt); note_launch();
+}
+void launch_face_geom(const RoundCounters* rc, int n_tris_bound, const int4* tri, const float4* pos, float4* flen,
+                      float4* fnrm, cudaStream_t s) {
+    k_face_geom<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(rc, tri, pos, flen, fnrm); note_launch();
 }
 void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
-                     const float4* pos, Quadric* q, cudaStream_t s) {
-    k_quadrics<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, pos, q);
+                     const float4* pos, const float4* fnrm, Quadric* q, cudaStream_t s) {
+    k_quadrics<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, pos, fnrm, q); note_launch();
 }
 void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s) {
-    k_edge_cost_capacity<<<1, 1, 0, s>>>(rc, d_cap);
-    k_edge_cost_zero<<<grid_for(phys_len, kT), kT, 0, s>>>(rc, edge_cost, phys_len);
+    k_edge_cost_capacity<<<1, 1, 0, s>>>(rc, d_cap); note_launch();
+    k_edge_cost_zero<<<grid_for(phys_len, kT), kT, 0, s>>>(rc, edge_cost, phys_len); note_launch();
 }
 void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int2* edges, const int* nt_off, const int* nt,
-                      const int4* tri, const float4* pos, const Quadric* q, const unsigned char* invalid,
-                      uint32_t* cost, unsigned long long* vmin, const float* d_scale, float tres, int is_stuck,
-                      cudaStream_t s) {
-    k_edge_cost<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, edges, nt_off, nt, tri, pos, q, invalid, cost, vmin, d_scale,
-                                                           tres, is_stuck);
+                      const int4* tri, const float4* pos, const float4* flen, const float4* fnrm, const Quadric* q,
+                      const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin, const float* d_scale,
+                      float tres, int is_stuck, cudaStream_t s) {
+    k_edge_cost<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, edges, nt_off, nt, tri, pos, flen, fnrm, q, invalid, cost,
+                                                           vmin, d_scale,
+                                                           tres, is_stuck); note_launch();
 }
 void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
                       unsigned long long* fkey, cudaStream_t s) {
-    k_face_keys<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(rc, tri, vmin, fkey);
+    k_face_keys<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(rc, tri, vmin, fkey); note_launch();
 }
 void launch_collapse(RoundCounters* rc, int n_edges_bound, const int2* edges, const uint32_t* cost, uint32_t collapse_t,
                      const unsigned long long* fkey, const int* nt_off, const int* nt, int4* tri, const int4* orig_tri,
                      float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s) {
     k_collapse<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, edges, cost, collapse_t, fkey, nt_off, nt, tri, orig_tri,
-                                                          pos, orig_pos, occ, win);
+                                                          pos, orig_pos, occ, win); note_launch();
 }
 void launch_compact_winners(const RoundCounters* rc, int n_edges_bound, const int* win_scan, int* collapsed,
                             cudaStream_t s) {
-    k_compact_winners<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, win_scan, collapsed);
+    k_compact_winners<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, win_scan, collapsed); note_launch();
 }
 void launch_remove_invalid(const RoundCounters* rc, int n_tris_bound, int4* tri, cudaStream_t s) {
-    k_remove_invalid<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(rc, tri);
+    k_remove_invalid<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(rc, tri); note_launch();
 }
 void launch_line_edges(RoundCounters* rc, int n_edges_bound, const int2* edges, const int* nt_off, const int* nt,
                        int4* tri, float4* pos, int* occ, int* line_buf, int line_cap, int* collapsed, cudaStream_t s) {
     (void)line_buf;
-    k_line_detect<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, edges, pos);
-    k_line_apply<<<1, 32, 0, s>>>(rc, edges, nt_off, nt, tri, pos, occ, collapsed, line_cap);
+    k_line_detect<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, edges, pos); note_launch();
+    k_line_apply<<<1, 32, 0, s>>>(rc, edges, nt_off, nt, tri, pos, occ, collapsed, line_cap); note_launch();
 }
 void launch_mark_query(const RoundCounters* rc, int n_edges_bound, const int* collapsed, const int2* edges,
                        const int* nt_off, const int* nt, int* qflag, cudaStream_t s) {
-    k_mark_query<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, collapsed, edges, nt_off, nt, qflag);
+    k_mark_query<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, collapsed, edges, nt_off, nt, qflag); note_launch();
 }
 void launch_compact_flags(const int* scan, int n_bound, const int* d_n, int* out_list, cudaStream_t s) {
-    k_compact_flags<<<grid_for(n_bound, kT), kT, 0, s>>>(scan, d_n, out_list);
+    k_compact_flags<<<grid_for(n_bound, kT), kT, 0, s>>>(scan, d_n, out_list); note_launch();
 }
 void launch_undo_check(RoundCounters* rc, int n_edges_bound, const int* collapsed, const int2* edges, const int* nt_off,
                        const int* nt, const unsigned char* hit, int* uflag, cudaStream_t s) {
-    k_undo_check<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, collapsed, edges, nt_off, nt, hit, uflag);
+    k_undo_check<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, collapsed, edges, nt_off, nt, hit, uflag); note_launch();
 }
 void launch_undo_apply(RoundCounters* rc, int n_edges_bound, const int* collapsed, const int* uscan, const int2* edges,
                        const int* nt_off, const int* nt, int4* tri, const int4* orig_tri, float4* pos,
                        const float4* orig_pos, int* occ, int* tmp_undo, int* undo_list, const int* pts_map,
                        int list_cap, cudaStream_t s) {
     k_undo_apply<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, collapsed, uscan, edges, nt_off, nt, tri, orig_tri, pos,
-                                                            orig_pos, occ, tmp_undo, undo_list, pts_map, list_cap, list_cap);
-    k_after_apply<<<1, 1, 0, s>>>(rc);
+                                                            orig_pos, occ, tmp_undo, undo_list, pts_map, list_cap, list_cap); note_launch();
+    k_after_apply<<<1, 1, 0, s>>>(rc); note_launch();
 }
-void launch_after_check(RoundCounters* rc, cudaStream_t s) { k_after_check<<<1, 1, 0, s>>>(rc); }
+void launch_after_check(RoundCounters* rc, cudaStream_t s) {
+    k_after_check<<<1, 1, 0, s>>>(rc); note_launch();
+}
 
 void launch_live_flags(const RoundCounters* rc, int n_tris_bound, const int4* tri, int* flags, cudaStream_t s) {
-    k_live_flags<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(rc, tri, flags);
+    k_live_flags<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(rc, tri, flags); note_launch();
 }
 void launch_compact_mesh(RoundCounters* rc, int n_pts_bound, int n_tris_bound, const float4* pos, const int* occ,
                          const int* pts_map, const int4* tri, const int* face_scan, float4* out_pos, int4* out_tri,
                          cudaStream_t s) {
     const int n = n_pts_bound > n_tris_bound ? n_pts_bound : n_tris_bound;
-    k_compact_mesh<<<grid_for(n, kT), kT, 0, s>>>(rc, pos, occ, pts_map, tri, face_scan, out_pos, out_tri);
+    k_compact_mesh<<<grid_for(n, kT), kT, 0, s>>>(rc, pos, occ, pts_map, tri, face_scan, out_pos, out_tri); note_launch();
 }
 void launch_export_round(const RoundCounters* rc, int n_pts, int n_tris, const float4* pos, const int4* tri,
                          const int* occ, const int* pts_map, const int* undo_list, float* verts, int* tris,
@@ -837,24 +905,24 @@ void launch_export_round(const RoundCounters* rc, int n_pts, int n_tris, const f
     (void)rc;
     const int n = n_pts > n_tris ? n_pts : n_tris;
     k_export_round<<<grid_for(n, kT), kT, 0, s>>>(n_pts, n_tris, pos, tri, occ, pts_map, undo_list, verts, tris, verts_occ,
-                                                  verts_map, verts_undo, n_undo);
+                                                  verts_map, verts_undo, n_undo); note_launch();
 }
 void launch_export_mesh(int n_pts, int n_tris, const float4* pos, const int4* tri, const float* add, float* verts,
                         int* tris, cudaStream_t s) {
     const int n = n_pts > n_tris ? n_pts : n_tris;
-    k_export_mesh<<<grid_for(n, kT), kT, 0, s>>>(n_pts, n_tris, pos, tri, add, verts, tris);
+    k_export_mesh<<<grid_for(n, kT), kT, 0, s>>>(n_pts, n_tris, pos, tri, add, verts, tris); note_launch();
 }
 
 void launch_center(const float* pts, const int* tris, int n_pts, int n_tris, float* face_mean, float* center,
                    float* d_scale, float4* pos_out, cudaStream_t s) {
     // center[0..2] = tris_mean; center[4..9] scratch (order-preserving extents)
-    k_face_means<<<grid_for(n_tris, kT), kT, 0, s>>>(pts, tris, n_tris, face_mean);
-    k_sequential_sum<<<1, 32, 0, s>>>(face_mean, n_tris, center);
+    k_face_means<<<grid_for(n_tris, kT), kT, 0, s>>>(pts, tris, n_tris, face_mean); note_launch();
+    k_sequential_sum<<<1, 1024, 0, s>>>(face_mean, n_tris, center); note_launch();
     unsigned* ext = (unsigned*)(center + 4);
     cudaMemsetAsync(ext, 0xFF, 3 * sizeof(unsigned), s);
     cudaMemsetAsync(ext + 3, 0x00, 3 * sizeof(unsigned), s);
-    k_center_points<<<grid_for(n_pts, kT), kT, 0, s>>>(pts, n_pts, center, pos_out, ext);
-    k_extents<<<1, 32, 0, s>>>(ext, d_scale);
+    k_center_points<<<grid_for(n_pts, kT), kT, 0, s>>>(pts, n_pts, center, pos_out, ext); note_launch();
+    k_extents<<<1, 32, 0, s>>>(ext, d_scale); note_launch();
 }
 
 }  // namespace pamo

@@ -8,6 +8,8 @@
 // reordered only where every branch it skips returns "no intersection" in the reference as well:
 //   * two or three shared vertex indices -> no intersection whatever the coplanarity test says;
 //   * two coordinate-shared vertices      -> no intersection whatever the coplanarity test says;
+//   * a float certificate of the reference's own coplanarity test (whose normal is not normalised, so on
+//     fine meshes nearly every pair of neighbours counts as coplanar and is skipped);
 //   * a float orientation filter with a rigorous error bound (Shewchuk's orient3d static bound written
 //     for binary32) that proves one triangle lies strictly on one side of the other's plane. For pairs
 //     with no shared vertex the reference then returns at its first or second side test (or earlier at
@@ -190,62 +192,121 @@ __device__ __forceinline__ bool strictly_one_side(const Tri9& A, const Tri9& B, 
     return true;
 }
 
-// The reference's per-pair decision: "cur" is the BVH hit, "qry" the querying face.
-// exact_count is incremented when the fp64 path runs.
-__device__ __forceinline__ bool pair_intersects(const float4 c0, const float4 c1, const float4 c2, const int4 ct,
-                                                const float4 q0, const float4 q1, const float4 q2, const int4 qt,
-                                                float eps, unsigned& exact_count) {
-    Tri9 A = {{{c0.x, c0.y, c0.z}, {c1.x, c1.y, c1.z}, {c2.x, c2.y, c2.z}}};
-    Tri9 B = {{{q0.x, q0.y, q0.z}, {q1.x, q1.y, q1.z}, {q2.x, q2.y, q2.z}}};
-    const int mx = floor_mean6(A.v[0][0], A.v[1][0], A.v[2][0], B.v[0][0], B.v[1][0], B.v[2][0]);
-    const int my = floor_mean6(A.v[0][1], A.v[1][1], A.v[2][1], B.v[0][1], B.v[1][1], B.v[2][1]);
-    const int mz = floor_mean6(A.v[0][2], A.v[1][2], A.v[2][2], B.v[0][2], B.v[1][2], B.v[2][2]);
+// Float certificate for the reference's coplanarity test (tri_tri_3d.cuh:99-129): +1 when every vertex of B
+// certainly has |n_a . (b - a1)| <= scale * 1e-6 in the reference's fp64 evaluation, -1 when one certainly
+// exceeds it, 0 when undecided. `scale` is the largest absolute coordinate of the six (exact in float).
+__device__ __forceinline__ int coplanar_f(const Tri9& A, const Tri9& B, float cmax) {
+    const float e0x = A.v[0][0] - A.v[1][0], e0y = A.v[0][1] - A.v[1][1], e0z = A.v[0][2] - A.v[1][2];
+    const float e1x = A.v[2][0] - A.v[1][0], e1y = A.v[2][1] - A.v[1][1], e1z = A.v[2][2] - A.v[1][2];
+    const float nsum = fabsf(e0y * e1z - e0z * e1y) + fabsf(e0z * e1x - e0x * e1z) + fabsf(e0x * e1y - e0y * e1x);
+    const float abs_err = 1e-10f * nsum * (cmax + 1.0f);
+    const float eps_lo = cmax * 1e-6f * (1.0f - 1e-5f), eps_hi = cmax * 1e-6f * (1.0f + 1e-5f);
+    bool all_in = true;
+    for (int k = 0; k < 3; ++k) {
+        const float* a0 = A.v[0];
+        const float* a1 = A.v[1];
+        const float* a2 = A.v[2];
+        const float* p = B.v[k];
+        const float adx = a0[0] - p[0], ady = a0[1] - p[1], adz = a0[2] - p[2];
+        const float bdx = a1[0] - p[0], bdy = a1[1] - p[1], bdz = a1[2] - p[2];
+        const float cdx = a2[0] - p[0], cdy = a2[1] - p[1], cdz = a2[2] - p[2];
+        const float bc = bdx * cdy - bdy * cdx, ca = cdx * ady - cdy * adx, ab = adx * bdy - ady * bdx;
+        const float det = adz * bc + bdz * ca + cdz * ab;
+        const float perm = (fabsf(bdx * cdy) + fabsf(bdy * cdx)) * fabsf(adz) + (fabsf(cdx * ady) + fabsf(cdy * adx)) * fabsf(bdz) +
+                           (fabsf(adx * bdy) + fabsf(ady * bdx)) * fabsf(cdz);
+        const float err = 8.0e-7f * perm + abs_err + 1e-30f;
+        const float m = fabsf(det);
+        if (m - err > eps_hi) return -1;  // this vertex certainly lies off the plane
+        if (m + err >= eps_lo) all_in = false;
+    }
+    return all_in ? 1 : 0;
+}
+
+// Translated pair geometry shared by the float filter and the fp64 path.
+struct PairGeom {
+    Tri9 A, B;  // A = BVH hit ("current"), B = querying face, both translated
+    int shared, sa, sb;
+    float cmax;
+};
+
+__device__ __forceinline__ void pair_geom(const float4 c0, const float4 c1, const float4 c2, const int4 ct, const float4 q0,
+                                          const float4 q1, const float4 q2, const int4 qt, PairGeom& g) {
+    g.A = {{{c0.x, c0.y, c0.z}, {c1.x, c1.y, c1.z}, {c2.x, c2.y, c2.z}}};
+    g.B = {{{q0.x, q0.y, q0.z}, {q1.x, q1.y, q1.z}, {q2.x, q2.y, q2.z}}};
+    const int mx = floor_mean6(g.A.v[0][0], g.A.v[1][0], g.A.v[2][0], g.B.v[0][0], g.B.v[1][0], g.B.v[2][0]);
+    const int my = floor_mean6(g.A.v[0][1], g.A.v[1][1], g.A.v[2][1], g.B.v[0][1], g.B.v[1][1], g.B.v[2][1]);
+    const int mz = floor_mean6(g.A.v[0][2], g.A.v[1][2], g.A.v[2][2], g.B.v[0][2], g.B.v[1][2], g.B.v[2][2]);
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
-        A.v[v][0] -= mx; A.v[v][1] -= my; A.v[v][2] -= mz;
-        B.v[v][0] -= mx; B.v[v][1] -= my; B.v[v][2] -= mz;
+        g.A.v[v][0] -= mx; g.A.v[v][1] -= my; g.A.v[v][2] -= mz;
+        g.B.v[v][0] -= mx; g.B.v[v][1] -= my; g.B.v[v][2] -= mz;
     }
     const int ca[3] = {ct.x, ct.y, ct.z}, qb[3] = {qt.x, qt.y, qt.z};
-    int shared = 0, sa = -1, sb = -1;
+    g.shared = 0;
+    g.sa = -1;
+    g.sb = -1;
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
         for (int b = 0; b < 3; ++b)
             if (ca[a] == qb[b]) {
-                ++shared;
-                sa = a;
-                sb = b;
+                ++g.shared;
+                g.sa = a;
+                g.sb = b;
             }
-    if (shared >= 2) return false;
+    g.cmax = 0.0f;
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) g.cmax = fmaxf(g.cmax, fmaxf(fabsf(g.A.v[v][d]), fabsf(g.B.v[v][d])));
+}
+
+// true when the reference's decision is certainly "no intersection" without the fp64 path
+__device__ __forceinline__ bool pair_certainly_disjoint(const PairGeom& g) {
+    if (g.shared >= 2) return true;
     {
         const float e6 = 1e-6f;
         int s = 0;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
-            s += (same_eps(A.v[i], B.v[0], e6) || same_eps(A.v[i], B.v[1], e6) || same_eps(A.v[i], B.v[2], e6)) ? 1 : 0;
+            s += (same_eps(g.A.v[i], g.B.v[0], e6) || same_eps(g.A.v[i], g.B.v[1], e6) || same_eps(g.A.v[i], g.B.v[2], e6)) ? 1 : 0;
+        if (s >= 2) return true;
+    }
+    if (coplanar_f(g.A, g.B, g.cmax) == 1) return true;
+    if (g.shared == 0) return strictly_one_side(g.A, g.B, -1, g.cmax) || strictly_one_side(g.B, g.A, -1, g.cmax);
+    return strictly_one_side(g.A, g.B, g.sb, g.cmax) && strictly_one_side(g.B, g.A, g.sa, g.cmax);
+}
+
+// the reference's fp64 decision on a translated pair
+__device__ __forceinline__ bool pair_exact(const PairGeom& g, float eps) {
+    if (g.shared >= 2) return false;
+    if (coplanar_db(g.A, g.B)) return false;
+    {
+        const float e6 = 1e-6f;
+        int s = 0;
+        for (int i = 0; i < 3; ++i)
+            s += (same_eps(g.A.v[i], g.B.v[0], e6) || same_eps(g.A.v[i], g.B.v[1], e6) || same_eps(g.A.v[i], g.B.v[2], e6)) ? 1 : 0;
         if (s >= 2) return false;
     }
-    float cmax = 0.0f;
-#pragma unroll
-    for (int v = 0; v < 3; ++v)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) cmax = fmaxf(cmax, fmaxf(fabsf(A.v[v][d]), fabsf(B.v[v][d])));
-    if (shared == 0) {
-        if (strictly_one_side(A, B, -1, cmax) || strictly_one_side(B, A, -1, cmax)) return false;
-    } else {
-        if (strictly_one_side(A, B, sb, cmax) && strictly_one_side(B, A, sa, cmax)) return false;
-    }
-    ++exact_count;
-    if (coplanar_db(A, B)) return false;
     float r1[3], r2[3];
-    if (!isect_tri_tri_db(A, B, r1, r2)) return false;
+    if (!isect_tri_tri_db(g.A, g.B, r1, r2)) return false;
     const float dx = fabsf(r2[0] - r1[0]), dy = fabsf(r2[1] - r1[1]), dz = fabsf(r2[2] - r1[2]);
     float d = -INFINITY;
     if (dx > d) d = dx;
     if (dy > d) d = dy;
     if (dz > d) d = dz;
-    if (d < eps && shared == 1) return false;
+    if (d < eps && g.shared == 1) return false;
     return true;
+}
+
+// The reference's full per-pair decision through the fp64 path: "cur" is the BVH hit, "qry" the querying
+// face. Arguments by value so that callers keep their own geometry in registers.
+__device__ __noinline__ bool pair_decide_exact(const float4 c0, const float4 c1, const float4 c2, const int4 ct,
+                                               const float4 q0, const float4 q1, const float4 q2, const int4 qt,
+                                               float eps) {
+    PairGeom g;
+    pair_geom(c0, c1, c2, ct, q0, q1, q2, qt, g);
+    return pair_exact(g, eps);
 }
 
 }  // namespace pamo

@@ -32,3 +32,20 @@ def euler(f):
     ne = len(np.unique(e, axis=0))
     nv = len(np.unique(f))
     return nv - ne + len(f)
+
+
+def with_degenerate_face(seed=5):
+    """A sphere with one face whose vertex repeats (index-degenerate)."""
+    v, f = sphere(5, seed=seed)
+    f = f.copy()
+    f[7] = [f[7, 0], f[7, 0], f[7, 2]]
+    return v, f
+
+
+def with_coincident_edge(seed=6):
+    """A sphere where one edge has both endpoints at the same position (zero length)."""
+    v, f = sphere(5, seed=seed)
+    v = v.copy()
+    a, b = f[11, 0], f[11, 1]
+    v[b] = v[a]
+    return v, f

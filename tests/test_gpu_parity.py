@@ -20,6 +20,8 @@ def _cases():
         "sphere4": meshes.sphere(4),
         "sphere8": meshes.sphere(8, L=5, sigma=0.05, seed=3),
         "open_patch": meshes.open_patch(),
+        "degenerate_face": meshes.with_degenerate_face(),
+        "coincident_edge": meshes.with_coincident_edge(),
     }
 
 
@@ -59,7 +61,7 @@ def _chain(v, f, rounds, gpu: bool):
     return outs
 
 
-@pytest.mark.parametrize("name", ["octahedron", "sphere4", "sphere8", "open_patch"])
+@pytest.mark.parametrize("name", ["octahedron", "sphere4", "sphere8", "open_patch", "degenerate_face", "coincident_edge"])
 def test_rounds_match_oracle(name):
     v, f = _cases()[name]
     g = _chain(v, f, 12, gpu=True)

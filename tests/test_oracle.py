@@ -94,3 +94,23 @@ def test_open_mesh_boundary_uses_stale_costs():
     isb = np.array([tuple(x) in boundary for x in e])
     assert isb.any()
     assert np.all(c[isb] == 0)
+
+
+def _slots(c, q, ci, qi):
+    ids, pts = {}, []
+    for tri, idx in ((c, ci), (q, qi)):
+        for p, i in zip(tri, idx):
+            if int(i) not in ids:
+                ids[int(i)] = len(pts)
+                pts.append(p)
+    return (np.array(pts, np.float32), np.array([ids[int(i)] for i in ci], np.int32),
+            np.array([ids[int(i)] for i in qi], np.int32))
+
+
+def test_pair_decision_matches_reference_golden():
+    g = np.load(os.path.join(GOLDEN, "tritri_cases.npz"))
+    exp = g["expected"]
+    assert exp.sum() > 1000 and (exp == 0).sum() > 1000
+    for k in range(len(exp)):
+        P, c, q = _slots(g["cur"][k], g["qry"][k], g["cur_ids"][k], g["qry_ids"][k])
+        assert orc.pair_intersects(P, c, q, 1e-3) == bool(exp[k]), k
