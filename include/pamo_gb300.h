@@ -82,6 +82,15 @@ int pamo_simplify_result(pamo_ctx* ctx, float* verts, int32_t* tris, pamo_stream
 /* Face count after each round of the last pamo_simplify_device call (host array of `capacity`). */
 int pamo_simplify_round_faces(const pamo_ctx* ctx, int32_t* faces_per_round, int32_t capacity);
 
+/*
+ * The reference's self-intersection check over a whole mesh (selfx::self_intersect,
+ * simp_cuda/src/bvh/self_intersect.cuh:151-392): face_hit[f] = 1 iff face f takes part in a (query, hit)
+ * pair the reference's tri-tri filter reports, else 0 (uint8, device buffer of n_triangles). Faces equal
+ * to (-1, -1, -1) are skipped. Synchronises `stream`.
+ */
+int pamo_self_intersect(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                        int32_t n_triangles, uint8_t* face_hit, pamo_stream stream);
+
 /* Totals over the rounds of the last pamo_simplify_device call, written to out[0..n): vertices, faces,
  * edges, winners, query-face tests (query faces x checks), candidate pairs, pairs that took the fp64 path,
  * intersection checks, live faces indexed by the LBVH (x checks), collapsed edges. Returns 10. No reference

@@ -34,6 +34,8 @@ def lib():
         L.oracle_tris_mean.argtypes = [P, P, I, P]
         L.oracle_run.argtypes = [P, P, P, I, I, D, I, F, I, LL, P, P]
         L.oracle_run_result.argtypes = [P, P, P, P]
+        L.oracle_self_intersect.argtypes = [P, P, P, I, I, P]
+        L.oracle_self_intersect.restype = LL
         _LIB = L
     return _LIB
 
@@ -120,6 +122,14 @@ class Oracle:
         out = np.zeros(max(n, 1), np.uint32)
         lib().oracle_edge_costs(self._h, _p(out))
         return out[:n]
+
+    def self_intersect(self, points, triangles):
+        """Per-face flags of the reference's global self-intersection check; returns (flags, hit tests)."""
+        pts = np.ascontiguousarray(points, np.float32)
+        tri = np.ascontiguousarray(triangles, np.int32)
+        out = np.zeros(len(tri), np.uint8)
+        n = lib().oracle_self_intersect(self._h, _p(pts), _p(tri), len(pts), len(tri), _p(out))
+        return out, int(n)
 
     def run(self, points, triangles, ratio, tolerance=4, threshold=1e-3, iters=1000000, min_verts=10000000000):
         """The stage-2 loop of PaMO.run: returns (verts, faces, faces_per_round)."""

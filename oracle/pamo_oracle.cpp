@@ -951,6 +951,19 @@ int oracle_pair_intersects(const float* pts, const int* cur, const int* qry, flo
 
 void oracle_tris_mean(const float* pts, const int* tris, int nT, float* out) { tris_mean_numpy(pts, tris, nT, out); }
 
+// selfx::self_intersect (self_intersect.cuh:151-392) on a whole mesh: out[f] = 1 iff face f belongs to a
+// (query, hit) pair the reference records. Returns the number of intersecting (query, hit) tests.
+long long oracle_self_intersect(void* h, const float* pts, const int* tris, int nP, int nT, unsigned char* out) {
+    Oracle& o = ((pamo_oracle_handle*)h)->o;
+    o.points.assign((const P3*)pts, (const P3*)pts + nP);
+    o.tris.assign((const F3*)tris, (const F3*)tris + nT);
+    o.n_pts = nP;
+    o.n_tris = nT;
+    long long hits = o.self_intersect();
+    std::memcpy(out, o.face_hit.data(), nT);
+    return hits;
+}
+
 // The stage-2 round loop of PaMO.run (pamo/__init__.py:95-163) with stage 1 and stage 3 off.
 // Returns the number of rounds; the result is read with oracle_run_result.
 int oracle_run(void* h, const float* pts, const int* tris, int nP, int nT, double ratio, int tolerance, float threshold,

@@ -5,7 +5,7 @@ The compute path is the CUDA library ``_lib/libpamo_gb300.so`` reached through i
 (include/pamo_gb300.h); build it with ``pamo_gb300._build.build()``.
 """
 
-from .api import Context, CUDSP_Free, PaMO, launch_count, round_faces, simplify  # noqa: F401
+from .api import Context, CUDSP_Free, PaMO, launch_count, round_faces, self_intersect, simplify  # noqa: F401
 from ._native import PamoError  # noqa: F401
 
-__all__ = ["Context", "CUDSP_Free", "PaMO", "PamoError", "simplify", "round_faces", "launch_count"]
+__all__ = ["Context", "CUDSP_Free", "PaMO", "PamoError", "simplify", "round_faces", "launch_count", "self_intersect"]

@@ -18,7 +18,7 @@ import torch
 
 from . import _native
 
-__all__ = ["Context", "CUDSP_Free", "PaMO", "simplify"]
+__all__ = ["Context", "CUDSP_Free", "PaMO", "simplify", "self_intersect"]
 
 
 def _ptr(t: torch.Tensor) -> ctypes.c_void_p:
@@ -175,6 +175,23 @@ def simplify(points: torch.Tensor, triangles: torch.Tensor, ratio: float, tolera
         faces = torch.empty((ont.value, 3), dtype=torch.int32, device=dev)
         _native.check(lib.pamo_simplify_result(ctx.handle, _ptr(verts), _ptr(faces), st), ctx.handle)
     return verts, faces, rounds.value
+
+
+def self_intersect(points: torch.Tensor, triangles: torch.Tensor, ctx: Context | None = None) -> torch.Tensor:
+    """Per-face flags (uint8, CUDA) of the reference's self-intersection check over the whole mesh."""
+    _check_input(points, "points", torch.float32)
+    _check_input(triangles, "triangles", torch.int32)
+    dev = points.device
+    if ctx is None:
+        ctx = Context(dev)
+    out = torch.empty(int(triangles.shape[0]), dtype=torch.uint8, device=dev)
+    with torch.cuda.device(dev):
+        _native.check(
+            _native.load().pamo_self_intersect(ctx.handle, _ptr(points), _ptr(triangles), int(points.shape[0]),
+                                               int(triangles.shape[0]), _ptr(out), _stream(dev)),
+            ctx.handle,
+        )
+    return out
 
 
 def launch_count() -> int:

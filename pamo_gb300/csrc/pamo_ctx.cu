@@ -610,6 +610,37 @@ int pamo_simplify_result(pamo_ctx* ctx, float* verts, int32_t* tris, pamo_stream
     return ctx->check(cudaGetLastError(), "export");
 }
 
+int pamo_self_intersect(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                        int32_t n_triangles, uint8_t* face_hit, pamo_stream stream) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (n_points < 1 || n_triangles < 1 || !points || !triangles || !face_hit)
+        return ctx->fail(PAMO_ERR_INVALID_ARG, "invalid sizes or null pointers");
+    cudaSetDevice(ctx->device);
+    ctx->stream = (cudaStream_t)stream;
+    cudaStream_t s = ctx->stream;
+    int r;
+    if ((r = ctx->ensure_vertex_buffers(n_points)) || (r = ctx->ensure_face_buffers(n_triangles))) return r;
+    RoundCounters* h = ctx->h_rc;
+    std::memset(h, 0, sizeof(RoundCounters));
+    h->n_pts = n_points;
+    h->n_tris = n_triangles;
+    cudaMemcpyAsync(ctx->rc, h, sizeof(RoundCounters), cudaMemcpyHostToDevice, s);
+    launch_load_points(points, n_points, ctx->pos.p, ctx->orig_pos.p, ctx->occ.p, s);
+    launch_load_tris(triangles, n_triangles, n_points, ctx->tri.p, ctx->rc, s);
+    // every live face queries
+    launch_live_flags(ctx->rc, n_triangles, ctx->tri.p, ctx->qflag.p, s);
+    exclusive_scan(ctx->qflag.p, ctx->qflag.p, &ctx->rc->n_tris, 1, &ctx->rc->n_query, ctx->scan_scratch, s);
+    launch_compact_flags(ctx->qflag.p, n_triangles, &ctx->rc->n_tris, ctx->qlist.p, s);
+    cudaMemsetAsync(ctx->hit.p, 0, n_triangles + 1, s);
+    bvh_build(ctx->bvh, ctx->tri.p, ctx->pos.p, ctx->rc, n_triangles, s);
+    bvh_query(ctx->bvh, ctx->tri.p, ctx->pos.p, ctx->qlist.p, ctx->qflag.p, ctx->hit.p, ctx->exact_list.p,
+              (int)ctx->exact_list.n, ctx->rc, n_triangles, kTriEps, s);
+    cudaMemcpyAsync(face_hit, ctx->hit.p, n_triangles, cudaMemcpyDeviceToDevice, s);
+    if ((r = ctx->read_counters())) return r;
+    return ctx->status_to_error(ctx->h_rc->status);
+}
+
 int pamo_profile_enable(pamo_ctx* ctx, int32_t enable) {
     if (!ctx) return PAMO_ERR_INVALID_ARG;
     cudaSetDevice(ctx->device);

@@ -49,3 +49,14 @@ def with_coincident_edge(seed=6):
     a, b = f[11, 0], f[11, 1]
     v[b] = v[a]
     return v, f
+
+
+def tangled(n=8, seed=9, frac=0.08, amp=0.25):
+    """A sphere with a fraction of vertices moved in random directions by up to `amp` (about two edge
+    lengths at n = 10), which folds the surface so that faces intersect."""
+    rng = np.random.default_rng(seed)
+    v, f = sphere(n, seed=seed)
+    v = v.copy()
+    pick = rng.choice(len(v), max(1, int(frac * len(v))), replace=False)
+    v[pick] += rng.uniform(-amp, amp, (len(pick), 3)).astype(np.float32)
+    return v, f

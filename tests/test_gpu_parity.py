@@ -22,6 +22,8 @@ def _cases():
         "open_patch": meshes.open_patch(),
         "degenerate_face": meshes.with_degenerate_face(),
         "coincident_edge": meshes.with_coincident_edge(),
+        "tangled": meshes.tangled(10, seed=9, amp=0.25),
+        "tangled_strong": meshes.tangled(10, seed=10, amp=0.4),
     }
 
 
@@ -61,7 +63,8 @@ def _chain(v, f, rounds, gpu: bool):
     return outs
 
 
-@pytest.mark.parametrize("name", ["octahedron", "sphere4", "sphere8", "open_patch", "degenerate_face", "coincident_edge"])
+@pytest.mark.parametrize("name", ["octahedron", "sphere4", "sphere8", "open_patch", "degenerate_face", "coincident_edge",
+                                  "tangled", "tangled_strong"])
 def test_rounds_match_oracle(name):
     v, f = _cases()[name]
     g = _chain(v, f, 12, gpu=True)
