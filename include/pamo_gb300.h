@@ -91,6 +91,19 @@ int pamo_simplify_round_faces(const pamo_ctx* ctx, int32_t* faces_per_round, int
 int pamo_self_intersect(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
                         int32_t n_triangles, uint8_t* face_hit, pamo_stream stream);
 
+/*
+ * pamo_self_intersect without any device allocation, for callers that must not allocate device memory
+ * (hosts that own a fixed memory budget and forbid cudaMalloc/cudaFree by plug-ins, or code that cannot
+ * afford the device synchronisation an allocation may cause). No counterpart in the reference.
+ * Same result as pamo_self_intersect; needs no context. Scratch is a 24 MiB array in device memory that
+ * the library holds on every GPU that loads it; its address is looked up on the first call made on each
+ * device, so make that first call before any stream capture. Limits: n_points <= 65536 and
+ * n_triangles <= 65536, else PAMO_ERR_CAPACITY. All calls share the scratch: calls that overlap on the
+ * GPU race. Uses the current device; synchronises `stream`.
+ */
+int pamo_self_intersect_noalloc(const float* points, const int32_t* triangles, int32_t n_points,
+                                int32_t n_triangles, uint8_t* face_hit, pamo_stream stream);
+
 /* Totals over the rounds of the last pamo_simplify_device call, written to out[0..n): vertices, faces,
  * edges, winners, query-face tests (query faces x checks), candidate pairs, pairs that took the fp64 path,
  * intersection checks, live faces indexed by the LBVH (x checks), collapsed edges. Returns 10. No reference

@@ -46,6 +46,7 @@ SIGNATURES = {
     "pamo_simplify_result": (ctypes.c_int, [_P, _P, _P, _P]),
     "pamo_simplify_round_faces": (ctypes.c_int, [_P, _PI32, _I32]),
     "pamo_self_intersect": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _P, _P]),
+    "pamo_self_intersect_noalloc": (ctypes.c_int, [_P, _P, _I32, _I32, _P, _P]),
     "pamo_run_totals": (ctypes.c_int, [_P, _PI64, _I32]),
     "pamo_launch_count": (ctypes.c_int64, []),
     "pamo_profile_enable": (ctypes.c_int, [_P, _I32]),
