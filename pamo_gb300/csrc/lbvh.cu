@@ -266,10 +266,13 @@ __global__ void __launch_bounds__(256) k_bottom_up(RoundCounters* rc, const int2
 }
 
 // ---------------------------------------------------------------- localized query
-// Pass 1 (k_query): one thread per query face walks the tree with its stack in shared memory. Every
-// overlapping leaf g is a candidate pair; a pair of two query faces is taken only by the lower face index
-// (and then flags both faces). Pairs the float certificates decide are done; the rest are appended to
-// the exact list for pass 2. Pass 2 (k_query_exact) evaluates the fp64 decision, one pair per thread.
+// 1. k_query_order: the query faces in leaf (Morton) order, so that neighbouring threads walk the same
+//    part of the tree and test neighbouring faces.
+// 2. k_traverse: one thread per query face walks the tree with its stack in shared memory and emits every
+//    overlapping leaf g as a candidate pair (f, g); a pair of two query faces is emitted only by the lower
+//    face index. Beyond the pair list's capacity the pair is decided in place.
+// 3. k_pairs: one thread per candidate pair runs the reference's decision in both orders (float
+//    certificates first, the fp64 path only for undecided pairs) and flags both faces when it holds.
 __device__ __forceinline__ int warp_append(int* counter) {
     const unsigned am = __activemask();
     const int lane = threadIdx.x & 31;
@@ -280,25 +283,56 @@ __device__ __forceinline__ int warp_append(int* counter) {
     return base + __popc(am & ((1u << lane) - 1u));
 }
 
-__global__ void __launch_bounds__(kQueryThreads) k_query(const int2* __restrict__ child, const float4* __restrict__ nlo,
-                                                          const float4* __restrict__ nhi, const float4* __restrict__ llo,
-                                                          const float4* __restrict__ lhi, const int* __restrict__ leaf_face,
-                                                          const float4* __restrict__ box_lo, const float4* __restrict__ box_hi,
-                                                          const int4* __restrict__ tri, const float4* __restrict__ pos,
-                                                          const int* __restrict__ qlist, const int* __restrict__ qscan,
-                                                          unsigned char* hit, int2* exact_list, int exact_cap,
-                                                          RoundCounters* rc, float eps) {
+__device__ __forceinline__ bool decide_pair(int f, int g, const int4* __restrict__ tri, const float4* __restrict__ pos,
+                                            float eps, unsigned& exact) {
+    const int4 qt = tri[f], gt = tri[g];
+    const float4 q0 = pos[qt.x], q1 = pos[qt.y], q2 = pos[qt.z];
+    const float4 g0 = pos[gt.x], g1 = pos[gt.y], g2 = pos[gt.z];
+    PairGeom ga, gb;
+    pair_geom(g0, g1, g2, gt, q0, q1, q2, qt, ga);  // reference order: the hit is "current"
+    pair_geom(q0, q1, q2, qt, g0, g1, g2, gt, gb);  // the order seen from g's own query
+    const bool need_a = !pair_certainly_disjoint(ga);
+    const bool need_b = !pair_certainly_disjoint(gb);
+    if (!need_a && !need_b) return false;
+    exact += (unsigned)need_a + (unsigned)need_b;
+    return (need_a && pair_decide_exact(g0, g1, g2, gt, q0, q1, q2, qt, eps)) ||
+           (need_b && pair_decide_exact(q0, q1, q2, qt, g0, g1, g2, gt, eps));
+}
+
+__global__ void __launch_bounds__(256) k_query_order(const RoundCounters* rc, const int* __restrict__ leaf_face,
+                                                     const int* __restrict__ qscan, int* flags) {
+    const int n = rc->n_live;
+    for (int i = gtid(); i < n; i += gstride()) {
+        const int f = leaf_face[i];
+        flags[i] = (qscan[f + 1] != qscan[f]) ? 1 : 0;
+    }
+    if (gtid() == 0) flags[n] = 0;
+}
+
+__global__ void __launch_bounds__(256) k_query_gather(const RoundCounters* rc, const int* __restrict__ leaf_face,
+                                                      const int* __restrict__ scan, int* qsorted) {
+    const int n = rc->n_live;
+    for (int i = gtid(); i < n; i += gstride())
+        if (scan[i + 1] != scan[i]) qsorted[scan[i]] = leaf_face[i];
+}
+
+__global__ void __launch_bounds__(kQueryThreads) k_traverse(const int2* __restrict__ child, const float4* __restrict__ nlo,
+                                                             const float4* __restrict__ nhi, const float4* __restrict__ llo,
+                                                             const float4* __restrict__ lhi, const int* __restrict__ leaf_face,
+                                                             const float4* __restrict__ box_lo,
+                                                             const float4* __restrict__ box_hi, const int4* __restrict__ tri,
+                                                             const float4* __restrict__ pos, const int* __restrict__ qsorted,
+                                                             const int* __restrict__ qscan, unsigned char* hit,
+                                                             int2* pairs_out, int pair_cap, RoundCounters* rc, float eps) {
     __shared__ int stack[kStackDepth][kQueryThreads];
-    const int nq = rc->n_query;
+    const int nq = rc->pad[2];
     const int nl = rc->n_live;
     int* n_list = &rc->pad[1];
-    unsigned long long pairs = 0;
+    unsigned long long npairs = 0;
     unsigned exact = 0;
     for (int qi = gtid(); qi < nq; qi += gstride()) {
-        const int f = qlist[qi];
-        const int4 qt = tri[f];
-        if (qt.x == -1 || nl < 2) continue;
-        const float4 q0 = pos[qt.x], q1 = pos[qt.y], q2 = pos[qt.z];
+        const int f = qsorted[qi];
+        if (nl < 2) continue;
         const float4 qlo = box_lo[f], qhi = box_hi[f];
         int sp = 0;
         int node = 0;
@@ -320,23 +354,13 @@ __global__ void __launch_bounds__(kQueryThreads) k_query(const int2* __restrict_
                     const int g = leaf_face[li];
                     if (g == f) continue;
                     if (g < f && qscan[g + 1] != qscan[g]) continue;  // the lower query face owns the pair
-                    const int4 gt = tri[g];
-                    const float4 g0 = pos[gt.x], g1 = pos[gt.y], g2 = pos[gt.z];
-                    ++pairs;
-                    PairGeom ga, gb;
-                    pair_geom(g0, g1, g2, gt, q0, q1, q2, qt, ga);  // reference order: hit is "current"
-                    pair_geom(q0, q1, q2, qt, g0, g1, g2, gt, gb);  // the order seen from g's own query
-                    const int mask = (pair_certainly_disjoint(ga) ? 0 : 1) | (pair_certainly_disjoint(gb) ? 0 : 2);
-                    if (mask) {
-                        exact += __popc(mask);
-                        const int at = warp_append(n_list);
-                        if (at < exact_cap) {
-                            exact_list[at] = make_int2(f, g | (mask << 30));
-                        } else if (((mask & 1) && pair_decide_exact(g0, g1, g2, gt, q0, q1, q2, qt, eps)) ||
-                                   ((mask & 2) && pair_decide_exact(q0, q1, q2, qt, g0, g1, g2, gt, eps))) {
-                            hit[f] = 1;
-                            hit[g] = 1;
-                        }
+                    ++npairs;
+                    const int at = warp_append(n_list);
+                    if (at < pair_cap) {
+                        pairs_out[at] = make_int2(f, g);
+                    } else if (decide_pair(f, g, tri, pos, eps, exact)) {
+                        hit[f] = 1;
+                        hit[g] = 1;
                     }
                 } else {
                     if (boxes_overlap(qlo, qhi, nlo[x], nhi[x])) next[nn++] = x;
@@ -358,34 +382,29 @@ __global__ void __launch_bounds__(kQueryThreads) k_query(const int2* __restrict_
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
-        pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+        npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
         exact += __shfl_xor_sync(0xffffffffu, exact, o);
     }
     if ((threadIdx.x & 31) == 0) {
-        if (pairs) atomicAdd(&rc->n_pairs, pairs);
+        if (npairs) atomicAdd(&rc->n_pairs, npairs);
         if (exact) atomicAdd(&rc->n_exact, (unsigned long long)exact);
     }
 }
 
-__global__ void __launch_bounds__(128) k_query_exact(const int4* __restrict__ tri, const float4* __restrict__ pos,
-                                                     const int2* __restrict__ exact_list, int exact_cap,
-                                                     unsigned char* hit, const RoundCounters* rc, float eps) {
-    const int n = min(rc->pad[1], exact_cap);
+__global__ void __launch_bounds__(128) k_pairs(const int4* __restrict__ tri, const float4* __restrict__ pos,
+                                               const int2* __restrict__ pair_list, int pair_cap, unsigned char* hit,
+                                               RoundCounters* rc, float eps) {
+    const int n = min(rc->pad[1], pair_cap);
+    unsigned exact = 0;
     for (int i = gtid(); i < n; i += gstride()) {
-        const int2 e = exact_list[i];
-        const int f = e.x, g = e.y & 0x3fffffff, mask = (unsigned)e.y >> 30;
-        if (hit[f] && hit[g]) continue;
-        const int4 qt = tri[f], gt = tri[g];
-        const float4 q0 = pos[qt.x], q1 = pos[qt.y], q2 = pos[qt.z];
-        const float4 g0 = pos[gt.x], g1 = pos[gt.y], g2 = pos[gt.z];
-        bool r = false;
-        if (mask & 1) r = pair_decide_exact(g0, g1, g2, gt, q0, q1, q2, qt, eps);
-        if (!r && (mask & 2)) r = pair_decide_exact(q0, q1, q2, qt, g0, g1, g2, gt, eps);
-        if (r) {
-            hit[f] = 1;
-            hit[g] = 1;
+        const int2 p = pair_list[i];
+        if (decide_pair(p.x, p.y, tri, pos, eps, exact)) {
+            hit[p.x] = 1;
+            hit[p.y] = 1;
         }
     }
+    for (int o = 16; o > 0; o >>= 1) exact += __shfl_xor_sync(0xffffffffu, exact, o);
+    if ((threadIdx.x & 31) == 0 && exact) atomicAdd(&rc->n_exact, (unsigned long long)exact);
 }
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -458,15 +477,22 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
 }
 
 void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, const int* qscan,
-               unsigned char* hit, int2* exact_list, int exact_cap, RoundCounters* rc, int n_query_bound, float eps,
+               unsigned char* hit, int2* pair_list, int pair_cap, RoundCounters* rc, int n_query_bound, float eps,
                cudaStream_t s) {
+    (void)qlist;
     cudaMemsetAsync(&rc->pad[1], 0, sizeof(int), s);
-    const int g = grid_for(n_query_bound, kQueryThreads, 16);
-    k_query<<<g, kQueryThreads, 0, s>>>(b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], b.box_lo, b.box_hi, tri, pos,
-                                        qlist, qscan, hit, exact_list, exact_cap, rc, eps);
+    // query faces in leaf order (uses the sort's second buffers, free after the build)
+    const int gF = grid_for(n_query_bound, 256);
+    k_query_order<<<gF, 256, 0, s>>>(rc, b.vals[0], qscan, b.live_scan);
     note_launch();
-    k_query_exact<<<grid_for((long long)n_query_bound * 4, 128, 16), 128, 0, s>>>(tri, pos, exact_list, exact_cap, hit, rc,
-                                                                                  eps);
+    exclusive_scan(b.live_scan, b.live_scan, &rc->n_live, 1, &rc->pad[2], b.scan_scratch, s);
+    k_query_gather<<<gF, 256, 0, s>>>(rc, b.vals[0], b.live_scan, b.vals[1]);
+    note_launch();
+    k_traverse<<<grid_for(n_query_bound, kQueryThreads, 16), kQueryThreads, 0, s>>>(
+        b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], b.box_lo, b.box_hi, tri, pos, b.vals[1], qscan, hit, pair_list,
+        pair_cap, rc, eps);
+    note_launch();
+    k_pairs<<<grid_for((long long)pair_cap, 128, 16), 128, 0, s>>>(tri, pos, pair_list, pair_cap, hit, rc, eps);
     note_launch();
 }
 

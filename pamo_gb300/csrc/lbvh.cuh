@@ -34,11 +34,11 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
 
 // For every face in the query list that is still live: hit[f] = 1 iff some live face g != f with an
 // overlapping closed AABB makes the reference's pair test true in either order. Query faces are taken
-// from qlist[0 .. rc->n_query); qscan is the exclusive scan of the query flags (membership test). Pairs the
-// float certificates cannot decide go through exact_list (capacity exact_cap; beyond it they are decided
-// in place).
+// as the faces f with qscan[f + 1] != qscan[f] (qscan: exclusive scan of the query flags), visited in leaf
+// order. Candidate pairs go through pair_list (capacity pair_cap; beyond it they are decided in place).
+// qlist is unused (kept for callers that hold one).
 void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, const int* qscan,
-               unsigned char* hit, int2* exact_list, int exact_cap, RoundCounters* rc, int n_query_bound, float eps,
+               unsigned char* hit, int2* pair_list, int pair_cap, RoundCounters* rc, int n_query_bound, float eps,
                cudaStream_t s);
 
 }  // namespace pamo

@@ -109,6 +109,7 @@ struct pamo_ctx {
     // ---- per-vertex working buffers ----
     DevBuf<float4> pos, orig_pos, pos_in, pos_out;
     DevBuf<int> occ, valence, cursor;
+    DevBuf<int> vedges, vcursor;  // edges per lower endpoint (offsets) and fill cursors
     DevBuf<Quadric> quad;
     DevBuf<unsigned long long> vmin;
     DevBuf<int> undo_in;
@@ -117,7 +118,6 @@ struct pamo_ctx {
     DevBuf<int4> tri, orig_tri, tri_in, tri_out;
     DevBuf<int> ecount, qflag, qlist, fflags, nt, shuffle_flags;
     DevBuf<unsigned long long> fkey;
-    DevBuf<float4> flen, fnrm;  // per-face edge lengths and unit normal
     DevBuf<unsigned char> hit;
     BvhBuffers bvh;
     char* bvh_mem = nullptr;
@@ -126,7 +126,8 @@ struct pamo_ctx {
     // ---- per-edge ----
     DevBuf<int2> edges;
     DevBuf<int> win, collapsed, uflag;
-    DevBuf<int2> exact_list;  // candidate pairs left to the fp64 decision
+    DevBuf<int> eorder;  // edge ids grouped by lower endpoint
+    DevBuf<int2> exact_list;  // candidate pairs of the self-intersection check
 
     // ---- small ----
     RoundCounters* rc = nullptr;
@@ -204,7 +205,7 @@ struct pamo_ctx {
         fr(edge_cost); fr(invalid); fr(pts_map); fr(undo_list); fr(tmp_undo);
         fr(pos); fr(orig_pos); fr(pos_in); fr(pos_out); fr(occ); fr(valence); fr(cursor); fr(quad); fr(vmin); fr(undo_in);
         fr(tri); fr(orig_tri); fr(tri_in); fr(tri_out); fr(ecount); fr(qflag); fr(qlist); fr(fflags); fr(nt);
-        fr(shuffle_flags); fr(fkey); fr(flen); fr(fnrm); fr(hit); fr(edges); fr(win); fr(collapsed); fr(uflag); fr(face_mean); fr(exact_list);
+        fr(shuffle_flags); fr(fkey); fr(eorder); fr(vedges); fr(vcursor); fr(hit); fr(edges); fr(win); fr(collapsed); fr(uflag); fr(face_mean); fr(exact_list);
         if (bvh_mem) cudaFree(bvh_mem);
         bvh_mem = nullptr;
         prof.destroy();
@@ -247,7 +248,7 @@ struct pamo_ctx {
         const size_t nc = c + c / 5;
         int r;
         if ((r = grow(pos, nc)) || (r = grow(orig_pos, nc)) || (r = grow(pos_out, nc)) || (r = grow(occ, nc + 1)) ||
-            (r = grow(valence, nc + 1)) || (r = grow(cursor, nc)) || (r = grow(quad, nc)) || (r = grow(vmin, nc)) ||
+            (r = grow(valence, nc + 1)) || (r = grow(cursor, nc)) || (r = grow(vedges, nc + 1)) || (r = grow(vcursor, nc)) || (r = grow(quad, nc)) || (r = grow(vmin, nc)) ||
             (r = grow(pos_in, nc)))
             return r;
         cap_v = nc;
@@ -262,10 +263,10 @@ struct pamo_ctx {
         if ((r = grow(tri, nc)) || (r = grow(orig_tri, nc)) || (r = grow(tri_in, nc)) || (r = grow(tri_out, nc)) ||
             (r = grow(ecount, nc + 1)) || (r = grow(qflag, nc + 1)) || (r = grow(qlist, nc)) || (r = grow(fflags, nc + 1)) ||
             (r = grow(nt, 3 * nc)) || (r = grow(shuffle_flags, 2 * nc + 40)) || (r = grow(fkey, nc)) || (r = grow(hit, nc)) ||
-            (r = grow(flen, nc)) || (r = grow(fnrm, nc)) ||
+            (r = grow(eorder, 2 * nc)) ||
             (r = grow(edges, 2 * nc)) || (r = grow(win, 2 * nc + 1)) || (r = grow(collapsed, 2 * nc)) ||
             (r = grow(uflag, 2 * nc + 1)) || (r = grow(face_mean, 3 * nc)) ||
-            (r = grow(exact_list, std::max<size_t>(1 << 20, 8 * nc))))
+            (r = grow(exact_list, std::max<size_t>(1 << 20, 16 * nc))))
             return r;
         // edge costs keep their stale contents when the physical buffer grows
         if ((r = grow(edge_cost, 2 * nc + 2 * nc / 5 + 2, true, true))) return r;
@@ -349,10 +350,13 @@ struct pamo_ctx {
         prof.begin(kPhAdj, s);
         cudaMemsetAsync(valence.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(cursor.p, 0, (nP + 1) * sizeof(int), s);
-        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, s);
+        cudaMemsetAsync(vedges.p, 0, (nP + 1) * sizeof(int), s);
+        cudaMemsetAsync(vcursor.p, 0, (nP + 1) * sizeof(int), s);
+        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s);
         exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
         exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s);
-        launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, s);
+        exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
+        launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p, eorder.p, s);
         launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
         const int* nt_off = valence.p;
         const int eb = 2 * nT;
@@ -360,18 +364,17 @@ struct pamo_ctx {
 
         // cost and selection
         prof.begin(kPhQuad, s);
-        launch_face_geom(rc, nT, tri.p, pos.p, flen.p, fnrm.p, s);
-        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, pos.p, fnrm.p, quad.p, s);
+        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, pos.p, quad.p, s);
         prof.end(kPhQuad, s);
         launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
         cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
         prof.begin(kPhCost, s);
-        launch_edge_cost(rc, eb, edges.p, nt_off, nt.p, tri.p, pos.p, flen.p, fnrm.p, quad.p, invalid.p, edge_cost.p,
-                         vmin.p, d_scale, threshold, is_stuck, s);
+        launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, invalid.p, edge_cost.p, vmin.p,
+                         d_scale, threshold, is_stuck, s);
         prof.end(kPhCost, s);
         prof.begin(kPhCollapse, s);
         launch_face_keys(rc, nT, tri.p, vmin.p, fkey.p, s);
-        launch_collapse(rc, eb, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p,
+        launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p,
                         orig_pos.p, occ.p, win.p, s);
         exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s);
         launch_compact_winners(rc, eb, win.p, collapsed.p, s);

@@ -103,7 +103,7 @@ __global__ void k_shuffle_gather(Feistel fb, const int* __restrict__ scan, const
 
 // ------------------------------------------------------------------ adjacency
 __global__ void __launch_bounds__(kT) k_face_counts(const int4* __restrict__ tri, const RoundCounters* rc, int* valence,
-                                                    int* ecount) {
+                                                    int* ecount, int* vedges) {
     const int n = rc->n_tris;
     for (int f = gtid(); f < n; f += gstride()) {
         const int4 t = tri[f];
@@ -115,13 +115,18 @@ __global__ void __launch_bounds__(kT) k_face_counts(const int4* __restrict__ tri
         atomicAdd(&valence[t.y], 1);
         atomicAdd(&valence[t.z], 1);
         ecount[f] = (t.x > t.y) + (t.y > t.z) + (t.z > t.x);  // count_edge_kernel, :306-316
+        // edges per lower endpoint, for the vertex-grouped processing order
+        if (t.x > t.y) atomicAdd(&vedges[t.y], 1);
+        if (t.y > t.z) atomicAdd(&vedges[t.z], 1);
+        if (t.z > t.x) atomicAdd(&vedges[t.x], 1);
     }
     if (gtid() == 0) ecount[n] = 0;
 }
 
 __global__ void __launch_bounds__(kT) k_fill_adjacency(const int4* __restrict__ tri, const RoundCounters* rc,
                                                        const int* __restrict__ nt_off, int* cursor, int* nt,
-                                                       const int* __restrict__ edge_off, int2* edges) {
+                                                       const int* __restrict__ edge_off, int2* edges,
+                                                       const int* __restrict__ voff, int* vcursor, int* eorder) {
     const int n = rc->n_tris;
     for (int f = gtid(); f < n; f += gstride()) {
         const int4 t = tri[f];
@@ -130,9 +135,18 @@ __global__ void __launch_bounds__(kT) k_fill_adjacency(const int4* __restrict__ 
         nt[nt_off[t.y] + atomicAdd(&cursor[t.y], 1)] = f;
         nt[nt_off[t.z] + atomicAdd(&cursor[t.z], 1)] = f;
         int e = edge_off[f];  // create_edge_kernel, :318-335
-        if (t.x > t.y) edges[e++] = make_int2(t.y, t.x);
-        if (t.y > t.z) edges[e++] = make_int2(t.z, t.y);
-        if (t.z > t.x) edges[e++] = make_int2(t.x, t.z);
+        if (t.x > t.y) {
+            eorder[voff[t.y] + atomicAdd(&vcursor[t.y], 1)] = e;
+            edges[e++] = make_int2(t.y, t.x);
+        }
+        if (t.y > t.z) {
+            eorder[voff[t.z] + atomicAdd(&vcursor[t.z], 1)] = e;
+            edges[e++] = make_int2(t.z, t.y);
+        }
+        if (t.z > t.x) {
+            eorder[voff[t.x] + atomicAdd(&vcursor[t.x], 1)] = e;
+            edges[e++] = make_int2(t.x, t.z);
+        }
     }
 }
 
@@ -152,39 +166,27 @@ __global__ void __launch_bounds__(kT) k_sort_adjacency(const RoundCounters* rc, 
     }
 }
 
-// ------------------------------------------------------------------ per-face geometry
-// Values several kernels of the round need for every face, computed once with the reference's formulas
-// (so they are bit-identical to recomputing them in place): the unit normal of tri2plane / the edge-cost
-// flip test, (v1 - v0) x (v2 - v0) / |.| (cusimp_free.cu:337-346, 520-521), and the three edge lengths
-// |p_i - p_j|, |p_j - p_k|, |p_k - p_i| of the ring-length sum and the skinny term (:449-484, 368-380).
-__global__ void __launch_bounds__(kT) k_face_geom(const RoundCounters* rc, const int4* __restrict__ tri,
-                                                  const float4* __restrict__ pos, float4* flen, float4* fnrm) {
-    const int n = rc->n_tris;
-    for (int f = gtid(); f < n; f += gstride()) {
-        const int4 t = tri[f];
-        if (face_killed(t)) continue;
-        const V3 v0 = v3(pos[t.x]), v1 = v3(pos[t.y]), v2 = v3(pos[t.z]);
-        V3 nrm = vcross(vsub(v1, v0), vsub(v2, v0));
-        nrm = vdiv(nrm, vnorm(nrm));
-        fnrm[f] = make_float4(nrm.x, nrm.y, nrm.z, 0.f);
-        flen[f] = make_float4(vnorm(vsub(v0, v1)), vnorm(vsub(v1, v2)), vnorm(vsub(v2, v0)), 0.f);
-    }
+// ------------------------------------------------------------------ quadrics (compute_vert_Q_kernel, :337-366)
+__device__ __forceinline__ void face_plane(const float4* __restrict__ pos, int4 t, float p[4]) {
+    const V3 v0 = v3(pos[t.x]), v1 = v3(pos[t.y]), v2 = v3(pos[t.z]);
+    V3 n = vcross(vsub(v1, v0), vsub(v2, v0));
+    n = vdiv(n, vnorm(n));
+    p[0] = n.x;
+    p[1] = n.y;
+    p[2] = n.z;
+    p[3] = -vdot(n, v0);
 }
 
-// ------------------------------------------------------------------ quadrics (compute_vert_Q_kernel, :337-366)
 __global__ void __launch_bounds__(kT) k_quadrics(const RoundCounters* rc, const int* __restrict__ nt_off,
                                                  const int* __restrict__ nt, const int4* __restrict__ tri,
-                                                 const float4* __restrict__ pos, const float4* __restrict__ fnrm,
-                                                 Quadric* q) {
+                                                 const float4* __restrict__ pos, Quadric* q) {
     const int n = rc->n_pts;
     for (int v = gtid(); v < n; v += gstride()) {
         float m00 = 0.f, m01 = 0.f, m02 = 0.f, m03 = 0.f, m11 = 0.f, m12 = 0.f, m13 = 0.f, m22 = 0.f, m23 = 0.f, m33 = 0.f;
         const int b = nt_off[v + 1];
         for (int s = nt_off[v]; s < b; ++s) {
-            const int f = nt[s];
-            const float4 nn = fnrm[f];
-            const V3 nrm = {nn.x, nn.y, nn.z};
-            const float p[4] = {nrm.x, nrm.y, nrm.z, -vdot(nrm, v3(pos[tri[f].x]))};
+            float p[4];
+            face_plane(pos, tri[nt[s]], p);
             m00 += p[0] * p[0]; m01 += p[0] * p[1]; m02 += p[0] * p[2]; m03 += p[0] * p[3];
             m11 += p[1] * p[1]; m12 += p[1] * p[2]; m13 += p[1] * p[3];
             m22 += p[2] * p[2]; m23 += p[2] * p[3];
@@ -213,51 +215,41 @@ __device__ __forceinline__ float tri_area(V3 p0, V3 p1, V3 p2) {
 }
 
 __device__ __forceinline__ void ring_len(int w, const int* __restrict__ nt_off, const int* __restrict__ nt,
-                                         const int4* __restrict__ tri, const float4* __restrict__ flen, float& len, int& cnt) {
+                                         const int4* __restrict__ tri, const float4* __restrict__ pos, float& len, int& cnt) {
     const int b = nt_off[w + 1];
     for (int s = nt_off[w]; s < b; ++s) {
-        const int f = nt[s];
-        const int4 t = tri[f];
-        const float4 L = flen[f];
-        if (t.x > t.y) { len += L.x; cnt++; }
-        if (t.y > t.z) { len += L.y; cnt++; }
-        if (t.z > t.x) { len += L.z; cnt++; }
+        const int4 t = tri[nt[s]];
+        if (t.x > t.y) { len += vnorm(vsub(v3(pos[t.x]), v3(pos[t.y]))); cnt++; }
+        if (t.y > t.z) { len += vnorm(vsub(v3(pos[t.y]), v3(pos[t.z]))); cnt++; }
+        if (t.z > t.x) { len += vnorm(vsub(v3(pos[t.z]), v3(pos[t.x]))); cnt++; }
     }
 }
 
 // normal-flip test and skinny term over the ring of w with w moved to vm (faces holding `other` skipped).
-// The flip sign dot(n_old, n_new / |n_new|) < 0 is taken from the unnormalised n_new when a float bound
-// proves it (|dot| > 1e-5 |n_old|_1 |n_new|_1, far above the ~1e-6 relative rounding of the normalised
-// form); otherwise the normalised form is evaluated exactly as the reference does.
+// The flip test dot(n_old/|n_old|, n_new/|n_new|) < 0 takes its sign from the unnormalised normals when a
+// float bound proves it (|dot| > 1e-5 |n_old|_1 |n_new|_1, far above the ~1e-6 relative rounding of the
+// normalised form); otherwise the normalised form is evaluated exactly as the reference does.
 __device__ __forceinline__ bool ring_skinny(int w, int other, V3 vm, const int* __restrict__ nt_off,
                                             const int* __restrict__ nt, const int4* __restrict__ tri,
-                                            const float4* __restrict__ pos, const float4* __restrict__ flen,
-                                            const float4* __restrict__ fnrm, float& qa, int& ntri) {
+                                            const float4* __restrict__ pos, float& qa, int& ntri) {
     const float k4s3 = 4.0f * sqrtf(3.0f);
     const int b = nt_off[w + 1];
     for (int s = nt_off[w]; s < b; ++s) {
-        const int f = nt[s];
-        const int4 t = tri[f];
+        const int4 t = tri[nt[s]];
         if (t.x == other || t.y == other || t.z == other) continue;
-        const float4 on4 = fnrm[f];
-        const V3 on = {on4.x, on4.y, on4.z};
-        const V3 n0 = (t.x == w) ? vm : v3(pos[t.x]);
-        const V3 n1 = (t.y == w) ? vm : v3(pos[t.y]);
-        const V3 n2 = (t.z == w) ? vm : v3(pos[t.z]);
+        const V3 o0 = v3(pos[t.x]), o1 = v3(pos[t.y]), o2 = v3(pos[t.z]);
+        const V3 n0 = (t.x == w) ? vm : o0, n1 = (t.y == w) ? vm : o1, n2 = (t.z == w) ? vm : o2;
+        const V3 ou = vcross(vsub(o1, o0), vsub(o2, o0));
         const V3 nu = vcross(vsub(n1, n0), vsub(n2, n0));
-        const float du = vdot(on, nu);
-        const float bound = 1e-5f * (fabsf(on.x) + fabsf(on.y) + fabsf(on.z)) * (fabsf(nu.x) + fabsf(nu.y) + fabsf(nu.z));
+        const float du = vdot(ou, nu);
+        const float bound = 1e-5f * (fabsf(ou.x) + fabsf(ou.y) + fabsf(ou.z)) * (fabsf(nu.x) + fabsf(nu.y) + fabsf(nu.z));
         if (du < -bound) return false;
         if (!(du > bound)) {
+            const V3 on = vdiv(ou, vnorm(ou));
             const V3 nn = vdiv(nu, vnorm(nu));
             if (vdot(on, nn) < 0) return false;
         }
-        const float4 L = flen[f];
-        // lengths |n0 - n1|, |n1 - n2|, |n2 - n0|: an edge without w keeps the face's own edge length
-        const bool wx = t.x == w, wy = t.y == w, wz = t.z == w;
-        const float l01 = (!wx && !wy) ? L.x : vnorm(vsub(n0, n1));
-        const float l12 = (!wy && !wz) ? L.y : vnorm(vsub(n1, n2));
-        const float l20 = (!wz && !wx) ? L.z : vnorm(vsub(n2, n0));
+        const float l01 = vnorm(vsub(n0, n1)), l12 = vnorm(vsub(n1, n2)), l20 = vnorm(vsub(n2, n0));
         const float sh = (l01 + l12 + l20) / 2;  // triangle_area (Heron), :368-375
         const float area = sqrtf(sh * (sh - l01) * (sh - l12) * (sh - l20));
         // the reference's operator precedence: only the first squared length divides (pow(x, 2) == x * x)
@@ -275,7 +267,6 @@ __device__ __forceinline__ uint32_t f2u_sat(float f) {
 // returns false when the reference leaves the stale cost in place
 __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restrict__ nt_off, const int* __restrict__ nt,
                                                 const int4* __restrict__ tri, const float4* __restrict__ pos,
-                                                const float4* __restrict__ flen, const float4* __restrict__ fnrm,
                                                 const Quadric* __restrict__ q, float scale, float tres, uint32_t& out) {
     // link condition
     int dup = 0;
@@ -294,16 +285,15 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
     if (dup != 2) return false;
     float len = 0.0f;
     int cnt = 0;
-    ring_len(u, nt_off, nt, tri, flen, len, cnt);
-    ring_len(v, nt_off, nt, tri, flen, len, cnt);
+    ring_len(u, nt_off, nt, tri, pos, len, cnt);
+    ring_len(v, nt_off, nt, tri, pos, len, cnt);
     const V3 v0 = v3(pos[u]), v1 = v3(pos[v]);
     len = len / (float)cnt / scale * tres;
     len = len + vnorm(vsub(v0, v1)) / scale * tres;
     const V3 vm = vdiv(vadd(v0, v1), 2.0f);
     float qa = 0.0f;
     int ntri = 0;
-    if (!ring_skinny(u, v, vm, nt_off, nt, tri, pos, flen, fnrm, qa, ntri) ||
-        !ring_skinny(v, u, vm, nt_off, nt, tri, pos, flen, fnrm, qa, ntri)) {
+    if (!ring_skinny(u, v, vm, nt_off, nt, tri, pos, qa, ntri) || !ring_skinny(v, u, vm, nt_off, nt, tri, pos, qa, ntri)) {
         out = 0xFFFFFFFFu;
         return true;
     }
@@ -325,16 +315,17 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
     return true;
 }
 
-__global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const int2* __restrict__ edges,
+__global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const int* __restrict__ eorder,
+                                                  const int2* __restrict__ edges,
                                                   const int* __restrict__ nt_off, const int* __restrict__ nt,
                                                   const int4* __restrict__ tri, const float4* __restrict__ pos,
-                                                  const float4* __restrict__ flen, const float4* __restrict__ fnrm,
                                                   const Quadric* __restrict__ q, const unsigned char* __restrict__ invalid,
                                                   uint32_t* cost, unsigned long long* vmin, const float* d_scale,
                                                   float tres, int is_stuck) {
     const int n = rc->n_edges;
     const float scale = *d_scale;
-    for (int e = gtid(); e < n; e += gstride()) {
+    for (int i = gtid(); i < n; i += gstride()) {
+        const int e = eorder[i];  // edges grouped by their lower vertex: neighbouring threads share rings
         const int2 ed = edges[e];
         const int u = ed.x, v = ed.y;
         uint32_t c = 0;
@@ -345,7 +336,7 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
         } else if (is_stuck) {
             write = false;
         } else {
-            write = edge_cost_value(u, v, nt_off, nt, tri, pos, flen, fnrm, q, scale, tres, c);
+            write = edge_cost_value(u, v, nt_off, nt, tri, pos, q, scale, tres, c);
         }
         if (write) cost[e] = c;
         else c = cost[e];  // stale value of an earlier round
@@ -429,14 +420,16 @@ __device__ __forceinline__ void restore_ring(int w, const int* __restrict__ nt_o
     }
 }
 
-__global__ void __launch_bounds__(kT) k_collapse(RoundCounters* rc, const int2* __restrict__ edges,
+__global__ void __launch_bounds__(kT) k_collapse(RoundCounters* rc, const int* __restrict__ eorder,
+                                                 const int2* __restrict__ edges,
                                                  const uint32_t* __restrict__ cost, uint32_t collapse_t,
                                                  const unsigned long long* __restrict__ fkey, const int* __restrict__ nt_off,
                                                  const int* __restrict__ nt, int4* tri, const int4* __restrict__ orig_tri,
                                                  float4* pos, const float4* __restrict__ orig_pos, int* occ, int* win) {
     const int n = rc->n_edges;
     if (gtid() == 0) win[n] = 0;
-    for (int e = gtid(); e < n; e += gstride()) {
+    for (int i = gtid(); i < n; i += gstride()) {
+        const int e = eorder[i];
         int w = 0;
         const uint32_t c = cost[e];
         if (c <= collapse_t) {
@@ -692,13 +685,23 @@ __global__ void __launch_bounds__(1024) k_sequential_sum(const float* __restrict
         } else if (lane < 3) {
             const int len = min(kSumTile, nf - t * kSumTile);
             const float* x = buf[cur][lane];
+            // the adds form one dependent chain; the shared-memory loads of the next 16 values are issued
+            // before the current 16 are added, so the chain runs at the add latency
             int k = 0;
-            for (; k + 8 <= len; k += 8) {
-                float v[8];
+            if (len >= 16) {
+                float v[16], w[16];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) v[j] = x[k + j];
+                for (int j = 0; j < 16; ++j) v[j] = x[j];
+                for (k = 16; k + 16 <= len; k += 16) {
 #pragma unroll
-                for (int j = 0; j < 8; ++j) s += v[j];
+                    for (int j = 0; j < 16; ++j) w[j] = x[k + j];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) s += v[j];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) v[j] = w[j];
+                }
+#pragma unroll
+                for (int j = 0; j < 16; ++j) s += v[j];
             }
             for (; k < len; ++k) s += x[k];
         }
@@ -814,33 +817,32 @@ void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4*
 }
 
 void launch_face_counts(const int4* tri, const RoundCounters* rc, int n_tris_bound, int* valence, int* ecount,
-                        cudaStream_t s) {
-    k_face_counts<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, valence, ecount); note_launch();
+                        int* vedges, cudaStream_t s) {
+    k_face_counts<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, valence, ecount, vedges); note_launch();
 }
 void launch_fill_adjacency(const int4* tri, const RoundCounters* rc, int n_tris_bound, const int* nt_off, int* cursor,
-                           int* nt, const int* edge_off, int2* edges, cudaStream_t s) {
-    k_fill_adjacency<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, nt_off, cursor, nt, edge_off, edges); note_launch();
+                           int* nt, const int* edge_off, int2* edges, const int* voff, int* vcursor, int* eorder,
+                           cudaStream_t s) {
+    k_fill_adjacency<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, nt_off, cursor, nt, edge_off, edges, voff, vcursor,
+                                                               eorder);
+    note_launch();
 }
 void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* nt_off, int* nt, cudaStream_t s) {
     k_sort_adjacency<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt); note_launch();
 }
-void launch_face_geom(const RoundCounters* rc, int n_tris_bound, const int4* tri, const float4* pos, float4* flen,
-                      float4* fnrm, cudaStream_t s) {
-    k_face_geom<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(rc, tri, pos, flen, fnrm); note_launch();
-}
 void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
-                     const float4* pos, const float4* fnrm, Quadric* q, cudaStream_t s) {
-    k_quadrics<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, pos, fnrm, q); note_launch();
+                     const float4* pos, Quadric* q, cudaStream_t s) {
+    k_quadrics<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, pos, q); note_launch();
 }
 void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s) {
     k_edge_cost_capacity<<<1, 1, 0, s>>>(rc, d_cap); note_launch();
     k_edge_cost_zero<<<grid_for(phys_len, kT), kT, 0, s>>>(rc, edge_cost, phys_len); note_launch();
 }
-void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int2* edges, const int* nt_off, const int* nt,
-                      const int4* tri, const float4* pos, const float4* flen, const float4* fnrm, const Quadric* q,
-                      const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin, const float* d_scale,
-                      float tres, int is_stuck, cudaStream_t s) {
-    k_edge_cost<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, edges, nt_off, nt, tri, pos, flen, fnrm, q, invalid, cost,
+void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
+                      const int* nt, const int4* tri, const float4* pos, const Quadric* q, const unsigned char* invalid,
+                      uint32_t* cost, unsigned long long* vmin, const float* d_scale, float tres, int is_stuck,
+                      cudaStream_t s) {
+    k_edge_cost<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, invalid, cost,
                                                            vmin, d_scale,
                                                            tres, is_stuck); note_launch();
 }
@@ -848,10 +850,10 @@ void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri
                       unsigned long long* fkey, cudaStream_t s) {
     k_face_keys<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(rc, tri, vmin, fkey); note_launch();
 }
-void launch_collapse(RoundCounters* rc, int n_edges_bound, const int2* edges, const uint32_t* cost, uint32_t collapse_t,
-                     const unsigned long long* fkey, const int* nt_off, const int* nt, int4* tri, const int4* orig_tri,
-                     float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s) {
-    k_collapse<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, edges, cost, collapse_t, fkey, nt_off, nt, tri, orig_tri,
+void launch_collapse(RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const uint32_t* cost,
+                     uint32_t collapse_t, const unsigned long long* fkey, const int* nt_off, const int* nt, int4* tri,
+                     const int4* orig_tri, float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s) {
+    k_collapse<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, cost, collapse_t, fkey, nt_off, nt, tri, orig_tri,
                                                           pos, orig_pos, occ, win); note_launch();
 }
 void launch_compact_winners(const RoundCounters* rc, int n_edges_bound, const int* win_scan, int* collapsed,

@@ -27,26 +27,25 @@ void launch_copy_tris(const int4* src, int4* dst, int n, cudaStream_t s);
 
 // ---- adjacency ----
 void launch_face_counts(const int4* tri, const RoundCounters* rc, int n_tris_bound, int* valence, int* ecount,
-                        cudaStream_t s);
+                        int* vedges, cudaStream_t s);
 void launch_fill_adjacency(const int4* tri, const RoundCounters* rc, int n_tris_bound, const int* nt_off, int* cursor,
-                           int* nt, const int* edge_off, int2* edges, cudaStream_t s);
+                           int* nt, const int* edge_off, int2* edges, const int* voff, int* vcursor, int* eorder,
+                           cudaStream_t s);
 void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* nt_off, int* nt, cudaStream_t s);
 
 // ---- cost, selection, collapse ----
-void launch_face_geom(const RoundCounters* rc, int n_tris_bound, const int4* tri, const float4* pos, float4* flen,
-                      float4* fnrm, cudaStream_t s);
 void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
-                     const float4* pos, const float4* fnrm, Quadric* q, cudaStream_t s);
+                     const float4* pos, Quadric* q, cudaStream_t s);
 void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s);
-void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int2* edges, const int* nt_off, const int* nt,
-                      const int4* tri, const float4* pos, const float4* flen, const float4* fnrm, const Quadric* q,
-                      const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin, const float* d_scale,
-                      float tres, int is_stuck, cudaStream_t s);
+void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
+                      const int* nt, const int4* tri, const float4* pos, const Quadric* q, const unsigned char* invalid,
+                      uint32_t* cost, unsigned long long* vmin, const float* d_scale, float tres, int is_stuck,
+                      cudaStream_t s);
 void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
                       unsigned long long* fkey, cudaStream_t s);
-void launch_collapse(RoundCounters* rc, int n_edges_bound, const int2* edges, const uint32_t* cost, uint32_t collapse_t,
-                     const unsigned long long* fkey, const int* nt_off, const int* nt, int4* tri, const int4* orig_tri,
-                     float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s);
+void launch_collapse(RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const uint32_t* cost,
+                     uint32_t collapse_t, const unsigned long long* fkey, const int* nt_off, const int* nt, int4* tri,
+                     const int4* orig_tri, float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s);
 void launch_compact_winners(const RoundCounters* rc, int n_edges_bound, const int* win_scan, int* collapsed,
                             cudaStream_t s);
 void launch_remove_invalid(const RoundCounters* rc, int n_tris_bound, int4* tri, cudaStream_t s);
