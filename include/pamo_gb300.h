@@ -123,6 +123,45 @@ int pamo_profile_enable(pamo_ctx* ctx, int32_t enable);
 /* Accumulated milliseconds and launch counts per phase; returns the number of phases. */
 int pamo_profile_read(const pamo_ctx* ctx, double* ms, int64_t* counts, int32_t n);
 
+/* ------------------------------------------------------------------------------------------------------
+ * Stage 3: safe projection of the simplified mesh onto the input ("GT") mesh.
+ * A pamo_stage3 handle replaces the reference's Stage3System (simp_cuda/safe_project/src/pamo_safe_project/
+ * system.py:28-110), which PaMO builds once and reuses across run() calls (simp_cuda/pamo/__init__.py:34-36).
+ * ------------------------------------------------------------------------------------------------------ */
+typedef struct pamo_stage3 pamo_stage3;
+
+/* Stage3System(Stage3Config(), device) with the default configuration (config.py:6-73). */
+int pamo_stage3_create(pamo_stage3** out, int device);
+
+/* Release the handle and its device buffers. */
+int pamo_stage3_destroy(pamo_stage3* s);
+
+/* Message of the last failed stage-3 call ("" when none). */
+const char* pamo_stage3_last_error(const pamo_stage3* s);
+
+/* Set one Stage3Config field by its reference name (config.py:6-73): n_newton_iters, n_cg_iters,
+ * n_line_search_iters, d_hat, coll_stiffness, contact_detection_radius, ee_classify_thres, ccd_slackness,
+ * ccd_thickness, ccd_max_iters, spd_max_iters, elas_young_modulus, elas_poisson_ratio, hinge_stiffness,
+ * mesh2gt_dist_stiffness, min_angle_thres (degrees), max_blocks. Unknown names: PAMO_ERR_INVALID_ARG. */
+int pamo_stage3_set_param(pamo_stage3* s, const char* name, double value);
+
+/*
+ * pamo_safe_project.process(gt_V, gt_F, stage2_V, stage2_F, n_iters) (processing.py:23-106): normalise by
+ * the GT mesh's mean and largest extent, register the mesh (Voronoi weights, StVK rest shapes, hinges),
+ * then n_iters steps of closest-point targets + n_newton_iters Newton iterations (contact detection,
+ * Jacobi PCG, step clamp, additive CCD, backtracking line search) (system.py:411-470). gt_points and
+ * points are float64 rows of 3 (device), triangles int32 rows of 3 (device); out_points receives the
+ * n_points x 3 float64 result in the input frame (device). The faces are unchanged. Synchronises `stream`.
+ */
+int pamo_safe_project(pamo_stage3* s, const double* gt_points, const int32_t* gt_triangles, int32_t n_gt_points,
+                      int32_t n_gt_triangles, const double* points, const int32_t* triangles, int32_t n_points,
+                      int32_t n_triangles, int32_t n_iters, double* out_points, pamo_stream stream);
+
+/* Diagnostics of the last pamo_safe_project call, out[0..n): particles, triangles, edges, hinges, steps,
+ * Newton iterations, most contacts in one detection, detection-radius halvings, do-nothing flag, final
+ * energy, contacts summed over detections. Returns 11. No reference counterpart (the reference logs these). */
+int pamo_stage3_stats(const pamo_stage3* s, double* out, int32_t n);
+
 #ifdef __cplusplus
 }
 #endif

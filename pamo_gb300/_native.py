@@ -51,7 +51,16 @@ SIGNATURES = {
     "pamo_launch_count": (ctypes.c_int64, []),
     "pamo_profile_enable": (ctypes.c_int, [_P, _I32]),
     "pamo_profile_read": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _PI64, _I32]),
+    "pamo_stage3_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int]),
+    "pamo_stage3_destroy": (ctypes.c_int, [_P]),
+    "pamo_stage3_last_error": (ctypes.c_char_p, [_P]),
+    "pamo_stage3_set_param": (ctypes.c_int, [_P, ctypes.c_char_p, _F64]),
+    "pamo_safe_project": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _P, _P, _I32, _I32, _I32, _P, _P]),
+    "pamo_stage3_stats": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _I32]),
 }
+
+STAGE3_STATS = ["particles", "triangles", "edges", "hinges", "steps", "newton_iters", "max_contacts",
+                "radius_halvings", "do_nothing", "energy", "total_contacts"]
 
 RUN_TOTALS = ["vertices", "faces", "edges", "winners", "query_tests", "pairs", "exact_pairs", "checks", "live_indexed",
               "collapsed"]

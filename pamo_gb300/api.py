@@ -224,8 +224,11 @@ class PaMO(torch.nn.Module):
         self.target_faces = None
         self._ctx: Context | None = None
         self.last_rounds = 0
+        self.system = None  # the reference builds its Stage3System here; it is made on the first run's device
         if use_stage3:
-            from . import safe_project  # noqa: F401  (raises if stage 3 is unavailable)
+            from . import safe_project
+
+            self.config = safe_project.Stage3Config()
 
     def run(self, points, triangles, ratio, tolerance=4, threshold=1e-3, iter=1000000, min_verts=10000000000):
         self.target_faces = max(int(ratio * len(triangles)), min_verts)
@@ -236,7 +239,12 @@ class PaMO(torch.nn.Module):
         verts_np = verts.cpu().numpy()
         faces_np = faces.cpu().numpy()
         if self.use_stage3:
+            # stage 3 (simp_cuda/pamo/__init__.py:165-176): the stage-2 mesh goes through trimesh's default
+            # processing, then 5 steps of safe projection with the system kept across calls
             from . import safe_project
 
-            verts_np, faces_np = safe_project.process(self.gt_mesh[0], self.gt_mesh[1], verts_np, faces_np, 5)
+            if self.system is None or self.system.device != points.device:
+                self.system = safe_project.Stage3System(self.config, points.device)
+            V2, F2 = safe_project.mesh_process(verts_np, faces_np)
+            verts_np, faces_np = safe_project.process(self.gt_mesh[0], self.gt_mesh[1], V2, F2, 5, system=self.system)
         return verts_np, faces_np

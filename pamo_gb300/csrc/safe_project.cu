@@ -1,0 +1,1791 @@
+// Stage 3 (safe projection) on GB300: kernels and the Newton driver.
+//
+// Reference: simp_cuda/safe_project/src/pamo_safe_project/ — processing.py:23-106 (normalisation, step
+// loop), system.py:167-272 (register_mesh), :411-470 (step), cg_solver.py:96-158 (Jacobi PCG),
+// energy.py:195-211 (distance to GT), :346-468 (StVK), :590-706 (hinge), :887-948 (contacts, barrier, CCD),
+// kernels/*.py (per-element formulas). The reference runs on a forked Warp that is not available, so the
+// formulas below follow the reference's kernels; where the reference calls a fork-only routine
+// (wp.spd_project_blocks) or Warp internals (BVH queries, mesh_query_point_no_sign) this file uses its own
+// implementation of the same mathematical operation (stated at each place).
+//
+// All simulation arrays are float32 as in the reference. Energies and the CG dot products are reduced in a
+// fixed order with compensated (two-sum) float accumulation, so the solve is deterministic apart from the
+// float atomics of the gradient, Hessian-diagonal and Hessian-vector scatters (same as the reference).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "../../include/pamo_gb300.h"
+#include "safe_project.cuh"
+#include "scan.cuh"
+
+namespace pamo {
+
+namespace {
+
+constexpr int kT = 256;
+constexpr int kRedBlocks = 256;
+constexpr int kQT = 128;
+constexpr int kStack = 64;
+
+// ------------------------------------------------------------------ float3 helpers (Warp vec3 semantics)
+struct F3 {
+    float x, y, z;
+};
+__device__ __forceinline__ F3 f3(float4 a) { return {a.x, a.y, a.z}; }
+__device__ __forceinline__ float4 f4(F3 a) { return make_float4(a.x, a.y, a.z, 0.f); }
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ F3 operator-(F3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ F3 operator*(float s, F3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ F3 operator*(F3 a, float s) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ F3 operator/(F3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ F3 cross(F3 a, F3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+__device__ __forceinline__ float length_sq(F3 a) { return dot(a, a); }
+__device__ __forceinline__ float length(F3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ F3 normalize(F3 a) {  // Warp: zero vector when the length is 0
+    const float l = length(a);
+    return l > 0.f ? a / l : F3{0.f, 0.f, 0.f};
+}
+__device__ __forceinline__ F3 fmin3(F3 a, F3 b) { return {fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)}; }
+__device__ __forceinline__ F3 fmax3(F3 a, F3 b) { return {fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)}; }
+__device__ __forceinline__ void atomic_add3(float4* a, int i, F3 v) {
+    atomicAdd(&a[i].x, v.x);
+    atomicAdd(&a[i].y, v.y);
+    atomicAdd(&a[i].z, v.z);
+}
+// Warp's step(x): 1 when x < 0, else 0
+__device__ __forceinline__ float wstep(float x) { return x < 0.f ? 1.f : 0.f; }
+
+// ------------------------------------------------------------------ distances (distance_kernels.py:8-30)
+__device__ __forceinline__ float pt_distance(F3 x0, F3 x1, F3 x2, F3 x3) {
+    return fabsf(dot(x0 - x1, normalize(cross(x2 - x1, x3 - x1))));
+}
+__device__ __forceinline__ float ee_distance(F3 x0, F3 x1, F3 x2, F3 x3) {
+    return fabsf(dot(x0 - x2, normalize(cross(x1 - x0, x3 - x2))));
+}
+__device__ __forceinline__ float pe_distance(F3 x0, F3 x1, F3 x2) { return length(cross(x1 - x0, x2 - x0)) / length(x1 - x2); }
+__device__ __forceinline__ float pp_distance(F3 x0, F3 x1) { return length(x1 - x0); }
+
+enum PT { PT_PT = 0, PT_PP01 = 1, PT_PP02 = 2, PT_PE012 = 3, PT_PP03 = 4, PT_PE031 = 5, PT_PE023 = 6 };
+enum EE { EE_PP02 = 0, EE_PP03 = 1, EE_PP12 = 2, EE_PP13 = 3, EE_PE023 = 4, EE_PE123 = 5, EE_PE201 = 6, EE_PE301 = 7,
+          EE_EE = 8 };
+enum Block { BLOCK_PT = 3, BLOCK_EE = 4 };
+
+// pt_pair_classify (distance_kernels.py:72-225)
+__device__ int pt_classify(F3 x0, F3 x1, F3 x2, F3 x3) {
+    F3 x10 = x0 - x1;
+    const F3 x12 = x2 - x1, x13 = x3 - x1;
+    const float area_sq = length_sq(cross(x12, x13));
+    if (area_sq <= 1e-6f * (length_sq(x12) * length_sq(x13)) || area_sq <= 1e-16f) {
+        const float d1 = length(x10), d2 = length(x0 - x2), d3 = length(x0 - x3);
+        if (d1 < d2) return d1 < d3 ? PT_PP01 : PT_PP03;
+        return d2 < d3 ? PT_PP02 : PT_PP03;
+    }
+    const F3 n = normalize(cross(x12, x13));
+    const F3 xp = x0 - dot(n, x10) * n;
+    x10 = xp - x1;
+    const F3 x20 = xp - x2, x30 = xp - x3;
+    const float a00 = dot(x12, x12), a01 = dot(x12, x13), a11 = dot(x13, x13);
+    const float b0 = dot(x10, x12), b1 = dot(x10, x13);
+    const float det = a00 * a11 - a01 * a01;
+    const float beta = b0 * a11 - b1 * a01;
+    const float gamma = a00 * b1 - b0 * a01;
+    const float alpha = det - beta - gamma;
+    const float nneg = wstep(alpha) + wstep(beta) + wstep(gamma);
+    if (nneg == 0.f) return PT_PT;
+    if (nneg == 1.f) {
+        if (alpha < 0.f) {
+            const F3 x23 = x3 - x2, x20b = x0 - x2;
+            const float dr = dot(x23, x20b);
+            if (dr < 0.f) return PT_PP02;
+            if (dr > dot(x23, x23)) return PT_PP03;
+            return PT_PE023;
+        } else if (beta < 0.f) {
+            const F3 x31 = x1 - x3, x30b = x0 - x3;
+            const float dr = dot(x31, x30b);
+            if (dr < 0.f) return PT_PP03;
+            if (dr > dot(x31, x31)) return PT_PP01;
+            return PT_PE031;
+        } else if (gamma < 0.f) {
+            const float dr = dot(x12, x10);
+            if (dr < 0.f) return PT_PP01;
+            if (dr > dot(x12, x12)) return PT_PP02;
+            return PT_PE012;
+        }
+        return -1;
+    }
+    if (alpha >= 0.f) {
+        const float d12 = dot(x12, x10), d13 = dot(x13, x10);
+        if (d12 > 0.f && d13 <= 0.f) return dot(x12, x20) > 0.f ? PT_PP02 : PT_PE012;
+        if (d13 > 0.f && d12 <= 0.f) return dot(x13, x30) > 0.f ? PT_PP03 : PT_PE031;
+        return PT_PP01;
+    } else if (beta >= 0.f) {
+        const F3 x23 = x3 - x2, x21 = x1 - x2;
+        const float d23 = dot(x23, x20), d21 = dot(x21, x20);
+        if (d23 > 0.f && d21 <= 0.f) return dot(x23, x30) > 0.f ? PT_PP03 : PT_PE023;
+        if (d21 > 0.f && d23 <= 0.f) return dot(x21, x10) > 0.f ? PT_PP01 : PT_PE012;
+        return PT_PP02;
+    }
+    const F3 x31 = x1 - x3, x32 = x2 - x3;
+    const float d31 = dot(x31, x30), d32 = dot(x32, x30);
+    if (d31 > 0.f && d32 <= 0.f) return dot(x31, x10) > 0.f ? PT_PP01 : PT_PE031;
+    if (d32 > 0.f && d31 <= 0.f) return dot(x32, x20) > 0.f ? PT_PP02 : PT_PE023;
+    return PT_PP03;
+}
+
+__device__ float pt_pair_distance(F3 x0, F3 x1, F3 x2, F3 x3, int t) {
+    switch (t) {
+        case PT_PT: return pt_distance(x0, x1, x2, x3);
+        case PT_PP01: return pp_distance(x0, x1);
+        case PT_PP02: return pp_distance(x0, x2);
+        case PT_PE012: return pe_distance(x0, x1, x2);
+        case PT_PP03: return pp_distance(x0, x3);
+        case PT_PE031: return pe_distance(x0, x3, x1);
+        case PT_PE023: return pe_distance(x0, x2, x3);
+    }
+    return 1e9f;
+}
+
+// ee_pair_classify (distance_kernels.py:300-418)
+__device__ int ee_classify(F3 x0, F3 x1, F3 x2, F3 x3, float sin_thres) {
+    const F3 e0 = x0 - x1, e1 = x2 - x3;
+    const float e0_sq = dot(e0, e0), e1_sq = dot(e1, e1);
+    const float a00 = e0_sq, a01 = -dot(e0, e1), a10 = dot(e0, e1), a11 = -e1_sq;
+    const float b0 = dot(x3 - x1, e0), b1 = dot(x3 - x1, e1);
+    const float mu0 = -(b0 * a11 - b1 * a01);
+    const float mu1 = -(a00 * b1 - a10 * b0);
+    const float detA = -(a00 * a11 - a01 * a10);
+    const float l0_sq = length_sq(e0), l1_sq = length_sq(e1);
+    const float edge_sin = length(cross(normalize(e0), normalize(e1)));
+    if (mu0 >= 0.f && mu0 <= detA && mu1 >= 0.f && mu1 <= detA && edge_sin >= sin_thres && l0_sq > 1e-15f && l1_sq > 1e-15f)
+        return EE_EE;
+    float best = 1e9f;
+    int type = -1;
+    auto consider = [&](float d, int t) {
+        if (d < best) {
+            best = d;
+            type = t;
+        }
+    };
+    const float t0 = dot(x0 - x3, e1);
+    if (t0 >= e1_sq) consider(pp_distance(x0, x2), EE_PP02);
+    else if (t0 <= 0.f) consider(pp_distance(x0, x3), EE_PP03);
+    else consider(pe_distance(x0, x2, x3), EE_PE023);
+    const float t1 = dot(x1 - x3, e1);
+    if (t1 >= e1_sq) consider(pp_distance(x1, x2), EE_PP12);
+    else if (t1 <= 0.f) consider(pp_distance(x1, x3), EE_PP13);
+    else consider(pe_distance(x1, x2, x3), EE_PE123);
+    const float t2 = dot(x2 - x1, e0);
+    if (t2 >= e0_sq) consider(pp_distance(x2, x0), EE_PP02);
+    else if (t2 <= 0.f) consider(pp_distance(x2, x1), EE_PP12);
+    else consider(pe_distance(x2, x0, x1), EE_PE201);
+    const float t3 = dot(x3 - x1, e0);
+    if (t3 >= e0_sq) consider(pp_distance(x3, x0), EE_PP03);
+    else if (t3 <= 0.f) consider(pp_distance(x3, x1), EE_PP13);
+    else consider(pe_distance(x3, x0, x1), EE_PE301);
+    return type;
+}
+
+__device__ float ee_pair_distance(F3 x0, F3 x1, F3 x2, F3 x3, int t) {
+    switch (t) {
+        case EE_PP02: return pp_distance(x0, x2);
+        case EE_PP03: return pp_distance(x0, x3);
+        case EE_PP12: return pp_distance(x1, x2);
+        case EE_PP13: return pp_distance(x1, x3);
+        case EE_PE023: return pe_distance(x0, x2, x3);
+        case EE_PE123: return pe_distance(x1, x2, x3);
+        case EE_PE201: return pe_distance(x2, x0, x1);
+        case EE_PE301: return pe_distance(x3, x0, x1);
+        case EE_EE: return ee_distance(x0, x1, x2, x3);
+    }
+    return 1e9f;
+}
+
+// ------------------------------------------------------------------ distance gradients (own derivation)
+// pp: d = |xa - xb|
+__device__ __forceinline__ void pp_grad(F3 xa, F3 xb, int a, int b, F3* g) {
+    const F3 u = normalize(xa - xb);
+    g[a] = u;
+    g[b] = -u;
+}
+// pe: distance from xa to the line (xb, xc); c = xb + t (xc - xb) the foot point, n = (xa - c)/|xa - c|
+__device__ __forceinline__ void pe_grad(F3 xa, F3 xb, F3 xc, int a, int b, int c, F3* g) {
+    const F3 e = xc - xb;
+    const float ee = dot(e, e);
+    const float t = ee > 0.f ? dot(xa - xb, e) / ee : 0.f;
+    const F3 n = normalize(xa - (xb + t * e));
+    g[a] = n;
+    g[b] = -(1.0f - t) * n;
+    g[c] = -t * n;
+}
+// pt: d = |n.(x0 - x1)|; the projection has barycentric weights (l1, l2, l3): dd/dx0 = s n, dd/dxi = -li s n
+__device__ __forceinline__ void pt_grad(F3 x0, F3 x1, F3 x2, F3 x3, F3* g) {
+    const F3 e1 = x2 - x1, e2 = x3 - x1;
+    const F3 n = normalize(cross(e1, e2));
+    const float sd = dot(n, x0 - x1);
+    const F3 sn = (sd < 0.f ? -1.f : 1.f) * n;
+    const F3 pr = x0 - sd * n - x1;
+    const float a00 = dot(e1, e1), a01 = dot(e1, e2), a11 = dot(e2, e2);
+    const float b0 = dot(pr, e1), b1 = dot(pr, e2);
+    const float det = a00 * a11 - a01 * a01;
+    const float l2 = det != 0.f ? (b0 * a11 - b1 * a01) / det : 0.f;
+    const float l3 = det != 0.f ? (a00 * b1 - b0 * a01) / det : 0.f;
+    const float l1 = 1.f - l2 - l3;
+    g[0] = sn;
+    g[1] = -l1 * sn;
+    g[2] = -l2 * sn;
+    g[3] = -l3 * sn;
+}
+// ee: d = |n.(c0 - c1)| with c0 = x0 + a (x1 - x0), c1 = x2 + b (x3 - x2) the closest points of the lines
+__device__ __forceinline__ void ee_grad(F3 x0, F3 x1, F3 x2, F3 x3, F3* g) {
+    const F3 d1 = x1 - x0, d2 = x3 - x2, r0 = x0 - x2;
+    const F3 n = normalize(cross(d1, d2));
+    const float sd = dot(n, r0);
+    const F3 sn = (sd < 0.f ? -1.f : 1.f) * n;
+    const float A = dot(d1, d1), B = dot(d1, d2), C = dot(d2, d2), D = dot(d1, r0), E = dot(d2, r0);
+    const float den = A * C - B * B;
+    const float a = den != 0.f ? (B * E - C * D) / den : 0.f;
+    const float b = den != 0.f ? (A * E - B * D) / den : 0.f;
+    g[0] = (1.f - a) * sn;
+    g[1] = a * sn;
+    g[2] = -(1.f - b) * sn;
+    g[3] = -b * sn;
+}
+
+__device__ void pt_pair_grad(F3 x0, F3 x1, F3 x2, F3 x3, int t, F3* g) {
+    g[0] = g[1] = g[2] = g[3] = F3{0.f, 0.f, 0.f};
+    switch (t) {
+        case PT_PT: pt_grad(x0, x1, x2, x3, g); break;
+        case PT_PP01: pp_grad(x0, x1, 0, 1, g); break;
+        case PT_PP02: pp_grad(x0, x2, 0, 2, g); break;
+        case PT_PE012: pe_grad(x0, x1, x2, 0, 1, 2, g); break;
+        case PT_PP03: pp_grad(x0, x3, 0, 3, g); break;
+        case PT_PE031: pe_grad(x0, x3, x1, 0, 3, 1, g); break;
+        case PT_PE023: pe_grad(x0, x2, x3, 0, 2, 3, g); break;
+    }
+}
+
+__device__ void ee_pair_grad(F3 x0, F3 x1, F3 x2, F3 x3, int t, F3* g) {
+    g[0] = g[1] = g[2] = g[3] = F3{0.f, 0.f, 0.f};
+    switch (t) {
+        case EE_PP02: pp_grad(x0, x2, 0, 2, g); break;
+        case EE_PP03: pp_grad(x0, x3, 0, 3, g); break;
+        case EE_PP12: pp_grad(x1, x2, 1, 2, g); break;
+        case EE_PP13: pp_grad(x1, x3, 1, 3, g); break;
+        case EE_PE023: pe_grad(x0, x2, x3, 0, 2, 3, g); break;
+        case EE_PE123: pe_grad(x1, x2, x3, 1, 2, 3, g); break;
+        case EE_PE201: pe_grad(x2, x0, x1, 2, 0, 1, g); break;
+        case EE_PE301: pe_grad(x3, x0, x1, 3, 0, 1, g); break;
+        case EE_EE: ee_grad(x0, x1, x2, x3, g); break;
+    }
+}
+
+// IPC log-barrier and derivatives (collision_energy.py:8-28); Warp's select(c, a, b) returns a when c is false
+__device__ __forceinline__ float barrier(float d, float dh) { return d >= dh ? 0.f : -(d - dh) * (d - dh) * logf(d / dh); }
+__device__ __forceinline__ float barrier_d1(float d, float dh) {
+    const float t = d - dh;
+    return d >= dh ? 0.f : -2.0f * t * logf(d / dh) - t * t / d;
+}
+__device__ __forceinline__ float barrier_d2(float d, float dh) {
+    return d >= dh ? 0.f : -2.0f * logf(d / dh) - 2.0f * (d - dh) / d - 1.0f + (dh * dh) / (d * d);
+}
+
+// ------------------------------------------------------------------ compensated reductions (deterministic)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+struct CSum {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        float t, e;
+        two_sum(s, x, t, e);
+        s = t;
+        c += e;
+    }
+    __device__ __forceinline__ void merge(const CSum& o) {
+        add(o.s);
+        c += o.c;
+    }
+};
+
+__device__ CSum block_reduce(CSum v) {
+    __shared__ float ss[32], cc[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        CSum w;
+        w.s = __shfl_down_sync(0xffffffffu, v.s, o);
+        w.c = __shfl_down_sync(0xffffffffu, v.c, o);
+        if (lane + o < 32) v.merge(w);
+    }
+    if (lane == 0) {
+        ss[warp] = v.s;
+        cc[warp] = v.c;
+    }
+    __syncthreads();
+    CSum r;
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        if (lane < nw) {
+            r.s = ss[lane];
+            r.c = cc[lane];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            CSum w;
+            w.s = __shfl_down_sync(0xffffffffu, r.s, o);
+            w.c = __shfl_down_sync(0xffffffffu, r.c, o);
+            if (lane + o < 32) r.merge(w);
+        }
+    }
+    __syncthreads();
+    return r;
+}
+
+// partial sums of vals[0..n) over a fixed split into kRedBlocks chunks
+__global__ void __launch_bounds__(kT) k_reduce(const float* __restrict__ vals, const int* d_n, int n_add, float2* partial) {
+    const int n = (d_n ? *d_n : 0) + n_add;
+    const int chunk = (n + kRedBlocks - 1) / kRedBlocks;
+    const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+    CSum acc;
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) acc.add(vals[i]);
+    CSum r = block_reduce(acc);
+    if (threadIdx.x == 0) partial[blockIdx.x] = make_float2(r.s, r.c);
+}
+
+// partial sums of a . b over vec3 arrays
+__global__ void __launch_bounds__(kT) k_reduce_dot(const float4* __restrict__ a, const float4* __restrict__ b, int n,
+                                                   float2* partial) {
+    const int chunk = (n + kRedBlocks - 1) / kRedBlocks;
+    const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+    CSum acc;
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const float4 x = a[i], y = b[i];
+        acc.add(x.x * y.x + x.y * y.y + x.z * y.z);
+    }
+    CSum r = block_reduce(acc);
+    if (threadIdx.x == 0) partial[blockIdx.x] = make_float2(r.s, r.c);
+}
+
+__global__ void __launch_bounds__(kT) k_reduce_finish(const float2* __restrict__ partial, float* out, float* copy_prev) {
+    CSum acc;
+    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) {
+        CSum p;
+        p.s = partial[i].x;
+        p.c = partial[i].y;
+        acc.merge(p);
+    }
+    CSum r = block_reduce(acc);
+    if (threadIdx.x == 0) {
+        if (copy_prev) *copy_prev = *out;
+        *out = r.s + r.c;
+    }
+}
+
+// ------------------------------------------------------------------ set-up kernels
+// normalisation of processing.py:15-21: centre = mean of the GT vertices, scale = 1 / max extent (float64)
+__global__ void k_norm_stats(const double* __restrict__ gt, int n, double* stats) {
+    // one block: fixed-order float64 sums and extents
+    __shared__ double sh[6][kT];
+    double s[3] = {0, 0, 0}, mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        for (int d = 0; d < 3; ++d) {
+            const double x = (double)gt[3 * i + d];
+            s[d] += x;
+            mn[d] = fmin(mn[d], x);
+            mx[d] = fmax(mx[d], x);
+        }
+    for (int d = 0; d < 3; ++d) {
+        sh[d][threadIdx.x] = s[d];
+        sh[3 + d][threadIdx.x] = 0;
+    }
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o)
+            for (int d = 0; d < 3; ++d) sh[d][threadIdx.x] += sh[d][threadIdx.x + o];
+        __syncthreads();
+    }
+    double c[3];
+    for (int d = 0; d < 3; ++d) c[d] = sh[d][0] / (double)n;
+    __syncthreads();
+    for (int d = 0; d < 3; ++d) {
+        sh[d][threadIdx.x] = mn[d];
+        sh[3 + d][threadIdx.x] = mx[d];
+    }
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o)
+            for (int d = 0; d < 3; ++d) {
+                sh[d][threadIdx.x] = fmin(sh[d][threadIdx.x], sh[d][threadIdx.x + o]);
+                sh[3 + d][threadIdx.x] = fmax(sh[3 + d][threadIdx.x], sh[3 + d][threadIdx.x + o]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double ext = 0;
+        for (int d = 0; d < 3; ++d) ext = fmax(ext, sh[3 + d][0] - sh[d][0]);
+        const double scale = 1.0 / ext;
+        for (int d = 0; d < 3; ++d) {
+            stats[d] = c[d];
+            stats[4 + d] = -c[d] * scale;  // t = -centre * scale
+        }
+        stats[3] = scale;
+    }
+}
+
+// V * scale + t in float64 (numpy), stored as float32 (the simulation arrays)
+template <typename T>
+__global__ void k_normalize(const T* __restrict__ in, int n, const double* __restrict__ st, float4* out, float4* copy) {
+    const double s = st[3];
+    for (int i = gtid(); i < n; i += gstride()) {
+        const float4 p = make_float4((float)((double)in[3 * i] * s + st[4]), (float)((double)in[3 * i + 1] * s + st[5]),
+                                     (float)((double)in[3 * i + 2] * s + st[6]), 0.f);
+        out[i] = p;
+        if (copy) copy[i] = p;
+    }
+}
+
+__global__ void k_denormalize(const float4* __restrict__ q, int n, const double* __restrict__ st, double* out) {
+    const double s = st[3];
+    for (int i = gtid(); i < n; i += gstride()) {
+        const float4 p = q[i];
+        out[3 * i] = ((double)p.x - st[4]) / s;
+        out[3 * i + 1] = ((double)p.y - st[5]) / s;
+        out[3 * i + 2] = ((double)p.z - st[6]) / s;
+    }
+}
+
+// int32 rows of 3 -> int4; an index outside [0, n_points) sets *bad and the face becomes (0, 0, 0)
+__global__ void k_tris4(const int* __restrict__ t, int n, int n_points, int4* out, int* bad) {
+    for (int i = gtid(); i < n; i += gstride()) {
+        int4 f = make_int4(t[3 * i], t[3 * i + 1], t[3 * i + 2], 0);
+        if ((unsigned)f.x >= (unsigned)n_points || (unsigned)f.y >= (unsigned)n_points ||
+            (unsigned)f.z >= (unsigned)n_points) {
+            atomicOr(bad, 1);
+            f = make_int4(0, 0, 0, 0);
+        }
+        out[i] = f;
+    }
+}
+
+// The float64 normalised position of vertex i, as numpy forms it from the float32 input (V * scale + t).
+struct D3 {
+    double x, y, z;
+};
+__device__ __forceinline__ D3 norm_pos(const double* __restrict__ pts, int i, const double* __restrict__ st) {
+    const double s = st[3];
+    return {(double)pts[3 * i] * s + st[4], (double)pts[3 * i + 1] * s + st[5], (double)pts[3 * i + 2] * s + st[6]};
+}
+__device__ __forceinline__ double dsq(D3 a, D3 b) {
+    const double x = a.x - b.x, y = a.y - b.y, z = a.z - b.z;
+    return (x * x + y * y) + z * z;
+}
+
+// Mixed Voronoi area per vertex (Meyer, Desbrun, Schroeder, Barr 2003) in the circumcentre form that
+// igl::massmatrix(V, F, MASSMATRIX_TYPE_VORONOI) evaluates in float64 (system.py:223-225): corner cosines
+// by the law of cosines, circumcentre barycentric weights cos_i * l_i normalised to sum 1, the vertex
+// taking half of the two sub-triangles beside it; an obtuse corner takes half the area, the others a quarter.
+// Accumulated into float64 per vertex, then rounded to float32 (the simulation's weights array).
+__global__ void k_voronoi(const double* __restrict__ pts, const double* __restrict__ st, const int4* __restrict__ tri,
+                          int nt, double* w) {
+    for (int f = gtid(); f < nt; f += gstride()) {
+        const int4 t = tri[f];
+        const int id[3] = {t.x, t.y, t.z};
+        const D3 p[3] = {norm_pos(pts, t.x, st), norm_pos(pts, t.y, st), norm_pos(pts, t.z, st)};
+        double l[3], l2[3];
+        for (int k = 0; k < 3; ++k) {  // l[k]: edge opposite corner k
+            l2[k] = dsq(p[(k + 1) % 3], p[(k + 2) % 3]);
+            l[k] = sqrt(l2[k]);
+        }
+        // doublearea by Heron's formula on the sorted lengths (Kahan's stable arrangement)
+        double a = l[0], b = l[1], c = l[2];
+        if (a < b) { const double tt = a; a = b; b = tt; }
+        if (b < c) { const double tt = b; b = c; c = tt; }
+        if (a < b) { const double tt = a; a = b; b = tt; }
+        double dblA = 0.5 * sqrt((a + (b + c)) * (c - (a - b)) * (c + (a - b)) * (a + (b - c)));
+        if (dblA != dblA) dblA = 0.0;
+        double cs[3], bc[3];
+        for (int k = 0; k < 3; ++k) {
+            const int j = (k + 1) % 3, m = (k + 2) % 3;
+            cs[k] = (l[m] * l[m] + l[j] * l[j] - l[k] * l[k]) / (l[j] * l[m] * 2.0);
+            bc[k] = cs[k] * l[k];
+        }
+        const double sum = bc[0] + bc[1] + bc[2];
+        double part[3], quad[3];
+        for (int k = 0; k < 3; ++k) part[k] = (bc[k] / sum) * (dblA * 0.5);
+        for (int k = 0; k < 3; ++k) quad[k] = (part[(k + 1) % 3] + part[(k + 2) % 3]) * 0.5;
+        for (int o = 0; o < 3; ++o)
+            if (cs[o] < 0)
+                for (int k = 0; k < 3; ++k) quad[k] = (k == o) ? 0.25 * dblA : 0.125 * dblA;
+        for (int k = 0; k < 3; ++k) atomicAdd(&w[id[k]], quad[k]);
+    }
+}
+
+__global__ void k_weights_f32(const double* __restrict__ w64, int n, float* w) {
+    for (int i = gtid(); i < n; i += gstride()) w[i] = (float)w64[i];
+}
+
+// elastic_preprocess_kernel (elastic_energy.py:7-37)
+__global__ void k_elastic_pre(const float4* __restrict__ xr, const int4* __restrict__ tri, int nt, float* area, float4* invDm) {
+    for (int f = gtid(); f < nt; f += gstride()) {
+        const int4 t = tri[f];
+        const F3 x0 = f3(xr[t.x]), x1 = f3(xr[t.y]), x2 = f3(xr[t.z]);
+        const F3 x01 = x1 - x0, x02 = x2 - x0;
+        const float W = 0.5f * length(cross(x01, x02));
+        const F3 b1 = normalize(x01);
+        F3 b2 = x02 - dot(x02, b1) * b1;
+        b2 = normalize(b2);
+        const float a = dot(b1, x01), b = dot(b1, x02), c = dot(b2, x01), d = dot(b2, x02);
+        const float det = a * d - b * c;
+        area[f] = W;
+        invDm[f] = make_float4(d / det, -b / det, -c / det, a / det);
+    }
+}
+
+// compute_hinge_angle (hinge_energy.py:4-18)
+__device__ __forceinline__ float hinge_angle(F3 x0, F3 x1, F3 x2, F3 x3) {
+    const F3 e12 = normalize(x2 - x1);
+    const F3 n1 = normalize(cross(e12, x0 - x1));
+    const F3 n2 = normalize(cross(x3 - x1, e12));
+    return atan2f(dot(cross(n1, n2), e12), dot(n1, n2));
+}
+
+__global__ void k_hinge_pre(const float4* __restrict__ xr, const int4* __restrict__ hinge, int nh, float2* rest) {
+    for (int h = gtid(); h < nh; h += gstride()) {
+        const int4 i = hinge[h];
+        const F3 x0 = f3(xr[i.x]), x1 = f3(xr[i.y]), x2 = f3(xr[i.z]), x3 = f3(xr[i.w]);
+        rest[h] = make_float2(hinge_angle(x0, x1, x2, x3), length(x1 - x2));
+    }
+}
+
+// The do-nothing test of system.py:214-221: min over igl::internal_angles(V, F) (float64, law of cosines on
+// squared edge lengths, acos without clamping) converted to degrees, compared with min_angle_thres. numpy's
+// min propagates NaN (a zero-length edge, or an acos argument rounded past 1), and NaN <= thres is false, so
+// one NaN angle anywhere disables the test. flag bit 0: some angle <= thres; bit 1: some angle is NaN.
+__global__ void k_min_angle(const double* __restrict__ pts, const double* __restrict__ st, const int4* __restrict__ tri,
+                            int nt, double thres_deg, int* flag) {
+    for (int f = gtid(); f < nt; f += gstride()) {
+        const int4 t = tri[f];
+        const D3 p[3] = {norm_pos(pts, t.x, st), norm_pos(pts, t.y, st), norm_pos(pts, t.z, st)};
+        double s[3];
+        for (int k = 0; k < 3; ++k) s[k] = dsq(p[(k + 1) % 3], p[(k + 2) % 3]);  // opposite corner k
+        for (int d = 0; d < 3; ++d) {
+            const double s1 = s[d], s2 = s[(d + 1) % 3], s3 = s[(d + 2) % 3];
+            const double ang = acos((s3 + s2 - s1) / (2. * sqrt(s3 * s2)));
+            const double deg = ang * 180.0 / 3.141592653589793;
+            if (deg != deg) atomicOr(flag, 2);
+            else if (deg <= thres_deg) atomicOr(flag, 1);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ closest point on the GT mesh
+// Closest point of p on triangle (a, b, c): Ericson, Real-Time Collision Detection, 5.1.5
+__device__ F3 closest_on_triangle(F3 p, F3 a, F3 b, F3 c) {
+    const F3 ab = b - a, ac = c - a, ap = p - a;
+    const float d1 = dot(ab, ap), d2 = dot(ac, ap);
+    if (d1 <= 0.f && d2 <= 0.f) return a;
+    const F3 bp = p - b;
+    const float d3 = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3 >= 0.f && d4 <= d3) return b;
+    const float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) return a + (d1 / (d1 - d3)) * ab;
+    const F3 cp = p - c;
+    const float d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d6 >= 0.f && d5 <= d6) return c;
+    const float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) return a + (d2 / (d2 - d6)) * ac;
+    const float va = d3 * d6 - d5 * d4;
+    if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) return b + ((d4 - d3) / ((d4 - d3) + (d5 - d6))) * (c - b);
+    const float den = 1.f / (va + vb + vc);
+    return a + (vb * den) * ab + (vc * den) * ac;
+}
+
+__device__ __forceinline__ float box_dist_sq(F3 p, float4 lo, float4 hi) {
+    const float dx = fmaxf(fmaxf(lo.x - p.x, 0.f), p.x - hi.x);
+    const float dy = fmaxf(fmaxf(lo.y - p.y, 0.f), p.y - hi.y);
+    const float dz = fmaxf(fmaxf(lo.z - p.z, 0.f), p.z - hi.z);
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// mesh_query_point_no_sign(gt, x, 1e9) + mesh_eval_position (geometry_kernels.py:81-93): nearest point of the
+// GT surface by branch and bound over the GT LBVH (stack in shared memory, nearer child first)
+__global__ void __launch_bounds__(kQT) k_closest_gt(const float4* __restrict__ q, int np, const int2* __restrict__ child,
+                                                    const float4* __restrict__ nlo, const float4* __restrict__ nhi,
+                                                    const float4* __restrict__ llo, const float4* __restrict__ lhi,
+                                                    const int* __restrict__ leaf_face, const int4* __restrict__ gtri,
+                                                    const float4* __restrict__ gpos, const RoundCounters* grc,
+                                                    float4* target, int* status) {
+    __shared__ int stack[kStack][kQT];
+    const int nl = grc->n_live;
+    for (int i = gtid(); i < np; i += gstride()) {
+        const F3 p = f3(q[i]);
+        float best = 1e18f;  // (max distance 1e9)^2
+        F3 bp = p;
+        auto leaf = [&](int li) {
+            const int4 t = gtri[leaf_face[li]];
+            const F3 c = closest_on_triangle(p, f3(gpos[t.x]), f3(gpos[t.y]), f3(gpos[t.z]));
+            const float d = length_sq(c - p);
+            if (d < best) {
+                best = d;
+                bp = c;
+            }
+        };
+        if (nl == 1) leaf(0);
+        if (nl >= 2) {
+            int sp = 0, node = 0, guard = 0;
+            while (true) {
+                if (++guard > (1 << 22)) {
+                    atomicOr(status, 2);
+                    break;
+                }
+                const int2 c = child[node];
+                int nxt[2];
+                float nd[2];
+                int nn = 0;
+                for (int side = 0; side < 2; ++side) {
+                    const int x = side ? c.y : c.x;
+                    const float d = x < 0 ? box_dist_sq(p, llo[~x], lhi[~x]) : box_dist_sq(p, nlo[x], nhi[x]);
+                    if (d >= best) continue;
+                    if (x < 0) leaf(~x);
+                    else {
+                        nxt[nn] = x;
+                        nd[nn] = d;
+                        ++nn;
+                    }
+                }
+                if (nn == 2) {
+                    if (nd[1] < nd[0]) {
+                        const int t = nxt[0]; nxt[0] = nxt[1]; nxt[1] = t;
+                    }
+                    if (sp >= kStack) {
+                        atomicOr(status, 4);
+                        break;
+                    }
+                    stack[sp++][threadIdx.x] = nxt[1];
+                    node = nxt[0];
+                } else if (nn == 1) {
+                    node = nxt[0];
+                } else {
+                    bool found = false;
+                    while (sp > 0) {
+                        node = stack[--sp][threadIdx.x];
+                        // re-test the stacked node against the current best
+                        if (box_dist_sq(p, nlo[node], nhi[node]) < best) {
+                            found = true;
+                            break;
+                        }
+                    }
+                    if (!found) break;
+                }
+            }
+        }
+        target[i] = f4(bp);
+    }
+}
+
+// ------------------------------------------------------------------ contact detection (contact_detection.py:144-216)
+template <bool kEdges>
+__global__ void __launch_bounds__(kQT) k_detect(const float4* __restrict__ x, int n_query, const int4* __restrict__ elems,
+                                                const int2* __restrict__ child, const float4* __restrict__ nlo,
+                                                const float4* __restrict__ nhi, const float4* __restrict__ llo,
+                                                const float4* __restrict__ lhi, const int* __restrict__ leaf_id,
+                                                const RoundCounters* brc, float thr, float ee_thres, int4* c_idx,
+                                                int2* c_type, int cap, SolverScalars* sc) {
+    __shared__ int stack[kStack][kQT];
+    const int nl = brc->n_live;
+    for (int qi = gtid(); qi < n_query; qi += gstride()) {
+        int i0, i1 = -1;
+        F3 x0, x1 = {0, 0, 0}, lo, hi;
+        if (!kEdges) {
+            i0 = qi;
+            x0 = f3(x[i0]);
+            lo = x0 - F3{thr, thr, thr};
+            hi = x0 + F3{thr, thr, thr};
+        } else {
+            const int4 e = elems[qi];
+            i0 = e.x;
+            i1 = e.y;
+            x0 = f3(x[i0]);
+            x1 = f3(x[i1]);
+            lo = fmin3(x0, x1) - F3{thr, thr, thr};
+            hi = fmax3(x0, x1) + F3{thr, thr, thr};
+        }
+        const float4 qlo = make_float4(lo.x, lo.y, lo.z, 0.f), qhi = make_float4(hi.x, hi.y, hi.z, 0.f);
+        auto overlap = [&](float4 a, float4 b) {
+            return !(qhi.x < a.x || b.x < qlo.x || qhi.y < a.y || b.y < qlo.y || qhi.z < a.z || b.z < qlo.z);
+        };
+        auto leaf = [&](int li) {
+            const int id = leaf_id[li];
+            const int4 t = elems[id];
+            if (!kEdges) {
+                if (i0 == t.x || i0 == t.y || i0 == t.z) return;
+                const F3 a = f3(x[t.x]), b = f3(x[t.y]), c = f3(x[t.z]);
+                const int ty = pt_classify(x0, a, b, c);
+                const float d = pt_pair_distance(x0, a, b, c, ty);
+                if (d <= thr) {
+                    const int at = atomicAdd(&sc->n_contacts_raw, 1);
+                    if (at < cap) {
+                        c_idx[at] = make_int4(i0, t.x, t.y, t.z);
+                        c_type[at] = make_int2(BLOCK_PT, ty);
+                    }
+                }
+            } else {
+                if (!(qi < id)) return;
+                const int i2 = t.x, i3 = t.y;
+                if (i0 == i2 || i0 == i3 || i1 == i2 || i1 == i3) return;
+                const F3 a = f3(x[i2]), b = f3(x[i3]);
+                const int ty = ee_classify(x0, x1, a, b, ee_thres);
+                const float d = ee_pair_distance(x0, x1, a, b, ty);
+                if (d <= thr) {
+                    const int at = atomicAdd(&sc->n_contacts_raw, 1);
+                    if (at < cap) {
+                        c_idx[at] = make_int4(i0, i1, i2, i3);
+                        c_type[at] = make_int2(BLOCK_EE, ty);
+                    }
+                }
+            }
+        };
+        if (nl == 1) {
+            if (overlap(llo[0], lhi[0])) leaf(0);
+            continue;
+        }
+        if (nl < 1) continue;
+        int sp = 0, node = 0, guard = 0;
+        while (true) {
+            if (++guard > (1 << 22)) {
+                atomicOr(&sc->status, 2);
+                break;
+            }
+            const int2 c = child[node];
+            int nxt[2];
+            int nn = 0;
+            for (int side = 0; side < 2; ++side) {
+                const int xx = side ? c.y : c.x;
+                if (xx < 0) {
+                    if (overlap(llo[~xx], lhi[~xx])) leaf(~xx);
+                } else if (overlap(nlo[xx], nhi[xx])) {
+                    nxt[nn++] = xx;
+                }
+            }
+            if (nn == 2) {
+                if (sp >= kStack) {
+                    atomicOr(&sc->status, 4);
+                    break;
+                }
+                stack[sp++][threadIdx.x] = nxt[1];
+                node = nxt[0];
+            } else if (nn == 1) {
+                node = nxt[0];
+            } else {
+                if (sp == 0) break;
+                node = stack[--sp][threadIdx.x];
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ energies (one value per element)
+// segments of e_elem: [0, NP) distance to GT, [NP, NP + NT) StVK, [.., + NH) hinge, [.., + NC) barrier
+__global__ void k_energy_m2gt(const float4* __restrict__ x, const float4* __restrict__ tgt, const float* __restrict__ w,
+                              float stiff, int np, float* e) {
+    for (int i = gtid(); i < np; i += gstride()) {
+        const float wi = w[i] * stiff;
+        e[i] = 0.5f * length_sq(f3(x[i]) - f3(tgt[i])) * wi;
+    }
+}
+
+struct Mat2 {
+    float a, b, c, d;  // [[a, b], [c, d]]
+};
+__device__ __forceinline__ Mat2 mmul(Mat2 x, Mat2 y) {
+    return {x.a * y.a + x.b * y.c, x.a * y.b + x.b * y.d, x.c * y.a + x.d * y.c, x.c * y.b + x.d * y.d};
+}
+__device__ __forceinline__ Mat2 mtr(Mat2 x) { return {x.a, x.c, x.b, x.d}; }
+__device__ __forceinline__ Mat2 madd(Mat2 x, Mat2 y) { return {x.a + y.a, x.b + y.b, x.c + y.c, x.d + y.d}; }
+__device__ __forceinline__ Mat2 mscale(float s, Mat2 x) { return {s * x.a, s * x.b, s * x.c, s * x.d}; }
+__device__ __forceinline__ float mtrace(Mat2 x) { return x.a + x.d; }
+
+struct ElasticLocal {
+    F3 b1, b2;
+    Mat2 F, invDm;
+    float W;
+};
+__device__ __forceinline__ ElasticLocal elastic_local(const float4* __restrict__ x, int4 t, float W, float4 inv) {
+    ElasticLocal L;
+    const F3 x0 = f3(x[t.x]), x1 = f3(x[t.y]), x2 = f3(x[t.z]);
+    const F3 x01 = x1 - x0, x02 = x2 - x0;
+    L.b1 = normalize(x01);
+    L.b2 = normalize(x02 - dot(x02, L.b1) * L.b1);
+    const Mat2 Ds = {dot(L.b1, x01), dot(L.b1, x02), dot(L.b2, x01), dot(L.b2, x02)};
+    L.invDm = {inv.x, inv.y, inv.z, inv.w};
+    L.F = mmul(Ds, L.invDm);
+    L.W = W;
+    return L;
+}
+
+__global__ void k_energy_elastic(const float4* __restrict__ x, const int4* __restrict__ tri, const float* __restrict__ area,
+                                 const float4* __restrict__ invDm, float mu, float la, int nt, float* e) {
+    for (int f = gtid(); f < nt; f += gstride()) {
+        const ElasticLocal L = elastic_local(x, tri[f], area[f], invDm[f]);
+        const Mat2 I = {1.f, 0.f, 0.f, 1.f};
+        const Mat2 E = mscale(0.5f, madd(mmul(mtr(L.F), L.F), mscale(-1.f, I)));
+        const float trE = mtrace(E);
+        e[f] = L.W * (mu * mtrace(mmul(E, mtr(E))) + 0.5f * la * trE * trE);
+    }
+}
+
+__global__ void k_energy_hinge(const float4* __restrict__ x, const int4* __restrict__ hinge, const float2* __restrict__ rest,
+                               float k, int nh, float* e) {
+    for (int h = gtid(); h < nh; h += gstride()) {
+        const int4 i = hinge[h];
+        const float th = hinge_angle(f3(x[i.x]), f3(x[i.y]), f3(x[i.z]), f3(x[i.w]));
+        const float dth = th - rest[h].x;
+        e[h] = 0.5f * k * dth * dth * rest[h].y;
+    }
+}
+
+// collision_energy_kernel (collision_energy.py:49-99): reclassify, store the type and distance
+__global__ void k_energy_contact(const float4* __restrict__ x, const int4* __restrict__ cidx, int2* ctype, float* cd,
+                                 const SolverScalars* sc, float kappa, float dh, float ee_thres, float* e) {
+    const int n = sc->n_contacts;
+    for (int b = gtid(); b < n; b += gstride()) {
+        const int4 i = cidx[b];
+        const F3 x0 = f3(x[i.x]), x1 = f3(x[i.y]), x2 = f3(x[i.z]), x3 = f3(x[i.w]);
+        int2 t = ctype[b];
+        float d;
+        if (t.x == BLOCK_PT) {
+            t.y = pt_classify(x0, x1, x2, x3);
+            d = pt_pair_distance(x0, x1, x2, x3, t.y);
+        } else {
+            t.y = ee_classify(x0, x1, x2, x3, ee_thres);
+            d = ee_pair_distance(x0, x1, x2, x3, t.y);
+        }
+        ctype[b] = t;
+        cd[b] = d;
+        e[b] = d < dh ? barrier(d, dh) * kappa : 0.f;
+    }
+}
+
+// ------------------------------------------------------------------ gradients and Hessian diagonal (coeff = -1)
+__global__ void k_diff_m2gt(const float4* __restrict__ x, const float4* __restrict__ tgt, const float* __restrict__ w,
+                            float stiff, float coeff, int np, float4* grad, float4* hd) {
+    for (int i = gtid(); i < np; i += gstride()) {
+        const float wi = w[i] * stiff;
+        atomic_add3(grad, i, (f3(x[i]) - f3(tgt[i])) * wi * coeff);
+        atomic_add3(hd, i, F3{wi, wi, wi});
+    }
+}
+
+__global__ void k_diff_elastic(const float4* __restrict__ x, const int4* __restrict__ tri, const float* __restrict__ area,
+                               const float4* __restrict__ invDm, float mu, float la, float coeff, int nt, float4* grad) {
+    for (int f = gtid(); f < nt; f += gstride()) {
+        const int4 t = tri[f];
+        const ElasticLocal L = elastic_local(x, t, area[f], invDm[f]);
+        const Mat2 I = {1.f, 0.f, 0.f, 1.f};
+        const Mat2 E = mscale(0.5f, madd(mmul(mtr(L.F), L.F), mscale(-1.f, I)));
+        const float trE = mtrace(E);
+        const Mat2 P = mmul(L.F, madd(mscale(2.f * mu, E), mscale(la * trE, I)));
+        const Mat2 H = mscale(coeff * L.W, mmul(P, mtr(L.invDm)));
+        const F3 f1 = H.a * L.b1 + H.c * L.b2;
+        const F3 f2 = H.b * L.b1 + H.d * L.b2;
+        atomic_add3(grad, t.x, -f1 - f2);
+        atomic_add3(grad, t.y, f1);
+        atomic_add3(grad, t.z, f2);
+    }
+}
+
+struct M33 {
+    float m[3][3];
+};
+__device__ __forceinline__ M33 outer(F3 a, F3 b) {
+    const float A[3] = {a.x, a.y, a.z}, B[3] = {b.x, b.y, b.z};
+    M33 r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) r.m[i][j] = A[i] * B[j];
+    return r;
+}
+__device__ __forceinline__ M33 tr(M33 a) {
+    M33 r;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) r.m[i][j] = a.m[j][i];
+    return r;
+}
+__device__ __forceinline__ M33 add(M33 a, M33 b) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) a.m[i][j] += b.m[i][j];
+    return a;
+}
+__device__ __forceinline__ M33 sub(M33 a, M33 b) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) a.m[i][j] -= b.m[i][j];
+    return a;
+}
+__device__ __forceinline__ M33 scl(float s, M33 a) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) a.m[i][j] *= s;
+    return a;
+}
+__device__ __forceinline__ M33 sym(M33 a) { return add(a, tr(a)); }
+
+// hinge_diff_kernel (hinge_energy.py:85-238): gradient, Hessian diagonal and the 4x4 blocks of 3x3
+__global__ void k_diff_hinge(const float4* __restrict__ x, const int4* __restrict__ hinge, const float2* __restrict__ rest,
+                             float k, float coeff, int nh, float* blocks, float4* grad, float4* hd) {
+    for (int h = gtid(); h < nh; h += gstride()) {
+        const int4 id = hinge[h];
+        const F3 x0 = f3(x[id.x]), x1 = f3(x[id.y]), x2 = f3(x[id.z]), x3 = f3(x[id.w]);
+        const float rest_angle = rest[h].x, rest_elen = rest[h].y;
+        const F3 e0 = x2 - x1, e1 = x0 - x2, e2 = x0 - x1, e1_ = x3 - x2, e2_ = x3 - x1;
+        const float e0_lensq = length_sq(e0);
+        const float e0_len = sqrtf(e0_lensq), e1_len = length(e1), e2_len = length(e2), e1_len_ = length(e1_),
+                    e2_len_ = length(e2_);
+        const F3 e0u = normalize(e0), e1u = normalize(e1), e2u = normalize(e2), e1u_ = normalize(e1_), e2u_ = normalize(e2_);
+        const float ca1 = dot(e2u, e0u), ca2 = -dot(e1u, e0u), ca1_ = dot(e2u_, e0u), ca2_ = -dot(e1u_, e0u);
+        const float h0 = length(cross(e1, e2)) / e0_len, h1 = length(cross(e0, e2)) / e1_len, h2 = length(cross(e0, e1)) / e2_len;
+        const float h0_ = length(cross(e1_, e2_)) / e0_len, h1_ = length(cross(e0, e2_)) / e1_len_,
+                    h2_ = length(cross(e0, e1_)) / e2_len_;
+        const F3 n = normalize(cross(e0, e2)), n_ = normalize(cross(e2_, e0));
+        const float theta = atan2f(dot(cross(n, n_), e0) / e0_len, dot(n, n_));
+        const float dE = k * (theta - rest_angle) * rest_elen;
+        const float d2E = k * rest_elen;
+        const F3 g1 = n * (ca2 / h1) + n_ * (ca2_ / h1_);
+        const F3 g2 = n * (ca1 / h2) + n_ * (ca1_ / h2_);
+        const F3 g0 = n * (-1.0f / h0);
+        const F3 g3 = n_ * (-1.0f / h0_);
+        atomic_add3(grad, id.x, dE * g0 * coeff);
+        atomic_add3(grad, id.y, dE * g1 * coeff);
+        atomic_add3(grad, id.z, dE * g2 * coeff);
+        atomic_add3(grad, id.w, dE * g3 * coeff);
+        const F3 m0 = normalize(cross(e0, n)), m1 = normalize(cross(e1, n)), m2 = normalize(cross(n, e2));
+        const F3 m0_ = normalize(cross(n_, e0)), m1_ = normalize(cross(n_, e1_)), m2_ = normalize(cross(e2_, n_));
+        const M33 M0 = outer(n, m0), M1 = outer(n, m1), M2 = outer(n, m2);
+        const M33 M0_ = outer(n_, m0_), M1_ = outer(n_, m1_), M2_ = outer(n_, m2_);
+        const M33 N0 = scl(1.f / e0_lensq, M0), N0_ = scl(1.f / e0_lensq, M0_);
+        const M33 P10 = scl(ca1 / (h1 * h0), tr(M0)), P11 = scl(ca1 / (h1 * h1), tr(M1)), P12 = scl(ca1 / (h1 * h2), tr(M2));
+        const M33 P20 = scl(ca2 / (h2 * h0), tr(M0)), P21 = scl(ca2 / (h2 * h1), tr(M1)), P22 = scl(ca2 / (h2 * h2), tr(M2));
+        const M33 P10_ = scl(ca1_ / (h1_ * h0_), tr(M0_)), P11_ = scl(ca1_ / (h1_ * h1_), tr(M1_)),
+                  P12_ = scl(ca1_ / (h1_ * h2_), tr(M2_));
+        const M33 P20_ = scl(ca2_ / (h2_ * h0_), tr(M0_)), P21_ = scl(ca2_ / (h2_ * h1_), tr(M1_)),
+                  P22_ = scl(ca2_ / (h2_ * h2_), tr(M2_));
+        const M33 Q0 = scl(1.f / (h0 * h0), M0), Q1 = scl(1.f / (h0 * h1), M1), Q2 = scl(1.f / (h0 * h2), M2);
+        const M33 Q0_ = scl(1.f / (h0_ * h0_), M0_), Q1_ = scl(1.f / (h0_ * h1_), M1_), Q2_ = scl(1.f / (h0_ * h2_), M2_);
+        M33 B[4][4];
+        B[0][0] = add(scl(-dE, sym(Q0)), scl(d2E, outer(g0, g0)));
+        B[3][3] = add(scl(-dE, sym(Q0_)), scl(d2E, outer(g3, g3)));
+        B[1][1] = add(scl(dE, sub(add(sub(sym(P11), N0), sym(P11_)), N0_)), scl(d2E, outer(g1, g1)));
+        B[2][2] = add(scl(dE, sub(add(sub(sym(P22), N0), sym(P22_)), N0_)), scl(d2E, outer(g2, g2)));
+        B[1][0] = add(scl(dE, sub(P10, Q1)), scl(d2E, outer(g1, g0)));
+        B[2][0] = add(scl(dE, sub(P20, Q2)), scl(d2E, outer(g2, g0)));
+        B[1][3] = add(scl(dE, sub(P10_, Q1_)), scl(d2E, outer(g1, g3)));
+        B[2][3] = add(scl(dE, sub(P20_, Q2_)), scl(d2E, outer(g2, g3)));
+        B[1][2] = add(scl(dE, add(add(add(add(add(P12, tr(P21)), N0), P12_), tr(P21_)), N0_)), scl(d2E, outer(g1, g2)));
+        B[0][3] = scl(d2E, outer(g0, g3));
+        B[0][1] = tr(B[1][0]);
+        B[0][2] = tr(B[2][0]);
+        B[3][1] = tr(B[1][3]);
+        B[3][2] = tr(B[2][3]);
+        B[2][1] = tr(B[1][2]);
+        B[3][0] = tr(B[0][3]);
+        float* out = blocks + (size_t)h * 144;
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b)
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) out[((a * 4 + b) * 3 + i) * 3 + j] = B[a][b].m[i][j];
+        const int ids[4] = {id.x, id.y, id.z, id.w};
+        for (int a = 0; a < 4; ++a) atomic_add3(hd, ids[a], F3{B[a][a].m[0][0], B[a][a].m[1][1], B[a][a].m[2][2]});
+    }
+}
+
+// block_spd_project_kernel (utils_kernels.py:21-39). The reference calls the fork-only
+// wp.spd_project_blocks(3, block, it_max); here the 9x9 matrix of blocks [0..2][0..2] is made positive
+// semi-definite by a cyclic Jacobi eigen-decomposition (it_max sweeps), clamping negative eigenvalues to
+// zero; the fourth block row and column are then set from the first three as the reference does.
+__global__ void k_spd_project(float* blocks, int nh, int sweeps) {
+    for (int h = gtid(); h < nh; h += gstride()) {
+        float* B = blocks + (size_t)h * 144;
+        float A[9][9], V[9][9];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b)
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) A[a * 3 + i][b * 3 + j] = B[((a * 4 + b) * 3 + i) * 3 + j];
+        for (int i = 0; i < 9; ++i)
+            for (int j = 0; j < 9; ++j) {
+                const float s = 0.5f * (A[i][j] + A[j][i]);
+                A[i][j] = s;
+                V[i][j] = (i == j) ? 1.f : 0.f;
+            }
+        for (int sw = 0; sw < sweeps; ++sw)
+            for (int p = 0; p < 8; ++p)
+                for (int q = p + 1; q < 9; ++q) {
+                    const float apq = A[p][q];
+                    if (fabsf(apq) < 1e-30f) continue;
+                    const float th = (A[q][q] - A[p][p]) / (2.f * apq);
+                    const float t = (th >= 0.f ? 1.f : -1.f) / (fabsf(th) + sqrtf(th * th + 1.f));
+                    const float c = 1.f / sqrtf(t * t + 1.f), s = t * c;
+                    for (int k = 0; k < 9; ++k) {
+                        const float akp = A[k][p], akq = A[k][q];
+                        A[k][p] = c * akp - s * akq;
+                        A[k][q] = s * akp + c * akq;
+                    }
+                    for (int k = 0; k < 9; ++k) {
+                        const float apk = A[p][k], aqk = A[q][k];
+                        A[p][k] = c * apk - s * aqk;
+                        A[q][k] = s * apk + c * aqk;
+                    }
+                    for (int k = 0; k < 9; ++k) {
+                        const float vkp = V[k][p], vkq = V[k][q];
+                        V[k][p] = c * vkp - s * vkq;
+                        V[k][q] = s * vkp + c * vkq;
+                    }
+                }
+        float lam[9];
+        for (int i = 0; i < 9; ++i) lam[i] = fmaxf(A[i][i], 0.f);
+        for (int i = 0; i < 9; ++i)
+            for (int j = 0; j < 9; ++j) {
+                float s = 0.f;
+                for (int k = 0; k < 9; ++k) s += V[i][k] * lam[k] * V[j][k];
+                A[i][j] = s;
+            }
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b)
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) B[((a * 4 + b) * 3 + i) * 3 + j] = A[a * 3 + i][b * 3 + j];
+        // block[3][j] = -sum_i block[i][j]; block[j][3] = block[3][j]^T; block[3][3] = -sum_j block[j][3]
+        for (int b = 0; b < 3; ++b)
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    float s = 0.f;
+                    for (int a = 0; a < 3; ++a) s -= B[((a * 4 + b) * 3 + i) * 3 + j];
+                    B[((3 * 4 + b) * 3 + i) * 3 + j] = s;
+                }
+        for (int b = 0; b < 3; ++b)
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) B[((b * 4 + 3) * 3 + i) * 3 + j] = B[((3 * 4 + b) * 3 + j) * 3 + i];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                float s = 0.f;
+                for (int b = 0; b < 3; ++b) s -= B[((b * 4 + 3) * 3 + i) * 3 + j];
+                B[((3 * 4 + 3) * 3 + i) * 3 + j] = s;
+            }
+    }
+}
+
+// collision_diff_kernel (collision_energy.py:192-254)
+__global__ void k_diff_contact(const float4* __restrict__ x, const int4* __restrict__ cidx, const int2* __restrict__ ctype,
+                               const float* __restrict__ cd, const SolverScalars* sc, float kappa, float dh, float coeff,
+                               float4* cdd, float4* grad, float4* hd) {
+    const int n = sc->n_contacts;
+    for (int b = gtid(); b < n; b += gstride()) {
+        const float d = cd[b];
+        if (d >= dh) continue;
+        const int4 i = cidx[b];
+        const F3 x0 = f3(x[i.x]), x1 = f3(x[i.y]), x2 = f3(x[i.z]), x3 = f3(x[i.w]);
+        const int2 t = ctype[b];
+        F3 g[4];
+        if (t.x == BLOCK_PT) pt_pair_grad(x0, x1, x2, x3, t.y, g);
+        else ee_pair_grad(x0, x1, x2, x3, t.y, g);
+        const float ddc = barrier_d1(d, dh) * kappa * coeff;
+        const float d2c = barrier_d2(d, dh) * kappa;
+        const int ids[4] = {i.x, i.y, i.z, i.w};
+        for (int k = 0; k < 4; ++k) {
+            cdd[4 * (size_t)b + k] = f4(g[k]);
+            atomic_add3(grad, ids[k], g[k] * ddc);
+            atomic_add3(hd, ids[k], d2c * F3{g[k].x * g[k].x, g[k].y * g[k].y, g[k].z * g[k].z});
+        }
+    }
+}
+
+// ------------------------------------------------------------------ Hessian-vector products
+__global__ void k_hvp(const float4* __restrict__ x, const float4* __restrict__ dx, const float* __restrict__ w, float stiff,
+                      int np, const int4* __restrict__ tri, const float* __restrict__ area, const float4* __restrict__ invDm,
+                      float mu, float la, int nt, const int4* __restrict__ hinge, const float* __restrict__ blocks, int nh,
+                      const int4* __restrict__ cidx, const float* __restrict__ cd, const float4* __restrict__ cdd,
+                      const SolverScalars* sc, float kappa, float dh, float4* out) {
+    const int nc = sc->n_contacts;
+    const long long total = (long long)np + nt + nh + nc;
+    for (long long g = gtid(); g < total; g += gstride()) {
+        if (g < np) {  // mesh2gt_pp_distance_energy_hess_dx_kernel
+            const int i = (int)g;
+            atomic_add3(out, i, f3(dx[i]) * (w[i] * stiff));
+        } else if (g < np + nt) {  // elastic_hess_dx_kernel (elastic_energy.py:151-220)
+            const int f = (int)(g - np);
+            const int4 t = tri[f];
+            const ElasticLocal L = elastic_local(x, t, area[f], invDm[f]);
+            const F3 dx01 = f3(dx[t.y]) - f3(dx[t.x]), dx02 = f3(dx[t.z]) - f3(dx[t.x]);
+            const Mat2 dDs = {dot(L.b1, dx01), dot(L.b1, dx02), dot(L.b2, dx01), dot(L.b2, dx02)};
+            const Mat2 dF = mmul(dDs, L.invDm);
+            const Mat2 I = {1.f, 0.f, 0.f, 1.f};
+            const Mat2 E = mscale(0.5f, madd(mmul(mtr(L.F), L.F), mscale(-1.f, I)));
+            const float trE = mtrace(E);
+            const Mat2 dE = mscale(0.5f, madd(mmul(mtr(dF), L.F), mmul(mtr(L.F), dF)));
+            const float trdE = mtrace(dE);
+            const Mat2 dP = madd(mmul(dF, madd(mscale(2.f * mu, E), mscale(la * trE, I))),
+                                 mmul(L.F, madd(mscale(2.f * mu, dE), mscale(la * trdE, I))));
+            const Mat2 dH = mscale(L.W, mmul(dP, mtr(L.invDm)));
+            const F3 df1 = dH.a * L.b1 + dH.c * L.b2;
+            const F3 df2 = dH.b * L.b1 + dH.d * L.b2;
+            atomic_add3(out, t.x, -df1 - df2);
+            atomic_add3(out, t.y, df1);
+            atomic_add3(out, t.z, df2);
+        } else if (g < np + nt + nh) {  // hinge_hess_dx_kernel (hinge_energy.py:241-274)
+            const int h = (int)(g - np - nt);
+            const int4 id = hinge[h];
+            const int ids[4] = {id.x, id.y, id.z, id.w};
+            const float* B = blocks + (size_t)h * 144;
+            F3 d[4];
+            for (int b = 0; b < 4; ++b) d[b] = f3(dx[ids[b]]);
+            for (int a = 0; a < 4; ++a) {
+                F3 acc = {0.f, 0.f, 0.f};
+                for (int b = 0; b < 4; ++b) {
+                    const float* M = B + (a * 4 + b) * 9;
+                    acc = acc + F3{M[0] * d[b].x + M[1] * d[b].y + M[2] * d[b].z, M[3] * d[b].x + M[4] * d[b].y + M[5] * d[b].z,
+                                   M[6] * d[b].x + M[7] * d[b].y + M[8] * d[b].z};
+                }
+                atomic_add3(out, ids[a], acc);
+            }
+        } else {  // collision_hess_dx_kernel (collision_energy.py:379-409), Gauss-Newton
+            const int b = (int)(g - np - nt - nh);
+            const float d = cd[b];
+            if (d >= dh) continue;
+            const float c = barrier_d2(d, dh) * kappa;
+            const int4 i = cidx[b];
+            const int ids[4] = {i.x, i.y, i.z, i.w};
+            F3 gg[4];
+            float s = 0.f;
+            for (int k = 0; k < 4; ++k) {
+                gg[k] = f3(cdd[4 * (size_t)b + k]);
+                s += dot(gg[k], f3(dx[ids[k]]));
+            }
+            for (int k = 0; k < 4; ++k) atomic_add3(out, ids[k], gg[k] * (s * c));
+        }
+    }
+}
+
+// ------------------------------------------------------------------ CG vector updates (solver_kernels.py)
+__global__ void k_cg_init(const float4* __restrict__ grad, const float4* __restrict__ hd, int np, float4* p, float4* r,
+                          float4* z, float4* v) {
+    for (int i = gtid(); i < np; i += gstride()) {
+        const float4 g = grad[i], d = hd[i];
+        p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        r[i] = g;
+        const float4 zz = make_float4(g.x / (d.x + 1e-6f), g.y / (d.y + 1e-6f), g.z / (d.z + 1e-6f), 0.f);
+        z[i] = zz;
+        v[i] = zz;
+    }
+}
+
+// update_p_r_z_compute_zr_kernel: p += a v, r -= a Av when v.Av > 1e-16; z = r / diag
+__global__ void k_cg_prz(const float4* __restrict__ v, const float4* __restrict__ Av, const float4* __restrict__ hd,
+                         const SolverScalars* sc, int np, float4* p, float4* r, float4* z) {
+    const float vAv = sc->v_A_v;
+    const float alpha = sc->z_r / vAv;
+    for (int i = gtid(); i < np; i += gstride()) {
+        float4 ri = r[i];
+        if (vAv > 1e-16f) {
+            const float4 vi = v[i], avi = Av[i];
+            float4 pi = p[i];
+            pi.x += alpha * vi.x; pi.y += alpha * vi.y; pi.z += alpha * vi.z;
+            ri.x -= alpha * avi.x; ri.y -= alpha * avi.y; ri.z -= alpha * avi.z;
+            p[i] = pi;
+            r[i] = ri;
+        }
+        const float4 d = hd[i];
+        z[i] = make_float4(ri.x / d.x, ri.y / d.y, ri.z / d.z, 0.f);
+    }
+}
+
+__global__ void k_cg_v(const float4* __restrict__ z, const SolverScalars* sc, int np, float4* v) {
+    const float s = sc->z_r / sc->z_r_last;
+    for (int i = gtid(); i < np; i += gstride()) {
+        const float4 zi = z[i], vi = v[i];
+        v[i] = make_float4(zi.x + s * vi.x, zi.y + s * vi.y, zi.z + s * vi.z, 0.f);
+    }
+}
+
+// clamp_p_kernel: keep |q_prev_newton + p - q_prev_detection| <= radius
+__global__ void k_clamp_p(float4* p, const float4* __restrict__ qn, const float4* __restrict__ qd, float radius, int np) {
+    for (int i = gtid(); i < np; i += gstride()) {
+        const F3 pi = f3(p[i]), qni = f3(qn[i]), qdi = f3(qd[i]);
+        const F3 dq = qni + pi - qdi;
+        if (length(dq) > radius) p[i] = f4(normalize(dq) * radius + qdi - qni);
+    }
+}
+
+// accd_kernel (ccd_kernels.py:9-111): additive CCD step bound per contact
+__global__ void k_accd(const float4* __restrict__ x, const float4* __restrict__ vel, const int4* __restrict__ cidx,
+                       const int2* __restrict__ ctype, SolverScalars* sc, float slackness, float thickness, int max_iters,
+                       float ee_thres) {
+    const int n = sc->n_contacts;
+    for (int b = gtid(); b < n; b += gstride()) {
+        const int4 id = cidx[b];
+        F3 x0 = f3(x[id.x]), x1 = f3(x[id.y]), x2 = f3(x[id.z]), x3 = f3(x[id.w]);
+        F3 v0 = f3(vel[id.x]), v1 = f3(vel[id.y]), v2 = f3(vel[id.z]), v3 = f3(vel[id.w]);
+        const int type1 = ctype[b].x;
+        const F3 va = (v0 + v1 + v2 + v3) / 4.0f;
+        v0 = v0 - va; v1 = v1 - va; v2 = v2 - va; v3 = v3 - va;
+        float lv;
+        if (type1 == BLOCK_PT) lv = length(v0) + fmaxf(length(v1), fmaxf(length(v2), length(v3)));
+        else lv = fmaxf(length(v0), length(v1)) + fmaxf(length(v2), length(v3));
+        if (lv < 1e-12f) continue;
+        auto dist = [&]() {
+            if (type1 == BLOCK_PT) return pt_pair_distance(x0, x1, x2, x3, pt_classify(x0, x1, x2, x3));
+            return ee_pair_distance(x0, x1, x2, x3, ee_classify(x0, x1, x2, x3, ee_thres));
+        };
+        float d = dist();
+        float dsq = d * d;
+        float dmt = fmaxf((dsq - thickness * thickness) / (sqrtf(dsq) + thickness), 0.f);
+        const float gap = (1.0f - slackness) * dmt;
+        float t = 0.f;
+        float tl = slackness * dmt / lv;
+        int it = 0;
+        while (true) {
+            x0 = x0 + tl * v0; x1 = x1 + tl * v1; x2 = x2 + tl * v2; x3 = x3 + tl * v3;
+            d = dist();
+            dsq = d * d;
+            dmt = fmaxf((dsq - thickness * thickness) / (sqrtf(dsq) + thickness), 0.f);
+            if ((it > 0 && dmt <= gap) || it >= max_iters) {
+                atomicMin((int*)&sc->ccd_step, __float_as_int(t));  // t >= 0: int order = float order
+                break;
+            }
+            t = t + tl;
+            if (t > 1.0f) break;
+            tl = 0.8f * dmt / lv;
+            ++it;
+        }
+    }
+}
+
+// line_search_kernel: q = q0 + ccd_step * 0.5^n * p unless an earlier step already lowered the energy
+__global__ void k_line_search(const float4* __restrict__ q0, const float4* __restrict__ p, const SolverScalars* sc, int n_halves,
+                              int np, float4* q) {
+    if (n_halves > 0 && sc->energy < sc->energy_prev) return;
+    const float a = sc->ccd_step * powf(0.5f, (float)n_halves);
+    for (int i = gtid(); i < np; i += gstride()) {
+        const float4 a0 = q0[i], pi = p[i];
+        q[i] = make_float4(a0.x + a * pi.x, a0.y + a * pi.y, a0.z + a * pi.z, 0.f);
+    }
+}
+
+__global__ void k_set_scalars(SolverScalars* sc, float ccd_step) { sc->ccd_step = ccd_step; }
+
+__global__ void k_copy_contact_count(SolverScalars* sc, int cap) {
+    const int n = sc->n_contacts_raw;
+    sc->n_contacts = n < cap ? n : cap;
+}
+
+}  // namespace
+
+// ================================================================== host driver
+Stage3::~Stage3() { release(); }
+
+template <typename T>
+int Stage3::grow(T*& p, size_t& cap, size_t n) {
+    if (p && cap >= n) return PAMO_OK;
+    if (p) {
+        cudaStreamSynchronize(stream);
+        cudaFree(p);
+        p = nullptr;
+    }
+    if (cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+    cap = n;
+    return PAMO_OK;
+}
+
+void Stage3::release() {
+    auto f = [](auto*& p) {
+        if (p) cudaFree(p);
+        p = nullptr;
+    };
+    f(gt_pos); f(gt_tri); f(gt_bvh_mem); f(gt_rc); f(q); f(q_rest); f(q_prev_newton); f(q_prev_det); f(p); f(target);
+    f(grad); f(hdiag); f(r); f(z); f(v); f(Av); f(vweight); f(tri); f(edge4); f(edge); f(el_area); f(el_invDm); f(hinge);
+    f(hinge_rest); f(hinge_blocks); f(c_idx); f(c_type); f(c_d); f(c_dd); f(e_elem); f(tri_bvh_mem); f(edge_bvh_mem);
+    f(tri_rc); f(edge_rc); f(sc); f(d_norm); f(scan_scratch);
+    if (h_sc) cudaFreeHost(h_sc);
+    h_sc = nullptr;
+}
+
+int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
+    int rr;
+    size_t c1;
+    if (!sc) {
+        if (cudaMalloc((void**)&sc, sizeof(SolverScalars)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+        if (cudaMallocHost((void**)&h_sc, sizeof(SolverScalars)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMallocHost");
+        if (cudaMalloc((void**)&d_norm, 16 * sizeof(double)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+        if (cudaMalloc((void**)&scan_scratch, (scan_scratch_ints() + 2 * kRedBlocks + 8) * sizeof(int)) != cudaSuccess)
+            return fail(PAMO_ERR_OOM, "cudaMalloc");
+        if (cudaMalloc((void**)&gt_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+        if (cudaMalloc((void**)&tri_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+        if (cudaMalloc((void**)&edge_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+    }
+    if (cap_gp < (size_t)ngp + 2) {
+        c1 = cap_gp;
+        if ((rr = grow(gt_pos, c1, (size_t)ngp + 2))) return rr;
+        cap_gp = c1;
+    }
+    if (cap_gt < (size_t)ngt + 2) {
+        c1 = cap_gt;
+        if ((rr = grow(gt_tri, c1, (size_t)ngt + 2))) return rr;
+        cap_gt = c1;
+    }
+    if (gt_bvh_cap < (size_t)ngt + 2) {
+        if (gt_bvh_mem) cudaFree(gt_bvh_mem);
+        if (cudaMalloc((void**)&gt_bvh_mem, bvh_bytes(ngt + 2)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+        bvh_carve(gt_bvh, ngt + 2, gt_bvh_mem);
+        gt_bvh_cap = (size_t)ngt + 2;
+    }
+    if (cap_v < (size_t)np + 2) {
+        const size_t n = (size_t)np + 2;
+        size_t c;
+        for (float4** b : {&q, &q_rest, &q_prev_newton, &q_prev_det, &p, &target, &grad, &hdiag, &r, &z, &v, &Av}) {
+            c = cap_v;
+            if ((rr = grow(*b, c, n))) return rr;
+        }
+        c = cap_v;
+        if ((rr = grow(vweight, c, n))) return rr;
+        cap_v = n;
+    }
+    if (cap_t < (size_t)nt + 2) {
+        const size_t n = (size_t)nt + 2;
+        size_t c = cap_t;
+        if ((rr = grow(tri, c, n))) return rr;
+        c = cap_t;
+        if ((rr = grow(el_area, c, n))) return rr;
+        c = cap_t;
+        if ((rr = grow(el_invDm, c, n))) return rr;
+        cap_t = n;
+        if (tri_bvh_mem) cudaFree(tri_bvh_mem);
+        if (cudaMalloc((void**)&tri_bvh_mem, bvh_bytes((int)n)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+        bvh_carve(tri_bvh, (int)n, tri_bvh_mem);
+        tri_bvh_cap = n;
+    }
+    if (cap_e < (size_t)ne + 2) {
+        const size_t n = (size_t)ne + 2;
+        size_t c = cap_e;
+        if ((rr = grow(edge, c, n))) return rr;
+        c = cap_e;
+        if ((rr = grow(edge4, c, n))) return rr;
+        cap_e = n;
+        if (edge_bvh_mem) cudaFree(edge_bvh_mem);
+        if (cudaMalloc((void**)&edge_bvh_mem, bvh_bytes((int)n)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+        bvh_carve(edge_bvh, (int)n, edge_bvh_mem);
+        edge_bvh_cap = n;
+    }
+    if (cap_h < (size_t)nh + 2) {
+        const size_t n = (size_t)nh + 2;
+        size_t c = cap_h;
+        if ((rr = grow(hinge, c, n))) return rr;
+        c = cap_h;
+        if ((rr = grow(hinge_rest, c, n))) return rr;
+        c = cap_h;
+        if ((rr = grow(hinge_blocks, c, n * 144))) return rr;
+        cap_h = n;
+    }
+    return PAMO_OK;
+}
+
+void Stage3::compute_energy(const float4* x) {
+    cudaStream_t s = stream;
+    const Stage3Params& P = params;
+    const float mu = P.elas_young_modulus / (2.f * (1.f + P.elas_poisson_ratio));
+    const float la = P.elas_young_modulus * P.elas_poisson_ratio / ((1.f + P.elas_poisson_ratio) * (1.f - 2.f * P.elas_poisson_ratio));
+    float* e = e_elem;
+    const int base_c = NP + NT + NH;
+    k_energy_m2gt<<<grid_for(NP, kT), kT, 0, s>>>(x, target, vweight, P.mesh2gt_dist_stiffness, NP, e);
+    note_launch();
+    k_energy_elastic<<<grid_for(NT, kT), kT, 0, s>>>(x, tri, el_area, el_invDm, mu, la, NT, e + NP);
+    note_launch();
+    k_energy_hinge<<<grid_for(NH, kT), kT, 0, s>>>(x, hinge, hinge_rest, P.hinge_stiffness, NH, e + NP + NT);
+    note_launch();
+    k_energy_contact<<<grid_for(std::max(1, h_sc->n_contacts), kT), kT, 0, s>>>(x, c_idx, c_type, c_d, sc, P.coll_stiffness,
+                                                                               P.d_hat, P.ee_classify_thres, e + base_c);
+    note_launch();
+    float2* part = (float2*)(scan_scratch + scan_scratch_ints());
+    k_reduce<<<kRedBlocks, kT, 0, s>>>(e, &sc->n_contacts, base_c, part);
+    note_launch();
+    k_reduce_finish<<<1, kT, 0, s>>>(part, &sc->energy, nullptr);
+    note_launch();
+}
+
+void Stage3::compute_diff() {
+    cudaStream_t s = stream;
+    const Stage3Params& P = params;
+    const float mu = P.elas_young_modulus / (2.f * (1.f + P.elas_poisson_ratio));
+    const float la = P.elas_young_modulus * P.elas_poisson_ratio / ((1.f + P.elas_poisson_ratio) * (1.f - 2.f * P.elas_poisson_ratio));
+    cudaMemsetAsync(grad, 0, NP * sizeof(float4), s);
+    cudaMemsetAsync(hdiag, 0, NP * sizeof(float4), s);
+    k_diff_m2gt<<<grid_for(NP, kT), kT, 0, s>>>(q, target, vweight, P.mesh2gt_dist_stiffness, -1.f, NP, grad, hdiag);
+    note_launch();
+    k_diff_elastic<<<grid_for(NT, kT), kT, 0, s>>>(q, tri, el_area, el_invDm, mu, la, -1.f, NT, grad);
+    note_launch();
+    k_diff_hinge<<<grid_for(NH, 128), 128, 0, s>>>(q, hinge, hinge_rest, P.hinge_stiffness, -1.f, NH, hinge_blocks, grad, hdiag);
+    note_launch();
+    k_spd_project<<<grid_for(NH, 64), 64, 0, s>>>(hinge_blocks, NH, P.spd_max_iters);
+    note_launch();
+    k_diff_contact<<<grid_for(std::max(1, h_sc->n_contacts), kT), kT, 0, s>>>(q, c_idx, c_type, c_d, sc, P.coll_stiffness,
+                                                                             P.d_hat, -1.f, c_dd, grad, hdiag);
+    note_launch();
+}
+
+void Stage3::hess_dx(const float4* dx, float4* out) {
+    cudaStream_t s = stream;
+    const Stage3Params& P = params;
+    const float mu = P.elas_young_modulus / (2.f * (1.f + P.elas_poisson_ratio));
+    const float la = P.elas_young_modulus * P.elas_poisson_ratio / ((1.f + P.elas_poisson_ratio) * (1.f - 2.f * P.elas_poisson_ratio));
+    cudaMemsetAsync(out, 0, NP * sizeof(float4), s);
+    const long long total = (long long)NP + NT + NH + std::max(1, h_sc->n_contacts);
+    k_hvp<<<grid_for(total, kT), kT, 0, s>>>(q, dx, vweight, P.mesh2gt_dist_stiffness, NP, tri, el_area, el_invDm, mu, la, NT,
+                                             hinge, hinge_blocks, NH, c_idx, c_d, c_dd, sc, P.coll_stiffness, P.d_hat, out);
+    note_launch();
+}
+
+void Stage3::cg_solve() {
+    cudaStream_t s = stream;
+    float2* part = (float2*)(scan_scratch + scan_scratch_ints());
+    k_cg_init<<<grid_for(NP, kT), kT, 0, s>>>(grad, hdiag, NP, p, r, z, v);
+    note_launch();
+    k_reduce_dot<<<kRedBlocks, kT, 0, s>>>(z, r, NP, part);
+    note_launch();
+    k_reduce_finish<<<1, kT, 0, s>>>(part, &sc->z_r, nullptr);
+    note_launch();
+    for (int it = 0; it < params.n_cg_iters; ++it) {
+        hess_dx(v, Av);
+        k_reduce_dot<<<kRedBlocks, kT, 0, s>>>(v, Av, NP, part);
+        note_launch();
+        k_reduce_finish<<<1, kT, 0, s>>>(part, &sc->v_A_v, nullptr);
+        note_launch();
+        k_cg_prz<<<grid_for(NP, kT), kT, 0, s>>>(v, Av, hdiag, sc, NP, p, r, z);
+        note_launch();
+        k_reduce_dot<<<kRedBlocks, kT, 0, s>>>(z, r, NP, part);
+        note_launch();
+        k_reduce_finish<<<1, kT, 0, s>>>(part, &sc->z_r, &sc->z_r_last);  // z_r_last = old z_r
+        note_launch();
+        k_cg_v<<<grid_for(NP, kT), kT, 0, s>>>(z, sc, NP, v);
+        note_launch();
+    }
+}
+
+int Stage3::detect_contacts(float radius) {
+    cudaStream_t s = stream;
+    const float thr = 2.0f * radius + params.d_hat;
+    // LBVHs of the current triangles and edges (boxes without margin; the query box carries the threshold)
+    RoundCounters h{};
+    h.n_pts = NP;
+    h.n_tris = NT;
+    cudaMemcpyAsync(tri_rc, &h, sizeof(h), cudaMemcpyHostToDevice, s);
+    h.n_tris = NE;
+    cudaMemcpyAsync(edge_rc, &h, sizeof(h), cudaMemcpyHostToDevice, s);
+    bvh_build(tri_bvh, tri, q, tri_rc, NT, s);
+    bvh_build(edge_bvh, edge4, q, edge_rc, NE, s);
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        const int cap = (int)std::min<size_t>(cap_c, (size_t)params.max_blocks);
+        cudaMemsetAsync(&sc->n_contacts_raw, 0, sizeof(int), s);
+        k_detect<false><<<grid_for(NP, kQT, 16), kQT, 0, s>>>(q, NP, tri, tri_bvh.child, tri_bvh.nlo, tri_bvh.nhi, tri_bvh.llo,
+                                                             tri_bvh.lhi, tri_bvh.vals[0], tri_rc, thr,
+                                                             params.ee_classify_thres, c_idx, c_type, cap, sc);
+        note_launch();
+        k_detect<true><<<grid_for(NE, kQT, 16), kQT, 0, s>>>(q, NE, edge4, edge_bvh.child, edge_bvh.nlo, edge_bvh.nhi,
+                                                            edge_bvh.llo, edge_bvh.lhi, edge_bvh.vals[0], edge_rc, thr,
+                                                            params.ee_classify_thres, c_idx, c_type, cap, sc);
+        note_launch();
+        k_copy_contact_count<<<1, 1, 0, s>>>(sc, cap);
+        note_launch();
+        cudaMemcpyAsync(h_sc, sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+        const long long raw = h_sc->n_contacts_raw;
+        if (raw > params.max_blocks) return -1;  // caller halves the radius (energy.py:942-948)
+        if (raw <= (long long)cap_c) break;
+        // grow the contact arrays and detect again (capacity only; the reference's limit is max_blocks)
+        const size_t n = (size_t)raw + raw / 2 + 1024;
+        size_t c = cap_c;
+        int rr;
+        if ((rr = grow(c_idx, c, n))) return rr;
+        c = cap_c;
+        if ((rr = grow(c_type, c, n))) return rr;
+        c = cap_c;
+        if ((rr = grow(c_d, c, n))) return rr;
+        c = cap_c;
+        if ((rr = grow(c_dd, c, 4 * n))) return rr;
+        cap_c = n;
+        c = cap_el;
+        if ((rr = grow(e_elem, c, (size_t)NP + NT + NH + n + 8))) return rr;
+        cap_el = c;
+    }
+    stats.max_contacts = std::max(stats.max_contacts, h_sc->n_contacts);
+    stats.total_contacts += h_sc->n_contacts;
+    return PAMO_OK;
+}
+
+int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, int n_gt_tris, const double* points,
+                const int* tris, int n_points, int n_tris, int n_iters, double* out_points, cudaStream_t s) {
+    stream = s;
+    err.clear();
+    stats = Stage3Stats{};
+    if (n_points < 3 || n_tris < 1 || n_gt_points < 3 || n_gt_tris < 1) return fail(PAMO_ERR_INVALID_ARG, "empty mesh");
+    // Topology on the host, once per call.
+    // Edges: trimesh's edges_unique (the face edges with sorted endpoints, unique rows). For two int32
+    // columns trimesh hashes a row (u, v) as u ^ (v << 32) and np.unique sorts the hashes, so the edges come
+    // ordered by (v, u); the same order is used here (it fixes which edge of an edge-edge pair is "first").
+    // Hinges: hinge_preprocess_slow_kernel (hinge_energy.py:21-57) pairs every directed edge (a, b), a < b,
+    // of a face t0 with every face t1 holding the edge as (b, a): hinge (opposite in t0, a, b, opposite in t1).
+    std::vector<int> hf((size_t)3 * n_tris);
+    if (cudaMemcpy(hf.data(), tris, hf.size() * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(PAMO_ERR_CUDA, "copy of the triangles");
+    std::vector<long long> ukeys;
+    std::vector<std::pair<long long, int>> dkeys;  // directed edge (a * n + b) -> face * 3 + corner
+    ukeys.reserve(hf.size());
+    dkeys.reserve(hf.size());
+    for (int f = 0; f < n_tris; ++f)
+        for (int k = 0; k < 3; ++k) {
+            const long long a = hf[3 * f + k], b = hf[3 * f + (k + 1) % 3];
+            if (a < 0 || b < 0 || a >= n_points || b >= n_points) return fail(PAMO_ERR_INVALID_ARG, "bad triangle index");
+            ukeys.push_back(std::max(a, b) * n_points + std::min(a, b));
+            dkeys.push_back({a * n_points + b, 3 * f + k});
+        }
+    std::sort(ukeys.begin(), ukeys.end());
+    ukeys.erase(std::unique(ukeys.begin(), ukeys.end()), ukeys.end());
+    std::sort(dkeys.begin(), dkeys.end());
+    std::vector<int> h_hinges;
+    for (int f = 0; f < n_tris; ++f)
+        for (int k = 0; k < 3; ++k) {
+            const int a = hf[3 * f + k], b = hf[3 * f + (k + 1) % 3], c = hf[3 * f + (k + 2) % 3];
+            if (!(a < b)) continue;
+            const long long key = (long long)b * n_points + a;
+            auto it = std::lower_bound(dkeys.begin(), dkeys.end(), std::make_pair(key, -1));
+            for (; it != dkeys.end() && it->first == key; ++it) {
+                const int f1 = it->second / 3, k1 = it->second % 3;
+                h_hinges.push_back(c);
+                h_hinges.push_back(a);
+                h_hinges.push_back(b);
+                h_hinges.push_back(hf[3 * f1 + (k1 + 2) % 3]);
+            }
+        }
+    NP = n_points;
+    NT = n_tris;
+    NE = (int)ukeys.size();
+    NH = (int)(h_hinges.size() / 4);
+    NGP = n_gt_points;
+    NGT = n_gt_tris;
+    stats.n_particles = NP;
+    stats.n_triangles = NT;
+    stats.n_edges = NE;
+    stats.n_hinges = NH;
+    int rr;
+    if ((rr = ensure(NP, NT, NE, NH, NGP, NGT))) return rr;
+    if (cap_c == 0) {
+        const size_t n = std::max<size_t>(1 << 16, (size_t)32 * (NP + NE));
+        size_t c = 0;
+        if ((rr = grow(c_idx, c, n))) return rr;
+        c = 0;
+        if ((rr = grow(c_type, c, n))) return rr;
+        c = 0;
+        if ((rr = grow(c_d, c, n))) return rr;
+        c = 0;
+        if ((rr = grow(c_dd, c, 4 * n))) return rr;
+        cap_c = n;
+    }
+    {
+        size_t c = cap_el;
+        if ((rr = grow(e_elem, c, (size_t)NP + NT + NH + cap_c + 8))) return rr;
+        cap_el = c;
+    }
+    std::vector<int4> e4(NE);
+    std::vector<int2> e2(NE);
+    for (int e = 0; e < NE; ++e) {
+        const int u = (int)(ukeys[e] % n_points), v = (int)(ukeys[e] / n_points);
+        e4[e] = make_int4(u, v, v, 0);
+        e2[e] = make_int2(u, v);
+    }
+    std::vector<int4> h4(NH);
+    for (int h = 0; h < NH; ++h) h4[h] = make_int4(h_hinges[4 * h], h_hinges[4 * h + 1], h_hinges[4 * h + 2], h_hinges[4 * h + 3]);
+    cudaMemcpyAsync(edge4, e4.data(), NE * sizeof(int4), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(edge, e2.data(), NE * sizeof(int2), cudaMemcpyHostToDevice, s);
+    if (NH) cudaMemcpyAsync(hinge, h4.data(), NH * sizeof(int4), cudaMemcpyHostToDevice, s);
+
+    // normalisation (processing.py:15-21, 57-59)
+    k_norm_stats<<<1, kT, 0, s>>>(gt_points, NGP, d_norm);
+    note_launch();
+    k_normalize<<<grid_for(NGP, kT), kT, 0, s>>>(gt_points, NGP, d_norm, gt_pos, nullptr);
+    note_launch();
+    cudaMemsetAsync(sc, 0, sizeof(SolverScalars), s);
+    k_tris4<<<grid_for(NGT, kT), kT, 0, s>>>(gt_tris, NGT, NGP, gt_tri, &sc->status);
+    note_launch();
+    k_normalize<<<grid_for(NP, kT), kT, 0, s>>>(points, NP, d_norm, q, q_rest);
+    note_launch();
+    k_tris4<<<grid_for(NT, kT), kT, 0, s>>>(tris, NT, NP, tri, &sc->status);
+    note_launch();
+    cudaMemcpyAsync(h_sc, sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    if (h_sc->status & 1) return fail(PAMO_ERR_INVALID_ARG, "GT triangle index out of range");
+    // GT LBVH (built once: the GT mesh does not move)
+    {
+        RoundCounters h{};
+        h.n_pts = NGP;
+        h.n_tris = NGT;
+        cudaMemcpyAsync(gt_rc, &h, sizeof(h), cudaMemcpyHostToDevice, s);
+        bvh_build(gt_bvh, gt_tri, gt_pos, gt_rc, NGT, s);
+    }
+    // register_mesh preprocessing (system.py:167-272): Voronoi areas, elastic rest shape, hinge rest state,
+    // minimum internal angle
+    double* w64 = reinterpret_cast<double*>(r);  // scratch: r is free until the first solve
+    cudaMemsetAsync(w64, 0, NP * sizeof(double), s);
+    k_voronoi<<<grid_for(NT, kT), kT, 0, s>>>(points, d_norm, tri, NT, w64);
+    note_launch();
+    k_weights_f32<<<grid_for(NP, kT), kT, 0, s>>>(w64, NP, vweight);
+    note_launch();
+    k_elastic_pre<<<grid_for(NT, kT), kT, 0, s>>>(q_rest, tri, NT, el_area, el_invDm);
+    note_launch();
+    if (NH) {
+        k_hinge_pre<<<grid_for(NH, kT), kT, 0, s>>>(q_rest, hinge, NH, hinge_rest);
+        note_launch();
+    }
+    k_min_angle<<<grid_for(NT, kT), kT, 0, s>>>(points, d_norm, tri, NT, (double)params.min_angle_thres, &sc->accepted);
+    note_launch();
+    cudaMemcpyAsync(h_sc, sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    stats.do_nothing = (h_sc->accepted == 1);  // some angle <= threshold and none NaN (system.py:214-221)
+    cudaMemsetAsync(&sc->accepted, 0, sizeof(int), s);
+
+    float radius = params.contact_detection_radius;
+    if (!stats.do_nothing) {
+        for (int step = 0; step < n_iters; ++step) {
+            ++stats.steps;
+            // _update_vertex_target: closest points on the GT surface
+            k_closest_gt<<<grid_for(NP, kQT, 16), kQT, 0, s>>>(q, NP, gt_bvh.child, gt_bvh.nlo, gt_bvh.nhi, gt_bvh.llo,
+                                                              gt_bvh.lhi, gt_bvh.vals[0], gt_tri, gt_pos, gt_rc, target,
+                                                              &sc->status);
+            note_launch();
+            for (int it = 0; it < params.n_newton_iters; ++it) {
+                ++stats.newton_iters;
+                cudaMemcpyAsync(q_prev_newton, q, NP * sizeof(float4), cudaMemcpyDeviceToDevice, s);
+                int d;
+                while ((d = detect_contacts(radius)) == -1) {
+                    radius *= 0.5f;  // too many contacts: halve the detection radius and retry
+                    if (++stats.radius_halvings > 40) return fail(PAMO_ERR_CAPACITY, "contacts exceed max_blocks");
+                }
+                if (d) return d;
+                cudaMemcpyAsync(q_prev_det, q, NP * sizeof(float4), cudaMemcpyDeviceToDevice, s);
+                compute_energy(q);
+                compute_diff();
+                cg_solve();
+                k_clamp_p<<<grid_for(NP, kT), kT, 0, s>>>(p, q_prev_newton, q_prev_det, params.contact_detection_radius,
+                                                          NP);
+                note_launch();
+                k_set_scalars<<<1, 1, 0, s>>>(sc, 1.0f);
+                note_launch();
+                k_accd<<<grid_for(std::max(1, h_sc->n_contacts), kT), kT, 0, s>>>(q, p, c_idx, c_type, sc, params.ccd_slackness,
+                                                                                 params.ccd_thickness, params.ccd_max_iters,
+                                                                                 params.ee_classify_thres);
+                note_launch();
+                // line search (system.py:394-409)
+                cudaMemcpyAsync(&sc->energy_prev, &sc->energy, sizeof(float), cudaMemcpyDeviceToDevice, s);
+                for (int n = 0; n < params.n_line_search_iters; ++n) {
+                    k_line_search<<<grid_for(NP, kT), kT, 0, s>>>(q_prev_newton, p, sc, n, NP, q);
+                    note_launch();
+                    compute_energy(q);
+                }
+            }
+        }
+    }
+    k_denormalize<<<grid_for(NP, kT), kT, 0, s>>>(q, NP, d_norm, out_points);
+    note_launch();
+    cudaMemcpyAsync(h_sc, sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    if (h_sc->status & 6) return fail(PAMO_ERR_ITER_LIMIT, "BVH traversal limit in stage 3");
+    stats.last_energy = h_sc->energy;
+    return PAMO_OK;
+}
+
+}  // namespace pamo
+
+// ================================================================== C ABI
+struct pamo_stage3 {
+    int device = 0;
+    pamo::Stage3 solver;
+};
+
+extern "C" {
+
+int pamo_stage3_create(pamo_stage3** out, int device) {
+    if (!out) return PAMO_ERR_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return PAMO_ERR_INVALID_ARG;
+    pamo_stage3* s = new pamo_stage3();
+    s->device = device;
+    *out = s;
+    return PAMO_OK;
+}
+
+int pamo_stage3_destroy(pamo_stage3* s) {
+    if (!s) return PAMO_ERR_INVALID_ARG;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(s->device);
+    delete s;
+    cudaSetDevice(prev);
+    return PAMO_OK;
+}
+
+const char* pamo_stage3_last_error(const pamo_stage3* s) { return s ? s->solver.err.c_str() : "null handle"; }
+
+int pamo_stage3_set_param(pamo_stage3* s, const char* name, double value) {
+    if (!s || !name) return PAMO_ERR_INVALID_ARG;
+    pamo::Stage3Params& P = s->solver.params;
+    const std::string n(name);
+    if (n == "n_newton_iters") P.n_newton_iters = (int)value;
+    else if (n == "n_cg_iters") P.n_cg_iters = (int)value;
+    else if (n == "n_line_search_iters") P.n_line_search_iters = (int)value;
+    else if (n == "d_hat") P.d_hat = (float)value;
+    else if (n == "coll_stiffness") P.coll_stiffness = (float)value;
+    else if (n == "contact_detection_radius") P.contact_detection_radius = (float)value;
+    else if (n == "ee_classify_thres") P.ee_classify_thres = (float)value;
+    else if (n == "ccd_slackness") P.ccd_slackness = (float)value;
+    else if (n == "ccd_thickness") P.ccd_thickness = (float)value;
+    else if (n == "ccd_max_iters") P.ccd_max_iters = (int)value;
+    else if (n == "spd_max_iters") P.spd_max_iters = (int)value;
+    else if (n == "elas_young_modulus") P.elas_young_modulus = (float)value;
+    else if (n == "elas_poisson_ratio") P.elas_poisson_ratio = (float)value;
+    else if (n == "hinge_stiffness") P.hinge_stiffness = (float)value;
+    else if (n == "mesh2gt_dist_stiffness") P.mesh2gt_dist_stiffness = (float)value;
+    else if (n == "min_angle_thres") P.min_angle_thres = (float)value;
+    else if (n == "max_blocks") P.max_blocks = (long long)value;
+    else {
+        s->solver.err = "unknown stage-3 parameter: " + n;
+        return PAMO_ERR_INVALID_ARG;
+    }
+    return PAMO_OK;
+}
+
+int pamo_safe_project(pamo_stage3* s, const double* gt_points, const int32_t* gt_triangles, int32_t n_gt_points,
+                      int32_t n_gt_triangles, const double* points, const int32_t* triangles, int32_t n_points,
+                      int32_t n_triangles, int32_t n_iters, double* out_points, pamo_stream stream) {
+    if (!s) return PAMO_ERR_INVALID_ARG;
+    if (!gt_points || !gt_triangles || !points || !triangles || !out_points || n_iters < 0) {
+        s->solver.err = "null pointer or negative n_iters";
+        return PAMO_ERR_INVALID_ARG;
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(s->device);
+    const int r = s->solver.run(gt_points, gt_triangles, n_gt_points, n_gt_triangles, points, triangles, n_points,
+                                n_triangles, n_iters, out_points, (cudaStream_t)stream);
+    cudaSetDevice(prev);
+    return r;
+}
+
+int pamo_stage3_stats(const pamo_stage3* s, double* out, int32_t n) {
+    if (!s || !out) return PAMO_ERR_INVALID_ARG;
+    const pamo::Stage3Stats& t = s->solver.stats;
+    const double v[11] = {(double)t.n_particles, (double)t.n_triangles, (double)t.n_edges, (double)t.n_hinges,
+                          (double)t.steps, (double)t.newton_iters, (double)t.max_contacts, (double)t.radius_halvings,
+                          (double)t.do_nothing, t.last_energy, (double)t.total_contacts};
+    for (int i = 0; i < n && i < 11; ++i) out[i] = v[i];
+    return 11;
+}
+
+}  // extern "C"

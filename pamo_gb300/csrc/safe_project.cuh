@@ -1,0 +1,123 @@
+// Stage 3 of PaMO: safe projection of the simplified mesh back onto the source ("GT") mesh — a Newton
+// solver over distance-to-GT, StVK membrane, hinge bending and an IPC log-barrier between nearby
+// point-triangle and edge-edge pairs, with Jacobi-preconditioned CG, a per-vertex step clamp, additive CCD
+// and a backtracking line search (simp_cuda/safe_project/src/pamo_safe_project/system.py:411-470).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+
+#include "lbvh.cuh"
+#include "pamo_common.cuh"
+
+namespace pamo {
+
+// Stage3Config defaults (pamo_safe_project/config.py:6-73)
+struct Stage3Params {
+    int n_newton_iters = 10;
+    int n_cg_iters = 40;
+    int n_line_search_iters = 10;
+    float d_hat = 1e-3f;
+    float coll_stiffness = 1e2f;
+    float contact_detection_radius = 1e-2f;
+    float ee_classify_thres = 1e-3f;
+    float ccd_slackness = 0.7f;
+    float ccd_thickness = 1e-6f;
+    int ccd_max_iters = 100;
+    int spd_max_iters = 3;
+    float elas_young_modulus = 0.1f;
+    float elas_poisson_ratio = 0.0f;
+    float hinge_stiffness = 1e-2f;
+    float mesh2gt_dist_stiffness = 1e3f;
+    float min_angle_thres = 0.0f;  // degrees
+    long long max_blocks = 1ll << 25;
+};
+
+// Device scalars of the solver (one struct so that graph nodes can read them by pointer).
+struct SolverScalars {
+    float energy, energy_prev, v_A_v, z_r, z_r_last, ccd_step;
+    int n_contacts, n_contacts_raw, accepted, status;
+    double energy_acc[2];  // compensated accumulator (sum, correction) while reducing
+    float pad[4];
+};
+
+struct Stage3Stats {
+    int n_particles = 0, n_triangles = 0, n_edges = 0, n_hinges = 0;
+    int steps = 0, newton_iters = 0, max_contacts = 0, radius_halvings = 0;
+    int do_nothing = 0;
+    double last_energy = 0.0;
+    long long total_contacts = 0;  // summed over Newton iterations
+};
+
+class Stage3 {
+public:
+    Stage3() = default;
+    ~Stage3();
+    // Runs process(gt_V, gt_F, V, F, n_iters) on device buffers; out_points receives float64 positions in
+    // the input frame. Returns a pamo_status code; err holds the message.
+    int run(const double* gt_points, const int* gt_tris, int n_gt_points, int n_gt_tris, const double* points,
+            const int* tris, int n_points, int n_tris, int n_iters, double* out_points, cudaStream_t s);
+    Stage3Params params;
+    Stage3Stats stats;
+    std::string err;
+
+private:
+    template <typename T>
+    int grow(T*& p, size_t& cap, size_t n);
+    int fail(int code, const std::string& m) {
+        err = m;
+        return code;
+    }
+    int ensure(int np, int nt, int ne, int nh, int ngp, int ngt);
+    void release();
+
+    // problem sizes
+    int NP = 0, NT = 0, NE = 0, NH = 0, NGP = 0, NGT = 0;
+    // capacities
+    size_t cap_v = 0, cap_t = 0, cap_e = 0, cap_h = 0, cap_gp = 0, cap_gt = 0, cap_c = 0, cap_el = 0;
+    // GT mesh and its LBVH
+    float4* gt_pos = nullptr;
+    int4* gt_tri = nullptr;
+    BvhBuffers gt_bvh{};
+    char* gt_bvh_mem = nullptr;
+    size_t gt_bvh_cap = 0;
+    RoundCounters* gt_rc = nullptr;
+    // simulated mesh
+    float4 *q = nullptr, *q_rest = nullptr, *q_prev_newton = nullptr, *q_prev_det = nullptr, *p = nullptr;
+    float4 *target = nullptr, *grad = nullptr, *hdiag = nullptr, *r = nullptr, *z = nullptr, *v = nullptr, *Av = nullptr;
+    float* vweight = nullptr;  // Voronoi area
+    int4* tri = nullptr;
+    int4* edge4 = nullptr;     // edges as (u, v, v, 0) for the edge LBVH
+    int2* edge = nullptr;
+    float* el_area = nullptr;
+    float4* el_invDm = nullptr;
+    int4* hinge = nullptr;
+    float2* hinge_rest = nullptr;  // (rest angle, rest edge length)
+    float* hinge_blocks = nullptr; // 16 mat33 per hinge
+    // contacts
+    int4* c_idx = nullptr;
+    int2* c_type = nullptr;
+    float* c_d = nullptr;
+    float4* c_dd = nullptr;    // 4 per contact
+    // per-element energies for the deterministic reduction
+    float* e_elem = nullptr;
+    // LBVHs over the current triangles and edges
+    BvhBuffers tri_bvh{}, edge_bvh{};
+    char *tri_bvh_mem = nullptr, *edge_bvh_mem = nullptr;
+    size_t tri_bvh_cap = 0, edge_bvh_cap = 0;
+    RoundCounters *tri_rc = nullptr, *edge_rc = nullptr;
+    SolverScalars* sc = nullptr;
+    SolverScalars* h_sc = nullptr;
+    double* d_norm = nullptr;  // [0..2] centre, [3] scale, [4..] scratch
+    int* scan_scratch = nullptr;
+    cudaStream_t stream = nullptr;
+
+    int detect_contacts(float radius);
+    void compute_energy(const float4* x);
+    void compute_diff();
+    void cg_solve();
+    void hess_dx(const float4* dx, float4* out);
+};
+
+}  // namespace pamo
