@@ -1,4 +1,5 @@
-"""Builds the CPU oracle (oracle/pamo_oracle.cpp) into oracle/build/libpamo_oracle.so.
+"""Builds the CPU oracle (oracle/pamo_oracle.cpp: stage 2, oracle/stage3_oracle.cpp: stage 3) into
+oracle/build/libpamo_oracle.so.
 
 Test infrastructure: the oracle is the checker of the CUDA path, loaded only by tests/, the smoke check of
 __graft_entry__ and the CPU-baseline leg of bench.py. -ffp-contract=off keeps every float product and sum
@@ -9,15 +10,15 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = os.path.join(HERE, "pamo_oracle.cpp")
+SRCS = [os.path.join(HERE, "pamo_oracle.cpp"), os.path.join(HERE, "stage3_oracle.cpp")]
 OUT = os.path.join(HERE, "build", "libpamo_oracle.so")
 
 
 def build(force: bool = False) -> str:
     os.makedirs(os.path.dirname(OUT), exist_ok=True)
-    if force or not os.path.exists(OUT) or os.path.getmtime(SRC) > os.path.getmtime(OUT):
+    if force or not os.path.exists(OUT) or any(os.path.getmtime(s) > os.path.getmtime(OUT) for s in SRCS):
         cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
-               "-o", OUT, SRC]
+               "-o", OUT, *SRCS]
         subprocess.run(cmd, check=True)
     return OUT
 

@@ -36,6 +36,9 @@ def lib():
         L.oracle_run_result.argtypes = [P, P, P, P]
         L.oracle_self_intersect.argtypes = [P, P, P, I, I, P]
         L.oracle_self_intersect.restype = LL
+        L.s3_oracle_run.argtypes = [P, P, I, I, P, P, I, I, I, P, P, P]
+        L.s3_oracle_probe.argtypes = [P, P, I, I, P, P, I, I, P, P, P, P, P, P, P, P, P]
+        L.s3_oracle_energy_at.argtypes = [P, P, I, I, P, P, I, I, P, P, P, P]
         _LIB = L
     return _LIB
 
@@ -143,3 +146,72 @@ class Oracle:
         fpr = np.zeros(max(rounds, 1), np.int32)
         lib().oracle_run_result(self._h, _p(V), _p(F), _p(fpr))
         return V, F, fpr[:rounds]
+
+
+# ------------------------------------------------------------------------------------------ stage 3
+STAGE3_PARAMS = ["n_newton_iters", "n_cg_iters", "n_line_search_iters", "d_hat", "coll_stiffness",
+                 "contact_detection_radius", "ee_classify_thres", "ccd_slackness", "ccd_thickness", "ccd_max_iters",
+                 "spd_max_iters", "elas_young_modulus", "elas_poisson_ratio", "hinge_stiffness",
+                 "mesh2gt_dist_stiffness", "min_angle_thres", "max_blocks"]
+STAGE3_DEFAULTS = dict(n_newton_iters=10, n_cg_iters=40, n_line_search_iters=10, d_hat=1e-3, coll_stiffness=1e2,
+                       contact_detection_radius=1e-2, ee_classify_thres=1e-3, ccd_slackness=0.7, ccd_thickness=1e-6,
+                       ccd_max_iters=100, spd_max_iters=3, elas_young_modulus=0.1, elas_poisson_ratio=0.0,
+                       hinge_stiffness=1e-2, mesh2gt_dist_stiffness=1e3, min_angle_thres=0.0, max_blocks=1 << 25)
+STAGE3_STATS = ["particles", "triangles", "edges", "hinges", "steps", "newton_iters", "max_contacts",
+                "radius_halvings", "do_nothing", "energy", "total_contacts"]
+
+
+def _s3_args(gt_V, gt_F, V, F, params):
+    P = dict(STAGE3_DEFAULTS)
+    P.update(params or {})
+    prm = np.array([float(P[k]) for k in STAGE3_PARAMS], np.float64)
+    gv = np.ascontiguousarray(gt_V, np.float64)
+    gf = np.ascontiguousarray(gt_F, np.int32)
+    v = np.ascontiguousarray(V, np.float64)
+    f = np.ascontiguousarray(F, np.int32)
+    return gv, gf, v, f, prm
+
+
+def stage3_run(gt_V, gt_F, V, F, n_iters: int, params: dict | None = None):
+    """Float64 restatement of process(gt_V, gt_F, V, F, n_iters): returns (V_out float64, stats dict)."""
+    gv, gf, v, f, prm = _s3_args(gt_V, gt_F, V, F, params)
+    out = np.zeros_like(v)
+    st = np.zeros(len(STAGE3_STATS), np.float64)
+    rc = lib().s3_oracle_run(_p(gv), _p(gf), len(gv), len(gf), _p(v), _p(f), len(v), len(f), int(n_iters), _p(prm),
+                             _p(out), _p(st))
+    if rc:
+        raise RuntimeError(f"stage-3 oracle failed with status {rc}")
+    return out, dict(zip(STAGE3_STATS, st.tolist()))
+
+
+def _opt(x):
+    return (None, None) if x is None else (np.ascontiguousarray(x, np.float64),) * 2
+
+
+def stage3_probe(gt_V, gt_F, V, F, dx, params: dict | None = None, x0=None):
+    """Energy, dE/dq, Hessian diagonal and H dx at x0 (normalised frame; None: the registered mesh)."""
+    gv, gf, v, f, prm = _s3_args(gt_V, gt_F, V, F, params)
+    x0a, _ = _opt(x0)
+    dxa = np.ascontiguousarray(dx, np.float64)
+    qn, g, h, hv = (np.zeros_like(v) for _ in range(4))
+    e = np.zeros(1, np.float64)
+    nc = ctypes.c_int(0)
+    rc = lib().s3_oracle_probe(_p(gv), _p(gf), len(gv), len(gf), _p(v), _p(f), len(v), len(f), _p(prm),
+                               None if x0a is None else _p(x0a), _p(dxa),
+                               _p(qn), _p(e), _p(g), _p(h), _p(hv), ctypes.byref(nc))
+    if rc:
+        raise RuntimeError(f"stage-3 oracle probe failed with status {rc}")
+    return dict(q=qn, energy=float(e[0]), grad=g, hdiag=h, hvp=hv, n_contacts=nc.value)
+
+
+def stage3_energy_at(gt_V, gt_F, V, F, x, params: dict | None = None, x0=None) -> float:
+    """Energy at x (normalised frame) with the targets and contacts of stage3_probe at x0."""
+    gv, gf, v, f, prm = _s3_args(gt_V, gt_F, V, F, params)
+    x0a, _ = _opt(x0)
+    xa = np.ascontiguousarray(x, np.float64)
+    e = np.zeros(1, np.float64)
+    rc = lib().s3_oracle_energy_at(_p(gv), _p(gf), len(gv), len(gf), _p(v), _p(f), len(v), len(f), _p(prm),
+                                   None if x0a is None else _p(x0a), _p(xa), _p(e))
+    if rc:
+        raise RuntimeError(f"stage-3 oracle energy failed with status {rc}")
+    return float(e[0])

@@ -541,9 +541,11 @@ __global__ void k_elastic_pre(const float4* __restrict__ xr, const int4* __restr
         F3 b2 = x02 - dot(x02, b1) * b1;
         b2 = normalize(b2);
         const float a = dot(b1, x01), b = dot(b1, x02), c = dot(b2, x01), d = dot(b2, x02);
-        const float det = a * d - b * c;
+        // wp.inverse of a 2x2: adjugate times 1/det, the zero matrix when det == 0
+        const float det = a * d - c * b;
+        const float id = det != 0.f ? 1.0f / det : 0.f;
         area[f] = W;
-        invDm[f] = make_float4(d / det, -b / det, -c / det, a / det);
+        invDm[f] = make_float4(d * id, -b * id, -c * id, a * id);
     }
 }
 
@@ -891,7 +893,7 @@ __global__ void k_diff_elastic(const float4* __restrict__ x, const int4* __restr
         const Mat2 E = mscale(0.5f, madd(mmul(mtr(L.F), L.F), mscale(-1.f, I)));
         const float trE = mtrace(E);
         const Mat2 P = mmul(L.F, madd(mscale(2.f * mu, E), mscale(la * trE, I)));
-        const Mat2 H = mscale(coeff * L.W, mmul(P, mtr(L.invDm)));
+        const Mat2 H = mmul(mscale(coeff * L.W, P), mtr(L.invDm));  // ((coeff W) P) invDm^T
         const F3 f1 = H.a * L.b1 + H.c * L.b2;
         const F3 f2 = H.b * L.b1 + H.d * L.b2;
         atomic_add3(grad, t.x, -f1 - f2);
@@ -1126,7 +1128,7 @@ __global__ void k_hvp(const float4* __restrict__ x, const float4* __restrict__ d
             const float trdE = mtrace(dE);
             const Mat2 dP = madd(mmul(dF, madd(mscale(2.f * mu, E), mscale(la * trE, I))),
                                  mmul(L.F, madd(mscale(2.f * mu, dE), mscale(la * trdE, I))));
-            const Mat2 dH = mscale(L.W, mmul(dP, mtr(L.invDm)));
+            const Mat2 dH = mmul(mscale(L.W, dP), mtr(L.invDm));
             const F3 df1 = dH.a * L.b1 + dH.c * L.b2;
             const F3 df2 = dH.b * L.b1 + dH.d * L.b2;
             atomic_add3(out, t.x, -df1 - df2);

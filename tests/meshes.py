@@ -60,3 +60,36 @@ def tangled(n=8, seed=9, frac=0.08, amp=0.25):
     pick = rng.choice(len(v), max(1, int(frac * len(v))), replace=False)
     v[pick] += rng.uniform(-amp, amp, (len(pick), 3)).astype(np.float32)
     return v, f
+
+
+def sheet_pair(n=8, gap=0.0006, shift=0.031, seed=1):
+    """Two parallel square grids (n x n vertices each) a small gap apart, slightly shifted in the plane, so
+    that point-triangle and edge-edge pairs across the gap are inside the contact barrier's range."""
+    def grid(z, off):
+        xs = np.linspace(0, 1, n)
+        X, Y = np.meshgrid(xs, xs, indexing="ij")
+        V = np.stack([X.ravel() + off, Y.ravel() + off * 0.7, np.full(n * n, z)], 1)
+        F = []
+        for i in range(n - 1):
+            for j in range(n - 1):
+                a, b, c, d = i * n + j, (i + 1) * n + j, (i + 1) * n + j + 1, i * n + j + 1
+                F += [(a, b, c), (a, c, d)]
+        return V, np.array(F, dtype=np.int32)
+
+    V1, F1 = grid(0.0, 0.0)
+    V2, F2 = grid(gap, shift)
+    V = np.vstack([V1, V2])
+    F = np.vstack([F1, F2 + len(V1)]).astype(np.int32)
+    rng = np.random.default_rng(seed)
+    V = V + rng.normal(0, 5e-5, V.shape) * np.array([1.0, 1.0, 0.0])
+    return V, F
+
+
+def stage3_pair(n_gt=16, n_mesh=6, noise=0.003, seed=11):
+    """A fine star-shaped GT mesh and a coarse, inflated and jittered star mesh of the same shape, as the
+    stage-2 output a projection starts from (float64)."""
+    GV, GF = synth.star_mesh(n_gt, 4, lambda l: 0.04, seed)
+    V, F = synth.star_mesh(n_mesh, 4, lambda l: 0.04, seed)
+    rng = np.random.default_rng(seed + 1)
+    V = V.astype(np.float64) * 1.02 + rng.normal(0, noise, V.shape)
+    return GV.astype(np.float64), GF, V, F
