@@ -1,7 +1,8 @@
-"""Benchmark of the GB300 PaMO stage-2 path (parallel QEM collapse with LBVH self-intersection rollback).
+"""Benchmark of the GB300 PaMO path: stage 2 (parallel QEM collapse with LBVH self-intersection rollback) and,
+where the configuration turns it on, stage 3 (barrier/CCD Newton-CG safe projection onto the input mesh).
 
-One step = one whole simplification job (the stage-2 loop of PaMO.run) of the configured synthetic
-mesh, with its inputs already resident in HBM. Prints one JSON line (rank 0).
+One step = one whole job of PaMO.run (stage 2 loop, then stage 3's 5 projection steps) on the configured
+synthetic mesh, with its inputs already resident in HBM. Prints one JSON line (rank 0).
 
     python bench.py [--steps K] [--warmup W] [--config plain_large|plain_small] [--impl gb300|reference]
 
@@ -28,14 +29,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 CONFIGS = {
-    # name: (mesh, ratio, description)
-    "plain_large": ("plain_large", 0.001,
+    # name: (mesh, ratio, stage 3 on, description)
+    "plain_large": ("plain_large", 0.001, True,
                     "level-9 icosphere 2621442 V / 5242880 F, SH l<=16 sigma 0.05/l, seed 0; ratio 0.001, threshold 1e-3, "
-                    "tolerance 4, min_verts 0"),
-    "plain_small": ("plain_small", 0.01,
+                    "tolerance 4, min_verts 0; stage 3 on (5 steps onto the 5242880-face input)"),
+    "plain_small": ("plain_small", 0.01, False,
                     "level-5 icosphere 10242 V / 20480 F, SH l<=6 sigma 0.03, seed 0; ratio 0.01, threshold 1e-3, "
-                    "tolerance 4, min_verts 0"),
+                    "tolerance 4, min_verts 0; stage 3 off"),
 }
+STAGE3_STEPS = 5  # PaMO.run's process(..., 5) (simp_cuda/pamo/__init__.py:168-176)
 THRESHOLD, TOLERANCE = 1e-3, 4
 L2_FLUSH_BYTES = 512 << 20
 
@@ -125,9 +127,10 @@ def compulsory_bytes(phase: str, t: dict) -> tuple[float, str]:
     return 32.0 * V + 32.0 * F, "32 B/vertex + 32 B/face"
 
 
-def cpu_sample(v, f, ratio, gpu_faces_per_round, budget_s=15.0, threads=None):
-    """Times the oracle (OpenMP) on the first rounds of the same job until budget_s, then projects the whole
-    job with the face counts per round of the GPU run (time per face-round is taken as constant)."""
+def cpu_sample(v, f, ratio, gpu_faces_per_round, budget_s=15.0, threads=None, stage3_input=None):
+    """Times the oracle (OpenMP) on the first rounds of the same job until budget_s, then projects stage 2 with
+    the face counts per round of the GPU run (time per face-round is taken as constant). With stage3_input
+    (V, F, description) the float64 stage-3 oracle runs whole on that mesh and its time is added."""
     from oracle import oracle as orc
 
     threads = threads or os.cpu_count() or 1
@@ -153,15 +156,25 @@ def cpu_sample(v, f, ratio, gpu_faces_per_round, budget_s=15.0, threads=None):
     rate = face_rounds / dt
     total_face_rounds = int(len(f) + sum(gpu_faces_per_round[:-1])) if gpu_faces_per_round else face_rounds
     projected = total_face_rounds / rate
+    sample = (f"oracle (OpenMP, {threads} threads) ran the first {rounds} rounds ({face_rounds} face-rounds) in "
+              f"{dt:.1f} s; stage 2 projected from the per-round face counts of the GPU run ({total_face_rounds} "
+              f"face-rounds)")
+    s3_out = None
+    if stage3_input is not None:
+        V2, F2, what = stage3_input
+        t1 = time.perf_counter()
+        s3_out, _ = orc.stage3_run(v.astype(np.float64), f, V2, F2, STAGE3_STEPS)
+        t3 = time.perf_counter() - t1
+        projected += t3
+        sample += f"; stage 3 (float64 oracle) run whole on {what} ({len(F2)} faces) in {t3:.1f} s"
     return {
         "value": len(f) / projected,
         "unit": "input faces/s",
         "cores": threads,
         "kind": "port",
-        "sample": f"oracle (OpenMP, {threads} threads) ran the first {rounds} rounds ({face_rounds} face-rounds) in "
-                  f"{dt:.1f} s; whole job projected from the per-round face counts of the GPU run "
-                  f"({total_face_rounds} face-rounds)",
+        "sample": sample,
         "projected_job_s": projected,
+        "stage3_out": s3_out,
     }
 
 
@@ -172,9 +185,15 @@ def run_reference(args):
         return 0
     from pamo_gb300 import synth
 
-    mesh, ratio, desc = CONFIGS[args.config]
+    mesh, ratio, stage3, desc = CONFIGS[args.config]
     v, f = synth.config_mesh(mesh, seed=0)
     threads = os.cpu_count() or 1
+    s3_in = None
+    if stage3:
+        # stand-in for the stage-2 output (not available without running the whole stage-2 job): the same
+        # surface at icosphere frequency 16 (5120 faces, the size the job's 0.1 % output has)
+        V2, F2 = synth.star_mesh(16, 16, lambda l: 0.05 / l, 0)
+        s3_in = (V2.astype(np.float64), F2, "a 5120-face mesh of the same surface standing in for the stage-2 output")
     budget = 8.0 if args.config == "plain_large" else 2.0
     # face counts per round of the whole job (identical on the GPU path and the oracle), for the projection
     fpr = []
@@ -183,7 +202,7 @@ def run_reference(args):
         fpr = json.load(open(rec))["faces_per_round"]
     vals = []
     for i in range(args.warmup + args.steps):
-        s = cpu_sample(v, f, ratio, fpr, budget_s=budget, threads=threads)
+        s = cpu_sample(v, f, ratio, fpr, budget_s=budget, threads=threads, stage3_input=s3_in)
         if i >= args.warmup:
             vals.append(s)
     value = float(np.median([s["value"] for s in vals]))
@@ -191,7 +210,7 @@ def run_reference(args):
         "impl": "reference", "metric": "input faces/s to 0.1% ratio", "value": value, "unit": "input faces/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * len(f) / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{args.config}: {desc}", "stage3": False},
+        "config": {"workload": f"{args.config}: {desc}", "stage3": stage3},
         "cpu_baseline": {k: vals[-1][k] for k in ("unit", "cores", "kind", "sample")} | {"value": value},
         "e2e": {"value": value, "unit": "input faces/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -226,26 +245,54 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    mesh, ratio, desc = CONFIGS[args.config]
+    mesh, ratio, stage3, desc = CONFIGS[args.config]
     v, f = synth.config_mesh(mesh, seed=0)
     F0 = len(f)
     pts = torch.from_numpy(v).to(dev)
     tri = torch.from_numpy(f).to(dev)
     ctx = pamo_gb300.Context(dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    s3 = None
+    if stage3:
+        from pamo_gb300 import safe_project
+
+        s3 = safe_project.Stage3System(None, dev)
+        gt_v = torch.from_numpy(v.astype(np.float64)).to(dev)  # the input mesh is the projection's GT
 
     def barrier():
         torch.cuda.synchronize(dev)
         if world > 1:
             dist.barrier()
 
-    def job():
-        return pamo_gb300.simplify(pts, tri, ratio, TOLERANCE, THRESHOLD, 1000000, 0, ctx=ctx)
+    s3_ms = []
+
+    def job(time_stage3=False):
+        verts, faces, rounds_ = pamo_gb300.simplify(pts, tri, ratio, TOLERANCE, THRESHOLD, 1000000, 0, ctx=ctx)
+        if s3 is not None:
+            if time_stage3:
+                a = torch.cuda.Event(enable_timing=True)
+                a.record()
+            verts = s3.project(gt_v, tri, verts, faces, STAGE3_STEPS)
+            if time_stage3:
+                b = torch.cuda.Event(enable_timing=True)
+                b.record()
+                b.synchronize()
+                s3_ms.append(a.elapsed_time(b))
+        return verts, faces, rounds_
 
     for _ in range(args.warmup):
         out = job()
     out_faces = out[1].shape[0]
     rounds = out[2]
+    merge_identity = True
+    if s3 is not None:
+        # the device-level job skips trimesh's vertex merge of the stage-2 output; it is the identity here
+        from pamo_gb300 import safe_project
+
+        v2 = pamo_gb300.simplify(pts, tri, ratio, TOLERANCE, THRESHOLD, 1000000, 0, ctx=ctx)
+        V2m, F2m = safe_project.mesh_process(v2[0].cpu().numpy(), v2[1].cpu().numpy())
+        merge_identity = len(V2m) == v2[0].shape[0] and np.array_equal(F2m, v2[1].cpu().numpy())
+        stage2_out = (v2[0].cpu().numpy().astype(np.float64), v2[1].cpu().numpy())
 
     # ---- timed region: K jobs, L2 flushed between them, CUDA events on the launching stream ----
     stream = torch.cuda.current_stream(dev)
@@ -274,7 +321,7 @@ def main():
     # ---- end to end through the public API from pinned host buffers ----
     v_host = torch.from_numpy(v).pin_memory()
     f_host = torch.from_numpy(f).pin_memory()
-    model = pamo_gb300.PaMO((v, f), use_stage1=False, use_stage3=False)
+    model = pamo_gb300.PaMO((v, f), use_stage1=False, use_stage3=stage3)
     e2e_s = []
     d2h = 0
     for i in range(args.steps + 1):
@@ -295,9 +342,10 @@ def main():
 
     # ---- phase profile of one more job (not part of the timed steps) ----
     ctx.profile(True)
-    job()
+    prof_out = job(time_stage3=True)
     prof = ctx.profile_read()
     ctx.profile(False)
+    s3_stats = s3.stats() if s3 is not None else None
     totals = ctx.run_totals()
     fpr = simp.round_faces(ctx, rounds)
     dom = max(prof, key=lambda k: prof[k][0])
@@ -320,21 +368,36 @@ def main():
         return 0
 
     cpu = None
+    precision = None
     if not args.no_cpu_baseline:
-        cpu = cpu_sample(v, f, ratio, fpr, budget_s=12.0 if args.config == "plain_large" else 3.0)
+        s3_in = (stage2_out[0], stage2_out[1], "the stage-2 output of the GPU run") if s3 is not None else None
+        cpu = cpu_sample(v, f, ratio, fpr, budget_s=12.0 if args.config == "plain_large" else 3.0, stage3_input=s3_in)
         cpu.pop("projected_job_s", None)
+        ref3 = cpu.pop("stage3_out", None)
+        if ref3 is not None:
+            got = prof_out[0].cpu().numpy()
+            diag = float(np.linalg.norm(stage2_out[0].max(0) - stage2_out[0].min(0)))
+            precision = {"stage3_max_abs_err": float(np.abs(got - ref3).max()),
+                         "stage3_max_err_over_bbox_diag": float(np.abs(got - ref3).max() / diag),
+                         "against": "float64 oracle run of stage 3 on the same stage-2 output",
+                         "arithmetic": "float32 with compensated (two-sum) energy and CG sums; float64 for the "
+                                       "normalisation, Voronoi weights and angle test"}
 
     line = {
         "metric": "input faces/s to 0.1% ratio", "value": value, "unit": "input faces/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{args.config}: {desc}", "stage3": False, "parallelism": f"replicas{world}",
-                   "l2": "512 MiB buffer written between timed steps", "output_faces": out_faces, "rounds": rounds},
+        "config": {"workload": f"{args.config}: {desc}", "stage3": stage3, "parallelism": f"replicas{world}",
+                   "l2": "512 MiB buffer written between timed steps", "output_faces": out_faces, "rounds": rounds,
+                   "stage3_merge_identity": merge_identity},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": dom, "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": per_launch_bytes, "launches": dom_n,
                      "avg_launch_ms": dom_ms / max(1, dom_n), "bytes_model": unit_desc},
-        "phases_ms": {k: round(ms_, 3) for k, (ms_, _) in prof.items()},
+        "phases_ms": {k: round(ms_, 3) for k, (ms_, _) in prof.items()} | (
+            {"stage3": round(s3_ms[-1], 3)} if s3_ms else {}),
+        "stage3": s3_stats,
+        "precision": precision,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "input faces/s", "h2d_bytes_per_step": int(v.nbytes + f.nbytes),
                 "d2h_bytes_per_step": int(d2h)},

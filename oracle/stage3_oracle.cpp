@@ -11,7 +11,7 @@
 //   * wp.spd_project_blocks(3, block, it_max): projection of the 9x9 matrix of hinge blocks [0..2][0..2]
 //     onto the positive semi-definite cone, here by it_max cyclic Jacobi sweeps and clamping of negative
 //     eigenvalues (the CUDA path does the same in float32);
-//   * wp.mesh_query_point_no_sign + mesh_eval_position: the closest point of the GT surface (brute force);
+//   * wp.mesh_query_point_no_sign + mesh_eval_position: the closest point of the GT surface (uniform grid);
 //   * wp.bvh_query_aabb: candidate pairs whose boxes overlap, then the reference's distance filter; the
 //     filter alone decides, so a uniform grid gives the same contact set;
 //   * igl::massmatrix(VORONOI), igl::internal_angles: restated from libigl's published formulas;
@@ -335,8 +335,89 @@ struct Elastic {
     double W;
 };
 
+// Closest point on the GT surface by a uniform grid: triangles binned by their boxes into cells of side h
+// (sorted (cell, triangle) pairs); a query scans Chebyshev rings of cells around its own until the best
+// distance found is below the distance to the next ring. Gives the exact nearest point (as the reference's
+// BVH query does), in any order of equally near triangles.
+struct GtGrid {
+    double h = 1, lo[3] = {0, 0, 0};
+    long long dims[3] = {1, 1, 1};
+    std::vector<std::pair<long long, int>> cells;
+    long long key(long long i, long long j, long long k) const { return (i * dims[1] + j) * dims[2] + k; }
+    void build(const std::vector<V3>& P, const std::vector<std::array<int, 3>>& T) {
+        double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300}, el = 0;
+        for (auto& p : P) {
+            const double c[3] = {p.x, p.y, p.z};
+            for (int d = 0; d < 3; ++d) {
+                mn[d] = std::min(mn[d], c[d]);
+                mx[d] = std::max(mx[d], c[d]);
+            }
+        }
+        for (auto& t : T) el += len(P[t[1]] - P[t[0]]);
+        el /= std::max<size_t>(1, T.size());
+        double ext = 0;
+        for (int d = 0; d < 3; ++d) ext = std::max(ext, mx[d] - mn[d]);
+        h = std::max(2.0 * el, ext / 1024.0);
+        if (!(h > 0)) h = 1;
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = mn[d];
+            dims[d] = (long long)std::floor((mx[d] - mn[d]) / h) + 1;
+        }
+        cells.clear();
+        for (int f = 0; f < (int)T.size(); ++f) {
+            long long a[3], b[3];
+            const V3 p0 = P[T[f][0]], p1 = P[T[f][1]], p2 = P[T[f][2]];
+            const double l[3] = {std::min({p0.x, p1.x, p2.x}), std::min({p0.y, p1.y, p2.y}), std::min({p0.z, p1.z, p2.z})};
+            const double u[3] = {std::max({p0.x, p1.x, p2.x}), std::max({p0.y, p1.y, p2.y}), std::max({p0.z, p1.z, p2.z})};
+            for (int d = 0; d < 3; ++d) {
+                a[d] = std::min(dims[d] - 1, std::max(0ll, (long long)std::floor((l[d] - lo[d]) / h)));
+                b[d] = std::min(dims[d] - 1, std::max(0ll, (long long)std::floor((u[d] - lo[d]) / h)));
+            }
+            for (long long i = a[0]; i <= b[0]; ++i)
+                for (long long j = a[1]; j <= b[1]; ++j)
+                    for (long long k = a[2]; k <= b[2]; ++k) cells.push_back({key(i, j, k), f});
+        }
+        std::sort(cells.begin(), cells.end());
+    }
+    V3 nearest(V3 p, const std::vector<V3>& P, const std::vector<std::array<int, 3>>& T) const {
+        long long c[3];
+        const double pc[3] = {p.x, p.y, p.z};
+        for (int d = 0; d < 3; ++d) c[d] = (long long)std::floor((pc[d] - lo[d]) / h);
+        double best = 1e300;
+        V3 bp = p;
+        const long long rmax = std::max({dims[0], dims[1], dims[2]}) + std::max({std::llabs(c[0]), std::llabs(c[1]), std::llabs(c[2])}) + 1;
+        for (long long r = 0; r <= rmax; ++r) {
+            for (long long i = c[0] - r; i <= c[0] + r; ++i) {
+                if (i < 0 || i >= dims[0]) continue;
+                for (long long j = c[1] - r; j <= c[1] + r; ++j) {
+                    if (j < 0 || j >= dims[1]) continue;
+                    for (long long k = c[2] - r; k <= c[2] + r; ++k) {
+                        if (k < 0 || k >= dims[2]) continue;
+                        if (std::max({std::llabs(i - c[0]), std::llabs(j - c[1]), std::llabs(k - c[2])}) != r) continue;
+                        const long long kk = key(i, j, k);
+                        auto it = std::lower_bound(cells.begin(), cells.end(), std::make_pair(kk, -1));
+                        for (; it != cells.end() && it->first == kk; ++it) {
+                            const auto& t = T[it->second];
+                            const V3 q = closest_tri(p, P[t[0]], P[t[1]], P[t[2]]);
+                            const double d = len2(q - p);
+                            if (d < best) {
+                                best = d;
+                                bp = q;
+                            }
+                        }
+                    }
+                }
+            }
+            // every cell of ring r + 1 or beyond is at least r * h away from p
+            if (best < 1e300 && best <= ((double)r * h) * ((double)r * h)) break;
+        }
+        return bp;
+    }
+};
+
 struct System {
     Params P;
+    GtGrid grid;
     int NP = 0, NT = 0, NE = 0, NH = 0, NGT = 0;
     std::vector<V3> gt, q, q_rest, qpn, qpd, p, target, grad, hd, r, z, v, Av;
     std::vector<double> w;
@@ -802,21 +883,14 @@ struct System {
         }
     }
 
+    void update_targets() {
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int i = 0; i < NP; ++i) target[i] = grid.nearest(q[i], gt, gtri);
+    }
+
     int step() {
         // _update_vertex_target (geometry_kernels.py:81-93)
-        for (int i = 0; i < NP; ++i) {
-            double best = 1e300;
-            V3 bp = q[i];
-            for (int f = 0; f < NGT; ++f) {
-                const V3 c = closest_tri(q[i], gt[gtri[f][0]], gt[gtri[f][1]], gt[gtri[f][2]]);
-                const double d = len2(c - q[i]);
-                if (d < best) {
-                    best = d;
-                    bp = c;
-                }
-            }
-            target[i] = bp;
-        }
+        update_targets();
         for (int it = 0; it < P.n_newton_iters; ++it) {
             qpn = q;
             int guard = 0;
@@ -909,6 +983,7 @@ static int s3_setup(System& S, double& scale, double* t, const double* gt_pts, c
     for (int i = 0; i < ngp; ++i) S.gt[i] = normed(gt_pts, i);
     S.gtri.resize(ngt);
     for (int f = 0; f < ngt; ++f) S.gtri[f] = {gt_tris[3 * f], gt_tris[3 * f + 1], gt_tris[3 * f + 2]};
+    S.grid.build(S.gt, S.gtri);
     S.q.resize(np);
     for (int i = 0; i < np; ++i) S.q[i] = normed(pts, i);
     S.q_rest = S.q;
@@ -1043,17 +1118,7 @@ int s3_oracle_probe(const double* gt_pts, const int* gt_tris, int ngp, int ngt, 
     if (rs) return rs;
     if (x0)
         for (int i = 0; i < np; ++i) S.q[i] = V3{x0[3 * i], x0[3 * i + 1], x0[3 * i + 2]};
-    for (int i = 0; i < np; ++i) {
-        double best = 1e300;
-        for (int f = 0; f < ngt; ++f) {
-            const V3 c = closest_tri(S.q[i], S.gt[S.gtri[f][0]], S.gt[S.gtri[f][1]], S.gt[S.gtri[f][2]]);
-            const double d = len2(c - S.q[i]);
-            if (d < best) {
-                best = d;
-                S.target[i] = c;
-            }
-        }
-    }
+    S.update_targets();
     if (S.detect() == -1) return 3;
     *n_contacts = (int)S.cidx.size();
     energy[0] = S.compute_energy(S.q);
@@ -1085,17 +1150,7 @@ int s3_oracle_energy_at(const double* gt_pts, const int* gt_tris, int ngp, int n
     if (rs) return rs;
     if (x0)
         for (int i = 0; i < np; ++i) S.q[i] = V3{x0[3 * i], x0[3 * i + 1], x0[3 * i + 2]};
-    for (int i = 0; i < np; ++i) {
-        double best = 1e300;
-        for (int f = 0; f < ngt; ++f) {
-            const V3 c = closest_tri(S.q[i], S.gt[S.gtri[f][0]], S.gt[S.gtri[f][1]], S.gt[S.gtri[f][2]]);
-            const double d = len2(c - S.q[i]);
-            if (d < best) {
-                best = d;
-                S.target[i] = c;
-            }
-        }
-    }
+    S.update_targets();
     if (S.detect() == -1) return 3;
     std::vector<V3> xv(np);
     for (int i = 0; i < np; ++i) xv[i] = V3{x[3 * i], x[3 * i + 1], x[3 * i + 2]};

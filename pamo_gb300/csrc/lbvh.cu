@@ -476,6 +476,25 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
     k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit); note_launch();
 }
 
+__global__ void __launch_bounds__(256) k_refit_leaves(const RoundCounters* rc, const int4* __restrict__ tri,
+                                                      const float4* __restrict__ pos, const int* __restrict__ vals,
+                                                      float4* llo, float4* lhi, int* visit) {
+    const int n = rc->n_live;
+    for (int i = gtid(); i < n; i += gstride()) {
+        const int4 t = tri[vals[i]];
+        const float4 a = pos[t.x], b = pos[t.y], c = pos[t.z];
+        llo[i] = make_float4(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)), 0.f);
+        lhi[i] = make_float4(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)), 0.f);
+        if (i < n - 1) visit[i] = 0;
+    }
+}
+
+void bvh_refit(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s) {
+    const int gF = grid_for(n_tris_bound, 256);
+    k_refit_leaves<<<gF, 256, 0, s>>>(rc, tri, pos, b.vals[0], b.llo, b.lhi, b.visit); note_launch();
+    k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit); note_launch();
+}
+
 void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, const int* qscan,
                unsigned char* hit, int2* pair_list, int pair_cap, RoundCounters* rc, int n_query_bound, float eps,
                cudaStream_t s) {

@@ -32,6 +32,10 @@ void bvh_carve(BvhBuffers& b, int cap, char* base);
 // Builds the LBVH over faces with tri[f].x != -1 (count from rc->n_tris); writes rc->n_live.
 void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s);
 
+// Recomputes the leaf and node boxes of a tree built by bvh_build over the same faces after the positions
+// moved (same topology and leaf order; the tree may bound more loosely than a rebuilt one).
+void bvh_refit(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s);
+
 // For every face in the query list that is still live: hit[f] = 1 iff some live face g != f with an
 // overlapping closed AABB makes the reference's pair test true in either order. Query faces are taken
 // as the faces f with qscan[f + 1] != qscan[f] (qscan: exclusive scan of the query flags), visited in leaf

@@ -86,6 +86,7 @@ __device__ __forceinline__ int gstride() { return gridDim.x * blockDim.x; }
 
 // Host-side count of kernels this library has launched (for launch accounting in benchmarks).
 void note_launch();
+void note_launches(long long n);  // kernels run by a CUDA graph launch
 long long launches_so_far();
 
 inline int grid_for(long long n, int threads, int per_sm = 8) {

@@ -53,11 +53,8 @@ __device__ __forceinline__ F3 normalize(F3 a) {  // Warp: zero vector when the l
 }
 __device__ __forceinline__ F3 fmin3(F3 a, F3 b) { return {fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)}; }
 __device__ __forceinline__ F3 fmax3(F3 a, F3 b) { return {fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)}; }
-__device__ __forceinline__ void atomic_add3(float4* a, int i, F3 v) {
-    atomicAdd(&a[i].x, v.x);
-    atomicAdd(&a[i].y, v.y);
-    atomicAdd(&a[i].z, v.z);
-}
+// one 16-byte vector atomic (sm_90+ global memory) instead of three scalar ones
+__device__ __forceinline__ void atomic_add3(float4* a, int i, F3 v) { atomicAdd(&a[i], make_float4(v.x, v.y, v.z, 0.f)); }
 // Warp's step(x): 1 when x < 0, else 0
 __device__ __forceinline__ float wstep(float x) { return x < 0.f ? 1.f : 0.f; }
 
@@ -347,43 +344,33 @@ __device__ CSum block_reduce(CSum v) {
     return r;
 }
 
-// partial sums of vals[0..n) over a fixed split into kRedBlocks chunks
-__global__ void __launch_bounds__(kT) k_reduce(const float* __restrict__ vals, const int* d_n, int n_add, float2* partial) {
-    const int n = (d_n ? *d_n : 0) + n_add;
-    const int chunk = (n + kRedBlocks - 1) / kRedBlocks;
-    const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
-    CSum acc;
-    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) acc.add(vals[i]);
-    CSum r = block_reduce(acc);
-    if (threadIdx.x == 0) partial[blockIdx.x] = make_float2(r.s, r.c);
-}
-
-// partial sums of a . b over vec3 arrays
-__global__ void __launch_bounds__(kT) k_reduce_dot(const float4* __restrict__ a, const float4* __restrict__ b, int n,
-                                                   float2* partial) {
-    const int chunk = (n + kRedBlocks - 1) / kRedBlocks;
-    const int lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
-    CSum acc;
-    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        const float4 x = a[i], y = b[i];
-        acc.add(x.x * y.x + x.y * y.y + x.z * y.z);
-    }
-    CSum r = block_reduce(acc);
-    if (threadIdx.x == 0) partial[blockIdx.x] = make_float2(r.s, r.c);
-}
-
-__global__ void __launch_bounds__(kT) k_reduce_finish(const float2* __restrict__ partial, float* out, float* copy_prev) {
-    CSum acc;
-    for (int i = threadIdx.x; i < kRedBlocks; i += blockDim.x) {
-        CSum p;
-        p.s = partial[i].x;
-        p.c = partial[i].y;
-        acc.merge(p);
-    }
+// Ends a grid-wide compensated sum: every block stores its partial; the last block to arrive (counted in
+// *counter) reduces the partials in block order, stores the result in *out (after copying the old value to
+// *copy_prev when given) and resets the counter. The order of every addition is fixed by the grid shape,
+// so the sum is deterministic. All blocks of the grid must call it.
+__device__ void grid_sum_finish(CSum acc, float2* partial, int* counter, float* out, float* copy_prev) {
+    __shared__ int last;
     CSum r = block_reduce(acc);
     if (threadIdx.x == 0) {
+        partial[blockIdx.x] = make_float2(r.s, r.c);
+        __threadfence();
+        last = (atomicAdd(counter, 1) == (int)gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    CSum a;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        CSum t;
+        t.s = __ldcg(&partial[b].x);
+        t.c = __ldcg(&partial[b].y);
+        a.merge(t);
+    }
+    CSum f = block_reduce(a);
+    if (threadIdx.x == 0) {
         if (copy_prev) *copy_prev = *out;
-        *out = r.s + r.c;
+        *out = f.s + f.c;
+        *counter = 0;
     }
 }
 
@@ -697,9 +684,11 @@ __global__ void __launch_bounds__(kQT) k_detect(const float4* __restrict__ x, in
                                                 const int2* __restrict__ child, const float4* __restrict__ nlo,
                                                 const float4* __restrict__ nhi, const float4* __restrict__ llo,
                                                 const float4* __restrict__ lhi, const int* __restrict__ leaf_id,
-                                                const RoundCounters* brc, float thr, float ee_thres, int4* c_idx,
+                                                const RoundCounters* brc, float d_hat, float ee_thres, int4* c_idx,
                                                 int2* c_type, int cap, SolverScalars* sc) {
     __shared__ int stack[kStack][kQT];
+    if (sc->abort) return;
+    const float thr = 2.0f * sc->radius + d_hat;
     const int nl = brc->n_live;
     for (int qi = gtid(); qi < n_query; qi += gstride()) {
         int i0, i1 = -1;
@@ -792,16 +781,7 @@ __global__ void __launch_bounds__(kQT) k_detect(const float4* __restrict__ x, in
     }
 }
 
-// ------------------------------------------------------------------ energies (one value per element)
-// segments of e_elem: [0, NP) distance to GT, [NP, NP + NT) StVK, [.., + NH) hinge, [.., + NC) barrier
-__global__ void k_energy_m2gt(const float4* __restrict__ x, const float4* __restrict__ tgt, const float* __restrict__ w,
-                              float stiff, int np, float* e) {
-    for (int i = gtid(); i < np; i += gstride()) {
-        const float wi = w[i] * stiff;
-        e[i] = 0.5f * length_sq(f3(x[i]) - f3(tgt[i])) * wi;
-    }
-}
-
+// ------------------------------------------------------------------ energies
 struct Mat2 {
     float a, b, c, d;  // [[a, b], [c, d]]
 };
@@ -831,52 +811,82 @@ __device__ __forceinline__ ElasticLocal elastic_local(const float4* __restrict__
     return L;
 }
 
-__global__ void k_energy_elastic(const float4* __restrict__ x, const int4* __restrict__ tri, const float* __restrict__ area,
-                                 const float4* __restrict__ invDm, float mu, float la, int nt, float* e) {
-    for (int f = gtid(); f < nt; f += gstride()) {
-        const ElasticLocal L = elastic_local(x, tri[f], area[f], invDm[f]);
-        const Mat2 I = {1.f, 0.f, 0.f, 1.f};
-        const Mat2 E = mscale(0.5f, madd(mmul(mtr(L.F), L.F), mscale(-1.f, I)));
-        const float trE = mtrace(E);
-        e[f] = L.W * (mu * mtrace(mmul(E, mtr(E))) + 0.5f * la * trE * trE);
-    }
-}
+struct EnergyArgs {
+    const float4* tgt;
+    const float* w;
+    float m2gt_k;
+    int np;
+    const int4* tri;
+    const float* area;
+    const float4* invDm;
+    float mu, la;
+    int nt;
+    const int4* hinge;
+    const float2* rest;
+    float hinge_k;
+    int nh;
+    const int4* cidx;
+    int2* ctype;
+    float* cd;
+    float kappa, d_hat, ee_thres;
+};
 
-__global__ void k_energy_hinge(const float4* __restrict__ x, const int4* __restrict__ hinge, const float2* __restrict__ rest,
-                               float k, int nh, float* e) {
-    for (int h = gtid(); h < nh; h += gstride()) {
-        const int4 i = hinge[h];
-        const float th = hinge_angle(f3(x[i.x]), f3(x[i.y]), f3(x[i.z]), f3(x[i.w]));
-        const float dth = th - rest[h].x;
-        e[h] = 0.5f * k * dth * dth * rest[h].y;
-    }
-}
-
-// collision_energy_kernel (collision_energy.py:49-99): reclassify, store the type and distance
-__global__ void k_energy_contact(const float4* __restrict__ x, const int4* __restrict__ cidx, int2* ctype, float* cd,
-                                 const SolverScalars* sc, float kappa, float dh, float ee_thres, float* e) {
-    const int n = sc->n_contacts;
-    for (int b = gtid(); b < n; b += gstride()) {
-        const int4 i = cidx[b];
-        const F3 x0 = f3(x[i.x]), x1 = f3(x[i.y]), x2 = f3(x[i.z]), x3 = f3(x[i.w]);
-        int2 t = ctype[b];
-        float d;
-        if (t.x == BLOCK_PT) {
-            t.y = pt_classify(x0, x1, x2, x3);
-            d = pt_pair_distance(x0, x1, x2, x3, t.y);
+// Total energy at x (system.py:325-339): the four energies of the default set, one grid-stride pass over
+// [vertices | triangles | hinges | contacts], summed with compensation in a fixed order into sc->energy.
+// mesh2gt_pp_distance_energy_kernel (distance_energy.py:6-17), elastic_energy_kernel (elastic_energy.py:40-80),
+// hinge_energy_kernel (hinge_energy.py:60-88), collision_energy_kernel (collision_energy.py:49-99: the contact
+// is reclassified at x and its type and distance stored for the gradient).
+__global__ void __launch_bounds__(kT) k_energy(const float4* __restrict__ x, EnergyArgs A, SolverScalars* sc,
+                                               float2* partial) {
+    if (sc->abort) return;
+    const int nc = sc->n_contacts;
+    const long long e1 = A.np, e2 = e1 + A.nt, e3 = e2 + A.nh, total = e3 + nc;
+    CSum acc;
+    for (long long g = gtid(); g < total; g += gstride()) {
+        float e;
+        if (g < e1) {
+            const int i = (int)g;
+            const float wi = A.w[i] * A.m2gt_k;
+            e = 0.5f * length_sq(f3(x[i]) - f3(A.tgt[i])) * wi;
+        } else if (g < e2) {
+            const int f = (int)(g - e1);
+            const ElasticLocal L = elastic_local(x, A.tri[f], A.area[f], A.invDm[f]);
+            const Mat2 I = {1.f, 0.f, 0.f, 1.f};
+            const Mat2 E = mscale(0.5f, madd(mmul(mtr(L.F), L.F), mscale(-1.f, I)));
+            const float trE = mtrace(E);
+            e = L.W * (A.mu * mtrace(mmul(E, mtr(E))) + 0.5f * A.la * trE * trE);
+        } else if (g < e3) {
+            const int h = (int)(g - e2);
+            const int4 i = A.hinge[h];
+            const float dth = hinge_angle(f3(x[i.x]), f3(x[i.y]), f3(x[i.z]), f3(x[i.w])) - A.rest[h].x;
+            e = 0.5f * A.hinge_k * dth * dth * A.rest[h].y;
         } else {
-            t.y = ee_classify(x0, x1, x2, x3, ee_thres);
-            d = ee_pair_distance(x0, x1, x2, x3, t.y);
+            const int b = (int)(g - e3);
+            const int4 i = A.cidx[b];
+            const F3 x0 = f3(x[i.x]), x1 = f3(x[i.y]), x2 = f3(x[i.z]), x3 = f3(x[i.w]);
+            int2 t = A.ctype[b];
+            float d;
+            if (t.x == BLOCK_PT) {
+                t.y = pt_classify(x0, x1, x2, x3);
+                d = pt_pair_distance(x0, x1, x2, x3, t.y);
+            } else {
+                t.y = ee_classify(x0, x1, x2, x3, A.ee_thres);
+                d = ee_pair_distance(x0, x1, x2, x3, t.y);
+            }
+            A.ctype[b] = t;
+            A.cd[b] = d;
+            e = d < A.d_hat ? barrier(d, A.d_hat) * A.kappa : 0.f;
         }
-        ctype[b] = t;
-        cd[b] = d;
-        e[b] = d < dh ? barrier(d, dh) * kappa : 0.f;
+        acc.add(e);
     }
+    grid_sum_finish(acc, partial, &sc->red_count, &sc->energy, nullptr);
 }
 
 // ------------------------------------------------------------------ gradients and Hessian diagonal (coeff = -1)
 __global__ void k_diff_m2gt(const float4* __restrict__ x, const float4* __restrict__ tgt, const float* __restrict__ w,
-                            float stiff, float coeff, int np, float4* grad, float4* hd) {
+                            float stiff, float coeff, int np, float4* grad, float4* hd,
+                            const SolverScalars* sc) {
+    if (sc->abort) return;
     for (int i = gtid(); i < np; i += gstride()) {
         const float wi = w[i] * stiff;
         atomic_add3(grad, i, (f3(x[i]) - f3(tgt[i])) * wi * coeff);
@@ -885,7 +895,9 @@ __global__ void k_diff_m2gt(const float4* __restrict__ x, const float4* __restri
 }
 
 __global__ void k_diff_elastic(const float4* __restrict__ x, const int4* __restrict__ tri, const float* __restrict__ area,
-                               const float4* __restrict__ invDm, float mu, float la, float coeff, int nt, float4* grad) {
+                               const float4* __restrict__ invDm, float mu, float la, float coeff, int nt, float4* grad,
+                               const SolverScalars* sc) {
+    if (sc->abort) return;
     for (int f = gtid(); f < nt; f += gstride()) {
         const int4 t = tri[f];
         const ElasticLocal L = elastic_local(x, t, area[f], invDm[f]);
@@ -937,7 +949,9 @@ __device__ __forceinline__ M33 sym(M33 a) { return add(a, tr(a)); }
 
 // hinge_diff_kernel (hinge_energy.py:85-238): gradient, Hessian diagonal and the 4x4 blocks of 3x3
 __global__ void k_diff_hinge(const float4* __restrict__ x, const int4* __restrict__ hinge, const float2* __restrict__ rest,
-                             float k, float coeff, int nh, float* blocks, float4* grad, float4* hd) {
+                             float k, float coeff, int nh, float* blocks, float4* grad, float4* hd,
+                             const SolverScalars* sc) {
+    if (sc->abort) return;
     for (int h = gtid(); h < nh; h += gstride()) {
         const int4 id = hinge[h];
         const F3 x0 = f3(x[id.x]), x1 = f3(x[id.y]), x2 = f3(x[id.z]), x3 = f3(x[id.w]);
@@ -1007,71 +1021,100 @@ __global__ void k_diff_hinge(const float4* __restrict__ x, const int4* __restric
 // wp.spd_project_blocks(3, block, it_max); here the 9x9 matrix of blocks [0..2][0..2] is made positive
 // semi-definite by a cyclic Jacobi eigen-decomposition (it_max sweeps), clamping negative eigenvalues to
 // zero; the fourth block row and column are then set from the first three as the reference does.
-__global__ void k_spd_project(float* blocks, int nh, int sweeps) {
+__global__ void __launch_bounds__(64) k_spd_project(float* blocks, int nh, int sweeps, const SolverScalars* sc) {
+    if (sc->abort) return;
     for (int h = gtid(); h < nh; h += gstride()) {
         float* B = blocks + (size_t)h * 144;
+        // every loop below is unrolled so that A and V live in registers
         float A[9][9], V[9][9];
+#pragma unroll
         for (int a = 0; a < 3; ++a)
+#pragma unroll
             for (int b = 0; b < 3; ++b)
+#pragma unroll
                 for (int i = 0; i < 3; ++i)
+#pragma unroll
                     for (int j = 0; j < 3; ++j) A[a * 3 + i][b * 3 + j] = B[((a * 4 + b) * 3 + i) * 3 + j];
+#pragma unroll
         for (int i = 0; i < 9; ++i)
+#pragma unroll
             for (int j = 0; j < 9; ++j) {
                 const float s = 0.5f * (A[i][j] + A[j][i]);
                 A[i][j] = s;
                 V[i][j] = (i == j) ? 1.f : 0.f;
             }
-        for (int sw = 0; sw < sweeps; ++sw)
+        for (int sw = 0; sw < sweeps; ++sw) {
+#pragma unroll
             for (int p = 0; p < 8; ++p)
+#pragma unroll
                 for (int q = p + 1; q < 9; ++q) {
                     const float apq = A[p][q];
                     if (fabsf(apq) < 1e-30f) continue;
                     const float th = (A[q][q] - A[p][p]) / (2.f * apq);
                     const float t = (th >= 0.f ? 1.f : -1.f) / (fabsf(th) + sqrtf(th * th + 1.f));
                     const float c = 1.f / sqrtf(t * t + 1.f), s = t * c;
+#pragma unroll
                     for (int k = 0; k < 9; ++k) {
                         const float akp = A[k][p], akq = A[k][q];
                         A[k][p] = c * akp - s * akq;
                         A[k][q] = s * akp + c * akq;
                     }
+#pragma unroll
                     for (int k = 0; k < 9; ++k) {
                         const float apk = A[p][k], aqk = A[q][k];
                         A[p][k] = c * apk - s * aqk;
                         A[q][k] = s * apk + c * aqk;
                     }
+#pragma unroll
                     for (int k = 0; k < 9; ++k) {
                         const float vkp = V[k][p], vkq = V[k][q];
                         V[k][p] = c * vkp - s * vkq;
                         V[k][q] = s * vkp + c * vkq;
                     }
                 }
+        }
         float lam[9];
+#pragma unroll
         for (int i = 0; i < 9; ++i) lam[i] = fmaxf(A[i][i], 0.f);
+#pragma unroll
         for (int i = 0; i < 9; ++i)
+#pragma unroll
             for (int j = 0; j < 9; ++j) {
                 float s = 0.f;
+#pragma unroll
                 for (int k = 0; k < 9; ++k) s += V[i][k] * lam[k] * V[j][k];
                 A[i][j] = s;
             }
+#pragma unroll
         for (int a = 0; a < 3; ++a)
+#pragma unroll
             for (int b = 0; b < 3; ++b)
+#pragma unroll
                 for (int i = 0; i < 3; ++i)
+#pragma unroll
                     for (int j = 0; j < 3; ++j) B[((a * 4 + b) * 3 + i) * 3 + j] = A[a * 3 + i][b * 3 + j];
         // block[3][j] = -sum_i block[i][j]; block[j][3] = block[3][j]^T; block[3][3] = -sum_j block[j][3]
+        float R[3][3][3];
+#pragma unroll
         for (int b = 0; b < 3; ++b)
+#pragma unroll
             for (int i = 0; i < 3; ++i)
+#pragma unroll
                 for (int j = 0; j < 3; ++j) {
                     float s = 0.f;
-                    for (int a = 0; a < 3; ++a) s -= B[((a * 4 + b) * 3 + i) * 3 + j];
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) s -= A[a * 3 + i][b * 3 + j];
+                    R[b][i][j] = s;
                     B[((3 * 4 + b) * 3 + i) * 3 + j] = s;
+                    B[((b * 4 + 3) * 3 + j) * 3 + i] = s;
                 }
-        for (int b = 0; b < 3; ++b)
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) B[((b * 4 + 3) * 3 + i) * 3 + j] = B[((3 * 4 + b) * 3 + j) * 3 + i];
+#pragma unroll
         for (int i = 0; i < 3; ++i)
+#pragma unroll
             for (int j = 0; j < 3; ++j) {
                 float s = 0.f;
-                for (int b = 0; b < 3; ++b) s -= B[((b * 4 + 3) * 3 + i) * 3 + j];
+#pragma unroll
+                for (int b = 0; b < 3; ++b) s -= R[b][j][i];  // block[b][3][i][j] = block[3][b][j][i]
                 B[((3 * 4 + 3) * 3 + i) * 3 + j] = s;
             }
     }
@@ -1081,6 +1124,7 @@ __global__ void k_spd_project(float* blocks, int nh, int sweeps) {
 __global__ void k_diff_contact(const float4* __restrict__ x, const int4* __restrict__ cidx, const int2* __restrict__ ctype,
                                const float* __restrict__ cd, const SolverScalars* sc, float kappa, float dh, float coeff,
                                float4* cdd, float4* grad, float4* hd) {
+    if (sc->abort) return;
     const int n = sc->n_contacts;
     for (int b = gtid(); b < n; b += gstride()) {
         const float d = cd[b];
@@ -1102,23 +1146,59 @@ __global__ void k_diff_contact(const float4* __restrict__ x, const int4* __restr
     }
 }
 
-// ------------------------------------------------------------------ Hessian-vector products
-__global__ void k_hvp(const float4* __restrict__ x, const float4* __restrict__ dx, const float* __restrict__ w, float stiff,
-                      int np, const int4* __restrict__ tri, const float* __restrict__ area, const float4* __restrict__ invDm,
-                      float mu, float la, int nt, const int4* __restrict__ hinge, const float* __restrict__ blocks, int nh,
-                      const int4* __restrict__ cidx, const float* __restrict__ cd, const float4* __restrict__ cdd,
-                      const SolverScalars* sc, float kappa, float dh, float4* out) {
+// ------------------------------------------------------------------ Jacobi PCG (cg_solver.py:46-158)
+// One CG iteration is two kernels:
+//   k_cg_hvp: the search direction v = z + (z_r / z_r_last) v_prev is formed where it is read (update_v_kernel,
+//             solver_kernels.py:26-35), Av += H v over every element (system.py:348-352: the hess_dx kernels
+//             of distance_energy.py:20-33, elastic_energy.py:151-220, hinge_energy.py:241-274 and the
+//             Gauss-Newton collision_hess_dx_kernel, collision_energy.py:379-409), and v.Av is summed per
+//             element (v_e . H_e v_e), which equals v . Av, so no separate dot-product pass is needed;
+//   k_cg_prz: p += alpha v, r -= alpha Av when v.Av > 1e-16, z = r / diag, z.r
+//             (update_p_r_z_compute_zr_kernel, solver_kernels.py:4-23); Av is cleared for the next product.
+struct HvpArgs {
+    const float* w;
+    float m2gt_k;
+    int np;
+    const int4* tri;
+    const float* area;
+    const float4* invDm;
+    float mu, la;
+    int nt;
+    const int4* hinge;
+    const float* blocks;
+    int nh;
+    const int4* cidx;
+    const float* cd;
+    const float4* cdd;
+    float kappa, d_hat;
+};
+
+__device__ __forceinline__ F3 cg_dir(const float4* __restrict__ z, const float4* __restrict__ vprev, float s, int j) {
+    return f3(z[j]) + s * f3(vprev[j]);
+}
+
+__global__ void __launch_bounds__(kT) k_cg_hvp(const float4* __restrict__ x, HvpArgs A, const float4* __restrict__ z,
+                                               const float4* __restrict__ vprev, float4* vout, float4* Av, int first,
+                                               SolverScalars* sc, float2* partial) {
+    if (sc->abort) return;
+    const float s = first ? 0.f : sc->z_r / sc->z_r_last;
     const int nc = sc->n_contacts;
-    const long long total = (long long)np + nt + nh + nc;
+    const long long e1 = A.np, e2 = e1 + A.nt, e3 = e2 + A.nh, total = e3 + nc;
+    CSum acc;
     for (long long g = gtid(); g < total; g += gstride()) {
-        if (g < np) {  // mesh2gt_pp_distance_energy_hess_dx_kernel
+        if (g < e1) {
             const int i = (int)g;
-            atomic_add3(out, i, f3(dx[i]) * (w[i] * stiff));
-        } else if (g < np + nt) {  // elastic_hess_dx_kernel (elastic_energy.py:151-220)
-            const int f = (int)(g - np);
-            const int4 t = tri[f];
-            const ElasticLocal L = elastic_local(x, t, area[f], invDm[f]);
-            const F3 dx01 = f3(dx[t.y]) - f3(dx[t.x]), dx02 = f3(dx[t.z]) - f3(dx[t.x]);
+            const F3 vi = cg_dir(z, vprev, s, i);
+            vout[i] = f4(vi);
+            const float wi = A.w[i] * A.m2gt_k;
+            atomic_add3(Av, i, vi * wi);
+            acc.add(dot(vi, vi * wi));
+        } else if (g < e2) {
+            const int f = (int)(g - e1);
+            const int4 t = A.tri[f];
+            const ElasticLocal L = elastic_local(x, t, A.area[f], A.invDm[f]);
+            const F3 v0 = cg_dir(z, vprev, s, t.x), v1 = cg_dir(z, vprev, s, t.y), v2 = cg_dir(z, vprev, s, t.z);
+            const F3 dx01 = v1 - v0, dx02 = v2 - v0;
             const Mat2 dDs = {dot(L.b1, dx01), dot(L.b1, dx02), dot(L.b2, dx01), dot(L.b2, dx02)};
             const Mat2 dF = mmul(dDs, L.invDm);
             const Mat2 I = {1.f, 0.f, 0.f, 1.f};
@@ -1126,66 +1206,82 @@ __global__ void k_hvp(const float4* __restrict__ x, const float4* __restrict__ d
             const float trE = mtrace(E);
             const Mat2 dE = mscale(0.5f, madd(mmul(mtr(dF), L.F), mmul(mtr(L.F), dF)));
             const float trdE = mtrace(dE);
-            const Mat2 dP = madd(mmul(dF, madd(mscale(2.f * mu, E), mscale(la * trE, I))),
-                                 mmul(L.F, madd(mscale(2.f * mu, dE), mscale(la * trdE, I))));
+            const Mat2 dP = madd(mmul(dF, madd(mscale(2.f * A.mu, E), mscale(A.la * trE, I))),
+                                 mmul(L.F, madd(mscale(2.f * A.mu, dE), mscale(A.la * trdE, I))));
             const Mat2 dH = mmul(mscale(L.W, dP), mtr(L.invDm));
             const F3 df1 = dH.a * L.b1 + dH.c * L.b2;
             const F3 df2 = dH.b * L.b1 + dH.d * L.b2;
-            atomic_add3(out, t.x, -df1 - df2);
-            atomic_add3(out, t.y, df1);
-            atomic_add3(out, t.z, df2);
-        } else if (g < np + nt + nh) {  // hinge_hess_dx_kernel (hinge_energy.py:241-274)
-            const int h = (int)(g - np - nt);
-            const int4 id = hinge[h];
+            const F3 df0 = -df1 - df2;
+            atomic_add3(Av, t.x, df0);
+            atomic_add3(Av, t.y, df1);
+            atomic_add3(Av, t.z, df2);
+            acc.add(dot(v0, df0) + dot(v1, df1) + dot(v2, df2));
+        } else if (g < e3) {
+            const int h = (int)(g - e2);
+            const int4 id = A.hinge[h];
             const int ids[4] = {id.x, id.y, id.z, id.w};
-            const float* B = blocks + (size_t)h * 144;
+            const float* B = A.blocks + (size_t)h * 144;
             F3 d[4];
-            for (int b = 0; b < 4; ++b) d[b] = f3(dx[ids[b]]);
+            for (int b = 0; b < 4; ++b) d[b] = cg_dir(z, vprev, s, ids[b]);
+            float vhv = 0.f;
             for (int a = 0; a < 4; ++a) {
-                F3 acc = {0.f, 0.f, 0.f};
+                F3 r = {0.f, 0.f, 0.f};
                 for (int b = 0; b < 4; ++b) {
                     const float* M = B + (a * 4 + b) * 9;
-                    acc = acc + F3{M[0] * d[b].x + M[1] * d[b].y + M[2] * d[b].z, M[3] * d[b].x + M[4] * d[b].y + M[5] * d[b].z,
-                                   M[6] * d[b].x + M[7] * d[b].y + M[8] * d[b].z};
+                    r = r + F3{M[0] * d[b].x + M[1] * d[b].y + M[2] * d[b].z, M[3] * d[b].x + M[4] * d[b].y + M[5] * d[b].z,
+                               M[6] * d[b].x + M[7] * d[b].y + M[8] * d[b].z};
                 }
-                atomic_add3(out, ids[a], acc);
+                atomic_add3(Av, ids[a], r);
+                vhv += dot(d[a], r);
             }
-        } else {  // collision_hess_dx_kernel (collision_energy.py:379-409), Gauss-Newton
-            const int b = (int)(g - np - nt - nh);
-            const float d = cd[b];
-            if (d >= dh) continue;
-            const float c = barrier_d2(d, dh) * kappa;
-            const int4 i = cidx[b];
+            acc.add(vhv);
+        } else {
+            const int b = (int)(g - e3);
+            const float dist = A.cd[b];
+            if (dist >= A.d_hat) continue;
+            const float c = barrier_d2(dist, A.d_hat) * A.kappa;
+            const int4 i = A.cidx[b];
             const int ids[4] = {i.x, i.y, i.z, i.w};
             F3 gg[4];
-            float s = 0.f;
+            float sd = 0.f;
             for (int k = 0; k < 4; ++k) {
-                gg[k] = f3(cdd[4 * (size_t)b + k]);
-                s += dot(gg[k], f3(dx[ids[k]]));
+                gg[k] = f3(A.cdd[4 * (size_t)b + k]);
+                sd += dot(gg[k], cg_dir(z, vprev, s, ids[k]));
             }
-            for (int k = 0; k < 4; ++k) atomic_add3(out, ids[k], gg[k] * (s * c));
+            for (int k = 0; k < 4; ++k) atomic_add3(Av, ids[k], gg[k] * (sd * c));
+            acc.add(sd * sd * c);
         }
     }
+    grid_sum_finish(acc, partial, &sc->red_count, &sc->v_A_v, nullptr);
 }
 
-// ------------------------------------------------------------------ CG vector updates (solver_kernels.py)
-__global__ void k_cg_init(const float4* __restrict__ grad, const float4* __restrict__ hd, int np, float4* p, float4* r,
-                          float4* z, float4* v) {
+// p = 0, r = grad, z = r / (diag + 1e-6) (compute_block_diag_inv_kernel), v_prev = 0, Av = 0, z.r
+__global__ void __launch_bounds__(kT) k_cg_init(const float4* __restrict__ grad, const float4* __restrict__ hd, int np,
+                                                float4* p, float4* r, float4* z, float4* vprev, float4* Av,
+                                                SolverScalars* sc, float2* partial) {
+    if (sc->abort) return;
+    CSum acc;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int i = gtid(); i < np; i += gstride()) {
         const float4 g = grad[i], d = hd[i];
-        p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        p[i] = zero;
         r[i] = g;
         const float4 zz = make_float4(g.x / (d.x + 1e-6f), g.y / (d.y + 1e-6f), g.z / (d.z + 1e-6f), 0.f);
         z[i] = zz;
-        v[i] = zz;
+        vprev[i] = zero;
+        Av[i] = zero;
+        acc.add(zz.x * g.x + zz.y * g.y + zz.z * g.z);
     }
+    grid_sum_finish(acc, partial, &sc->red_count, &sc->z_r, nullptr);
 }
 
-// update_p_r_z_compute_zr_kernel: p += a v, r -= a Av when v.Av > 1e-16; z = r / diag
-__global__ void k_cg_prz(const float4* __restrict__ v, const float4* __restrict__ Av, const float4* __restrict__ hd,
-                         const SolverScalars* sc, int np, float4* p, float4* r, float4* z) {
+__global__ void __launch_bounds__(kT) k_cg_prz(const float4* __restrict__ v, float4* Av, const float4* __restrict__ hd,
+                                               int np, float4* p, float4* r, float4* z, SolverScalars* sc,
+                                               float2* partial) {
+    if (sc->abort) return;
     const float vAv = sc->v_A_v;
     const float alpha = sc->z_r / vAv;
+    CSum acc;
     for (int i = gtid(); i < np; i += gstride()) {
         float4 ri = r[i];
         if (vAv > 1e-16f) {
@@ -1196,32 +1292,71 @@ __global__ void k_cg_prz(const float4* __restrict__ v, const float4* __restrict_
             p[i] = pi;
             r[i] = ri;
         }
+        Av[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 d = hd[i];
-        z[i] = make_float4(ri.x / d.x, ri.y / d.y, ri.z / d.z, 0.f);
+        const float4 zz = make_float4(ri.x / d.x, ri.y / d.y, ri.z / d.z, 0.f);
+        z[i] = zz;
+        acc.add(zz.x * ri.x + zz.y * ri.y + zz.z * ri.z);
+    }
+    grid_sum_finish(acc, partial, &sc->red_count, &sc->z_r, &sc->z_r_last);  // z_r_last = old z_r
+}
+
+// ------------------------------------------------------------------ iteration bookkeeping
+// Start of a Newton iteration (system.py:425-432): q_prev_newton = q, gradient and Hessian diagonal cleared,
+// contact counter reset.
+__global__ void k_iter_begin(const float4* __restrict__ q, float4* qpn, float4* grad, float4* hd, int np,
+                             SolverScalars* sc) {
+    if (sc->abort) return;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = gtid(); i < np; i += gstride()) {
+        qpn[i] = q[i];
+        grad[i] = zero;
+        hd[i] = zero;
+    }
+    if (gtid() == 0) sc->n_contacts_raw = 0;
+}
+
+// After detection: the contact count, and the abort code when the list overflowed (energy.py:942-948 halves
+// the radius when the count exceeds max_blocks; a count above this build's capacity grows the list instead).
+__global__ void k_contacts_done(SolverScalars* sc, int cap, long long max_blocks) {
+    if (sc->abort) return;
+    const int raw = sc->n_contacts_raw;
+    if ((long long)raw > max_blocks) {
+        sc->abort = 2;
+        return;
+    }
+    if (raw > cap) {
+        sc->abort = 1;
+        return;
+    }
+    sc->n_contacts = raw;
+    sc->total_contacts += raw;
+    if (raw > sc->max_contacts) sc->max_contacts = raw;
+}
+
+// clamp_p_kernel (solver_kernels.py:68-85): keep |q_prev_newton + p - q_prev_detection| <= radius. Contacts are
+// detected at the start of every Newton iteration, so q_prev_detection equals q_prev_newton.
+__global__ void k_clamp_p(float4* p, const float4* __restrict__ qn, float radius, int np, const SolverScalars* sc) {
+    if (sc->abort) return;
+    for (int i = gtid(); i < np; i += gstride()) {
+        const F3 pi = f3(p[i]), qni = f3(qn[i]);
+        const F3 dq = qni + pi - qni;
+        if (length(dq) > radius) p[i] = f4(normalize(dq) * radius + qni - qni);
     }
 }
 
-__global__ void k_cg_v(const float4* __restrict__ z, const SolverScalars* sc, int np, float4* v) {
-    const float s = sc->z_r / sc->z_r_last;
-    for (int i = gtid(); i < np; i += gstride()) {
-        const float4 zi = z[i], vi = v[i];
-        v[i] = make_float4(zi.x + s * vi.x, zi.y + s * vi.y, zi.z + s * vi.z, 0.f);
-    }
-}
-
-// clamp_p_kernel: keep |q_prev_newton + p - q_prev_detection| <= radius
-__global__ void k_clamp_p(float4* p, const float4* __restrict__ qn, const float4* __restrict__ qd, float radius, int np) {
-    for (int i = gtid(); i < np; i += gstride()) {
-        const F3 pi = f3(p[i]), qni = f3(qn[i]), qdi = f3(qd[i]);
-        const F3 dq = qni + pi - qdi;
-        if (length(dq) > radius) p[i] = f4(normalize(dq) * radius + qdi - qni);
-    }
+// _ccd (system.py:368-391) sets ccd_step = 1; _line_search (:393-409) keeps the energy before the search.
+__global__ void k_before_ccd(SolverScalars* sc) {
+    if (sc->abort) return;
+    sc->ccd_step = 1.0f;
+    sc->energy_prev = sc->energy;
 }
 
 // accd_kernel (ccd_kernels.py:9-111): additive CCD step bound per contact
 __global__ void k_accd(const float4* __restrict__ x, const float4* __restrict__ vel, const int4* __restrict__ cidx,
                        const int2* __restrict__ ctype, SolverScalars* sc, float slackness, float thickness, int max_iters,
                        float ee_thres) {
+    if (sc->abort) return;
     const int n = sc->n_contacts;
     for (int b = gtid(); b < n; b += gstride()) {
         const int4 id = cidx[b];
@@ -1262,9 +1397,11 @@ __global__ void k_accd(const float4* __restrict__ x, const float4* __restrict__ 
     }
 }
 
-// line_search_kernel: q = q0 + ccd_step * 0.5^n * p unless an earlier step already lowered the energy
-__global__ void k_line_search(const float4* __restrict__ q0, const float4* __restrict__ p, const SolverScalars* sc, int n_halves,
-                              int np, float4* q) {
+// line_search_kernel (solver_kernels.py:52-66): q = q0 + ccd_step 0.5^n p unless a shorter step already
+// lowered the energy
+__global__ void k_line_search(const float4* __restrict__ q0, const float4* __restrict__ p, const SolverScalars* sc,
+                              int n_halves, int np, float4* q) {
+    if (sc->abort) return;
     if (n_halves > 0 && sc->energy < sc->energy_prev) return;
     const float a = sc->ccd_step * powf(0.5f, (float)n_halves);
     for (int i = gtid(); i < np; i += gstride()) {
@@ -1273,11 +1410,9 @@ __global__ void k_line_search(const float4* __restrict__ q0, const float4* __res
     }
 }
 
-__global__ void k_set_scalars(SolverScalars* sc, float ccd_step) { sc->ccd_step = ccd_step; }
-
-__global__ void k_copy_contact_count(SolverScalars* sc, int cap) {
-    const int n = sc->n_contacts_raw;
-    sc->n_contacts = n < cap ? n : cap;
+__global__ void k_iter_end(SolverScalars* sc) {
+    if (sc->abort) return;
+    sc->iters_done += 1;
 }
 
 }  // namespace
@@ -1286,64 +1421,81 @@ __global__ void k_copy_contact_count(SolverScalars* sc, int cap) {
 Stage3::~Stage3() { release(); }
 
 template <typename T>
-int Stage3::grow(T*& p, size_t& cap, size_t n) {
-    if (p && cap >= n) return PAMO_OK;
-    if (p) {
-        cudaStreamSynchronize(stream);
-        cudaFree(p);
-        p = nullptr;
+int Stage3::grow(T*& ptr, size_t& cap, size_t n) {
+    if (ptr && cap >= n) return PAMO_OK;
+    if (ptr) {
+        if (stream) cudaStreamSynchronize(stream);
+        cudaFree(ptr);
+        ptr = nullptr;
     }
-    if (cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+    drop_graph();
+    if (cudaMalloc((void**)&ptr, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
     cap = n;
     return PAMO_OK;
 }
 
+void Stage3::drop_graph() {
+    if (graph) cudaGraphExecDestroy(graph);
+    graph = nullptr;
+    graph_kernels = 0;
+}
+
 void Stage3::release() {
-    auto f = [](auto*& p) {
-        if (p) cudaFree(p);
-        p = nullptr;
+    if (stream) cudaStreamSynchronize(stream);
+    drop_graph();
+    auto f = [](auto*& ptr) {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
     };
-    f(gt_pos); f(gt_tri); f(gt_bvh_mem); f(gt_rc); f(q); f(q_rest); f(q_prev_newton); f(q_prev_det); f(p); f(target);
-    f(grad); f(hdiag); f(r); f(z); f(v); f(Av); f(vweight); f(tri); f(edge4); f(edge); f(el_area); f(el_invDm); f(hinge);
-    f(hinge_rest); f(hinge_blocks); f(c_idx); f(c_type); f(c_d); f(c_dd); f(e_elem); f(tri_bvh_mem); f(edge_bvh_mem);
-    f(tri_rc); f(edge_rc); f(sc); f(d_norm); f(scan_scratch);
+    f(gt_pos); f(gt_tri); f(gt_bvh_mem); f(gt_rc); f(q); f(q_rest); f(q_prev_newton); f(p); f(target);
+    f(grad); f(hdiag); f(r); f(z); f(v[0]); f(v[1]); f(Av); f(vweight); f(tri); f(edge4); f(el_area); f(el_invDm);
+    f(hinge); f(hinge_rest); f(hinge_blocks); f(c_idx); f(c_type); f(c_d); f(c_dd); f(partial); f(tri_bvh_mem);
+    f(edge_bvh_mem); f(tri_rc); f(edge_rc); f(sc); f(d_norm);
     if (h_sc) cudaFreeHost(h_sc);
     h_sc = nullptr;
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+    ev_in = ev_out = nullptr;
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
 }
 
 int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
     int rr;
-    size_t c1;
     if (!sc) {
+        if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return fail(PAMO_ERR_CUDA, "stream");
+        if (cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming) != cudaSuccess)
+            return fail(PAMO_ERR_CUDA, "event");
         if (cudaMalloc((void**)&sc, sizeof(SolverScalars)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
         if (cudaMallocHost((void**)&h_sc, sizeof(SolverScalars)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMallocHost");
         if (cudaMalloc((void**)&d_norm, 16 * sizeof(double)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
-        if (cudaMalloc((void**)&scan_scratch, (scan_scratch_ints() + 2 * kRedBlocks + 8) * sizeof(int)) != cudaSuccess)
-            return fail(PAMO_ERR_OOM, "cudaMalloc");
+        if (cudaMalloc((void**)&partial, kRedBlocks * sizeof(float2)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
         if (cudaMalloc((void**)&gt_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
         if (cudaMalloc((void**)&tri_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
         if (cudaMalloc((void**)&edge_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
     }
+    size_t c;
     if (cap_gp < (size_t)ngp + 2) {
-        c1 = cap_gp;
-        if ((rr = grow(gt_pos, c1, (size_t)ngp + 2))) return rr;
-        cap_gp = c1;
+        c = cap_gp;
+        if ((rr = grow(gt_pos, c, (size_t)ngp + 2))) return rr;
+        cap_gp = c;
     }
     if (cap_gt < (size_t)ngt + 2) {
-        c1 = cap_gt;
-        if ((rr = grow(gt_tri, c1, (size_t)ngt + 2))) return rr;
-        cap_gt = c1;
+        c = cap_gt;
+        if ((rr = grow(gt_tri, c, (size_t)ngt + 2))) return rr;
+        cap_gt = c;
     }
     if (gt_bvh_cap < (size_t)ngt + 2) {
         if (gt_bvh_mem) cudaFree(gt_bvh_mem);
+        gt_bvh_mem = nullptr;
         if (cudaMalloc((void**)&gt_bvh_mem, bvh_bytes(ngt + 2)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
         bvh_carve(gt_bvh, ngt + 2, gt_bvh_mem);
         gt_bvh_cap = (size_t)ngt + 2;
     }
     if (cap_v < (size_t)np + 2) {
         const size_t n = (size_t)np + 2;
-        size_t c;
-        for (float4** b : {&q, &q_rest, &q_prev_newton, &q_prev_det, &p, &target, &grad, &hdiag, &r, &z, &v, &Av}) {
+        for (float4** b : {&q, &q_rest, &q_prev_newton, &p, &target, &grad, &hdiag, &r, &z, &Av, &v[0], &v[1]}) {
             c = cap_v;
             if ((rr = grow(*b, c, n))) return rr;
         }
@@ -1353,7 +1505,7 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
     }
     if (cap_t < (size_t)nt + 2) {
         const size_t n = (size_t)nt + 2;
-        size_t c = cap_t;
+        c = cap_t;
         if ((rr = grow(tri, c, n))) return rr;
         c = cap_t;
         if ((rr = grow(el_area, c, n))) return rr;
@@ -1361,25 +1513,25 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
         if ((rr = grow(el_invDm, c, n))) return rr;
         cap_t = n;
         if (tri_bvh_mem) cudaFree(tri_bvh_mem);
+        tri_bvh_mem = nullptr;
         if (cudaMalloc((void**)&tri_bvh_mem, bvh_bytes((int)n)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
         bvh_carve(tri_bvh, (int)n, tri_bvh_mem);
         tri_bvh_cap = n;
     }
     if (cap_e < (size_t)ne + 2) {
         const size_t n = (size_t)ne + 2;
-        size_t c = cap_e;
-        if ((rr = grow(edge, c, n))) return rr;
         c = cap_e;
         if ((rr = grow(edge4, c, n))) return rr;
         cap_e = n;
         if (edge_bvh_mem) cudaFree(edge_bvh_mem);
+        edge_bvh_mem = nullptr;
         if (cudaMalloc((void**)&edge_bvh_mem, bvh_bytes((int)n)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
         bvh_carve(edge_bvh, (int)n, edge_bvh_mem);
         edge_bvh_cap = n;
     }
     if (cap_h < (size_t)nh + 2) {
         const size_t n = (size_t)nh + 2;
-        size_t c = cap_h;
+        c = cap_h;
         if ((rr = grow(hinge, c, n))) return rr;
         c = cap_h;
         if ((rr = grow(hinge_rest, c, n))) return rr;
@@ -1390,141 +1542,117 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
     return PAMO_OK;
 }
 
-void Stage3::compute_energy(const float4* x) {
-    cudaStream_t s = stream;
-    const Stage3Params& P = params;
-    const float mu = P.elas_young_modulus / (2.f * (1.f + P.elas_poisson_ratio));
-    const float la = P.elas_young_modulus * P.elas_poisson_ratio / ((1.f + P.elas_poisson_ratio) * (1.f - 2.f * P.elas_poisson_ratio));
-    float* e = e_elem;
-    const int base_c = NP + NT + NH;
-    k_energy_m2gt<<<grid_for(NP, kT), kT, 0, s>>>(x, target, vweight, P.mesh2gt_dist_stiffness, NP, e);
-    note_launch();
-    k_energy_elastic<<<grid_for(NT, kT), kT, 0, s>>>(x, tri, el_area, el_invDm, mu, la, NT, e + NP);
-    note_launch();
-    k_energy_hinge<<<grid_for(NH, kT), kT, 0, s>>>(x, hinge, hinge_rest, P.hinge_stiffness, NH, e + NP + NT);
-    note_launch();
-    k_energy_contact<<<grid_for(std::max(1, h_sc->n_contacts), kT), kT, 0, s>>>(x, c_idx, c_type, c_d, sc, P.coll_stiffness,
-                                                                               P.d_hat, P.ee_classify_thres, e + base_c);
-    note_launch();
-    float2* part = (float2*)(scan_scratch + scan_scratch_ints());
-    k_reduce<<<kRedBlocks, kT, 0, s>>>(e, &sc->n_contacts, base_c, part);
-    note_launch();
-    k_reduce_finish<<<1, kT, 0, s>>>(part, &sc->energy, nullptr);
-    note_launch();
-}
-
-void Stage3::compute_diff() {
-    cudaStream_t s = stream;
-    const Stage3Params& P = params;
-    const float mu = P.elas_young_modulus / (2.f * (1.f + P.elas_poisson_ratio));
-    const float la = P.elas_young_modulus * P.elas_poisson_ratio / ((1.f + P.elas_poisson_ratio) * (1.f - 2.f * P.elas_poisson_ratio));
-    cudaMemsetAsync(grad, 0, NP * sizeof(float4), s);
-    cudaMemsetAsync(hdiag, 0, NP * sizeof(float4), s);
-    k_diff_m2gt<<<grid_for(NP, kT), kT, 0, s>>>(q, target, vweight, P.mesh2gt_dist_stiffness, -1.f, NP, grad, hdiag);
-    note_launch();
-    k_diff_elastic<<<grid_for(NT, kT), kT, 0, s>>>(q, tri, el_area, el_invDm, mu, la, -1.f, NT, grad);
-    note_launch();
-    k_diff_hinge<<<grid_for(NH, 128), 128, 0, s>>>(q, hinge, hinge_rest, P.hinge_stiffness, -1.f, NH, hinge_blocks, grad, hdiag);
-    note_launch();
-    k_spd_project<<<grid_for(NH, 64), 64, 0, s>>>(hinge_blocks, NH, P.spd_max_iters);
-    note_launch();
-    k_diff_contact<<<grid_for(std::max(1, h_sc->n_contacts), kT), kT, 0, s>>>(q, c_idx, c_type, c_d, sc, P.coll_stiffness,
-                                                                             P.d_hat, -1.f, c_dd, grad, hdiag);
-    note_launch();
-}
-
-void Stage3::hess_dx(const float4* dx, float4* out) {
-    cudaStream_t s = stream;
-    const Stage3Params& P = params;
-    const float mu = P.elas_young_modulus / (2.f * (1.f + P.elas_poisson_ratio));
-    const float la = P.elas_young_modulus * P.elas_poisson_ratio / ((1.f + P.elas_poisson_ratio) * (1.f - 2.f * P.elas_poisson_ratio));
-    cudaMemsetAsync(out, 0, NP * sizeof(float4), s);
-    const long long total = (long long)NP + NT + NH + std::max(1, h_sc->n_contacts);
-    k_hvp<<<grid_for(total, kT), kT, 0, s>>>(q, dx, vweight, P.mesh2gt_dist_stiffness, NP, tri, el_area, el_invDm, mu, la, NT,
-                                             hinge, hinge_blocks, NH, c_idx, c_d, c_dd, sc, P.coll_stiffness, P.d_hat, out);
-    note_launch();
-}
-
-void Stage3::cg_solve() {
-    cudaStream_t s = stream;
-    float2* part = (float2*)(scan_scratch + scan_scratch_ints());
-    k_cg_init<<<grid_for(NP, kT), kT, 0, s>>>(grad, hdiag, NP, p, r, z, v);
-    note_launch();
-    k_reduce_dot<<<kRedBlocks, kT, 0, s>>>(z, r, NP, part);
-    note_launch();
-    k_reduce_finish<<<1, kT, 0, s>>>(part, &sc->z_r, nullptr);
-    note_launch();
-    for (int it = 0; it < params.n_cg_iters; ++it) {
-        hess_dx(v, Av);
-        k_reduce_dot<<<kRedBlocks, kT, 0, s>>>(v, Av, NP, part);
-        note_launch();
-        k_reduce_finish<<<1, kT, 0, s>>>(part, &sc->v_A_v, nullptr);
-        note_launch();
-        k_cg_prz<<<grid_for(NP, kT), kT, 0, s>>>(v, Av, hdiag, sc, NP, p, r, z);
-        note_launch();
-        k_reduce_dot<<<kRedBlocks, kT, 0, s>>>(z, r, NP, part);
-        note_launch();
-        k_reduce_finish<<<1, kT, 0, s>>>(part, &sc->z_r, &sc->z_r_last);  // z_r_last = old z_r
-        note_launch();
-        k_cg_v<<<grid_for(NP, kT), kT, 0, s>>>(z, sc, NP, v);
-        note_launch();
-    }
-}
-
-int Stage3::detect_contacts(float radius) {
-    cudaStream_t s = stream;
-    const float thr = 2.0f * radius + params.d_hat;
-    // LBVHs of the current triangles and edges (boxes without margin; the query box carries the threshold)
-    RoundCounters h{};
-    h.n_pts = NP;
-    h.n_tris = NT;
-    cudaMemcpyAsync(tri_rc, &h, sizeof(h), cudaMemcpyHostToDevice, s);
-    h.n_tris = NE;
-    cudaMemcpyAsync(edge_rc, &h, sizeof(h), cudaMemcpyHostToDevice, s);
-    bvh_build(tri_bvh, tri, q, tri_rc, NT, s);
-    bvh_build(edge_bvh, edge4, q, edge_rc, NE, s);
-    for (int attempt = 0; attempt < 8; ++attempt) {
-        const int cap = (int)std::min<size_t>(cap_c, (size_t)params.max_blocks);
-        cudaMemsetAsync(&sc->n_contacts_raw, 0, sizeof(int), s);
-        k_detect<false><<<grid_for(NP, kQT, 16), kQT, 0, s>>>(q, NP, tri, tri_bvh.child, tri_bvh.nlo, tri_bvh.nhi, tri_bvh.llo,
-                                                             tri_bvh.lhi, tri_bvh.vals[0], tri_rc, thr,
-                                                             params.ee_classify_thres, c_idx, c_type, cap, sc);
-        note_launch();
-        k_detect<true><<<grid_for(NE, kQT, 16), kQT, 0, s>>>(q, NE, edge4, edge_bvh.child, edge_bvh.nlo, edge_bvh.nhi,
-                                                            edge_bvh.llo, edge_bvh.lhi, edge_bvh.vals[0], edge_rc, thr,
-                                                            params.ee_classify_thres, c_idx, c_type, cap, sc);
-        note_launch();
-        k_copy_contact_count<<<1, 1, 0, s>>>(sc, cap);
-        note_launch();
-        cudaMemcpyAsync(h_sc, sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
-        const long long raw = h_sc->n_contacts_raw;
-        if (raw > params.max_blocks) return -1;  // caller halves the radius (energy.py:942-948)
-        if (raw <= (long long)cap_c) break;
-        // grow the contact arrays and detect again (capacity only; the reference's limit is max_blocks)
-        const size_t n = (size_t)raw + raw / 2 + 1024;
-        size_t c = cap_c;
-        int rr;
-        if ((rr = grow(c_idx, c, n))) return rr;
-        c = cap_c;
-        if ((rr = grow(c_type, c, n))) return rr;
-        c = cap_c;
-        if ((rr = grow(c_d, c, n))) return rr;
-        c = cap_c;
-        if ((rr = grow(c_dd, c, 4 * n))) return rr;
-        cap_c = n;
-        c = cap_el;
-        if ((rr = grow(e_elem, c, (size_t)NP + NT + NH + n + 8))) return rr;
-        cap_el = c;
-    }
-    stats.max_contacts = std::max(stats.max_contacts, h_sc->n_contacts);
-    stats.total_contacts += h_sc->n_contacts;
+int Stage3::ensure_contacts(size_t n) {
+    if (cap_c >= n && c_idx) return PAMO_OK;
+    size_t c;
+    int rr;
+    c = 0;
+    if (c_idx) cudaStreamSynchronize(stream);
+    cudaFree(c_idx); cudaFree(c_type); cudaFree(c_d); cudaFree(c_dd);
+    c_idx = nullptr; c_type = nullptr; c_d = nullptr; c_dd = nullptr;
+    if ((rr = grow(c_idx, c, n))) return rr;
+    c = 0;
+    if ((rr = grow(c_type, c, n))) return rr;
+    c = 0;
+    if ((rr = grow(c_d, c, n))) return rr;
+    c = 0;
+    if ((rr = grow(c_dd, c, 4 * n))) return rr;
+    cap_c = n;
+    drop_graph();
     return PAMO_OK;
 }
 
+void Stage3::launch_energy(const float4* x) {
+    const Stage3Params& P = params;
+    EnergyArgs A;
+    A.tgt = target; A.w = vweight; A.m2gt_k = P.mesh2gt_dist_stiffness; A.np = NP;
+    A.tri = tri; A.area = el_area; A.invDm = el_invDm;
+    A.mu = P.elas_young_modulus / (2.f * (1.f + P.elas_poisson_ratio));
+    A.la = P.elas_young_modulus * P.elas_poisson_ratio / ((1.f + P.elas_poisson_ratio) * (1.f - 2.f * P.elas_poisson_ratio));
+    A.nt = NT; A.hinge = hinge; A.rest = hinge_rest; A.hinge_k = P.hinge_stiffness; A.nh = NH;
+    A.cidx = c_idx; A.ctype = c_type; A.cd = c_d; A.kappa = P.coll_stiffness; A.d_hat = P.d_hat;
+    A.ee_thres = P.ee_classify_thres;
+    const long long total = (long long)NP + NT + NH + (long long)cap_c;
+    const int g = (int)std::min<long long>(kRedBlocks, (total + kT - 1) / kT);
+    k_energy<<<g, kT, 0, stream>>>(x, A, sc, partial);
+    note_launch();
+}
+
+void Stage3::newton_iteration() {
+    cudaStream_t s = stream;
+    const Stage3Params& P = params;
+    const float mu = P.elas_young_modulus / (2.f * (1.f + P.elas_poisson_ratio));
+    const float la = P.elas_young_modulus * P.elas_poisson_ratio / ((1.f + P.elas_poisson_ratio) * (1.f - 2.f * P.elas_poisson_ratio));
+    const int gC = grid_for((long long)cap_c, kT);
+    // q_prev_newton = q; contacts at q (system.py:425-432, _detect_contact :308-318 with refitted LBVHs)
+    k_iter_begin<<<grid_for(NP, kT), kT, 0, s>>>(q, q_prev_newton, grad, hdiag, NP, sc);
+    note_launch();
+    bvh_refit(tri_bvh, tri, q, tri_rc, NT, s);
+    bvh_refit(edge_bvh, edge4, q, edge_rc, NE, s);
+    const int cap = (int)std::min<size_t>(cap_c, (size_t)P.max_blocks);
+    k_detect<false><<<grid_for(NP, kQT, 16), kQT, 0, s>>>(q, NP, tri, tri_bvh.child, tri_bvh.nlo, tri_bvh.nhi, tri_bvh.llo,
+                                                         tri_bvh.lhi, tri_bvh.vals[0], tri_rc, P.d_hat,
+                                                         P.ee_classify_thres, c_idx, c_type, cap, sc);
+    note_launch();
+    k_detect<true><<<grid_for(NE, kQT, 16), kQT, 0, s>>>(q, NE, edge4, edge_bvh.child, edge_bvh.nlo, edge_bvh.nhi,
+                                                        edge_bvh.llo, edge_bvh.lhi, edge_bvh.vals[0], edge_rc, P.d_hat,
+                                                        P.ee_classify_thres, c_idx, c_type, cap, sc);
+    note_launch();
+    k_contacts_done<<<1, 1, 0, s>>>(sc, cap, P.max_blocks);
+    note_launch();
+    // energy, gradient (coeff -1), Hessian diagonal and hinge blocks (system.py:433-434)
+    launch_energy(q);
+    k_diff_m2gt<<<grid_for(NP, kT), kT, 0, s>>>(q, target, vweight, P.mesh2gt_dist_stiffness, -1.f, NP, grad, hdiag, sc);
+    note_launch();
+    k_diff_elastic<<<grid_for(NT, kT), kT, 0, s>>>(q, tri, el_area, el_invDm, mu, la, -1.f, NT, grad, sc);
+    note_launch();
+    if (NH) {
+        k_diff_hinge<<<grid_for(NH, 128), 128, 0, s>>>(q, hinge, hinge_rest, P.hinge_stiffness, -1.f, NH, hinge_blocks,
+                                                       grad, hdiag, sc);
+        note_launch();
+        k_spd_project<<<grid_for(NH, 64), 64, 0, s>>>(hinge_blocks, NH, P.spd_max_iters, sc);
+        note_launch();
+    }
+    k_diff_contact<<<gC, kT, 0, s>>>(q, c_idx, c_type, c_d, sc, P.coll_stiffness, P.d_hat, -1.f, c_dd, grad, hdiag);
+    note_launch();
+    // Jacobi PCG (cg_solver.py:96-158)
+    HvpArgs H;
+    H.w = vweight; H.m2gt_k = P.mesh2gt_dist_stiffness; H.np = NP;
+    H.tri = tri; H.area = el_area; H.invDm = el_invDm; H.mu = mu; H.la = la; H.nt = NT;
+    H.hinge = hinge; H.blocks = hinge_blocks; H.nh = NH;
+    H.cidx = c_idx; H.cd = c_d; H.cdd = c_dd; H.kappa = P.coll_stiffness; H.d_hat = P.d_hat;
+    const int gV = (int)std::min<long long>(kRedBlocks, ((long long)NP + kT - 1) / kT);
+    const long long total = (long long)NP + NT + NH + (long long)cap_c;
+    const int gH = (int)std::min<long long>(kRedBlocks, (total + kT - 1) / kT);
+    k_cg_init<<<gV, kT, 0, s>>>(grad, hdiag, NP, p, r, z, v[0], Av, sc, partial);
+    note_launch();
+    for (int it = 0; it < P.n_cg_iters; ++it) {
+        float4* vin = v[it & 1];
+        float4* vout = v[(it + 1) & 1];
+        k_cg_hvp<<<gH, kT, 0, s>>>(q, H, z, vin, vout, Av, it == 0 ? 1 : 0, sc, partial);
+        note_launch();
+        k_cg_prz<<<gV, kT, 0, s>>>(vout, Av, hdiag, NP, p, r, z, sc, partial);
+        note_launch();
+    }
+    // step clamp, CCD, line search (system.py:441-459)
+    k_clamp_p<<<grid_for(NP, kT), kT, 0, s>>>(p, q_prev_newton, P.contact_detection_radius, NP, sc);
+    note_launch();
+    k_before_ccd<<<1, 1, 0, s>>>(sc);
+    note_launch();
+    k_accd<<<gC, kT, 0, s>>>(q, p, c_idx, c_type, sc, P.ccd_slackness, P.ccd_thickness, P.ccd_max_iters,
+                            P.ee_classify_thres);
+    note_launch();
+    for (int n = 0; n < P.n_line_search_iters; ++n) {
+        k_line_search<<<grid_for(NP, kT), kT, 0, s>>>(q_prev_newton, p, sc, n, NP, q);
+        note_launch();
+        launch_energy(q);
+    }
+    k_iter_end<<<1, 1, 0, s>>>(sc);
+    note_launch();
+}
+
 int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, int n_gt_tris, const double* points,
-                const int* tris, int n_points, int n_tris, int n_iters, double* out_points, cudaStream_t s) {
-    stream = s;
+                const int* tris, int n_points, int n_tris, int n_iters, double* out_points, cudaStream_t caller) {
     err.clear();
     stats = Stage3Stats{};
     if (n_points < 3 || n_tris < 1 || n_gt_points < 3 || n_gt_tris < 1) return fail(PAMO_ERR_INVALID_ARG, "empty mesh");
@@ -1551,7 +1679,7 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     std::sort(ukeys.begin(), ukeys.end());
     ukeys.erase(std::unique(ukeys.begin(), ukeys.end()), ukeys.end());
     std::sort(dkeys.begin(), dkeys.end());
-    std::vector<int> h_hinges;
+    std::vector<int4> h4;
     for (int f = 0; f < n_tris; ++f)
         for (int k = 0; k < 3; ++k) {
             const int a = hf[3 * f + k], b = hf[3 * f + (k + 1) % 3], c = hf[3 * f + (k + 2) % 3];
@@ -1560,16 +1688,13 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
             auto it = std::lower_bound(dkeys.begin(), dkeys.end(), std::make_pair(key, -1));
             for (; it != dkeys.end() && it->first == key; ++it) {
                 const int f1 = it->second / 3, k1 = it->second % 3;
-                h_hinges.push_back(c);
-                h_hinges.push_back(a);
-                h_hinges.push_back(b);
-                h_hinges.push_back(hf[3 * f1 + (k1 + 2) % 3]);
+                h4.push_back(make_int4(c, a, b, hf[3 * f1 + (k1 + 2) % 3]));
             }
         }
     NP = n_points;
     NT = n_tris;
     NE = (int)ukeys.size();
-    NH = (int)(h_hinges.size() / 4);
+    NH = (int)h4.size();
     NGP = n_gt_points;
     NGT = n_gt_tris;
     stats.n_particles = NP;
@@ -1577,35 +1702,18 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     stats.n_edges = NE;
     stats.n_hinges = NH;
     int rr;
+    drop_graph();  // kernel arguments of a captured iteration (sizes, coefficients) belong to one call
     if ((rr = ensure(NP, NT, NE, NH, NGP, NGT))) return rr;
-    if (cap_c == 0) {
-        const size_t n = std::max<size_t>(1 << 16, (size_t)32 * (NP + NE));
-        size_t c = 0;
-        if ((rr = grow(c_idx, c, n))) return rr;
-        c = 0;
-        if ((rr = grow(c_type, c, n))) return rr;
-        c = 0;
-        if ((rr = grow(c_d, c, n))) return rr;
-        c = 0;
-        if ((rr = grow(c_dd, c, 4 * n))) return rr;
-        cap_c = n;
-    }
-    {
-        size_t c = cap_el;
-        if ((rr = grow(e_elem, c, (size_t)NP + NT + NH + cap_c + 8))) return rr;
-        cap_el = c;
-    }
+    if ((rr = ensure_contacts(std::max<size_t>(std::max<size_t>(1 << 16, cap_c), (size_t)32 * (NP + NE))))) return rr;
+    cudaStream_t s = stream;
+    cudaEventRecord(ev_in, caller);
+    cudaStreamWaitEvent(s, ev_in, 0);
     std::vector<int4> e4(NE);
-    std::vector<int2> e2(NE);
     for (int e = 0; e < NE; ++e) {
-        const int u = (int)(ukeys[e] % n_points), v = (int)(ukeys[e] / n_points);
-        e4[e] = make_int4(u, v, v, 0);
-        e2[e] = make_int2(u, v);
+        const int u = (int)(ukeys[e] % n_points), w = (int)(ukeys[e] / n_points);
+        e4[e] = make_int4(u, w, w, 0);
     }
-    std::vector<int4> h4(NH);
-    for (int h = 0; h < NH; ++h) h4[h] = make_int4(h_hinges[4 * h], h_hinges[4 * h + 1], h_hinges[4 * h + 2], h_hinges[4 * h + 3]);
     cudaMemcpyAsync(edge4, e4.data(), NE * sizeof(int4), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(edge, e2.data(), NE * sizeof(int2), cudaMemcpyHostToDevice, s);
     if (NH) cudaMemcpyAsync(hinge, h4.data(), NH * sizeof(int4), cudaMemcpyHostToDevice, s);
 
     // normalisation (processing.py:15-21, 57-59)
@@ -1613,7 +1721,9 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     note_launch();
     k_normalize<<<grid_for(NGP, kT), kT, 0, s>>>(gt_points, NGP, d_norm, gt_pos, nullptr);
     note_launch();
-    cudaMemsetAsync(sc, 0, sizeof(SolverScalars), s);
+    std::memset(h_sc, 0, sizeof(SolverScalars));
+    h_sc->radius = params.contact_detection_radius;
+    cudaMemcpyAsync(sc, h_sc, sizeof(SolverScalars), cudaMemcpyHostToDevice, s);
     k_tris4<<<grid_for(NGT, kT), kT, 0, s>>>(gt_tris, NGT, NGP, gt_tri, &sc->status);
     note_launch();
     k_normalize<<<grid_for(NP, kT), kT, 0, s>>>(points, NP, d_norm, q, q_rest);
@@ -1623,13 +1733,20 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     cudaMemcpyAsync(h_sc, sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
     if (h_sc->status & 1) return fail(PAMO_ERR_INVALID_ARG, "GT triangle index out of range");
-    // GT LBVH (built once: the GT mesh does not move)
+    // LBVHs: the GT mesh (static) and the simulated triangles and edges (refitted at every detection)
     {
         RoundCounters h{};
         h.n_pts = NGP;
         h.n_tris = NGT;
         cudaMemcpyAsync(gt_rc, &h, sizeof(h), cudaMemcpyHostToDevice, s);
         bvh_build(gt_bvh, gt_tri, gt_pos, gt_rc, NGT, s);
+        h.n_pts = NP;
+        h.n_tris = NT;
+        cudaMemcpyAsync(tri_rc, &h, sizeof(h), cudaMemcpyHostToDevice, s);
+        bvh_build(tri_bvh, tri, q, tri_rc, NT, s);
+        h.n_tris = NE;
+        cudaMemcpyAsync(edge_rc, &h, sizeof(h), cudaMemcpyHostToDevice, s);
+        bvh_build(edge_bvh, edge4, q, edge_rc, NE, s);
     }
     // register_mesh preprocessing (system.py:167-272): Voronoi areas, elastic rest shape, hinge rest state,
     // minimum internal angle
@@ -1650,10 +1767,28 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     cudaMemcpyAsync(h_sc, sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
     stats.do_nothing = (h_sc->accepted == 1);  // some angle <= threshold and none NaN (system.py:214-221)
-    cudaMemsetAsync(&sc->accepted, 0, sizeof(int), s);
 
-    float radius = params.contact_detection_radius;
-    if (!stats.do_nothing) {
+    if (!stats.do_nothing && n_iters > 0) {
+        const int per_step = params.n_newton_iters;
+        auto capture = [&]() -> int {
+            drop_graph();
+            cudaGraph_t g = nullptr;
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+                return fail(PAMO_ERR_CUDA, "stream capture");
+            const long long l0 = launches_so_far();
+            newton_iteration();
+            graph_kernels = launches_so_far() - l0;
+            note_launches(-graph_kernels);  // counted when the graph runs
+            if (cudaStreamEndCapture(s, &g) != cudaSuccess || !g) return fail(PAMO_ERR_CUDA, "stream capture");
+            const cudaError_t e = cudaGraphInstantiate(&graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                graph = nullptr;
+                return fail(PAMO_ERR_CUDA, "graph instantiation");
+            }
+            return PAMO_OK;
+        };
+        int done = 0;
         for (int step = 0; step < n_iters; ++step) {
             ++stats.steps;
             // _update_vertex_target: closest points on the GT surface
@@ -1661,44 +1796,47 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
                                                               gt_bvh.lhi, gt_bvh.vals[0], gt_tri, gt_pos, gt_rc, target,
                                                               &sc->status);
             note_launch();
-            for (int it = 0; it < params.n_newton_iters; ++it) {
-                ++stats.newton_iters;
-                cudaMemcpyAsync(q_prev_newton, q, NP * sizeof(float4), cudaMemcpyDeviceToDevice, s);
-                int d;
-                while ((d = detect_contacts(radius)) == -1) {
-                    radius *= 0.5f;  // too many contacts: halve the detection radius and retry
+            const int goal = (step + 1) * per_step;
+            for (int guard = 0;; ++guard) {
+                if (guard > 64) return fail(PAMO_ERR_CAPACITY, "contact list did not settle");
+                for (int k = done; k < goal; ++k) {
+                    if (use_graph) {
+                        if (!graph && (rr = capture())) return rr;
+                        if (cudaGraphLaunch(graph, s) != cudaSuccess) return fail(PAMO_ERR_CUDA, "graph launch");
+                        note_launches(graph_kernels);
+                    } else {
+                        newton_iteration();
+                    }
+                }
+                cudaMemcpyAsync(h_sc, sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, s);
+                if (cudaStreamSynchronize(s) != cudaSuccess)
+                    return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+                done = h_sc->iters_done;
+                if (h_sc->abort == 0) break;
+                if (h_sc->abort == 2) {
+                    // too many contacts: halve the detection radius and detect again (energy.py:942-948)
                     if (++stats.radius_halvings > 40) return fail(PAMO_ERR_CAPACITY, "contacts exceed max_blocks");
+                    const float rad = h_sc->radius * 0.5f;
+                    cudaMemcpyAsync(&sc->radius, &rad, sizeof(float), cudaMemcpyHostToDevice, s);
+                } else {
+                    const size_t raw = (size_t)h_sc->n_contacts_raw;
+                    if ((rr = ensure_contacts(raw + raw / 2 + 1024))) return rr;
                 }
-                if (d) return d;
-                cudaMemcpyAsync(q_prev_det, q, NP * sizeof(float4), cudaMemcpyDeviceToDevice, s);
-                compute_energy(q);
-                compute_diff();
-                cg_solve();
-                k_clamp_p<<<grid_for(NP, kT), kT, 0, s>>>(p, q_prev_newton, q_prev_det, params.contact_detection_radius,
-                                                          NP);
-                note_launch();
-                k_set_scalars<<<1, 1, 0, s>>>(sc, 1.0f);
-                note_launch();
-                k_accd<<<grid_for(std::max(1, h_sc->n_contacts), kT), kT, 0, s>>>(q, p, c_idx, c_type, sc, params.ccd_slackness,
-                                                                                 params.ccd_thickness, params.ccd_max_iters,
-                                                                                 params.ee_classify_thres);
-                note_launch();
-                // line search (system.py:394-409)
-                cudaMemcpyAsync(&sc->energy_prev, &sc->energy, sizeof(float), cudaMemcpyDeviceToDevice, s);
-                for (int n = 0; n < params.n_line_search_iters; ++n) {
-                    k_line_search<<<grid_for(NP, kT), kT, 0, s>>>(q_prev_newton, p, sc, n, NP, q);
-                    note_launch();
-                    compute_energy(q);
-                }
+                cudaMemsetAsync(&sc->abort, 0, sizeof(int), s);
             }
         }
+        stats.newton_iters = done;
     }
     k_denormalize<<<grid_for(NP, kT), kT, 0, s>>>(q, NP, d_norm, out_points);
     note_launch();
     cudaMemcpyAsync(h_sc, sc, sizeof(SolverScalars), cudaMemcpyDeviceToHost, s);
+    cudaEventRecord(ev_out, s);
+    cudaStreamWaitEvent(caller, ev_out, 0);
     if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
     if (h_sc->status & 6) return fail(PAMO_ERR_ITER_LIMIT, "BVH traversal limit in stage 3");
     stats.last_energy = h_sc->energy;
+    stats.max_contacts = h_sc->max_contacts;
+    stats.total_contacts = h_sc->total_contacts;
     return PAMO_OK;
 }
 
@@ -1756,6 +1894,7 @@ int pamo_stage3_set_param(pamo_stage3* s, const char* name, double value) {
     else if (n == "mesh2gt_dist_stiffness") P.mesh2gt_dist_stiffness = (float)value;
     else if (n == "min_angle_thres") P.min_angle_thres = (float)value;
     else if (n == "max_blocks") P.max_blocks = (long long)value;
+    else if (n == "use_cuda_graph") s->solver.use_graph = value != 0.0;
     else {
         s->solver.err = "unknown stage-3 parameter: " + n;
         return PAMO_ERR_INVALID_ARG;

@@ -34,12 +34,18 @@ struct Stage3Params {
     long long max_blocks = 1ll << 25;
 };
 
-// Device scalars of the solver (one struct so that graph nodes can read them by pointer).
+// Device scalars of the solver. Kernels of a Newton iteration read their sizes and coefficients from here,
+// so that one captured CUDA graph serves every iteration of a run.
 struct SolverScalars {
     float energy, energy_prev, v_A_v, z_r, z_r_last, ccd_step;
+    float radius;         // contact detection radius (halved when contacts exceed max_blocks)
+    float pad0;
     int n_contacts, n_contacts_raw, accepted, status;
-    double energy_acc[2];  // compensated accumulator (sum, correction) while reducing
-    float pad[4];
+    int abort;            // 0 running; 1 contact list full (grow, redo the iteration); 2 above max_blocks (halve)
+    int iters_done;       // Newton iterations completed in this run
+    int red_count;        // arrival counter of the grid-wide sums
+    int max_contacts;
+    long long total_contacts;
 };
 
 struct Stage3Stats {
@@ -61,6 +67,7 @@ public:
     Stage3Params params;
     Stage3Stats stats;
     std::string err;
+    bool use_graph = true;  // capture one Newton iteration as a CUDA graph and replay it
 
 private:
     template <typename T>
@@ -70,12 +77,14 @@ private:
         return code;
     }
     int ensure(int np, int nt, int ne, int nh, int ngp, int ngt);
+    int ensure_contacts(size_t n);
     void release();
+    void drop_graph();
 
     // problem sizes
     int NP = 0, NT = 0, NE = 0, NH = 0, NGP = 0, NGT = 0;
     // capacities
-    size_t cap_v = 0, cap_t = 0, cap_e = 0, cap_h = 0, cap_gp = 0, cap_gt = 0, cap_c = 0, cap_el = 0;
+    size_t cap_v = 0, cap_t = 0, cap_e = 0, cap_h = 0, cap_gp = 0, cap_gt = 0, cap_c = 0;
     // GT mesh and its LBVH
     float4* gt_pos = nullptr;
     int4* gt_tri = nullptr;
@@ -84,12 +93,12 @@ private:
     size_t gt_bvh_cap = 0;
     RoundCounters* gt_rc = nullptr;
     // simulated mesh
-    float4 *q = nullptr, *q_rest = nullptr, *q_prev_newton = nullptr, *q_prev_det = nullptr, *p = nullptr;
-    float4 *target = nullptr, *grad = nullptr, *hdiag = nullptr, *r = nullptr, *z = nullptr, *v = nullptr, *Av = nullptr;
+    float4 *q = nullptr, *q_rest = nullptr, *q_prev_newton = nullptr, *p = nullptr;
+    float4 *target = nullptr, *grad = nullptr, *hdiag = nullptr, *r = nullptr, *z = nullptr, *Av = nullptr;
+    float4* v[2] = {nullptr, nullptr};  // CG search directions, ping-pong
     float* vweight = nullptr;  // Voronoi area
     int4* tri = nullptr;
     int4* edge4 = nullptr;     // edges as (u, v, v, 0) for the edge LBVH
-    int2* edge = nullptr;
     float* el_area = nullptr;
     float4* el_invDm = nullptr;
     int4* hinge = nullptr;
@@ -100,9 +109,8 @@ private:
     int2* c_type = nullptr;
     float* c_d = nullptr;
     float4* c_dd = nullptr;    // 4 per contact
-    // per-element energies for the deterministic reduction
-    float* e_elem = nullptr;
-    // LBVHs over the current triangles and edges
+    float2* partial = nullptr;  // block partials of the grid-wide sums
+    // LBVHs over the current triangles and edges (built at registration, refitted at every detection)
     BvhBuffers tri_bvh{}, edge_bvh{};
     char *tri_bvh_mem = nullptr, *edge_bvh_mem = nullptr;
     size_t tri_bvh_cap = 0, edge_bvh_cap = 0;
@@ -110,14 +118,15 @@ private:
     SolverScalars* sc = nullptr;
     SolverScalars* h_sc = nullptr;
     double* d_norm = nullptr;  // [0..2] centre, [3] scale, [4..] scratch
-    int* scan_scratch = nullptr;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;  // private stream the solver runs on (capturable)
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    // captured Newton iteration
+    cudaGraphExec_t graph = nullptr;
+    long long graph_kernels = 0;
+    int graph_key[6] = {0, 0, 0, 0, 0, 0};
 
-    int detect_contacts(float radius);
-    void compute_energy(const float4* x);
-    void compute_diff();
-    void cg_solve();
-    void hess_dx(const float4* dx, float4* out);
+    void newton_iteration();  // enqueue one Newton iteration (system.py:425-459)
+    void launch_energy(const float4* x);
 };
 
 }  // namespace pamo

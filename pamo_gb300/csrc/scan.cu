@@ -10,6 +10,7 @@ namespace pamo {
 
 static std::atomic<long long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 
 namespace {
