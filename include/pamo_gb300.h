@@ -1,6 +1,6 @@
 /*
- * pamo_gb300 — C ABI of the GB300-native PaMO stage-2 simplifier (parallel QEM edge collapse with LBVH
- * self-intersection rollback).
+ * pamo_gb300 — C ABI of the GB300-native PaMO simplifier: stage 2 (parallel QEM edge collapse with LBVH
+ * self-intersection rollback) and stage 3 (barrier/CCD Newton-CG safe projection onto the input mesh).
  *
  * Every pointer argument named points/triangles/verts/tris/verts_* is a DEVICE pointer on the context's
  * GPU unless stated otherwise; sizes are element counts (points = rows of 3 float32, triangles = rows of 3
@@ -159,7 +159,8 @@ int pamo_safe_project(pamo_stage3* s, const double* gt_points, const int32_t* gt
 
 /* Diagnostics of the last pamo_safe_project call, out[0..n): particles, triangles, edges, hinges, steps,
  * Newton iterations, most contacts in one detection, detection-radius halvings, do-nothing flag, final
- * energy, contacts summed over detections. Returns 11. No reference counterpart (the reference logs these). */
+ * energy, contacts summed over detections, rebuilds of the contact candidate lists. Returns 12. No reference
+ * counterpart (the reference logs these). */
 int pamo_stage3_stats(const pamo_stage3* s, double* out, int32_t n);
 
 #ifdef __cplusplus

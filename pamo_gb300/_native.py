@@ -60,7 +60,7 @@ SIGNATURES = {
 }
 
 STAGE3_STATS = ["particles", "triangles", "edges", "hinges", "steps", "newton_iters", "max_contacts",
-                "radius_halvings", "do_nothing", "energy", "total_contacts"]
+                "radius_halvings", "do_nothing", "energy", "total_contacts", "candidate_rebuilds"]
 
 RUN_TOTALS = ["vertices", "faces", "edges", "winners", "query_tests", "pairs", "exact_pairs", "checks", "live_indexed",
               "collapsed"]

@@ -240,7 +240,8 @@ __global__ void __launch_bounds__(256) k_karras(const RoundCounters* rc, const u
 
 __global__ void __launch_bounds__(256) k_bottom_up(RoundCounters* rc, const int2* child, const int* iparent,
                                                     const int* lparent, const float4* llo, const float4* lhi,
-                                                    float4* nlo, float4* nhi, int* visit) {
+                                                    float4* nlo, float4* nhi, int* visit, const int* active = nullptr) {
+    if (active && *active == 0) return;
     const int n = rc->n_live;
     for (int i = gtid(); i < n; i += gstride()) {
         int p = lparent[i];
@@ -478,7 +479,8 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
 
 __global__ void __launch_bounds__(256) k_refit_leaves(const RoundCounters* rc, const int4* __restrict__ tri,
                                                       const float4* __restrict__ pos, const int* __restrict__ vals,
-                                                      float4* llo, float4* lhi, int* visit) {
+                                                      float4* llo, float4* lhi, int* visit, const int* active) {
+    if (active && *active == 0) return;
     const int n = rc->n_live;
     for (int i = gtid(); i < n; i += gstride()) {
         const int4 t = tri[vals[i]];
@@ -489,10 +491,12 @@ __global__ void __launch_bounds__(256) k_refit_leaves(const RoundCounters* rc, c
     }
 }
 
-void bvh_refit(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s) {
+void bvh_refit(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s,
+               const int* active) {
     const int gF = grid_for(n_tris_bound, 256);
-    k_refit_leaves<<<gF, 256, 0, s>>>(rc, tri, pos, b.vals[0], b.llo, b.lhi, b.visit); note_launch();
-    k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit); note_launch();
+    k_refit_leaves<<<gF, 256, 0, s>>>(rc, tri, pos, b.vals[0], b.llo, b.lhi, b.visit, active); note_launch();
+    k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit, active);
+    note_launch();
 }
 
 void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, const int* qscan,

@@ -33,8 +33,10 @@ void bvh_carve(BvhBuffers& b, int cap, char* base);
 void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s);
 
 // Recomputes the leaf and node boxes of a tree built by bvh_build over the same faces after the positions
-// moved (same topology and leaf order; the tree may bound more loosely than a rebuilt one).
-void bvh_refit(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s);
+// moved (same topology and leaf order; the tree may bound more loosely than a rebuilt one). With `active`,
+// the kernels do nothing unless *active != 0 (a device flag, so the call can sit in a captured graph).
+void bvh_refit(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s,
+               const int* active = nullptr);
 
 // For every face in the query list that is still live: hit[f] = 1 iff some live face g != f with an
 // overlapping closed AABB makes the reference's pair test true in either order. Query faces are taken

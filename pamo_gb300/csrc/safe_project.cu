@@ -18,6 +18,8 @@
 #include <numeric>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "../../include/pamo_gb300.h"
 #include "safe_project.cuh"
 #include "scan.cuh"
@@ -28,6 +30,7 @@ namespace {
 
 constexpr int kT = 256;
 constexpr int kRedBlocks = 256;
+constexpr int kPartials = 4096;  // >= 2 x the largest cooperative grid
 constexpr int kQT = 128;
 constexpr int kStack = 64;
 
@@ -375,51 +378,73 @@ __device__ void grid_sum_finish(CSum acc, float2* partial, int* counter, float* 
 }
 
 // ------------------------------------------------------------------ set-up kernels
-// normalisation of processing.py:15-21: centre = mean of the GT vertices, scale = 1 / max extent (float64)
-__global__ void k_norm_stats(const double* __restrict__ gt, int n, double* stats) {
-    // one block: fixed-order float64 sums and extents
-    __shared__ double sh[6][kT];
+// normalisation of processing.py:15-21: centre = mean of the GT vertices, scale = 1 / max extent (float64).
+// Two passes with a fixed summation order: per-block sums, minima and maxima of contiguous chunks, then one
+// block combines them in block order.
+constexpr int kNormBlocks = 4 * 152;
+
+__global__ void __launch_bounds__(kT) k_norm_partial(const double* __restrict__ gt, int n, double* part) {
+    __shared__ double sh[9][kT];
+    const long long chunk = ((long long)n + gridDim.x - 1) / gridDim.x;
+    const long long lo = chunk * blockIdx.x, hi = min((long long)n, lo + chunk);
     double s[3] = {0, 0, 0}, mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x)
         for (int d = 0; d < 3; ++d) {
-            const double x = (double)gt[3 * i + d];
+            const double x = gt[3 * i + d];
             s[d] += x;
             mn[d] = fmin(mn[d], x);
             mx[d] = fmax(mx[d], x);
         }
     for (int d = 0; d < 3; ++d) {
         sh[d][threadIdx.x] = s[d];
-        sh[3 + d][threadIdx.x] = 0;
-    }
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o)
-            for (int d = 0; d < 3; ++d) sh[d][threadIdx.x] += sh[d][threadIdx.x + o];
-        __syncthreads();
-    }
-    double c[3];
-    for (int d = 0; d < 3; ++d) c[d] = sh[d][0] / (double)n;
-    __syncthreads();
-    for (int d = 0; d < 3; ++d) {
-        sh[d][threadIdx.x] = mn[d];
-        sh[3 + d][threadIdx.x] = mx[d];
+        sh[3 + d][threadIdx.x] = mn[d];
+        sh[6 + d][threadIdx.x] = mx[d];
     }
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
         if ((int)threadIdx.x < o)
             for (int d = 0; d < 3; ++d) {
-                sh[d][threadIdx.x] = fmin(sh[d][threadIdx.x], sh[d][threadIdx.x + o]);
-                sh[3 + d][threadIdx.x] = fmax(sh[3 + d][threadIdx.x], sh[3 + d][threadIdx.x + o]);
+                sh[d][threadIdx.x] += sh[d][threadIdx.x + o];
+                sh[3 + d][threadIdx.x] = fmin(sh[3 + d][threadIdx.x], sh[3 + d][threadIdx.x + o]);
+                sh[6 + d][threadIdx.x] = fmax(sh[6 + d][threadIdx.x], sh[6 + d][threadIdx.x + o]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x < 9) part[(size_t)blockIdx.x * 9 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void __launch_bounds__(kT) k_norm_final(const double* __restrict__ part, int nparts, int n, double* stats) {
+    __shared__ double sh[9][kT];
+    double s[3] = {0, 0, 0}, mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x)
+        for (int d = 0; d < 3; ++d) {
+            s[d] += part[(size_t)b * 9 + d];
+            mn[d] = fmin(mn[d], part[(size_t)b * 9 + 3 + d]);
+            mx[d] = fmax(mx[d], part[(size_t)b * 9 + 6 + d]);
+        }
+    for (int d = 0; d < 3; ++d) {
+        sh[d][threadIdx.x] = s[d];
+        sh[3 + d][threadIdx.x] = mn[d];
+        sh[6 + d][threadIdx.x] = mx[d];
+    }
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o)
+            for (int d = 0; d < 3; ++d) {
+                sh[d][threadIdx.x] += sh[d][threadIdx.x + o];
+                sh[3 + d][threadIdx.x] = fmin(sh[3 + d][threadIdx.x], sh[3 + d][threadIdx.x + o]);
+                sh[6 + d][threadIdx.x] = fmax(sh[6 + d][threadIdx.x], sh[6 + d][threadIdx.x + o]);
             }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
         double ext = 0;
-        for (int d = 0; d < 3; ++d) ext = fmax(ext, sh[3 + d][0] - sh[d][0]);
+        for (int d = 0; d < 3; ++d) ext = fmax(ext, sh[6 + d][0] - sh[3 + d][0]);
         const double scale = 1.0 / ext;
         for (int d = 0; d < 3; ++d) {
-            stats[d] = c[d];
-            stats[4 + d] = -c[d] * scale;  // t = -centre * scale
+            const double c = sh[d][0] / (double)n;
+            stats[d] = c;
+            stats[4 + d] = -c * scale;  // t = -centre * scale
         }
         stats[3] = scale;
     }
@@ -678,34 +703,69 @@ __global__ void __launch_bounds__(kQT) k_closest_gt(const float4* __restrict__ q
     }
 }
 
-// ------------------------------------------------------------------ contact detection (contact_detection.py:144-216)
-template <bool kEdges>
-__global__ void __launch_bounds__(kQT) k_detect(const float4* __restrict__ x, int n_query, const int4* __restrict__ elems,
-                                                const int2* __restrict__ child, const float4* __restrict__ nlo,
-                                                const float4* __restrict__ nhi, const float4* __restrict__ llo,
-                                                const float4* __restrict__ lhi, const int* __restrict__ leaf_id,
-                                                const RoundCounters* brc, float d_hat, float ee_thres, int4* c_idx,
-                                                int2* c_type, int cap, SolverScalars* sc) {
-    __shared__ int stack[kStack][kQT];
+// ------------------------------------------------------------------ contact detection (contact_detection.py:120-216)
+// The reference queries its BVHs with boxes of half-width 2 radius + d_hat around every vertex and every edge
+// and keeps the point-triangle and edge-edge pairs (no shared vertex; edge pairs with e0 < e1) whose
+// classified distance is <= 2 radius + d_hat. The box query only filters candidates, so this build keeps a
+// candidate list made with the half-width plus a skin, valid while no vertex moved more than half the skin
+// (in any coordinate) since it was built, and re-evaluates the distance filter on it every iteration. The
+// contact set is the reference's; the LBVH traversal runs only when the list is rebuilt.
+__device__ __forceinline__ int warp_append(int* counter) {
+    const unsigned am = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(am) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(am));
+    base = __shfl_sync(am, base, leader);
+    return base + __popc(am & ((1u << lane) - 1u));
+}
+
+// rebuild when some vertex moved more than half the skin since the lists were built
+__global__ void k_disp_check(const float4* __restrict__ q, const float4* __restrict__ qref, int np, float half_skin,
+                             SolverScalars* sc) {
     if (sc->abort) return;
-    const float thr = 2.0f * sc->radius + d_hat;
+    bool moved = false;
+    for (int i = gtid(); i < np; i += gstride()) {
+        const float4 a = q[i], b = qref[i];
+        moved |= fmaxf(fabsf(a.x - b.x), fmaxf(fabsf(a.y - b.y), fabsf(a.z - b.z))) > half_skin;
+    }
+    if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) sc->rebuild = 1;
+}
+
+__global__ void k_cand_begin(SolverScalars* sc) {
+    if (sc->abort || !sc->rebuild) return;
+    sc->n_cand_pt = 0;
+    sc->n_cand_ee = 0;
+}
+
+// LBVH traversal emitting candidate pairs whose boxes overlap within reach (one thread per query, stack in
+// shared memory, bounded).
+template <bool kEdges>
+__global__ void __launch_bounds__(kQT) k_candidates(const float4* __restrict__ x, int n_query, const int4* __restrict__ elems,
+                                                    const int2* __restrict__ child, const float4* __restrict__ nlo,
+                                                    const float4* __restrict__ nhi, const float4* __restrict__ llo,
+                                                    const float4* __restrict__ lhi, const int* __restrict__ leaf_id,
+                                                    const RoundCounters* brc, float d_hat, float skin, int2* out,
+                                                    int cap, int* counter, SolverScalars* sc) {
+    __shared__ int stack[kStack][kQT];
+    if (sc->abort || !sc->rebuild) return;
+    const float reach = 2.0f * sc->radius + d_hat + skin;
     const int nl = brc->n_live;
     for (int qi = gtid(); qi < n_query; qi += gstride()) {
         int i0, i1 = -1;
-        F3 x0, x1 = {0, 0, 0}, lo, hi;
+        F3 lo, hi;
         if (!kEdges) {
             i0 = qi;
-            x0 = f3(x[i0]);
-            lo = x0 - F3{thr, thr, thr};
-            hi = x0 + F3{thr, thr, thr};
+            const F3 x0 = f3(x[i0]);
+            lo = x0 - F3{reach, reach, reach};
+            hi = x0 + F3{reach, reach, reach};
         } else {
             const int4 e = elems[qi];
             i0 = e.x;
             i1 = e.y;
-            x0 = f3(x[i0]);
-            x1 = f3(x[i1]);
-            lo = fmin3(x0, x1) - F3{thr, thr, thr};
-            hi = fmax3(x0, x1) + F3{thr, thr, thr};
+            const F3 x0 = f3(x[i0]), x1 = f3(x[i1]);
+            lo = fmin3(x0, x1) - F3{reach, reach, reach};
+            hi = fmax3(x0, x1) + F3{reach, reach, reach};
         }
         const float4 qlo = make_float4(lo.x, lo.y, lo.z, 0.f), qhi = make_float4(hi.x, hi.y, hi.z, 0.f);
         auto overlap = [&](float4 a, float4 b) {
@@ -716,31 +776,12 @@ __global__ void __launch_bounds__(kQT) k_detect(const float4* __restrict__ x, in
             const int4 t = elems[id];
             if (!kEdges) {
                 if (i0 == t.x || i0 == t.y || i0 == t.z) return;
-                const F3 a = f3(x[t.x]), b = f3(x[t.y]), c = f3(x[t.z]);
-                const int ty = pt_classify(x0, a, b, c);
-                const float d = pt_pair_distance(x0, a, b, c, ty);
-                if (d <= thr) {
-                    const int at = atomicAdd(&sc->n_contacts_raw, 1);
-                    if (at < cap) {
-                        c_idx[at] = make_int4(i0, t.x, t.y, t.z);
-                        c_type[at] = make_int2(BLOCK_PT, ty);
-                    }
-                }
             } else {
                 if (!(qi < id)) return;
-                const int i2 = t.x, i3 = t.y;
-                if (i0 == i2 || i0 == i3 || i1 == i2 || i1 == i3) return;
-                const F3 a = f3(x[i2]), b = f3(x[i3]);
-                const int ty = ee_classify(x0, x1, a, b, ee_thres);
-                const float d = ee_pair_distance(x0, x1, a, b, ty);
-                if (d <= thr) {
-                    const int at = atomicAdd(&sc->n_contacts_raw, 1);
-                    if (at < cap) {
-                        c_idx[at] = make_int4(i0, i1, i2, i3);
-                        c_type[at] = make_int2(BLOCK_EE, ty);
-                    }
-                }
+                if (i0 == t.x || i0 == t.y || i1 == t.x || i1 == t.y) return;
             }
+            const int at = warp_append(counter);
+            if (at < cap) out[at] = make_int2(qi, id);
         };
         if (nl == 1) {
             if (overlap(llo[0], lhi[0])) leaf(0);
@@ -776,6 +817,56 @@ __global__ void __launch_bounds__(kQT) k_detect(const float4* __restrict__ x, in
             } else {
                 if (sp == 0) break;
                 node = stack[--sp][threadIdx.x];
+            }
+        }
+    }
+}
+
+// overflow of a candidate list: grow it and redo the iteration; otherwise the lists now hold positions q
+__global__ void k_cand_done(const float4* __restrict__ q, float4* qref, int np, int cap_pt, int cap_ee,
+                            SolverScalars* sc) {
+    if (sc->abort || !sc->rebuild) return;
+    if (sc->n_cand_pt > cap_pt || sc->n_cand_ee > cap_ee) {
+        if (gtid() == 0) sc->abort = 3;
+        return;
+    }
+    for (int i = gtid(); i < np; i += gstride()) qref[i] = q[i];
+}
+
+// the reference's distance filter on the candidates (detect_pt_contact_bvh_kernel, detect_ee_contact_bvh_kernel)
+__global__ void __launch_bounds__(kT) k_filter(const float4* __restrict__ x, const int2* __restrict__ cpt,
+                                               const int2* __restrict__ cee, const int4* __restrict__ tri,
+                                               const int4* __restrict__ edge4, float d_hat, float ee_thres,
+                                               int4* c_idx, int2* c_type, int cap, SolverScalars* sc) {
+    if (sc->abort) return;
+    const float thr = 2.0f * sc->radius + d_hat;
+    const int npt = sc->n_cand_pt, nee = sc->n_cand_ee;
+    for (int g = gtid(); g < npt + nee; g += gstride()) {
+        int4 id;
+        int block, ty;
+        float d;
+        if (g < npt) {
+            const int2 c = cpt[g];
+            const int4 t = tri[c.y];
+            id = make_int4(c.x, t.x, t.y, t.z);
+            const F3 x0 = f3(x[id.x]), x1 = f3(x[id.y]), x2 = f3(x[id.z]), x3 = f3(x[id.w]);
+            ty = pt_classify(x0, x1, x2, x3);
+            d = pt_pair_distance(x0, x1, x2, x3, ty);
+            block = BLOCK_PT;
+        } else {
+            const int2 c = cee[g - npt];
+            const int4 a = edge4[c.x], b = edge4[c.y];
+            id = make_int4(a.x, a.y, b.x, b.y);
+            const F3 x0 = f3(x[id.x]), x1 = f3(x[id.y]), x2 = f3(x[id.z]), x3 = f3(x[id.w]);
+            ty = ee_classify(x0, x1, x2, x3, ee_thres);
+            d = ee_pair_distance(x0, x1, x2, x3, ty);
+            block = BLOCK_EE;
+        }
+        if (d <= thr) {
+            const int at = warp_append(&sc->n_contacts_raw);
+            if (at < cap) {
+                c_idx[at] = id;
+                c_type[at] = make_int2(block, ty);
             }
         }
     }
@@ -1021,7 +1112,7 @@ __global__ void k_diff_hinge(const float4* __restrict__ x, const int4* __restric
 // wp.spd_project_blocks(3, block, it_max); here the 9x9 matrix of blocks [0..2][0..2] is made positive
 // semi-definite by a cyclic Jacobi eigen-decomposition (it_max sweeps), clamping negative eigenvalues to
 // zero; the fourth block row and column are then set from the first three as the reference does.
-__global__ void __launch_bounds__(64) k_spd_project(float* blocks, int nh, int sweeps, const SolverScalars* sc) {
+__global__ void __launch_bounds__(32) k_spd_project(float* blocks, int nh, int sweeps, const SolverScalars* sc) {
     if (sc->abort) return;
     for (int h = gtid(); h < nh; h += gstride()) {
         float* B = blocks + (size_t)h * 144;
@@ -1050,9 +1141,13 @@ __global__ void __launch_bounds__(64) k_spd_project(float* blocks, int nh, int s
                 for (int q = p + 1; q < 9; ++q) {
                     const float apq = A[p][q];
                     if (fabsf(apq) < 1e-30f) continue;
-                    const float th = (A[q][q] - A[p][p]) / (2.f * apq);
-                    const float t = (th >= 0.f ? 1.f : -1.f) / (fabsf(th) + sqrtf(th * th + 1.f));
-                    const float c = 1.f / sqrtf(t * t + 1.f), s = t * c;
+                    // rotation angle by the fast (approximate) reciprocal and square-root instructions: the
+                    // projection only needs an orthogonal rotation that shrinks the off-diagonal entry
+                    const float th = __fdividef(A[q][q] - A[p][p], 2.f * apq);
+                    const float r2 = fmaf(th, th, 1.f);
+                    const float t = fabsf(th) > 1e18f ? __fdividef(0.5f, th)
+                                                      : copysignf(__fdividef(1.f, fabsf(th) + r2 * rsqrtf(r2)), th);
+                    const float c = rsqrtf(fmaf(t, t, 1.f)), s = t * c;
 #pragma unroll
                     for (int k = 0; k < 9; ++k) {
                         const float akp = A[k][p], akq = A[k][q];
@@ -1147,14 +1242,14 @@ __global__ void k_diff_contact(const float4* __restrict__ x, const int4* __restr
 }
 
 // ------------------------------------------------------------------ Jacobi PCG (cg_solver.py:46-158)
-// One CG iteration is two kernels:
-//   k_cg_hvp: the search direction v = z + (z_r / z_r_last) v_prev is formed where it is read (update_v_kernel,
-//             solver_kernels.py:26-35), Av += H v over every element (system.py:348-352: the hess_dx kernels
-//             of distance_energy.py:20-33, elastic_energy.py:151-220, hinge_energy.py:241-274 and the
-//             Gauss-Newton collision_hess_dx_kernel, collision_energy.py:379-409), and v.Av is summed per
-//             element (v_e . H_e v_e), which equals v . Av, so no separate dot-product pass is needed;
-//   k_cg_prz: p += alpha v, r -= alpha Av when v.Av > 1e-16, z = r / diag, z.r
-//             (update_p_r_z_compute_zr_kernel, solver_kernels.py:4-23); Av is cleared for the next product.
+// Per CG iteration two phases, separated by grid barriers inside one cooperative kernel:
+//   Hessian product: the search direction v = z + (z_r / z_r_last) v_prev is formed where it is read
+//     (update_v_kernel, solver_kernels.py:26-35), Av += H v over every element (system.py:348-352: the hess_dx
+//     kernels of distance_energy.py:20-33, elastic_energy.py:151-220, hinge_energy.py:241-274 and the
+//     Gauss-Newton collision_hess_dx_kernel, collision_energy.py:379-409), and v.Av is summed per element
+//     (v_e . H_e v_e, which equals v . Av), so no separate dot-product pass is needed;
+//   p/r/z: p += alpha v, r -= alpha Av when v.Av > 1e-16, z = r / diag, z.r (update_p_r_z_compute_zr_kernel,
+//     solver_kernels.py:4-23); Av is cleared for the next product.
 struct HvpArgs {
     const float* w;
     float m2gt_k;
@@ -1177,15 +1272,14 @@ __device__ __forceinline__ F3 cg_dir(const float4* __restrict__ z, const float4*
     return f3(z[j]) + s * f3(vprev[j]);
 }
 
-__global__ void __launch_bounds__(kT) k_cg_hvp(const float4* __restrict__ x, HvpArgs A, const float4* __restrict__ z,
-                                               const float4* __restrict__ vprev, float4* vout, float4* Av, int first,
-                                               SolverScalars* sc, float2* partial) {
-    if (sc->abort) return;
-    const float s = first ? 0.f : sc->z_r / sc->z_r_last;
-    const int nc = sc->n_contacts;
+// Av += H v over the elements gtid, gtid + stride, ...; returns this thread's part of v.Av. The direction is
+// v = z + s v_prev, written to vout by the vertex terms.
+__device__ __forceinline__ CSum hvp_elements(const float4* __restrict__ x, const HvpArgs& A, const float4* __restrict__ z,
+                                             const float4* __restrict__ vprev, float4* vout, float4* Av, float s, int nc,
+                                             long long first, long long stride) {
     const long long e1 = A.np, e2 = e1 + A.nt, e3 = e2 + A.nh, total = e3 + nc;
     CSum acc;
-    for (long long g = gtid(); g < total; g += gstride()) {
+    for (long long g = first; g < total; g += stride) {
         if (g < e1) {
             const int i = (int)g;
             const F3 vi = cg_dir(z, vprev, s, i);
@@ -1220,14 +1314,23 @@ __global__ void __launch_bounds__(kT) k_cg_hvp(const float4* __restrict__ x, Hvp
             const int h = (int)(g - e2);
             const int4 id = A.hinge[h];
             const int ids[4] = {id.x, id.y, id.z, id.w};
-            const float* B = A.blocks + (size_t)h * 144;
+            const float4* B4 = reinterpret_cast<const float4*>(A.blocks + (size_t)h * 144);
+            float Bm[144];
+#pragma unroll
+            for (int k = 0; k < 36; ++k) {
+                const float4 b = B4[k];
+                Bm[4 * k] = b.x; Bm[4 * k + 1] = b.y; Bm[4 * k + 2] = b.z; Bm[4 * k + 3] = b.w;
+            }
             F3 d[4];
+#pragma unroll
             for (int b = 0; b < 4; ++b) d[b] = cg_dir(z, vprev, s, ids[b]);
             float vhv = 0.f;
+#pragma unroll
             for (int a = 0; a < 4; ++a) {
                 F3 r = {0.f, 0.f, 0.f};
+#pragma unroll
                 for (int b = 0; b < 4; ++b) {
-                    const float* M = B + (a * 4 + b) * 9;
+                    const float* M = Bm + (a * 4 + b) * 9;
                     r = r + F3{M[0] * d[b].x + M[1] * d[b].y + M[2] * d[b].z, M[3] * d[b].x + M[4] * d[b].y + M[5] * d[b].z,
                                M[6] * d[b].x + M[7] * d[b].y + M[8] * d[b].z};
                 }
@@ -1252,17 +1355,16 @@ __global__ void __launch_bounds__(kT) k_cg_hvp(const float4* __restrict__ x, Hvp
             acc.add(sd * sd * c);
         }
     }
-    grid_sum_finish(acc, partial, &sc->red_count, &sc->v_A_v, nullptr);
+    return acc;
 }
 
-// p = 0, r = grad, z = r / (diag + 1e-6) (compute_block_diag_inv_kernel), v_prev = 0, Av = 0, z.r
-__global__ void __launch_bounds__(kT) k_cg_init(const float4* __restrict__ grad, const float4* __restrict__ hd, int np,
-                                                float4* p, float4* r, float4* z, float4* vprev, float4* Av,
-                                                SolverScalars* sc, float2* partial) {
-    if (sc->abort) return;
+// p = 0, r = grad, z = r / (diag + 1e-6) (compute_block_diag_inv_kernel), v_prev = 0, Av = 0; returns z.r part
+__device__ __forceinline__ CSum cg_init_vertices(const float4* __restrict__ grad, const float4* __restrict__ hd, int np,
+                                                 float4* p, float4* r, float4* z, float4* vprev, float4* Av, int first,
+                                                 int stride) {
     CSum acc;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int i = gtid(); i < np; i += gstride()) {
+    for (int i = first; i < np; i += stride) {
         const float4 g = grad[i], d = hd[i];
         p[i] = zero;
         r[i] = g;
@@ -1272,17 +1374,16 @@ __global__ void __launch_bounds__(kT) k_cg_init(const float4* __restrict__ grad,
         Av[i] = zero;
         acc.add(zz.x * g.x + zz.y * g.y + zz.z * g.z);
     }
-    grid_sum_finish(acc, partial, &sc->red_count, &sc->z_r, nullptr);
+    return acc;
 }
 
-__global__ void __launch_bounds__(kT) k_cg_prz(const float4* __restrict__ v, float4* Av, const float4* __restrict__ hd,
-                                               int np, float4* p, float4* r, float4* z, SolverScalars* sc,
-                                               float2* partial) {
-    if (sc->abort) return;
-    const float vAv = sc->v_A_v;
-    const float alpha = sc->z_r / vAv;
+// p += alpha v, r -= alpha Av when v.Av > 1e-16, z = r / diag, Av = 0; returns z.r part
+__device__ __forceinline__ CSum cg_prz_vertices(const float4* __restrict__ v, float4* Av, const float4* __restrict__ hd,
+                                                int np, float4* p, float4* r, float4* z, float zr, float vAv, int first,
+                                                int stride) {
+    const float alpha = zr / vAv;
     CSum acc;
-    for (int i = gtid(); i < np; i += gstride()) {
+    for (int i = first; i < np; i += stride) {
         float4 ri = r[i];
         if (vAv > 1e-16f) {
             const float4 vi = v[i], avi = Av[i];
@@ -1298,7 +1399,161 @@ __global__ void __launch_bounds__(kT) k_cg_prz(const float4* __restrict__ v, flo
         z[i] = zz;
         acc.add(zz.x * ri.x + zz.y * ri.y + zz.z * ri.z);
     }
-    grid_sum_finish(acc, partial, &sc->red_count, &sc->z_r, &sc->z_r_last);  // z_r_last = old z_r
+    return acc;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(volatile unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Barrier across all blocks of a cooperative launch (co-residency guaranteed). The spin is bounded: on
+// time-out it records kErrIterLimit in *status and lets the block go on (the host then reports the error).
+__device__ __forceinline__ void grid_barrier(unsigned* count, volatile unsigned* gen, int* status) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(count, 1u) == gridDim.x - 1) {
+            *count = 0;
+            __threadfence();
+            atomicAdd((unsigned*)gen, 1u);
+        } else {
+            long long spins = 0;
+            while (ld_acquire(gen) == g) {
+                if (++spins > (1ll << 28)) {
+                    atomicOr(status, kErrIterLimit);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// Sum of the per-block partials in block order, the same value in every block (after a barrier).
+__device__ __forceinline__ float grid_partials_sum(const float2* partial) {
+    __shared__ float result;
+    CSum a;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        CSum t;
+        t.s = __ldcg(&partial[b].x);
+        t.c = __ldcg(&partial[b].y);
+        a.merge(t);
+    }
+    CSum f = block_reduce(a);
+    if (threadIdx.x == 0) result = f.s + f.c;
+    __syncthreads();
+    const float v = result;
+    __syncthreads();
+    return v;
+}
+
+__device__ __forceinline__ void store_partial(CSum acc, float2* partial) {
+    CSum r = block_reduce(acc);
+    if (threadIdx.x == 0) partial[blockIdx.x] = make_float2(r.s, r.c);
+}
+
+struct CgState {
+    unsigned count, gen;
+};
+
+// The whole Jacobi PCG solve (cg_solver.py:96-158, n_cg_iters iterations) as one cooperative kernel: each
+// iteration is the Hessian product phase and the p/r/z phase, with a grid barrier after each. Every block
+// forms the same totals (v.Av, z.r) from the block partials in block order.
+__global__ void __launch_bounds__(kT) k_cg_solve(const float4* __restrict__ x, HvpArgs A, const float4* __restrict__ grad,
+                                                 const float4* __restrict__ hd, float4* p, float4* r, float4* z,
+                                                 float4* v0, float4* v1, float4* Av, int n_iters, SolverScalars* sc,
+                                                 float2* partial, CgState* bar) {
+    if (sc->abort) return;
+    const int nc = sc->n_contacts;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    float2* part_a = partial;
+    float2* part_b = partial + gridDim.x;
+    store_partial(cg_init_vertices(grad, hd, A.np, p, r, z, v0, Av, tid, nthreads), part_a);
+    grid_barrier(&bar->count, &bar->gen, &sc->status);
+    float zr = grid_partials_sum(part_a), zr_last = zr;
+    for (int it = 0; it < n_iters; ++it) {
+        const float4* vin = (it & 1) ? v1 : v0;
+        float4* vout = (it & 1) ? v0 : v1;
+        const float s_dir = it == 0 ? 0.f : zr / zr_last;
+        // partials alternate between two buffers phase by phase: a buffer is rewritten only after the next
+        // barrier, which every block reaches after it has read that buffer
+        store_partial(hvp_elements(x, A, z, vin, vout, Av, s_dir, nc, tid, nthreads), part_b);
+        grid_barrier(&bar->count, &bar->gen, &sc->status);
+        const float vAv = grid_partials_sum(part_b);
+        store_partial(cg_prz_vertices(vout, Av, hd, A.np, p, r, z, zr, vAv, tid, nthreads), part_a);
+        grid_barrier(&bar->count, &bar->gen, &sc->status);
+        zr_last = zr;
+        zr = grid_partials_sum(part_a);
+        if (blockIdx.x == 0 && threadIdx.x == 0) sc->v_A_v = vAv;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        sc->z_r = zr;
+        sc->z_r_last = zr_last;
+    }
+}
+
+// The same solve inside one thread-block cluster (up to 16 CTAs): the barriers are the hardware cluster
+// barrier and the block partials are exchanged through distributed shared memory instead of a grid-wide
+// barrier through global memory. Selected with cg_mode 2.
+constexpr int kClusterThreads = 512;
+
+__global__ void __launch_bounds__(kClusterThreads) k_cg_cluster(const float4* __restrict__ x, HvpArgs A,
+                                                                const float4* __restrict__ grad,
+                                                                const float4* __restrict__ hd, float4* p, float4* r,
+                                                                float4* z, float4* v0, float4* v1, float4* Av,
+                                                                int n_iters, SolverScalars* sc) {
+    namespace cgr = cooperative_groups;
+    cgr::cluster_group cl = cgr::this_cluster();
+    __shared__ float2 slot[2];
+    __shared__ float total;
+    if (sc->abort) return;  // the same value in every CTA: the flag is written only by earlier kernels
+    const int nc = sc->n_contacts;
+    const unsigned nblk = cl.num_blocks();
+    const int tid = (int)(cl.block_rank() * blockDim.x + threadIdx.x), nthreads = (int)(nblk * blockDim.x);
+    int phase = 0;
+    // cluster-wide compensated total, the same in every CTA (partials merged in rank order)
+    auto cluster_total = [&](CSum acc) -> float {
+        const int k = phase++ & 1;  // a slot is rewritten only after the next cluster barrier
+        CSum br = block_reduce(acc);
+        if (threadIdx.x == 0) slot[k] = make_float2(br.s, br.c);
+        cl.sync();
+        if (threadIdx.x == 0) {
+            CSum a;
+            for (unsigned b = 0; b < nblk; ++b) {
+                const float2 t2 = *cl.map_shared_rank(&slot[k], b);
+                CSum t;
+                t.s = t2.x;
+                t.c = t2.y;
+                a.merge(t);
+            }
+            total = a.s + a.c;
+        }
+        __syncthreads();
+        const float v = total;
+        __syncthreads();
+        return v;
+    };
+    float zr = cluster_total(cg_init_vertices(grad, hd, A.np, p, r, z, v0, Av, tid, nthreads)), zr_last = zr;
+    float vAv = 0.f;
+    for (int it = 0; it < n_iters; ++it) {
+        const float4* vin = (it & 1) ? v1 : v0;
+        float4* vout = (it & 1) ? v0 : v1;
+        const float s_dir = it == 0 ? 0.f : zr / zr_last;
+        vAv = cluster_total(hvp_elements(x, A, z, vin, vout, Av, s_dir, nc, tid, nthreads));
+        const float zr_new = cluster_total(cg_prz_vertices(vout, Av, hd, A.np, p, r, z, zr, vAv, tid, nthreads));
+        zr_last = zr;
+        zr = zr_new;
+    }
+    if (cl.block_rank() == 0 && threadIdx.x == 0) {
+        sc->v_A_v = vAv;
+        sc->z_r = zr;
+        sc->z_r_last = zr_last;
+    }
+    cl.sync();  // no CTA leaves while another may still read its shared memory
 }
 
 // ------------------------------------------------------------------ iteration bookkeeping
@@ -1332,6 +1587,8 @@ __global__ void k_contacts_done(SolverScalars* sc, int cap, long long max_blocks
     sc->n_contacts = raw;
     sc->total_contacts += raw;
     if (raw > sc->max_contacts) sc->max_contacts = raw;
+    if (sc->rebuild) sc->n_rebuilds += 1;
+    sc->rebuild = 0;
 }
 
 // clamp_p_kernel (solver_kernels.py:68-85): keep |q_prev_newton + p - q_prev_detection| <= radius. Contacts are
@@ -1448,9 +1705,9 @@ void Stage3::release() {
         ptr = nullptr;
     };
     f(gt_pos); f(gt_tri); f(gt_bvh_mem); f(gt_rc); f(q); f(q_rest); f(q_prev_newton); f(p); f(target);
-    f(grad); f(hdiag); f(r); f(z); f(v[0]); f(v[1]); f(Av); f(vweight); f(tri); f(edge4); f(el_area); f(el_invDm);
+    f(grad); f(hdiag); f(r); f(z); f(v[0]); f(v[1]); f(Av); f(vweight); f(q_ref); f(cand_pt); f(cand_ee); f(tri); f(edge4); f(el_area); f(el_invDm);
     f(hinge); f(hinge_rest); f(hinge_blocks); f(c_idx); f(c_type); f(c_d); f(c_dd); f(partial); f(tri_bvh_mem);
-    f(edge_bvh_mem); f(tri_rc); f(edge_rc); f(sc); f(d_norm);
+    f(edge_bvh_mem); f(tri_rc); f(edge_rc); f(sc); f(d_norm); f(cg_bar);
     if (h_sc) cudaFreeHost(h_sc);
     h_sc = nullptr;
     if (ev_in) cudaEventDestroy(ev_in);
@@ -1469,8 +1726,28 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
             return fail(PAMO_ERR_CUDA, "event");
         if (cudaMalloc((void**)&sc, sizeof(SolverScalars)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
         if (cudaMallocHost((void**)&h_sc, sizeof(SolverScalars)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMallocHost");
-        if (cudaMalloc((void**)&d_norm, 16 * sizeof(double)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
-        if (cudaMalloc((void**)&partial, kRedBlocks * sizeof(float2)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+        if (cudaMalloc((void**)&d_norm, (16 + 9 * kNormBlocks) * sizeof(double)) != cudaSuccess)
+            return fail(PAMO_ERR_OOM, "cudaMalloc");
+        if (cudaMalloc((void**)&partial, kPartials * sizeof(float2)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+        if (cudaMalloc((void**)&cg_bar, 64) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+        cudaMemset(cg_bar, 0, 64);
+        int dev = 0, nsm = 0, occ = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_solve, kT, 0);
+        coop_max_blocks = std::max(1, nsm * std::max(occ, 0));
+        n_sm = std::max(1, nsm);
+        // largest cluster the device runs k_cg_cluster with (16 needs the non-portable opt-in)
+        cluster_size = 1;
+        if (cudaFuncSetAttribute(k_cg_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(16);
+            cfg.blockDim = dim3(kClusterThreads);
+            int cs = 0;
+            if (cudaOccupancyMaxPotentialClusterSize(&cs, k_cg_cluster, &cfg) == cudaSuccess) cluster_size = std::min(cs, 16);
+        }
+        cudaGetLastError();  // a refused attribute leaves the cooperative path in use
+        if (cluster_size < 2) cluster_size = 1;
         if (cudaMalloc((void**)&gt_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
         if (cudaMalloc((void**)&tri_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
         if (cudaMalloc((void**)&edge_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
@@ -1495,7 +1772,7 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
     }
     if (cap_v < (size_t)np + 2) {
         const size_t n = (size_t)np + 2;
-        for (float4** b : {&q, &q_rest, &q_prev_newton, &p, &target, &grad, &hdiag, &r, &z, &Av, &v[0], &v[1]}) {
+        for (float4** b : {&q, &q_rest, &q_prev_newton, &q_ref, &p, &target, &grad, &hdiag, &r, &z, &Av, &v[0], &v[1]}) {
             c = cap_v;
             if ((rr = grow(*b, c, n))) return rr;
         }
@@ -1562,6 +1839,22 @@ int Stage3::ensure_contacts(size_t n) {
     return PAMO_OK;
 }
 
+int Stage3::ensure_candidates(size_t npt, size_t nee) {
+    size_t c;
+    int rr;
+    if (cap_cpt < npt || !cand_pt) {
+        c = cand_pt ? cap_cpt : 0;
+        if ((rr = grow(cand_pt, c, npt))) return rr;
+        cap_cpt = c;
+    }
+    if (cap_cee < nee || !cand_ee) {
+        c = cand_ee ? cap_cee : 0;
+        if ((rr = grow(cand_ee, c, nee))) return rr;
+        cap_cee = c;
+    }
+    return PAMO_OK;
+}
+
 void Stage3::launch_energy(const float4* x) {
     const Stage3Params& P = params;
     EnergyArgs A;
@@ -1587,16 +1880,26 @@ void Stage3::newton_iteration() {
     // q_prev_newton = q; contacts at q (system.py:425-432, _detect_contact :308-318 with refitted LBVHs)
     k_iter_begin<<<grid_for(NP, kT), kT, 0, s>>>(q, q_prev_newton, grad, hdiag, NP, sc);
     note_launch();
-    bvh_refit(tri_bvh, tri, q, tri_rc, NT, s);
-    bvh_refit(edge_bvh, edge4, q, edge_rc, NE, s);
-    const int cap = (int)std::min<size_t>(cap_c, (size_t)P.max_blocks);
-    k_detect<false><<<grid_for(NP, kQT, 16), kQT, 0, s>>>(q, NP, tri, tri_bvh.child, tri_bvh.nlo, tri_bvh.nhi, tri_bvh.llo,
-                                                         tri_bvh.lhi, tri_bvh.vals[0], tri_rc, P.d_hat,
-                                                         P.ee_classify_thres, c_idx, c_type, cap, sc);
+    const float skin = 2.0f * P.contact_detection_radius + P.d_hat;
+    k_disp_check<<<grid_for(NP, kT), kT, 0, s>>>(q, q_ref, NP, 0.5f * skin, sc);
     note_launch();
-    k_detect<true><<<grid_for(NE, kQT, 16), kQT, 0, s>>>(q, NE, edge4, edge_bvh.child, edge_bvh.nlo, edge_bvh.nhi,
-                                                        edge_bvh.llo, edge_bvh.lhi, edge_bvh.vals[0], edge_rc, P.d_hat,
-                                                        P.ee_classify_thres, c_idx, c_type, cap, sc);
+    k_cand_begin<<<1, 1, 0, s>>>(sc);
+    note_launch();
+    bvh_refit(tri_bvh, tri, q, tri_rc, NT, s, &sc->rebuild);
+    bvh_refit(edge_bvh, edge4, q, edge_rc, NE, s, &sc->rebuild);
+    k_candidates<false><<<grid_for(NP, kQT, 16), kQT, 0, s>>>(q, NP, tri, tri_bvh.child, tri_bvh.nlo, tri_bvh.nhi,
+                                                             tri_bvh.llo, tri_bvh.lhi, tri_bvh.vals[0], tri_rc, P.d_hat,
+                                                             skin, cand_pt, (int)cap_cpt, &sc->n_cand_pt, sc);
+    note_launch();
+    k_candidates<true><<<grid_for(NE, kQT, 16), kQT, 0, s>>>(q, NE, edge4, edge_bvh.child, edge_bvh.nlo, edge_bvh.nhi,
+                                                            edge_bvh.llo, edge_bvh.lhi, edge_bvh.vals[0], edge_rc,
+                                                            P.d_hat, skin, cand_ee, (int)cap_cee, &sc->n_cand_ee, sc);
+    note_launch();
+    k_cand_done<<<grid_for(NP, kT), kT, 0, s>>>(q, q_ref, NP, (int)cap_cpt, (int)cap_cee, sc);
+    note_launch();
+    const int cap = (int)std::min<size_t>(cap_c, (size_t)P.max_blocks);
+    k_filter<<<grid_for((long long)(cap_cpt + cap_cee), kT), kT, 0, s>>>(q, cand_pt, cand_ee, tri, edge4, P.d_hat,
+                                                                        P.ee_classify_thres, c_idx, c_type, cap, sc);
     note_launch();
     k_contacts_done<<<1, 1, 0, s>>>(sc, cap, P.max_blocks);
     note_launch();
@@ -1610,7 +1913,7 @@ void Stage3::newton_iteration() {
         k_diff_hinge<<<grid_for(NH, 128), 128, 0, s>>>(q, hinge, hinge_rest, P.hinge_stiffness, -1.f, NH, hinge_blocks,
                                                        grad, hdiag, sc);
         note_launch();
-        k_spd_project<<<grid_for(NH, 64), 64, 0, s>>>(hinge_blocks, NH, P.spd_max_iters, sc);
+        k_spd_project<<<grid_for(NH, 32, 64), 32, 0, s>>>(hinge_blocks, NH, P.spd_max_iters, sc);
         note_launch();
     }
     k_diff_contact<<<gC, kT, 0, s>>>(q, c_idx, c_type, c_d, sc, P.coll_stiffness, P.d_hat, -1.f, c_dd, grad, hdiag);
@@ -1621,17 +1924,42 @@ void Stage3::newton_iteration() {
     H.tri = tri; H.area = el_area; H.invDm = el_invDm; H.mu = mu; H.la = la; H.nt = NT;
     H.hinge = hinge; H.blocks = hinge_blocks; H.nh = NH;
     H.cidx = c_idx; H.cd = c_d; H.cdd = c_dd; H.kappa = P.coll_stiffness; H.d_hat = P.d_hat;
-    const int gV = (int)std::min<long long>(kRedBlocks, ((long long)NP + kT - 1) / kT);
-    const long long total = (long long)NP + NT + NH + (long long)cap_c;
-    const int gH = (int)std::min<long long>(kRedBlocks, (total + kT - 1) / kT);
-    k_cg_init<<<gV, kT, 0, s>>>(grad, hdiag, NP, p, r, z, v[0], Av, sc, partial);
-    note_launch();
-    for (int it = 0; it < P.n_cg_iters; ++it) {
-        float4* vin = v[it & 1];
-        float4* vout = v[(it + 1) & 1];
-        k_cg_hvp<<<gH, kT, 0, s>>>(q, H, z, vin, vout, Av, it == 0 ? 1 : 0, sc, partial);
+    const long long elems_all = (long long)NP + NT + NH;
+    // the cluster kernel measured slower than the grid-wide one on the 5k-face stage-2 output (fewer threads
+    // per element pass), so it runs only when asked for
+    const bool use_cluster = cluster_size > 1 && cg_mode == 2 && elems_all > 0;
+    if (use_cluster) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cluster_size);
+        cfg.blockDim = dim3(kClusterThreads);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = cluster_size;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_cg_cluster, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r, z,
+                           v[0], v[1], Av, P.n_cg_iters, sc);
         note_launch();
-        k_cg_prz<<<gV, kT, 0, s>>>(vout, Av, hdiag, NP, p, r, z, sc, partial);
+    } else {
+        // one cooperative launch: about one block per 256 elements, at most one block per SM
+        const long long elems = (long long)NP + NT + NH;
+        int g = (int)std::min<long long>((elems + kT - 1) / kT, (long long)n_sm);
+        g = std::max(1, std::min(g, std::min(coop_max_blocks, kPartials / 2)));
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(g);
+        cfg.blockDim = dim3(kT);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        CgState* bar = reinterpret_cast<CgState*>(cg_bar);
+        cudaLaunchKernelEx(&cfg, k_cg_solve, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r, z, v[0],
+                           v[1], Av, P.n_cg_iters, sc, partial, bar);
         note_launch();
     }
     // step clamp, CCD, line search (system.py:441-459)
@@ -1705,7 +2033,10 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     drop_graph();  // kernel arguments of a captured iteration (sizes, coefficients) belong to one call
     if ((rr = ensure(NP, NT, NE, NH, NGP, NGT))) return rr;
     if ((rr = ensure_contacts(std::max<size_t>(std::max<size_t>(1 << 16, cap_c), (size_t)32 * (NP + NE))))) return rr;
+    if ((rr = ensure_candidates(std::max<size_t>(1 << 16, (size_t)64 * NP), std::max<size_t>(1 << 16, (size_t)64 * NE))))
+        return rr;
     cudaStream_t s = stream;
+    cudaMemsetAsync(cg_bar, 0, sizeof(unsigned), s);  // barrier arrival count (after an aborted barrier)
     cudaEventRecord(ev_in, caller);
     cudaStreamWaitEvent(s, ev_in, 0);
     std::vector<int4> e4(NE);
@@ -1717,12 +2048,15 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     if (NH) cudaMemcpyAsync(hinge, h4.data(), NH * sizeof(int4), cudaMemcpyHostToDevice, s);
 
     // normalisation (processing.py:15-21, 57-59)
-    k_norm_stats<<<1, kT, 0, s>>>(gt_points, NGP, d_norm);
+    k_norm_partial<<<kNormBlocks, kT, 0, s>>>(gt_points, NGP, d_norm + 16);
+    note_launch();
+    k_norm_final<<<1, kT, 0, s>>>(d_norm + 16, kNormBlocks, NGP, d_norm);
     note_launch();
     k_normalize<<<grid_for(NGP, kT), kT, 0, s>>>(gt_points, NGP, d_norm, gt_pos, nullptr);
     note_launch();
     std::memset(h_sc, 0, sizeof(SolverScalars));
     h_sc->radius = params.contact_detection_radius;
+    h_sc->rebuild = 1;  // candidate lists are built in the first iteration
     cudaMemcpyAsync(sc, h_sc, sizeof(SolverScalars), cudaMemcpyHostToDevice, s);
     k_tris4<<<grid_for(NGT, kT), kT, 0, s>>>(gt_tris, NGT, NGP, gt_tri, &sc->status);
     note_launch();
@@ -1818,6 +2152,9 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
                     if (++stats.radius_halvings > 40) return fail(PAMO_ERR_CAPACITY, "contacts exceed max_blocks");
                     const float rad = h_sc->radius * 0.5f;
                     cudaMemcpyAsync(&sc->radius, &rad, sizeof(float), cudaMemcpyHostToDevice, s);
+                } else if (h_sc->abort == 3) {
+                    const size_t a = (size_t)h_sc->n_cand_pt, b = (size_t)h_sc->n_cand_ee;
+                    if ((rr = ensure_candidates(a + a / 2 + 1024, b + b / 2 + 1024))) return rr;
                 } else {
                     const size_t raw = (size_t)h_sc->n_contacts_raw;
                     if ((rr = ensure_contacts(raw + raw / 2 + 1024))) return rr;
@@ -1837,6 +2174,7 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     stats.last_energy = h_sc->energy;
     stats.max_contacts = h_sc->max_contacts;
     stats.total_contacts = h_sc->total_contacts;
+    stats.candidate_rebuilds = h_sc->n_rebuilds;
     return PAMO_OK;
 }
 
@@ -1895,6 +2233,7 @@ int pamo_stage3_set_param(pamo_stage3* s, const char* name, double value) {
     else if (n == "min_angle_thres") P.min_angle_thres = (float)value;
     else if (n == "max_blocks") P.max_blocks = (long long)value;
     else if (n == "use_cuda_graph") s->solver.use_graph = value != 0.0;
+    else if (n == "cg_mode") s->solver.cg_mode = (int)value;  // 0 or 1 grid-cooperative, 2 one cluster
     else {
         s->solver.err = "unknown stage-3 parameter: " + n;
         return PAMO_ERR_INVALID_ARG;
@@ -1922,11 +2261,11 @@ int pamo_safe_project(pamo_stage3* s, const double* gt_points, const int32_t* gt
 int pamo_stage3_stats(const pamo_stage3* s, double* out, int32_t n) {
     if (!s || !out) return PAMO_ERR_INVALID_ARG;
     const pamo::Stage3Stats& t = s->solver.stats;
-    const double v[11] = {(double)t.n_particles, (double)t.n_triangles, (double)t.n_edges, (double)t.n_hinges,
+    const double v[12] = {(double)t.n_particles, (double)t.n_triangles, (double)t.n_edges, (double)t.n_hinges,
                           (double)t.steps, (double)t.newton_iters, (double)t.max_contacts, (double)t.radius_halvings,
-                          (double)t.do_nothing, t.last_energy, (double)t.total_contacts};
-    for (int i = 0; i < n && i < 11; ++i) out[i] = v[i];
-    return 11;
+                          (double)t.do_nothing, t.last_energy, (double)t.total_contacts, (double)t.candidate_rebuilds};
+    for (int i = 0; i < n && i < 12; ++i) out[i] = v[i];
+    return 12;
 }
 
 }  // extern "C"

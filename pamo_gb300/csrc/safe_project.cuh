@@ -41,10 +41,14 @@ struct SolverScalars {
     float radius;         // contact detection radius (halved when contacts exceed max_blocks)
     float pad0;
     int n_contacts, n_contacts_raw, accepted, status;
-    int abort;            // 0 running; 1 contact list full (grow, redo the iteration); 2 above max_blocks (halve)
+    int abort;            // 0 running; 1 contact list full, 3 candidate list full (grow, redo the iteration);
+                          // 2 contacts above max_blocks (halve the radius, redo)
     int iters_done;       // Newton iterations completed in this run
     int red_count;        // arrival counter of the grid-wide sums
     int max_contacts;
+    int rebuild;          // candidate lists are rebuilt in this iteration
+    int n_cand_pt, n_cand_ee;  // candidate pairs (true counts, may exceed the capacities)
+    int n_rebuilds;
     long long total_contacts;
 };
 
@@ -54,6 +58,7 @@ struct Stage3Stats {
     int do_nothing = 0;
     double last_energy = 0.0;
     long long total_contacts = 0;  // summed over Newton iterations
+    int candidate_rebuilds = 0;    // Newton iterations that rebuilt the contact candidate lists
 };
 
 class Stage3 {
@@ -68,6 +73,8 @@ public:
     Stage3Stats stats;
     std::string err;
     bool use_graph = true;  // capture one Newton iteration as a CUDA graph and replay it
+    int cg_mode = 0;        // PCG kernel: 0 or 1 grid-wide cooperative launch, 2 one thread-block cluster
+    int cluster_size = 1;   // CTAs of the cluster kernel (device limit, at most 16)
 
 private:
     template <typename T>
@@ -78,6 +85,7 @@ private:
     }
     int ensure(int np, int nt, int ne, int nh, int ngp, int ngt);
     int ensure_contacts(size_t n);
+    int ensure_candidates(size_t npt, size_t nee);
     void release();
     void drop_graph();
 
@@ -94,6 +102,7 @@ private:
     RoundCounters* gt_rc = nullptr;
     // simulated mesh
     float4 *q = nullptr, *q_rest = nullptr, *q_prev_newton = nullptr, *p = nullptr;
+    float4* q_ref = nullptr;  // positions at the last build of the candidate lists
     float4 *target = nullptr, *grad = nullptr, *hdiag = nullptr, *r = nullptr, *z = nullptr, *Av = nullptr;
     float4* v[2] = {nullptr, nullptr};  // CG search directions, ping-pong
     float* vweight = nullptr;  // Voronoi area
@@ -109,7 +118,14 @@ private:
     int2* c_type = nullptr;
     float* c_d = nullptr;
     float4* c_dd = nullptr;    // 4 per contact
+    // candidate pairs within the detection reach plus a skin, kept while no vertex moved more than half the
+    // skin (point-triangle: (vertex, triangle); edge-edge: (edge, edge))
+    int2* cand_pt = nullptr;
+    int2* cand_ee = nullptr;
+    size_t cap_cpt = 0, cap_cee = 0;
     float2* partial = nullptr;  // block partials of the grid-wide sums
+    void* cg_bar = nullptr;     // grid-barrier state of the cooperative CG kernel
+    int coop_max_blocks = 1, n_sm = 1;
     // LBVHs over the current triangles and edges (built at registration, refitted at every detection)
     BvhBuffers tri_bvh{}, edge_bvh{};
     char *tri_bvh_mem = nullptr, *edge_bvh_mem = nullptr;
@@ -117,7 +133,7 @@ private:
     RoundCounters *tri_rc = nullptr, *edge_rc = nullptr;
     SolverScalars* sc = nullptr;
     SolverScalars* h_sc = nullptr;
-    double* d_norm = nullptr;  // [0..2] centre, [3] scale, [4..] scratch
+    double* d_norm = nullptr;  // [0..2] centre, [3] scale, [4..6] offset t, [16..] per-block partials
     cudaStream_t stream = nullptr;  // private stream the solver runs on (capturable)
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     // captured Newton iteration
