@@ -56,6 +56,14 @@ __device__ __forceinline__ F3 normalize(F3 a) {  // Warp: zero vector when the l
 }
 __device__ __forceinline__ F3 fmin3(F3 a, F3 b) { return {fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)}; }
 __device__ __forceinline__ F3 fmax3(F3 a, F3 b) { return {fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)}; }
+// Hinge Hessians are kept as the packed upper triangle of their symmetric top-left 9x9 part (45 floats, padded
+// to 48): the reference's block_spd_project_kernel (utils_kernels.py:21-39) sets the fourth block row and
+// column to minus the sums of the first three, so H v follows from that part alone (see hvp_elements).
+constexpr int kHingeStride = 48;
+__host__ __device__ constexpr int sym9(int i, int j) {
+    return i <= j ? i * 9 - i * (i - 1) / 2 + (j - i) : j * 9 - j * (j - 1) / 2 + (i - j);
+}
+
 // one 16-byte vector atomic (sm_90+ global memory) instead of three scalar ones
 __device__ __forceinline__ void atomic_add3(float4* a, int i, F3 v) { atomicAdd(&a[i], make_float4(v.x, v.y, v.z, 0.f)); }
 // Warp's step(x): 1 when x < 0, else 0
@@ -1098,11 +1106,17 @@ __global__ void k_diff_hinge(const float4* __restrict__ x, const int4* __restric
         B[3][2] = tr(B[2][3]);
         B[2][1] = tr(B[1][2]);
         B[3][0] = tr(B[0][3]);
-        float* out = blocks + (size_t)h * 144;
-        for (int a = 0; a < 4; ++a)
-            for (int b = 0; b < 4; ++b)
-                for (int i = 0; i < 3; ++i)
-                    for (int j = 0; j < 3; ++j) out[((a * 4 + b) * 3 + i) * 3 + j] = B[a][b].m[i][j];
+        // the symmetric top-left 9x9 (blocks [0..2][0..2]) for the PSD projection
+        float* out = blocks + (size_t)h * kHingeStride;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int b = a; b < 3; ++b)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j)
+                        if (b * 3 + j >= a * 3 + i) out[sym9(a * 3 + i, b * 3 + j)] = B[a][b].m[i][j];
         const int ids[4] = {id.x, id.y, id.z, id.w};
         for (int a = 0; a < 4; ++a) atomic_add3(hd, ids[a], F3{B[a][a].m[0][0], B[a][a].m[1][1], B[a][a].m[2][2]});
     }
@@ -1115,23 +1129,14 @@ __global__ void k_diff_hinge(const float4* __restrict__ x, const int4* __restric
 __global__ void __launch_bounds__(32) k_spd_project(float* blocks, int nh, int sweeps, const SolverScalars* sc) {
     if (sc->abort) return;
     for (int h = gtid(); h < nh; h += gstride()) {
-        float* B = blocks + (size_t)h * 144;
+        float* B = blocks + (size_t)h * kHingeStride;
         // every loop below is unrolled so that A and V live in registers
         float A[9][9], V[9][9];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b)
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
-#pragma unroll
-                    for (int j = 0; j < 3; ++j) A[a * 3 + i][b * 3 + j] = B[((a * 4 + b) * 3 + i) * 3 + j];
 #pragma unroll
         for (int i = 0; i < 9; ++i)
 #pragma unroll
             for (int j = 0; j < 9; ++j) {
-                const float s = 0.5f * (A[i][j] + A[j][i]);
-                A[i][j] = s;
+                A[i][j] = B[sym9(i, j)];
                 V[i][j] = (i == j) ? 1.f : 0.f;
             }
         for (int sw = 0; sw < sweeps; ++sw) {
@@ -1181,37 +1186,9 @@ __global__ void __launch_bounds__(32) k_spd_project(float* blocks, int nh, int s
                 A[i][j] = s;
             }
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+        for (int i = 0; i < 9; ++i)
 #pragma unroll
-            for (int b = 0; b < 3; ++b)
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
-#pragma unroll
-                    for (int j = 0; j < 3; ++j) B[((a * 4 + b) * 3 + i) * 3 + j] = A[a * 3 + i][b * 3 + j];
-        // block[3][j] = -sum_i block[i][j]; block[j][3] = block[3][j]^T; block[3][3] = -sum_j block[j][3]
-        float R[3][3][3];
-#pragma unroll
-        for (int b = 0; b < 3; ++b)
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    float s = 0.f;
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) s -= A[a * 3 + i][b * 3 + j];
-                    R[b][i][j] = s;
-                    B[((3 * 4 + b) * 3 + i) * 3 + j] = s;
-                    B[((b * 4 + 3) * 3 + j) * 3 + i] = s;
-                }
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                float s = 0.f;
-#pragma unroll
-                for (int b = 0; b < 3; ++b) s -= R[b][j][i];  // block[b][3][i][j] = block[3][b][j][i]
-                B[((3 * 4 + 3) * 3 + i) * 3 + j] = s;
-            }
+            for (int j = i; j < 9; ++j) B[sym9(i, j)] = A[i][j];
     }
 }
 
@@ -1314,29 +1291,40 @@ __device__ __forceinline__ CSum hvp_elements(const float4* __restrict__ x, const
             const int h = (int)(g - e2);
             const int4 id = A.hinge[h];
             const int ids[4] = {id.x, id.y, id.z, id.w};
-            const float4* B4 = reinterpret_cast<const float4*>(A.blocks + (size_t)h * 144);
-            float Bm[144];
+            // H v with the fourth block row/column minus the sums of the first three: for w_a = v_a - v_3,
+            // (H v)_a = sum_b A_ab w_b (a < 3), (H v)_3 = -sum_a (H v)_a, and v.H v = w.A w
+            const float4* B4 = reinterpret_cast<const float4*>(A.blocks + (size_t)h * kHingeStride);
+            float Bm[kHingeStride];
 #pragma unroll
-            for (int k = 0; k < 36; ++k) {
+            for (int k = 0; k < kHingeStride / 4; ++k) {
                 const float4 b = B4[k];
                 Bm[4 * k] = b.x; Bm[4 * k + 1] = b.y; Bm[4 * k + 2] = b.z; Bm[4 * k + 3] = b.w;
             }
-            F3 d[4];
+            const F3 d3 = cg_dir(z, vprev, s, ids[3]);
+            float w[9];
 #pragma unroll
-            for (int b = 0; b < 4; ++b) d[b] = cg_dir(z, vprev, s, ids[b]);
-            float vhv = 0.f;
-#pragma unroll
-            for (int a = 0; a < 4; ++a) {
-                F3 r = {0.f, 0.f, 0.f};
-#pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const float* M = Bm + (a * 4 + b) * 9;
-                    r = r + F3{M[0] * d[b].x + M[1] * d[b].y + M[2] * d[b].z, M[3] * d[b].x + M[4] * d[b].y + M[5] * d[b].z,
-                               M[6] * d[b].x + M[7] * d[b].y + M[8] * d[b].z};
-                }
-                atomic_add3(Av, ids[a], r);
-                vhv += dot(d[a], r);
+            for (int b = 0; b < 3; ++b) {
+                const F3 wb = cg_dir(z, vprev, s, ids[b]) - d3;
+                w[3 * b] = wb.x; w[3 * b + 1] = wb.y; w[3 * b + 2] = wb.z;
             }
+            float u[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                float t = 0.f;
+#pragma unroll
+                for (int j = 0; j < 9; ++j) t += Bm[sym9(i, j)] * w[j];
+                u[i] = t;
+            }
+            float vhv = 0.f;
+            F3 sum = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const F3 ua = {u[3 * a], u[3 * a + 1], u[3 * a + 2]};
+                atomic_add3(Av, ids[a], ua);
+                sum = sum + ua;
+                vhv += w[3 * a] * ua.x + w[3 * a + 1] * ua.y + w[3 * a + 2] * ua.z;
+            }
+            atomic_add3(Av, ids[3], -sum);
             acc.add(vhv);
         } else {
             const int b = (int)(g - e3);
@@ -1463,7 +1451,8 @@ struct CgState {
 // The whole Jacobi PCG solve (cg_solver.py:96-158, n_cg_iters iterations) as one cooperative kernel: each
 // iteration is the Hessian product phase and the p/r/z phase, with a grid barrier after each. Every block
 // forms the same totals (v.Av, z.r) from the block partials in block order.
-__global__ void __launch_bounds__(kT) k_cg_solve(const float4* __restrict__ x, HvpArgs A, const float4* __restrict__ grad,
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads) k_cg_solve(const float4* __restrict__ x, HvpArgs A, const float4* __restrict__ grad,
                                                  const float4* __restrict__ hd, float4* p, float4* r, float4* z,
                                                  float4* v0, float4* v1, float4* Av, int n_iters, SolverScalars* sc,
                                                  float2* partial, CgState* bar) {
@@ -1734,7 +1723,7 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
         int dev = 0, nsm = 0, occ = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_solve, kT, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_solve<128>, 128, 0);
         coop_max_blocks = std::max(1, nsm * std::max(occ, 0));
         n_sm = std::max(1, nsm);
         // largest cluster the device runs k_cg_cluster with (16 needs the non-portable opt-in)
@@ -1813,7 +1802,7 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
         c = cap_h;
         if ((rr = grow(hinge_rest, c, n))) return rr;
         c = cap_h;
-        if ((rr = grow(hinge_blocks, c, n * 144))) return rr;
+        if ((rr = grow(hinge_blocks, c, n * kHingeStride))) return rr;
         cap_h = n;
     }
     return PAMO_OK;
@@ -1944,13 +1933,14 @@ void Stage3::newton_iteration() {
                            v[0], v[1], Av, P.n_cg_iters, sc);
         note_launch();
     } else {
-        // one cooperative launch: about one block per 256 elements, at most one block per SM
+        // one cooperative launch: about one thread per element, at most one block per SM
+        const int bt = cg_mode == 3 ? 256 : 128;
         const long long elems = (long long)NP + NT + NH;
-        int g = (int)std::min<long long>((elems + kT - 1) / kT, (long long)n_sm);
+        int g = (int)std::min<long long>((elems + bt - 1) / bt, (long long)n_sm);
         g = std::max(1, std::min(g, std::min(coop_max_blocks, kPartials / 2)));
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(g);
-        cfg.blockDim = dim3(kT);
+        cfg.blockDim = dim3(bt);
         cfg.stream = s;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeCooperative;
@@ -1958,8 +1948,12 @@ void Stage3::newton_iteration() {
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         CgState* bar = reinterpret_cast<CgState*>(cg_bar);
-        cudaLaunchKernelEx(&cfg, k_cg_solve, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r, z, v[0],
-                           v[1], Av, P.n_cg_iters, sc, partial, bar);
+        if (bt == 256)
+            cudaLaunchKernelEx(&cfg, k_cg_solve<256>, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r,
+                               z, v[0], v[1], Av, P.n_cg_iters, sc, partial, bar);
+        else
+            cudaLaunchKernelEx(&cfg, k_cg_solve<128>, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r,
+                               z, v[0], v[1], Av, P.n_cg_iters, sc, partial, bar);
         note_launch();
     }
     // step clamp, CCD, line search (system.py:441-459)
@@ -2233,7 +2227,7 @@ int pamo_stage3_set_param(pamo_stage3* s, const char* name, double value) {
     else if (n == "min_angle_thres") P.min_angle_thres = (float)value;
     else if (n == "max_blocks") P.max_blocks = (long long)value;
     else if (n == "use_cuda_graph") s->solver.use_graph = value != 0.0;
-    else if (n == "cg_mode") s->solver.cg_mode = (int)value;  // 0 or 1 grid-cooperative, 2 one cluster
+    else if (n == "cg_mode") s->solver.cg_mode = (int)value;  // 0/1 grid-cooperative (128), 2 cluster, 3 (256)
     else {
         s->solver.err = "unknown stage-3 parameter: " + n;
         return PAMO_ERR_INVALID_ARG;

@@ -73,7 +73,7 @@ public:
     Stage3Stats stats;
     std::string err;
     bool use_graph = true;  // capture one Newton iteration as a CUDA graph and replay it
-    int cg_mode = 0;        // PCG kernel: 0 or 1 grid-wide cooperative launch, 2 one thread-block cluster
+    int cg_mode = 0;        // PCG kernel: 0/1 grid-wide cooperative, 128 threads; 3: 256 threads; 2: one cluster
     int cluster_size = 1;   // CTAs of the cluster kernel (device limit, at most 16)
 
 private:
@@ -112,7 +112,7 @@ private:
     float4* el_invDm = nullptr;
     int4* hinge = nullptr;
     float2* hinge_rest = nullptr;  // (rest angle, rest edge length)
-    float* hinge_blocks = nullptr; // 16 mat33 per hinge
+    float* hinge_blocks = nullptr; // packed symmetric 9x9 Hessian part per hinge (48 floats)
     // contacts
     int4* c_idx = nullptr;
     int2* c_type = nullptr;
