@@ -76,6 +76,16 @@ int pamo_simplify_device(pamo_ctx* ctx, const float* points, const int32_t* tria
                          int64_t min_verts, int32_t* out_n_points, int32_t* out_n_triangles, int32_t* out_rounds,
                          pamo_stream stream);
 
+/*
+ * The Blender add-on's whole-loop entry point (pamo_blender/cusimpinterface.cu:55-161) with HOST pointers:
+ * in_verts [n_verts*3] float32, in_tris [n_tris*3] int32, in_out_nv_ni = {n_verts, n_tris} on entry and the
+ * output sizes on return; out_verts/out_tris must hold at least the input sizes. Scale = the largest extent of
+ * the input bounding box, no centring, rounds until 4 rounds in a row remove no face (no target), as the
+ * reference. One context per device is kept between calls, like the reference's static CUSimp_Free.
+ * Uses the current device and the legacy default stream; returns a pamo_status (the reference returns void).
+ */
+int pamo_simplify(float* in_verts, int* in_tris, float* out_verts, int* out_tris, int* in_out_nv_ni, float threshold);
+
 /* Copy the result of pamo_simplify_device (centring undone, as the reference's run() returns it). */
 int pamo_simplify_result(pamo_ctx* ctx, float* verts, int32_t* tris, pamo_stream stream);
 

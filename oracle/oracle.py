@@ -34,6 +34,7 @@ def lib():
         L.oracle_tris_mean.argtypes = [P, P, I, P]
         L.oracle_run.argtypes = [P, P, P, I, I, D, I, F, I, LL, P, P]
         L.oracle_run_result.argtypes = [P, P, P, P]
+        L.oracle_run_blender.argtypes = [P, P, P, I, I, F, P, P]
         L.oracle_self_intersect.argtypes = [P, P, P, I, I, P]
         L.oracle_self_intersect.restype = LL
         L.s3_oracle_run.argtypes = [P, P, I, I, P, P, I, I, I, P, P, P]
@@ -147,6 +148,19 @@ class Oracle:
         lib().oracle_run_result(self._h, _p(V), _p(F), _p(fpr))
         return V, F, fpr[:rounds]
 
+    def run_blender(self, points, triangles, threshold=1e-3):
+        """The Blender add-on's pamo_simplify loop: returns (verts, faces, faces_per_round)."""
+        pts = np.ascontiguousarray(points, np.float32)
+        tri = np.ascontiguousarray(triangles, np.int32)
+        onp, ont = ctypes.c_int(), ctypes.c_int()
+        rounds = lib().oracle_run_blender(self._h, _p(pts), _p(tri), len(pts), len(tri), float(threshold),
+                                          ctypes.byref(onp), ctypes.byref(ont))
+        V = np.zeros((onp.value, 3), np.float32)
+        F = np.zeros((ont.value, 3), np.int32)
+        fpr = np.zeros(max(rounds, 1), np.int32)
+        lib().oracle_run_result(self._h, _p(V), _p(F), _p(fpr))
+        return V, F, fpr[:rounds]
+
 
 # ------------------------------------------------------------------------------------------ stage 3
 STAGE3_PARAMS = ["n_newton_iters", "n_cg_iters", "n_line_search_iters", "d_hat", "coll_stiffness",
@@ -158,7 +172,7 @@ STAGE3_DEFAULTS = dict(n_newton_iters=10, n_cg_iters=40, n_line_search_iters=10,
                        ccd_max_iters=100, spd_max_iters=3, elas_young_modulus=0.1, elas_poisson_ratio=0.0,
                        hinge_stiffness=1e-2, mesh2gt_dist_stiffness=1e3, min_angle_thres=0.0, max_blocks=1 << 25)
 STAGE3_STATS = ["particles", "triangles", "edges", "hinges", "steps", "newton_iters", "max_contacts",
-                "radius_halvings", "do_nothing", "energy", "total_contacts"]
+                "radius_halvings", "do_nothing", "energy", "total_contacts"]  # the oracle's 11 entries
 
 
 def _s3_args(gt_V, gt_F, V, F, params):

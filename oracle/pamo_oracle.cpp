@@ -966,17 +966,20 @@ long long oracle_self_intersect(void* h, const float* pts, const int* tris, int 
 
 // The stage-2 round loop of PaMO.run (pamo/__init__.py:95-163) with stage 1 and stage 3 off.
 // Returns the number of rounds; the result is read with oracle_run_result.
-int oracle_run(void* h, const float* pts, const int* tris, int nP, int nT, double ratio, int tolerance, float threshold,
-               int iters, long long min_verts, int* out_nP, int* out_nT) {
+// The round loop. PaMO.run (pamo/__init__.py:95-163): centring by tris_mean, stop at the target face count or
+// at 10 faces, tolerance compared with ==. Blender entry (pamo_blender/cusimpinterface.cu:57-161, blender=true):
+// no centring, no target, stop when >= tolerance rounds in a row removed no face.
+static int run_loop(void* h, const float* pts, const int* tris, int nP, int nT, long long target, int tolerance,
+                    float threshold, int iters, bool blender, int* out_nP, int* out_nT) {
     auto* H = (pamo_oracle_handle*)h;
     Oracle& o = H->o;
     RunState& R = H->run;
-    long long target = std::max((long long)(ratio * (double)nT), min_verts);
-    float mean[3];
-    tris_mean_numpy(pts, tris, nT, mean);
+    float mean[3] = {0.f, 0.f, 0.f};
+    if (!blender) tris_mean_numpy(pts, tris, nT, mean);
     std::vector<float> verts(pts, pts + 3 * (size_t)nP);
-    for (int v = 0; v < nP; ++v)
-        for (int d = 0; d < 3; ++d) verts[3 * v + d] = verts[3 * v + d] - mean[d];
+    if (!blender)
+        for (int v = 0; v < nP; ++v)
+            for (int d = 0; d < 3; ++d) verts[3 * v + d] = verts[3 * v + d] - mean[d];
     std::vector<int> faces(tris, tris + 3 * (size_t)nT);
     float ext[3];
     for (int d = 0; d < 3; ++d) {
@@ -1013,7 +1016,7 @@ int oracle_run(void* h, const float* pts, const int* tris, int nP, int nT, doubl
         faces.swap(nf);
         const int nf_cur = (int)(faces.size() / 3);
         R.faces_per_round.push_back(nf_cur);
-        if (nf_cur <= target || nf_cur <= 10) break;
+        if (!blender && (nf_cur <= target || nf_cur <= 10)) break;
         if (nf_cur == nf_prev) {
             count++;
         } else {
@@ -1021,16 +1024,30 @@ int oracle_run(void* h, const float* pts, const int* tris, int nP, int nT, doubl
             stuck = false;
         }
         if (count >= 2) stuck = true;
-        if (count == tolerance) break;
+        if (blender ? count >= tolerance : count == tolerance) break;
     }
-    for (size_t v = 0; v < verts.size() / 3; ++v)
-        for (int d = 0; d < 3; ++d) verts[3 * v + d] = verts[3 * v + d] + mean[d];
+    if (!blender)
+        for (size_t v = 0; v < verts.size() / 3; ++v)
+            for (int d = 0; d < 3; ++d) verts[3 * v + d] = verts[3 * v + d] + mean[d];
     R.verts.swap(verts);
     R.faces.swap(faces);
     R.rounds = rounds;
     *out_nP = (int)(R.verts.size() / 3);
     *out_nT = (int)(R.faces.size() / 3);
     return rounds;
+}
+
+int oracle_run(void* h, const float* pts, const int* tris, int nP, int nT, double ratio, int tolerance, float threshold,
+               int iters, long long min_verts, int* out_nP, int* out_nT) {
+    const long long target = std::max((long long)(ratio * (double)nT), min_verts);
+    return run_loop(h, pts, tris, nP, nT, target, tolerance, threshold, iters, false, out_nP, out_nT);
+}
+
+// pamo_simplify of the Blender add-on: scale from the host bounding box of the raw vertices
+// (cusimpinterface.cu:62-75), tolerance 4, 1000000 rounds at most
+int oracle_run_blender(void* h, const float* pts, const int* tris, int nP, int nT, float threshold, int* out_nP,
+                       int* out_nT) {
+    return run_loop(h, pts, tris, nP, nT, -1, 4, threshold, 1000000, true, out_nP, out_nT);
 }
 
 void oracle_run_result(void* h, float* verts, int* faces, int* faces_per_round) {

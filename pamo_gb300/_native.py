@@ -43,6 +43,7 @@ SIGNATURES = {
         ctypes.c_int,
         [_P, _P, _P, _I32, _I32, _F64, _I32, _F32, _I32, _I64, _PI32, _PI32, _PI32, _P],
     ),
+    "pamo_simplify": (ctypes.c_int, [_P, _P, _P, _P, _P, _F32]),
     "pamo_simplify_result": (ctypes.c_int, [_P, _P, _P, _P]),
     "pamo_simplify_round_faces": (ctypes.c_int, [_P, _PI32, _I32]),
     "pamo_self_intersect": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _P, _P]),

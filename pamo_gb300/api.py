@@ -177,6 +177,23 @@ def simplify(points: torch.Tensor, triangles: torch.Tensor, ratio: float, tolera
     return verts, faces, rounds.value
 
 
+def pamo_simplify(verts, tris, threshold: float = 1e-3):
+    """The Blender add-on's whole-loop call (pamo_blender/cusimpinterface.cu:55-161) on host arrays: float32
+    [N,3] vertices and int32 [M,3] triangles in, simplified (verts, tris) NumPy arrays out. No centring, no
+    target face count: rounds run until 4 rounds in a row remove no face. Uses the current CUDA device."""
+    v = np.ascontiguousarray(verts, dtype=np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
+    vo = np.zeros_like(v)
+    to = np.zeros_like(t)
+    sh = np.array([len(v), len(t)], dtype=np.int32)
+    lib = _native.load()
+    st = lib.pamo_simplify(v.ctypes.data, t.ctypes.data, vo.ctypes.data, to.ctypes.data, sh.ctypes.data,
+                           ctypes.c_float(threshold))
+    if st != _native.PAMO_OK:
+        raise _native.PamoError(st, "pamo_simplify")
+    return vo[: sh[0]].copy(), to[: sh[1]].copy()
+
+
 def self_intersect(points: torch.Tensor, triangles: torch.Tensor, ctx: Context | None = None) -> torch.Tensor:
     """Per-face flags (uint8, CUDA) of the reference's self-intersection check over the whole mesh."""
     _check_input(points, "points", torch.float32)

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "../../include/pamo_gb300.h"
@@ -523,30 +524,34 @@ int pamo_round_stats(const pamo_ctx* ctx, int64_t* out, int32_t n) {
     return PAMO_OK;
 }
 
-int pamo_simplify_device(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
-                         int32_t n_triangles, double ratio, int32_t tolerance, float threshold, int32_t iter,
-                         int64_t min_verts, int32_t* out_n_points, int32_t* out_n_triangles, int32_t* out_rounds,
-                         pamo_stream stream) {
-    if (!ctx) return PAMO_ERR_INVALID_ARG;
-    ctx->err.clear();
-    if (n_points < 1 || n_triangles < 1 || !points || !triangles)
-        return ctx->fail(PAMO_ERR_INVALID_ARG, "invalid sizes or null pointers");
-    cudaSetDevice(ctx->device);
-    ctx->stream = (cudaStream_t)stream;
-    cudaStream_t s = ctx->stream;
+}  // extern "C"
+
+namespace {
+
+// The round loop shared by PaMO.run (simp_cuda/pamo/__init__.py:95-163: centring, stop at the target face
+// count or at 10 faces) and the Blender entry point (pamo_blender/cusimpinterface.cu:57-161: no centring,
+// no target, stop only after `tolerance` rounds without progress).
+struct LoopOptions {
+    long long target = -1;  // stop when faces <= target (negative: never)
+    bool stop_small = true; // stop when faces <= 10
+    bool centre = true;     // subtract tris_mean first
+    bool tolerance_ge = false;  // stop when count >= tolerance (Blender) instead of count == tolerance (PaMO.run)
+};
+
+int simplify_loop(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points, int32_t n_triangles,
+                  const LoopOptions& opt, int32_t tolerance, float threshold, int32_t iter, int32_t* out_n_points,
+                  int32_t* out_n_triangles, int32_t* out_rounds, cudaStream_t s) {
+    ctx->stream = s;
     ctx->have_run = false;
     ctx->faces_per_round.clear();
     for (auto& t : ctx->tot) t = 0;
     int r;
     if ((r = ctx->ensure_vertex_buffers(n_points)) || (r = ctx->ensure_face_buffers(n_triangles))) return r;
 
-    // target_faces = max(int(ratio * F), min_verts) (pamo/__init__.py:97)
-    const long long target = std::max((long long)(ratio * (double)n_triangles), (long long)min_verts);
-
     // centring and scale on the device, with numpy's float32 summation order
     ctx->prof.begin(kPhCenter, s);
     launch_center(points, triangles, n_points, n_triangles, ctx->face_mean.p, ctx->d_center, ctx->d_scale,
-                  ctx->pos_in.p, s);
+                  ctx->pos_in.p, s, opt.centre);
     ctx->prof.end(kPhCenter, s);
 
     int np = n_points, nf = n_triangles;
@@ -584,7 +589,7 @@ int pamo_simplify_device(pamo_ctx* ctx, const float* points, const int32_t* tria
         std::swap(ctx->pos_in, ctx->pos_out);
         std::swap(ctx->tri_in, ctx->tri_out);
         ctx->faces_per_round.push_back(nf);
-        if (nf <= target || nf <= 10) break;
+        if ((opt.target >= 0 && nf <= opt.target) || (opt.stop_small && nf <= 10)) break;
         if (nf == nf_prev) {
             count++;
         } else {
@@ -592,7 +597,7 @@ int pamo_simplify_device(pamo_ctx* ctx, const float* points, const int32_t* tria
             stuck = 0;
         }
         if (count >= 2) stuck = 1;
-        if (count == tolerance) break;
+        if (opt.tolerance_ge ? count >= tolerance : count == tolerance) break;
     }
     ctx->run_np = np;
     ctx->run_nt = nf;
@@ -601,6 +606,74 @@ int pamo_simplify_device(pamo_ctx* ctx, const float* points, const int32_t* tria
     if (out_n_triangles) *out_n_triangles = nf;
     if (out_rounds) *out_rounds = rounds;
     return PAMO_OK;
+}
+
+std::mutex g_blender_mu;
+pamo_ctx* g_blender_ctx[64] = {};  // one context per device, kept like the reference's static CUSimp_Free
+
+}  // namespace
+
+extern "C" {
+
+int pamo_simplify_device(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                         int32_t n_triangles, double ratio, int32_t tolerance, float threshold, int32_t iter,
+                         int64_t min_verts, int32_t* out_n_points, int32_t* out_n_triangles, int32_t* out_rounds,
+                         pamo_stream stream) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (n_points < 1 || n_triangles < 1 || !points || !triangles)
+        return ctx->fail(PAMO_ERR_INVALID_ARG, "invalid sizes or null pointers");
+    cudaSetDevice(ctx->device);
+    LoopOptions opt;
+    // target_faces = max(int(ratio * F), min_verts) (pamo/__init__.py:97)
+    opt.target = std::max((long long)(ratio * (double)n_triangles), (long long)min_verts);
+    return simplify_loop(ctx, points, triangles, n_points, n_triangles, opt, tolerance, threshold, iter, out_n_points,
+                         out_n_triangles, out_rounds, (cudaStream_t)stream);
+}
+
+int pamo_simplify(float* in_verts, int* in_tris, float* out_verts, int* out_tris, int* in_out_nv_ni, float threshold) {
+    if (!in_verts || !in_tris || !out_verts || !out_tris || !in_out_nv_ni) return PAMO_ERR_INVALID_ARG;
+    const int nv = in_out_nv_ni[0], nt = in_out_nv_ni[1];
+    if (nv < 1 || nt < 1) return PAMO_ERR_INVALID_ARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return PAMO_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_blender_mu);
+    pamo_ctx*& ctx = g_blender_ctx[dev];
+    int r;
+    if (!ctx && (r = pamo_ctx_create(&ctx, dev))) return r;
+    ctx->err.clear();
+    float* d_v = nullptr;
+    int* d_t = nullptr;
+    if (cudaMalloc((void**)&d_v, (size_t)nv * 3 * sizeof(float)) != cudaSuccess ||
+        cudaMalloc((void**)&d_t, (size_t)nt * 3 * sizeof(int)) != cudaSuccess) {
+        cudaFree(d_v);
+        cudaFree(d_t);
+        return ctx->fail(PAMO_ERR_OOM, "cudaMalloc");
+    }
+    cudaStream_t s = nullptr;
+    cudaMemcpyAsync(d_v, in_verts, (size_t)nv * 3 * sizeof(float), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_t, in_tris, (size_t)nt * 3 * sizeof(int), cudaMemcpyHostToDevice, s);
+    LoopOptions opt;
+    opt.target = -1;
+    opt.stop_small = false;
+    opt.centre = false;
+    opt.tolerance_ge = true;
+    int onv = 0, ont = 0, rounds = 0;
+    r = simplify_loop(ctx, d_v, d_t, nv, nt, opt, 4, threshold, 1000000, &onv, &ont, &rounds, s);
+    if (!r) {
+        // the result is written over the input device copies (both are at least as large)
+        launch_export_mesh(ctx->run_np, ctx->run_nt, ctx->pos_in.p, ctx->tri_in.p, ctx->d_center, d_v, d_t, s);
+        cudaMemcpyAsync(out_verts, d_v, (size_t)onv * 3 * sizeof(float), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(out_tris, d_t, (size_t)ont * 3 * sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) r = ctx->fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+        else {
+            in_out_nv_ni[0] = onv;
+            in_out_nv_ni[1] = ont;
+        }
+    }
+    cudaFree(d_v);
+    cudaFree(d_t);
+    return r;
 }
 
 int pamo_simplify_result(pamo_ctx* ctx, float* verts, int32_t* tris, pamo_stream stream) {

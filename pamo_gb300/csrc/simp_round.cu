@@ -916,10 +916,14 @@ void launch_export_mesh(int n_pts, int n_tris, const float4* pos, const int4* tr
 }
 
 void launch_center(const float* pts, const int* tris, int n_pts, int n_tris, float* face_mean, float* center,
-                   float* d_scale, float4* pos_out, cudaStream_t s) {
-    // center[0..2] = tris_mean; center[4..9] scratch (order-preserving extents)
-    k_face_means<<<grid_for(n_tris, kT), kT, 0, s>>>(pts, tris, n_tris, face_mean); note_launch();
-    k_sequential_sum<<<1, 1024, 0, s>>>(face_mean, n_tris, center); note_launch();
+                   float* d_scale, float4* pos_out, cudaStream_t s, bool centre) {
+    // center[0..2] = tris_mean (zero when not centring); center[4..9] scratch (order-preserving extents)
+    if (centre) {
+        k_face_means<<<grid_for(n_tris, kT), kT, 0, s>>>(pts, tris, n_tris, face_mean); note_launch();
+        k_sequential_sum<<<1, 1024, 0, s>>>(face_mean, n_tris, center); note_launch();
+    } else {
+        cudaMemsetAsync(center, 0, 4 * sizeof(float), s);
+    }
     unsigned* ext = (unsigned*)(center + 4);
     cudaMemsetAsync(ext, 0xFF, 3 * sizeof(unsigned), s);
     cudaMemsetAsync(ext + 3, 0x00, 3 * sizeof(unsigned), s);

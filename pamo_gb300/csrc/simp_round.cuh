@@ -76,7 +76,8 @@ void launch_export_mesh(int n_pts, int n_tris, const float4* pos, const int4* tr
 
 // ---- whole-loop helpers ----
 void launch_center(const float* pts, const int* tris, int n_pts, int n_tris, float* face_mean, float* center,
-                   float* d_scale, float4* pos_out, cudaStream_t s);
+                   float* d_scale, float4* pos_out, cudaStream_t s,
+                   bool centre = true);
 void launch_after_check(RoundCounters* rc, cudaStream_t s);
 
 }  // namespace pamo

@@ -124,3 +124,20 @@ def test_operator_input_checks():
     with pytest.raises(RuntimeError):
         op.forward(torch.from_numpy(v).double().cuda(), torch.from_numpy(f).cuda(),
                    torch.zeros(0, dtype=torch.int32).cuda(), 0, 2.0, 1e-3, False, True)
+
+
+@pytest.mark.parametrize("name", ["sphere8", "plain_small"])
+def test_blender_entry_matches_oracle(name):
+    """pamo_simplify (the Blender add-on's host-pointer whole loop) against the oracle's restatement of
+    pamo_blender/cusimpinterface.cu:57-161, twice in a row on the kept context (its state carries over)."""
+    import pamo_gb300
+    from pamo_gb300 import synth
+
+    v, f = meshes.sphere(8, L=5, sigma=0.05, seed=3) if name == "sphere8" else synth.config_mesh("plain_small")
+    o = orc.Oracle()
+    for _ in range(2):
+        V, F = pamo_gb300.pamo_simplify(v, f, 1e-3)
+        Vo, Fo, fpr = o.run_blender(v, f, 1e-3)
+        assert len(fpr) >= 5 and np.all(fpr[-4:] == fpr[-1])  # stopped after 4 rounds without progress
+        assert np.array_equal(F, Fo)
+        assert np.array_equal(V, Vo)
