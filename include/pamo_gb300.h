@@ -41,6 +41,15 @@ int pamo_ctx_destroy(pamo_ctx* ctx);
 /* Message of the last failed call on this context ("" when none). */
 const char* pamo_ctx_last_error(const pamo_ctx* ctx);
 
+/* Put the context in the state of a newly created one (as constructing a new CUDSP_Free does,
+ * simp_cuda/src/pybind.cpp:16-19): the state the reference carries between calls (stale edge costs,
+ * invalid-vertex table, previous compaction map, undo list, capacity bookkeeping) is dropped; device
+ * buffers are kept for reuse. Lets one context serve independent jobs with the results of fresh instances. */
+int pamo_ctx_reset(pamo_ctx* ctx, pamo_stream stream);
+
+/* Device memory the context currently holds, in bytes (no reference counterpart; used for admission). */
+int64_t pamo_ctx_device_bytes(const pamo_ctx* ctx);
+
 /*
  * One simplification round: CUDSP_Free.forward(points, triangles, verts_undo, n_verts_undo, scale,
  * threshold, is_stuck, init) (simp_cuda/src/pybind.cpp:52-72 -> CUSimp_Free::forward,
@@ -132,6 +141,59 @@ int pamo_profile_enable(pamo_ctx* ctx, int32_t enable);
 
 /* Accumulated milliseconds and launch counts per phase; returns the number of phases. */
 int pamo_profile_read(const pamo_ctx* ctx, double* ms, int64_t* counts, int32_t n);
+
+/* ------------------------------------------------------------------------------------------------------
+ * Many meshes on one GPU (no reference counterpart: the reference runs one PaMO object at a time). A pool of
+ * worker contexts, each on its own CUDA stream and host thread, runs the whole PaMO.run loop
+ * (pamo_simplify_device) per mesh. Every job starts from the state of a new context (pamo_ctx_reset), so each
+ * result equals the mesh's result alone.
+ * ------------------------------------------------------------------------------------------------------ */
+typedef struct pamo_batch pamo_batch;
+typedef struct pamo_server pamo_server;
+
+int pamo_batch_create(pamo_batch** out, int device, int32_t n_workers);
+int pamo_batch_destroy(pamo_batch* b);
+const char* pamo_batch_last_error(const pamo_batch* b);
+
+/* Simplify n_meshes meshes given in CSR form: points [V_total*3] float32 and triangles [F_total*3] int32 (device),
+ * mesh m owning rows vert_offsets[m]..vert_offsets[m+1] and face_offsets[m]..face_offsets[m+1] (host arrays of
+ * n_meshes+1), its triangle indices local to its own vertices; ratios[m] per mesh (host); tolerance, threshold,
+ * iter and min_verts as PaMO.run. Results (centring undone) are written packed in mesh order into out_points
+ * and out_triangles (device, room for the input sizes), with their CSR offsets in out_vert_offsets and
+ * out_face_offsets (host, n_meshes+1). Synchronises `stream`. */
+int pamo_batch_simplify(pamo_batch* b, const float* points, const int32_t* triangles, const int64_t* vert_offsets,
+                        const int64_t* face_offsets, int32_t n_meshes, const double* ratios, int32_t tolerance,
+                        float threshold, int32_t iter, int64_t min_verts, float* out_points, int32_t* out_triangles,
+                        int64_t* out_vert_offsets, int64_t* out_face_offsets, pamo_stream stream);
+
+/* Rounds each mesh of the last batch ran (host array); returns the number written. */
+int pamo_batch_rounds(const pamo_batch* b, int32_t* rounds, int32_t capacity);
+
+/* A request loop: n_workers workers; requests queue in arrival order and are admitted while the device bytes
+ * they are estimated to need (pamo_server_job_bytes) fit hbm_budget_bytes (a request larger than the budget
+ * runs alone). */
+int pamo_server_create(pamo_server** out, int device, int32_t n_workers, int64_t hbm_budget_bytes);
+int pamo_server_destroy(pamo_server* s);
+const char* pamo_server_last_error(const pamo_server* s);
+
+/* Submit one PaMO.run job (stage 2, min_verts 0) on HOST arrays (copied before returning). */
+int pamo_server_submit(pamo_server* s, const float* points, const int32_t* triangles, int32_t n_points,
+                       int32_t n_triangles, double ratio, int32_t tolerance, float threshold, int64_t* request_id);
+
+/* Wait up to timeout_ms for a finished request: returns 1 with its id, status, output sizes and times_ms[3]
+ * (queued until admitted, admitted until finished, submitted until finished), or 0 on time-out. */
+int pamo_server_wait(pamo_server* s, int32_t timeout_ms, int64_t* request_id, int32_t* status, int32_t* out_n_points,
+                     int32_t* out_n_triangles, double* times_ms);
+
+/* Copy a finished request's result into host arrays (sizes from pamo_server_wait) and release it. */
+int pamo_server_fetch(pamo_server* s, int64_t request_id, float* points, int32_t* triangles);
+
+/* Counters, out[0..n): bytes in use, most bytes in use so far, requests admitted, finished, queued, budget.
+ * Returns 6. */
+int pamo_server_stats(pamo_server* s, int64_t* out, int32_t n);
+
+/* The admission estimate of a job's device bytes. */
+int64_t pamo_server_job_bytes(int32_t n_points, int32_t n_triangles);
 
 /* ------------------------------------------------------------------------------------------------------
  * Stage 3: safe projection of the simplified mesh onto the input ("GT") mesh.

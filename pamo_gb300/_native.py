@@ -35,6 +35,8 @@ SIGNATURES = {
     "pamo_ctx_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int]),
     "pamo_ctx_destroy": (ctypes.c_int, [_P]),
     "pamo_ctx_last_error": (ctypes.c_char_p, [_P]),
+    "pamo_ctx_reset": (ctypes.c_int, [_P, _P]),
+    "pamo_ctx_device_bytes": (ctypes.c_int64, [_P]),
     "pamo_forward_round": (ctypes.c_int, [_P, _P, _P, _P, _I32, _I32, _I32, _F32, _F32, _I32, _I32, _P]),
     "pamo_round_sizes": (ctypes.c_int, [_P, _PI32, _PI32, _PI32]),
     "pamo_round_outputs": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
@@ -52,6 +54,19 @@ SIGNATURES = {
     "pamo_launch_count": (ctypes.c_int64, []),
     "pamo_profile_enable": (ctypes.c_int, [_P, _I32]),
     "pamo_profile_read": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _PI64, _I32]),
+    "pamo_batch_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, _I32]),
+    "pamo_batch_destroy": (ctypes.c_int, [_P]),
+    "pamo_batch_last_error": (ctypes.c_char_p, [_P]),
+    "pamo_batch_simplify": (ctypes.c_int, [_P, _P, _P, _P, _P, _I32, _P, _I32, _F32, _I32, _I64, _P, _P, _P, _P, _P]),
+    "pamo_batch_rounds": (ctypes.c_int, [_P, _PI32, _I32]),
+    "pamo_server_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, _I32, _I64]),
+    "pamo_server_destroy": (ctypes.c_int, [_P]),
+    "pamo_server_last_error": (ctypes.c_char_p, [_P]),
+    "pamo_server_submit": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _F64, _I32, _F32, _PI64]),
+    "pamo_server_wait": (ctypes.c_int, [_P, _I32, _PI64, _PI32, _PI32, _PI32, ctypes.POINTER(ctypes.c_double)]),
+    "pamo_server_fetch": (ctypes.c_int, [_P, _I64, _P, _P]),
+    "pamo_server_stats": (ctypes.c_int, [_P, _PI64, _I32]),
+    "pamo_server_job_bytes": (ctypes.c_int64, [_I32, _I32]),
     "pamo_stage3_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int]),
     "pamo_stage3_destroy": (ctypes.c_int, [_P]),
     "pamo_stage3_last_error": (ctypes.c_char_p, [_P]),

@@ -61,6 +61,14 @@ class Context:
         except Exception:
             pass
 
+    def reset(self) -> None:
+        """Drop the state kept between calls (as a newly created context); buffers are kept."""
+        _native.check(_native.load().pamo_ctx_reset(self.handle, _stream(self.device)), self.handle)
+
+    def device_bytes(self) -> int:
+        """Device memory the context holds."""
+        return int(_native.load().pamo_ctx_device_bytes(self.handle))
+
     def profile(self, enable: bool = True) -> None:
         """Enable (and reset) or disable the per-phase CUDA-event timers."""
         _native.check(_native.load().pamo_profile_enable(self.handle, int(enable)), self.handle)

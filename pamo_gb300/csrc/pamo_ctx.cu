@@ -31,6 +31,7 @@ template <typename T>
 struct DevBuf {
     T* p = nullptr;
     size_t n = 0;  // elements
+    size_t bytes() const { return p ? n * sizeof(T) : 0; }
 };
 
 inline uint32_t collapse_threshold(float threshold) {  // cusimp_free.cu:923, saturating
@@ -227,7 +228,12 @@ struct pamo_ctx {
         logical_pts = n + n / 5;
         const size_t len = logical_pts + 1;
         int r;
+        // the reference allocates new (here: zero-filled) buffers; a large enough one is cleared in place
         auto fresh = [&](auto& b) {
+            if (b.p && b.n >= len) {
+                cudaMemsetAsync(b.p, 0, b.n * sizeof(*b.p), stream);
+                return (int)PAMO_OK;
+            }
             if (b.p) {
                 cudaStreamSynchronize(stream);
                 cudaFree(b.p);
@@ -241,6 +247,30 @@ struct pamo_ctx {
         if ((r = fresh(undo_list))) return r;
         if ((r = fresh(tmp_undo))) return r;
         return PAMO_OK;
+    }
+
+    // State as in a newly created context (a new CUSimp_Free in the reference): no logical capacities, and
+    // the buffers the reference reads before writing zeroed when they are next sized. Buffers are kept.
+    void reset_state(cudaStream_t s) {
+        stream = s;
+        logical_pts = 0;
+        cudaMemsetAsync(d_ecap, 0, sizeof(int), s);
+        if (edge_cost.p) cudaMemsetAsync(edge_cost.p, 0, edge_cost.n * sizeof(uint32_t), s);
+        have_round = false;
+        have_run = false;
+    }
+
+    size_t device_bytes() const {
+        size_t b = 0;
+        b += pos.bytes() + orig_pos.bytes() + pos_in.bytes() + pos_out.bytes() + occ.bytes() + valence.bytes() +
+             cursor.bytes() + vedges.bytes() + vcursor.bytes() + quad.bytes() + vmin.bytes() + undo_in.bytes();
+        b += tri.bytes() + orig_tri.bytes() + tri_in.bytes() + tri_out.bytes() + ecount.bytes() + qflag.bytes() +
+             qlist.bytes() + fflags.bytes() + nt.bytes() + shuffle_flags.bytes() + fkey.bytes() + hit.bytes() +
+             edges.bytes() + win.bytes() + collapsed.bytes() + uflag.bytes() + eorder.bytes() + exact_list.bytes() +
+             face_mean.bytes();
+        b += edge_cost.bytes() + invalid.bytes() + pts_map.bytes() + undo_list.bytes() + tmp_undo.bytes();
+        b += bvh_cap ? bvh_bytes((int)bvh_cap) : 0;
+        return b;
     }
 
     int ensure_vertex_buffers(size_t n) {
@@ -470,6 +500,16 @@ int pamo_ctx_destroy(pamo_ctx* ctx) {
 }
 
 const char* pamo_ctx_last_error(const pamo_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int pamo_ctx_reset(pamo_ctx* ctx, pamo_stream stream) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    ctx->err.clear();
+    ctx->reset_state((cudaStream_t)stream);
+    return ctx->check(cudaGetLastError(), "reset");
+}
+
+int64_t pamo_ctx_device_bytes(const pamo_ctx* ctx) { return ctx ? (int64_t)ctx->device_bytes() : -1; }
 
 int pamo_forward_round(pamo_ctx* ctx, const float* points, const int32_t* triangles, const int32_t* verts_undo,
                        int32_t n_verts_undo, int32_t n_points, int32_t n_triangles, float scale, float threshold,
