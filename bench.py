@@ -4,7 +4,7 @@ where the configuration turns it on, stage 3 (barrier/CCD Newton-CG safe project
 One step = one whole job of PaMO.run (stage 2 loop, then stage 3's 5 projection steps) on the configured
 synthetic mesh, with its inputs already resident in HBM. Prints one JSON line (rank 0).
 
-    python bench.py [--steps K] [--warmup W] [--config plain_large|plain_small] [--impl gb300|reference]
+    python bench.py [--steps K] [--warmup W] [--config plain_large|plain_small|batch256|serve] [--impl gb300|reference]
 
 Multi-GPU: a mesh does not shard (every round needs a whole-mesh independent set and intersection check),
 so N GPUs run N independent replicas of the job ("replicas only"); value = N * input faces / slowest rank.
@@ -218,15 +218,168 @@ def run_reference(args):
     return 0
 
 
+def synth_batch(n_meshes, f_lo, f_hi, seed):
+    """Star-shaped meshes with face counts log-uniform in [f_lo, f_hi] (icosphere frequency round(sqrt(F/20))),
+    SH l <= 6, c ~ N(0, 0.03^2), one seed per mesh; ratios uniform in [0.001, 0.01]."""
+    from pamo_gb300 import synth
+
+    rng = np.random.default_rng(seed)
+    fs = np.exp(rng.uniform(np.log(f_lo), np.log(f_hi), n_meshes))
+    ns = np.maximum(1, np.round(np.sqrt(fs / 20.0)).astype(int))
+    ratios = rng.uniform(0.001, 0.01, n_meshes)
+    meshes = [synth.star_mesh(int(n), 6, lambda l: 0.03, seed * 100000 + i) for i, n in enumerate(ns)]
+    return meshes, ratios
+
+
+def run_batch(args):
+    """Batching: 256 meshes (5k-200k faces) per step through the worker pool, against the plain path (one
+    context, one mesh after the other) on the same meshes."""
+    import torch
+
+    import pamo_gb300
+    from pamo_gb300.batch import Batch, pack, unpack
+
+    dev = torch.device("cuda", 0)
+    meshes, ratios = synth_batch(256, 5e3, 2e5, 7)
+    P, T, voff, foff = pack(meshes)
+    F0 = int(foff[-1])
+    Pd, Td = torch.from_numpy(P).to(dev), torch.from_numpy(T).to(dev)
+    # plain path: one context, fresh state per mesh, sequential
+    ctx = pamo_gb300.Context(dev)
+    plain_out = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(len(meshes)):
+        ctx.reset()
+        V, Fo, _ = pamo_gb300.simplify(Pd[voff[i]:voff[i + 1]], Td[foff[i]:foff[i + 1]], float(ratios[i]), TOLERANCE,
+                                      THRESHOLD, 1000000, 0, ctx=ctx)
+        plain_out.append((V, Fo))
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    b = Batch(dev, workers=args.workers)
+    for _ in range(args.warmup):
+        out = b.simplify_csr(Pd, Td, voff, foff, ratios)
+    stream = torch.cuda.current_stream(dev)
+    launches0 = pamo_gb300.launch_count()
+    ms = []
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = b.simplify_csr(Pd, Td, voff, foff, ratios)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+    launches = pamo_gb300.launch_count() - launches0
+    res = unpack(*out)
+    identical = all(np.array_equal(res[i][1], plain_out[i][1].cpu().numpy()) and
+                    np.array_equal(res[i][0], plain_out[i][0].cpu().numpy()) for i in range(len(meshes)))
+    # end to end: host arrays in, host arrays out
+    e2e = []
+    Ph, Th = torch.from_numpy(P).pin_memory(), torch.from_numpy(T).pin_memory()
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        o = b.simplify_csr(Ph.to(dev, non_blocking=True), Th.to(dev, non_blocking=True), voff, foff, ratios)
+        host = (o[0].cpu().numpy(), o[1].cpu().numpy())
+        e2e.append(time.perf_counter() - t0)
+    value = F0 / (float(np.mean(ms)) / 1000.0)
+    line = {
+        "metric": "input faces/s, batch of 256 meshes", "value": value, "unit": "input faces/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(ms)), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batch256: 256 star meshes, faces log-uniform 5k-200k (" + str(F0) + " faces), ratios "
+                               "U[0.001,0.01], threshold 1e-3, tolerance 4, min_verts 0",
+                   "workers": args.workers, "parallelism": "one GPU, worker contexts on separate streams"},
+        "plain": {"value": F0 / plain_s, "seconds": plain_s, "how": "one context, one mesh after the other"},
+        "vs_plain": (F0 / (float(np.mean(ms)) / 1000.0)) / (F0 / plain_s),
+        "identical_to_plain": bool(identical),
+        "e2e": {"value": F0 / float(np.mean(e2e)), "unit": "input faces/s", "h2d_bytes_per_step": int(P.nbytes + T.nbytes),
+                "d2h_bytes_per_step": int(host[0].nbytes + host[1].nbytes)},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_serve(args):
+    """Serving: a Poisson stream of requests (mean 50/s), faces log-uniform in [10k, 2M], ratios U[0.001,0.01],
+    admitted by an 80 GB device-memory budget; p50/p99 latency (arrival to result) and faces/s, against the
+    plain path (the same stream through one worker)."""
+    import torch
+
+    from pamo_gb300.batch import Server
+
+    n_req = args.requests
+    pool, _ = synth_batch(48, 1e4, 2e6, 11)  # distinct meshes the requests draw from
+    rng = np.random.default_rng(12)
+    pick = rng.integers(0, len(pool), n_req)
+    ratios = rng.uniform(0.001, 0.01, n_req)
+    arrivals = np.cumsum(rng.exponential(1.0 / 50.0, n_req))
+    F_total = int(sum(len(pool[k][1]) for k in pick))
+
+    def stream(workers):
+        srv = Server("cuda:0", workers=workers, hbm_budget_bytes=80 << 30)
+        lat = np.zeros(n_req)
+        ids = {}
+        t0 = time.perf_counter()
+        done = 0
+        i = 0
+        while done < n_req:
+            now = time.perf_counter() - t0
+            while i < n_req and arrivals[i] <= now:
+                v, f = pool[pick[i]]
+                ids[srv.submit(v, f, float(ratios[i]))] = i
+                i += 1
+            w = srv.wait(1 if i < n_req else 1000)
+            while w is not None:
+                rid, st, npt, ntr, times = w
+                if st != 0:
+                    raise RuntimeError(f"request {rid} failed with status {st}")
+                k = ids[rid]
+                srv.fetch(rid, npt, ntr)
+                lat[k] = (time.perf_counter() - t0) - arrivals[k]
+                done += 1
+                w = srv.wait(0)
+        wall = time.perf_counter() - t0
+        stats = srv.stats()
+        srv.close()
+        return lat, wall, stats
+
+    lat, wall, stats = stream(args.workers)
+    lat1, wall1, _ = stream(1)
+    line = {
+        "metric": "serving p50/p99 latency and input faces/s", "value": F_total / wall, "unit": "input faces/s",
+        "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": wall * 1000.0, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"serve: {n_req} requests, Poisson arrivals mean 50/s, faces log-uniform 10k-2M drawn "
+                               f"from 48 distinct meshes, ratios U[0.001,0.01], 80 GB budget", "workers": args.workers},
+        "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3)},
+        "plain": {"value": F_total / wall1, "latency_ms": {"p50": float(np.percentile(lat1, 50) * 1e3),
+                                                           "p99": float(np.percentile(lat1, 99) * 1e3)},
+                  "how": "the same stream through one worker"},
+        "server": stats,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--config", default="plain_large", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="plain_large", choices=sorted(CONFIGS) + ["batch256", "serve"])
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workers", type=int, default=8, help="worker contexts for --config batch256 / serve")
+    ap.add_argument("--requests", type=int, default=2000, help="requests for --config serve")
     args = ap.parse_args()
+    if args.config == "batch256":
+        return run_batch(args)
+    if args.config == "serve":
+        return run_serve(args)
     if args.impl == "reference":
         return run_reference(args)
 
