@@ -50,6 +50,13 @@ int pamo_ctx_reset(pamo_ctx* ctx, pamo_stream stream);
 /* Device memory the context currently holds, in bytes (no reference counterpart; used for admission). */
 int64_t pamo_ctx_device_bytes(const pamo_ctx* ctx);
 
+/* Execution options of pamo_simplify_device (results are the same with any setting):
+ *   "device_rounds" (default 1): rounds after the first read their sizes and loop state from device memory
+ *                                and synchronise once per round (plus once per extra undo pass);
+ *   "graphs"        (default 1): those rounds run as CUDA graphs cached per size class.
+ * The phase timers (pamo_profile_enable) use the host-sized path. */
+int pamo_ctx_set_option(pamo_ctx* ctx, const char* name, int64_t value);
+
 /*
  * One simplification round: CUDSP_Free.forward(points, triangles, verts_undo, n_verts_undo, scale,
  * threshold, is_stuck, init) (simp_cuda/src/pybind.cpp:52-72 -> CUSimp_Free::forward,

@@ -65,6 +65,10 @@ class Context:
         """Drop the state kept between calls (as a newly created context); buffers are kept."""
         _native.check(_native.load().pamo_ctx_reset(self.handle, _stream(self.device)), self.handle)
 
+    def set_option(self, name: str, value: int) -> None:
+        """Execution options of the whole loop ("device_rounds", "graphs"); results do not depend on them."""
+        _native.check(_native.load().pamo_ctx_set_option(self.handle, name.encode(), int(value)), self.handle)
+
     def device_bytes(self) -> int:
         """Device memory the context holds."""
         return int(_native.load().pamo_ctx_device_bytes(self.handle))

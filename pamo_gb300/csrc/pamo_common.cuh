@@ -50,6 +50,17 @@ struct RoundCounters {
     int pad[6];
 };
 
+// State of the PaMO.run loop kept on the device between rounds, so that a round can run without host input
+// (pamo/__init__.py:131-159: sizes after compaction, undo vertices carried to the next call, the no-progress
+// count and is_stuck).
+struct LoopState {
+    int np, nf;    // vertices and faces the round starts with
+    int nu;        // undo vertices carried into the round
+    int is_stuck;
+    int count;     // rounds in a row without progress
+    int pad[3];
+};
+
 struct Quadric {  // symmetric 4x4: a = (m00 m01 m02 m03), b = (m11 m12 m13 m22), c = (m23 m33 - -)
     float4 a, b, c;
 };

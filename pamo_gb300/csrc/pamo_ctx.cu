@@ -10,7 +10,9 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "../../include/pamo_gb300.h"
@@ -137,6 +139,27 @@ struct pamo_ctx {
     int* scan_scratch = nullptr;
     float* d_scale = nullptr;
     float* d_center = nullptr;  // [16]
+    LoopState* d_ls = nullptr;  // [0] this round, [1] the next one
+    cudaStream_t own_stream = nullptr;  // for callers on the legacy default stream (graphs need a capturable one)
+    cudaEvent_t ev_join = nullptr;
+
+    int ensure_own_stream() {
+        if (own_stream) return PAMO_OK;
+        if (cudaStreamCreateWithFlags(&own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming) != cudaSuccess)
+            return fail(PAMO_ERR_CUDA, "stream creation");
+        return PAMO_OK;
+    }
+
+    // captured device-driven rounds: (input buffer, face class, vertex class, kind) -> graph; dropped whenever
+    // a buffer is reallocated (kernel arguments hold the buffer addresses)
+    struct RoundGraph {
+        cudaGraphExec_t exec = nullptr;
+        long long kernels = 0;
+    };
+    std::map<std::tuple<const void*, int, int, int>, RoundGraph> graphs;
+    bool use_graphs = true;     // device rounds as cached graphs
+    bool device_rounds = true;  // rounds after the first from device-resident sizes (pamo_simplify_device)
     DevBuf<float> face_mean;
     float* h_pinned_f = nullptr;
 
@@ -165,9 +188,16 @@ struct pamo_ctx {
         return fail(e == cudaErrorMemoryAllocation ? PAMO_ERR_OOM : PAMO_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
     }
 
+    void drop_graphs() {
+        for (auto& kv : graphs)
+            if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        graphs.clear();
+    }
+
     template <typename T>
     int grow(DevBuf<T>& b, size_t n, bool keep = false, bool zero = false) {
         if (b.n >= n && b.p) return PAMO_OK;
+        drop_graphs();
         T* p = nullptr;
         cudaError_t e = cudaMalloc((void**)&p, n * sizeof(T));
         if (e != cudaSuccess) return check(e, "cudaMalloc");
@@ -192,6 +222,7 @@ struct pamo_ctx {
         if ((r = check(cudaMalloc((void**)&d_ecap, sizeof(int)), "cudaMalloc"))) return r;
         if ((r = check(cudaMalloc((void**)&d_scale, sizeof(float)), "cudaMalloc"))) return r;
         if ((r = check(cudaMalloc((void**)&d_center, 16 * sizeof(float)), "cudaMalloc"))) return r;
+        if ((r = check(cudaMalloc((void**)&d_ls, 2 * sizeof(LoopState)), "cudaMalloc"))) return r;
         cudaMemset(d_ecap, 0, sizeof(int));
         return PAMO_OK;
     }
@@ -218,6 +249,12 @@ struct pamo_ctx {
         if (d_ecap) cudaFree(d_ecap);
         if (d_scale) cudaFree(d_scale);
         if (d_center) cudaFree(d_center);
+        if (d_ls) cudaFree(d_ls);
+        drop_graphs();
+        if (own_stream) cudaStreamDestroy(own_stream);
+        if (ev_join) cudaEventDestroy(ev_join);
+        own_stream = nullptr;
+        ev_join = nullptr;
         rc = nullptr;
     }
 
@@ -302,6 +339,7 @@ struct pamo_ctx {
         // edge costs keep their stale contents when the physical buffer grows
         if ((r = grow(edge_cost, 2 * nc + 2 * nc / 5 + 2, true, true))) return r;
         if (bvh_cap < nc) {
+            drop_graphs();
             if (bvh_mem) {
                 cudaStreamSynchronize(stream);
                 cudaFree(bvh_mem);
@@ -324,6 +362,108 @@ struct pamo_ctx {
         r = check(cudaStreamSynchronize(stream), "round");
         prof.collect();
         return r;
+    }
+
+    // One device-driven round (the rounds after the first in pamo_simplify_device): every size and flag comes
+    // from d_ls and rc, and nPb/nTb only bound the grids, so the same launches serve every round of a size
+    // class and can be captured as a graph. kind 0: the whole round, with the compaction and the next round's
+    // state computed as if no undo pass follows; kind 1: one more undo pass (cusimp_free.cu:1016-1040), then
+    // the compaction and next state again. The same kernels and order as round() plus the compaction of
+    // simplify_loop.
+    void round_dev(int kind, int nPb, int nTb, float threshold) {
+        cudaStream_t s = stream;
+        const int* nt_off = valence.p;
+        const int eb = 2 * nTb;
+        const int list_cap = (int)undo_list.n;
+        const uint32_t collapse_t = collapse_threshold(threshold);
+        if (kind == 0) {
+            launch_round_begin(rc, d_ls, d_ls + 1, s);
+            launch_undo_bookkeeping_dev(undo_in.p, d_ls, list_cap, tmp_undo.p, undo_list.p, pts_map.p, (int)pts_map.n,
+                                        invalid.p, (int)invalid.n, s);
+            launch_load_points4_dev(pos_in.p, rc, nPb, pos.p, orig_pos.p, occ.p, s);
+            launch_copy_tris_dev(tri_in.p, tri.p, rc, nTb, s);
+            launch_copy_tris_dev(tri.p, orig_tri.p, rc, nTb, s);
+            launch_zero_vertex_counts_dev(rc, nPb, valence.p, cursor.p, vedges.p, vcursor.p, s);
+            launch_face_counts(tri.p, rc, nTb, valence.p, ecount.p, vedges.p, s);
+            exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
+            exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s);
+            exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
+            launch_fill_adjacency(tri.p, rc, nTb, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p,
+                                  eorder.p, s);
+            launch_sort_adjacency(rc, nPb, valence.p, nt.p, s);
+            launch_quadrics(rc, nPb, nt_off, nt.p, tri.p, pos.p, quad.p, s);
+            launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
+            launch_fill_u64_dev(rc, nPb, vmin.p, ~0ull, s);
+            launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, invalid.p, edge_cost.p,
+                             vmin.p, d_scale, threshold, 0, s, &d_ls->is_stuck);
+            launch_face_keys(rc, nTb, tri.p, vmin.p, fkey.p, s);
+            launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p,
+                            pos.p, orig_pos.p, occ.p, win.p, s);
+            exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s);
+            launch_compact_winners(rc, eb, win.p, collapsed.p, s);
+            launch_remove_invalid(rc, nTb, tri.p, s);
+            launch_line_edges(rc, eb, edges.p, nt_off, nt.p, tri.p, pos.p, occ.p, nullptr, (int)collapsed.n,
+                              collapsed.p, s);
+            launch_zero_face_ints_dev(rc, nTb, qflag.p, s);
+            launch_mark_query(rc, eb, collapsed.p, edges.p, nt_off, nt.p, qflag.p, s);
+            exclusive_scan(qflag.p, qflag.p, &rc->n_tris, 1, &rc->n_query, scan_scratch, s);
+            launch_compact_flags(qflag.p, nTb, &rc->n_tris, qlist.p, s);
+        } else {
+            launch_undo_apply(rc, eb, collapsed.p, uflag.p, edges.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p, orig_pos.p,
+                              occ.p, tmp_undo.p, undo_list.p, pts_map.p, list_cap, s);
+        }
+        // intersection check
+        launch_zero_face_bytes_dev(rc, nTb, hit.p, s);
+        bvh_build(bvh, tri.p, pos.p, rc, nTb, s);
+        bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, (int)exact_list.n, rc, nTb, kTriEps, s);
+        launch_undo_check(rc, eb, collapsed.p, edges.p, nt_off, nt.p, hit.p, uflag.p, s);
+        exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s);
+        launch_after_check(rc, s);
+        // compaction map (cusimp_free.cu:1042-1045), compaction (pamo/__init__.py:136-140), next round's state
+        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
+        launch_live_flags(rc, nTb, tri.p, fflags.p, s);
+        exclusive_scan(fflags.p, fflags.p, &rc->n_tris, 1, nullptr, scan_scratch, s);
+        launch_compact_mesh(rc, nPb, nTb, pos.p, occ.p, pts_map.p, tri.p, fflags.p, pos_out.p, tri_out.p, s);
+        launch_round_end(rc, d_ls, d_ls + 1, undo_list.p, undo_in.p, (int)std::min(undo_in.n, undo_list.n), list_cap, s);
+    }
+
+    // Enqueue round_dev through a cached graph of its size class (or directly when graphs are off or the
+    // phase timers are on).
+    int run_round_dev(int kind, int np, int nf, float threshold) {
+        // size class: the next power of two from 1024 up to 2^19; every grid is at its cap from 2^19 elements on,
+        // and all loops are grid-stride over the device sizes
+        auto cls = [](int n) {
+            int b = 1024;
+            while (b < n && b < (1 << 19)) b <<= 1;
+            return b;
+        };
+        const int nPb = cls(np), nTb = cls(nf);
+        if (!use_graphs || prof.on) {
+            round_dev(kind, nPb, nTb, threshold);
+            return check(cudaGetLastError(), "kernel launch");
+        }
+        int tbits;
+        std::memcpy(&tbits, &threshold, sizeof(int));
+        const auto key = std::make_tuple((const void*)pos_in.p, nTb * 2 + kind, nPb, tbits);
+        auto it = graphs.find(key);
+        if (it == graphs.end()) {
+            cudaGraph_t g = nullptr;
+            if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+                return fail(PAMO_ERR_CUDA, "stream capture");
+            const long long l0 = launches_so_far();
+            round_dev(kind, nPb, nTb, threshold);
+            RoundGraph rg;
+            rg.kernels = launches_so_far() - l0;
+            note_launches(-rg.kernels);  // counted when the graph runs
+            if (cudaStreamEndCapture(stream, &g) != cudaSuccess || !g) return fail(PAMO_ERR_CUDA, "stream capture");
+            const cudaError_t e = cudaGraphInstantiate(&rg.exec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail(PAMO_ERR_CUDA, "graph instantiation");
+            it = graphs.emplace(key, rg).first;
+        }
+        if (cudaGraphLaunch(it->second.exec, stream) != cudaSuccess) return fail(PAMO_ERR_CUDA, "graph launch");
+        note_launches(it->second.kernels);
+        return PAMO_OK;
     }
 
     int status_to_error(int bits) {
@@ -511,6 +651,15 @@ int pamo_ctx_reset(pamo_ctx* ctx, pamo_stream stream) {
 
 int64_t pamo_ctx_device_bytes(const pamo_ctx* ctx) { return ctx ? (int64_t)ctx->device_bytes() : -1; }
 
+int pamo_ctx_set_option(pamo_ctx* ctx, const char* name, int64_t value) {
+    if (!ctx || !name) return PAMO_ERR_INVALID_ARG;
+    const std::string n(name);
+    if (n == "graphs") ctx->use_graphs = value != 0;
+    else if (n == "device_rounds") ctx->device_rounds = value != 0;
+    else return ctx->fail(PAMO_ERR_INVALID_ARG, "unknown option %s", name);
+    return PAMO_OK;
+}
+
 int pamo_forward_round(pamo_ctx* ctx, const float* points, const int32_t* triangles, const int32_t* verts_undo,
                        int32_t n_verts_undo, int32_t n_points, int32_t n_triangles, float scale, float threshold,
                        int32_t is_stuck, int32_t init, pamo_stream stream) {
@@ -578,9 +727,33 @@ struct LoopOptions {
     bool tolerance_ge = false;  // stop when count >= tolerance (Blender) instead of count == tolerance (PaMO.run)
 };
 
+int simplify_loop_on(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                     int32_t n_triangles, const LoopOptions& opt, int32_t tolerance, float threshold, int32_t iter,
+                     int32_t* out_n_points, int32_t* out_n_triangles, int32_t* out_rounds, cudaStream_t s);
+
+// Graphs cannot be captured on the legacy default stream: the loop then runs on the context's own stream,
+// ordered after the caller's work and before the caller's next work by events.
 int simplify_loop(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points, int32_t n_triangles,
                   const LoopOptions& opt, int32_t tolerance, float threshold, int32_t iter, int32_t* out_n_points,
                   int32_t* out_n_triangles, int32_t* out_rounds, cudaStream_t s) {
+    if (s != nullptr && s != cudaStreamLegacy)
+        return simplify_loop_on(ctx, points, triangles, n_points, n_triangles, opt, tolerance, threshold, iter,
+                                out_n_points, out_n_triangles, out_rounds, s);
+    int r;
+    if ((r = ctx->ensure_own_stream())) return r;
+    cudaEventRecord(ctx->ev_join, s);
+    cudaStreamWaitEvent(ctx->own_stream, ctx->ev_join, 0);
+    r = simplify_loop_on(ctx, points, triangles, n_points, n_triangles, opt, tolerance, threshold, iter, out_n_points,
+                         out_n_triangles, out_rounds, ctx->own_stream);
+    cudaEventRecord(ctx->ev_join, ctx->own_stream);
+    cudaStreamWaitEvent(s, ctx->ev_join, 0);
+    ctx->stream = s;
+    return r;
+}
+
+int simplify_loop_on(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                     int32_t n_triangles, const LoopOptions& opt, int32_t tolerance, float threshold, int32_t iter,
+                     int32_t* out_n_points, int32_t* out_n_triangles, int32_t* out_rounds, cudaStream_t s) {
     ctx->stream = s;
     ctx->have_run = false;
     ctx->faces_per_round.clear();
@@ -597,14 +770,55 @@ int simplify_loop(pamo_ctx* ctx, const float* points, const int32_t* triangles, 
     int np = n_points, nf = n_triangles;
     int nu = 0;
     int count = 0, stuck = 0, init = 1, rounds = 0;
+    // rounds after the first run from device-resident sizes and state (optionally as cached graphs); with the
+    // phase timers on, every round takes the host-sized path that times each phase
+    const bool dev_rounds = ctx->device_rounds && !ctx->prof.on;
+    if (dev_rounds) {
+        LoopState L = {};
+        L.np = n_points;
+        L.nf = n_triangles;
+        cudaMemcpyAsync(ctx->d_ls, &L, sizeof(L), cudaMemcpyHostToDevice, s);
+    }
     for (int it = 0; it < iter; ++it) {
         const int nf_prev = nf;
-        if (nu > 0) cudaMemcpyAsync(ctx->undo_in.p, ctx->undo_list.p, nu * sizeof(int), cudaMemcpyDeviceToDevice, s);
-        if (init) r = ctx->round(nullptr, ctx->pos_in.p, triangles, nullptr, ctx->undo_in.p, nu, np, nf, threshold, stuck,
-                                 init, false);
-        else r = ctx->round(nullptr, ctx->pos_in.p, nullptr, ctx->tri_in.p, ctx->undo_in.p, nu, np, nf, threshold, stuck,
-                            init, false);
-        if (r) return r;
+        if (!dev_rounds || init) {
+            if (nu > 0) cudaMemcpyAsync(ctx->undo_in.p, ctx->undo_list.p, nu * sizeof(int), cudaMemcpyDeviceToDevice, s);
+            if (init) r = ctx->round(nullptr, ctx->pos_in.p, triangles, nullptr, ctx->undo_in.p, nu, np, nf, threshold,
+                                     stuck, init, false);
+            else r = ctx->round(nullptr, ctx->pos_in.p, nullptr, ctx->tri_in.p, ctx->undo_in.p, nu, np, nf, threshold,
+                                stuck, init, false);
+            if (r) return r;
+            nu = ctx->last.n_vertices_undo;
+            // the device rounds copy the undo list into undo_in themselves: size it once for the whole list
+            if ((r = ctx->grow(ctx->undo_in, dev_rounds ? std::max((size_t)nu + 1, ctx->undo_list.n) : (size_t)nu + 1)))
+                return r;
+            // compaction (pamo/__init__.py:136-140)
+            ctx->prof.begin(kPhCompact, s);
+            launch_live_flags(ctx->rc, nf, ctx->tri.p, ctx->fflags.p, s);
+            exclusive_scan(ctx->fflags.p, ctx->fflags.p, &ctx->rc->n_tris, 1, nullptr, ctx->scan_scratch, s);
+            launch_compact_mesh(ctx->rc, np, nf, ctx->pos.p, ctx->occ.p, ctx->pts_map.p, ctx->tri.p, ctx->fflags.p,
+                                ctx->pos_out.p, ctx->tri_out.p, s);
+            ctx->prof.end(kPhCompact, s);
+            if (dev_rounds)
+                launch_round_end(ctx->rc, ctx->d_ls, ctx->d_ls + 1, ctx->undo_list.p, ctx->undo_in.p,
+                                 (int)std::min(ctx->undo_in.n, ctx->undo_list.n), (int)ctx->undo_list.n, s);
+            if ((r = ctx->read_counters())) return r;
+        } else {
+            if ((r = ctx->run_round_dev(0, np, nf, threshold))) return r;
+            if ((r = ctx->read_counters())) return r;
+            int extra = 0;
+            while (ctx->h_rc->n_undo != 0) {  // cusimp_free.cu:1016-1040
+                ++extra;
+                if ((r = ctx->run_round_dev(1, np, nf, threshold))) return r;
+                if ((r = ctx->read_counters())) return r;
+                if (extra == kMaxExtraPasses) break;
+            }
+            if ((r = ctx->status_to_error(ctx->h_rc->status))) return r;
+            if ((size_t)ctx->h_rc->n_vertices_undo > ctx->undo_list.n)
+                return ctx->fail(PAMO_ERR_CAPACITY, "undo-vertex list longer than its capacity");
+            ctx->last = *ctx->h_rc;
+            ctx->have_round = true;
+        }
         ++rounds;
         init = 0;
         {
@@ -614,16 +828,6 @@ int simplify_loop(pamo_ctx* ctx, const float* points, const int32_t* triangles, 
             t[4] += (long long)c.n_query * c.passes; t[5] += (long long)c.n_pairs; t[6] += (long long)c.n_exact;
             t[7] += c.passes; t[8] += (long long)c.n_live * c.passes; t[9] += c.n_collapsed;
         }
-        nu = ctx->last.n_vertices_undo;
-        if ((r = ctx->grow(ctx->undo_in, (size_t)nu + 1))) return r;
-        // compaction (pamo/__init__.py:136-140)
-        ctx->prof.begin(kPhCompact, s);
-        launch_live_flags(ctx->rc, nf, ctx->tri.p, ctx->fflags.p, s);
-        exclusive_scan(ctx->fflags.p, ctx->fflags.p, &ctx->rc->n_tris, 1, nullptr, ctx->scan_scratch, s);
-        launch_compact_mesh(ctx->rc, np, nf, ctx->pos.p, ctx->occ.p, ctx->pts_map.p, ctx->tri.p, ctx->fflags.p,
-                            ctx->pos_out.p, ctx->tri_out.p, s);
-        ctx->prof.end(kPhCompact, s);
-        if ((r = ctx->read_counters())) return r;
         np = ctx->h_rc->n_pts_out;
         nf = ctx->h_rc->n_tris_out;
         std::swap(ctx->pos_in, ctx->pos_out);

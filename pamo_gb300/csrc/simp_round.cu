@@ -321,7 +321,8 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
                                                   const int4* __restrict__ tri, const float4* __restrict__ pos,
                                                   const Quadric* __restrict__ q, const unsigned char* __restrict__ invalid,
                                                   uint32_t* cost, unsigned long long* vmin, const float* d_scale,
-                                                  float tres, int is_stuck) {
+                                                  float tres, int is_stuck_host, const int* is_stuck_dev) {
+    const int is_stuck = is_stuck_dev ? *is_stuck_dev : is_stuck_host;
     const int n = rc->n_edges;
     const float scale = *d_scale;
     for (int i = gtid(); i < n; i += gstride()) {
@@ -750,6 +751,111 @@ __global__ void k_extents(const unsigned* ext, float* scale) {
     *scale = (ez > m) ? ez : m;
 }
 
+// ================================================================== device-driven rounds
+// The same steps as the host-sized launchers, with every size read from the device (LoopState, RoundCounters),
+// so that one captured graph serves every round of a size class.
+
+// *ls = *next; the round's counters as forward() sets them (a stuck round starts its undo list with the
+// carried-over entries)
+__global__ void k_round_begin(RoundCounters* rc, LoopState* ls, const LoopState* next) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const LoopState L = *next;
+    *ls = L;
+    RoundCounters z = {};
+    z.n_pts = L.np;
+    z.n_tris = L.nf;
+    if (L.is_stuck) {
+        z.first_undo = L.nu;
+        z.n_vertices_undo = L.nu;
+    }
+    *rc = z;
+}
+
+// not stuck and undo vertices carried in: the invalid table is cleared (cusimp_free.cu:905-908)
+__global__ void k_invalid_clear_dev(const LoopState* ls, unsigned char* invalid, int len) {
+    if (ls->is_stuck || ls->nu == 0) return;
+    for (int i = gtid(); i < len; i += gstride()) invalid[i] = 0;
+}
+
+// stuck: the undo list restarts from the carried vertices mapped through the previous map (:869-878);
+// then the carried vertices are marked invalid (:880-889)
+__global__ void k_undo_book_dev(const int* __restrict__ verts_undo, const LoopState* ls, int* tmp_undo, int* undo_list,
+                                const int* __restrict__ pts_map, int map_len, unsigned char* invalid, int len) {
+    const int n = ls->nu;
+    const bool stuck = ls->is_stuck != 0;
+    for (int a = gtid(); a < n; a += gstride()) {
+        const int x = verts_undo[a];
+        if (stuck) {
+            tmp_undo[a] = x;
+            undo_list[a] = (x >= 0 && x < map_len) ? pts_map[x] : 0;
+        }
+        if (x >= 0 && x < len) invalid[x] = 1;
+    }
+}
+
+__global__ void k_load_points4_dev(const float4* __restrict__ pts, const RoundCounters* rc, float4* pos, float4* orig,
+                                   int* occ) {
+    const int n = rc->n_pts;
+    for (int v = gtid(); v < n; v += gstride()) {
+        const float4 p = pts[v];
+        pos[v] = p;
+        orig[v] = p;
+        occ[v] = 1;
+    }
+    if (gtid() == 0) occ[n] = 0;
+}
+
+__global__ void k_copy_tris_dev(const int4* __restrict__ src, int4* dst, const RoundCounters* rc) {
+    const int n = rc->n_tris;
+    for (int f = gtid(); f < n; f += gstride()) dst[f] = src[f];
+}
+
+// valence, cursor, vedges, vcursor = 0 over n_pts + 1 entries
+__global__ void k_zero_vertex_counts_dev(const RoundCounters* rc, int* a, int* b, int* c, int* d) {
+    const int n = rc->n_pts + 1;
+    for (int i = gtid(); i < n; i += gstride()) a[i] = b[i] = c[i] = d[i] = 0;
+}
+
+__global__ void k_fill_u64_dev(const RoundCounters* rc, unsigned long long* p, unsigned long long v) {
+    const int n = rc->n_pts + 1;
+    for (int i = gtid(); i < n; i += gstride()) p[i] = v;
+}
+
+__global__ void k_zero_face_ints_dev(const RoundCounters* rc, int* p) {
+    const int n = rc->n_tris + 1;
+    for (int i = gtid(); i < n; i += gstride()) p[i] = 0;
+}
+
+__global__ void k_zero_face_bytes_dev(const RoundCounters* rc, unsigned char* p) {
+    const int n = rc->n_tris + 1;
+    for (int i = gtid(); i < n; i += gstride()) p[i] = 0;
+}
+
+// After compaction: the next round's state (pamo/__init__.py:131-159: sizes, undo vertices, the no-progress
+// count and is_stuck) computed from this round's start state; recomputing it after an undo pass is harmless.
+__global__ void k_round_end(const RoundCounters* rc, const LoopState* ls, LoopState* next) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    LoopState L = *ls;
+    const int nf = rc->n_tris_out;
+    if (nf == L.nf) {
+        L.count += 1;
+    } else {
+        L.count = 0;
+        L.is_stuck = 0;
+    }
+    if (L.count >= 2) L.is_stuck = 1;
+    L.np = rc->n_pts_out;
+    L.nf = nf;
+    L.nu = rc->n_vertices_undo;
+    *next = L;
+}
+
+// undo vertices carried to the next round (the host loop's copy of the previous undo list)
+__global__ void k_copy_undo_dev(const RoundCounters* rc, const int* __restrict__ src, int* dst, int cap) {
+    const int n = min(rc->n_vertices_undo, cap);
+    for (int i = gtid(); i < n; i += gstride()) dst[i] = src[i];
+}
+
 }  // namespace
 
 // ================================================================== host launchers
@@ -841,10 +947,9 @@ void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cos
 void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
                       const int* nt, const int4* tri, const float4* pos, const Quadric* q, const unsigned char* invalid,
                       uint32_t* cost, unsigned long long* vmin, const float* d_scale, float tres, int is_stuck,
-                      cudaStream_t s) {
+                      cudaStream_t s, const int* is_stuck_dev) {
     k_edge_cost<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, invalid, cost,
-                                                           vmin, d_scale,
-                                                           tres, is_stuck); note_launch();
+                                                           vmin, d_scale, tres, is_stuck, is_stuck_dev); note_launch();
 }
 void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
                       unsigned long long* fkey, cudaStream_t s) {
@@ -929,6 +1034,44 @@ void launch_center(const float* pts, const int* tris, int n_pts, int n_tris, flo
     cudaMemsetAsync(ext + 3, 0x00, 3 * sizeof(unsigned), s);
     k_center_points<<<grid_for(n_pts, kT), kT, 0, s>>>(pts, n_pts, center, pos_out, ext); note_launch();
     k_extents<<<1, 32, 0, s>>>(ext, d_scale); note_launch();
+}
+
+// ---- device-driven rounds ----
+void launch_round_begin(RoundCounters* rc, LoopState* ls, const LoopState* next, cudaStream_t s) {
+    k_round_begin<<<1, 32, 0, s>>>(rc, ls, next); note_launch();
+}
+void launch_undo_bookkeeping_dev(const int* verts_undo, const LoopState* ls, int n_undo_bound, int* tmp_undo,
+                                 int* undo_list, const int* pts_map, int pts_map_len, unsigned char* invalid,
+                                 int invalid_len, cudaStream_t s) {
+    k_invalid_clear_dev<<<grid_for(invalid_len, kT), kT, 0, s>>>(ls, invalid, invalid_len); note_launch();
+    k_undo_book_dev<<<grid_for(n_undo_bound, kT), kT, 0, s>>>(verts_undo, ls, tmp_undo, undo_list, pts_map, pts_map_len,
+                                                             invalid, invalid_len); note_launch();
+}
+void launch_load_points4_dev(const float4* pts, const RoundCounters* rc, int n_pts_bound, float4* pos, float4* orig_pos,
+                             int* occ, cudaStream_t s) {
+    k_load_points4_dev<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(pts, rc, pos, orig_pos, occ); note_launch();
+}
+void launch_copy_tris_dev(const int4* src, int4* dst, const RoundCounters* rc, int n_tris_bound, cudaStream_t s) {
+    k_copy_tris_dev<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(src, dst, rc); note_launch();
+}
+void launch_zero_vertex_counts_dev(const RoundCounters* rc, int n_pts_bound, int* a, int* b, int* c, int* d,
+                                   cudaStream_t s) {
+    k_zero_vertex_counts_dev<<<grid_for(n_pts_bound + 1, kT), kT, 0, s>>>(rc, a, b, c, d); note_launch();
+}
+void launch_fill_u64_dev(const RoundCounters* rc, int n_pts_bound, unsigned long long* p, unsigned long long v,
+                         cudaStream_t s) {
+    k_fill_u64_dev<<<grid_for(n_pts_bound + 1, kT), kT, 0, s>>>(rc, p, v); note_launch();
+}
+void launch_zero_face_ints_dev(const RoundCounters* rc, int n_tris_bound, int* p, cudaStream_t s) {
+    k_zero_face_ints_dev<<<grid_for(n_tris_bound + 1, kT), kT, 0, s>>>(rc, p); note_launch();
+}
+void launch_zero_face_bytes_dev(const RoundCounters* rc, int n_tris_bound, unsigned char* p, cudaStream_t s) {
+    k_zero_face_bytes_dev<<<grid_for(n_tris_bound + 1, kT), kT, 0, s>>>(rc, p); note_launch();
+}
+void launch_round_end(const RoundCounters* rc, const LoopState* ls, LoopState* next, const int* undo_list, int* undo_in,
+                      int undo_cap, int n_undo_bound, cudaStream_t s) {
+    k_round_end<<<1, 32, 0, s>>>(rc, ls, next); note_launch();
+    k_copy_undo_dev<<<grid_for(n_undo_bound, kT), kT, 0, s>>>(rc, undo_list, undo_in, undo_cap); note_launch();
 }
 
 }  // namespace pamo

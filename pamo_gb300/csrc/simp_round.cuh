@@ -40,7 +40,8 @@ void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cos
 void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
                       const int* nt, const int4* tri, const float4* pos, const Quadric* q, const unsigned char* invalid,
                       uint32_t* cost, unsigned long long* vmin, const float* d_scale, float tres, int is_stuck,
-                      cudaStream_t s);
+                      cudaStream_t s,
+                      const int* is_stuck_dev = nullptr);
 void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
                       unsigned long long* fkey, cudaStream_t s);
 void launch_collapse(RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const uint32_t* cost,
@@ -79,5 +80,22 @@ void launch_center(const float* pts, const int* tris, int n_pts, int n_tris, flo
                    float* d_scale, float4* pos_out, cudaStream_t s,
                    bool centre = true);
 void launch_after_check(RoundCounters* rc, cudaStream_t s);
+
+// ---- device-driven rounds: sizes from LoopState / RoundCounters, host values only bound the grids ----
+void launch_round_begin(RoundCounters* rc, LoopState* ls, const LoopState* next, cudaStream_t s);
+void launch_undo_bookkeeping_dev(const int* verts_undo, const LoopState* ls, int n_undo_bound, int* tmp_undo,
+                                 int* undo_list, const int* pts_map, int pts_map_len, unsigned char* invalid,
+                                 int invalid_len, cudaStream_t s);
+void launch_load_points4_dev(const float4* pts, const RoundCounters* rc, int n_pts_bound, float4* pos, float4* orig_pos,
+                             int* occ, cudaStream_t s);
+void launch_copy_tris_dev(const int4* src, int4* dst, const RoundCounters* rc, int n_tris_bound, cudaStream_t s);
+void launch_zero_vertex_counts_dev(const RoundCounters* rc, int n_pts_bound, int* a, int* b, int* c, int* d,
+                                   cudaStream_t s);
+void launch_fill_u64_dev(const RoundCounters* rc, int n_pts_bound, unsigned long long* p, unsigned long long v,
+                         cudaStream_t s);
+void launch_zero_face_ints_dev(const RoundCounters* rc, int n_tris_bound, int* p, cudaStream_t s);
+void launch_zero_face_bytes_dev(const RoundCounters* rc, int n_tris_bound, unsigned char* p, cudaStream_t s);
+void launch_round_end(const RoundCounters* rc, const LoopState* ls, LoopState* next, const int* undo_list, int* undo_in,
+                      int undo_cap, int n_undo_bound, cudaStream_t s);
 
 }  // namespace pamo

@@ -141,3 +141,25 @@ def test_blender_entry_matches_oracle(name):
         assert len(fpr) >= 5 and np.all(fpr[-4:] == fpr[-1])  # stopped after 4 rounds without progress
         assert np.array_equal(F, Fo)
         assert np.array_equal(V, Vo)
+
+
+@pytest.mark.parametrize("mode", [(1, 1), (1, 0), (0, 0)])
+def test_loop_execution_modes_agree(mode):
+    """The whole loop gives the oracle's result with device-driven rounds as graphs, as direct launches, and
+    with the host-sized rounds."""
+    import pamo_gb300
+    from pamo_gb300 import synth
+
+    v, f = synth.config_mesh("plain_small")
+    ctx = pamo_gb300.Context("cuda:0")
+    ctx.set_option("device_rounds", mode[0])
+    ctx.set_option("graphs", mode[1])
+    pts = torch.tensor(v, device="cuda")
+    tri = torch.tensor(f, device="cuda", dtype=torch.int32)
+    Vo, Fo, fpr = orc.Oracle().run(v, f, 0.01, 4, 1e-3, 1000000, 0)
+    for _ in range(2):  # the second run replays the cached graphs
+        ctx.reset()
+        V, F, rounds = pamo_gb300.simplify(pts, tri, 0.01, 4, 1e-3, 1000000, 0, ctx=ctx)
+        assert rounds == len(fpr)
+        assert np.array_equal(F.cpu().numpy(), Fo)
+        assert np.array_equal(V.cpu().numpy(), Vo)
