@@ -375,6 +375,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workers", type=int, default=8, help="worker contexts for --config batch256 / serve")
     ap.add_argument("--requests", type=int, default=2000, help="requests for --config serve")
+    ap.add_argument("--one-job", action="store_true",
+                    help="run one job of the configuration and exit (for profiler captures; prints no JSON)")
     args = ap.parse_args()
     if args.config == "batch256":
         return run_batch(args)
@@ -433,6 +435,11 @@ def main():
                 s3_ms.append(a.elapsed_time(b))
         return verts, faces, rounds_
 
+    if args.one_job:
+        out = job()
+        torch.cuda.synchronize(dev)
+        print(f"one job: {F0} -> {out[1].shape[0]} faces in {out[2]} rounds")
+        return 0
     for _ in range(args.warmup):
         out = job()
     out_faces = out[1].shape[0]
