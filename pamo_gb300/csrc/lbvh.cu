@@ -317,9 +317,11 @@ __global__ void __launch_bounds__(256) k_query_gather(const RoundCounters* rc, c
         if (scan[i + 1] != scan[i]) qsorted[scan[i]] = leaf_face[i];
 }
 
-__global__ void __launch_bounds__(kQueryThreads) k_traverse(const int2* __restrict__ child, const float4* __restrict__ nlo,
-                                                             const float4* __restrict__ nhi, const float4* __restrict__ llo,
-                                                             const float4* __restrict__ lhi, const int* __restrict__ leaf_face,
+__device__ __forceinline__ bool box_overlap4(float4 qlo, float4 qhi, float4 lo, float4 hi) {
+    return !(qhi.x < lo.x || hi.x < qlo.x || qhi.y < lo.y || hi.y < qlo.y || qhi.z < lo.z || hi.z < qlo.z);
+}
+
+__global__ void __launch_bounds__(kQueryThreads) k_traverse(const float4* __restrict__ packed,
                                                              const float4* __restrict__ box_lo,
                                                              const float4* __restrict__ box_hi, const int4* __restrict__ tri,
                                                              const float4* __restrict__ pos, const int* __restrict__ qsorted,
@@ -343,16 +345,17 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse(const int2* __restri
                 atomicOr(&rc->status, kErrIterLimit);
                 break;
             }
-            const int2 c = child[node];
+            const float4* rec = packed + 4 * (size_t)node;
+            const float4 alo = __ldg(rec), ahi = __ldg(rec + 1), blo = __ldg(rec + 2), bhi = __ldg(rec + 3);
             int next[2];
             int nn = 0;
 #pragma unroll
             for (int side = 0; side < 2; ++side) {
-                const int x = side == 0 ? c.x : c.y;
+                const float4 lo = side ? blo : alo, hi = side ? bhi : ahi;
+                if (!box_overlap4(qlo, qhi, lo, hi)) continue;
+                const int x = __float_as_int(lo.w);
                 if (x < 0) {
-                    const int li = ~x;
-                    if (!boxes_overlap(qlo, qhi, llo[li], lhi[li])) continue;
-                    const int g = leaf_face[li];
+                    const int g = __float_as_int(hi.w);
                     if (g == f) continue;
                     if (g < f && qscan[g + 1] != qscan[g]) continue;  // the lower query face owns the pair
                     ++npairs;
@@ -364,7 +367,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse(const int2* __restri
                         hit[g] = 1;
                     }
                 } else {
-                    if (boxes_overlap(qlo, qhi, nlo[x], nhi[x])) next[nn++] = x;
+                    next[nn++] = x;
                 }
             }
             if (nn == 2) {
@@ -426,6 +429,7 @@ size_t bvh_bytes(int cap) {
     b += align256(4 * c);                   // visit
     b += align256(4 * 8);                   // scene
     b += align256(4 * scan_scratch_ints());
+    b += align256(64 * c);                  // packed internal nodes
     return b;
 }
 
@@ -456,6 +460,40 @@ void bvh_carve(BvhBuffers& b, int cap, char* base) {
     b.visit = (int*)take(4 * c);
     b.scene = (unsigned*)take(4 * 8);
     b.scan_scratch = (int*)take(4 * scan_scratch_ints());
+    b.packed = (float4*)take(64 * c);
+}
+
+// one 64-byte record per internal node holding both children's boxes (and leaf face ids), so that a traversal
+// step reads one record instead of the child pair and two boxes from separate arrays
+__global__ void __launch_bounds__(256) k_pack_nodes(const RoundCounters* rc, const int2* __restrict__ child,
+                                                     const float4* __restrict__ nlo, const float4* __restrict__ nhi,
+                                                     const float4* __restrict__ llo, const float4* __restrict__ lhi,
+                                                     const int* __restrict__ leaf_face, float4* packed) {
+    const int n = rc->n_live;
+    for (int i = gtid(); i < n - 1; i += gstride()) {
+        const int2 c = child[i];
+        float4 out[4];
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const int x = side ? c.y : c.x;
+            float4 lo, hi;
+            int face = -1;
+            if (x < 0) {
+                lo = llo[~x];
+                hi = lhi[~x];
+                face = leaf_face[~x];
+            } else {
+                lo = __ldcg(&nlo[x]);
+                hi = __ldcg(&nhi[x]);
+            }
+            lo.w = __int_as_float(x);
+            hi.w = __int_as_float(face);
+            out[2 * side] = lo;
+            out[2 * side + 1] = hi;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) packed[4 * (size_t)i + k] = out[k];
+    }
 }
 
 void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s) {
@@ -475,6 +513,7 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
     k_leaves<<<gF, 256, 0, s>>>(rc, b.vals[0], b.box_lo, b.box_hi, b.llo, b.lhi, b.visit, b.lparent); note_launch();
     k_karras<<<gF, 256, 0, s>>>(rc, b.keys[0], b.child, b.iparent, b.lparent); note_launch();
     k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit); note_launch();
+    k_pack_nodes<<<gF, 256, 0, s>>>(rc, b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], b.packed); note_launch();
 }
 
 __global__ void __launch_bounds__(256) k_refit_leaves(const RoundCounters* rc, const int4* __restrict__ tri,
@@ -512,8 +551,7 @@ void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const in
     k_query_gather<<<gF, 256, 0, s>>>(rc, b.vals[0], b.live_scan, b.vals[1]);
     note_launch();
     k_traverse<<<grid_for(n_query_bound, kQueryThreads, 16), kQueryThreads, 0, s>>>(
-        b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], b.box_lo, b.box_hi, tri, pos, b.vals[1], qscan, hit, pair_list,
-        pair_cap, rc, eps);
+        b.packed, b.box_lo, b.box_hi, tri, pos, b.vals[1], qscan, hit, pair_list, pair_cap, rc, eps);
     note_launch();
     k_pairs<<<grid_for((long long)pair_cap, 128, 16), 128, 0, s>>>(tri, pos, pair_list, pair_cap, hit, rc, eps);
     note_launch();
