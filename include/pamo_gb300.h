@@ -53,7 +53,9 @@ int64_t pamo_ctx_device_bytes(const pamo_ctx* ctx);
 /* Execution options of pamo_simplify_device (results are the same with any setting):
  *   "device_rounds" (default 1): rounds after the first read their sizes and loop state from device memory
  *                                and synchronise once per round (plus once per extra undo pass);
- *   "graphs"        (default 1): those rounds run as CUDA graphs cached per size class.
+ *   "graphs"        (default 1): those rounds run as CUDA graphs cached per size class;
+ *   "bvh_reuse"     (default 1): those rounds refit the LBVH carried from the previous round (rebuilt when a
+ *                                quarter of its leaves lost their faces) instead of building it each round.
  * The phase timers (pamo_profile_enable) use the host-sized path. */
 int pamo_ctx_set_option(pamo_ctx* ctx, const char* name, int64_t value);
 
@@ -107,6 +109,10 @@ int pamo_simplify_result(pamo_ctx* ctx, float* verts, int32_t* tris, pamo_stream
 
 /* Face count after each round of the last pamo_simplify_device call (host array of `capacity`). */
 int pamo_simplify_round_faces(const pamo_ctx* ctx, int32_t* faces_per_round, int32_t capacity);
+
+/* Host wall-clock milliseconds of each round of the last pamo_simplify_device call (every round ends with a
+ * synchronisation); returns the number written. No reference counterpart (diagnostics). */
+int pamo_simplify_round_ms(const pamo_ctx* ctx, double* ms, int32_t capacity);
 
 /*
  * The reference's self-intersection check over a whole mesh (selfx::self_intersect,

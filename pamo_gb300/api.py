@@ -69,6 +69,12 @@ class Context:
         """Execution options of the whole loop ("device_rounds", "graphs"); results do not depend on them."""
         _native.check(_native.load().pamo_ctx_set_option(self.handle, name.encode(), int(value)), self.handle)
 
+    def round_ms(self) -> list:
+        """Host wall time of each round of the last whole-loop call."""
+        out = (ctypes.c_double * 4096)()
+        n = _native.load().pamo_simplify_round_ms(self.handle, out, 4096)
+        return list(out[: max(n, 0)])
+
     def device_bytes(self) -> int:
         """Device memory the context holds."""
         return int(_native.load().pamo_ctx_device_bytes(self.handle))

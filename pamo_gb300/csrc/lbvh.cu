@@ -46,14 +46,20 @@ __device__ __forceinline__ bool boxes_overlap(float4 alo, float4 ahi, float4 blo
 // ---------------------------------------------------------------- boxes + scene bounds
 __global__ void __launch_bounds__(256) k_boxes(const int4* __restrict__ tri, const float4* __restrict__ pos,
                                                 const RoundCounters* rc, float4* box_lo, float4* box_hi, int* live,
-                                                unsigned* scene) {
+                                                unsigned* scene, int all_faces) {
     const int n = rc->n_tris;
     float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int f = gtid(); f < n; f += gstride()) {
         int4 t = tri[f];
         int is_live = (t.x != -1);
-        live[f] = is_live;
-        if (!is_live) continue;
+        live[f] = all_faces ? 1 : is_live;
+        if (!is_live) {
+            if (all_faces) {  // an empty box: overlaps nothing
+                box_lo[f] = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
+                box_hi[f] = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+            }
+            continue;
+        }
         float4 a = pos[t.x], b = pos[t.y], c = pos[t.z];
         float4 lo = make_float4(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)), 0.f);
         float4 hi = make_float4(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)), 0.f);
@@ -305,7 +311,7 @@ __global__ void __launch_bounds__(256) k_query_order(const RoundCounters* rc, co
     const int n = rc->n_live;
     for (int i = gtid(); i < n; i += gstride()) {
         const int f = leaf_face[i];
-        flags[i] = (qscan[f + 1] != qscan[f]) ? 1 : 0;
+        flags[i] = (f >= 0 && qscan[f + 1] != qscan[f]) ? 1 : 0;  // f < 0: a leaf whose face is gone
     }
     if (gtid() == 0) flags[n] = 0;
 }
@@ -430,6 +436,7 @@ size_t bvh_bytes(int cap) {
     b += align256(4 * 8);                   // scene
     b += align256(4 * scan_scratch_ints());
     b += align256(64 * c);                  // packed internal nodes
+    b += align256(16);                      // meta
     return b;
 }
 
@@ -461,6 +468,7 @@ void bvh_carve(BvhBuffers& b, int cap, char* base) {
     b.scene = (unsigned*)take(4 * 8);
     b.scan_scratch = (int*)take(4 * scan_scratch_ints());
     b.packed = (float4*)take(64 * c);
+    b.meta = (int*)take(16);
 }
 
 // one 64-byte record per internal node holding both children's boxes (and leaf face ids), so that a traversal
@@ -468,8 +476,9 @@ void bvh_carve(BvhBuffers& b, int cap, char* base) {
 __global__ void __launch_bounds__(256) k_pack_nodes(const RoundCounters* rc, const int2* __restrict__ child,
                                                      const float4* __restrict__ nlo, const float4* __restrict__ nhi,
                                                      const float4* __restrict__ llo, const float4* __restrict__ lhi,
-                                                     const int* __restrict__ leaf_face, float4* packed) {
+                                                     const int* __restrict__ leaf_face, float4* packed, int* meta) {
     const int n = rc->n_live;
+    if (gtid() == 0) meta[0] = n;
     for (int i = gtid(); i < n - 1; i += gstride()) {
         const int2 c = child[i];
         float4 out[4];
@@ -496,11 +505,12 @@ __global__ void __launch_bounds__(256) k_pack_nodes(const RoundCounters* rc, con
     }
 }
 
-void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s) {
+void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s,
+               bool all_faces) {
     cudaMemsetAsync(b.scene, 0xFF, 3 * sizeof(unsigned), s);
     cudaMemsetAsync(b.scene + 3, 0x00, 3 * sizeof(unsigned), s);
     const int gF = grid_for(n_tris_bound, 256);
-    k_boxes<<<gF, 256, 0, s>>>(tri, pos, rc, b.box_lo, b.box_hi, b.live_scan, b.scene); note_launch();
+    k_boxes<<<gF, 256, 0, s>>>(tri, pos, rc, b.box_lo, b.box_hi, b.live_scan, b.scene, all_faces ? 1 : 0); note_launch();
     exclusive_scan(b.live_scan, b.live_scan, &rc->n_tris, 1, &rc->n_live, b.scan_scratch, s);
     k_morton<<<gF, 256, 0, s>>>(rc, b.live_scan, b.box_lo, b.box_hi, b.scene, b.keys[0], b.vals[0]); note_launch();
     for (int pass = 0; pass < 4; ++pass) {
@@ -513,7 +523,7 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
     k_leaves<<<gF, 256, 0, s>>>(rc, b.vals[0], b.box_lo, b.box_hi, b.llo, b.lhi, b.visit, b.lparent); note_launch();
     k_karras<<<gF, 256, 0, s>>>(rc, b.keys[0], b.child, b.iparent, b.lparent); note_launch();
     k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit); note_launch();
-    k_pack_nodes<<<gF, 256, 0, s>>>(rc, b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], b.packed); note_launch();
+    k_pack_nodes<<<gF, 256, 0, s>>>(rc, b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], b.packed, b.meta); note_launch();
 }
 
 __global__ void __launch_bounds__(256) k_refit_leaves(const RoundCounters* rc, const int4* __restrict__ tri,
@@ -535,6 +545,56 @@ void bvh_refit(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
     const int gF = grid_for(n_tris_bound, 256);
     k_refit_leaves<<<gF, 256, 0, s>>>(rc, tri, pos, b.vals[0], b.llo, b.lhi, b.visit, active); note_launch();
     k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit, active);
+    note_launch();
+}
+
+__global__ void __launch_bounds__(256) k_reuse_leaves(RoundCounters* rc, const int4* __restrict__ tri,
+                                                      const float4* __restrict__ box_lo, const float4* __restrict__ box_hi,
+                                                      const int* __restrict__ new_ids, int* leaf_face, float4* llo,
+                                                      float4* lhi, int* visit, const int* meta) {
+    const int n = meta[0];
+    if (gtid() == 0) rc->n_live = n;
+    for (int i = gtid(); i < n; i += gstride()) {
+        int f;
+        if (new_ids) {
+            f = new_ids[i];
+            leaf_face[i] = f;
+        } else {
+            f = leaf_face[i];
+        }
+        if (f >= 0 && tri[f].x != -1) {
+            llo[i] = box_lo[f];
+            lhi[i] = box_hi[f];
+        } else {
+            llo[i] = make_float4(INFINITY, INFINITY, INFINITY, 0.f);
+            lhi[i] = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+        }
+        if (i < n - 1) visit[i] = 0;
+    }
+}
+
+// next[i] = the leaf's face in the next numbering; reads the current ids only, so it can be repeated
+__global__ void __launch_bounds__(256) k_remap_leaves(const int* meta, const int* __restrict__ fscan,
+                                                      const int* __restrict__ leaf_face, int* next) {
+    const int n = meta[0];
+    for (int i = gtid(); i < n; i += gstride()) {
+        const int f = leaf_face[i];
+        next[i] = (f >= 0 && fscan[f + 1] != fscan[f]) ? fscan[f] : -1;
+    }
+}
+
+void bvh_refit_faces(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound,
+                     cudaStream_t s, bool next_round) {
+    const int gF = grid_for(n_tris_bound, 256);
+    k_boxes<<<gF, 256, 0, s>>>(tri, pos, rc, b.box_lo, b.box_hi, b.live_scan, b.scene, 1); note_launch();
+    k_reuse_leaves<<<gF, 256, 0, s>>>(rc, tri, b.box_lo, b.box_hi, next_round ? (const int*)b.keys[1] : nullptr,
+                                      b.vals[0], b.llo, b.lhi, b.visit, b.meta); note_launch();
+    k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit); note_launch();
+    k_pack_nodes<<<gF, 256, 0, s>>>(rc, b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], b.packed, b.meta); note_launch();
+}
+
+void bvh_remap(BvhBuffers& b, const int* fscan, int n_tris_bound, cudaStream_t s) {
+    k_remap_leaves<<<grid_for(n_tris_bound, 256), 256, 0, s>>>(b.meta, fscan, b.vals[0], (int*)b.keys[1]);
     note_launch();
 }
 

@@ -27,13 +27,27 @@ struct BvhBuffers {
     // lo.w = child reference (>= 0 internal node, < 0 leaf ~i), hi.w = the leaf's face id (or -1), as int bits
     float4* packed = nullptr;
     int* scan_scratch = nullptr;
+    int* meta = nullptr;               // [0]: leaves of the current tree (kept across refits)
 };
 
 size_t bvh_bytes(int cap);
 void bvh_carve(BvhBuffers& b, int cap, char* base);
 
-// Builds the LBVH over faces with tri[f].x != -1 (count from rc->n_tris); writes rc->n_live.
-void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s);
+// Builds the LBVH over faces with tri[f].x != -1 (count from rc->n_tris); writes rc->n_live. With all_faces,
+// every face slot below rc->n_tris is a leaf and a removed face has an empty box, so that the tree can be
+// refitted after faces are removed or restored (bvh_refit_faces) and carried to the next round (bvh_remap).
+void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s,
+               bool all_faces = false);
+
+// New boxes for the leaves of a tree built with all_faces (a removed face, or a leaf whose face is gone, gets an
+// empty box that overlaps nothing); sets rc->n_live to the tree's leaf count. next_round: first take the leaf
+// face ids bvh_remap computed for this round's numbering.
+void bvh_refit_faces(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound,
+                     cudaStream_t s, bool next_round);
+
+// After a compaction with exclusive scan fscan of the kept faces: the leaves' face ids in the new numbering
+// (-1 for faces not kept), kept aside until bvh_refit_faces(next_round = true); repeating it is harmless.
+void bvh_remap(BvhBuffers& b, const int* fscan, int n_tris_bound, cudaStream_t s);
 
 // Recomputes the leaf and node boxes of a tree built by bvh_build over the same faces after the positions
 // moved (same topology and leaf order; the tree may bound more loosely than a rebuilt one). With `active`,

@@ -6,6 +6,7 @@
 // reference's capacity policy (new capacity = n + n/5, fresh buffers read as zero) is kept for these
 // buffers because it decides when their contents are reset.
 #include <algorithm>
+#include <chrono>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -160,6 +161,7 @@ struct pamo_ctx {
     std::map<std::tuple<const void*, int, int, int>, RoundGraph> graphs;
     bool use_graphs = true;     // device rounds as cached graphs
     bool device_rounds = true;  // rounds after the first from device-resident sizes (pamo_simplify_device)
+    bool bvh_reuse = true;      // device rounds refit the LBVH carried from the previous round
     DevBuf<float> face_mean;
     float* h_pinned_f = nullptr;
 
@@ -170,6 +172,7 @@ struct pamo_ctx {
     bool have_run = false;
     int run_np = 0, run_nt = 0;
     std::vector<int> faces_per_round;
+    std::vector<double> round_ms;  // host wall time of each round of the last loop (rounds end with a sync)
     // totals over the rounds of the last pamo_simplify_device call
     long long tot[10] = {};
 
@@ -366,17 +369,18 @@ struct pamo_ctx {
 
     // One device-driven round (the rounds after the first in pamo_simplify_device): every size and flag comes
     // from d_ls and rc, and nPb/nTb only bound the grids, so the same launches serve every round of a size
-    // class and can be captured as a graph. kind 0: the whole round, with the compaction and the next round's
-    // state computed as if no undo pass follows; kind 1: one more undo pass (cusimp_free.cu:1016-1040), then
-    // the compaction and next state again. The same kernels and order as round() plus the compaction of
-    // simplify_loop.
+    // class and can be captured as a graph. kind 0 / 2: the whole round, with the compaction and the next
+    // round's state computed as if no undo pass follows, building the LBVH afresh (0) or refitting the one
+    // carried from the previous round (2); kind 1: one more undo pass (cusimp_free.cu:1016-1040), then the
+    // compaction and next state again. The same kernels and order as round() plus the compaction of
+    // simplify_loop; the LBVH only filters candidate pairs, so building or refitting gives the same pairs.
     void round_dev(int kind, int nPb, int nTb, float threshold) {
         cudaStream_t s = stream;
         const int* nt_off = valence.p;
         const int eb = 2 * nTb;
         const int list_cap = (int)undo_list.n;
         const uint32_t collapse_t = collapse_threshold(threshold);
-        if (kind == 0) {
+        if (kind != 1) {
             launch_round_begin(rc, d_ls, d_ls + 1, s);
             launch_undo_bookkeeping_dev(undo_in.p, d_ls, list_cap, tmp_undo.p, undo_list.p, pts_map.p, (int)pts_map.n,
                                         invalid.p, (int)invalid.n, s);
@@ -412,9 +416,10 @@ struct pamo_ctx {
             launch_undo_apply(rc, eb, collapsed.p, uflag.p, edges.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p, orig_pos.p,
                               occ.p, tmp_undo.p, undo_list.p, pts_map.p, list_cap, s);
         }
-        // intersection check
+        // intersection check; the LBVH spans every face slot of the round and is refitted when reused
         launch_zero_face_bytes_dev(rc, nTb, hit.p, s);
-        bvh_build(bvh, tri.p, pos.p, rc, nTb, s);
+        if (kind == 0) bvh_build(bvh, tri.p, pos.p, rc, nTb, s, true);
+        else bvh_refit_faces(bvh, tri.p, pos.p, rc, nTb, s, kind == 2);
         bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, (int)exact_list.n, rc, nTb, kTriEps, s);
         launch_undo_check(rc, eb, collapsed.p, edges.p, nt_off, nt.p, hit.p, uflag.p, s);
         exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s);
@@ -424,6 +429,7 @@ struct pamo_ctx {
         launch_live_flags(rc, nTb, tri.p, fflags.p, s);
         exclusive_scan(fflags.p, fflags.p, &rc->n_tris, 1, nullptr, scan_scratch, s);
         launch_compact_mesh(rc, nPb, nTb, pos.p, occ.p, pts_map.p, tri.p, fflags.p, pos_out.p, tri_out.p, s);
+        bvh_remap(bvh, fflags.p, nTb, s);  // the tree's leaves in the next round's face numbering
         launch_round_end(rc, d_ls, d_ls + 1, undo_list.p, undo_in.p, (int)std::min(undo_in.n, undo_list.n), list_cap, s);
     }
 
@@ -444,7 +450,7 @@ struct pamo_ctx {
         }
         int tbits;
         std::memcpy(&tbits, &threshold, sizeof(int));
-        const auto key = std::make_tuple((const void*)pos_in.p, nTb * 2 + kind, nPb, tbits);
+        const auto key = std::make_tuple((const void*)pos_in.p, nTb * 4 + kind, nPb, tbits);
         auto it = graphs.find(key);
         if (it == graphs.end()) {
             cudaGraph_t g = nullptr;
@@ -656,6 +662,7 @@ int pamo_ctx_set_option(pamo_ctx* ctx, const char* name, int64_t value) {
     const std::string n(name);
     if (n == "graphs") ctx->use_graphs = value != 0;
     else if (n == "device_rounds") ctx->device_rounds = value != 0;
+    else if (n == "bvh_reuse") ctx->bvh_reuse = value != 0;
     else return ctx->fail(PAMO_ERR_INVALID_ARG, "unknown option %s", name);
     return PAMO_OK;
 }
@@ -757,6 +764,8 @@ int simplify_loop_on(pamo_ctx* ctx, const float* points, const int32_t* triangle
     ctx->stream = s;
     ctx->have_run = false;
     ctx->faces_per_round.clear();
+    ctx->round_ms.clear();
+    auto t_round = std::chrono::steady_clock::now();
     for (auto& t : ctx->tot) t = 0;
     int r;
     if ((r = ctx->ensure_vertex_buffers(n_points)) || (r = ctx->ensure_face_buffers(n_triangles))) return r;
@@ -773,6 +782,7 @@ int simplify_loop_on(pamo_ctx* ctx, const float* points, const int32_t* triangle
     // rounds after the first run from device-resident sizes and state (optionally as cached graphs); with the
     // phase timers on, every round takes the host-sized path that times each phase
     const bool dev_rounds = ctx->device_rounds && !ctx->prof.on;
+    int tree_leaves = 0;  // leaves of the LBVH carried between device rounds (0: none)
     if (dev_rounds) {
         LoopState L = {};
         L.np = n_points;
@@ -804,7 +814,10 @@ int simplify_loop_on(pamo_ctx* ctx, const float* points, const int32_t* triangle
                                  (int)std::min(ctx->undo_in.n, ctx->undo_list.n), (int)ctx->undo_list.n, s);
             if ((r = ctx->read_counters())) return r;
         } else {
-            if ((r = ctx->run_round_dev(0, np, nf, threshold))) return r;
+            // rebuild the LBVH when a quarter of its leaves lost their faces, else refit the carried one
+            const bool rebuild = !ctx->bvh_reuse || tree_leaves == 0 || (long long)nf * 4 < (long long)tree_leaves * 3;
+            if (rebuild) tree_leaves = nf;
+            if ((r = ctx->run_round_dev(rebuild ? 0 : 2, np, nf, threshold))) return r;
             if ((r = ctx->read_counters())) return r;
             int extra = 0;
             while (ctx->h_rc->n_undo != 0) {  // cusimp_free.cu:1016-1040
@@ -833,6 +846,11 @@ int simplify_loop_on(pamo_ctx* ctx, const float* points, const int32_t* triangle
         std::swap(ctx->pos_in, ctx->pos_out);
         std::swap(ctx->tri_in, ctx->tri_out);
         ctx->faces_per_round.push_back(nf);
+        {
+            const auto t_now = std::chrono::steady_clock::now();
+            ctx->round_ms.push_back(std::chrono::duration<double, std::milli>(t_now - t_round).count());
+            t_round = t_now;
+        }
         if ((opt.target >= 0 && nf <= opt.target) || (opt.stop_small && nf <= 10)) break;
         if (nf == nf_prev) {
             count++;
@@ -990,6 +1008,13 @@ int pamo_run_totals(const pamo_ctx* ctx, int64_t* out, int32_t n) {
 }
 
 int64_t pamo_launch_count(void) { return launches_so_far(); }
+
+int pamo_simplify_round_ms(const pamo_ctx* ctx, double* ms, int32_t capacity) {
+    if (!ctx || !ms) return PAMO_ERR_INVALID_ARG;
+    const int n = std::min<int>(capacity, (int)ctx->round_ms.size());
+    for (int i = 0; i < n; ++i) ms[i] = ctx->round_ms[i];
+    return n;
+}
 
 int pamo_simplify_round_faces(const pamo_ctx* ctx, int32_t* faces_per_round, int32_t capacity) {
     if (!ctx || !faces_per_round) return PAMO_ERR_INVALID_ARG;
