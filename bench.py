@@ -373,7 +373,7 @@ def main():
     ap.add_argument("--config", default="plain_large", choices=sorted(CONFIGS) + ["batch256", "serve"])
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workers", type=int, default=8, help="worker contexts for --config batch256 / serve")
+    ap.add_argument("--workers", type=int, default=16, help="worker contexts for --config batch256 / serve")
     ap.add_argument("--requests", type=int, default=2000, help="requests for --config serve")
     ap.add_argument("--one-job", action="store_true",
                     help="run one job of the configuration and exit (for profiler captures; prints no JSON)")
