@@ -529,7 +529,16 @@ def main():
 
     cpu = None
     precision = None
+    quality = None
     if not args.no_cpu_baseline:
+        from oracle import oracle as orc
+
+        def orc_si(V, F):
+            return orc.self_intersections(V, F)[0]
+
+        def orc_hd(Va, Fa, Vb, Fb):
+            return orc.hausdorff(Va, Fa, Vb, Fb)[0]
+
         s3_in = (stage2_out[0], stage2_out[1], "the stage-2 output of the GPU run") if s3 is not None else None
         cpu = cpu_sample(v, f, ratio, fpr, budget_s=12.0 if args.config == "plain_large" else 3.0, stage3_input=s3_in)
         cpu.pop("projected_job_s", None)
@@ -542,6 +551,17 @@ def main():
                          "against": "float64 oracle run of stage 3 on the same stage-2 output",
                          "arithmetic": "float32 with compensated (two-sum) energy and CG sums; float64 for the "
                                        "normalisation, Voronoi weights and angle test"}
+        # output checks: exact-predicate self-intersection count and Hausdorff distance to the input
+        fin = (prof_out[0].double().cpu().numpy(), prof_out[1].cpu().numpy())
+        diag_in = float(np.linalg.norm(v.max(0) - v.min(0)))
+        quality = {"output_faces": int(len(fin[1])),
+                   "self_intersecting_pairs": orc_si(*fin),
+                   "hausdorff_over_bbox_diag": orc_hd(fin[0], fin[1], v, f) / diag_in,
+                   "how": "face pairs meeting beyond shared vertices/edges, exact orientation predicates; two-sided "
+                          "vertex Hausdorff distance to the input mesh over the input's bounding-box diagonal"}
+        if s3 is not None:
+            quality["stage2_self_intersecting_pairs"] = orc_si(*stage2_out)
+            quality["stage2_hausdorff_over_bbox_diag"] = orc_hd(stage2_out[0], stage2_out[1], v, f) / diag_in
 
     line = {
         "metric": "input faces/s to 0.1% ratio", "value": value, "unit": "input faces/s", "n_gpus": world,
@@ -558,6 +578,7 @@ def main():
             {"stage3": round(s3_ms[-1], 3)} if s3_ms else {}),
         "stage3": s3_stats,
         "precision": precision,
+        "quality": quality,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "input faces/s", "h2d_bytes_per_step": int(v.nbytes + f.nbytes),
                 "d2h_bytes_per_step": int(d2h)},

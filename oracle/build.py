@@ -1,5 +1,5 @@
-"""Builds the CPU oracle (oracle/pamo_oracle.cpp: stage 2, oracle/stage3_oracle.cpp: stage 3) into
-oracle/build/libpamo_oracle.so.
+"""Builds the CPU oracle (oracle/pamo_oracle.cpp: stage 2, oracle/stage3_oracle.cpp: stage 3,
+oracle/mesh_check.cpp: exact self-intersection check and Hausdorff distance) into oracle/build/libpamo_oracle.so.
 
 Test infrastructure: the oracle is the checker of the CUDA path, loaded only by tests/, the smoke check of
 __graft_entry__ and the CPU-baseline leg of bench.py. -ffp-contract=off keeps every float product and sum
@@ -10,7 +10,7 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRCS = [os.path.join(HERE, "pamo_oracle.cpp"), os.path.join(HERE, "stage3_oracle.cpp")]
+SRCS = [os.path.join(HERE, n) for n in ("pamo_oracle.cpp", "stage3_oracle.cpp", "mesh_check.cpp")]
 OUT = os.path.join(HERE, "build", "libpamo_oracle.so")
 
 

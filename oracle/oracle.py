@@ -37,6 +37,14 @@ def lib():
         L.oracle_run_blender.argtypes = [P, P, P, I, I, F, P, P]
         L.oracle_self_intersect.argtypes = [P, P, P, I, I, P]
         L.oracle_self_intersect.restype = LL
+        L.check_self_intersections.argtypes = [P, I, P, I, P, I]
+        L.check_self_intersections.restype = LL
+        L.check_self_intersections_all_pairs.argtypes = [P, I, P, I]
+        L.check_self_intersections_all_pairs.restype = LL
+        L.hausdorff.argtypes = [P, I, P, I, P, I, P, I, P]
+        L.hausdorff.restype = D
+        L.exact_orient3d.argtypes = [P]
+        L.exact_orient3d.restype = I
         L.s3_oracle_run.argtypes = [P, P, I, I, P, P, I, I, I, P, P, P]
         L.s3_oracle_probe.argtypes = [P, P, I, I, P, P, I, I, P, P, P, P, P, P, P, P, P]
         L.s3_oracle_energy_at.argtypes = [P, P, I, I, P, P, I, I, P, P, P, P]
@@ -229,3 +237,39 @@ def stage3_energy_at(gt_V, gt_F, V, F, x, params: dict | None = None, x0=None) -
     if rc:
         raise RuntimeError(f"stage-3 oracle energy failed with status {rc}")
     return float(e[0])
+
+
+def exact_orient3d(a, b, c, d) -> int:
+    """Sign of det[a-d; b-d; c-d], exact for double inputs (expansion arithmetic)."""
+    p = np.ascontiguousarray(np.concatenate([a, b, c, d]), np.float64)
+    return int(lib().exact_orient3d(_p(p)))
+
+
+def self_intersections(points, tris, max_pairs: int = 64):
+    """(count, pairs [k,2]) of face pairs of the mesh that meet beyond their shared vertices and edge, decided
+    with exact orientation predicates."""
+    P = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+    T = np.ascontiguousarray(tris, np.int32).reshape(-1, 3)
+    pairs = np.zeros((max(max_pairs, 1), 2), np.int32)
+    n = int(lib().check_self_intersections(_p(P), len(P), _p(T), len(T), _p(pairs), max_pairs))
+    if n < 0:
+        raise ValueError("triangle index out of range")
+    return n, pairs[: min(n, max_pairs)]
+
+
+def self_intersections_all_pairs(points, tris) -> int:
+    """The same count as self_intersections, testing every pair of faces (small meshes only)."""
+    P = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+    T = np.ascontiguousarray(tris, np.int32).reshape(-1, 3)
+    return int(lib().check_self_intersections_all_pairs(_p(P), len(P), _p(T), len(T)))
+
+
+def hausdorff(va, fa, vb, fb):
+    """(two-sided, A->B, B->A) vertex Hausdorff distances between two triangle meshes."""
+    A = np.ascontiguousarray(va, np.float64).reshape(-1, 3)
+    B = np.ascontiguousarray(vb, np.float64).reshape(-1, 3)
+    FA = np.ascontiguousarray(fa, np.int32).reshape(-1, 3)
+    FB = np.ascontiguousarray(fb, np.int32).reshape(-1, 3)
+    out = np.zeros(2, np.float64)
+    h = lib().hausdorff(_p(A), len(A), _p(FA), len(FA), _p(B), len(B), _p(FB), len(FB), _p(out))
+    return float(h), float(out[0]), float(out[1])

@@ -124,3 +124,8 @@ def test_pamo_run_with_stage3():
         return np.abs(np.linalg.norm(P, axis=1) - np.linalg.norm(V[idx], axis=1)).mean()
 
     assert radial_err(v3) < 0.5 * radial_err(v2.astype(np.float64))
+    # exact-predicate check of both outputs, and the one-sided Hausdorff distance from the output's vertices
+    # to the input surface shrinks under the projection
+    assert orc.self_intersections(v2, f2)[0] == 0
+    assert orc.self_intersections(v3, f3)[0] == 0
+    assert orc.hausdorff(v3, f3, V, F)[1] < 0.5 * orc.hausdorff(v2, f2, V, F)[1]
