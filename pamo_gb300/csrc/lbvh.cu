@@ -36,13 +36,6 @@ __device__ __forceinline__ unsigned expand10(unsigned v) {
     return v;
 }
 
-__device__ __forceinline__ bool boxes_overlap(float4 alo, float4 ahi, float4 blo, float4 bhi) {
-    if (ahi.x < blo.x || bhi.x < alo.x) return false;
-    if (ahi.y < blo.y || bhi.y < alo.y) return false;
-    if (ahi.z < blo.z || bhi.z < alo.z) return false;
-    return true;
-}
-
 // ---------------------------------------------------------------- boxes + scene bounds
 __global__ void __launch_bounds__(256) k_boxes(const int4* __restrict__ tri, const float4* __restrict__ pos,
                                                 const RoundCounters* rc, float4* box_lo, float4* box_hi, int* live,
@@ -277,7 +270,7 @@ __global__ void __launch_bounds__(256) k_bottom_up(RoundCounters* rc, const int2
 //    part of the tree and test neighbouring faces.
 // 2. k_traverse: one thread per query face walks the tree with its stack in shared memory and emits every
 //    overlapping leaf g as a candidate pair (f, g); a pair of two query faces is emitted only by the lower
-//    face index. Beyond the pair list's capacity the pair is decided in place.
+//    face index. Queries whose pairs do not fit the list walk again after k_pairs and decide in place.
 // 3. k_pairs: one thread per candidate pair runs the reference's decision in both orders (float
 //    certificates first, the fp64 path only for undecided pairs) and flags both faces when it holds.
 __device__ __forceinline__ int warp_append(int* counter) {
@@ -327,25 +320,36 @@ __device__ __forceinline__ bool box_overlap4(float4 qlo, float4 qhi, float4 lo, 
     return !(qhi.x < lo.x || hi.x < qlo.x || qhi.y < lo.y || hi.y < qlo.y || qhi.z < lo.z || hi.z < qlo.z);
 }
 
+// kRedo = false: the first walk. Candidate pairs go to the pair list; a query whose pair does not fit stops
+// and is marked in redo[qi]. kRedo = true: only when the list overflowed, the marked queries walk again and
+// decide every pair in place (pairs already listed are decided twice, which sets the same flags).
+template <bool kRedo>
 __global__ void __launch_bounds__(kQueryThreads) k_traverse(const float4* __restrict__ packed,
                                                              const float4* __restrict__ box_lo,
                                                              const float4* __restrict__ box_hi, const int4* __restrict__ tri,
                                                              const float4* __restrict__ pos, const int* __restrict__ qsorted,
                                                              const int* __restrict__ qscan, unsigned char* hit,
-                                                             int2* pairs_out, int pair_cap, RoundCounters* rc, float eps) {
+                                                             int2* pairs_out, int pair_cap, RoundCounters* rc, float eps,
+                                                             int* redo) {
     __shared__ int stack[kStackDepth][kQueryThreads];
+    int* n_list = &rc->pad[1];
+    if (kRedo && *n_list <= pair_cap) return;
     const int nq = rc->pad[2];
     const int nl = rc->n_live;
-    int* n_list = &rc->pad[1];
     unsigned long long npairs = 0;
     unsigned exact = 0;
     for (int qi = gtid(); qi < nq; qi += gstride()) {
+        if (kRedo && redo[qi] == 0) continue;
         const int f = qsorted[qi];
-        if (nl < 2) continue;
+        if (nl < 2) {
+            if (!kRedo) redo[qi] = 0;
+            continue;
+        }
         const float4 qlo = box_lo[f], qhi = box_hi[f];
         int sp = 0;
         int node = 0;
         int guard = 0;
+        bool over = false;
         while (true) {
             if (++guard > (1 << 22)) {
                 atomicOr(&rc->status, kErrIterLimit);
@@ -364,18 +368,25 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse(const float4* __rest
                     const int g = __float_as_int(hi.w);
                     if (g == f) continue;
                     if (g < f && qscan[g + 1] != qscan[g]) continue;  // the lower query face owns the pair
-                    ++npairs;
-                    const int at = warp_append(n_list);
-                    if (at < pair_cap) {
-                        pairs_out[at] = make_int2(f, g);
-                    } else if (decide_pair(f, g, tri, pos, eps, exact)) {
-                        hit[f] = 1;
-                        hit[g] = 1;
+                    if (kRedo) {
+                        if (decide_pair(f, g, tri, pos, eps, exact)) {
+                            hit[f] = 1;
+                            hit[g] = 1;
+                        }
+                    } else {
+                        const int at = warp_append(n_list);
+                        if (at < pair_cap) {
+                            pairs_out[at] = make_int2(f, g);
+                            ++npairs;
+                        } else {
+                            over = true;
+                        }
                     }
                 } else {
                     next[nn++] = x;
                 }
             }
+            if (!kRedo && over) break;
             if (nn == 2) {
                 if (sp >= kStackDepth) {
                     atomicOr(&rc->status, kErrStackOverflow);
@@ -390,6 +401,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse(const float4* __rest
                 node = stack[--sp][threadIdx.x];
             }
         }
+        if (!kRedo) redo[qi] = over ? 1 : 0;
     }
     for (int o = 16; o > 0; o >>= 1) {
         npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
@@ -440,7 +452,7 @@ size_t bvh_bytes(int cap) {
     return b;
 }
 
-void bvh_carve(BvhBuffers& b, int cap, char* base) {
+void bvh_carve(BvhBuffers& b, int cap, char* base, bool clear_scan_scratch) {
     size_t c = (size_t)cap + 1;
     char* p = base;
     auto take = [&](size_t bytes) {
@@ -469,6 +481,7 @@ void bvh_carve(BvhBuffers& b, int cap, char* base) {
     b.scan_scratch = (int*)take(4 * scan_scratch_ints());
     b.packed = (float4*)take(64 * c);
     b.meta = (int*)take(16);
+    if (clear_scan_scratch) scan_scratch_clear(b.scan_scratch);
 }
 
 // one 64-byte record per internal node holding both children's boxes (and leaf face ids), so that a traversal
@@ -511,12 +524,12 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
     cudaMemsetAsync(b.scene + 3, 0x00, 3 * sizeof(unsigned), s);
     const int gF = grid_for(n_tris_bound, 256);
     k_boxes<<<gF, 256, 0, s>>>(tri, pos, rc, b.box_lo, b.box_hi, b.live_scan, b.scene, all_faces ? 1 : 0); note_launch();
-    exclusive_scan(b.live_scan, b.live_scan, &rc->n_tris, 1, &rc->n_live, b.scan_scratch, s);
+    exclusive_scan(b.live_scan, b.live_scan, &rc->n_tris, 1, &rc->n_live, b.scan_scratch, s, &rc->status);
     k_morton<<<gF, 256, 0, s>>>(rc, b.live_scan, b.box_lo, b.box_hi, b.scene, b.keys[0], b.vals[0]); note_launch();
     for (int pass = 0; pass < 4; ++pass) {
         const int in = pass & 1, out = in ^ 1;
         k_rs_hist<<<kSortTiles, kSortThreads, 0, s>>>(b.keys[in], &rc->n_live, 8 * pass, b.hist); note_launch();
-        exclusive_scan(b.hist, b.hist, nullptr, 256 * kSortTiles, nullptr, b.scan_scratch, s);
+        exclusive_scan(b.hist, b.hist, nullptr, 256 * kSortTiles, nullptr, b.scan_scratch, s, &rc->status);
         k_rs_scatter<<<kSortTiles, kSortThreads, 0, s>>>(b.keys[in], b.vals[in], b.keys[out], b.vals[out], &rc->n_live,
                                                          8 * pass, b.hist); note_launch();
     }
@@ -607,13 +620,18 @@ void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const in
     const int gF = grid_for(n_query_bound, 256);
     k_query_order<<<gF, 256, 0, s>>>(rc, b.vals[0], qscan, b.live_scan);
     note_launch();
-    exclusive_scan(b.live_scan, b.live_scan, &rc->n_live, 1, &rc->pad[2], b.scan_scratch, s);
+    exclusive_scan(b.live_scan, b.live_scan, &rc->n_live, 1, &rc->pad[2], b.scan_scratch, s, &rc->status);
     k_query_gather<<<gF, 256, 0, s>>>(rc, b.vals[0], b.live_scan, b.vals[1]);
     note_launch();
-    k_traverse<<<grid_for(n_query_bound, kQueryThreads, 16), kQueryThreads, 0, s>>>(
-        b.packed, b.box_lo, b.box_hi, tri, pos, b.vals[1], qscan, hit, pair_list, pair_cap, rc, eps);
+    // b.visit (free between a tree's bottom-up passes) holds the per-query overflow marks
+    const int gQ = grid_for(n_query_bound, kQueryThreads, 16);
+    k_traverse<false><<<gQ, kQueryThreads, 0, s>>>(b.packed, b.box_lo, b.box_hi, tri, pos, b.vals[1], qscan, hit,
+                                                   pair_list, pair_cap, rc, eps, b.visit);
     note_launch();
     k_pairs<<<grid_for((long long)pair_cap, 128, 16), 128, 0, s>>>(tri, pos, pair_list, pair_cap, hit, rc, eps);
+    note_launch();
+    k_traverse<true><<<gQ, kQueryThreads, 0, s>>>(b.packed, b.box_lo, b.box_hi, tri, pos, b.vals[1], qscan, hit,
+                                                  pair_list, pair_cap, rc, eps, b.visit);
     note_launch();
 }
 

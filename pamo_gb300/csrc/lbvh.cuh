@@ -31,7 +31,9 @@ struct BvhBuffers {
 };
 
 size_t bvh_bytes(int cap);
-void bvh_carve(BvhBuffers& b, int cap, char* base);
+// Lays the buffers out from base; clear_scan_scratch zeroes the tree's scan scratch (synchronous), which
+// memory that is not zero-initialised needs before its first build.
+void bvh_carve(BvhBuffers& b, int cap, char* base, bool clear_scan_scratch = true);
 
 // Builds the LBVH over faces with tri[f].x != -1 (count from rc->n_tris); writes rc->n_live. With all_faces,
 // every face slot below rc->n_tris is a leaf and a removed face has an empty box, so that the tree can be

@@ -109,6 +109,7 @@ struct pamo_ctx {
     DevBuf<uint32_t> edge_cost;
     DevBuf<unsigned char> invalid;
     DevBuf<int> pts_map, undo_list, tmp_undo;
+    DevBuf<int> pts_map_prev;  // device rounds: the previous round's map while this round's replaces pts_map
     int* d_ecap = nullptr;  // reference's allocated_edge_cost, kept on the device
 
     // ---- per-vertex working buffers ----
@@ -162,6 +163,12 @@ struct pamo_ctx {
     bool use_graphs = true;     // device rounds as cached graphs
     bool device_rounds = true;  // rounds after the first from device-resident sizes (pamo_simplify_device)
     bool bvh_reuse = true;      // device rounds refit the LBVH carried from the previous round
+    long long pair_cap_limit = 0;  // > 0: at most this many listed candidate pairs per check (tests the overflow path)
+
+    int pair_cap() const {
+        const long long n = (long long)exact_list.n;
+        return (int)(pair_cap_limit > 0 && pair_cap_limit < n ? pair_cap_limit : n);
+    }
     DevBuf<float> face_mean;
     float* h_pinned_f = nullptr;
 
@@ -222,6 +229,7 @@ struct pamo_ctx {
         if ((r = check(cudaMallocHost((void**)&h_rc, sizeof(RoundCounters)), "cudaMallocHost"))) return r;
         if ((r = check(cudaMallocHost((void**)&h_pinned_f, 64 * sizeof(float)), "cudaMallocHost"))) return r;
         if ((r = check(cudaMalloc((void**)&scan_scratch, scan_scratch_ints() * sizeof(int)), "cudaMalloc"))) return r;
+        if (scan_scratch_clear(scan_scratch)) return check(cudaGetLastError(), "scan scratch");
         if ((r = check(cudaMalloc((void**)&d_ecap, sizeof(int)), "cudaMalloc"))) return r;
         if ((r = check(cudaMalloc((void**)&d_scale, sizeof(float)), "cudaMalloc"))) return r;
         if ((r = check(cudaMalloc((void**)&d_center, 16 * sizeof(float)), "cudaMalloc"))) return r;
@@ -238,7 +246,7 @@ struct pamo_ctx {
             b.p = nullptr;
             b.n = 0;
         };
-        fr(edge_cost); fr(invalid); fr(pts_map); fr(undo_list); fr(tmp_undo);
+        fr(edge_cost); fr(invalid); fr(pts_map); fr(pts_map_prev); fr(undo_list); fr(tmp_undo);
         fr(pos); fr(orig_pos); fr(pos_in); fr(pos_out); fr(occ); fr(valence); fr(cursor); fr(quad); fr(vmin); fr(undo_in);
         fr(tri); fr(orig_tri); fr(tri_in); fr(tri_out); fr(ecount); fr(qflag); fr(qlist); fr(fflags); fr(nt);
         fr(shuffle_flags); fr(fkey); fr(eorder); fr(vedges); fr(vcursor); fr(hit); fr(edges); fr(win); fr(collapsed); fr(uflag); fr(face_mean); fr(exact_list);
@@ -286,6 +294,7 @@ struct pamo_ctx {
         if ((r = fresh(pts_map))) return r;
         if ((r = fresh(undo_list))) return r;
         if ((r = fresh(tmp_undo))) return r;
+        if ((r = grow(pts_map_prev, len))) return r;
         return PAMO_OK;
     }
 
@@ -308,7 +317,8 @@ struct pamo_ctx {
              qlist.bytes() + fflags.bytes() + nt.bytes() + shuffle_flags.bytes() + fkey.bytes() + hit.bytes() +
              edges.bytes() + win.bytes() + collapsed.bytes() + uflag.bytes() + eorder.bytes() + exact_list.bytes() +
              face_mean.bytes();
-        b += edge_cost.bytes() + invalid.bytes() + pts_map.bytes() + undo_list.bytes() + tmp_undo.bytes();
+        b += edge_cost.bytes() + invalid.bytes() + pts_map.bytes() + pts_map_prev.bytes() + undo_list.bytes() +
+             tmp_undo.bytes();
         b += bvh_cap ? bvh_bytes((int)bvh_cap) : 0;
         return b;
     }
@@ -384,14 +394,15 @@ struct pamo_ctx {
             launch_round_begin(rc, d_ls, d_ls + 1, s);
             launch_undo_bookkeeping_dev(undo_in.p, d_ls, list_cap, tmp_undo.p, undo_list.p, pts_map.p, (int)pts_map.n,
                                         invalid.p, (int)invalid.n, s);
+            launch_copy_map_dev(d_ls, pts_map.p, pts_map_prev.p, nPb, s);
             launch_load_points4_dev(pos_in.p, rc, nPb, pos.p, orig_pos.p, occ.p, s);
             launch_copy_tris_dev(tri_in.p, tri.p, rc, nTb, s);
             launch_copy_tris_dev(tri.p, orig_tri.p, rc, nTb, s);
             launch_zero_vertex_counts_dev(rc, nPb, valence.p, cursor.p, vedges.p, vcursor.p, s);
             launch_face_counts(tri.p, rc, nTb, valence.p, ecount.p, vedges.p, s);
-            exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
-            exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s);
-            exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
+            exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
+            exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status);
+            exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
             launch_fill_adjacency(tri.p, rc, nTb, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p,
                                   eorder.p, s);
             launch_sort_adjacency(rc, nPb, valence.p, nt.p, s);
@@ -403,31 +414,31 @@ struct pamo_ctx {
             launch_face_keys(rc, nTb, tri.p, vmin.p, fkey.p, s);
             launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p,
                             pos.p, orig_pos.p, occ.p, win.p, s);
-            exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s);
+            exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s, &rc->status);
             launch_compact_winners(rc, eb, win.p, collapsed.p, s);
             launch_remove_invalid(rc, nTb, tri.p, s);
             launch_line_edges(rc, eb, edges.p, nt_off, nt.p, tri.p, pos.p, occ.p, nullptr, (int)collapsed.n,
                               collapsed.p, s);
             launch_zero_face_ints_dev(rc, nTb, qflag.p, s);
             launch_mark_query(rc, eb, collapsed.p, edges.p, nt_off, nt.p, qflag.p, s);
-            exclusive_scan(qflag.p, qflag.p, &rc->n_tris, 1, &rc->n_query, scan_scratch, s);
+            exclusive_scan(qflag.p, qflag.p, &rc->n_tris, 1, &rc->n_query, scan_scratch, s, &rc->status);
             launch_compact_flags(qflag.p, nTb, &rc->n_tris, qlist.p, s);
         } else {
             launch_undo_apply(rc, eb, collapsed.p, uflag.p, edges.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p, orig_pos.p,
-                              occ.p, tmp_undo.p, undo_list.p, pts_map.p, list_cap, s);
+                              occ.p, tmp_undo.p, undo_list.p, pts_map_prev.p, list_cap, s);
         }
         // intersection check; the LBVH spans every face slot of the round and is refitted when reused
         launch_zero_face_bytes_dev(rc, nTb, hit.p, s);
         if (kind == 0) bvh_build(bvh, tri.p, pos.p, rc, nTb, s, true);
         else bvh_refit_faces(bvh, tri.p, pos.p, rc, nTb, s, kind == 2);
-        bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, (int)exact_list.n, rc, nTb, kTriEps, s);
+        bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, pair_cap(), rc, nTb, kTriEps, s);
         launch_undo_check(rc, eb, collapsed.p, edges.p, nt_off, nt.p, hit.p, uflag.p, s);
-        exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s);
+        exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s, &rc->status);
         launch_after_check(rc, s);
         // compaction map (cusimp_free.cu:1042-1045), compaction (pamo/__init__.py:136-140), next round's state
-        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
+        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
         launch_live_flags(rc, nTb, tri.p, fflags.p, s);
-        exclusive_scan(fflags.p, fflags.p, &rc->n_tris, 1, nullptr, scan_scratch, s);
+        exclusive_scan(fflags.p, fflags.p, &rc->n_tris, 1, nullptr, scan_scratch, s, &rc->status);
         launch_compact_mesh(rc, nPb, nTb, pos.p, occ.p, pts_map.p, tri.p, fflags.p, pos_out.p, tri_out.p, s);
         bvh_remap(bvh, fflags.p, nTb, s);  // the tree's leaves in the next round's face numbering
         launch_round_end(rc, d_ls, d_ls + 1, undo_list.p, undo_in.p, (int)std::min(undo_in.n, undo_list.n), list_cap, s);
@@ -518,7 +529,7 @@ struct pamo_ctx {
         else if (tri_src != tris4) launch_load_tris4(tris4, nT, tri_src, s);
         if (init) {
             Feistel fb = make_feistel((unsigned long long)nT);
-            if (nT > 0) launch_shuffle_tris(fb, shuffle_flags.p, scan_scratch, tri_src, tri.p, nT, s);
+            if (nT > 0) launch_shuffle_tris(fb, shuffle_flags.p, scan_scratch, tri_src, tri.p, nT, s, &rc->status);
         }
         launch_copy_tris(tri.p, orig_tri.p, nT, s);
         prof.end(kPhLoad, s);
@@ -530,9 +541,9 @@ struct pamo_ctx {
         cudaMemsetAsync(vedges.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(vcursor.p, 0, (nP + 1) * sizeof(int), s);
         launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s);
-        exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
-        exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s);
-        exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
+        exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
+        exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status);
+        exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
         launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p, eorder.p, s);
         launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
         const int* nt_off = valence.p;
@@ -553,7 +564,7 @@ struct pamo_ctx {
         launch_face_keys(rc, nT, tri.p, vmin.p, fkey.p, s);
         launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p,
                         orig_pos.p, occ.p, win.p, s);
-        exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s);
+        exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s, &rc->status);
         launch_compact_winners(rc, eb, win.p, collapsed.p, s);
         prof.end(kPhCollapse, s);
         prof.begin(kPhMarks, s);
@@ -563,7 +574,7 @@ struct pamo_ctx {
         // faces whose intersections decide the undo: rings of the considered collapsed edges
         cudaMemsetAsync(qflag.p, 0, (nT + 1) * sizeof(int), s);
         launch_mark_query(rc, eb, collapsed.p, edges.p, nt_off, nt.p, qflag.p, s);
-        exclusive_scan(qflag.p, qflag.p, &rc->n_tris, 1, &rc->n_query, scan_scratch, s);
+        exclusive_scan(qflag.p, qflag.p, &rc->n_tris, 1, &rc->n_query, scan_scratch, s, &rc->status);
         launch_compact_flags(qflag.p, nT, &rc->n_tris, qlist.p, s);
         prof.end(kPhMarks, s);
 
@@ -575,10 +586,10 @@ struct pamo_ctx {
             bvh_build(bvh, tri.p, pos.p, rc, nT, s);
             prof.end(kPhBvh, s);
             prof.begin(kPhQuery, s);
-            bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, (int)exact_list.n, rc, nT, kTriEps, s);
+            bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, pair_cap(), rc, nT, kTriEps, s);
             prof.end(kPhQuery, s);
             launch_undo_check(rc, eb, collapsed.p, edges.p, nt_off, nt.p, hit.p, uflag.p, s);
-            exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s);
+            exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s, &rc->status);
             launch_after_check(rc, s);
         };
         check_pass();
@@ -594,7 +605,7 @@ struct pamo_ctx {
         }
 
         // compaction map (cusimp_free.cu:1042-1045)
-        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s);
+        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
         (void)operator_mode;
         if ((r = read_counters())) return r;
         if ((r = status_to_error(h_rc->status))) return r;
@@ -663,7 +674,10 @@ int pamo_ctx_set_option(pamo_ctx* ctx, const char* name, int64_t value) {
     if (n == "graphs") ctx->use_graphs = value != 0;
     else if (n == "device_rounds") ctx->device_rounds = value != 0;
     else if (n == "bvh_reuse") ctx->bvh_reuse = value != 0;
-    else return ctx->fail(PAMO_ERR_INVALID_ARG, "unknown option %s", name);
+    else if (n == "pair_cap") {
+        ctx->pair_cap_limit = value;
+        ctx->drop_graphs();
+    } else return ctx->fail(PAMO_ERR_INVALID_ARG, "unknown option %s", name);
     return PAMO_OK;
 }
 
@@ -805,7 +819,7 @@ int simplify_loop_on(pamo_ctx* ctx, const float* points, const int32_t* triangle
             // compaction (pamo/__init__.py:136-140)
             ctx->prof.begin(kPhCompact, s);
             launch_live_flags(ctx->rc, nf, ctx->tri.p, ctx->fflags.p, s);
-            exclusive_scan(ctx->fflags.p, ctx->fflags.p, &ctx->rc->n_tris, 1, nullptr, ctx->scan_scratch, s);
+            exclusive_scan(ctx->fflags.p, ctx->fflags.p, &ctx->rc->n_tris, 1, nullptr, ctx->scan_scratch, s, &ctx->rc->status);
             launch_compact_mesh(ctx->rc, np, nf, ctx->pos.p, ctx->occ.p, ctx->pts_map.p, ctx->tri.p, ctx->fflags.p,
                                 ctx->pos_out.p, ctx->tri_out.p, s);
             ctx->prof.end(kPhCompact, s);
@@ -968,12 +982,12 @@ int pamo_self_intersect(pamo_ctx* ctx, const float* points, const int32_t* trian
     launch_load_tris(triangles, n_triangles, n_points, ctx->tri.p, ctx->rc, s);
     // every live face queries
     launch_live_flags(ctx->rc, n_triangles, ctx->tri.p, ctx->qflag.p, s);
-    exclusive_scan(ctx->qflag.p, ctx->qflag.p, &ctx->rc->n_tris, 1, &ctx->rc->n_query, ctx->scan_scratch, s);
+    exclusive_scan(ctx->qflag.p, ctx->qflag.p, &ctx->rc->n_tris, 1, &ctx->rc->n_query, ctx->scan_scratch, s, &ctx->rc->status);
     launch_compact_flags(ctx->qflag.p, n_triangles, &ctx->rc->n_tris, ctx->qlist.p, s);
     cudaMemsetAsync(ctx->hit.p, 0, n_triangles + 1, s);
     bvh_build(ctx->bvh, ctx->tri.p, ctx->pos.p, ctx->rc, n_triangles, s);
     bvh_query(ctx->bvh, ctx->tri.p, ctx->pos.p, ctx->qlist.p, ctx->qflag.p, ctx->hit.p, ctx->exact_list.p,
-              (int)ctx->exact_list.n, ctx->rc, n_triangles, kTriEps, s);
+              ctx->pair_cap(), ctx->rc, n_triangles, kTriEps, s);
     cudaMemcpyAsync(face_hit, ctx->hit.p, n_triangles, cudaMemcpyDeviceToDevice, s);
     if ((r = ctx->read_counters())) return r;
     return ctx->status_to_error(ctx->h_rc->status);

@@ -7,13 +7,19 @@ namespace pamo {
 
 constexpr int kScanTiles = 4 * 152;
 
-// scratch ints needed by exclusive_scan
-inline size_t scan_scratch_ints() { return kScanTiles + 32; }
+// scratch ints needed by exclusive_scan (8 header ints and a 64-bit status word per tile)
+inline size_t scan_scratch_ints() { return 8 + 2 * (size_t)kScanTiles; }
 
 // out[i] = sum_{j<i} in[i] for i in [0, n), n = (d_n ? *d_n : 0) + n_add. in == out is allowed.
 // If d_total is given, *d_total = sum of all n inputs. Inputs are int32 counts (no overflow checks).
+// The scratch must be all zero before the first scan (scan_scratch_clear, or zero-initialised static memory);
+// every scan leaves it zero again. One scratch serves one stream at a time. A look-back that waits too long
+// sets kErrIterLimit in *err (when given).
 void exclusive_scan(const int* in, int* out, const int* d_n, int n_add, int* d_total, int* scratch,
-                    cudaStream_t s);
+                    cudaStream_t s, int* err = nullptr);
+
+// Zeroes a freshly allocated scan scratch (synchronous); returns nonzero on a CUDA error.
+int scan_scratch_clear(int* scratch);
 
 __device__ __forceinline__ int warp_inclusive_scan(int v) {
 #pragma unroll

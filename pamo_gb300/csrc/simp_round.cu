@@ -208,11 +208,6 @@ __device__ __forceinline__ int next_after(int4 t, int v) {
     return -1;
 }
 
-__device__ __forceinline__ float tri_area(V3 p0, V3 p1, V3 p2) {
-    const float a = vnorm(vsub(p0, p1)), b = vnorm(vsub(p1, p2)), c = vnorm(vsub(p2, p0));
-    const float s = (a + b + c) / 2;
-    return sqrtf(s * (s - a) * (s - b) * (s - c));
-}
 
 __device__ __forceinline__ void ring_len(int w, const int* __restrict__ nt_off, const int* __restrict__ nt,
                                          const int4* __restrict__ tri, const float4* __restrict__ pos, float& len, int& cnt) {
@@ -850,6 +845,13 @@ __global__ void k_round_end(const RoundCounters* rc, const LoopState* ls, LoopSt
     *next = L;
 }
 
+// the previous round's compaction map, kept for the undo passes of this round (the round's own compaction
+// overwrites pts_map before an undo pass may follow); undo entries index it with this round's vertex ids (< np)
+__global__ void k_copy_map_dev(const LoopState* ls, const int* __restrict__ src, int* dst) {
+    const int n = ls->np;
+    for (int i = gtid(); i < n; i += gstride()) dst[i] = src[i];
+}
+
 // undo vertices carried to the next round (the host loop's copy of the previous undo list)
 __global__ void k_copy_undo_dev(const RoundCounters* rc, const int* __restrict__ src, int* dst, int cap) {
     const int n = min(rc->n_vertices_undo, cap);
@@ -914,11 +916,12 @@ void launch_load_tris4(const int4* tris, int n, int4* tri, cudaStream_t s) {
 void launch_copy_tris(const int4* src, int4* dst, int n, cudaStream_t s) {
     k_copy4<<<grid_for(n, kT), kT, 0, s>>>(src, dst, n); note_launch();
 }
-void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4* src, int4* dst, int n, cudaStream_t s) {
+void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4* src, int4* dst, int n, cudaStream_t s,
+                         int* err) {
     (void)n;
     const int g = grid_for((long long)fb.n, kT);
     k_shuffle_flags<<<g, kT, 0, s>>>(fb, flags); note_launch();
-    exclusive_scan(flags, flags, nullptr, (int)fb.n + 1, nullptr, scan_scratch, s);
+    exclusive_scan(flags, flags, nullptr, (int)fb.n + 1, nullptr, scan_scratch, s, err);
     k_shuffle_gather<<<g, kT, 0, s>>>(fb, flags, src, dst); note_launch();
 }
 
@@ -984,6 +987,9 @@ void launch_compact_flags(const int* scan, int n_bound, const int* d_n, int* out
 void launch_undo_check(RoundCounters* rc, int n_edges_bound, const int* collapsed, const int2* edges, const int* nt_off,
                        const int* nt, const unsigned char* hit, int* uflag, cudaStream_t s) {
     k_undo_check<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, collapsed, edges, nt_off, nt, hit, uflag); note_launch();
+}
+void launch_copy_map_dev(const LoopState* ls, const int* pts_map, int* pts_map_prev, int n_pts_bound, cudaStream_t s) {
+    k_copy_map_dev<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(ls, pts_map, pts_map_prev); note_launch();
 }
 void launch_undo_apply(RoundCounters* rc, int n_edges_bound, const int* collapsed, const int* uscan, const int2* edges,
                        const int* nt_off, const int* nt, int4* tri, const int4* orig_tri, float4* pos,

@@ -22,7 +22,8 @@ void launch_load_points(const float* pts, int n, float4* pos, float4* orig_pos, 
 void launch_load_points4(const float4* pts, int n, float4* pos, float4* orig_pos, int* occ, cudaStream_t s);
 void launch_load_tris(const int* tris, int n, int n_pts, int4* tri, RoundCounters* rc, cudaStream_t s);
 void launch_load_tris4(const int4* tris, int n, int4* tri, cudaStream_t s);
-void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4* tmp, int4* tri, int n, cudaStream_t s);
+void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4* tmp, int4* tri, int n, cudaStream_t s,
+                         int* err = nullptr);
 void launch_copy_tris(const int4* src, int4* dst, int n, cudaStream_t s);
 
 // ---- adjacency ----
@@ -83,6 +84,8 @@ void launch_after_check(RoundCounters* rc, cudaStream_t s);
 
 // ---- device-driven rounds: sizes from LoopState / RoundCounters, host values only bound the grids ----
 void launch_round_begin(RoundCounters* rc, LoopState* ls, const LoopState* next, cudaStream_t s);
+// pts_map_prev[0, ls->np) = pts_map: the previous round's map, read by this round's undo passes
+void launch_copy_map_dev(const LoopState* ls, const int* pts_map, int* pts_map_prev, int n_pts_bound, cudaStream_t s);
 void launch_undo_bookkeeping_dev(const int* verts_undo, const LoopState* ls, int n_undo_bound, int* tmp_undo,
                                  int* undo_list, const int* pts_map, int pts_map_len, unsigned char* invalid,
                                  int invalid_len, cudaStream_t s);

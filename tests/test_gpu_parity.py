@@ -143,23 +143,45 @@ def test_blender_entry_matches_oracle(name):
         assert np.array_equal(V, Vo)
 
 
-@pytest.mark.parametrize("mode", [(1, 1), (1, 0), (0, 0)])
-def test_loop_execution_modes_agree(mode):
-    """The whole loop gives the oracle's result with device-driven rounds as graphs, as direct launches, and
-    with the host-sized rounds."""
+@pytest.mark.parametrize("mode", [(1, 1, 1), (1, 1, 0), (1, 0, 1), (0, 0, 0)])
+@pytest.mark.parametrize("name,ratio", [("plain_small", 0.01), ("tangled", 0.05), ("tangled_strong", 0.05)])
+def test_loop_execution_modes_agree(mode, name, ratio):
+    """The whole loop gives the oracle's result with device-driven rounds as graphs (with the carried LBVH and
+    with one built every round), as direct launches, and with the host-sized rounds; the tangled meshes take
+    undo passes in many rounds."""
     import pamo_gb300
     from pamo_gb300 import synth
 
-    v, f = synth.config_mesh("plain_small")
+    v, f = synth.config_mesh("plain_small") if name == "plain_small" else _cases()[name]
     ctx = pamo_gb300.Context("cuda:0")
     ctx.set_option("device_rounds", mode[0])
     ctx.set_option("graphs", mode[1])
+    ctx.set_option("bvh_reuse", mode[2])
     pts = torch.tensor(v, device="cuda")
     tri = torch.tensor(f, device="cuda", dtype=torch.int32)
-    Vo, Fo, fpr = orc.Oracle().run(v, f, 0.01, 4, 1e-3, 1000000, 0)
+    Vo, Fo, fpr = orc.Oracle().run(v, f, ratio, 4, 1e-3, 1000000, 0)
     for _ in range(2):  # the second run replays the cached graphs
         ctx.reset()
-        V, F, rounds = pamo_gb300.simplify(pts, tri, 0.01, 4, 1e-3, 1000000, 0, ctx=ctx)
+        V, F, rounds = pamo_gb300.simplify(pts, tri, ratio, 4, 1e-3, 1000000, 0, ctx=ctx)
         assert rounds == len(fpr)
         assert np.array_equal(F.cpu().numpy(), Fo)
         assert np.array_equal(V.cpu().numpy(), Vo)
+
+
+@pytest.mark.parametrize("name,cap", [("tangled_strong", 16), ("plain_small", 256)])
+def test_pair_list_overflow_matches_oracle(name, cap):
+    """With the candidate-pair list cut to a few entries, the queries that overflow it walk the tree again and
+    decide their pairs in place; the whole loop still gives the oracle's result."""
+    import pamo_gb300
+    from pamo_gb300 import synth
+
+    v, f = synth.config_mesh("plain_small") if name == "plain_small" else _cases()[name]
+    ctx = pamo_gb300.Context("cuda:0")
+    ctx.set_option("pair_cap", cap)
+    pts = torch.tensor(v, device="cuda")
+    tri = torch.tensor(f, device="cuda", dtype=torch.int32)
+    Vo, Fo, fpr = orc.Oracle().run(v, f, 0.05, 4, 1e-3, 1000000, 0)
+    V, F, rounds = pamo_gb300.simplify(pts, tri, 0.05, 4, 1e-3, 1000000, 0, ctx=ctx)
+    assert rounds == len(fpr)
+    assert np.array_equal(F.cpu().numpy(), Fo)
+    assert np.array_equal(V.cpu().numpy(), Vo)
