@@ -18,7 +18,10 @@ namespace {
 constexpr int kSortTiles = 4 * kNumSM;
 constexpr int kSortThreads = 256;
 constexpr int kQueryThreads = 128;
-constexpr int kStackDepth = 64;
+constexpr int kStackDepth = 64;  // enough for any tree (depth <= 62 + 1)
+constexpr int kShortStack = 24;  // first walk: deeper queries are handed to the second walk
+constexpr int kPairChunk = 32;   // list slots a lane takes at a time
+constexpr int kQueryBit = 1 << 30;  // set on a packed leaf's face id when the face is a query face
 
 __device__ __forceinline__ unsigned f2ord(float f) {
     unsigned u = __float_as_uint(f);
@@ -268,21 +271,11 @@ __global__ void __launch_bounds__(256) k_bottom_up(RoundCounters* rc, const int2
 // ---------------------------------------------------------------- localized query
 // 1. k_query_order: the query faces in leaf (Morton) order, so that neighbouring threads walk the same
 //    part of the tree and test neighbouring faces.
-// 2. k_traverse: one thread per query face walks the tree with its stack in shared memory and emits every
-//    overlapping leaf g as a candidate pair (f, g); a pair of two query faces is emitted only by the lower
-//    face index. Queries whose pairs do not fit the list walk again after k_pairs and decide in place.
+// 2. k_traverse_list: one thread per query face walks the tree with a short stack in shared memory and emits
+//    every overlapping leaf g as a candidate pair (f, g); a pair of two query faces is emitted only by the lower
+//    face index. Queries that overflow the list or the stack walk again (k_traverse_redo) and decide in place.
 // 3. k_pairs: one thread per candidate pair runs the reference's decision in both orders (float
 //    certificates first, the fp64 path only for undecided pairs) and flags both faces when it holds.
-__device__ __forceinline__ int warp_append(int* counter) {
-    const unsigned am = __activemask();
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(am) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(counter, __popc(am));
-    base = __shfl_sync(am, base, leader);
-    return base + __popc(am & ((1u << lane) - 1u));
-}
-
 __device__ __forceinline__ bool decide_pair(int f, int g, const int4* __restrict__ tri, const float4* __restrict__ pos,
                                             float eps, unsigned& exact) {
     const int4 qt = tri[f], gt = tri[g];
@@ -320,36 +313,126 @@ __device__ __forceinline__ bool box_overlap4(float4 qlo, float4 qhi, float4 lo, 
     return !(qhi.x < lo.x || hi.x < qlo.x || qhi.y < lo.y || hi.y < qlo.y || qhi.z < lo.z || hi.z < qlo.z);
 }
 
-// kRedo = false: the first walk. Candidate pairs go to the pair list; a query whose pair does not fit stops
-// and is marked in redo[qi]. kRedo = true: only when the list overflowed, the marked queries walk again and
-// decide every pair in place (pairs already listed are decided twice, which sets the same flags).
-template <bool kRedo>
-__global__ void __launch_bounds__(kQueryThreads) k_traverse(const float4* __restrict__ packed,
-                                                             const float4* __restrict__ box_lo,
-                                                             const float4* __restrict__ box_hi, const int4* __restrict__ tri,
-                                                             const float4* __restrict__ pos, const int* __restrict__ qsorted,
-                                                             const int* __restrict__ qscan, unsigned char* hit,
-                                                             int2* pairs_out, int pair_cap, RoundCounters* rc, float eps,
-                                                             int* redo) {
-    __shared__ int stack[kStackDepth][kQueryThreads];
+// First walk: candidate pairs go to the pair list. The loop is flat: a thread whose query is done takes its
+// next query in the same iteration in which the other lanes of its warp take their next node, so the lanes
+// stay busy until the warp runs out of queries. A query whose pair does not fit the list, or whose deferred
+// siblings do not fit the short stack, stops and is marked in redo[qi] (and counted in rc->pad[3]).
+__global__ void __launch_bounds__(kQueryThreads) k_traverse_list(const float4* __restrict__ packed,
+                                                                  const float4* __restrict__ box_lo,
+                                                                  const float4* __restrict__ box_hi,
+                                                                  const int* __restrict__ qsorted, int2* pairs_out,
+                                                                  int pair_cap, RoundCounters* rc, int* redo) {
+    __shared__ int stack[kShortStack][kQueryThreads];
     int* n_list = &rc->pad[1];
-    if (kRedo && *n_list <= pair_cap) return;
     const int nq = rc->pad[2];
-    const int nl = rc->n_live;
+    const bool empty = rc->n_live < 2;
     unsigned long long npairs = 0;
-    unsigned exact = 0;
-    for (int qi = gtid(); qi < nq; qi += gstride()) {
-        if (kRedo && redo[qi] == 0) continue;
-        const int f = qsorted[qi];
-        if (nl < 2) {
-            if (!kRedo) redo[qi] = 0;
+    // each lane fills its own chunk of kPairChunk list slots, so that one atomic on the list length serves
+    // many pairs (a single counter is an L2 hot spot); unused slots of a lane's last chunk are set to -1
+    const int lane = threadIdx.x & 31;
+    int cbase = -1, cused = kPairChunk;
+    int qi = gtid() - gstride();
+    int f = 0, node = -1, sp = 0, guard = 0;
+    float4 qlo = make_float4(0.f, 0.f, 0.f, 0.f), qhi = qlo;
+    while (true) {
+        if (node < 0) {
+            qi += gstride();
+            if (qi >= nq) break;
+            redo[qi] = 0;
+            if (empty) continue;
+            f = qsorted[qi];
+            qlo = box_lo[f];
+            qhi = box_hi[f];
+            node = 0;
+            sp = 0;
+            guard = 0;
+        }
+        if (++guard > (1 << 22)) {
+            atomicOr(&rc->status, kErrIterLimit);
+            node = -1;
             continue;
         }
+        const float4* rec = packed + 4 * (size_t)node;
+        const float4 alo = __ldg(rec), ahi = __ldg(rec + 1), blo = __ldg(rec + 2), bhi = __ldg(rec + 3);
+        int next[2];
+        int nn = 0;
+        bool abandon = false;
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const float4 lo = side ? blo : alo, hi = side ? bhi : ahi;
+            if (!box_overlap4(qlo, qhi, lo, hi)) continue;
+            const int x = __float_as_int(lo.w);
+            if (x < 0) {
+                const int graw = __float_as_int(hi.w);
+                const int g = graw & ~kQueryBit;
+                if (g == f) continue;
+                if (g < f && (graw & kQueryBit)) continue;  // the lower query face owns the pair
+                if (cused == kPairChunk) {
+                    const unsigned am = __activemask();
+                    const int leader = __ffs(am) - 1;
+                    int b = 0;
+                    if (lane == leader) b = atomicAdd(n_list, kPairChunk * __popc(am));
+                    b = __shfl_sync(am, b, leader);
+                    cbase = b + kPairChunk * __popc(am & ((1u << lane) - 1u));
+                    cused = 0;
+                }
+                const int at = cbase + cused++;
+                if (at < pair_cap) {
+                    pairs_out[at] = make_int2(f, g);
+                    ++npairs;
+                } else {
+                    abandon = true;
+                }
+            } else {
+                next[nn++] = x;
+            }
+        }
+        if (nn == 2) {
+            if (sp >= kShortStack) {
+                abandon = true;
+            } else {
+                stack[sp++][threadIdx.x] = next[1];
+                node = next[0];
+            }
+        } else if (nn == 1) {
+            node = next[0];
+        } else {
+            node = sp > 0 ? stack[--sp][threadIdx.x] : -1;
+        }
+        if (abandon) {
+            redo[qi] = 1;
+            atomicAdd(&rc->pad[3], 1);
+            node = -1;
+        }
+    }
+    if (cbase >= 0)
+        for (int k = cused; k < kPairChunk && cbase + k < pair_cap; ++k) pairs_out[cbase + k] = make_int2(-1, -1);
+    __syncwarp();
+    for (int o = 16; o > 0; o >>= 1) npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
+    if (lane == 0 && npairs) atomicAdd(&rc->n_pairs, npairs);
+}
+
+// Second walk, only when the first marked queries: each marked query walks the whole tree again with a stack
+// deep enough for any tree (the Karras split prefix grows by at least one of the 62 key bits per level) and
+// decides every pair in place (pairs already listed are decided twice, which sets the same flags).
+__global__ void __launch_bounds__(kQueryThreads) k_traverse_redo(const float4* __restrict__ packed,
+                                                                  const float4* __restrict__ box_lo,
+                                                                  const float4* __restrict__ box_hi,
+                                                                  const int4* __restrict__ tri,
+                                                                  const float4* __restrict__ pos,
+                                                                  const int* __restrict__ qsorted, unsigned char* hit,
+                                                                  RoundCounters* rc, float eps, const int* redo) {
+    __shared__ int stack[kStackDepth][kQueryThreads];
+    if (rc->pad[3] == 0) return;
+    const int nq = rc->pad[2];
+    unsigned exact = 0;
+    for (int qi = gtid(); qi < nq; qi += gstride()) {
+        if (redo[qi] == 0) continue;
+        const int f = qsorted[qi];
         const float4 qlo = box_lo[f], qhi = box_hi[f];
         int sp = 0;
         int node = 0;
         int guard = 0;
-        bool over = false;
         while (true) {
             if (++guard > (1 << 22)) {
                 atomicOr(&rc->status, kErrIterLimit);
@@ -365,28 +448,18 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse(const float4* __rest
                 if (!box_overlap4(qlo, qhi, lo, hi)) continue;
                 const int x = __float_as_int(lo.w);
                 if (x < 0) {
-                    const int g = __float_as_int(hi.w);
+                    const int graw = __float_as_int(hi.w);
+                    const int g = graw & ~kQueryBit;
                     if (g == f) continue;
-                    if (g < f && qscan[g + 1] != qscan[g]) continue;  // the lower query face owns the pair
-                    if (kRedo) {
-                        if (decide_pair(f, g, tri, pos, eps, exact)) {
-                            hit[f] = 1;
-                            hit[g] = 1;
-                        }
-                    } else {
-                        const int at = warp_append(n_list);
-                        if (at < pair_cap) {
-                            pairs_out[at] = make_int2(f, g);
-                            ++npairs;
-                        } else {
-                            over = true;
-                        }
+                    if (g < f && (graw & kQueryBit)) continue;
+                    if (decide_pair(f, g, tri, pos, eps, exact)) {
+                        hit[f] = 1;
+                        hit[g] = 1;
                     }
                 } else {
                     next[nn++] = x;
                 }
             }
-            if (!kRedo && over) break;
             if (nn == 2) {
                 if (sp >= kStackDepth) {
                     atomicOr(&rc->status, kErrStackOverflow);
@@ -401,16 +474,9 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse(const float4* __rest
                 node = stack[--sp][threadIdx.x];
             }
         }
-        if (!kRedo) redo[qi] = over ? 1 : 0;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        npairs += __shfl_xor_sync(0xffffffffu, npairs, o);
-        exact += __shfl_xor_sync(0xffffffffu, exact, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (npairs) atomicAdd(&rc->n_pairs, npairs);
-        if (exact) atomicAdd(&rc->n_exact, (unsigned long long)exact);
-    }
+    for (int o = 16; o > 0; o >>= 1) exact += __shfl_xor_sync(0xffffffffu, exact, o);
+    if ((threadIdx.x & 31) == 0 && exact) atomicAdd(&rc->n_exact, (unsigned long long)exact);
 }
 
 __global__ void __launch_bounds__(128) k_pairs(const int4* __restrict__ tri, const float4* __restrict__ pos,
@@ -420,6 +486,7 @@ __global__ void __launch_bounds__(128) k_pairs(const int4* __restrict__ tri, con
     unsigned exact = 0;
     for (int i = gtid(); i < n; i += gstride()) {
         const int2 p = pair_list[i];
+        if (p.x < 0) continue;  // an unused slot of a chunk
         if (decide_pair(p.x, p.y, tri, pos, eps, exact)) {
             hit[p.x] = 1;
             hit[p.y] = 1;
@@ -489,7 +556,8 @@ void bvh_carve(BvhBuffers& b, int cap, char* base, bool clear_scan_scratch) {
 __global__ void __launch_bounds__(256) k_pack_nodes(const RoundCounters* rc, const int2* __restrict__ child,
                                                      const float4* __restrict__ nlo, const float4* __restrict__ nhi,
                                                      const float4* __restrict__ llo, const float4* __restrict__ lhi,
-                                                     const int* __restrict__ leaf_face, float4* packed, int* meta) {
+                                                     const int* __restrict__ leaf_face, const int* __restrict__ qscan,
+                                                     float4* packed, int* meta) {
     const int n = rc->n_live;
     if (gtid() == 0) meta[0] = n;
     for (int i = gtid(); i < n - 1; i += gstride()) {
@@ -504,6 +572,7 @@ __global__ void __launch_bounds__(256) k_pack_nodes(const RoundCounters* rc, con
                 lo = llo[~x];
                 hi = lhi[~x];
                 face = leaf_face[~x];
+                if (qscan && face >= 0 && qscan[face + 1] != qscan[face]) face |= kQueryBit;
             } else {
                 lo = __ldcg(&nlo[x]);
                 hi = __ldcg(&nhi[x]);
@@ -519,7 +588,7 @@ __global__ void __launch_bounds__(256) k_pack_nodes(const RoundCounters* rc, con
 }
 
 void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s,
-               bool all_faces) {
+               bool all_faces, const int* qscan) {
     cudaMemsetAsync(b.scene, 0xFF, 3 * sizeof(unsigned), s);
     cudaMemsetAsync(b.scene + 3, 0x00, 3 * sizeof(unsigned), s);
     const int gF = grid_for(n_tris_bound, 256);
@@ -536,7 +605,7 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
     k_leaves<<<gF, 256, 0, s>>>(rc, b.vals[0], b.box_lo, b.box_hi, b.llo, b.lhi, b.visit, b.lparent); note_launch();
     k_karras<<<gF, 256, 0, s>>>(rc, b.keys[0], b.child, b.iparent, b.lparent); note_launch();
     k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit); note_launch();
-    k_pack_nodes<<<gF, 256, 0, s>>>(rc, b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], b.packed, b.meta); note_launch();
+    k_pack_nodes<<<gF, 256, 0, s>>>(rc, b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], qscan, b.packed, b.meta); note_launch();
 }
 
 __global__ void __launch_bounds__(256) k_refit_leaves(const RoundCounters* rc, const int4* __restrict__ tri,
@@ -597,13 +666,13 @@ __global__ void __launch_bounds__(256) k_remap_leaves(const int* meta, const int
 }
 
 void bvh_refit_faces(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound,
-                     cudaStream_t s, bool next_round) {
+                     cudaStream_t s, bool next_round, const int* qscan) {
     const int gF = grid_for(n_tris_bound, 256);
     k_boxes<<<gF, 256, 0, s>>>(tri, pos, rc, b.box_lo, b.box_hi, b.live_scan, b.scene, 1); note_launch();
     k_reuse_leaves<<<gF, 256, 0, s>>>(rc, tri, b.box_lo, b.box_hi, next_round ? (const int*)b.keys[1] : nullptr,
                                       b.vals[0], b.llo, b.lhi, b.visit, b.meta); note_launch();
     k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit); note_launch();
-    k_pack_nodes<<<gF, 256, 0, s>>>(rc, b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], b.packed, b.meta); note_launch();
+    k_pack_nodes<<<gF, 256, 0, s>>>(rc, b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], qscan, b.packed, b.meta); note_launch();
 }
 
 void bvh_remap(BvhBuffers& b, const int* fscan, int n_tris_bound, cudaStream_t s) {
@@ -615,7 +684,7 @@ void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const in
                unsigned char* hit, int2* pair_list, int pair_cap, RoundCounters* rc, int n_query_bound, float eps,
                cudaStream_t s) {
     (void)qlist;
-    cudaMemsetAsync(&rc->pad[1], 0, sizeof(int), s);
+    cudaMemsetAsync(&rc->pad[1], 0, 3 * sizeof(int), s);  // list length, query count, redo count
     // query faces in leaf order (uses the sort's second buffers, free after the build)
     const int gF = grid_for(n_query_bound, 256);
     k_query_order<<<gF, 256, 0, s>>>(rc, b.vals[0], qscan, b.live_scan);
@@ -623,15 +692,21 @@ void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const in
     exclusive_scan(b.live_scan, b.live_scan, &rc->n_live, 1, &rc->pad[2], b.scan_scratch, s, &rc->status);
     k_query_gather<<<gF, 256, 0, s>>>(rc, b.vals[0], b.live_scan, b.vals[1]);
     note_launch();
-    // b.visit (free between a tree's bottom-up passes) holds the per-query overflow marks
-    const int gQ = grid_for(n_query_bound, kQueryThreads, 16);
-    k_traverse<false><<<gQ, kQueryThreads, 0, s>>>(b.packed, b.box_lo, b.box_hi, tri, pos, b.vals[1], qscan, hit,
-                                                   pair_list, pair_cap, rc, eps, b.visit);
+    // b.visit (free between a tree's bottom-up passes) holds the per-query redo marks
+    static int blocks_per_sm = 0;
+    if (blocks_per_sm == 0) {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_traverse_list, kQueryThreads, 0) != cudaSuccess || nb < 1)
+            nb = 4;
+        blocks_per_sm = nb;
+    }
+    k_traverse_list<<<grid_for(n_query_bound, kQueryThreads, blocks_per_sm), kQueryThreads, 0, s>>>(
+        b.packed, b.box_lo, b.box_hi, b.vals[1], pair_list, pair_cap, rc, b.visit);
     note_launch();
     k_pairs<<<grid_for((long long)pair_cap, 128, 16), 128, 0, s>>>(tri, pos, pair_list, pair_cap, hit, rc, eps);
     note_launch();
-    k_traverse<true><<<gQ, kQueryThreads, 0, s>>>(b.packed, b.box_lo, b.box_hi, tri, pos, b.vals[1], qscan, hit,
-                                                  pair_list, pair_cap, rc, eps, b.visit);
+    k_traverse_redo<<<grid_for(n_query_bound, kQueryThreads, 4), kQueryThreads, 0, s>>>(
+        b.packed, b.box_lo, b.box_hi, tri, pos, b.vals[1], hit, rc, eps, b.visit);
     note_launch();
 }
 

@@ -38,14 +38,15 @@ void bvh_carve(BvhBuffers& b, int cap, char* base, bool clear_scan_scratch = tru
 // Builds the LBVH over faces with tri[f].x != -1 (count from rc->n_tris); writes rc->n_live. With all_faces,
 // every face slot below rc->n_tris is a leaf and a removed face has an empty box, so that the tree can be
 // refitted after faces are removed or restored (bvh_refit_faces) and carried to the next round (bvh_remap).
+// qscan (exclusive scan of the query flags, or null) marks the query faces in the packed leaves for bvh_query.
 void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s,
-               bool all_faces = false);
+               bool all_faces = false, const int* qscan = nullptr);
 
 // New boxes for the leaves of a tree built with all_faces (a removed face, or a leaf whose face is gone, gets an
 // empty box that overlaps nothing); sets rc->n_live to the tree's leaf count. next_round: first take the leaf
 // face ids bvh_remap computed for this round's numbering.
 void bvh_refit_faces(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound,
-                     cudaStream_t s, bool next_round);
+                     cudaStream_t s, bool next_round, const int* qscan = nullptr);
 
 // After a compaction with exclusive scan fscan of the kept faces: the leaves' face ids in the new numbering
 // (-1 for faces not kept), kept aside until bvh_refit_faces(next_round = true); repeating it is harmless.
@@ -60,7 +61,8 @@ void bvh_refit(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
 // For every face in the query list that is still live: hit[f] = 1 iff some live face g != f with an
 // overlapping closed AABB makes the reference's pair test true in either order. Query faces are taken
 // as the faces f with qscan[f + 1] != qscan[f] (qscan: exclusive scan of the query flags), visited in leaf
-// order. Candidate pairs go through pair_list (capacity pair_cap; beyond it they are decided in place).
+// order. The tree must have been built or refitted with the same qscan (face ids below 2^30). Candidate pairs
+// go through pair_list (capacity pair_cap; queries beyond it decide their pairs in place).
 // qlist is unused (kept for callers that hold one).
 void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, const int* qscan,
                unsigned char* hit, int2* pair_list, int pair_cap, RoundCounters* rc, int n_query_bound, float eps,

@@ -337,6 +337,7 @@ struct pamo_ctx {
     }
 
     int ensure_face_buffers(size_t n) {
+        if (n >= (size_t)(1 << 30) - 8) return fail(PAMO_ERR_CAPACITY, "more than 2^30 faces");
         const size_t c = n + 2;
         if (c <= cap_f && tri.p) return PAMO_OK;
         const size_t nc = c + c / 5;
@@ -429,8 +430,8 @@ struct pamo_ctx {
         }
         // intersection check; the LBVH spans every face slot of the round and is refitted when reused
         launch_zero_face_bytes_dev(rc, nTb, hit.p, s);
-        if (kind == 0) bvh_build(bvh, tri.p, pos.p, rc, nTb, s, true);
-        else bvh_refit_faces(bvh, tri.p, pos.p, rc, nTb, s, kind == 2);
+        if (kind == 0) bvh_build(bvh, tri.p, pos.p, rc, nTb, s, true, qflag.p);
+        else bvh_refit_faces(bvh, tri.p, pos.p, rc, nTb, s, kind == 2, qflag.p);
         bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, pair_cap(), rc, nTb, kTriEps, s);
         launch_undo_check(rc, eb, collapsed.p, edges.p, nt_off, nt.p, hit.p, uflag.p, s);
         exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s, &rc->status);
@@ -583,7 +584,7 @@ struct pamo_ctx {
         auto check_pass = [&]() {
             cudaMemsetAsync(hit.p, 0, nT + 1, s);
             prof.begin(kPhBvh, s);
-            bvh_build(bvh, tri.p, pos.p, rc, nT, s);
+            bvh_build(bvh, tri.p, pos.p, rc, nT, s, false, qflag.p);
             prof.end(kPhBvh, s);
             prof.begin(kPhQuery, s);
             bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, pair_cap(), rc, nT, kTriEps, s);
@@ -985,7 +986,7 @@ int pamo_self_intersect(pamo_ctx* ctx, const float* points, const int32_t* trian
     exclusive_scan(ctx->qflag.p, ctx->qflag.p, &ctx->rc->n_tris, 1, &ctx->rc->n_query, ctx->scan_scratch, s, &ctx->rc->status);
     launch_compact_flags(ctx->qflag.p, n_triangles, &ctx->rc->n_tris, ctx->qlist.p, s);
     cudaMemsetAsync(ctx->hit.p, 0, n_triangles + 1, s);
-    bvh_build(ctx->bvh, ctx->tri.p, ctx->pos.p, ctx->rc, n_triangles, s);
+    bvh_build(ctx->bvh, ctx->tri.p, ctx->pos.p, ctx->rc, n_triangles, s, false, ctx->qflag.p);
     bvh_query(ctx->bvh, ctx->tri.p, ctx->pos.p, ctx->qlist.p, ctx->qflag.p, ctx->hit.p, ctx->exact_list.p,
               ctx->pair_cap(), ctx->rc, n_triangles, kTriEps, s);
     cudaMemcpyAsync(face_hit, ctx->hit.p, n_triangles, cudaMemcpyDeviceToDevice, s);
