@@ -70,6 +70,17 @@ int pamo_forward_round(pamo_ctx* ctx, const float* points, const int32_t* triang
                        int32_t n_verts_undo, int32_t n_points, int32_t n_triangles, float scale, float threshold,
                        int32_t is_stuck, int32_t init, pamo_stream stream);
 
+/*
+ * One round of the legacy simplifier without rollback, _C.CUDSP().forward(points, triangles, scale,
+ * threshold, init) (simp_cuda/src/pybind.cpp:140-182, CUSimp::forward at simp_cuda/src/cusimp.cu:587-720):
+ * the same selection and collapse as pamo_forward_round with the legacy cost (the mean ring length counted
+ * twice, no skinny penalty factor), no invalid table, stuck mode, face clean-up, self-intersection check or
+ * undo. Outputs through pamo_round_sizes / pamo_round_outputs (verts, tris, verts_occ, verts_map; no undo
+ * list). Use a context of its own: the stale edge costs it keeps are those of this variant.
+ */
+int pamo_legacy_round(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                      int32_t n_triangles, float scale, float threshold, int32_t init, pamo_stream stream);
+
 /* Shapes of the five outputs of the last round: verts [n_points,3], tris [n_triangles,3],
  * verts_occ [n_points,1], verts_map [n_points,1], verts_undo [n_verts_undo] (simp_cuda/src/pybind.cpp:74-102). */
 int pamo_round_sizes(const pamo_ctx* ctx, int32_t* n_points, int32_t* n_triangles, int32_t* n_verts_undo);

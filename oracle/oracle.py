@@ -25,6 +25,7 @@ def lib():
         L.oracle_set_threads.argtypes = [P, I]
         L.oracle_forward.argtypes = [P, P, P, P, I, I, I, F, F, I, I]
         L.oracle_counts.argtypes = [P, P]
+        L.oracle_forward_legacy.argtypes = [P, P, P, I, I, F, F, I]
         L.oracle_outputs.argtypes = [P, P, P, P, P, P]
         L.oracle_collapsed.argtypes = [P, P]
         L.oracle_edge_costs.argtypes = [P, P]
@@ -93,6 +94,38 @@ class Oracle:
                 lib().oracle_destroy(self._h)
         except Exception:
             pass
+
+    def forward_legacy(self, points, triangles, scale, threshold, init):
+        """One round of the legacy CUSimp (simp_cuda/src/cusimp.cu:587-720): (verts, tris, occ, map)."""
+        pts = np.ascontiguousarray(points, np.float32)
+        tri = np.ascontiguousarray(triangles, np.int32)
+        lib().oracle_forward_legacy(self._h, _p(pts), _p(tri), len(pts), len(tri), float(scale), float(threshold),
+                                    int(bool(init)))
+        nP, nT = len(pts), len(tri)
+        verts = np.zeros((nP, 3), np.float32)
+        tris = np.zeros((nT, 3), np.int32)
+        occ = np.zeros((nP, 1), np.int32)
+        vmap = np.zeros((nP, 1), np.int32)
+        undo = np.zeros(1, np.int32)
+        lib().oracle_outputs(self._h, _p(verts), _p(tris), _p(occ), _p(vmap), _p(undo))
+        return verts, tris, occ, vmap
+
+    def run_legacy(self, points, triangles, threshold=0.001, iters=1000):
+        """PaSP.run (simp_cuda/pamo/__init__.py:197-227): (verts, faces, rounds)."""
+        v = np.ascontiguousarray(points, np.float32)
+        f = np.ascontiguousarray(triangles, np.int32)
+        ext = v.max(0) - v.min(0)
+        scale = max(max(ext[0], ext[1]), ext[2])
+        rounds = 0
+        for it in range(iters):
+            n0 = len(f)
+            verts, tris, occ, vmap = self.forward_legacy(v, f, scale, threshold, it == 0)
+            rounds = it + 1
+            v = verts[occ[:, 0].astype(bool)]
+            f = vmap[:, 0][tris[tris[:, 0] >= 0]].astype(np.int32)
+            if len(f) == n0:
+                break
+        return v, f, rounds
 
     def forward(self, points, triangles, verts_undo, n_verts_undo, scale, threshold, is_stuck, init):
         pts = np.ascontiguousarray(points, np.float32)

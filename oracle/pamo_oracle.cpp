@@ -592,6 +592,42 @@ struct Oracle {
         return f2u_sat(rclamp(tot, 0.0f, COST_RANGE) / COST_RANGE * UINT32_MAX_F);
     }
 
+    // compute_edge_cost_kernel of the legacy CUSimp (cusimp.cu:270-471): the same link condition, rings and
+    // flip test; `edge_len += edge_len + |e|/s*t` counts the mean ring length twice; no skinny penalty factor;
+    // no invalid table
+    uint32_t edge_cost_legacy(int e, float scale, float tres, bool& write) const {
+        const int u = eu[e], v = ev[e];
+        write = true;
+        int dup = 0;
+        for (int a = nt_off[u]; a < nt_off[u + 1]; ++a) {
+            int iu = next_after(tris[nt[a]], u);
+            for (int b = nt_off[v]; b < nt_off[v + 1]; ++b) {
+                int iv = next_after(tris[nt[b]], v);
+                if (iu == iv) dup++;
+                if (dup > 2) return 0xFFFFFFFFu;
+            }
+        }
+        if (dup != 2) { write = false; return 0; }
+        float len = 0.0f;
+        int cnt = 0;
+        ring_len(u, len, cnt);
+        ring_len(v, len, cnt);
+        P3 v0 = points[u], v1 = points[v];
+        len = len / (float)cnt / scale * tres;
+        len += len + vnorm(vsub(v0, v1)) / scale * tres;
+        P3 vm = vdiv(vadd(v0, v1), 2.0f);
+        float qa = 0.0f;
+        int ntri = 0;
+        if (!ring_skinny(u, v, vm, qa, ntri)) return 0xFFFFFFFFu;
+        if (!ring_skinny(v, u, vm, qa, ntri)) return 0xFFFFFFFFu;
+        Q44 Q;
+        for (int a = 0; a < 16; ++a) Q.m[a] = vq[u].m[a] + vq[v].m[a];
+        float v4[4] = {vm.x, vm.y, vm.z, 1.0f};
+        float cost = vTMv(Q, v4) / (scale * scale);
+        float tot = cost + len + qa / (float)ntri * tres;
+        return f2u_sat(rclamp(tot, 0.0f, COST_RANGE) / COST_RANGE * UINT32_MAX_F);
+    }
+
     void compute_costs(float scale, float tres, bool is_stuck) {  // cusimp_free.cu:382-585
 #pragma omp parallel for schedule(dynamic, 1024) num_threads(threads)
         for (int e = 0; e < n_edges; ++e) {
@@ -645,7 +681,7 @@ struct Oracle {
         return false;
     }
 
-    void collapse(uint32_t collapse_t) {  // collapse_edge_kernel, cusimp_free.cu:639-774
+    void collapse(uint32_t collapse_t, bool restore = true) {  // collapse_edge_kernel, cusimp_free.cu:639-774
         std::vector<uint8_t> win(n_edges, 0);
 #pragma omp parallel for schedule(dynamic, 1024) num_threads(threads)
         for (int e = 0; e < n_edges; ++e) {
@@ -671,6 +707,7 @@ struct Oracle {
             points[v] = {0, 0, 0};
             occ[v] = 0;
             rewire(u, v);
+            if (!restore) continue;  // the legacy collapse (cusimp.cu:512-585) keeps every winner
             bool sk = ring_has_skinny(u);
             if (!sk) sk = ring_has_skinny(v);
             if (sk) {
@@ -775,6 +812,51 @@ struct Oracle {
             restore_ring(u);
             restore_ring(v);
         }
+    }
+
+    // CUSimp::forward (cusimp.cu:587-720): one legacy round, no rollback; the compaction map over nP + 1 entries
+    int forward_legacy(const float* pts, const int* tris_in, int nP, int nT, float scale, float threshold, bool init) {
+        status = 0;
+        n_vertices_undo = 0;
+        const float tres = threshold;
+        const uint32_t collapse_t = f2u_sat(rclamp(threshold, 0.0f, COST_RANGE) / COST_RANGE * UINT32_MAX_F);
+        n_pts = nP;
+        n_tris = nT;
+        ensure_pts(nP);
+        points.assign((const P3*)pts, (const P3*)pts + nP);
+        occ.assign(nP + 1, 1);
+        occ[nP] = 0;
+        tris.assign((const F3*)tris_in, (const F3*)tris_in + nT);
+        if (init) {
+            std::vector<int> perm;
+            shuffle_perm((uint64_t)nT, perm);
+            std::vector<F3> t2(nT);
+            for (int r = 0; r < nT; ++r) t2[r] = tris[perm[r]];
+            tris.swap(t2);
+        }
+        orig_points = points;
+        orig_tris = tris;
+        build_csr();
+        build_edges();
+        compute_quadrics();
+        ensure_edge_cost(n_edges);
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(threads)
+        for (int e = 0; e < n_edges; ++e) {
+            bool write;
+            uint32_t c = edge_cost_legacy(e, scale, tres, write);
+            if (write) edge_cost[e] = c;
+        }
+        propagate();
+        collapse(collapse_t, false);
+        n_collapsed_total = n_collapsed_regular;
+        n_considered = 0;
+        n_undo_passes = 0;
+        int acc = 0;
+        for (int v = 0; v <= nP; ++v) {
+            pts_map[v] = acc;
+            acc += occ[v];
+        }
+        return status;
     }
 
     int forward(const float* pts, const int* tris_in, const int* verts_undo, int nU, int nP, int nT, float scale,
@@ -905,6 +987,11 @@ int oracle_set_threads(void* h, int n) {
 int oracle_forward(void* h, const float* pts, const int* tris, const int* verts_undo, int n_verts_undo, int nP, int nT,
                    float scale, float threshold, int is_stuck, int init) {
     return ((pamo_oracle_handle*)h)->o.forward(pts, tris, verts_undo, n_verts_undo, nP, nT, scale, threshold, is_stuck != 0, init != 0);
+}
+
+int oracle_forward_legacy(void* h, const float* pts, const int* tris, int nP, int nT, float scale, float threshold,
+                          int init) {
+    return ((pamo_oracle_handle*)h)->o.forward_legacy(pts, tris, nP, nT, scale, threshold, init != 0);
 }
 
 // counts[0..9] = n_pts, n_tris, n_vertices_undo, n_edges, n_collapsed_regular, n_collapsed_total, n_considered,

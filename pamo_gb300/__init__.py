@@ -1,5 +1,6 @@
 """pamo_gb300 — GB300-native (sm_103a) PaMO: stage 2 (parallel QEM edge collapse with LBVH self-intersection
-rollback) behind the reference's ``CUDSP_Free`` operator and ``PaMO.run`` API, and stage 3 (barrier/CCD
+rollback) behind the reference's ``CUDSP_Free`` operator and ``PaMO.run`` API, the legacy simplifier without
+rollback (``CUDSP``, ``PaSP``), and stage 3 (barrier/CCD
 Newton-CG safe projection, ``pamo_gb300.safe_project``).
 
 The compute path is the CUDA library ``_lib/libpamo_gb300.so`` reached through its C ABI
@@ -7,9 +8,11 @@ The compute path is the CUDA library ``_lib/libpamo_gb300.so`` reached through i
 """
 
 from .api import (  # noqa: F401
+    CUDSP,
     Context,
     CUDSP_Free,
     PaMO,
+    PaSP,
     launch_count,
     pamo_simplify,
     round_faces,
@@ -18,5 +21,5 @@ from .api import (  # noqa: F401
 )
 from ._native import PamoError  # noqa: F401
 
-__all__ = ["Context", "CUDSP_Free", "PaMO", "PamoError", "simplify", "pamo_simplify", "round_faces", "launch_count",
+__all__ = ["Context", "CUDSP", "CUDSP_Free", "PaMO", "PaSP", "PamoError", "simplify", "pamo_simplify", "round_faces", "launch_count",
            "self_intersect"]

@@ -164,6 +164,67 @@ class CUDSP_Free:
         return self._ctx.stats()
 
 
+class CUDSP:
+    """One round of the legacy simplifier without rollback per ``forward`` call (drop-in for
+    ``pamo._C.CUDSP``, simp_cuda/src/pybind.cpp:106-182; ``pamo_legacy_round`` of the C ABI)."""
+
+    def __init__(self):
+        self._ctx: Context | None = None
+
+    def _context(self, device: torch.device) -> Context:
+        if self._ctx is None or self._ctx.device != device:
+            self._ctx = Context(device)
+        return self._ctx
+
+    def forward(self, points, triangles, scale, threshold, init):
+        _check_input(points, "points", torch.float32)
+        _check_input(triangles, "triangles", torch.int32)
+        dev = points.device
+        ctx = self._context(dev)
+        lib = _native.load()
+        n_pts, n_tris = int(points.shape[0]), int(triangles.shape[0])
+        with torch.cuda.device(dev):
+            st = _stream(dev)
+            _native.check(lib.pamo_legacy_round(ctx.handle, _ptr(points), _ptr(triangles), n_pts, n_tris, float(scale),
+                                                float(threshold), int(bool(init)), st), ctx.handle)
+            verts = torch.empty((n_pts, 3), dtype=torch.float32, device=dev)
+            tris = torch.empty((n_tris, 3), dtype=torch.int32, device=dev)
+            occ = torch.empty((n_pts, 1), dtype=torch.int32, device=dev)
+            vmap = torch.empty((n_pts, 1), dtype=torch.int32, device=dev)
+            _native.check(lib.pamo_round_outputs(ctx.handle, _ptr(verts), _ptr(tris), _ptr(occ), _ptr(vmap), None, st),
+                          ctx.handle)
+        return verts, tris, occ, vmap
+
+
+class PaSP:
+    """The legacy loop ``PaSP.run`` (simp_cuda/pamo/__init__.py:181-227): rounds of ``CUDSP.forward`` with
+    compaction until a round removes no face or ``iter`` rounds ran; the scale is the largest extent of the
+    input's bounding box. Returns (verts, faces) CUDA tensors; ``iterations`` holds the rounds run."""
+
+    def __init__(self):
+        self.sp = CUDSP()
+        self.iterations = 0
+
+    def run(self, points, triangles, threshold=0.001, iter=1000):
+        verts, faces = points, triangles
+        scale = max(max(verts[:, 0].max() - verts[:, 0].min(), verts[:, 1].max() - verts[:, 1].min()),
+                    verts[:, 2].max() - verts[:, 2].min())
+        init = True
+        self.iterations = 0
+        for it in range(iter):
+            num_faces = faces.shape[0]
+            verts, faces, verts_occ, verts_map = self.sp.forward(verts.contiguous(), faces.contiguous(), float(scale),
+                                                                 threshold, init)
+            self.iterations = it + 1
+            verts = verts[verts_occ.view(-1).bool()]
+            faces = faces[faces[:, 0] >= 0]
+            faces = verts_map.view(-1)[faces.long()].to(torch.int32)
+            init = False
+            if faces.shape[0] == num_faces:
+                break
+        return verts, faces
+
+
 def _mesh_arrays(mesh):
     if isinstance(mesh, (tuple, list)) and len(mesh) == 2:
         return np.asarray(mesh[0]), np.asarray(mesh[1])

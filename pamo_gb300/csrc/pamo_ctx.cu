@@ -368,6 +368,53 @@ struct pamo_ctx {
         return PAMO_OK;
     }
 
+    // One round of the legacy simplifier CUSimp::forward (cusimp.cu:587-720): the cost without the penalty
+    // factor and with the ring length counted twice, no invalid table, stuck mode, face clean-up,
+    // self-intersection check or undo; the compaction map over n_pts + 1 entries.
+    int legacy_round(const float* pts3, const int* tris3, int nP, int nT, float threshold, int init) {
+        cudaStream_t s = stream;
+        int r;
+        if ((r = ensure_vertex_buffers(nP)) || (r = ensure_face_buffers(nT)) || (r = ensure_pts_state(nP))) return r;
+        std::memset(h_rc, 0, sizeof(RoundCounters));
+        h_rc->n_pts = nP;
+        h_rc->n_tris = nT;
+        cudaMemcpyAsync(rc, h_rc, sizeof(RoundCounters), cudaMemcpyHostToDevice, s);
+        const uint32_t collapse_t = collapse_threshold(threshold);
+        launch_load_points(pts3, nP, pos.p, orig_pos.p, occ.p, s);
+        int4* tri_src = init ? tri_in.p : tri.p;
+        launch_load_tris(tris3, nT, nP, tri_src, rc, s);
+        if (init) {
+            Feistel fb = make_feistel((unsigned long long)nT);
+            if (nT > 0) launch_shuffle_tris(fb, shuffle_flags.p, scan_scratch, tri_src, tri.p, nT, s, &rc->status);
+        }
+        cudaMemsetAsync(valence.p, 0, (nP + 1) * sizeof(int), s);
+        cudaMemsetAsync(cursor.p, 0, (nP + 1) * sizeof(int), s);
+        cudaMemsetAsync(vedges.p, 0, (nP + 1) * sizeof(int), s);
+        cudaMemsetAsync(vcursor.p, 0, (nP + 1) * sizeof(int), s);
+        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s);
+        exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
+        exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status);
+        exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
+        launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p, eorder.p, s);
+        launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
+        const int* nt_off = valence.p;
+        const int eb = 2 * nT;
+        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, pos.p, quad.p, s);
+        launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
+        cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
+        launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, invalid.p, edge_cost.p, vmin.p,
+                         d_scale, threshold, 0, s, nullptr, true);
+        launch_face_keys(rc, nT, tri.p, vmin.p, fkey.p, s);
+        launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p,
+                        orig_pos.p, occ.p, win.p, s, false);
+        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
+        if ((r = read_counters())) return r;
+        if ((r = status_to_error(h_rc->status))) return r;
+        last = *h_rc;
+        last.n_vertices_undo = 0;
+        return PAMO_OK;
+    }
+
     // Host copy of the counters (synchronises the stream).
     int read_counters() {
         int r;
@@ -701,6 +748,26 @@ int pamo_forward_round(pamo_ctx* ctx, const float* points, const int32_t* triang
     ctx->out_np = n_points;
     ctx->out_nt = n_triangles;
     ctx->out_nu = ctx->last.n_vertices_undo;
+    return PAMO_OK;
+}
+
+int pamo_legacy_round(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                      int32_t n_triangles, float scale, float threshold, int32_t init, pamo_stream stream) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (n_points < 1 || n_triangles < 1 || !points || !triangles)
+        return ctx->fail(PAMO_ERR_INVALID_ARG, "invalid sizes or null pointers");
+    cudaSetDevice(ctx->device);
+    ctx->stream = (cudaStream_t)stream;
+    ctx->have_round = false;
+    ctx->h_pinned_f[0] = scale;
+    cudaMemcpyAsync(ctx->d_scale, ctx->h_pinned_f, sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    int r = ctx->legacy_round(points, triangles, n_points, n_triangles, threshold, init);
+    if (r) return r;
+    ctx->have_round = true;
+    ctx->out_np = n_points;
+    ctx->out_nt = n_triangles;
+    ctx->out_nu = 0;
     return PAMO_OK;
 }
 

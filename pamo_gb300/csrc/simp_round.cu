@@ -259,7 +259,10 @@ __device__ __forceinline__ uint32_t f2u_sat(float f) {
     return __float2uint_rz(f);  // round toward zero, saturating like the reference's uint32_t(float) on the GPU
 }
 
-// returns false when the reference leaves the stale cost in place
+// returns false when the reference leaves the stale cost in place. kLegacy: the cost of CUSimp
+// (cusimp.cu:270-471): the mean ring length is counted twice (`edge_len += edge_len + |e|`) and the skinny term
+// has no penalty factor.
+template <bool kLegacy>
 __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restrict__ nt_off, const int* __restrict__ nt,
                                                 const int4* __restrict__ tri, const float4* __restrict__ pos,
                                                 const Quadric* __restrict__ q, float scale, float tres, uint32_t& out) {
@@ -284,7 +287,8 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
     ring_len(v, nt_off, nt, tri, pos, len, cnt);
     const V3 v0 = v3(pos[u]), v1 = v3(pos[v]);
     len = len / (float)cnt / scale * tres;
-    len = len + vnorm(vsub(v0, v1)) / scale * tres;
+    if (kLegacy) len = len + (len + vnorm(vsub(v0, v1)) / scale * tres);
+    else len = len + vnorm(vsub(v0, v1)) / scale * tres;
     const V3 vm = vdiv(vadd(v0, v1), 2.0f);
     float qa = 0.0f;
     int ntri = 0;
@@ -292,7 +296,7 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
         out = 0xFFFFFFFFu;
         return true;
     }
-    qa = 5.0f * qa;  // SKINNY_TRIANGLE_PENALTY
+    if (!kLegacy) qa = 5.0f * qa;  // SKINNY_TRIANGLE_PENALTY
     const Quadric Qu = q[u], Qv = q[v];
     const float m00 = Qu.a.x + Qv.a.x, m01 = Qu.a.y + Qv.a.y, m02 = Qu.a.z + Qv.a.z, m03 = Qu.a.w + Qv.a.w;
     const float m11 = Qu.b.x + Qv.b.x, m12 = Qu.b.y + Qv.b.y, m13 = Qu.b.z + Qv.b.z, m22 = Qu.b.w + Qv.b.w;
@@ -310,6 +314,7 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
     return true;
 }
 
+template <bool kLegacy>
 __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const int* __restrict__ eorder,
                                                   const int2* __restrict__ edges,
                                                   const int* __restrict__ nt_off, const int* __restrict__ nt,
@@ -326,13 +331,13 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
         const int u = ed.x, v = ed.y;
         uint32_t c = 0;
         bool write;
-        if (invalid[u] && invalid[v]) {
+        if (!kLegacy && invalid[u] && invalid[v]) {
             c = 0xFFFFFFFFu;
             write = true;
-        } else if (is_stuck) {
+        } else if (!kLegacy && is_stuck) {
             write = false;
         } else {
-            write = edge_cost_value(u, v, nt_off, nt, tri, pos, q, scale, tres, c);
+            write = edge_cost_value<kLegacy>(u, v, nt_off, nt, tri, pos, q, scale, tres, c);
         }
         if (write) cost[e] = c;
         else c = cost[e];  // stale value of an earlier round
@@ -416,6 +421,8 @@ __device__ __forceinline__ void restore_ring(int w, const int* __restrict__ nt_o
     }
 }
 
+// kRestore = false: CUSimp's collapse (cusimp.cu:512-585), without the skinny-ring restore
+template <bool kRestore>
 __global__ void __launch_bounds__(kT) k_collapse(RoundCounters* rc, const int* __restrict__ eorder,
                                                  const int2* __restrict__ edges,
                                                  const uint32_t* __restrict__ cost, uint32_t collapse_t,
@@ -443,8 +450,8 @@ __global__ void __launch_bounds__(kT) k_collapse(RoundCounters* rc, const int* _
                 pos[v] = make_float4(0.f, 0.f, 0.f, 0.f);
                 occ[v] = 0;
                 rewire(u, v, nt_off, nt, tri);
-                bool sk = ring_has_skinny(u, nt_off, nt, tri, pos);
-                if (!sk) sk = ring_has_skinny(v, nt_off, nt, tri, pos);
+                bool sk = kRestore && ring_has_skinny(u, nt_off, nt, tri, pos);
+                if (kRestore && !sk) sk = ring_has_skinny(v, nt_off, nt, tri, pos);
                 if (sk) {
                     occ[v] = 1;
                     pos[u] = orig_pos[u];
@@ -950,9 +957,14 @@ void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cos
 void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
                       const int* nt, const int4* tri, const float4* pos, const Quadric* q, const unsigned char* invalid,
                       uint32_t* cost, unsigned long long* vmin, const float* d_scale, float tres, int is_stuck,
-                      cudaStream_t s, const int* is_stuck_dev) {
-    k_edge_cost<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, invalid, cost,
-                                                           vmin, d_scale, tres, is_stuck, is_stuck_dev); note_launch();
+                      cudaStream_t s, const int* is_stuck_dev, bool legacy) {
+    if (legacy)
+        k_edge_cost<true><<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, invalid,
+                                                                     cost, vmin, d_scale, tres, 0, nullptr);
+    else
+        k_edge_cost<false><<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, invalid,
+                                                                      cost, vmin, d_scale, tres, is_stuck, is_stuck_dev);
+    note_launch();
 }
 void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
                       unsigned long long* fkey, cudaStream_t s) {
@@ -960,9 +972,15 @@ void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri
 }
 void launch_collapse(RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const uint32_t* cost,
                      uint32_t collapse_t, const unsigned long long* fkey, const int* nt_off, const int* nt, int4* tri,
-                     const int4* orig_tri, float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s) {
-    k_collapse<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, cost, collapse_t, fkey, nt_off, nt, tri, orig_tri,
-                                                          pos, orig_pos, occ, win); note_launch();
+                     const int4* orig_tri, float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s,
+                     bool restore) {
+    if (restore)
+        k_collapse<true><<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, cost, collapse_t, fkey, nt_off, nt,
+                                                                    tri, orig_tri, pos, orig_pos, occ, win);
+    else
+        k_collapse<false><<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, cost, collapse_t, fkey, nt_off, nt,
+                                                                     tri, orig_tri, pos, orig_pos, occ, win);
+    note_launch();
 }
 void launch_compact_winners(const RoundCounters* rc, int n_edges_bound, const int* win_scan, int* collapsed,
                             cudaStream_t s) {

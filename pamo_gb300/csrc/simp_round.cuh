@@ -41,13 +41,13 @@ void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cos
 void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
                       const int* nt, const int4* tri, const float4* pos, const Quadric* q, const unsigned char* invalid,
                       uint32_t* cost, unsigned long long* vmin, const float* d_scale, float tres, int is_stuck,
-                      cudaStream_t s,
-                      const int* is_stuck_dev = nullptr);
+                      cudaStream_t s, const int* is_stuck_dev = nullptr, bool legacy = false);
 void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
                       unsigned long long* fkey, cudaStream_t s);
 void launch_collapse(RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const uint32_t* cost,
                      uint32_t collapse_t, const unsigned long long* fkey, const int* nt_off, const int* nt, int4* tri,
-                     const int4* orig_tri, float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s);
+                     const int4* orig_tri, float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s,
+                     bool restore = true);
 void launch_compact_winners(const RoundCounters* rc, int n_edges_bound, const int* win_scan, int* collapsed,
                             cudaStream_t s);
 void launch_remove_invalid(const RoundCounters* rc, int n_tris_bound, int4* tri, cudaStream_t s);

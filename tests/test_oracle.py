@@ -114,3 +114,21 @@ def test_pair_decision_matches_reference_golden():
     for k in range(len(exp)):
         P, c, q = _slots(g["cur"][k], g["qry"][k], g["cur_ids"][k], g["qry_ids"][k])
         assert orc.pair_intersects(P, c, q, 1e-3) == bool(exp[k]), k
+
+
+def test_legacy_round_outputs_are_consistent():
+    """One legacy CUSimp round (no rollback): the map is the exclusive scan of the occupancy, removed vertices are
+    zeroed, the surviving faces reference occupied vertices, and the loop converges."""
+    v, f = meshes.sphere(10)
+    o = orc.Oracle()
+    scale = float(np.max(v.max(0) - v.min(0)))
+    verts, tris, occ, vmap = o.forward_legacy(v, f, scale, 1e-3, True)
+    occ = occ[:, 0]
+    assert np.array_equal(vmap[:, 0], np.concatenate([[0], np.cumsum(occ)[:-1]]))
+    assert occ.sum() < len(v)
+    assert np.all(verts[occ == 0] == 0)
+    live = tris[tris[:, 0] >= 0]
+    assert len(live) < len(f) and np.all(occ[live] == 1)
+    V, F, rounds = orc.Oracle().run_legacy(v, f)
+    assert 1 < rounds < 1000 and len(F) < len(f)
+    assert F.min() >= 0 and F.max() < len(V)
