@@ -237,9 +237,9 @@ int pamo_batch_rounds(const pamo_batch* b, int32_t* rounds, int32_t capacity) {
 namespace {
 
 // Device bytes a job is taken to need while it runs: the working buffers a context allocates for its sizes
-// (face and vertex arrays with the context's growth factor 1.2: about 530 B per face and 190 B per vertex,
-// rounded up to 600 and 330), its input and output copies, and 16 MiB of fixed-size scratch.
-int64_t job_bytes(int64_t nv, int64_t nf) { return 600 * nf + 330 * nv + 2 * (12 * nv + 12 * nf) + (16ll << 20); }
+// (face and vertex arrays with the context's growth factor 1.2: about 615 B per face and 195 B per vertex,
+// rounded up to 680 and 330), its input and output copies, and 16 MiB of fixed-size scratch.
+int64_t job_bytes(int64_t nv, int64_t nf) { return 680 * nf + 330 * nv + 2 * (12 * nv + 12 * nf) + (16ll << 20); }
 
 struct Request {
     int64_t id = 0;

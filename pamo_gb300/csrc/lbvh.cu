@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(256) k_leaves(const RoundCounters* rc, const i
 }
 
 __global__ void __launch_bounds__(256) k_karras(const RoundCounters* rc, const unsigned* keys, int2* child, int* iparent,
-                                                 int* lparent) {
+                                                 int* lparent, int2* range) {
     const int n = rc->n_live;
     for (int i = gtid(); i < n - 1; i += gstride()) {
         const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -220,6 +220,7 @@ __global__ void __launch_bounds__(256) k_karras(const RoundCounters* rc, const u
         } while (t > 1);
         const int gamma = i + s * d + (d < 0 ? -1 : 0);
         const int lo = min(i, j), hi = max(i, j);
+        range[i] = make_int2(lo, hi);
         int left, right;
         if (lo == gamma) {
             left = ~gamma;
@@ -240,32 +241,126 @@ __global__ void __launch_bounds__(256) k_karras(const RoundCounters* rc, const u
     }
 }
 
-__global__ void __launch_bounds__(256) k_bottom_up(RoundCounters* rc, const int2* child, const int* iparent,
-                                                    const int* lparent, const float4* llo, const float4* lhi,
-                                                    float4* nlo, float4* nhi, int* visit, const int* active = nullptr) {
+// Bottom-up boxes over tiles of kTileLeaves consecutive leaves, one thread per leaf. A Karras node covers a
+// contiguous leaf range with its own index at one end, so every node whose range lies inside a tile has its
+// index inside the tile too: those nodes count arrivals and keep their boxes in shared memory (the tile's leaf
+// boxes are staged there as well); a chain that reaches a node whose range leaves the tile continues with
+// global arrival counters (visit[], zeroed by the leaf kernels) and global boxes (nlo/nhi). The second arrival
+// at a node writes its packed record (kPack) and, with kNodes or when the node's parent may lie outside the
+// tile, its box to nlo/nhi. A node's range, children and parent are loaded together before its arrival count.
+constexpr int kTileLeaves = 512;
+constexpr int kTileThreads = kTileLeaves;
+
+template <bool kPack, bool kNodes>
+__global__ void __launch_bounds__(kTileThreads, 3) k_bottom_up_tiles(RoundCounters* rc, const int2* child,
+                                                                  const int* iparent, const int* lparent,
+                                                                  const int2* range, const float4* llo,
+                                                                  const float4* lhi, float4* nlo, float4* nhi, int* visit,
+                                                                  const int* leaf_face, const int* qscan, float4* packed,
+                                                                  int* meta_out, const int* active) {
+    __shared__ int svisit[kTileLeaves];
+    __shared__ float4 slo[kTileLeaves], shi[kTileLeaves];    // internal nodes a .. b-2
+    __shared__ float4 sllo[kTileLeaves], slhi[kTileLeaves];  // leaves a .. b-1
     if (active && *active == 0) return;
     const int n = rc->n_live;
-    for (int i = gtid(); i < n; i += gstride()) {
-        int p = lparent[i];
+    if (kPack && blockIdx.x == 0 && threadIdx.x == 0) meta_out[0] = n;
+    // tiles in a block-stride loop: the leaf count is read on the device and may exceed the launch's bound
+    for (int a = blockIdx.x * kTileLeaves; a < n; a += gridDim.x * kTileLeaves) {
+        const int b = min(a + kTileLeaves, n);  // leaves [a, b)
+        const int leaf = a + threadIdx.x;
+        __syncthreads();  // the previous tile's shared state is no longer read
+        svisit[threadIdx.x] = 0;
+        float4 blo = make_float4(0.f, 0.f, 0.f, 0.f), bhi = blo;
+        int p = -1;
+        if (leaf < b) {
+            blo = __ldcg(&llo[leaf]);
+            bhi = __ldcg(&lhi[leaf]);
+            sllo[threadIdx.x] = blo;
+            slhi[threadIdx.x] = bhi;
+            p = lparent[leaf];
+        }
+        __syncthreads();
+        int ref = ~leaf;
+        bool inside = true;  // the chain is still inside the tile
         int guard = 0;
         while (p >= 0) {
-            __threadfence();
-            if (atomicAdd(&visit[p], 1) == 0) break;
-            const int2 c = child[p];
-            float4 alo, ahi, blo, bhi;
-            if (c.x < 0) { alo = __ldcg(&llo[~c.x]); ahi = __ldcg(&lhi[~c.x]); }
-            else { alo = __ldcg(&nlo[c.x]); ahi = __ldcg(&nhi[c.x]); }
-            if (c.y < 0) { blo = __ldcg(&llo[~c.y]); bhi = __ldcg(&lhi[~c.y]); }
-            else { blo = __ldcg(&nlo[c.y]); bhi = __ldcg(&nhi[c.y]); }
-            __stcg(&nlo[p], make_float4(fminf(alo.x, blo.x), fminf(alo.y, blo.y), fminf(alo.z, blo.z), 0.f));
-            __stcg(&nhi[p], make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y), fmaxf(ahi.z, bhi.z), 0.f));
-            p = iparent[p];
             if (++guard > 4096) {
                 atomicOr(&rc->status, kErrIterLimit);
                 break;
             }
+            const int2 rg = range[p];
+            const int2 c = child[p];
+            const int pp = iparent[p];
+            const bool p_in = inside && rg.x >= a && rg.y < b;
+            if (p_in) {
+                __threadfence_block();
+                if (atomicAdd(&svisit[p - a], 1) == 0) break;
+                __threadfence_block();
+            } else {
+                // leaving the tile: the other child's chain reads this child's box from global memory
+                if (ref >= 0 && inside && !kNodes) {
+                    __stcg(&nlo[ref], blo);
+                    __stcg(&nhi[ref], bhi);
+                }
+                inside = false;
+                __threadfence();
+                if (atomicAdd(&visit[p], 1) == 0) break;
+                __threadfence();
+            }
+            float4 alo, ahi, clo, chi;
+            if (p_in) {  // both children are in this tile
+                if (c.x < 0) { alo = sllo[~c.x - a]; ahi = slhi[~c.x - a]; }
+                else { alo = slo[c.x - a]; ahi = shi[c.x - a]; }
+                if (c.y < 0) { clo = sllo[~c.y - a]; chi = slhi[~c.y - a]; }
+                else { clo = slo[c.y - a]; chi = shi[c.y - a]; }
+            } else {
+                if (c.x < 0) { alo = __ldcg(&llo[~c.x]); ahi = __ldcg(&lhi[~c.x]); }
+                else { alo = __ldcg(&nlo[c.x]); ahi = __ldcg(&nhi[c.x]); }
+                if (c.y < 0) { clo = __ldcg(&llo[~c.y]); chi = __ldcg(&lhi[~c.y]); }
+                else { clo = __ldcg(&nlo[c.y]); chi = __ldcg(&nhi[c.y]); }
+            }
+            blo = make_float4(fminf(alo.x, clo.x), fminf(alo.y, clo.y), fminf(alo.z, clo.z), 0.f);
+            bhi = make_float4(fmaxf(ahi.x, chi.x), fmaxf(ahi.y, chi.y), fmaxf(ahi.z, chi.z), 0.f);
+            if (p_in) {
+                slo[p - a] = blo;
+                shi[p - a] = bhi;
+            }
+            if (kNodes || !p_in) {
+                __stcg(&nlo[p], blo);
+                __stcg(&nhi[p], bhi);
+            }
+            if (kPack) {
+                int fa = -1, fc = -1;
+                if (c.x < 0) {
+                    fa = leaf_face[~c.x];
+                    if (qscan && fa >= 0 && qscan[fa + 1] != qscan[fa]) fa |= kQueryBit;
+                }
+                if (c.y < 0) {
+                    fc = leaf_face[~c.y];
+                    if (qscan && fc >= 0 && qscan[fc + 1] != qscan[fc]) fc |= kQueryBit;
+                }
+                float4* rec = packed + 4 * (size_t)p;
+                alo.w = __int_as_float(c.x);
+                ahi.w = __int_as_float(fa);
+                clo.w = __int_as_float(c.y);
+                chi.w = __int_as_float(fc);
+                rec[0] = alo;
+                rec[1] = ahi;
+                rec[2] = clo;
+                rec[3] = chi;
+            }
+            ref = p;
+            p = pp;
         }
     }
+}
+
+// blocks for k_bottom_up_tiles: a tile per block up to the resident count (the bound may be capped below the
+// leaf count, which the block-stride loop covers)
+inline int tile_grid(int n_bound) {
+    int g = (n_bound + kTileLeaves - 1) / kTileLeaves;
+    if (n_bound >= (1 << 19) && g < 3 * kNumSM) g = 3 * kNumSM;
+    return g < 1 ? 1 : g;
 }
 
 // ---------------------------------------------------------------- localized query
@@ -509,6 +604,7 @@ size_t bvh_bytes(int cap) {
     b += 2 * align256(4 * c);               // vals
     b += align256(4 * (256 * (size_t)kSortTiles + 1));
     b += align256(8 * c);                   // child
+    b += align256(8 * c);                   // range
     b += 2 * align256(4 * c);               // iparent, lparent
     b += 4 * align256(16 * c);              // nlo nhi llo lhi
     b += align256(4 * c);                   // visit
@@ -537,6 +633,7 @@ void bvh_carve(BvhBuffers& b, int cap, char* base, bool clear_scan_scratch) {
     b.vals[1] = (int*)take(4 * c);
     b.hist = (int*)take(4 * (256 * (size_t)kSortTiles + 1));
     b.child = (int2*)take(8 * c);
+    b.range = (int2*)take(8 * c);
     b.iparent = (int*)take(4 * c);
     b.lparent = (int*)take(4 * c);
     b.nlo = (float4*)take(16 * c);
@@ -551,44 +648,8 @@ void bvh_carve(BvhBuffers& b, int cap, char* base, bool clear_scan_scratch) {
     if (clear_scan_scratch) scan_scratch_clear(b.scan_scratch);
 }
 
-// one 64-byte record per internal node holding both children's boxes (and leaf face ids), so that a traversal
-// step reads one record instead of the child pair and two boxes from separate arrays
-__global__ void __launch_bounds__(256) k_pack_nodes(const RoundCounters* rc, const int2* __restrict__ child,
-                                                     const float4* __restrict__ nlo, const float4* __restrict__ nhi,
-                                                     const float4* __restrict__ llo, const float4* __restrict__ lhi,
-                                                     const int* __restrict__ leaf_face, const int* __restrict__ qscan,
-                                                     float4* packed, int* meta) {
-    const int n = rc->n_live;
-    if (gtid() == 0) meta[0] = n;
-    for (int i = gtid(); i < n - 1; i += gstride()) {
-        const int2 c = child[i];
-        float4 out[4];
-#pragma unroll
-        for (int side = 0; side < 2; ++side) {
-            const int x = side ? c.y : c.x;
-            float4 lo, hi;
-            int face = -1;
-            if (x < 0) {
-                lo = llo[~x];
-                hi = lhi[~x];
-                face = leaf_face[~x];
-                if (qscan && face >= 0 && qscan[face + 1] != qscan[face]) face |= kQueryBit;
-            } else {
-                lo = __ldcg(&nlo[x]);
-                hi = __ldcg(&nhi[x]);
-            }
-            lo.w = __int_as_float(x);
-            hi.w = __int_as_float(face);
-            out[2 * side] = lo;
-            out[2 * side + 1] = hi;
-        }
-#pragma unroll
-        for (int k = 0; k < 4; ++k) packed[4 * (size_t)i + k] = out[k];
-    }
-}
-
 void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s,
-               bool all_faces, const int* qscan) {
+               bool all_faces, const int* qscan, bool nodes) {
     cudaMemsetAsync(b.scene, 0xFF, 3 * sizeof(unsigned), s);
     cudaMemsetAsync(b.scene + 3, 0x00, 3 * sizeof(unsigned), s);
     const int gF = grid_for(n_tris_bound, 256);
@@ -603,9 +664,17 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
                                                          8 * pass, b.hist); note_launch();
     }
     k_leaves<<<gF, 256, 0, s>>>(rc, b.vals[0], b.box_lo, b.box_hi, b.llo, b.lhi, b.visit, b.lparent); note_launch();
-    k_karras<<<gF, 256, 0, s>>>(rc, b.keys[0], b.child, b.iparent, b.lparent); note_launch();
-    k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit); note_launch();
-    k_pack_nodes<<<gF, 256, 0, s>>>(rc, b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], qscan, b.packed, b.meta); note_launch();
+    k_karras<<<gF, 256, 0, s>>>(rc, b.keys[0], b.child, b.iparent, b.lparent, b.range); note_launch();
+    const int gT = tile_grid(n_tris_bound);
+    if (nodes)
+        k_bottom_up_tiles<true, true><<<gT, kTileThreads, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.range,
+                                                                  b.llo, b.lhi, b.nlo, b.nhi, b.visit, b.vals[0], qscan,
+                                                                  b.packed, b.meta, nullptr);
+    else
+        k_bottom_up_tiles<true, false><<<gT, kTileThreads, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.range,
+                                                                   b.llo, b.lhi, b.nlo, b.nhi, b.visit, b.vals[0], qscan,
+                                                                   b.packed, b.meta, nullptr);
+    note_launch();
 }
 
 __global__ void __launch_bounds__(256) k_refit_leaves(const RoundCounters* rc, const int4* __restrict__ tri,
@@ -626,7 +695,10 @@ void bvh_refit(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
                const int* active) {
     const int gF = grid_for(n_tris_bound, 256);
     k_refit_leaves<<<gF, 256, 0, s>>>(rc, tri, pos, b.vals[0], b.llo, b.lhi, b.visit, active); note_launch();
-    k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit, active);
+    const int gT = tile_grid(n_tris_bound);
+    k_bottom_up_tiles<false, true><<<gT, kTileThreads, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.range, b.llo,
+                                                               b.lhi, b.nlo, b.nhi, b.visit, nullptr, nullptr, nullptr,
+                                                               nullptr, active);
     note_launch();
 }
 
@@ -671,8 +743,10 @@ void bvh_refit_faces(BvhBuffers& b, const int4* tri, const float4* pos, RoundCou
     k_boxes<<<gF, 256, 0, s>>>(tri, pos, rc, b.box_lo, b.box_hi, b.live_scan, b.scene, 1); note_launch();
     k_reuse_leaves<<<gF, 256, 0, s>>>(rc, tri, b.box_lo, b.box_hi, next_round ? (const int*)b.keys[1] : nullptr,
                                       b.vals[0], b.llo, b.lhi, b.visit, b.meta); note_launch();
-    k_bottom_up<<<gF, 256, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit); note_launch();
-    k_pack_nodes<<<gF, 256, 0, s>>>(rc, b.child, b.nlo, b.nhi, b.llo, b.lhi, b.vals[0], qscan, b.packed, b.meta); note_launch();
+    k_bottom_up_tiles<true, false><<<tile_grid(n_tris_bound), kTileThreads, 0, s>>>(
+        rc, b.child, b.iparent, b.lparent, b.range, b.llo, b.lhi, b.nlo, b.nhi, b.visit, b.vals[0], qscan,
+        b.packed, b.meta, nullptr);
+    note_launch();
 }
 
 void bvh_remap(BvhBuffers& b, const int* fscan, int n_tris_bound, cudaStream_t s) {

@@ -15,6 +15,7 @@ struct BvhBuffers {
     int* vals[2] = {nullptr, nullptr};       // face ids, sort ping-pong
     int* hist = nullptr;               // radix histograms [256 * kSortTiles + 1]
     int2* child = nullptr;             // internal node children; v < 0 encodes leaf ~v
+    int2* range = nullptr;             // internal node leaf range [lo, hi] (the node index is one end)
     int* iparent = nullptr;            // parent of internal node
     int* lparent = nullptr;            // parent of leaf
     float4* nlo = nullptr;             // internal node boxes
@@ -39,8 +40,10 @@ void bvh_carve(BvhBuffers& b, int cap, char* base, bool clear_scan_scratch = tru
 // every face slot below rc->n_tris is a leaf and a removed face has an empty box, so that the tree can be
 // refitted after faces are removed or restored (bvh_refit_faces) and carried to the next round (bvh_remap).
 // qscan (exclusive scan of the query flags, or null) marks the query faces in the packed leaves for bvh_query.
+// nodes: also keep the internal node boxes nlo/nhi for every node (the traversals of the projection stage read
+// them); the packed records that bvh_query reads are always written.
 void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s,
-               bool all_faces = false, const int* qscan = nullptr);
+               bool all_faces = false, const int* qscan = nullptr, bool nodes = true);
 
 // New boxes for the leaves of a tree built with all_faces (a removed face, or a leaf whose face is gone, gets an
 // empty box that overlaps nothing); sets rc->n_live to the tree's leaf count. next_round: first take the leaf

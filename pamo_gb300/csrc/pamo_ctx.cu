@@ -123,6 +123,8 @@ struct pamo_ctx {
     // ---- per-face ----
     DevBuf<int4> tri, orig_tri, tri_in, tri_out;
     DevBuf<int> ecount, qflag, qlist, fflags, nt, shuffle_flags;
+    DevBuf<int> nxt;        // per CSR slot: the vertex after the ring's vertex in the slot's face
+    DevBuf<float4> fgeo;    // per face: edge lengths, unnormalised normal, plane (three float4)
     DevBuf<unsigned long long> fkey;
     DevBuf<unsigned char> hit;
     BvhBuffers bvh;
@@ -248,7 +250,7 @@ struct pamo_ctx {
         };
         fr(edge_cost); fr(invalid); fr(pts_map); fr(pts_map_prev); fr(undo_list); fr(tmp_undo);
         fr(pos); fr(orig_pos); fr(pos_in); fr(pos_out); fr(occ); fr(valence); fr(cursor); fr(quad); fr(vmin); fr(undo_in);
-        fr(tri); fr(orig_tri); fr(tri_in); fr(tri_out); fr(ecount); fr(qflag); fr(qlist); fr(fflags); fr(nt);
+        fr(nxt); fr(fgeo); fr(tri); fr(orig_tri); fr(tri_in); fr(tri_out); fr(ecount); fr(qflag); fr(qlist); fr(fflags); fr(nt);
         fr(shuffle_flags); fr(fkey); fr(eorder); fr(vedges); fr(vcursor); fr(hit); fr(edges); fr(win); fr(collapsed); fr(uflag); fr(face_mean); fr(exact_list);
         if (bvh_mem) cudaFree(bvh_mem);
         bvh_mem = nullptr;
@@ -313,6 +315,7 @@ struct pamo_ctx {
         size_t b = 0;
         b += pos.bytes() + orig_pos.bytes() + pos_in.bytes() + pos_out.bytes() + occ.bytes() + valence.bytes() +
              cursor.bytes() + vedges.bytes() + vcursor.bytes() + quad.bytes() + vmin.bytes() + undo_in.bytes();
+        b += nxt.bytes() + fgeo.bytes();
         b += tri.bytes() + orig_tri.bytes() + tri_in.bytes() + tri_out.bytes() + ecount.bytes() + qflag.bytes() +
              qlist.bytes() + fflags.bytes() + nt.bytes() + shuffle_flags.bytes() + fkey.bytes() + hit.bytes() +
              edges.bytes() + win.bytes() + collapsed.bytes() + uflag.bytes() + eorder.bytes() + exact_list.bytes() +
@@ -344,7 +347,7 @@ struct pamo_ctx {
         int r;
         if ((r = grow(tri, nc)) || (r = grow(orig_tri, nc)) || (r = grow(tri_in, nc)) || (r = grow(tri_out, nc)) ||
             (r = grow(ecount, nc + 1)) || (r = grow(qflag, nc + 1)) || (r = grow(qlist, nc)) || (r = grow(fflags, nc + 1)) ||
-            (r = grow(nt, 3 * nc)) || (r = grow(shuffle_flags, 2 * nc + 40)) || (r = grow(fkey, nc)) || (r = grow(hit, nc)) ||
+            (r = grow(nt, 3 * nc)) || (r = grow(nxt, 3 * nc)) || (r = grow(fgeo, 3 * nc)) || (r = grow(shuffle_flags, 2 * nc + 40)) || (r = grow(fkey, nc)) || (r = grow(hit, nc)) ||
             (r = grow(eorder, 2 * nc)) ||
             (r = grow(edges, 2 * nc)) || (r = grow(win, 2 * nc + 1)) || (r = grow(collapsed, 2 * nc)) ||
             (r = grow(uflag, 2 * nc + 1)) || (r = grow(face_mean, 3 * nc)) ||
@@ -391,7 +394,7 @@ struct pamo_ctx {
         cudaMemsetAsync(cursor.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(vedges.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(vcursor.p, 0, (nP + 1) * sizeof(int), s);
-        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s);
+        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
         exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
         exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status);
         exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
@@ -399,10 +402,10 @@ struct pamo_ctx {
         launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
         const int* nt_off = valence.p;
         const int eb = 2 * nT;
-        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, pos.p, quad.p, s);
+        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s);
         launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
         cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
-        launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, invalid.p, edge_cost.p, vmin.p,
+        launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p, vmin.p,
                          d_scale, threshold, 0, s, nullptr, true);
         launch_face_keys(rc, nT, tri.p, vmin.p, fkey.p, s);
         launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p,
@@ -447,17 +450,17 @@ struct pamo_ctx {
             launch_copy_tris_dev(tri_in.p, tri.p, rc, nTb, s);
             launch_copy_tris_dev(tri.p, orig_tri.p, rc, nTb, s);
             launch_zero_vertex_counts_dev(rc, nPb, valence.p, cursor.p, vedges.p, vcursor.p, s);
-            launch_face_counts(tri.p, rc, nTb, valence.p, ecount.p, vedges.p, s);
+            launch_face_counts(tri.p, rc, nTb, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
             exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
             exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status);
             exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
             launch_fill_adjacency(tri.p, rc, nTb, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p,
                                   eorder.p, s);
             launch_sort_adjacency(rc, nPb, valence.p, nt.p, s);
-            launch_quadrics(rc, nPb, nt_off, nt.p, tri.p, pos.p, quad.p, s);
+            launch_quadrics(rc, nPb, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s);
             launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
             launch_fill_u64_dev(rc, nPb, vmin.p, ~0ull, s);
-            launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, invalid.p, edge_cost.p,
+            launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p,
                              vmin.p, d_scale, threshold, 0, s, &d_ls->is_stuck);
             launch_face_keys(rc, nTb, tri.p, vmin.p, fkey.p, s);
             launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p,
@@ -477,7 +480,7 @@ struct pamo_ctx {
         }
         // intersection check; the LBVH spans every face slot of the round and is refitted when reused
         launch_zero_face_bytes_dev(rc, nTb, hit.p, s);
-        if (kind == 0) bvh_build(bvh, tri.p, pos.p, rc, nTb, s, true, qflag.p);
+        if (kind == 0) bvh_build(bvh, tri.p, pos.p, rc, nTb, s, true, qflag.p, false);
         else bvh_refit_faces(bvh, tri.p, pos.p, rc, nTb, s, kind == 2, qflag.p);
         bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, pair_cap(), rc, nTb, kTriEps, s);
         launch_undo_check(rc, eb, collapsed.p, edges.p, nt_off, nt.p, hit.p, uflag.p, s);
@@ -588,7 +591,7 @@ struct pamo_ctx {
         cudaMemsetAsync(cursor.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(vedges.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(vcursor.p, 0, (nP + 1) * sizeof(int), s);
-        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s);
+        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
         exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
         exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status);
         exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
@@ -600,12 +603,12 @@ struct pamo_ctx {
 
         // cost and selection
         prof.begin(kPhQuad, s);
-        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, pos.p, quad.p, s);
+        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s);
         prof.end(kPhQuad, s);
         launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
         cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
         prof.begin(kPhCost, s);
-        launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, invalid.p, edge_cost.p, vmin.p,
+        launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p, vmin.p,
                          d_scale, threshold, is_stuck, s);
         prof.end(kPhCost, s);
         prof.begin(kPhCollapse, s);
@@ -631,7 +634,7 @@ struct pamo_ctx {
         auto check_pass = [&]() {
             cudaMemsetAsync(hit.p, 0, nT + 1, s);
             prof.begin(kPhBvh, s);
-            bvh_build(bvh, tri.p, pos.p, rc, nT, s, false, qflag.p);
+            bvh_build(bvh, tri.p, pos.p, rc, nT, s, false, qflag.p, false);
             prof.end(kPhBvh, s);
             prof.begin(kPhQuery, s);
             bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, pair_cap(), rc, nT, kTriEps, s);
@@ -1053,7 +1056,7 @@ int pamo_self_intersect(pamo_ctx* ctx, const float* points, const int32_t* trian
     exclusive_scan(ctx->qflag.p, ctx->qflag.p, &ctx->rc->n_tris, 1, &ctx->rc->n_query, ctx->scan_scratch, s, &ctx->rc->status);
     launch_compact_flags(ctx->qflag.p, n_triangles, &ctx->rc->n_tris, ctx->qlist.p, s);
     cudaMemsetAsync(ctx->hit.p, 0, n_triangles + 1, s);
-    bvh_build(ctx->bvh, ctx->tri.p, ctx->pos.p, ctx->rc, n_triangles, s, false, ctx->qflag.p);
+    bvh_build(ctx->bvh, ctx->tri.p, ctx->pos.p, ctx->rc, n_triangles, s, false, ctx->qflag.p, false);
     bvh_query(ctx->bvh, ctx->tri.p, ctx->pos.p, ctx->qlist.p, ctx->qflag.p, ctx->hit.p, ctx->exact_list.p,
               ctx->pair_cap(), ctx->rc, n_triangles, kTriEps, s);
     cudaMemcpyAsync(face_hit, ctx->hit.p, n_triangles, cudaMemcpyDeviceToDevice, s);

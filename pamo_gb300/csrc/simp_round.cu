@@ -102,14 +102,34 @@ __global__ void k_shuffle_gather(Feistel fb, const int* __restrict__ scan, const
 }
 
 // ------------------------------------------------------------------ adjacency
+// Per-face values that the vertex rings read many times (every face lies in three rings and every ring is
+// read once per incident edge), each computed by the same operations as where the reference computes it:
+//   fgeo[3f]     = |p_x - p_y|, |p_y - p_z|, |p_z - p_x| and, as int bits, which of t.x > t.y, t.y > t.z,
+//                  t.z > t.x hold (the ring edge-length terms, :449-484);
+//   fgeo[3f + 1] = the unnormalised normal cross(p_y - p_x, p_z - p_x) and its L1 norm (the flip test);
+//   fgeo[3f + 2] = the face plane of tri2plane (:337-346).
+__device__ __forceinline__ void face_plane(const float4* __restrict__ pos, int4 t, float p[4]);
+
 __global__ void __launch_bounds__(kT) k_face_counts(const int4* __restrict__ tri, const RoundCounters* rc, int* valence,
-                                                    int* ecount, int* vedges) {
+                                                    int* ecount, int* vedges, const float4* __restrict__ pos,
+                                                    float4* fgeo) {
     const int n = rc->n_tris;
     for (int f = gtid(); f < n; f += gstride()) {
         const int4 t = tri[f];
         if (face_killed(t)) {
             ecount[f] = 0;
             continue;
+        }
+        if (fgeo) {
+            const V3 o0 = v3(pos[t.x]), o1 = v3(pos[t.y]), o2 = v3(pos[t.z]);
+            const int mask = (t.x > t.y ? 1 : 0) | (t.y > t.z ? 2 : 0) | (t.z > t.x ? 4 : 0);
+            fgeo[3 * (size_t)f] = make_float4(vnorm(vsub(o0, o1)), vnorm(vsub(o1, o2)), vnorm(vsub(o2, o0)),
+                                              __int_as_float(mask));
+            const V3 ou = vcross(vsub(o1, o0), vsub(o2, o0));
+            fgeo[3 * (size_t)f + 1] = make_float4(ou.x, ou.y, ou.z, fabsf(ou.x) + fabsf(ou.y) + fabsf(ou.z));
+            float pl[4];
+            face_plane(pos, t, pl);
+            fgeo[3 * (size_t)f + 2] = make_float4(pl[0], pl[1], pl[2], pl[3]);
         }
         atomicAdd(&valence[t.x], 1);
         atomicAdd(&valence[t.y], 1);
@@ -177,16 +197,22 @@ __device__ __forceinline__ void face_plane(const float4* __restrict__ pos, int4 
     p[3] = -vdot(n, v0);
 }
 
+__device__ __forceinline__ int next_after(int4 t, int v);
+
+// Quadrics from the face planes of fgeo; also nxt[s] = the vertex after v in ring face s (the link condition's
+// per-slot value).
 __global__ void __launch_bounds__(kT) k_quadrics(const RoundCounters* rc, const int* __restrict__ nt_off,
                                                  const int* __restrict__ nt, const int4* __restrict__ tri,
-                                                 const float4* __restrict__ pos, Quadric* q) {
+                                                 const float4* __restrict__ fgeo, Quadric* q, int* nxt) {
     const int n = rc->n_pts;
     for (int v = gtid(); v < n; v += gstride()) {
         float m00 = 0.f, m01 = 0.f, m02 = 0.f, m03 = 0.f, m11 = 0.f, m12 = 0.f, m13 = 0.f, m22 = 0.f, m23 = 0.f, m33 = 0.f;
         const int b = nt_off[v + 1];
         for (int s = nt_off[v]; s < b; ++s) {
-            float p[4];
-            face_plane(pos, tri[nt[s]], p);
+            const int f = nt[s];
+            nxt[s] = next_after(tri[f], v);
+            const float4 pl = fgeo[3 * (size_t)f + 2];
+            const float p[4] = {pl.x, pl.y, pl.z, pl.w};
             m00 += p[0] * p[0]; m01 += p[0] * p[1]; m02 += p[0] * p[2]; m03 += p[0] * p[3];
             m11 += p[1] * p[1]; m12 += p[1] * p[2]; m13 += p[1] * p[3];
             m22 += p[2] * p[2]; m23 += p[2] * p[3];
@@ -210,13 +236,14 @@ __device__ __forceinline__ int next_after(int4 t, int v) {
 
 
 __device__ __forceinline__ void ring_len(int w, const int* __restrict__ nt_off, const int* __restrict__ nt,
-                                         const int4* __restrict__ tri, const float4* __restrict__ pos, float& len, int& cnt) {
+                                         const float4* __restrict__ fgeo, float& len, int& cnt) {
     const int b = nt_off[w + 1];
     for (int s = nt_off[w]; s < b; ++s) {
-        const int4 t = tri[nt[s]];
-        if (t.x > t.y) { len += vnorm(vsub(v3(pos[t.x]), v3(pos[t.y]))); cnt++; }
-        if (t.y > t.z) { len += vnorm(vsub(v3(pos[t.y]), v3(pos[t.z]))); cnt++; }
-        if (t.z > t.x) { len += vnorm(vsub(v3(pos[t.z]), v3(pos[t.x]))); cnt++; }
+        const float4 g = fgeo[3 * (size_t)nt[s]];
+        const int mask = __float_as_int(g.w);
+        if (mask & 1) { len += g.x; cnt++; }
+        if (mask & 2) { len += g.y; cnt++; }
+        if (mask & 4) { len += g.z; cnt++; }
     }
 }
 
@@ -226,25 +253,32 @@ __device__ __forceinline__ void ring_len(int w, const int* __restrict__ nt_off, 
 // normalised form); otherwise the normalised form is evaluated exactly as the reference does.
 __device__ __forceinline__ bool ring_skinny(int w, int other, V3 vm, const int* __restrict__ nt_off,
                                             const int* __restrict__ nt, const int4* __restrict__ tri,
-                                            const float4* __restrict__ pos, float& qa, int& ntri) {
+                                            const float4* __restrict__ pos, const float4* __restrict__ fgeo, float& qa,
+                                            int& ntri) {
     const float k4s3 = 4.0f * sqrtf(3.0f);
     const int b = nt_off[w + 1];
     for (int s = nt_off[w]; s < b; ++s) {
-        const int4 t = tri[nt[s]];
+        const int f = nt[s];
+        const int4 t = tri[f];
         if (t.x == other || t.y == other || t.z == other) continue;
-        const V3 o0 = v3(pos[t.x]), o1 = v3(pos[t.y]), o2 = v3(pos[t.z]);
-        const V3 n0 = (t.x == w) ? vm : o0, n1 = (t.y == w) ? vm : o1, n2 = (t.z == w) ? vm : o2;
-        const V3 ou = vcross(vsub(o1, o0), vsub(o2, o0));
+        const bool wx = t.x == w, wy = t.y == w, wz = t.z == w;
+        const V3 n0 = wx ? vm : v3(pos[t.x]), n1 = wy ? vm : v3(pos[t.y]), n2 = wz ? vm : v3(pos[t.z]);
+        const float4 og = fgeo[3 * (size_t)f + 1];
+        const V3 ou = {og.x, og.y, og.z};
         const V3 nu = vcross(vsub(n1, n0), vsub(n2, n0));
         const float du = vdot(ou, nu);
-        const float bound = 1e-5f * (fabsf(ou.x) + fabsf(ou.y) + fabsf(ou.z)) * (fabsf(nu.x) + fabsf(nu.y) + fabsf(nu.z));
+        const float bound = 1e-5f * og.w * (fabsf(nu.x) + fabsf(nu.y) + fabsf(nu.z));
         if (du < -bound) return false;
         if (!(du > bound)) {
             const V3 on = vdiv(ou, vnorm(ou));
             const V3 nn = vdiv(nu, vnorm(nu));
             if (vdot(on, nn) < 0) return false;
         }
-        const float l01 = vnorm(vsub(n0, n1)), l12 = vnorm(vsub(n1, n2)), l20 = vnorm(vsub(n2, n0));
+        // an edge without w keeps its length (same operations as the per-face value)
+        const float4 lg = fgeo[3 * (size_t)f];
+        const float l01 = (wx || wy) ? vnorm(vsub(n0, n1)) : lg.x;
+        const float l12 = (wy || wz) ? vnorm(vsub(n1, n2)) : lg.y;
+        const float l20 = (wz || wx) ? vnorm(vsub(n2, n0)) : lg.z;
         const float sh = (l01 + l12 + l20) / 2;  // triangle_area (Heron), :368-375
         const float area = sqrtf(sh * (sh - l01) * (sh - l12) * (sh - l20));
         // the reference's operator precedence: only the first squared length divides (pow(x, 2) == x * x)
@@ -265,14 +299,15 @@ __device__ __forceinline__ uint32_t f2u_sat(float f) {
 template <bool kLegacy>
 __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restrict__ nt_off, const int* __restrict__ nt,
                                                 const int4* __restrict__ tri, const float4* __restrict__ pos,
-                                                const Quadric* __restrict__ q, float scale, float tres, uint32_t& out) {
+                                                const Quadric* __restrict__ q, const float4* __restrict__ fgeo,
+                                                const int* __restrict__ nxt, float scale, float tres, uint32_t& out) {
     // link condition
     int dup = 0;
     const int ua = nt_off[u], ub = nt_off[u + 1], va = nt_off[v], vb = nt_off[v + 1];
     for (int a = ua; a < ub; ++a) {
-        const int iu = next_after(tri[nt[a]], u);
+        const int iu = nxt[a];
         for (int b = va; b < vb; ++b) {
-            const int iv = next_after(tri[nt[b]], v);
+            const int iv = nxt[b];
             if (iu == iv) dup++;
             if (dup > 2) {
                 out = 0xFFFFFFFFu;
@@ -283,8 +318,8 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
     if (dup != 2) return false;
     float len = 0.0f;
     int cnt = 0;
-    ring_len(u, nt_off, nt, tri, pos, len, cnt);
-    ring_len(v, nt_off, nt, tri, pos, len, cnt);
+    ring_len(u, nt_off, nt, fgeo, len, cnt);
+    ring_len(v, nt_off, nt, fgeo, len, cnt);
     const V3 v0 = v3(pos[u]), v1 = v3(pos[v]);
     len = len / (float)cnt / scale * tres;
     if (kLegacy) len = len + (len + vnorm(vsub(v0, v1)) / scale * tres);
@@ -292,7 +327,8 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
     const V3 vm = vdiv(vadd(v0, v1), 2.0f);
     float qa = 0.0f;
     int ntri = 0;
-    if (!ring_skinny(u, v, vm, nt_off, nt, tri, pos, qa, ntri) || !ring_skinny(v, u, vm, nt_off, nt, tri, pos, qa, ntri)) {
+    if (!ring_skinny(u, v, vm, nt_off, nt, tri, pos, fgeo, qa, ntri) ||
+        !ring_skinny(v, u, vm, nt_off, nt, tri, pos, fgeo, qa, ntri)) {
         out = 0xFFFFFFFFu;
         return true;
     }
@@ -319,7 +355,8 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
                                                   const int2* __restrict__ edges,
                                                   const int* __restrict__ nt_off, const int* __restrict__ nt,
                                                   const int4* __restrict__ tri, const float4* __restrict__ pos,
-                                                  const Quadric* __restrict__ q, const unsigned char* __restrict__ invalid,
+                                                  const Quadric* __restrict__ q, const float4* __restrict__ fgeo,
+                                                  const int* __restrict__ nxt, const unsigned char* __restrict__ invalid,
                                                   uint32_t* cost, unsigned long long* vmin, const float* d_scale,
                                                   float tres, int is_stuck_host, const int* is_stuck_dev) {
     const int is_stuck = is_stuck_dev ? *is_stuck_dev : is_stuck_host;
@@ -337,7 +374,7 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
         } else if (!kLegacy && is_stuck) {
             write = false;
         } else {
-            write = edge_cost_value<kLegacy>(u, v, nt_off, nt, tri, pos, q, scale, tres, c);
+            write = edge_cost_value<kLegacy>(u, v, nt_off, nt, tri, pos, q, fgeo, nxt, scale, tres, c);
         }
         if (write) cost[e] = c;
         else c = cost[e];  // stale value of an earlier round
@@ -933,8 +970,8 @@ void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4*
 }
 
 void launch_face_counts(const int4* tri, const RoundCounters* rc, int n_tris_bound, int* valence, int* ecount,
-                        int* vedges, cudaStream_t s) {
-    k_face_counts<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, valence, ecount, vedges); note_launch();
+                        int* vedges, cudaStream_t s, const float4* pos, float4* fgeo) {
+    k_face_counts<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, valence, ecount, vedges, pos, fgeo); note_launch();
 }
 void launch_fill_adjacency(const int4* tri, const RoundCounters* rc, int n_tris_bound, const int* nt_off, int* cursor,
                            int* nt, const int* edge_off, int2* edges, const int* voff, int* vcursor, int* eorder,
@@ -947,22 +984,23 @@ void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* 
     k_sort_adjacency<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt); note_launch();
 }
 void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
-                     const float4* pos, Quadric* q, cudaStream_t s) {
-    k_quadrics<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, pos, q); note_launch();
+                     const float4* fgeo, Quadric* q, int* nxt, cudaStream_t s) {
+    k_quadrics<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, fgeo, q, nxt); note_launch();
 }
 void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s) {
     k_edge_cost_capacity<<<1, 1, 0, s>>>(rc, d_cap); note_launch();
     k_edge_cost_zero<<<grid_for(phys_len, kT), kT, 0, s>>>(rc, edge_cost, phys_len); note_launch();
 }
 void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
-                      const int* nt, const int4* tri, const float4* pos, const Quadric* q, const unsigned char* invalid,
-                      uint32_t* cost, unsigned long long* vmin, const float* d_scale, float tres, int is_stuck,
-                      cudaStream_t s, const int* is_stuck_dev, bool legacy) {
+                      const int* nt, const int4* tri, const float4* pos, const Quadric* q, const float4* fgeo,
+                      const int* nxt, const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin,
+                      const float* d_scale, float tres, int is_stuck, cudaStream_t s, const int* is_stuck_dev, bool legacy) {
     if (legacy)
-        k_edge_cost<true><<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, invalid,
-                                                                     cost, vmin, d_scale, tres, 0, nullptr);
+        k_edge_cost<true><<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt,
+                                                                     invalid, cost, vmin, d_scale, tres, 0, nullptr);
     else
-        k_edge_cost<false><<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, invalid,
+        k_edge_cost<false><<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt,
+                                                                      invalid,
                                                                       cost, vmin, d_scale, tres, is_stuck, is_stuck_dev);
     note_launch();
 }

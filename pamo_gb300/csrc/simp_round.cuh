@@ -27,8 +27,9 @@ void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4*
 void launch_copy_tris(const int4* src, int4* dst, int n, cudaStream_t s);
 
 // ---- adjacency ----
+// with fgeo: also the per-face geometry the rings read (three float4 per face, from pos)
 void launch_face_counts(const int4* tri, const RoundCounters* rc, int n_tris_bound, int* valence, int* ecount,
-                        int* vedges, cudaStream_t s);
+                        int* vedges, cudaStream_t s, const float4* pos = nullptr, float4* fgeo = nullptr);
 void launch_fill_adjacency(const int4* tri, const RoundCounters* rc, int n_tris_bound, const int* nt_off, int* cursor,
                            int* nt, const int* edge_off, int2* edges, const int* voff, int* vcursor, int* eorder,
                            cudaStream_t s);
@@ -36,12 +37,13 @@ void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* 
 
 // ---- cost, selection, collapse ----
 void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
-                     const float4* pos, Quadric* q, cudaStream_t s);
+                     const float4* fgeo, Quadric* q, int* nxt, cudaStream_t s);
 void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s);
 void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
-                      const int* nt, const int4* tri, const float4* pos, const Quadric* q, const unsigned char* invalid,
-                      uint32_t* cost, unsigned long long* vmin, const float* d_scale, float tres, int is_stuck,
-                      cudaStream_t s, const int* is_stuck_dev = nullptr, bool legacy = false);
+                      const int* nt, const int4* tri, const float4* pos, const Quadric* q, const float4* fgeo,
+                      const int* nxt, const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin,
+                      const float* d_scale, float tres, int is_stuck, cudaStream_t s, const int* is_stuck_dev = nullptr,
+                      bool legacy = false);
 void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
                       unsigned long long* fkey, cudaStream_t s);
 void launch_collapse(RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const uint32_t* cost,
