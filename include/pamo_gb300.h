@@ -126,6 +126,15 @@ int pamo_simplify_round_faces(const pamo_ctx* ctx, int32_t* faces_per_round, int
 int pamo_simplify_round_ms(const pamo_ctx* ctx, double* ms, int32_t capacity);
 
 /*
+ * The centre PaMO.run subtracts before simplifying: preprocess_mesh's tris_mean (simp_cuda/pamo/__init__.py:
+ * 60-64), numpy float32 semantics: per face ((a + b) + c) / 3, then the sequential float32 sum over faces in
+ * face order divided by the face count. Device points/triangles; out3 is a host array of 3 floats.
+ * Synchronises `stream`.
+ */
+int pamo_tris_mean(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                   int32_t n_triangles, float* out3, pamo_stream stream);
+
+/*
  * The reference's self-intersection check over a whole mesh (selfx::self_intersect,
  * simp_cuda/src/bvh/self_intersect.cuh:151-392): face_hit[f] = 1 iff face f takes part in a (query, hit)
  * pair the reference's tri-tri filter reports, else 0 (uint8, device buffer of n_triangles). Faces equal

@@ -18,8 +18,9 @@ from .api import (  # noqa: F401
     round_faces,
     self_intersect,
     simplify,
+    tris_mean,
 )
 from ._native import PamoError  # noqa: F401
 
 __all__ = ["Context", "CUDSP", "CUDSP_Free", "PaMO", "PaSP", "PamoError", "simplify", "pamo_simplify", "round_faces", "launch_count",
-           "self_intersect"]
+           "self_intersect", "tris_mean"]

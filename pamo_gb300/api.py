@@ -290,6 +290,24 @@ def self_intersect(points: torch.Tensor, triangles: torch.Tensor, ctx: Context |
     return out
 
 
+def tris_mean(points: torch.Tensor, triangles: torch.Tensor, ctx: Context | None = None) -> np.ndarray:
+    """The centre ``PaMO.run`` subtracts (preprocess_mesh's ``tris_mean``, simp_cuda/pamo/__init__.py:60-64) with
+    numpy float32 semantics, computed on the GPU: float32 [3]."""
+    _check_input(points, "points", torch.float32)
+    _check_input(triangles, "triangles", torch.int32)
+    dev = points.device
+    if ctx is None:
+        ctx = Context(dev)
+    out = np.zeros(3, np.float32)
+    with torch.cuda.device(dev):
+        _native.check(
+            _native.load().pamo_tris_mean(ctx.handle, _ptr(points), _ptr(triangles), int(points.shape[0]),
+                                          int(triangles.shape[0]), out.ctypes.data, _stream(dev)),
+            ctx.handle,
+        )
+    return out
+
+
 def launch_count() -> int:
     """Kernels launched by the CUDA library since it was loaded."""
     return int(_native.load().pamo_launch_count())

@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(256) k_morton(const RoundCounters* rc, const i
 
 // ---------------------------------------------------------------- stable LSD radix sort
 __device__ __forceinline__ void sort_chunk(int n, int& lo, int& hi) {
-    long long chunk = ((long long)n + kSortTiles - 1) / kSortTiles;
+    long long chunk = ((long long)n + gridDim.x - 1) / gridDim.x;
     chunk = (chunk + kSortThreads - 1) / kSortThreads * kSortThreads;
     long long a = chunk * blockIdx.x, b = a + chunk;
     lo = (int)(a < n ? a : n);
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kSortThreads) k_rs_hist(const unsigned* __rest
     sort_chunk(*d_n, lo, hi);
     for (int i = lo + threadIdx.x; i < hi; i += kSortThreads) atomicAdd(&h[(keys[i] >> shift) & 0xFF], 1);
     __syncthreads();
-    hist[threadIdx.x * kSortTiles + blockIdx.x] = h[threadIdx.x];
+    hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
 }
 
 // Each tile of 256 keys is ranked stably: lanes of a warp with the same digit find each other with
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kSortThreads) k_rs_scatter(const unsigned* __r
     __shared__ int wcnt[W][256];
     __shared__ int tot[256];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    base[threadIdx.x] = hist[threadIdx.x * kSortTiles + blockIdx.x];
+    base[threadIdx.x] = hist[threadIdx.x * gridDim.x + blockIdx.x];
     for (int w = 0; w < W; ++w) wcnt[w][threadIdx.x] = 0;
     __syncthreads();
     int lo, hi;
@@ -654,13 +654,18 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
     cudaMemsetAsync(b.scene + 3, 0x00, 3 * sizeof(unsigned), s);
     const int gF = grid_for(n_tris_bound, 256);
     k_boxes<<<gF, 256, 0, s>>>(tri, pos, rc, b.box_lo, b.box_hi, b.live_scan, b.scene, all_faces ? 1 : 0); note_launch();
-    exclusive_scan(b.live_scan, b.live_scan, &rc->n_tris, 1, &rc->n_live, b.scan_scratch, s, &rc->status);
+    exclusive_scan(b.live_scan, b.live_scan, &rc->n_tris, 1, &rc->n_live, b.scan_scratch, s, &rc->status, n_tris_bound);
     k_morton<<<gF, 256, 0, s>>>(rc, b.live_scan, b.box_lo, b.box_hi, b.scene, b.keys[0], b.vals[0]); note_launch();
+    // sort tiles from the launch's bound (about 2048 keys per tile; all kSortTiles from 2^19 on, where callers
+    // cap their bounds); the histogram is
+    // digit-major over the tiles, so its scan gives each tile's output offset per digit
+    long long st = n_tris_bound >= (1 << 19) ? kSortTiles : ((long long)n_tris_bound + 2047) / 2048;
+    const int sort_tiles = (int)(st < 1 ? 1 : (st > kSortTiles ? kSortTiles : st));
     for (int pass = 0; pass < 4; ++pass) {
         const int in = pass & 1, out = in ^ 1;
-        k_rs_hist<<<kSortTiles, kSortThreads, 0, s>>>(b.keys[in], &rc->n_live, 8 * pass, b.hist); note_launch();
-        exclusive_scan(b.hist, b.hist, nullptr, 256 * kSortTiles, nullptr, b.scan_scratch, s, &rc->status);
-        k_rs_scatter<<<kSortTiles, kSortThreads, 0, s>>>(b.keys[in], b.vals[in], b.keys[out], b.vals[out], &rc->n_live,
+        k_rs_hist<<<sort_tiles, kSortThreads, 0, s>>>(b.keys[in], &rc->n_live, 8 * pass, b.hist); note_launch();
+        exclusive_scan(b.hist, b.hist, nullptr, 256 * sort_tiles, nullptr, b.scan_scratch, s, &rc->status, 0);
+        k_rs_scatter<<<sort_tiles, kSortThreads, 0, s>>>(b.keys[in], b.vals[in], b.keys[out], b.vals[out], &rc->n_live,
                                                          8 * pass, b.hist); note_launch();
     }
     k_leaves<<<gF, 256, 0, s>>>(rc, b.vals[0], b.box_lo, b.box_hi, b.llo, b.lhi, b.visit, b.lparent); note_launch();
@@ -763,7 +768,8 @@ void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const in
     const int gF = grid_for(n_query_bound, 256);
     k_query_order<<<gF, 256, 0, s>>>(rc, b.vals[0], qscan, b.live_scan);
     note_launch();
-    exclusive_scan(b.live_scan, b.live_scan, &rc->n_live, 1, &rc->pad[2], b.scan_scratch, s, &rc->status);
+    exclusive_scan(b.live_scan, b.live_scan, &rc->n_live, 1, &rc->pad[2], b.scan_scratch, s, &rc->status,
+                   n_query_bound);
     k_query_gather<<<gF, 256, 0, s>>>(rc, b.vals[0], b.live_scan, b.vals[1]);
     note_launch();
     // b.visit (free between a tree's bottom-up passes) holds the per-query redo marks

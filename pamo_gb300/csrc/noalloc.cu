@@ -127,7 +127,8 @@ extern "C" int pamo_self_intersect_noalloc(const float* points, const int32_t* t
     pamo::launch_load_points(points, n_points, L.pos, L.orig_pos, L.occ, s);
     pamo::launch_load_tris(triangles, n_triangles, n_points, L.tri, L.rc, s);
     pamo::launch_live_flags(L.rc, n_triangles, L.tri, L.qflag, s);
-    pamo::exclusive_scan(L.qflag, L.qflag, &L.rc->n_tris, 1, &L.rc->n_query, L.scan_scratch, s, &L.rc->status);
+    pamo::exclusive_scan(L.qflag, L.qflag, &L.rc->n_tris, 1, &L.rc->n_query, L.scan_scratch, s, &L.rc->status,
+                         n_triangles);
     pamo::launch_compact_flags(L.qflag, n_triangles, &L.rc->n_tris, L.qlist, s);
     pamo::bvh_build(bvh, L.tri, L.pos, L.rc, n_triangles, s, false, L.qflag, false);
     pamo::bvh_query(bvh, L.tri, L.pos, L.qlist, L.qflag, L.hit, L.exact, kExactCap, L.rc, n_triangles, kTriEps, s);

@@ -395,9 +395,9 @@ struct pamo_ctx {
         cudaMemsetAsync(vedges.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(vcursor.p, 0, (nP + 1) * sizeof(int), s);
         launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
-        exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
-        exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status);
-        exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
+        exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nP);
+        exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status, nT);
+        exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nP);
         launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p, eorder.p, s);
         launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
         const int* nt_off = valence.p;
@@ -410,7 +410,7 @@ struct pamo_ctx {
         launch_face_keys(rc, nT, tri.p, vmin.p, fkey.p, s);
         launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p,
                         orig_pos.p, occ.p, win.p, s, false);
-        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
+        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nP);
         if ((r = read_counters())) return r;
         if ((r = status_to_error(h_rc->status))) return r;
         last = *h_rc;
@@ -451,9 +451,9 @@ struct pamo_ctx {
             launch_copy_tris_dev(tri.p, orig_tri.p, rc, nTb, s);
             launch_zero_vertex_counts_dev(rc, nPb, valence.p, cursor.p, vedges.p, vcursor.p, s);
             launch_face_counts(tri.p, rc, nTb, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
-            exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
-            exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status);
-            exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
+            exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nPb);
+            exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status, nTb);
+            exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nPb);
             launch_fill_adjacency(tri.p, rc, nTb, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p,
                                   eorder.p, s);
             launch_sort_adjacency(rc, nPb, valence.p, nt.p, s);
@@ -465,14 +465,14 @@ struct pamo_ctx {
             launch_face_keys(rc, nTb, tri.p, vmin.p, fkey.p, s);
             launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p,
                             pos.p, orig_pos.p, occ.p, win.p, s);
-            exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s, &rc->status);
+            exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s, &rc->status, eb);
             launch_compact_winners(rc, eb, win.p, collapsed.p, s);
             launch_remove_invalid(rc, nTb, tri.p, s);
             launch_line_edges(rc, eb, edges.p, nt_off, nt.p, tri.p, pos.p, occ.p, nullptr, (int)collapsed.n,
                               collapsed.p, s);
             launch_zero_face_ints_dev(rc, nTb, qflag.p, s);
             launch_mark_query(rc, eb, collapsed.p, edges.p, nt_off, nt.p, qflag.p, s);
-            exclusive_scan(qflag.p, qflag.p, &rc->n_tris, 1, &rc->n_query, scan_scratch, s, &rc->status);
+            exclusive_scan(qflag.p, qflag.p, &rc->n_tris, 1, &rc->n_query, scan_scratch, s, &rc->status, nTb);
             launch_compact_flags(qflag.p, nTb, &rc->n_tris, qlist.p, s);
         } else {
             launch_undo_apply(rc, eb, collapsed.p, uflag.p, edges.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p, orig_pos.p,
@@ -484,12 +484,12 @@ struct pamo_ctx {
         else bvh_refit_faces(bvh, tri.p, pos.p, rc, nTb, s, kind == 2, qflag.p);
         bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, pair_cap(), rc, nTb, kTriEps, s);
         launch_undo_check(rc, eb, collapsed.p, edges.p, nt_off, nt.p, hit.p, uflag.p, s);
-        exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s, &rc->status);
+        exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s, &rc->status, eb);
         launch_after_check(rc, s);
         // compaction map (cusimp_free.cu:1042-1045), compaction (pamo/__init__.py:136-140), next round's state
-        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
+        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nPb);
         launch_live_flags(rc, nTb, tri.p, fflags.p, s);
-        exclusive_scan(fflags.p, fflags.p, &rc->n_tris, 1, nullptr, scan_scratch, s, &rc->status);
+        exclusive_scan(fflags.p, fflags.p, &rc->n_tris, 1, nullptr, scan_scratch, s, &rc->status, nTb);
         launch_compact_mesh(rc, nPb, nTb, pos.p, occ.p, pts_map.p, tri.p, fflags.p, pos_out.p, tri_out.p, s);
         bvh_remap(bvh, fflags.p, nTb, s);  // the tree's leaves in the next round's face numbering
         launch_round_end(rc, d_ls, d_ls + 1, undo_list.p, undo_in.p, (int)std::min(undo_in.n, undo_list.n), list_cap, s);
@@ -592,9 +592,9 @@ struct pamo_ctx {
         cudaMemsetAsync(vedges.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(vcursor.p, 0, (nP + 1) * sizeof(int), s);
         launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
-        exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
-        exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status);
-        exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
+        exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nP);
+        exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status, nT);
+        exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nP);
         launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p, eorder.p, s);
         launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
         const int* nt_off = valence.p;
@@ -615,7 +615,7 @@ struct pamo_ctx {
         launch_face_keys(rc, nT, tri.p, vmin.p, fkey.p, s);
         launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p,
                         orig_pos.p, occ.p, win.p, s);
-        exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s, &rc->status);
+        exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s, &rc->status, eb);
         launch_compact_winners(rc, eb, win.p, collapsed.p, s);
         prof.end(kPhCollapse, s);
         prof.begin(kPhMarks, s);
@@ -625,7 +625,7 @@ struct pamo_ctx {
         // faces whose intersections decide the undo: rings of the considered collapsed edges
         cudaMemsetAsync(qflag.p, 0, (nT + 1) * sizeof(int), s);
         launch_mark_query(rc, eb, collapsed.p, edges.p, nt_off, nt.p, qflag.p, s);
-        exclusive_scan(qflag.p, qflag.p, &rc->n_tris, 1, &rc->n_query, scan_scratch, s, &rc->status);
+        exclusive_scan(qflag.p, qflag.p, &rc->n_tris, 1, &rc->n_query, scan_scratch, s, &rc->status, nT);
         launch_compact_flags(qflag.p, nT, &rc->n_tris, qlist.p, s);
         prof.end(kPhMarks, s);
 
@@ -640,7 +640,7 @@ struct pamo_ctx {
             bvh_query(bvh, tri.p, pos.p, qlist.p, qflag.p, hit.p, exact_list.p, pair_cap(), rc, nT, kTriEps, s);
             prof.end(kPhQuery, s);
             launch_undo_check(rc, eb, collapsed.p, edges.p, nt_off, nt.p, hit.p, uflag.p, s);
-            exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s, &rc->status);
+            exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s, &rc->status, eb);
             launch_after_check(rc, s);
         };
         check_pass();
@@ -656,7 +656,7 @@ struct pamo_ctx {
         }
 
         // compaction map (cusimp_free.cu:1042-1045)
-        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status);
+        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nP);
         (void)operator_mode;
         if ((r = read_counters())) return r;
         if ((r = status_to_error(h_rc->status))) return r;
@@ -890,7 +890,8 @@ int simplify_loop_on(pamo_ctx* ctx, const float* points, const int32_t* triangle
             // compaction (pamo/__init__.py:136-140)
             ctx->prof.begin(kPhCompact, s);
             launch_live_flags(ctx->rc, nf, ctx->tri.p, ctx->fflags.p, s);
-            exclusive_scan(ctx->fflags.p, ctx->fflags.p, &ctx->rc->n_tris, 1, nullptr, ctx->scan_scratch, s, &ctx->rc->status);
+            exclusive_scan(ctx->fflags.p, ctx->fflags.p, &ctx->rc->n_tris, 1, nullptr, ctx->scan_scratch, s, &ctx->rc->status,
+                           nf);
             launch_compact_mesh(ctx->rc, np, nf, ctx->pos.p, ctx->occ.p, ctx->pts_map.p, ctx->tri.p, ctx->fflags.p,
                                 ctx->pos_out.p, ctx->tri_out.p, s);
             ctx->prof.end(kPhCompact, s);
@@ -1033,6 +1034,24 @@ int pamo_simplify_result(pamo_ctx* ctx, float* verts, int32_t* tris, pamo_stream
     return ctx->check(cudaGetLastError(), "export");
 }
 
+int pamo_tris_mean(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                   int32_t n_triangles, float* out3, pamo_stream stream) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (n_points < 1 || n_triangles < 1 || !points || !triangles || !out3)
+        return ctx->fail(PAMO_ERR_INVALID_ARG, "invalid sizes or null pointers");
+    cudaSetDevice(ctx->device);
+    ctx->stream = (cudaStream_t)stream;
+    int r;
+    if ((r = ctx->ensure_vertex_buffers(n_points)) || (r = ctx->ensure_face_buffers(n_triangles))) return r;
+    launch_center(points, triangles, n_points, n_triangles, ctx->face_mean.p, ctx->d_center, ctx->d_scale,
+                  ctx->pos_out.p, ctx->stream, true);
+    cudaMemcpyAsync(ctx->h_pinned_f, ctx->d_center, 3 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if ((r = ctx->check(cudaStreamSynchronize(ctx->stream), "tris_mean"))) return r;
+    for (int d = 0; d < 3; ++d) out3[d] = ctx->h_pinned_f[d];
+    return PAMO_OK;
+}
+
 int pamo_self_intersect(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
                         int32_t n_triangles, uint8_t* face_hit, pamo_stream stream) {
     if (!ctx) return PAMO_ERR_INVALID_ARG;
@@ -1053,7 +1072,8 @@ int pamo_self_intersect(pamo_ctx* ctx, const float* points, const int32_t* trian
     launch_load_tris(triangles, n_triangles, n_points, ctx->tri.p, ctx->rc, s);
     // every live face queries
     launch_live_flags(ctx->rc, n_triangles, ctx->tri.p, ctx->qflag.p, s);
-    exclusive_scan(ctx->qflag.p, ctx->qflag.p, &ctx->rc->n_tris, 1, &ctx->rc->n_query, ctx->scan_scratch, s, &ctx->rc->status);
+    exclusive_scan(ctx->qflag.p, ctx->qflag.p, &ctx->rc->n_tris, 1, &ctx->rc->n_query, ctx->scan_scratch, s,
+                   &ctx->rc->status, n_triangles);
     launch_compact_flags(ctx->qflag.p, n_triangles, &ctx->rc->n_tris, ctx->qlist.p, s);
     cudaMemsetAsync(ctx->hit.p, 0, n_triangles + 1, s);
     bvh_build(ctx->bvh, ctx->tri.p, ctx->pos.p, ctx->rc, n_triangles, s, false, ctx->qflag.p, false);

@@ -31,9 +31,9 @@ __device__ __forceinline__ void st_release(unsigned long long* p, unsigned long 
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// chunk of tile t: whole passes, at least one, tiles in element order
+// chunk of tile t (of gridDim.x tiles): whole passes, at least one, tiles in element order
 __device__ __forceinline__ void chunk_of(int n, int t, int& lo, int& hi) {
-    long long chunk = ((long long)n + kScanTiles - 1) / kScanTiles;
+    long long chunk = ((long long)n + gridDim.x - 1) / gridDim.x;
     chunk = (chunk + kPass - 1) / kPass * kPass;
     long long a = chunk * t, b = a + chunk;
     lo = (int)(a < n ? a : n);
@@ -163,8 +163,13 @@ __global__ void __launch_bounds__(kThreads) k_scan(const int* in, int* out, cons
 }  // namespace
 
 void exclusive_scan(const int* in, int* out, const int* d_n, int n_add, int* d_total, int* scratch, cudaStream_t s,
-                    int* err) {
-    k_scan<<<kScanTiles, kThreads, 0, s>>>(in, out, d_n, n_add, d_total, scratch, err); note_launch();
+                    int* err, long long n_bound) {
+    int tiles = kScanTiles;
+    if (n_bound >= 0 && n_bound < (1 << 19)) {  // callers cap their bounds at 2^19 (every grid full from there)
+        const long long want = (n_bound + n_add + kPass - 1) / kPass;
+        tiles = (int)(want < 1 ? 1 : (want > kScanTiles ? kScanTiles : want));
+    }
+    k_scan<<<tiles, kThreads, 0, s>>>(in, out, d_n, n_add, d_total, scratch, err); note_launch();
 }
 
 int scan_scratch_clear(int* scratch) {

@@ -14,9 +14,10 @@ inline size_t scan_scratch_ints() { return 8 + 2 * (size_t)kScanTiles; }
 // If d_total is given, *d_total = sum of all n inputs. Inputs are int32 counts (no overflow checks).
 // The scratch must be all zero before the first scan (scan_scratch_clear, or zero-initialised static memory);
 // every scan leaves it zero again. One scratch serves one stream at a time. A look-back that waits too long
-// sets kErrIterLimit in *err (when given).
+// sets kErrIterLimit in *err (when given). n_bound >= 0: an upper bound of *d_n known when the launch is made,
+// which sizes the grid (any value gives the same result; a low one only makes the tiles longer).
 void exclusive_scan(const int* in, int* out, const int* d_n, int n_add, int* d_total, int* scratch,
-                    cudaStream_t s, int* err = nullptr);
+                    cudaStream_t s, int* err = nullptr, long long n_bound = -1);
 
 // Zeroes a freshly allocated scan scratch (synchronous); returns nonzero on a CUDA error.
 int scan_scratch_clear(int* scratch);

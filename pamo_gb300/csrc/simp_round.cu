@@ -701,53 +701,178 @@ __global__ void k_face_means(const float* __restrict__ pts, const int* __restric
     }
 }
 
-constexpr int kSumTile = 2048;
 
-__global__ void __launch_bounds__(1024) k_sequential_sum(const float* __restrict__ fm, int nf, float* center) {
-    __shared__ float buf[2][3][kSumTile];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ntiles = (nf + kSumTile - 1) / kSumTile;
-    auto load = [&](int t, int slot, int first_thread, int nthreads) {
-        const int base = t * kSumTile;
-        const int len = min(kSumTile, nf - base);
-        for (int i = (int)threadIdx.x - first_thread; i < 3 * kSumTile; i += nthreads) {
-            const int d = i / kSumTile, k = i - d * kSumTile;
-            if (k < len) buf[slot][d][k] = fm[(size_t)d * nf + base + k];
-        }
-    };
-    if (ntiles > 0) load(0, 0, 0, blockDim.x);
+// The sequential float32 sum s_k = fl(s_(k-1) + x_k) of numpy's axis-0 reduction, exact, with window
+// parallelism (one block per coordinate). While the running sum stays inside one binade [2^e, 2^(e+1)) (float
+// spacing u = 2^(e-23)) and off its end points, fl(s + x) = s + u * round(x / u): the rounded increments are
+// integers, so a window's running sums are s + u * (prefix sums of the increments), exact in int64. Each element
+// is checked (its running sum inside [2^23 + 1, 2^24 - 1] units of u, its increment not a half-way tie, whose
+// rounding would depend on the sum's parity); the first element that fails is added with a float add and the
+// next window starts after it. Where failures are dense (a sum near zero, or crossing binades quickly), a
+// stretch is summed in order by one thread.
+constexpr int kSumThreads = 1024;
+constexpr int kSumPer = 16;
+constexpr int kSumWindow = kSumThreads * kSumPer;
+
+__global__ void __launch_bounds__(kSumThreads) k_exact_sequential_sum(const float* __restrict__ fm, int nf,
+                                                                      float* center) {
+    const float* x = fm + (size_t)blockIdx.x * nf;
+    constexpr int kStage = 4096;
+    __shared__ long long wsum[32];
+    __shared__ int wmin[32];
+    __shared__ float stage[kStage];
+    __shared__ float s_sh;
+    __shared__ int k_sh, burst_sh, fail_sh, short_sh;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        s_sh = 0.0f;
+        k_sh = 0;
+        burst_sh = 0;
+        short_sh = 0;
+    }
     __syncthreads();
-    float s = 0.0f;
-    for (int t = 0; t < ntiles; ++t) {
-        const int cur = t & 1;
-        if (warp != 0) {
-            if (t + 1 < ntiles) load(t + 1, cur ^ 1, 32, blockDim.x - 32);
-        } else if (lane < 3) {
-            const int len = min(kSumTile, nf - t * kSumTile);
-            const float* x = buf[cur][lane];
-            // the adds form one dependent chain; the shared-memory loads of the next 16 values are issued
-            // before the current 16 are added, so the chain runs at the add latency
-            int k = 0;
-            if (len >= 16) {
-                float v[16], w[16];
-#pragma unroll
-                for (int j = 0; j < 16; ++j) v[j] = x[j];
-                for (k = 16; k + 16 <= len; k += 16) {
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) w[j] = x[k + j];
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) s += v[j];
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) v[j] = w[j];
-                }
-#pragma unroll
-                for (int j = 0; j < 16; ++j) s += v[j];
+    while (true) {
+        const float s = s_sh;
+        const int k = k_sh;
+        const int burst = burst_sh;
+        __syncthreads();  // everyone has read the state
+        if (k >= nf) break;
+        int e = 0;
+        bool par = burst == 0 && s != 0.0f && isfinite(s);
+        if (par) {
+            e = ilogbf(s);
+            par = e >= -125 && e <= 126;
+        }
+        if (!par) {
+            // in order, staged through shared memory: a burst after dense failures, 64 elements while the sum is
+            // zero or subnormal, the rest when it is not finite (every later sum stays so)
+            const int n = min(burst > 0 ? burst : (isfinite(s) ? 64 : nf - k), nf - k);
+            float t = s;
+            for (int c = 0; c < n; c += kStage) {
+                const int m = min(kStage, n - c);
+                for (int i = threadIdx.x; i < m; i += kSumThreads) stage[i] = x[k + c + i];
+                __syncthreads();
+                if (threadIdx.x == 0)
+                    for (int i = 0; i < m; ++i) t += stage[i];
+                __syncthreads();
             }
-            for (; k < len; ++k) s += x[k];
+            if (threadIdx.x == 0) {
+                s_sh = t;
+                k_sh = k + n;
+                burst_sh = 0;
+            }
+            __syncthreads();
+            continue;
+        }
+        // integer arithmetic on the float bits (the fp64 pipe is too slow for this): s = S * u with u = 2^(e-23),
+        // x / u = +-m * 2^(ex - e) for x's 24-bit significand m
+        const unsigned sb = __float_as_uint(s);
+        const long long S = (sb >> 31) ? -(long long)((sb & 0x7FFFFFu) | 0x800000u) : (long long)((sb & 0x7FFFFFu) | 0x800000u);
+        const int base = k + threadIdx.x * kSumPer;
+        const int wend = min(k + kSumWindow, nf);
+        long long q[kSumPer];
+        unsigned badm = 0;
+        long long tsum = 0;
+#pragma unroll
+        for (int i = 0; i < kSumPer; ++i) {
+            const int idx = base + i;
+            q[i] = 0;
+            if (idx < wend) {
+                const unsigned b = __float_as_uint(x[idx]);
+                const int bex = (int)((b >> 23) & 0xFFu);
+                if (bex == 0xFF) {
+                    badm |= 1u << i;  // inf or nan
+                } else if ((b & 0x7FFFFFFFu) != 0u) {
+                    const long long m = bex ? (long long)((b & 0x7FFFFFu) | 0x800000u) : (long long)(b & 0x7FFFFFu);
+                    const int sh = (bex ? bex - 127 : -126) - e;  // x / u = m * 2^sh
+                    long long mag;
+                    if (sh >= 0) {
+                        if (sh > 16) badm |= 1u << i;  // |x / u| >= 2^40: leaves the binade anyway
+                        mag = sh > 16 ? 0 : m << sh;
+                    } else if (-sh >= 25) {
+                        mag = 0;  // |x / u| < 1/2
+                    } else {
+                        const int kk = -sh;
+                        const long long rem = m & ((1ll << kk) - 1), half = 1ll << (kk - 1);
+                        if (rem == half) badm |= 1u << i;  // a tie: rounds by the sum's parity
+                        mag = (m >> kk) + (rem > half ? 1 : 0);
+                    }
+                    q[i] = (b >> 31) ? -mag : mag;
+                }
+            }
+            tsum += q[i];
+        }
+        // block exclusive scan of the per-thread sums
+        long long inc = tsum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            long long w = wsum[lane];
+            long long wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long t = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += t;
+            }
+            wsum[lane] = wi - w;
+        }
+        __syncthreads();
+        long long R = S + wsum[warp] + inc - tsum;
+        const long long lo = s > 0.0f ? (1ll << 23) + 1 : -((1ll << 24) - 1);
+        const long long hi = s > 0.0f ? (1ll << 24) - 1 : -((1ll << 23) + 1);
+        int first = nf;
+#pragma unroll
+        for (int i = 0; i < kSumPer; ++i) {
+            const int idx = base + i;
+            if (idx < wend && first == nf) {
+                R += q[i];
+                if ((badm >> i & 1u) || R < lo || R > hi) first = idx;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
+        if (lane == 0) wmin[warp] = first;
+        __syncthreads();
+        if (warp == 0) {
+            int m = wmin[lane];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if (lane == 0) fail_sh = m;
+        }
+        __syncthreads();
+        const int f = min(fail_sh, wend);  // elements [k, f) are exact; f fails (or ends the window)
+        // the owner of element f - 1 publishes the sum after it
+        if (f > k && (f - 1 - k) / kSumPer == (int)threadIdx.x) {
+            long long r = S + wsum[warp] + inc - tsum;
+            for (int i = 0; i <= (f - 1 - k) % kSumPer; ++i) r += q[i];
+            // r * u with 2^23 < |r| < 2^24: the float with r's significand and s's exponent
+            s_sh = __uint_as_float((r < 0 ? 0x80000000u : 0u) | ((unsigned)(e + 127) << 23) |
+                                   ((unsigned)(r < 0 ? -r : r) & 0x7FFFFFu));
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (f < wend) {  // the failing element: a float add in order
+                s_sh = s_sh + x[f];
+                k_sh = f + 1;
+                // four windows in a row that advanced less than 32 elements: sum the next 1024 in order
+                short_sh = (f - k < 32) ? short_sh + 1 : 0;
+                if (short_sh >= 4) {
+                    burst_sh = 1024;
+                    short_sh = 0;
+                }
+            } else {
+                k_sh = wend;
+                short_sh = 0;
+            }
         }
         __syncthreads();
     }
-    if (warp == 0 && lane < 3) center[lane] = s / (float)nf;
+    if (threadIdx.x == 0) center[blockIdx.x] = s_sh / (float)nf;
 }
 
 __global__ void k_center_points(const float* __restrict__ pts, int np, const float* __restrict__ center, float4* out,
@@ -965,7 +1090,7 @@ void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4*
     (void)n;
     const int g = grid_for((long long)fb.n, kT);
     k_shuffle_flags<<<g, kT, 0, s>>>(fb, flags); note_launch();
-    exclusive_scan(flags, flags, nullptr, (int)fb.n + 1, nullptr, scan_scratch, s, err);
+    exclusive_scan(flags, flags, nullptr, (int)fb.n + 1, nullptr, scan_scratch, s, err, 0);
     k_shuffle_gather<<<g, kT, 0, s>>>(fb, flags, src, dst); note_launch();
 }
 
@@ -1087,7 +1212,7 @@ void launch_center(const float* pts, const int* tris, int n_pts, int n_tris, flo
     // center[0..2] = tris_mean (zero when not centring); center[4..9] scratch (order-preserving extents)
     if (centre) {
         k_face_means<<<grid_for(n_tris, kT), kT, 0, s>>>(pts, tris, n_tris, face_mean); note_launch();
-        k_sequential_sum<<<1, 1024, 0, s>>>(face_mean, n_tris, center); note_launch();
+        k_exact_sequential_sum<<<3, kSumThreads, 0, s>>>(face_mean, n_tris, center); note_launch();
     } else {
         cudaMemsetAsync(center, 0, 4 * sizeof(float), s);
     }

@@ -185,3 +185,37 @@ def test_pair_list_overflow_matches_oracle(name, cap):
     assert rounds == len(fpr)
     assert np.array_equal(F.cpu().numpy(), Fo)
     assert np.array_equal(V.cpu().numpy(), Vo)
+
+
+def _tris_mean_cases():
+    from pamo_gb300 import synth
+
+    rng = np.random.default_rng(5)
+    cases = {"plain_small": synth.config_mesh("plain_small", seed=0)}
+    v, f = meshes.sphere(40)
+    cases["sphere40"] = (v, f)
+    # sums that wander through zero and across many binades, with offsets, signs and magnitudes mixed
+    n = 300000
+    fr = rng.integers(0, n, (n, 3)).astype(np.int32)
+    for name, pts in {
+        "centred_noise": rng.normal(0, 1, (n, 3)),
+        "offset": rng.normal(0, 1, (n, 3)) + [1e3, -2e2, 0.5],
+        "mixed_scales": rng.normal(0, 1, (n, 3)) * 10.0 ** rng.integers(-6, 6, (n, 1)),
+        "dyadic": rng.integers(-64, 64, (n, 3)) / 8.0,  # many exact ties in the sum
+    }.items():
+        cases[name] = (pts.astype(np.float32), fr)
+    return cases
+
+
+@pytest.mark.parametrize("name", sorted(_tris_mean_cases()))
+def test_tris_mean_matches_numpy(name):
+    """The centring sum (exact sequential float32 order, computed with window parallelism) equals numpy's
+    float32 tris.mean(axis=1).mean(axis=0) bit for bit."""
+    import pamo_gb300
+
+    v, f = _tris_mean_cases()[name]
+    got = pamo_gb300.tris_mean(torch.from_numpy(v).cuda(), torch.from_numpy(f).cuda())
+    want = np.asarray(v, np.float32)[f].mean(axis=1).mean(axis=0)
+    assert want.dtype == np.float32
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (got, want)
+    assert np.array_equal(got, orc.tris_mean(v, f))
