@@ -125,6 +125,11 @@ int pamo_simplify_round_faces(const pamo_ctx* ctx, int32_t* faces_per_round, int
  * synchronisation); returns the number written. No reference counterpart (diagnostics). */
 int pamo_simplify_round_ms(const pamo_ctx* ctx, double* ms, int32_t capacity);
 
+/* Device time of each round of the last loop: the time between events recorded around the round's graph
+ * launches (0 for rounds launched without graphs); the gap to pamo_simplify_round_ms is host turnaround.
+ * Returns the number written. Diagnostics. */
+int pamo_simplify_round_gpu_ms(const pamo_ctx* ctx, double* ms, int32_t capacity);
+
 /*
  * The centre PaMO.run subtracts before simplifying: preprocess_mesh's tris_mean (simp_cuda/pamo/__init__.py:
  * 60-64), numpy float32 semantics: per face ((a + b) + c) / 3, then the sequential float32 sum over faces in

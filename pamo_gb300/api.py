@@ -75,6 +75,12 @@ class Context:
         n = _native.load().pamo_simplify_round_ms(self.handle, out, 4096)
         return list(out[: max(n, 0)])
 
+    def round_gpu_ms(self) -> list:
+        """Device time of each round of the last whole-loop call (events around its graph launches)."""
+        out = (ctypes.c_double * 4096)()
+        n = _native.load().pamo_simplify_round_gpu_ms(self.handle, out, 4096)
+        return list(out[: max(n, 0)])
+
     def device_bytes(self) -> int:
         """Device memory the context holds."""
         return int(_native.load().pamo_ctx_device_bytes(self.handle))

@@ -182,6 +182,9 @@ struct pamo_ctx {
     int run_np = 0, run_nt = 0;
     std::vector<int> faces_per_round;
     std::vector<double> round_ms;  // host wall time of each round of the last loop (rounds end with a sync)
+    std::vector<double> round_gpu_ms;  // device time of each device round's graph launches (events around them)
+    cudaEvent_t ev_g0 = nullptr, ev_g1 = nullptr;
+    double cur_gpu_ms = 0.0;
     // totals over the rounds of the last pamo_simplify_device call
     long long tot[10] = {};
 
@@ -264,6 +267,9 @@ struct pamo_ctx {
         if (d_center) cudaFree(d_center);
         if (d_ls) cudaFree(d_ls);
         drop_graphs();
+        if (ev_g0) cudaEventDestroy(ev_g0);
+        if (ev_g1) cudaEventDestroy(ev_g1);
+        ev_g0 = ev_g1 = nullptr;
         if (own_stream) cudaStreamDestroy(own_stream);
         if (ev_join) cudaEventDestroy(ev_join);
         own_stream = nullptr;
@@ -529,9 +535,21 @@ struct pamo_ctx {
             if (e != cudaSuccess) return fail(PAMO_ERR_CUDA, "graph instantiation");
             it = graphs.emplace(key, rg).first;
         }
+        if (!ev_g0) {
+            cudaEventCreate(&ev_g0);
+            cudaEventCreate(&ev_g1);
+        }
+        cudaEventRecord(ev_g0, stream);
         if (cudaGraphLaunch(it->second.exec, stream) != cudaSuccess) return fail(PAMO_ERR_CUDA, "graph launch");
+        cudaEventRecord(ev_g1, stream);
         note_launches(it->second.kernels);
         return PAMO_OK;
+    }
+
+    // device time of the graph launched last (call after the stream has been synchronised)
+    void note_graph_time() {
+        float ms = 0.f;
+        if (ev_g0 && cudaEventElapsedTime(&ms, ev_g0, ev_g1) == cudaSuccess) cur_gpu_ms += ms;
     }
 
     int status_to_error(int bits) {
@@ -850,6 +868,8 @@ int simplify_loop_on(pamo_ctx* ctx, const float* points, const int32_t* triangle
     ctx->have_run = false;
     ctx->faces_per_round.clear();
     ctx->round_ms.clear();
+    ctx->round_gpu_ms.clear();
+    ctx->cur_gpu_ms = 0.0;
     auto t_round = std::chrono::steady_clock::now();
     for (auto& t : ctx->tot) t = 0;
     int r;
@@ -903,13 +923,16 @@ int simplify_loop_on(pamo_ctx* ctx, const float* points, const int32_t* triangle
             // rebuild the LBVH when a quarter of its leaves lost their faces, else refit the carried one
             const bool rebuild = !ctx->bvh_reuse || tree_leaves == 0 || (long long)nf * 4 < (long long)tree_leaves * 3;
             if (rebuild) tree_leaves = nf;
+            ctx->cur_gpu_ms = 0.0;
             if ((r = ctx->run_round_dev(rebuild ? 0 : 2, np, nf, threshold))) return r;
             if ((r = ctx->read_counters())) return r;
+            ctx->note_graph_time();
             int extra = 0;
             while (ctx->h_rc->n_undo != 0) {  // cusimp_free.cu:1016-1040
                 ++extra;
                 if ((r = ctx->run_round_dev(1, np, nf, threshold))) return r;
                 if ((r = ctx->read_counters())) return r;
+                ctx->note_graph_time();
                 if (extra == kMaxExtraPasses) break;
             }
             if ((r = ctx->status_to_error(ctx->h_rc->status))) return r;
@@ -935,6 +958,8 @@ int simplify_loop_on(pamo_ctx* ctx, const float* points, const int32_t* triangle
         {
             const auto t_now = std::chrono::steady_clock::now();
             ctx->round_ms.push_back(std::chrono::duration<double, std::milli>(t_now - t_round).count());
+            ctx->round_gpu_ms.push_back(ctx->cur_gpu_ms);
+            ctx->cur_gpu_ms = 0.0;
             t_round = t_now;
         }
         if ((opt.target >= 0 && nf <= opt.target) || (opt.stop_small && nf <= 10)) break;
@@ -1118,6 +1143,13 @@ int pamo_simplify_round_ms(const pamo_ctx* ctx, double* ms, int32_t capacity) {
     if (!ctx || !ms) return PAMO_ERR_INVALID_ARG;
     const int n = std::min<int>(capacity, (int)ctx->round_ms.size());
     for (int i = 0; i < n; ++i) ms[i] = ctx->round_ms[i];
+    return n;
+}
+
+int pamo_simplify_round_gpu_ms(const pamo_ctx* ctx, double* ms, int32_t capacity) {
+    if (!ctx || !ms) return PAMO_ERR_INVALID_ARG;
+    const int n = std::min<int>(capacity, (int)ctx->round_gpu_ms.size());
+    for (int i = 0; i < n; ++i) ms[i] = ctx->round_gpu_ms[i];
     return n;
 }
 
