@@ -574,7 +574,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse_redo(const float4* _
     if ((threadIdx.x & 31) == 0 && exact) atomicAdd(&rc->n_exact, (unsigned long long)exact);
 }
 
-__global__ void __launch_bounds__(128) k_pairs(const int4* __restrict__ tri, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(128, 6) k_pairs(const int4* __restrict__ tri, const float4* __restrict__ pos,
                                                const int2* __restrict__ pair_list, int pair_cap, unsigned char* hit,
                                                RoundCounters* rc, float eps) {
     const int n = min(rc->pad[1], pair_cap);
