@@ -1398,14 +1398,18 @@ __device__ __forceinline__ unsigned ld_acquire(volatile unsigned* p) {
 
 // Barrier across all blocks of a cooperative launch (co-residency guaranteed). The spin is bounded: on
 // time-out it records kErrIterLimit in *status and lets the block go on (the host then reports the error).
+// Arrival is a release (the block's writes, ordered before it by the block barrier, become visible with it),
+// departure an acquire; acq_rel fences are enough for that and cheaper than sequentially consistent ones.
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
 __device__ __forceinline__ void grid_barrier(unsigned* count, volatile unsigned* gen, int* status) {
     __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned g = *gen;
-        __threadfence();
+        fence_acq_rel_gpu();
         if (atomicAdd(count, 1u) == gridDim.x - 1) {
             *count = 0;
-            __threadfence();
+            fence_acq_rel_gpu();
             atomicAdd((unsigned*)gen, 1u);
         } else {
             long long spins = 0;
@@ -1416,7 +1420,7 @@ __device__ __forceinline__ void grid_barrier(unsigned* count, volatile unsigned*
                 }
             }
         }
-        __threadfence();
+        fence_acq_rel_gpu();
     }
     __syncthreads();
 }
