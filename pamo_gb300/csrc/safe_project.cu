@@ -1492,7 +1492,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_solve(const float4* __restrict_
 // The same solve inside one thread-block cluster (up to 16 CTAs): the barriers are the hardware cluster
 // barrier and the block partials are exchanged through distributed shared memory instead of a grid-wide
 // barrier through global memory. Selected with cg_mode 2.
-constexpr int kClusterThreads = 512;
+constexpr int kClusterThreads = 1024;
 
 __global__ void __launch_bounds__(kClusterThreads) k_cg_cluster(const float4* __restrict__ x, HvpArgs A,
                                                                 const float4* __restrict__ grad,
@@ -1514,16 +1514,17 @@ __global__ void __launch_bounds__(kClusterThreads) k_cg_cluster(const float4* __
         CSum br = block_reduce(acc);
         if (threadIdx.x == 0) slot[k] = make_float2(br.s, br.c);
         cl.sync();
-        if (threadIdx.x == 0) {
+        if (threadIdx.x < 32) {  // one remote read per lane, merged in rank order through shuffles
+            const unsigned lane = threadIdx.x;
+            const float2 t2 = lane < nblk ? *cl.map_shared_rank(&slot[k], lane) : make_float2(0.f, 0.f);
             CSum a;
             for (unsigned b = 0; b < nblk; ++b) {
-                const float2 t2 = *cl.map_shared_rank(&slot[k], b);
                 CSum t;
-                t.s = t2.x;
-                t.c = t2.y;
+                t.s = __shfl_sync(0xffffffffu, t2.x, (int)b);
+                t.c = __shfl_sync(0xffffffffu, t2.y, (int)b);
                 a.merge(t);
             }
-            total = a.s + a.c;
+            if (lane == 0) total = a.s + a.c;
         }
         __syncthreads();
         const float v = total;
