@@ -125,10 +125,15 @@ int pamo_simplify_round_faces(const pamo_ctx* ctx, int32_t* faces_per_round, int
  * synchronisation); returns the number written. No reference counterpart (diagnostics). */
 int pamo_simplify_round_ms(const pamo_ctx* ctx, double* ms, int32_t capacity);
 
-/* Device time of each round of the last loop: the time between events recorded around the round's graph
- * launches (0 for rounds launched without graphs); the gap to pamo_simplify_round_ms is host turnaround.
- * Returns the number written. Diagnostics. */
+/* Device time of each round of the last loop, with pamo_ctx_set_option(ctx, "time_rounds", 1): the time between
+ * events recorded around the round's graph launches (0 for rounds launched without graphs or with the option
+ * off); the gap to pamo_simplify_round_ms is host turnaround. Returns the number written. Diagnostics. */
 int pamo_simplify_round_gpu_ms(const pamo_ctx* ctx, double* ms, int32_t capacity);
+
+/* With pamo_ctx_set_option(ctx, "time_edge_cost", 1), events are recorded around every edge-cost kernel launch
+ * (also inside the cached round graphs); this returns their summed duration in ms and the number of launches
+ * since the option was set or the last reset (reset != 0 clears them). Diagnostics. */
+int pamo_kernel_time(pamo_ctx* ctx, double* ms, int64_t* launches, int32_t reset);
 
 /*
  * The centre PaMO.run subtracts before simplifying: preprocess_mesh's tris_mean (simp_cuda/pamo/__init__.py:

@@ -52,6 +52,7 @@ SIGNATURES = {
     "pamo_simplify_result": (ctypes.c_int, [_P, _P, _P, _P]),
     "pamo_simplify_round_faces": (ctypes.c_int, [_P, _PI32, _I32]),
     "pamo_simplify_round_ms": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _I32]),
+    "pamo_kernel_time": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64), _I32]),
     "pamo_simplify_round_gpu_ms": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _I32]),
     "pamo_self_intersect": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _P, _P]),
     "pamo_self_intersect_noalloc": (ctypes.c_int, [_P, _P, _I32, _I32, _P, _P]),

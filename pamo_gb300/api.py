@@ -75,6 +75,13 @@ class Context:
         n = _native.load().pamo_simplify_round_ms(self.handle, out, 4096)
         return list(out[: max(n, 0)])
 
+    def kernel_time(self, reset: bool = False):
+        """(summed ms, launches) of the edge-cost kernel while the "time_edge_cost" option is on."""
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        _native.check(_native.load().pamo_kernel_time(self.handle, ctypes.byref(ms), ctypes.byref(n), int(reset)),
+                      self.handle)
+        return ms.value, n.value
+
     def round_gpu_ms(self) -> list:
         """Device time of each round of the last whole-loop call (events around its graph launches)."""
         out = (ctypes.c_double * 4096)()

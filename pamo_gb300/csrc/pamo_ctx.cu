@@ -183,7 +183,36 @@ struct pamo_ctx {
     std::vector<int> faces_per_round;
     std::vector<double> round_ms;  // host wall time of each round of the last loop (rounds end with a sync)
     std::vector<double> round_gpu_ms;  // device time of each device round's graph launches (events around them)
+    // edge-cost kernel timer: events recorded around every k_edge_cost launch (captured into the round graphs)
+    bool time_cost = false;
+    cudaEvent_t ev_c0 = nullptr, ev_c1 = nullptr;
+    double cost_ms = 0.0;
+    long long cost_n = 0;
+    // recorded as event-record nodes when the stream is being captured into a round graph (the external flag is
+    // valid only during a capture)
+    void record_timer(cudaEvent_t ev, cudaStream_t s) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(s, &cs);
+        if (cs == cudaStreamCaptureStatusActive) cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal);
+        else cudaEventRecord(ev, s);
+    }
+    void cost_begin(cudaStream_t s) {
+        if (time_cost) record_timer(ev_c0, s);
+    }
+    void cost_end(cudaStream_t s) {
+        if (time_cost) record_timer(ev_c1, s);
+    }
+    // after the stream was synchronised: add the last edge-cost launch's duration
+    void cost_note() {
+        float t = 0.f;
+        if (time_cost && cudaEventElapsedTime(&t, ev_c0, ev_c1) == cudaSuccess) {
+            cost_ms += t;
+            ++cost_n;
+        }
+    }
     cudaEvent_t ev_g0 = nullptr, ev_g1 = nullptr;
+    bool time_rounds = false;  // option "time_rounds": timing events around the round graphs (off: events with
+                               // timing on every launch cost concurrency between the streams of a worker pool)
     double cur_gpu_ms = 0.0;
     // totals over the rounds of the last pamo_simplify_device call
     long long tot[10] = {};
@@ -267,6 +296,9 @@ struct pamo_ctx {
         if (d_center) cudaFree(d_center);
         if (d_ls) cudaFree(d_ls);
         drop_graphs();
+        if (ev_c0) cudaEventDestroy(ev_c0);
+        if (ev_c1) cudaEventDestroy(ev_c1);
+        ev_c0 = ev_c1 = nullptr;
         if (ev_g0) cudaEventDestroy(ev_g0);
         if (ev_g1) cudaEventDestroy(ev_g1);
         ev_g0 = ev_g1 = nullptr;
@@ -466,8 +498,10 @@ struct pamo_ctx {
             launch_quadrics(rc, nPb, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s);
             launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
             launch_fill_u64_dev(rc, nPb, vmin.p, ~0ull, s);
+            cost_begin(s);
             launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p,
                              vmin.p, d_scale, threshold, 0, s, &d_ls->is_stuck);
+            cost_end(s);
             launch_face_keys(rc, nTb, tri.p, vmin.p, fkey.p, s);
             launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p,
                             pos.p, orig_pos.p, occ.p, win.p, s);
@@ -535,13 +569,13 @@ struct pamo_ctx {
             if (e != cudaSuccess) return fail(PAMO_ERR_CUDA, "graph instantiation");
             it = graphs.emplace(key, rg).first;
         }
-        if (!ev_g0) {
+        if (time_rounds && !ev_g0) {
             cudaEventCreate(&ev_g0);
             cudaEventCreate(&ev_g1);
         }
-        cudaEventRecord(ev_g0, stream);
+        if (time_rounds) cudaEventRecord(ev_g0, stream);
         if (cudaGraphLaunch(it->second.exec, stream) != cudaSuccess) return fail(PAMO_ERR_CUDA, "graph launch");
-        cudaEventRecord(ev_g1, stream);
+        if (time_rounds) cudaEventRecord(ev_g1, stream);
         note_launches(it->second.kernels);
         return PAMO_OK;
     }
@@ -549,7 +583,7 @@ struct pamo_ctx {
     // device time of the graph launched last (call after the stream has been synchronised)
     void note_graph_time() {
         float ms = 0.f;
-        if (ev_g0 && cudaEventElapsedTime(&ms, ev_g0, ev_g1) == cudaSuccess) cur_gpu_ms += ms;
+        if (time_rounds && ev_g0 && cudaEventElapsedTime(&ms, ev_g0, ev_g1) == cudaSuccess) cur_gpu_ms += ms;
     }
 
     int status_to_error(int bits) {
@@ -626,8 +660,10 @@ struct pamo_ctx {
         launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
         cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
         prof.begin(kPhCost, s);
+        cost_begin(s);
         launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p, vmin.p,
                          d_scale, threshold, is_stuck, s);
+        cost_end(s);
         prof.end(kPhCost, s);
         prof.begin(kPhCollapse, s);
         launch_face_keys(rc, nT, tri.p, vmin.p, fkey.p, s);
@@ -663,6 +699,7 @@ struct pamo_ctx {
         };
         check_pass();
         if ((r = read_counters())) return r;
+        cost_note();
         int extra = 0;
         while (h_rc->n_undo != 0) {
             ++extra;
@@ -743,7 +780,18 @@ int pamo_ctx_set_option(pamo_ctx* ctx, const char* name, int64_t value) {
     if (n == "graphs") ctx->use_graphs = value != 0;
     else if (n == "device_rounds") ctx->device_rounds = value != 0;
     else if (n == "bvh_reuse") ctx->bvh_reuse = value != 0;
-    else if (n == "pair_cap") {
+    else if (n == "time_rounds") ctx->time_rounds = value != 0;
+    else if (n == "time_edge_cost") {
+        ctx->time_cost = value != 0;
+        if (ctx->time_cost && !ctx->ev_c0) {
+            cudaSetDevice(ctx->device);
+            cudaEventCreate(&ctx->ev_c0);
+            cudaEventCreate(&ctx->ev_c1);
+        }
+        ctx->cost_ms = 0.0;
+        ctx->cost_n = 0;
+        ctx->drop_graphs();
+    } else if (n == "pair_cap") {
         ctx->pair_cap_limit = value;
         ctx->drop_graphs();
     } else return ctx->fail(PAMO_ERR_INVALID_ARG, "unknown option %s", name);
@@ -927,6 +975,7 @@ int simplify_loop_on(pamo_ctx* ctx, const float* points, const int32_t* triangle
             if ((r = ctx->run_round_dev(rebuild ? 0 : 2, np, nf, threshold))) return r;
             if ((r = ctx->read_counters())) return r;
             ctx->note_graph_time();
+            ctx->cost_note();
             int extra = 0;
             while (ctx->h_rc->n_undo != 0) {  // cusimp_free.cu:1016-1040
                 ++extra;
@@ -1144,6 +1193,17 @@ int pamo_simplify_round_ms(const pamo_ctx* ctx, double* ms, int32_t capacity) {
     const int n = std::min<int>(capacity, (int)ctx->round_ms.size());
     for (int i = 0; i < n; ++i) ms[i] = ctx->round_ms[i];
     return n;
+}
+
+int pamo_kernel_time(pamo_ctx* ctx, double* ms, int64_t* launches, int32_t reset) {
+    if (!ctx || !ms || !launches) return PAMO_ERR_INVALID_ARG;
+    *ms = ctx->cost_ms;
+    *launches = ctx->cost_n;
+    if (reset) {
+        ctx->cost_ms = 0.0;
+        ctx->cost_n = 0;
+    }
+    return PAMO_OK;
 }
 
 int pamo_simplify_round_gpu_ms(const pamo_ctx* ctx, double* ms, int32_t capacity) {
