@@ -278,6 +278,23 @@ int pamo_safe_project(pamo_stage3* s, const double* gt_points, const int32_t* gt
  * counterpart (the reference logs these). */
 int pamo_stage3_stats(const pamo_stage3* s, double* out, int32_t n);
 
+/* ---------------------------------------------------------------- evaluation (metrics.py:7-107)
+ * Squared distances from points to a triangle mesh, as igl.point_mesh_squared_distance and
+ * trimesh.proximity.closest_point compute them for the reference's Chamfer and Hausdorff distances
+ * (simp_cuda/safe_project/src/pamo_safe_project/metrics.py:7-50): out_sqdist[i] = min over faces of the
+ * squared float64 distance from points[i] to the face, out_face[i] = that face (lowest index on ties; may be
+ * NULL). All arrays are device arrays (float64 [n,3], int32 [m,3]). Synchronises `stream`. */
+int pamo_point_mesh_sqdist(const double* points, int32_t n_points, const double* vertices, int32_t n_vertices,
+                           const int32_t* triangles, int32_t n_triangles, double* out_sqdist, int32_t* out_face,
+                           pamo_stream stream);
+
+/* Per-face minimum angles in radians (metrics.py:55-107): out_edge_form as compute_min_angle_VF computes
+ * the corner angles (from the face's edge vectors, cosines clipped to [-1, 1]), out_igl_form as
+ * igl.internal_angles does (law of cosines on the edge lengths), NaN for a face with a repeated index. Either
+ * output may be NULL. Device arrays; synchronises `stream`. */
+int pamo_face_min_angles(const double* vertices, const int32_t* triangles, int32_t n_triangles, double* out_edge_form,
+                         double* out_igl_form, pamo_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,6 +40,8 @@ SIGNATURES = {
     "pamo_ctx_set_option": (ctypes.c_int, [_P, ctypes.c_char_p, _I64]),
     "pamo_forward_round": (ctypes.c_int, [_P, _P, _P, _P, _I32, _I32, _I32, _F32, _F32, _I32, _I32, _P]),
     "pamo_legacy_round": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _F32, _F32, _I32, _P]),
+    "pamo_point_mesh_sqdist": (ctypes.c_int, [_P, _I32, _P, _I32, _P, _I32, _P, _P, _P]),
+    "pamo_face_min_angles": (ctypes.c_int, [_P, _P, _I32, _P, _P, _P]),
     "pamo_tris_mean": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _P, _P]),
     "pamo_round_sizes": (ctypes.c_int, [_P, _PI32, _PI32, _PI32]),
     "pamo_round_outputs": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
