@@ -295,6 +295,30 @@ int pamo_point_mesh_sqdist(const double* points, int32_t n_points, const double*
 int pamo_face_min_angles(const double* vertices, const int32_t* triangles, int32_t n_triangles, double* out_edge_form,
                          double* out_igl_form, pamo_stream stream);
 
+/* ---------------------------------------------------------------- stage 1 (remeshing)
+ * PaMO.remesh (simp_cuda/pamo/__init__.py:58-93): preprocess_mesh's normalisation into the unit cube, a
+ * narrow-band distance field of the triangles on a resolution^3 grid (band 3 / R) with the inside found by a
+ * flood fill from the grid boundary, its level set at 0.9 voxel extracted as a closed triangle mesh, mapped
+ * back to the input's frame minus mean3 (the tris_mean of pamo_tris_mean, as the reference's remesh output
+ * is). The reference calls torchcumesh2sdf and pdmc for this; both are absent, so the construction is this
+ * library's own (dual extraction, one vertex per sign-changing cell). Device points/triangles; sizes out;
+ * fetch the mesh with pamo_remesh_result. */
+typedef struct pamo_remesher pamo_remesher;
+int pamo_remesher_create(pamo_remesher** out, int32_t device);
+int pamo_remesher_destroy(pamo_remesher* m);
+int pamo_remesh(pamo_remesher* m, const float* points, const int32_t* triangles, int32_t n_points, int32_t n_triangles,
+                int32_t resolution, const float* mean3, int32_t* out_n_points, int32_t* out_n_triangles,
+                pamo_stream stream);
+int pamo_remesh_result(pamo_remesher* m, float* verts, int32_t* tris, pamo_stream stream);
+
+/* The stage-2 loop of PaMO.run with an explicit face target (target_faces computed by the caller, e.g. from the
+ * input's face count when stage 1 replaced the mesh) and centring optional (off when the points are already
+ * centred, as after stage 1). Otherwise as pamo_simplify_device. */
+int pamo_simplify_device_target(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                                int32_t n_triangles, int64_t target_faces, int32_t tolerance, float threshold,
+                                int32_t iter, int32_t centre, int32_t* out_n_points, int32_t* out_n_triangles,
+                                int32_t* out_rounds, pamo_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,14 +13,17 @@ from .api import (  # noqa: F401
     CUDSP_Free,
     PaMO,
     PaSP,
+    Remesher,
     launch_count,
     pamo_simplify,
     round_faces,
     self_intersect,
     simplify,
+    simplify_to_target,
     tris_mean,
 )
 from ._native import PamoError  # noqa: F401
 
 __all__ = ["Context", "CUDSP", "CUDSP_Free", "PaMO", "PaSP", "PamoError", "simplify", "pamo_simplify", "round_faces", "launch_count",
-           "self_intersect", "tris_mean"]
+           "self_intersect", "tris_mean", "Remesher",
+           "simplify_to_target"]

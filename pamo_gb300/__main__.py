@@ -2,8 +2,8 @@
 
     python -m pamo_gb300 -i input.obj -o output.obj -r 0.1 [-mv 0] --disable_stage1 [--disable_stage3] [--metrics]
 
-Same flags as example.py (example.py:14-21). Stage 1 (remeshing) is not part of this build, so
-``--disable_stage1`` must be given. ``--metrics`` adds the reference's evaluation (metrics.py): Chamfer and
+Same flags as example.py (example.py:14-21); stage 1 runs the GPU remesher (``pamo_gb300.Remesher``) unless
+``--disable_stage1`` is given. ``--metrics`` adds the reference's evaluation (metrics.py): Chamfer and
 Hausdorff distances to the input, the smallest angle and the bad-triangle ratios of the output, and the
 reference's self-intersection check of the output.
 """
@@ -28,17 +28,13 @@ def main(argv=None) -> int:
     ap.add_argument("--disable_stage3", action="store_true", help="Disable safe projection")
     ap.add_argument("--metrics", action="store_true", help="Report the reference's evaluation metrics")
     args = ap.parse_args(argv)
-    if not args.disable_stage1:
-        print("stage 1 (remeshing) is not part of this build: pass --disable_stage1", file=sys.stderr)
-        return 2
-
     import pamo_gb300
     from pamo_gb300 import mesh_io, metrics
 
     V, F = mesh_io.load_obj(args.input)
     print(f"# of input verts : {len(V)}")
     print(f"# of input faces : {len(F)}")
-    model = pamo_gb300.PaMO((V, F), use_stage1=False, use_stage3=not args.disable_stage3)
+    model = pamo_gb300.PaMO((V, F), use_stage1=not args.disable_stage1, use_stage3=not args.disable_stage3)
     pts = torch.from_numpy(V).float().cuda()
     tri = torch.from_numpy(F).int().cuda()
     torch.cuda.synchronize()

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIBNAME = "libpamo_gb300.so"
 SOURCES = ["scan.cu", "lbvh.cu", "simp_round.cu", "pamo_ctx.cu", "noalloc.cu", "safe_project.cu", "batch.cu",
-           "metrics.cu"]
+           "metrics.cu", "remesh.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "--fmad=false", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2"]
 

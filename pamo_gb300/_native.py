@@ -42,6 +42,14 @@ SIGNATURES = {
     "pamo_legacy_round": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _F32, _F32, _I32, _P]),
     "pamo_point_mesh_sqdist": (ctypes.c_int, [_P, _I32, _P, _I32, _P, _I32, _P, _P, _P]),
     "pamo_face_min_angles": (ctypes.c_int, [_P, _P, _I32, _P, _P, _P]),
+    "pamo_remesher_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), _I32]),
+    "pamo_remesher_destroy": (ctypes.c_int, [_P]),
+    "pamo_remesh": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _I32, _P, ctypes.POINTER(ctypes.c_int32),
+                                   ctypes.POINTER(ctypes.c_int32), _P]),
+    "pamo_remesh_result": (ctypes.c_int, [_P, _P, _P, _P]),
+    "pamo_simplify_device_target": (ctypes.c_int, [_P, _P, _P, _I32, _I32, ctypes.c_int64, _I32, _F32, _I32, _I32,
+                                                   ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                                                   ctypes.POINTER(ctypes.c_int32), _P]),
     "pamo_tris_mean": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _P, _P]),
     "pamo_round_sizes": (ctypes.c_int, [_P, _PI32, _PI32, _PI32]),
     "pamo_round_outputs": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),

@@ -269,6 +269,74 @@ def simplify(points: torch.Tensor, triangles: torch.Tensor, ratio: float, tolera
     return verts, faces, rounds.value
 
 
+def simplify_to_target(points: torch.Tensor, triangles: torch.Tensor, target_faces: int, tolerance: int = 4,
+                       threshold: float = 1e-3, iter: int = 1000000, centre: bool = True, ctx: Context | None = None):
+    """The stage-2 loop with an explicit face target and optional centring (``pamo_simplify_device_target``).
+    Returns (verts, faces, rounds) as CUDA tensors."""
+    _check_input(points, "points", torch.float32)
+    _check_input(triangles, "triangles", torch.int32)
+    dev = points.device
+    if ctx is None:
+        ctx = Context(dev)
+    lib = _native.load()
+    with torch.cuda.device(dev):
+        st = _stream(dev)
+        onp, ont, rounds = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _native.check(
+            lib.pamo_simplify_device_target(ctx.handle, _ptr(points), _ptr(triangles), int(points.shape[0]),
+                                            int(triangles.shape[0]), int(target_faces), int(tolerance),
+                                            float(threshold), int(iter), int(bool(centre)), ctypes.byref(onp),
+                                            ctypes.byref(ont), ctypes.byref(rounds), st),
+            ctx.handle,
+        )
+        verts = torch.empty((onp.value, 3), dtype=torch.float32, device=dev)
+        faces = torch.empty((ont.value, 3), dtype=torch.int32, device=dev)
+        _native.check(lib.pamo_simplify_result(ctx.handle, _ptr(verts), _ptr(faces), st), ctx.handle)
+    return verts, faces, rounds.value
+
+
+class Remesher:
+    """Stage 1 of ``PaMO.run`` (``PaMO.remesh``, simp_cuda/pamo/__init__.py:58-93) on the GPU
+    (``pamo_remesh``): a closed mesh at 0.9 voxel outside the input's surface on a ``resolution``^3 grid, in the
+    input's frame minus ``mean3``."""
+
+    def __init__(self, device=None):
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        h = ctypes.c_void_p()
+        _native.check(_native.load().pamo_remesher_create(ctypes.byref(h), self.device.index or 0))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _native.load().pamo_remesher_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def remesh(self, points: torch.Tensor, triangles: torch.Tensor, resolution: int, mean3):
+        _check_input(points, "points", torch.float32)
+        _check_input(triangles, "triangles", torch.int32)
+        m = np.ascontiguousarray(mean3, np.float32)
+        lib = _native.load()
+        with torch.cuda.device(self.device):
+            st = _stream(self.device)
+            nv, nf = ctypes.c_int32(), ctypes.c_int32()
+            r = lib.pamo_remesh(self._h, _ptr(points), _ptr(triangles), int(points.shape[0]), int(triangles.shape[0]),
+                                int(resolution), m.ctypes.data, ctypes.byref(nv), ctypes.byref(nf), st)
+            if r != _native.PAMO_OK:
+                raise _native.PamoError(r, "pamo_remesh")
+            v = torch.empty((nv.value, 3), dtype=torch.float32, device=self.device)
+            f = torch.empty((nf.value, 3), dtype=torch.int32, device=self.device)
+            r = lib.pamo_remesh_result(self._h, _ptr(v), _ptr(f), st)
+            if r != _native.PAMO_OK:
+                raise _native.PamoError(r, "pamo_remesh_result")
+        return v, f
+
+
 def pamo_simplify(verts, tris, threshold: float = 1e-3):
     """The Blender add-on's whole-loop call (pamo_blender/cusimpinterface.cu:55-161) on host arrays: float32
     [N,3] vertices and int32 [M,3] triangles in, simplified (verts, tris) NumPy arrays out. No centring, no
@@ -335,14 +403,15 @@ def round_faces(ctx: Context, rounds: int):
 class PaMO(torch.nn.Module):
     """Drop-in for ``pamo.PaMO`` (simp_cuda/pamo/__init__.py:18-178).
 
-    ``input_mesh`` is any object with ``vertices`` and ``faces`` (a trimesh, or a ``(V, F)`` pair). Stage 1
-    (SDF remeshing) is not part of this build: ``use_stage1=True`` raises ``NotImplementedError``.
+    ``input_mesh`` is any object with ``vertices`` and ``faces`` (a trimesh, or a ``(V, F)`` pair). Stage 1 runs
+    on the GPU (``Remesher``: narrow-band distance field, flood-filled sign, dual extraction) in place of the
+    reference's torchcumesh2sdf and pdmc, which are absent; its output therefore differs from the reference's
+    in vertex placement and count (parity unpinned), while the stage-2 target stays ``ratio`` times the input's
+    face count as in the reference.
     """
 
     def __init__(self, input_mesh, use_stage1: bool = True, use_stage3: bool = True):
         super().__init__()
-        if use_stage1:
-            raise NotImplementedError("stage 1 (SDF + dual marching cubes remeshing) is not provided; pass use_stage1=False")
         self.use_stage1 = use_stage1
         self.use_stage3 = use_stage3
         V, F = _mesh_arrays(input_mesh)
@@ -350,6 +419,8 @@ class PaMO(torch.nn.Module):
         self.gt_mesh = (np.array(V, copy=True), np.array(F, copy=True))
         self.target_faces = None
         self._ctx: Context | None = None
+        self._remesher: Remesher | None = None
+        self.R = 256  # vol2mesh resolution (pamo/__init__.py:50-52), lowered for small targets in run()
         self.last_rounds = 0
         self.system = None  # the reference builds its Stage3System here; it is made on the first run's device
         if use_stage3:
@@ -361,7 +432,23 @@ class PaMO(torch.nn.Module):
         self.target_faces = max(int(ratio * len(triangles)), min_verts)
         if self._ctx is None or self._ctx.device != points.device:
             self._ctx = Context(points.device)
-        verts, faces, rounds = simplify(points, triangles, ratio, tolerance, threshold, iter, min_verts, ctx=self._ctx)
+        if self.use_stage1:
+            # stage 1 (pamo/__init__.py:104-113): remesh the centred input, then simplify without centring again,
+            # and add the centre back at the end
+            if self.target_faces <= 1000:
+                self.R = 128
+            if self.target_faces <= 50:
+                self.R = 64
+            if self._remesher is None or self._remesher.device != points.device:
+                self._remesher = Remesher(points.device)
+            mean = tris_mean(points, triangles, ctx=self._ctx)
+            rv, rf = self._remesher.remesh(points, triangles, self.R, mean)
+            verts, faces, rounds = simplify_to_target(rv, rf, self.target_faces, tolerance, threshold, iter,
+                                                      centre=False, ctx=self._ctx)
+            verts = verts + torch.from_numpy(mean).to(verts.device)
+        else:
+            verts, faces, rounds = simplify(points, triangles, ratio, tolerance, threshold, iter, min_verts,
+                                            ctx=self._ctx)
         self.last_rounds = rounds
         verts_np = verts.cpu().numpy()
         faces_np = faces.cpu().numpy()

@@ -1053,6 +1053,22 @@ int pamo_simplify_device(pamo_ctx* ctx, const float* points, const int32_t* tria
                          out_n_triangles, out_rounds, (cudaStream_t)stream);
 }
 
+int pamo_simplify_device_target(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                                int32_t n_triangles, int64_t target_faces, int32_t tolerance, float threshold,
+                                int32_t iter, int32_t centre, int32_t* out_n_points, int32_t* out_n_triangles,
+                                int32_t* out_rounds, pamo_stream stream) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (n_points < 1 || n_triangles < 1 || !points || !triangles)
+        return ctx->fail(PAMO_ERR_INVALID_ARG, "invalid sizes or null pointers");
+    cudaSetDevice(ctx->device);
+    LoopOptions opt;
+    opt.target = (long long)target_faces;
+    opt.centre = centre != 0;
+    return simplify_loop(ctx, points, triangles, n_points, n_triangles, opt, tolerance, threshold, iter, out_n_points,
+                         out_n_triangles, out_rounds, (cudaStream_t)stream);
+}
+
 int pamo_simplify(float* in_verts, int* in_tris, float* out_verts, int* out_tris, int* in_out_nv_ni, float threshold) {
     if (!in_verts || !in_tris || !out_verts || !out_tris || !in_out_nv_ni) return PAMO_ERR_INVALID_ARG;
     const int nv = in_out_nv_ni[0], nt = in_out_nv_ni[1];
