@@ -566,7 +566,7 @@ def main():
                          "stage3_max_err_over_bbox_diag": float(np.abs(got - ref3).max() / diag),
                          "against": "float64 oracle run of stage 3 on the same stage-2 output",
                          "arithmetic": "float32 with compensated (two-sum) energy and CG sums; float64 for the "
-                                       "normalisation, Voronoi weights and angle test"}
+                                       "CCD step, the normalisation, Voronoi weights and angle test"}
         # output checks: exact-predicate self-intersection count and Hausdorff distance to the input
         fin = (prof_out[0].double().cpu().numpy(), prof_out[1].cpu().numpy())
         diag_in = float(np.linalg.norm(v.max(0) - v.min(0)))

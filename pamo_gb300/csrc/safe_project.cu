@@ -1648,6 +1648,204 @@ __global__ void k_accd(const float4* __restrict__ x, const float4* __restrict__ 
     }
 }
 
+// ------------------------------------------------------------------ CCD in float64
+// The precision mode's "float64 CCD roots": the additive CCD above with positions, step directions, the
+// pair classification, the distances and the advancement in float64 (Warp's kernels run it in float32). The
+// resulting step is rounded down to float, so that it never exceeds the float64 time of impact bound.
+__device__ __forceinline__ D3 d3(float4 a) { return {(double)a.x, (double)a.y, (double)a.z}; }
+__device__ __forceinline__ D3 operator+(D3 a, D3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ D3 operator-(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ D3 operator*(double s, D3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ D3 operator/(D3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ D3 cross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+__device__ __forceinline__ double length_sq(D3 a) { return dot(a, a); }
+__device__ __forceinline__ double length(D3 a) { return sqrt(dot(a, a)); }
+__device__ __forceinline__ D3 normalize(D3 a) {
+    const double l = length(a);
+    return l > 0.0 ? a / l : D3{0.0, 0.0, 0.0};
+}
+__device__ __forceinline__ double wstep(double x) { return x < 0.0 ? 1.0 : 0.0; }
+__device__ __forceinline__ double pt_distance(D3 x0, D3 x1, D3 x2, D3 x3) {
+    return fabs(dot(x0 - x1, normalize(cross(x2 - x1, x3 - x1))));
+}
+__device__ __forceinline__ double ee_distance(D3 x0, D3 x1, D3 x2, D3 x3) {
+    return fabs(dot(x0 - x2, normalize(cross(x1 - x0, x3 - x2))));
+}
+__device__ __forceinline__ double pe_distance(D3 x0, D3 x1, D3 x2) { return length(cross(x1 - x0, x2 - x0)) / length(x1 - x2); }
+__device__ __forceinline__ double pp_distance(D3 x0, D3 x1) { return length(x1 - x0); }
+
+__device__ int pt_classify(D3 x0, D3 x1, D3 x2, D3 x3) {
+    D3 x10 = x0 - x1;
+    const D3 x12 = x2 - x1, x13 = x3 - x1;
+    const double area_sq = length_sq(cross(x12, x13));
+    if (area_sq <= 1e-6 * (length_sq(x12) * length_sq(x13)) || area_sq <= 1e-16) {
+        const double e1 = length(x10), e2 = length(x0 - x2), e3 = length(x0 - x3);
+        if (e1 < e2) return e1 < e3 ? PT_PP01 : PT_PP03;
+        return e2 < e3 ? PT_PP02 : PT_PP03;
+    }
+    const D3 n = normalize(cross(x12, x13));
+    const D3 xp = x0 - dot(n, x10) * n;
+    x10 = xp - x1;
+    const D3 x20 = xp - x2, x30 = xp - x3;
+    const double a00 = dot(x12, x12), a01 = dot(x12, x13), a11 = dot(x13, x13);
+    const double b0 = dot(x10, x12), b1 = dot(x10, x13);
+    const double det = a00 * a11 - a01 * a01;
+    const double beta = b0 * a11 - b1 * a01;
+    const double gamma = a00 * b1 - b0 * a01;
+    const double alpha = det - beta - gamma;
+    const double nneg = wstep(alpha) + wstep(beta) + wstep(gamma);
+    if (nneg == 0.0) return PT_PT;
+    if (nneg == 1.0) {
+        if (alpha < 0.0) {
+            const D3 x23 = x3 - x2, x20b = x0 - x2;
+            const double dr = dot(x23, x20b);
+            if (dr < 0.0) return PT_PP02;
+            if (dr > dot(x23, x23)) return PT_PP03;
+            return PT_PE023;
+        } else if (beta < 0.0) {
+            const D3 x31 = x1 - x3, x30b = x0 - x3;
+            const double dr = dot(x31, x30b);
+            if (dr < 0.0) return PT_PP03;
+            if (dr > dot(x31, x31)) return PT_PP01;
+            return PT_PE031;
+        } else if (gamma < 0.0) {
+            const double dr = dot(x12, x10);
+            if (dr < 0.0) return PT_PP01;
+            if (dr > dot(x12, x12)) return PT_PP02;
+            return PT_PE012;
+        }
+        return -1;
+    }
+    if (alpha >= 0.0) {
+        const double d12 = dot(x12, x10), d13 = dot(x13, x10);
+        if (d12 > 0.0 && d13 <= 0.0) return dot(x12, x20) > 0.0 ? PT_PP02 : PT_PE012;
+        if (d13 > 0.0 && d12 <= 0.0) return dot(x13, x30) > 0.0 ? PT_PP03 : PT_PE031;
+        return PT_PP01;
+    } else if (beta >= 0.0) {
+        const D3 x23 = x3 - x2, x21 = x1 - x2;
+        const double d23 = dot(x23, x20), d21 = dot(x21, x20);
+        if (d23 > 0.0 && d21 <= 0.0) return dot(x23, x30) > 0.0 ? PT_PP03 : PT_PE023;
+        if (d21 > 0.0 && d23 <= 0.0) return dot(x21, x10) > 0.0 ? PT_PP01 : PT_PE012;
+        return PT_PP02;
+    }
+    const D3 x31 = x1 - x3, x32 = x2 - x3;
+    const double d31 = dot(x31, x30), d32 = dot(x32, x30);
+    if (d31 > 0.0 && d32 <= 0.0) return dot(x31, x10) > 0.0 ? PT_PP01 : PT_PE031;
+    if (d32 > 0.0 && d31 <= 0.0) return dot(x32, x20) > 0.0 ? PT_PP02 : PT_PE023;
+    return PT_PP03;
+}
+
+__device__ double pt_pair_distance(D3 x0, D3 x1, D3 x2, D3 x3, int t) {
+    switch (t) {
+        case PT_PT: return pt_distance(x0, x1, x2, x3);
+        case PT_PP01: return pp_distance(x0, x1);
+        case PT_PP02: return pp_distance(x0, x2);
+        case PT_PE012: return pe_distance(x0, x1, x2);
+        case PT_PP03: return pp_distance(x0, x3);
+        case PT_PE031: return pe_distance(x0, x3, x1);
+        case PT_PE023: return pe_distance(x0, x2, x3);
+    }
+    return 1e9;
+}
+
+__device__ int ee_classify(D3 x0, D3 x1, D3 x2, D3 x3, double sin_thres) {
+    const D3 e0 = x0 - x1, e1 = x2 - x3;
+    const double e0_sq = dot(e0, e0), e1_sq = dot(e1, e1);
+    const double a00 = e0_sq, a01 = -dot(e0, e1), a10 = dot(e0, e1), a11 = -e1_sq;
+    const double b0 = dot(x3 - x1, e0), b1 = dot(x3 - x1, e1);
+    const double mu0 = -(b0 * a11 - b1 * a01);
+    const double mu1 = -(a00 * b1 - a10 * b0);
+    const double detA = -(a00 * a11 - a01 * a10);
+    const double edge_sin = length(cross(normalize(e0), normalize(e1)));
+    if (mu0 >= 0.0 && mu0 <= detA && mu1 >= 0.0 && mu1 <= detA && edge_sin >= sin_thres && e0_sq > 1e-15 && e1_sq > 1e-15)
+        return EE_EE;
+    double best = 1e9;
+    int type = -1;
+    auto consider = [&](double d, int t) {
+        if (d < best) {
+            best = d;
+            type = t;
+        }
+    };
+    const double t0 = dot(x0 - x3, e1);
+    if (t0 >= e1_sq) consider(pp_distance(x0, x2), EE_PP02);
+    else if (t0 <= 0.0) consider(pp_distance(x0, x3), EE_PP03);
+    else consider(pe_distance(x0, x2, x3), EE_PE023);
+    const double t1 = dot(x1 - x3, e1);
+    if (t1 >= e1_sq) consider(pp_distance(x1, x2), EE_PP12);
+    else if (t1 <= 0.0) consider(pp_distance(x1, x3), EE_PP13);
+    else consider(pe_distance(x1, x2, x3), EE_PE123);
+    const double t2 = dot(x2 - x1, e0);
+    if (t2 >= e0_sq) consider(pp_distance(x2, x0), EE_PP02);
+    else if (t2 <= 0.0) consider(pp_distance(x2, x1), EE_PP12);
+    else consider(pe_distance(x2, x0, x1), EE_PE201);
+    const double t3 = dot(x3 - x1, e0);
+    if (t3 >= e0_sq) consider(pp_distance(x3, x0), EE_PP03);
+    else if (t3 <= 0.0) consider(pp_distance(x3, x1), EE_PP13);
+    else consider(pe_distance(x3, x0, x1), EE_PE301);
+    return type;
+}
+
+__device__ double ee_pair_distance(D3 x0, D3 x1, D3 x2, D3 x3, int t) {
+    switch (t) {
+        case EE_PP02: return pp_distance(x0, x2);
+        case EE_PP03: return pp_distance(x0, x3);
+        case EE_PP12: return pp_distance(x1, x2);
+        case EE_PP13: return pp_distance(x1, x3);
+        case EE_PE023: return pe_distance(x0, x2, x3);
+        case EE_PE123: return pe_distance(x1, x2, x3);
+        case EE_PE201: return pe_distance(x2, x0, x1);
+        case EE_PE301: return pe_distance(x3, x0, x1);
+        case EE_EE: return ee_distance(x0, x1, x2, x3);
+    }
+    return 1e9;
+}
+
+__global__ void k_accd_fp64(const float4* __restrict__ x, const float4* __restrict__ vel, const int4* __restrict__ cidx,
+                            const int2* __restrict__ ctype, SolverScalars* sc, double slackness, double thickness,
+                            int max_iters, double ee_thres) {
+    if (sc->abort) return;
+    const int n = sc->n_contacts;
+    for (int b = gtid(); b < n; b += gstride()) {
+        const int4 id = cidx[b];
+        D3 x0 = d3(x[id.x]), x1 = d3(x[id.y]), x2 = d3(x[id.z]), x3 = d3(x[id.w]);
+        D3 v0 = d3(vel[id.x]), v1 = d3(vel[id.y]), v2 = d3(vel[id.z]), v3 = d3(vel[id.w]);
+        const int type1 = ctype[b].x;
+        const D3 va = (v0 + v1 + v2 + v3) / 4.0;
+        v0 = v0 - va; v1 = v1 - va; v2 = v2 - va; v3 = v3 - va;
+        double lv;
+        if (type1 == BLOCK_PT) lv = length(v0) + fmax(length(v1), fmax(length(v2), length(v3)));
+        else lv = fmax(length(v0), length(v1)) + fmax(length(v2), length(v3));
+        if (lv < 1e-12) continue;
+        auto dist = [&]() {
+            if (type1 == BLOCK_PT) return pt_pair_distance(x0, x1, x2, x3, pt_classify(x0, x1, x2, x3));
+            return ee_pair_distance(x0, x1, x2, x3, ee_classify(x0, x1, x2, x3, ee_thres));
+        };
+        double d = dist();
+        double dsq = d * d;
+        double dmt = fmax((dsq - thickness * thickness) / (sqrt(dsq) + thickness), 0.0);
+        const double gap = (1.0 - slackness) * dmt;
+        double t = 0.0;
+        double tl = slackness * dmt / lv;
+        int it = 0;
+        while (true) {
+            x0 = x0 + tl * v0; x1 = x1 + tl * v1; x2 = x2 + tl * v2; x3 = x3 + tl * v3;
+            d = dist();
+            dsq = d * d;
+            dmt = fmax((dsq - thickness * thickness) / (sqrt(dsq) + thickness), 0.0);
+            if ((it > 0 && dmt <= gap) || it >= max_iters) {
+                atomicMin((int*)&sc->ccd_step, __float_as_int(__double2float_rd(t)));  // t >= 0: int order = float order
+                break;
+            }
+            t = t + tl;
+            if (t > 1.0) break;
+            tl = 0.8 * dmt / lv;
+            ++it;
+        }
+    }
+}
+
 // line_search_kernel (solver_kernels.py:52-66): q = q0 + ccd_step 0.5^n p unless a shorter step already
 // lowered the energy
 __global__ void k_line_search(const float4* __restrict__ q0, const float4* __restrict__ p, const SolverScalars* sc,
@@ -1966,8 +2164,12 @@ void Stage3::newton_iteration() {
     note_launch();
     k_before_ccd<<<1, 1, 0, s>>>(sc);
     note_launch();
-    k_accd<<<gC, kT, 0, s>>>(q, p, c_idx, c_type, sc, P.ccd_slackness, P.ccd_thickness, P.ccd_max_iters,
-                            P.ee_classify_thres);
+    if (P.ccd_fp64)
+        k_accd_fp64<<<gC, kT, 0, s>>>(q, p, c_idx, c_type, sc, (double)P.ccd_slackness, (double)P.ccd_thickness,
+                                      P.ccd_max_iters, (double)P.ee_classify_thres);
+    else
+        k_accd<<<gC, kT, 0, s>>>(q, p, c_idx, c_type, sc, P.ccd_slackness, P.ccd_thickness, P.ccd_max_iters,
+                                P.ee_classify_thres);
     note_launch();
     for (int n = 0; n < P.n_line_search_iters; ++n) {
         k_line_search<<<grid_for(NP, kT), kT, 0, s>>>(q_prev_newton, p, sc, n, NP, q);
@@ -2232,6 +2434,7 @@ int pamo_stage3_set_param(pamo_stage3* s, const char* name, double value) {
     else if (n == "min_angle_thres") P.min_angle_thres = (float)value;
     else if (n == "max_blocks") P.max_blocks = (long long)value;
     else if (n == "use_cuda_graph") s->solver.use_graph = value != 0.0;
+    else if (n == "ccd_fp64") P.ccd_fp64 = value != 0.0;
     else if (n == "cg_mode") s->solver.cg_mode = (int)value;  // 0/1 grid-cooperative (128), 2 cluster, 3 (256)
     else {
         s->solver.err = "unknown stage-3 parameter: " + n;

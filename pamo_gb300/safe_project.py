@@ -44,6 +44,8 @@ class Stage3Config:
     mesh2gt_dist_stiffness: float = 1e3
     min_angle_thres: float = 0.0
     max_blocks: int = 1 << 25
+    # this build's precision mode: the CCD step in float64 (False: float32, as Warp's kernels compute it)
+    ccd_fp64: bool = True
 
 
 class Stage3System:
