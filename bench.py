@@ -544,6 +544,7 @@ def main():
         return 0
 
     cpu = None
+    cpu_qem = None
     precision = None
     quality = None
     if not args.no_cpu_baseline:
@@ -567,6 +568,17 @@ def main():
                          "against": "float64 oracle run of stage 3 on the same stage-2 output",
                          "arithmetic": "float32 with compensated (two-sum) energy and CG sums; float64 for the "
                                        "CCD step, the normalisation, Voronoi weights and angle test"}
+        # conventional CPU baseline: sequential priority-queue QEM (one host thread) on a time budget, projected to
+        # the collapses the job needs (each removes two faces)
+        t_q = time.perf_counter()
+        n_col, _left = orc.cpu_qem(v, f, max(int(ratio * len(f)), 0), 8.0)
+        dt_q = time.perf_counter() - t_q
+        need = max(1, (len(f) - int(ratio * len(f))) // 2)
+        proj_q = dt_q * need / max(1, n_col)
+        cpu_qem = {"value": len(f) / proj_q, "unit": "input faces/s", "cores": 1,
+                   "kind": "sequential priority-queue QEM (Garland-Heckbert, midpoint placement, link and flip checks)",
+                   "sample": f"{n_col} collapses in {dt_q:.1f} s including set-up; projected to the {need} collapses "
+                             f"of the job"}
         # output checks: exact-predicate self-intersection count and Hausdorff distance to the input
         fin = (prof_out[0].double().cpu().numpy(), prof_out[1].cpu().numpy())
         diag_in = float(np.linalg.norm(v.max(0) - v.min(0)))
@@ -598,6 +610,7 @@ def main():
         "precision": precision,
         "quality": quality,
         "cpu_baseline": cpu,
+        "cpu_qem": cpu_qem,
         "e2e": {"value": e2e, "unit": "input faces/s", "h2d_bytes_per_step": int(v.nbytes + f.nbytes),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),

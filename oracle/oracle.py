@@ -44,6 +44,8 @@ def lib():
         L.check_self_intersections_all_pairs.restype = LL
         L.hausdorff.argtypes = [P, I, P, I, P, I, P, I, P]
         L.hausdorff.restype = D
+        L.cpu_qem_simplify.argtypes = [P, I, P, I, LL, D, P]
+        L.cpu_qem_simplify.restype = LL
         L.exact_orient3d.argtypes = [P]
         L.exact_orient3d.restype = I
         L.s3_oracle_run.argtypes = [P, P, I, I, P, P, I, I, I, P, P, P]
@@ -306,3 +308,13 @@ def hausdorff(va, fa, vb, fb):
     out = np.zeros(2, np.float64)
     h = lib().hausdorff(_p(A), len(A), _p(FA), len(FA), _p(B), len(B), _p(FB), len(FB), _p(out))
     return float(h), float(out[0]), float(out[1])
+
+
+def cpu_qem(points, tris, target_faces: int, time_budget_s: float = 0.0):
+    """The sequential priority-queue QEM baseline (oracle/cpu_qem.cpp): (collapses, faces left)."""
+    P = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    T = np.ascontiguousarray(tris, np.int32).reshape(-1, 3)
+    left = ctypes.c_longlong()
+    n = lib().cpu_qem_simplify(_p(P), len(P), _p(T), len(T), int(target_faces), float(time_budget_s),
+                               ctypes.byref(left))
+    return int(n), int(left.value)
