@@ -256,7 +256,12 @@ def run_batch(args):
         plain_out.append((V, Fo))
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
-    b = Batch(dev, workers=args.workers)
+    workers = args.workers
+    if workers == 0:  # tune the worker count on a sample of the batch first
+        from pamo_gb300 import autotune
+
+        workers = autotune.tune_batch(meshes[::4], ratios[::4])["best"]
+    b = Batch(dev, workers=workers)
     for _ in range(args.warmup):
         out = b.simplify_csr(Pd, Td, voff, foff, ratios)
     stream = torch.cuda.current_stream(dev)
@@ -290,7 +295,7 @@ def run_batch(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "batch256: 256 star meshes, faces log-uniform 5k-200k (" + str(F0) + " faces), ratios "
                                "U[0.001,0.01], threshold 1e-3, tolerance 4, min_verts 0",
-                   "workers": args.workers, "parallelism": "one GPU, worker contexts on separate streams"},
+                   "workers": workers, "parallelism": "one GPU, worker contexts on separate streams"},
         "plain": {"value": F0 / plain_s, "seconds": plain_s, "how": "one context, one mesh after the other"},
         "vs_plain": (F0 / (float(np.mean(ms)) / 1000.0)) / (F0 / plain_s),
         "identical_to_plain": bool(identical),
@@ -347,6 +352,10 @@ def run_serve(args):
         srv.close()
         return lat, wall, stats
 
+    if args.workers == 0:
+        from pamo_gb300 import autotune
+
+        args.workers = autotune.best_workers()
     lat, wall, stats = stream(args.workers)
     lat1, wall1, _ = stream(1)
     line = {
@@ -373,7 +382,8 @@ def main():
     ap.add_argument("--config", default="plain_large", choices=sorted(CONFIGS) + ["batch256", "serve"])
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workers", type=int, default=16, help="worker contexts for --config batch256 / serve")
+    ap.add_argument("--workers", type=int, default=16,
+                    help="worker contexts for --config batch256 / serve (0: tuned on a sample first)")
     ap.add_argument("--requests", type=int, default=2000, help="requests for --config serve")
     ap.add_argument("--one-job", action="store_true",
                     help="run one job of the configuration and exit (for profiler captures; prints no JSON)")

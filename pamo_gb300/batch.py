@@ -23,8 +23,12 @@ def _err(lib_fn, handle) -> str:
 class Batch:
     """A worker pool for batches of meshes in CSR form (``pamo_batch_*``)."""
 
-    def __init__(self, device=None, workers: int = 16):
+    def __init__(self, device=None, workers: int | None = None):
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        if workers is None:
+            from .autotune import best_workers
+
+            workers = best_workers()
         lib = _native.load()
         h = ctypes.c_void_p()
         st = lib.pamo_batch_create(ctypes.byref(h), self.device.index or 0, int(workers))
@@ -89,7 +93,7 @@ def unpack(points, triangles, voff, foff):
 
 
 def simplify_batch(meshes, ratios, tolerance: int = 4, threshold: float = 1e-3, iter: int = 1000000,
-                   min_verts: int = 0, workers: int = 16, batch: Batch | None = None):
+                   min_verts: int = 0, workers: int | None = None, batch: Batch | None = None):
     """Simplify a list of (V, F) meshes; returns a list of (V float32, F int32) NumPy results."""
     batch = batch or Batch(workers=workers)
     P, T, voff, foff = pack(meshes)
@@ -102,8 +106,12 @@ class Server:
     """A request loop (``pamo_server_*``): requests are admitted in arrival order while their estimated device
     bytes fit ``hbm_budget_bytes``, then run on the next free worker."""
 
-    def __init__(self, device=None, workers: int = 16, hbm_budget_bytes: int = 80 << 30):
+    def __init__(self, device=None, workers: int | None = None, hbm_budget_bytes: int = 80 << 30):
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        if workers is None:
+            from .autotune import best_workers
+
+            workers = best_workers()
         lib = _native.load()
         h = ctypes.c_void_p()
         st = lib.pamo_server_create(ctypes.byref(h), self.device.index or 0, int(workers), int(hbm_budget_bytes))

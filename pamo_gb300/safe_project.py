@@ -65,6 +65,9 @@ class Stage3System:
         self._lib = lib
         self._h = h
         self._applied = None
+        from .autotune import best_cg_mode
+
+        lib.pamo_stage3_set_param(h, b"cg_mode", float(best_cg_mode()))
 
     def __del__(self):
         h = getattr(self, "_h", None)

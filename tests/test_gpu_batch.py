@@ -93,3 +93,15 @@ def test_job_bytes_covers_a_context():
                             4, 1e-3, 1000000, 0, ctx=ctx)
         need = ctx.device_bytes() + 2 * (12 * len(v) + 12 * len(f))
         assert need <= Server.job_bytes(len(v), len(f))
+
+
+def test_autotune_picks_a_candidate_and_caches_it(tmp_path, monkeypatch):
+    from pamo_gb300 import autotune
+    from pamo_gb300.synth import star_mesh
+
+    monkeypatch.setenv("PAMO_GB300_TUNE", str(tmp_path / "tune.json"))
+    meshes = [star_mesh(8 + i, 4, lambda l: 0.03, i) for i in range(6)]
+    res = autotune.tune_batch(meshes, 0.05, candidates=(2, 4), repeats=1)
+    assert res["best"] in (2, 4) and res[2] > 0 and res[4] > 0
+    assert autotune.best_workers() == res["best"]
+    assert (tmp_path / "tune.json").exists()
