@@ -935,9 +935,13 @@ struct EnergyArgs {
 // mesh2gt_pp_distance_energy_kernel (distance_energy.py:6-17), elastic_energy_kernel (elastic_energy.py:40-80),
 // hinge_energy_kernel (hinge_energy.py:60-88), collision_energy_kernel (collision_energy.py:49-99: the contact
 // is reclassified at x and its type and distance stored for the gradient).
+// ls_n >= 1: the energy of line-search trial ls_n, skipped (like the trial itself, k_line_search) once an
+// earlier trial was accepted: q and therefore the energy, distances and contact types are already those of the
+// accepted trial. Every block reads the same flags: the last block writes sc->energy only after all have started.
 __global__ void __launch_bounds__(kT) k_energy(const float4* __restrict__ x, EnergyArgs A, SolverScalars* sc,
-                                               float2* partial) {
+                                               float2* partial, int ls_n) {
     if (sc->abort) return;
+    if (ls_n > 0 && sc->energy < sc->energy_prev) return;
     const int nc = sc->n_contacts;
     const long long e1 = A.np, e2 = e1 + A.nt, e3 = e2 + A.nh, total = e3 + nc;
     CSum acc;
@@ -1249,14 +1253,25 @@ __device__ __forceinline__ F3 cg_dir(const float4* __restrict__ z, const float4*
     return f3(z[j]) + s * f3(vprev[j]);
 }
 
+// The vertex ids of element g of hvp_elements (a triangle, hinge or contact; zeros for a vertex term or past
+// the end). They do not change during a solve, so a thread loads those of its first element once.
+__device__ __forceinline__ int4 element_ids(const HvpArgs& A, int nc, long long g) {
+    const long long e1 = A.np, e2 = e1 + A.nt, e3 = e2 + A.nh, total = e3 + nc;
+    if (g < e1 || g >= total) return make_int4(0, 0, 0, 0);
+    if (g < e2) return A.tri[g - e1];
+    if (g < e3) return A.hinge[g - e2];
+    return A.cidx[g - e3];
+}
+
 // Av += H v over the elements gtid, gtid + stride, ...; returns this thread's part of v.Av. The direction is
-// v = z + s v_prev, written to vout by the vertex terms.
+// v = z + s v_prev, written to vout by the vertex terms. ids0 = element_ids(first).
 __device__ __forceinline__ CSum hvp_elements(const float4* __restrict__ x, const HvpArgs& A, const float4* __restrict__ z,
                                              const float4* __restrict__ vprev, float4* vout, float4* Av, float s, int nc,
-                                             long long first, long long stride) {
+                                             long long first, long long stride, int4 ids0) {
     const long long e1 = A.np, e2 = e1 + A.nt, e3 = e2 + A.nh, total = e3 + nc;
     CSum acc;
     for (long long g = first; g < total; g += stride) {
+        const bool cached = g == first;
         if (g < e1) {
             const int i = (int)g;
             const F3 vi = cg_dir(z, vprev, s, i);
@@ -1266,7 +1281,7 @@ __device__ __forceinline__ CSum hvp_elements(const float4* __restrict__ x, const
             acc.add(dot(vi, vi * wi));
         } else if (g < e2) {
             const int f = (int)(g - e1);
-            const int4 t = A.tri[f];
+            const int4 t = cached ? ids0 : A.tri[f];
             const ElasticLocal L = elastic_local(x, t, A.area[f], A.invDm[f]);
             const F3 v0 = cg_dir(z, vprev, s, t.x), v1 = cg_dir(z, vprev, s, t.y), v2 = cg_dir(z, vprev, s, t.z);
             const F3 dx01 = v1 - v0, dx02 = v2 - v0;
@@ -1289,7 +1304,7 @@ __device__ __forceinline__ CSum hvp_elements(const float4* __restrict__ x, const
             acc.add(dot(v0, df0) + dot(v1, df1) + dot(v2, df2));
         } else if (g < e3) {
             const int h = (int)(g - e2);
-            const int4 id = A.hinge[h];
+            const int4 id = cached ? ids0 : A.hinge[h];
             const int ids[4] = {id.x, id.y, id.z, id.w};
             // H v with the fourth block row/column minus the sums of the first three: for w_a = v_a - v_3,
             // (H v)_a = sum_b A_ab w_b (a < 3), (H v)_3 = -sum_a (H v)_a, and v.H v = w.A w
@@ -1331,7 +1346,7 @@ __device__ __forceinline__ CSum hvp_elements(const float4* __restrict__ x, const
             const float dist = A.cd[b];
             if (dist >= A.d_hat) continue;
             const float c = barrier_d2(dist, A.d_hat) * A.kappa;
-            const int4 i = A.cidx[b];
+            const int4 i = cached ? ids0 : A.cidx[b];
             const int ids[4] = {i.x, i.y, i.z, i.w};
             F3 gg[4];
             float sd = 0.f;
@@ -1365,24 +1380,36 @@ __device__ __forceinline__ CSum cg_init_vertices(const float4* __restrict__ grad
     return acc;
 }
 
-// p += alpha v, r -= alpha Av when v.Av > 1e-16, z = r / diag, Av = 0; returns z.r part
+// The vertex values the p/r/z phase reads, loaded for a thread's first vertex before v.Av is known.
+struct PrzVertex {
+    float4 v, av, p, r, d;
+};
+
+__device__ __forceinline__ PrzVertex prz_load(const float4* __restrict__ v, const float4* Av,
+                                              const float4* __restrict__ hd, const float4* p, const float4* r, int i) {
+    return PrzVertex{v[i], Av[i], p[i], r[i], hd[i]};
+}
+
+// p += alpha v, r -= alpha Av when v.Av > 1e-16, z = r / diag, Av = 0; returns z.r part. `pre` holds the values
+// of vertex `first` (when first < np), loaded before the block partials of v.Av were summed.
 __device__ __forceinline__ CSum cg_prz_vertices(const float4* __restrict__ v, float4* Av, const float4* __restrict__ hd,
                                                 int np, float4* p, float4* r, float4* z, float zr, float vAv, int first,
-                                                int stride) {
+                                                int stride, const PrzVertex& pre) {
     const float alpha = zr / vAv;
     CSum acc;
     for (int i = first; i < np; i += stride) {
-        float4 ri = r[i];
+        const bool cached = i == first;
+        float4 ri = cached ? pre.r : r[i];
         if (vAv > 1e-16f) {
-            const float4 vi = v[i], avi = Av[i];
-            float4 pi = p[i];
+            const float4 vi = cached ? pre.v : v[i], avi = cached ? pre.av : Av[i];
+            float4 pi = cached ? pre.p : p[i];
             pi.x += alpha * vi.x; pi.y += alpha * vi.y; pi.z += alpha * vi.z;
             ri.x -= alpha * avi.x; ri.y -= alpha * avi.y; ri.z -= alpha * avi.z;
             p[i] = pi;
             r[i] = ri;
         }
         Av[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 d = hd[i];
+        const float4 d = cached ? pre.d : hd[i];
         const float4 zz = make_float4(ri.x / d.x, ri.y / d.y, ri.z / d.z, 0.f);
         z[i] = zz;
         acc.add(zz.x * ri.x + zz.y * ri.y + zz.z * ri.z);
@@ -1396,31 +1423,25 @@ __device__ __forceinline__ unsigned ld_acquire(volatile unsigned* p) {
     return v;
 }
 
-// Barrier across all blocks of a cooperative launch (co-residency guaranteed). The spin is bounded: on
-// time-out it records kErrIterLimit in *status and lets the block go on (the host then reports the error).
-// Arrival is a release (the block's writes, ordered before it by the block barrier, become visible with it),
-// departure an acquire; acq_rel fences are enough for that and cheaper than sequentially consistent ones.
-__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
-
-__device__ __forceinline__ void grid_barrier(unsigned* count, volatile unsigned* gen, int* status) {
+// Barrier across all blocks of a cooperative launch (co-residency guaranteed), sense-reversing on one counter
+// that starts at zero: block 0 adds 2^31 - (gridDim.x - 1) and every other block adds 1, so the counter's top
+// bit flips exactly when the last block arrives and its low 31 bits are zero again for the next barrier (no
+// reset, nothing to do for the last arrival but its own add). Arrival is a release (the block's writes,
+// ordered before it by the block barrier, become visible with it), the poll an acquire. The spin is bounded:
+// on time-out it records kErrIterLimit in *status and lets the block go on (the host then reports the error).
+__device__ __forceinline__ void grid_barrier(unsigned* count, int* status) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned g = *gen;
-        fence_acq_rel_gpu();
-        if (atomicAdd(count, 1u) == gridDim.x - 1) {
-            *count = 0;
-            fence_acq_rel_gpu();
-            atomicAdd((unsigned*)gen, 1u);
-        } else {
-            long long spins = 0;
-            while (ld_acquire(gen) == g) {
-                if (++spins > (1ll << 28)) {
-                    atomicOr(status, kErrIterLimit);
-                    break;
-                }
+        const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
+        unsigned old;
+        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(count), "r"(inc) : "memory");
+        long long spins = 0;
+        while (((ld_acquire(count) ^ old) & 0x80000000u) == 0u) {
+            if (++spins > (1ll << 28)) {
+                atomicOr(status, kErrIterLimit);
+                break;
             }
         }
-        fence_acq_rel_gpu();
     }
     __syncthreads();
 }
@@ -1449,7 +1470,7 @@ __device__ __forceinline__ void store_partial(CSum acc, float2* partial) {
 }
 
 struct CgState {
-    unsigned count, gen;
+    unsigned count;  // grid_barrier's counter, zeroed before each stage-3 run
 };
 
 // The whole Jacobi PCG solve (cg_solver.py:96-158, n_cg_iters iterations) as one cooperative kernel: each
@@ -1465,8 +1486,9 @@ __global__ void __launch_bounds__(kThreads) k_cg_solve(const float4* __restrict_
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
     float2* part_a = partial;
     float2* part_b = partial + gridDim.x;
+    const int4 ids0 = element_ids(A, nc, tid);  // fixed for the whole solve
     store_partial(cg_init_vertices(grad, hd, A.np, p, r, z, v0, Av, tid, nthreads), part_a);
-    grid_barrier(&bar->count, &bar->gen, &sc->status);
+    grid_barrier(&bar->count, &sc->status);
     float zr = grid_partials_sum(part_a), zr_last = zr;
     for (int it = 0; it < n_iters; ++it) {
         const float4* vin = (it & 1) ? v1 : v0;
@@ -1474,11 +1496,14 @@ __global__ void __launch_bounds__(kThreads) k_cg_solve(const float4* __restrict_
         const float s_dir = it == 0 ? 0.f : zr / zr_last;
         // partials alternate between two buffers phase by phase: a buffer is rewritten only after the next
         // barrier, which every block reaches after it has read that buffer
-        store_partial(hvp_elements(x, A, z, vin, vout, Av, s_dir, nc, tid, nthreads), part_b);
-        grid_barrier(&bar->count, &bar->gen, &sc->status);
+        store_partial(hvp_elements(x, A, z, vin, vout, Av, s_dir, nc, tid, nthreads, ids0), part_b);
+        grid_barrier(&bar->count, &sc->status);
+        // this thread's vertex loads go out before the partials are summed (they do not depend on v.Av)
+        PrzVertex pre{};
+        if (tid < A.np) pre = prz_load(vout, Av, hd, p, r, tid);
         const float vAv = grid_partials_sum(part_b);
-        store_partial(cg_prz_vertices(vout, Av, hd, A.np, p, r, z, zr, vAv, tid, nthreads), part_a);
-        grid_barrier(&bar->count, &bar->gen, &sc->status);
+        store_partial(cg_prz_vertices(vout, Av, hd, A.np, p, r, z, zr, vAv, tid, nthreads, pre), part_a);
+        grid_barrier(&bar->count, &sc->status);
         zr_last = zr;
         zr = grid_partials_sum(part_a);
         if (blockIdx.x == 0 && threadIdx.x == 0) sc->v_A_v = vAv;
@@ -1531,14 +1556,17 @@ __global__ void __launch_bounds__(kClusterThreads) k_cg_cluster(const float4* __
         __syncthreads();
         return v;
     };
+    const int4 ids0 = element_ids(A, nc, tid);
     float zr = cluster_total(cg_init_vertices(grad, hd, A.np, p, r, z, v0, Av, tid, nthreads)), zr_last = zr;
     float vAv = 0.f;
     for (int it = 0; it < n_iters; ++it) {
         const float4* vin = (it & 1) ? v1 : v0;
         float4* vout = (it & 1) ? v0 : v1;
         const float s_dir = it == 0 ? 0.f : zr / zr_last;
-        vAv = cluster_total(hvp_elements(x, A, z, vin, vout, Av, s_dir, nc, tid, nthreads));
-        const float zr_new = cluster_total(cg_prz_vertices(vout, Av, hd, A.np, p, r, z, zr, vAv, tid, nthreads));
+        vAv = cluster_total(hvp_elements(x, A, z, vin, vout, Av, s_dir, nc, tid, nthreads, ids0));
+        PrzVertex pre{};
+        if (tid < A.np) pre = prz_load(vout, Av, hd, p, r, tid);
+        const float zr_new = cluster_total(cg_prz_vertices(vout, Av, hd, A.np, p, r, z, zr, vAv, tid, nthreads, pre));
         zr_last = zr;
         zr = zr_new;
     }
@@ -2047,7 +2075,7 @@ int Stage3::ensure_candidates(size_t npt, size_t nee) {
     return PAMO_OK;
 }
 
-void Stage3::launch_energy(const float4* x) {
+void Stage3::launch_energy(const float4* x, int ls_n) {
     const Stage3Params& P = params;
     EnergyArgs A;
     A.tgt = target; A.w = vweight; A.m2gt_k = P.mesh2gt_dist_stiffness; A.np = NP;
@@ -2059,7 +2087,7 @@ void Stage3::launch_energy(const float4* x) {
     A.ee_thres = P.ee_classify_thres;
     const long long total = (long long)NP + NT + NH + (long long)cap_c;
     const int g = (int)std::min<long long>(kRedBlocks, (total + kT - 1) / kT);
-    k_energy<<<g, kT, 0, stream>>>(x, A, sc, partial);
+    k_energy<<<g, kT, 0, stream>>>(x, A, sc, partial, ls_n);
     note_launch();
 }
 
@@ -2174,7 +2202,7 @@ void Stage3::newton_iteration() {
     for (int n = 0; n < P.n_line_search_iters; ++n) {
         k_line_search<<<grid_for(NP, kT), kT, 0, s>>>(q_prev_newton, p, sc, n, NP, q);
         note_launch();
-        launch_energy(q);
+        launch_energy(q, n);
     }
     k_iter_end<<<1, 1, 0, s>>>(sc);
     note_launch();

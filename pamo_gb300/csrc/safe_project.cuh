@@ -143,7 +143,7 @@ private:
     int graph_key[6] = {0, 0, 0, 0, 0, 0};
 
     void newton_iteration();  // enqueue one Newton iteration (system.py:425-459)
-    void launch_energy(const float4* x);
+    void launch_energy(const float4* x, int ls_n = -1);
 };
 
 }  // namespace pamo
