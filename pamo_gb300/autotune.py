@@ -3,7 +3,7 @@
 * ``tune_batch``: the number of worker contexts (one CUDA stream and host thread each) of ``Batch`` and
   ``Server``: too few leave the GPU idle between the small kernels of late rounds, too many split it into
   slices that each run slower. Each candidate simplifies the same sample of meshes; the fastest wins.
-* ``tune_stage3``: the thread-block size of the cooperative PCG of stage 3 (128 or 256 threads, the
+* ``tune_stage3``: the thread-block size of the cooperative PCG of stage 3 (128, 256 or 512 threads, the
   ``cg_mode`` option) on a sample projection.
 
 Results are stored in a JSON file (``$PAMO_GB300_TUNE`` or ``~/.cache/pamo_gb300/autotune.json``) under the
@@ -76,13 +76,14 @@ def tune_batch(meshes, ratios, candidates=(4, 8, 12, 16, 24, 32), repeats: int =
     return result
 
 
-def tune_stage3(gt_V, gt_F, V, F, n_iters: int = 5, store: bool = True) -> dict:
-    """Time stage 3 with the 128- and 256-thread cooperative PCG; returns {cg_mode: seconds, "best": mode}."""
+def tune_stage3(gt_V, gt_F, V, F, n_iters: int = 5, store: bool = True, modes=(0, 3, 4)) -> dict:
+    """Time stage 3 with the 128-, 256- and 512-thread cooperative PCG (cg_mode 0, 3, 4); returns
+    {cg_mode: seconds, "best": mode}."""
     from . import safe_project
 
     dev = torch.device("cuda", torch.cuda.current_device())
     result = {}
-    for mode in (0, 3):
+    for mode in modes:
         s = safe_project.Stage3System(None, dev)
         s._lib.pamo_stage3_set_param(s._h, b"cg_mode", float(mode))
         s.project(gt_V, gt_F, V, F, n_iters)  # warm-up

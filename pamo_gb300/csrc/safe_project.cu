@@ -1130,69 +1130,74 @@ __global__ void k_diff_hinge(const float4* __restrict__ x, const int4* __restric
 // wp.spd_project_blocks(3, block, it_max); here the 9x9 matrix of blocks [0..2][0..2] is made positive
 // semi-definite by a cyclic Jacobi eigen-decomposition (it_max sweeps), clamping negative eigenvalues to
 // zero; the fourth block row and column are then set from the first three as the reference does.
-__global__ void __launch_bounds__(32) k_spd_project(float* blocks, int nh, int sweeps, const SolverScalars* sc) {
+// Nine lanes per hinge (three hinges per warp; lanes 27-31 only take part in the warp barriers), lane k owning
+// row k of A and of the eigenvector matrix V in shared memory. Each rotation (p, q) of the cyclic order is
+// applied in two parallel halves, columns p and q of every row and then rows p and q of every column, which is
+// the sequential update's order entry by entry, so the result is the one-thread-per-hinge sweep's bit for bit;
+// the sweeps stay a loop with run-time (p, q) instead of a fully unrolled register version, whose code (tens
+// of KB per sweep) streamed through the instruction cache with one warp per SM.
+constexpr int kSpdWarps = 4;
+
+__global__ void __launch_bounds__(32 * kSpdWarps) k_spd_project(float* blocks, int nh, int sweeps,
+                                                                const SolverScalars* sc) {
     if (sc->abort) return;
-    for (int h = gtid(); h < nh; h += gstride()) {
-        float* B = blocks + (size_t)h * kHingeStride;
-        // every loop below is unrolled so that A and V live in registers
-        float A[9][9], V[9][9];
-#pragma unroll
-        for (int i = 0; i < 9; ++i)
-#pragma unroll
+    __shared__ float sA[kSpdWarps][3][81], sV[kSpdWarps][3][81];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int grp = lane / 9;
+    const bool owner = grp < 3;                 // lanes 27-31 read group 0's rows but never write
+    const int g = owner ? grp : 0, k = owner ? lane - 9 * grp : 0;
+    float* A = sA[warp][g];
+    float* V = sV[warp][g];
+    const long long warps = (long long)gridDim.x * kSpdWarps;
+    for (long long base = ((long long)blockIdx.x * kSpdWarps + warp) * 3; base < nh; base += warps * 3) {
+        const long long h = base + g;
+        const bool live = owner && h < nh;
+        float* B = blocks + (size_t)(live ? h : 0) * kHingeStride;
+        if (live)
             for (int j = 0; j < 9; ++j) {
-                A[i][j] = B[sym9(i, j)];
-                V[i][j] = (i == j) ? 1.f : 0.f;
+                A[9 * k + j] = B[sym9(k, j)];
+                V[9 * k + j] = (k == j) ? 1.f : 0.f;
             }
-        for (int sw = 0; sw < sweeps; ++sw) {
-#pragma unroll
+        __syncwarp();
+        for (int sw = 0; sw < sweeps; ++sw)
             for (int p = 0; p < 8; ++p)
-#pragma unroll
                 for (int q = p + 1; q < 9; ++q) {
-                    const float apq = A[p][q];
-                    if (fabsf(apq) < 1e-30f) continue;
+                    const float apq = A[9 * p + q];
+                    const bool rot = !(fabsf(apq) < 1e-30f);
                     // rotation angle by the fast (approximate) reciprocal and square-root instructions: the
                     // projection only needs an orthogonal rotation that shrinks the off-diagonal entry
-                    const float th = __fdividef(A[q][q] - A[p][p], 2.f * apq);
+                    const float th = __fdividef(A[9 * q + q] - A[9 * p + p], 2.f * apq);
                     const float r2 = fmaf(th, th, 1.f);
                     const float t = fabsf(th) > 1e18f ? __fdividef(0.5f, th)
                                                       : copysignf(__fdividef(1.f, fabsf(th) + r2 * rsqrtf(r2)), th);
-                    const float c = rsqrtf(fmaf(t, t, 1.f)), s = t * c;
-#pragma unroll
-                    for (int k = 0; k < 9; ++k) {
-                        const float akp = A[k][p], akq = A[k][q];
-                        A[k][p] = c * akp - s * akq;
-                        A[k][q] = s * akp + c * akq;
+                    const float c = rsqrtf(fmaf(t, t, 1.f)), sn = t * c;
+                    const float akp = A[9 * k + p], akq = A[9 * k + q];
+                    __syncwarp();  // the angle's entries are read before they change
+                    if (live && rot) {
+                        A[9 * k + p] = c * akp - sn * akq;
+                        A[9 * k + q] = sn * akp + c * akq;
                     }
-#pragma unroll
-                    for (int k = 0; k < 9; ++k) {
-                        const float apk = A[p][k], aqk = A[q][k];
-                        A[p][k] = c * apk - s * aqk;
-                        A[q][k] = s * apk + c * aqk;
+                    __syncwarp();
+                    const float apk = A[9 * p + k], aqk = A[9 * q + k];
+                    if (live && rot) {
+                        A[9 * p + k] = c * apk - sn * aqk;
+                        A[9 * q + k] = sn * apk + c * aqk;
+                        const float vkp = V[9 * k + p], vkq = V[9 * k + q];
+                        V[9 * k + p] = c * vkp - sn * vkq;
+                        V[9 * k + q] = sn * vkp + c * vkq;
                     }
-#pragma unroll
-                    for (int k = 0; k < 9; ++k) {
-                        const float vkp = V[k][p], vkq = V[k][q];
-                        V[k][p] = c * vkp - s * vkq;
-                        V[k][q] = s * vkp + c * vkq;
-                    }
+                    __syncwarp();
                 }
-        }
-        float lam[9];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) lam[i] = fmaxf(A[i][i], 0.f);
-#pragma unroll
-        for (int i = 0; i < 9; ++i)
-#pragma unroll
-            for (int j = 0; j < 9; ++j) {
-                float s = 0.f;
-#pragma unroll
-                for (int k = 0; k < 9; ++k) s += V[i][k] * lam[k] * V[j][k];
-                A[i][j] = s;
+        if (live) {
+            float lam[9];
+            for (int i = 0; i < 9; ++i) lam[i] = fmaxf(A[9 * i + i], 0.f);
+            for (int j = k; j < 9; ++j) {
+                float acc = 0.f;
+                for (int i = 0; i < 9; ++i) acc += V[9 * k + i] * lam[i] * V[9 * j + i];
+                B[sym9(k, j)] = acc;
             }
-#pragma unroll
-        for (int i = 0; i < 9; ++i)
-#pragma unroll
-            for (int j = i; j < 9; ++j) B[sym9(i, j)] = A[i][j];
+        }
+        __syncwarp();  // the group's rows are read before the next hinge overwrites them
     }
 }
 
@@ -1632,12 +1637,21 @@ __global__ void k_before_ccd(SolverScalars* sc) {
 }
 
 // accd_kernel (ccd_kernels.py:9-111): additive CCD step bound per contact
+// Contact b of the spread order: a warp takes 32 consecutive contacts and consecutive warps are warp 0 of
+// consecutive blocks, then warp 1, ...: the few heavy CCD contacts of a step land on as many SMs as there are
+// active warps (the float64 pipe of one SM is what bounds the float64 CCD), not on the first blocks' SMs.
+__device__ __forceinline__ long long spread_first() {
+    return ((long long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x) * 32 + (threadIdx.x & 31);
+}
+__device__ __forceinline__ long long spread_stride() { return (long long)gridDim.x * blockDim.x; }
+
 __global__ void k_accd(const float4* __restrict__ x, const float4* __restrict__ vel, const int4* __restrict__ cidx,
                        const int2* __restrict__ ctype, SolverScalars* sc, float slackness, float thickness, int max_iters,
                        float ee_thres) {
     if (sc->abort) return;
     const int n = sc->n_contacts;
-    for (int b = gtid(); b < n; b += gstride()) {
+    for (long long bb = spread_first(); bb < n; bb += spread_stride()) {
+        const int b = (int)bb;
         const int4 id = cidx[b];
         F3 x0 = f3(x[id.x]), x1 = f3(x[id.y]), x2 = f3(x[id.z]), x3 = f3(x[id.w]);
         F3 v0 = f3(vel[id.x]), v1 = f3(vel[id.y]), v2 = f3(vel[id.z]), v3 = f3(vel[id.w]);
@@ -1835,7 +1849,8 @@ __global__ void k_accd_fp64(const float4* __restrict__ x, const float4* __restri
                             int max_iters, double ee_thres) {
     if (sc->abort) return;
     const int n = sc->n_contacts;
-    for (int b = gtid(); b < n; b += gstride()) {
+    for (long long bb = spread_first(); bb < n; bb += spread_stride()) {
+        const int b = (int)bb;
         const int4 id = cidx[b];
         D3 x0 = d3(x[id.x]), x1 = d3(x[id.y]), x2 = d3(x[id.z]), x3 = d3(x[id.w]);
         D3 v0 = d3(vel[id.x]), v1 = d3(vel[id.y]), v2 = d3(vel[id.z]), v3 = d3(vel[id.w]);
@@ -2133,7 +2148,8 @@ void Stage3::newton_iteration() {
         k_diff_hinge<<<grid_for(NH, 128), 128, 0, s>>>(q, hinge, hinge_rest, P.hinge_stiffness, -1.f, NH, hinge_blocks,
                                                        grad, hdiag, sc);
         note_launch();
-        k_spd_project<<<grid_for(NH, 32, 64), 32, 0, s>>>(hinge_blocks, NH, P.spd_max_iters, sc);
+        k_spd_project<<<grid_for((NH + 3 * kSpdWarps - 1) / (3 * kSpdWarps), 1, 16), 32 * kSpdWarps, 0, s>>>(
+            hinge_blocks, NH, P.spd_max_iters, sc);
         note_launch();
     }
     k_diff_contact<<<gC, kT, 0, s>>>(q, c_idx, c_type, c_d, sc, P.coll_stiffness, P.d_hat, -1.f, c_dd, grad, hdiag);
@@ -2164,10 +2180,13 @@ void Stage3::newton_iteration() {
                            v[0], v[1], Av, P.n_cg_iters, sc);
         note_launch();
     } else {
-        // one cooperative launch: about one thread per element, at most one block per SM
-        const int bt = cg_mode == 3 ? 256 : 128;
+        // one cooperative launch: about one thread per element, at most one block per SM (cg_mode 0, 3, 4); or
+        // at least one block per SM (5: 128 threads, 6: 64 threads, two blocks per SM)
+        const int bt = cg_mode == 3 ? 256 : cg_mode == 4 ? 512 : cg_mode == 6 ? 64 : 128;
         const long long elems = (long long)NP + NT + NH;
         int g = (int)std::min<long long>((elems + bt - 1) / bt, (long long)n_sm);
+        if (cg_mode == 5) g = (int)std::max<long long>((elems + bt - 1) / bt, (long long)n_sm);
+        if (cg_mode == 6) g = (int)std::max<long long>((elems + bt - 1) / bt, 2ll * n_sm);
         g = std::max(1, std::min(g, std::min(coop_max_blocks, kPartials / 2)));
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(g);
@@ -2179,7 +2198,13 @@ void Stage3::newton_iteration() {
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         CgState* bar = reinterpret_cast<CgState*>(cg_bar);
-        if (bt == 256)
+        if (bt == 64)
+            cudaLaunchKernelEx(&cfg, k_cg_solve<64>, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r,
+                               z, v[0], v[1], Av, P.n_cg_iters, sc, partial, bar);
+        else if (bt == 512)
+            cudaLaunchKernelEx(&cfg, k_cg_solve<512>, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r,
+                               z, v[0], v[1], Av, P.n_cg_iters, sc, partial, bar);
+        else if (bt == 256)
             cudaLaunchKernelEx(&cfg, k_cg_solve<256>, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r,
                                z, v[0], v[1], Av, P.n_cg_iters, sc, partial, bar);
         else
@@ -2463,7 +2488,7 @@ int pamo_stage3_set_param(pamo_stage3* s, const char* name, double value) {
     else if (n == "max_blocks") P.max_blocks = (long long)value;
     else if (n == "use_cuda_graph") s->solver.use_graph = value != 0.0;
     else if (n == "ccd_fp64") P.ccd_fp64 = value != 0.0;
-    else if (n == "cg_mode") s->solver.cg_mode = (int)value;  // 0/1 grid-cooperative (128), 2 cluster, 3 (256)
+    else if (n == "cg_mode") s->solver.cg_mode = (int)value;  // 0/1 grid-cooperative (128), 2 cluster, 3 (256), 4 (512), 5 (128, >= 1 block per SM), 6 (64, >= 2 blocks per SM)
     else {
         s->solver.err = "unknown stage-3 parameter: " + n;
         return PAMO_ERR_INVALID_ARG;

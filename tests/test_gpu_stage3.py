@@ -96,6 +96,20 @@ def test_default_steps_match_oracle(case, steps):
     assert abs(st["energy"] - so["energy"]) <= 1e-4 * abs(so["energy"])
 
 
+@pytest.mark.parametrize("cg_mode", [0, 2, 3, 4, 5, 6])
+def test_every_pcg_launch_shape_matches_oracle(cg_mode):
+    """The cooperative PCG with 128-, 256- and 512-thread blocks (cg_mode 0, 3, 4), with at least one or two
+    blocks per SM (5, 6) and the cluster PCG (2)."""
+    from pamo_gb300 import safe_project
+
+    GV, GF, V, F = _cases()["sheets_push"]
+    s = safe_project.Stage3System(None, "cuda:0")
+    s._lib.pamo_stage3_set_param(s._h, b"cg_mode", float(cg_mode))
+    out = s.project(GV, GF, V, F, 3).cpu().numpy()
+    ref, _ = orc.stage3_run(GV, GF, V, F, 3)
+    assert np.abs(out - ref).max() <= TOL * _diag(V)
+
+
 def test_pamo_run_with_stage3():
     """PaMO(use_stage3=True).run: the stage-2 result projected onto the input, intersection-free, and equal to
     the oracle's projection of the same stage-2 mesh."""
