@@ -1442,7 +1442,9 @@ __device__ __forceinline__ void grid_barrier(unsigned* count, int* status) {
         asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(count), "r"(inc) : "memory");
         long long spins = 0;
         while (((ld_acquire(count) ^ old) & 0x80000000u) == 0u) {
-            if (++spins > (1ll << 28)) {
+            // after a time-out anywhere in the grid every later wait gives up at once, so the kernel ends soon
+            if ((spins & 255) == 255 && (*(volatile int*)status & kErrIterLimit)) break;
+            if (++spins > (1ll << 22)) {
                 atomicOr(status, kErrIterLimit);
                 break;
             }
@@ -2425,6 +2427,7 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     cudaStreamWaitEvent(caller, ev_out, 0);
     if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
     if (h_sc->status & 6) return fail(PAMO_ERR_ITER_LIMIT, "BVH traversal limit in stage 3");
+    if (h_sc->status & kErrIterLimit) return fail(PAMO_ERR_ITER_LIMIT, "grid barrier of the PCG timed out");
     stats.last_energy = h_sc->energy;
     stats.max_contacts = h_sc->max_contacts;
     stats.total_contacts = h_sc->total_contacts;
