@@ -95,6 +95,14 @@ __device__ __forceinline__ T ldg(const T* p) {
 __device__ __forceinline__ int gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
 __device__ __forceinline__ int gstride() { return gridDim.x * blockDim.x; }
 
+// Item order that spreads heavy, clustered items over the SMs: a warp takes 32 consecutive items and
+// consecutive warps are warp 0 of consecutive blocks, then warp 1, ... (the blocks of a grid are spread
+// over the SMs first), so a run of heavy items lands on many SMs instead of the few blocks that hold it.
+__device__ __forceinline__ long long spread_first() {
+    return ((long long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x) * 32 + (threadIdx.x & 31);
+}
+__device__ __forceinline__ long long spread_stride() { return (long long)gridDim.x * blockDim.x; }
+
 // Host-side count of kernels this library has launched (for launch accounting in benchmarks).
 void note_launch();
 void note_launches(long long n);  // kernels run by a CUDA graph launch

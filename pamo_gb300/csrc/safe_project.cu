@@ -1639,14 +1639,8 @@ __global__ void k_before_ccd(SolverScalars* sc) {
 }
 
 // accd_kernel (ccd_kernels.py:9-111): additive CCD step bound per contact
-// Contact b of the spread order: a warp takes 32 consecutive contacts and consecutive warps are warp 0 of
-// consecutive blocks, then warp 1, ...: the few heavy CCD contacts of a step land on as many SMs as there are
-// active warps (the float64 pipe of one SM is what bounds the float64 CCD), not on the first blocks' SMs.
-__device__ __forceinline__ long long spread_first() {
-    return ((long long)(threadIdx.x >> 5) * gridDim.x + blockIdx.x) * 32 + (threadIdx.x & 31);
-}
-__device__ __forceinline__ long long spread_stride() { return (long long)gridDim.x * blockDim.x; }
-
+// Contacts in the spread order (spread_first): the few heavy CCD contacts of a step land on as many SMs as there
+// are active warps (the float64 pipe of one SM is what bounds the float64 CCD), not on the first blocks' SMs.
 __global__ void k_accd(const float4* __restrict__ x, const float4* __restrict__ vel, const int4* __restrict__ cidx,
                        const int2* __restrict__ ctype, SolverScalars* sc, float slackness, float thickness, int max_iters,
                        float ee_thres) {
