@@ -910,6 +910,9 @@ __device__ __forceinline__ ElasticLocal elastic_local(const float4* __restrict__
     return L;
 }
 
+}  // namespace
+
+// Arguments of the energy kernels (declared in the header for Stage3::energy_args).
 struct EnergyArgs {
     const float4* tgt;
     const float* w;
@@ -930,6 +933,8 @@ struct EnergyArgs {
     float kappa, d_hat, ee_thres;
 };
 
+namespace {
+
 // Total energy at x (system.py:325-339): the four energies of the default set, one grid-stride pass over
 // [vertices | triangles | hinges | contacts], summed with compensation in a fixed order into sc->energy.
 // mesh2gt_pp_distance_energy_kernel (distance_energy.py:6-17), elastic_energy_kernel (elastic_energy.py:40-80),
@@ -938,14 +943,13 @@ struct EnergyArgs {
 // ls_n >= 1: the energy of line-search trial ls_n, skipped (like the trial itself, k_line_search) once an
 // earlier trial was accepted: q and therefore the energy, distances and contact types are already those of the
 // accepted trial. Every block reads the same flags: the last block writes sc->energy only after all have started.
-__global__ void __launch_bounds__(kT) k_energy(const float4* __restrict__ x, EnergyArgs A, SolverScalars* sc,
-                                               float2* partial, int ls_n) {
-    if (sc->abort) return;
-    if (ls_n > 0 && sc->energy < sc->energy_prev) return;
-    const int nc = sc->n_contacts;
+// The energy terms of elements first, first + stride, ... of [vertices | triangles | hinges | contacts], summed
+// with compensation in the thread.
+__device__ __forceinline__ CSum energy_elements(const float4* __restrict__ x, const EnergyArgs& A, int nc, long long first,
+                                                long long stride) {
     const long long e1 = A.np, e2 = e1 + A.nt, e3 = e2 + A.nh, total = e3 + nc;
     CSum acc;
-    for (long long g = gtid(); g < total; g += gstride()) {
+    for (long long g = first; g < total; g += stride) {
         float e;
         if (g < e1) {
             const int i = (int)g;
@@ -982,6 +986,14 @@ __global__ void __launch_bounds__(kT) k_energy(const float4* __restrict__ x, Ene
         }
         acc.add(e);
     }
+    return acc;
+}
+
+__global__ void __launch_bounds__(kT) k_energy(const float4* __restrict__ x, EnergyArgs A, SolverScalars* sc,
+                                               float2* partial, int ls_n) {
+    if (sc->abort) return;
+    if (ls_n > 0 && sc->energy < sc->energy_prev) return;
+    const CSum acc = energy_elements(x, A, sc->n_contacts, gtid(), gstride());
     grid_sum_finish(acc, partial, &sc->red_count, &sc->energy, nullptr);
 }
 
@@ -1521,6 +1533,35 @@ __global__ void __launch_bounds__(kThreads) k_cg_solve(const float4* __restrict_
     }
 }
 
+// The line search (system.py:393-409 with line_search_kernel, solver_kernels.py:52-66) as one cooperative
+// launch on k_energy's grid: trial n sets q = q0 + ccd_step 0.5^n p, its energy is summed as k_energy sums it
+// (the same threads, block partials and order, so the same value), and the search stops at the first trial whose
+// energy is below the energy before it. In place of n_trials launches of k_line_search and k_energy, most of
+// which found an earlier trial accepted and returned at once.
+__global__ void __launch_bounds__(kT) k_line_search_coop(const float4* __restrict__ q0, const float4* __restrict__ p,
+                                                         float4* q, EnergyArgs A, int n_trials, SolverScalars* sc,
+                                                         float2* partial, CgState* bar) {
+    if (sc->abort) return;
+    const int nc = sc->n_contacts;
+    const float e_prev = sc->energy_prev, step = sc->ccd_step;
+    float e = sc->energy;
+    for (int n = 0; n < n_trials; ++n) {
+        const float a = step * powf(0.5f, (float)n);
+        for (int i = gtid(); i < A.np; i += gstride()) {
+            const float4 a0 = q0[i], pi = p[i];
+            q[i] = make_float4(a0.x + a * pi.x, a0.y + a * pi.y, a0.z + a * pi.z, 0.f);
+        }
+        grid_barrier(&bar->count, &sc->status);
+        // partials alternate between two buffers trial by trial (rewritten only after the next barrier)
+        float2* part = partial + (size_t)(n & 1) * gridDim.x;
+        store_partial(energy_elements(q, A, nc, gtid(), gstride()), part);
+        grid_barrier(&bar->count, &sc->status);
+        e = grid_partials_sum(part);
+        if (e < e_prev) break;  // the same total in every block
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->energy = e;
+}
+
 // The same solve inside one thread-block cluster (up to 16 CTAs): the barriers are the hardware cluster
 // barrier and the block partials are exchanged through distributed shared memory instead of a grid-wide
 // barrier through global memory. Selected with cg_mode 2.
@@ -1967,6 +2008,9 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_solve<128>, 128, 0);
         coop_max_blocks = std::max(1, nsm * std::max(occ, 0));
+        int occ_ls = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ls, k_line_search_coop, kT, 0);
+        ls_coop_max_blocks = nsm * std::max(occ_ls, 0);
         n_sm = std::max(1, nsm);
         // largest cluster the device runs k_cg_cluster with (16 needs the non-portable opt-in)
         cluster_size = 1;
@@ -2086,7 +2130,7 @@ int Stage3::ensure_candidates(size_t npt, size_t nee) {
     return PAMO_OK;
 }
 
-void Stage3::launch_energy(const float4* x, int ls_n) {
+EnergyArgs Stage3::energy_args() const {
     const Stage3Params& P = params;
     EnergyArgs A;
     A.tgt = target; A.w = vweight; A.m2gt_k = P.mesh2gt_dist_stiffness; A.np = NP;
@@ -2096,9 +2140,16 @@ void Stage3::launch_energy(const float4* x, int ls_n) {
     A.nt = NT; A.hinge = hinge; A.rest = hinge_rest; A.hinge_k = P.hinge_stiffness; A.nh = NH;
     A.cidx = c_idx; A.ctype = c_type; A.cd = c_d; A.kappa = P.coll_stiffness; A.d_hat = P.d_hat;
     A.ee_thres = P.ee_classify_thres;
+    return A;
+}
+
+int Stage3::energy_grid() const {
     const long long total = (long long)NP + NT + NH + (long long)cap_c;
-    const int g = (int)std::min<long long>(kRedBlocks, (total + kT - 1) / kT);
-    k_energy<<<g, kT, 0, stream>>>(x, A, sc, partial, ls_n);
+    return (int)std::min<long long>(kRedBlocks, (total + kT - 1) / kT);
+}
+
+void Stage3::launch_energy(const float4* x, int ls_n) {
+    k_energy<<<energy_grid(), kT, 0, stream>>>(x, energy_args(), sc, partial, ls_n);
     note_launch();
 }
 
@@ -2220,10 +2271,28 @@ void Stage3::newton_iteration() {
         k_accd<<<gC, kT, 0, s>>>(q, p, c_idx, c_type, sc, P.ccd_slackness, P.ccd_thickness, P.ccd_max_iters,
                                 P.ee_classify_thres);
     note_launch();
-    for (int n = 0; n < P.n_line_search_iters; ++n) {
-        k_line_search<<<grid_for(NP, kT), kT, 0, s>>>(q_prev_newton, p, sc, n, NP, q);
+    const int g_ls = energy_grid();
+    if (ls_mode == 1 && P.n_line_search_iters > 0 && g_ls <= ls_coop_max_blocks && 2 * g_ls <= kPartials) {
+        // the whole search in one cooperative launch on the energy's grid (co-residency checked at set-up)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(g_ls);
+        cfg.blockDim = dim3(kT);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        CgState* ls_bar = reinterpret_cast<CgState*>(static_cast<char*>(cg_bar) + 32);
+        cudaLaunchKernelEx(&cfg, k_line_search_coop, (const float4*)q_prev_newton, (const float4*)p, q, energy_args(),
+                           P.n_line_search_iters, sc, partial, ls_bar);
         note_launch();
-        launch_energy(q, n);
+    } else {
+        for (int n = 0; n < P.n_line_search_iters; ++n) {
+            k_line_search<<<grid_for(NP, kT), kT, 0, s>>>(q_prev_newton, p, sc, n, NP, q);
+            note_launch();
+            launch_energy(q, n);
+        }
     }
     k_iter_end<<<1, 1, 0, s>>>(sc);
     note_launch();
@@ -2286,7 +2355,7 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     if ((rr = ensure_candidates(std::max<size_t>(1 << 16, (size_t)64 * NP), std::max<size_t>(1 << 16, (size_t)64 * NE))))
         return rr;
     cudaStream_t s = stream;
-    cudaMemsetAsync(cg_bar, 0, sizeof(unsigned), s);  // barrier arrival count (after an aborted barrier)
+    cudaMemsetAsync(cg_bar, 0, 64, s);  // the barrier counters of the PCG and of the line search
     cudaEventRecord(ev_in, caller);
     cudaStreamWaitEvent(s, ev_in, 0);
     std::vector<int4> e4(NE);
@@ -2485,6 +2554,7 @@ int pamo_stage3_set_param(pamo_stage3* s, const char* name, double value) {
     else if (n == "max_blocks") P.max_blocks = (long long)value;
     else if (n == "use_cuda_graph") s->solver.use_graph = value != 0.0;
     else if (n == "ccd_fp64") P.ccd_fp64 = value != 0.0;
+    else if (n == "ls_mode") s->solver.ls_mode = (int)value;  // 1 cooperative line search, 0 launches per trial
     else if (n == "cg_mode") s->solver.cg_mode = (int)value;  // 0/1 grid-cooperative (128), 2 cluster, 3 (256), 4 (512), 5 (128, >= 1 block per SM), 6 (64, >= 2 blocks per SM)
     else {
         s->solver.err = "unknown stage-3 parameter: " + n;

@@ -62,6 +62,8 @@ struct Stage3Stats {
     int candidate_rebuilds = 0;    // Newton iterations that rebuilt the contact candidate lists
 };
 
+struct EnergyArgs;  // arguments of the energy kernels (safe_project.cu)
+
 class Stage3 {
 public:
     Stage3() = default;
@@ -75,6 +77,7 @@ public:
     std::string err;
     bool use_graph = true;  // capture one Newton iteration as a CUDA graph and replay it
     int cg_mode = 0;        // PCG kernel: 0/1 grid-wide cooperative, 128 threads; 3: 256 threads; 2: one cluster
+    int ls_mode = 1;        // line search: 1 one cooperative launch, 0 a launch pair per trial
     int cluster_size = 1;   // CTAs of the cluster kernel (device limit, at most 16)
 
 private:
@@ -127,6 +130,7 @@ private:
     float2* partial = nullptr;  // block partials of the grid-wide sums
     void* cg_bar = nullptr;     // grid-barrier state of the cooperative CG kernel
     int coop_max_blocks = 1, n_sm = 1;
+    int ls_coop_max_blocks = 0;  // co-resident blocks of the cooperative line search
     // LBVHs over the current triangles and edges (built at registration, refitted at every detection)
     BvhBuffers tri_bvh{}, edge_bvh{};
     char *tri_bvh_mem = nullptr, *edge_bvh_mem = nullptr;
@@ -144,6 +148,8 @@ private:
 
     void newton_iteration();  // enqueue one Newton iteration (system.py:425-459)
     void launch_energy(const float4* x, int ls_n = -1);
+    EnergyArgs energy_args() const;
+    int energy_grid() const;  // blocks of the energy sum (k_energy and the line search)
 };
 
 }  // namespace pamo

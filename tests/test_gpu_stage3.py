@@ -110,6 +110,20 @@ def test_every_pcg_launch_shape_matches_oracle(cg_mode):
     assert np.abs(out - ref).max() <= TOL * _diag(V)
 
 
+@pytest.mark.parametrize("ls_mode", [0, 1])
+def test_line_search_modes_match_oracle(ls_mode):
+    """The line search as one cooperative launch (1) and as a launch pair per trial (0)."""
+    from pamo_gb300 import safe_project
+
+    GV, GF, V, F = _cases()["sheets_push"]
+    s = safe_project.Stage3System(None, "cuda:0")
+    s._lib.pamo_stage3_set_param(s._h, b"ls_mode", float(ls_mode))
+    out = s.project(GV, GF, V, F, 5).cpu().numpy()
+    ref, so = orc.stage3_run(GV, GF, V, F, 5)
+    assert np.abs(out - ref).max() <= TOL * _diag(V)
+    assert abs(s.stats()["energy"] - so["energy"]) <= 1e-4 * abs(so["energy"])
+
+
 def test_pamo_run_with_stage3():
     """PaMO(use_stage3=True).run: the stage-2 result projected onto the input, intersection-free, and equal to
     the oracle's projection of the same stage-2 mesh."""
