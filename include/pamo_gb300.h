@@ -257,7 +257,11 @@ const char* pamo_stage3_last_error(const pamo_stage3* s);
 /* Set one Stage3Config field by its reference name (config.py:6-73): n_newton_iters, n_cg_iters,
  * n_line_search_iters, d_hat, coll_stiffness, contact_detection_radius, ee_classify_thres, ccd_slackness,
  * ccd_thickness, ccd_max_iters, spd_max_iters, elas_young_modulus, elas_poisson_ratio, hinge_stiffness,
- * mesh2gt_dist_stiffness, min_angle_thres (degrees), max_blocks. Unknown names: PAMO_ERR_INVALID_ARG. */
+ * mesh2gt_dist_stiffness, min_angle_thres (degrees), max_blocks. Execution knobs that leave the method
+ * unchanged: use_cuda_graph (0/1), ccd_fp64 (1: float64 CCD step, the default; 0: float32 like the reference),
+ * cg_mode (PCG launch shape: 0 cooperative 128-thread blocks, 2 one thread-block cluster, 3/4 256/512-thread
+ * blocks, 5/6 at least one/two blocks per SM), ls_mode (1: the line search as one cooperative launch, 0: a
+ * launch pair per trial). Unknown names: PAMO_ERR_INVALID_ARG. */
 int pamo_stage3_set_param(pamo_stage3* s, const char* name, double value);
 
 /*
