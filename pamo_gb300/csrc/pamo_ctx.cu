@@ -262,8 +262,11 @@ struct pamo_ctx {
         if ((r = check(cudaMalloc((void**)&rc, sizeof(RoundCounters)), "cudaMalloc"))) return r;
         if ((r = check(cudaMallocHost((void**)&h_rc, sizeof(RoundCounters)), "cudaMallocHost"))) return r;
         if ((r = check(cudaMallocHost((void**)&h_pinned_f, 64 * sizeof(float)), "cudaMallocHost"))) return r;
-        if ((r = check(cudaMalloc((void**)&scan_scratch, scan_scratch_ints() * sizeof(int)), "cudaMalloc"))) return r;
-        if (scan_scratch_clear(scan_scratch)) return check(cudaGetLastError(), "scan scratch");
+        // one scratch per job of a combined scan launch (exclusive_scans)
+        if ((r = check(cudaMalloc((void**)&scan_scratch, kMaxScanJobs * scan_scratch_ints() * sizeof(int)), "cudaMalloc")))
+            return r;
+        for (int k = 0; k < kMaxScanJobs; ++k)
+            if (scan_scratch_clear(scan_scratch + k * scan_scratch_ints())) return check(cudaGetLastError(), "scan scratch");
         if ((r = check(cudaMalloc((void**)&d_ecap, sizeof(int)), "cudaMalloc"))) return r;
         if ((r = check(cudaMalloc((void**)&d_scale, sizeof(float)), "cudaMalloc"))) return r;
         if ((r = check(cudaMalloc((void**)&d_center, 16 * sizeof(float)), "cudaMalloc"))) return r;
@@ -433,9 +436,7 @@ struct pamo_ctx {
         cudaMemsetAsync(vedges.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(vcursor.p, 0, (nP + 1) * sizeof(int), s);
         launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
-        exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nP);
-        exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status, nT);
-        exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nP);
+        scan_adjacency_counts(s, std::max(nP, nT));
         launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p, eorder.p, s);
         launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
         const int* nt_off = valence.p;
@@ -489,9 +490,7 @@ struct pamo_ctx {
             launch_copy_tris_dev(tri.p, orig_tri.p, rc, nTb, s);
             launch_zero_vertex_counts_dev(rc, nPb, valence.p, cursor.p, vedges.p, vcursor.p, s);
             launch_face_counts(tri.p, rc, nTb, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
-            exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nPb);
-            exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status, nTb);
-            exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nPb);
+            scan_adjacency_counts(s, std::max(nPb, nTb));
             launch_fill_adjacency(tri.p, rc, nTb, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p,
                                   eorder.p, s);
             launch_sort_adjacency(rc, nPb, valence.p, nt.p, s);
@@ -527,12 +526,29 @@ struct pamo_ctx {
         exclusive_scan(uflag.p, uflag.p, &rc->n_considered, 1, &rc->n_undo, scan_scratch, s, &rc->status, eb);
         launch_after_check(rc, s);
         // compaction map (cusimp_free.cu:1042-1045), compaction (pamo/__init__.py:136-140), next round's state
-        exclusive_scan(occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nPb);
         launch_live_flags(rc, nTb, tri.p, fflags.p, s);
-        exclusive_scan(fflags.p, fflags.p, &rc->n_tris, 1, nullptr, scan_scratch, s, &rc->status, nTb);
+        scan_compaction_maps(s, std::max(nPb, nTb));
         launch_compact_mesh(rc, nPb, nTb, pos.p, occ.p, pts_map.p, tri.p, fflags.p, pos_out.p, tri_out.p, s);
         bvh_remap(bvh, fflags.p, nTb, s);  // the tree's leaves in the next round's face numbering
         launch_round_end(rc, d_ls, d_ls + 1, undo_list.p, undo_in.p, (int)std::min(undo_in.n, undo_list.n), list_cap, s);
+    }
+
+    // Vertex valences, per-face edge counts (their total is the edge count) and per-vertex edge counts, scanned
+    // by one launch (three independent scans, each on its own scratch).
+    void scan_adjacency_counts(cudaStream_t s, long long bound) {
+        const size_t sz = scan_scratch_ints();
+        const ScanJob jobs[3] = {{valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch},
+                                 {ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch + sz},
+                                 {vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch + 2 * sz}};
+        exclusive_scans(jobs, 3, s, &rc->status, bound);
+    }
+
+    // The vertex compaction map (occ -> pts_map) and the live-face offsets, scanned by one launch.
+    void scan_compaction_maps(cudaStream_t s, long long bound) {
+        const size_t sz = scan_scratch_ints();
+        const ScanJob jobs[2] = {{occ.p, pts_map.p, &rc->n_pts, 1, nullptr, scan_scratch},
+                                 {fflags.p, fflags.p, &rc->n_tris, 1, nullptr, scan_scratch + sz}};
+        exclusive_scans(jobs, 2, s, &rc->status, bound);
     }
 
     // Enqueue round_dev through a cached graph of its size class (or directly when graphs are off or the
@@ -644,9 +660,7 @@ struct pamo_ctx {
         cudaMemsetAsync(vedges.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(vcursor.p, 0, (nP + 1) * sizeof(int), s);
         launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
-        exclusive_scan(valence.p, valence.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nP);
-        exclusive_scan(ecount.p, ecount.p, &rc->n_tris, 1, &rc->n_edges, scan_scratch, s, &rc->status, nT);
-        exclusive_scan(vedges.p, vedges.p, &rc->n_pts, 1, nullptr, scan_scratch, s, &rc->status, nP);
+        scan_adjacency_counts(s, std::max(nP, nT));
         launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p, eorder.p, s);
         launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
         const int* nt_off = valence.p;

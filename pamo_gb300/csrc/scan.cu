@@ -3,6 +3,7 @@
 #include "pamo_common.cuh"
 #include "scan.cuh"
 
+#include <algorithm>
 #include <atomic>
 
 namespace pamo {
@@ -54,8 +55,20 @@ __device__ __forceinline__ void load4(const int* in, int idx, int hi, int v[kIte
 // with Decoupled Look-back", 2016). Tile ids come from an atomic counter in launch order, so a tile only ever
 // waits for tiles whose blocks are already running; each tile publishes its aggregate before it looks back.
 // The last block to finish clears the counters and status words for the next scan on the same scratch.
-__global__ void __launch_bounds__(kThreads) k_scan(const int* in, int* out, const int* d_n, int n_add, int* d_total,
-                                                   int* scratch, int* err) {
+// Up to kMaxScanJobs independent scans in one launch: job blockIdx.y, each with its own scratch, so that
+// their tiles never wait for one another.
+struct ScanJobs {
+    ScanJob j[kMaxScanJobs];
+};
+
+__global__ void __launch_bounds__(kThreads) k_scan(ScanJobs jobs, int* err) {
+    const ScanJob& J = jobs.j[blockIdx.y];
+    const int* in = J.in;
+    int* out = J.out;
+    const int* d_n = J.d_n;
+    const int n_add = J.n_add;
+    int* d_total = J.d_total;
+    int* scratch = J.scratch;
     __shared__ int sm[33];
     __shared__ int s_tile, s_prefix;
     unsigned long long* status = reinterpret_cast<unsigned long long*>(scratch + kHeader);
@@ -162,14 +175,26 @@ __global__ void __launch_bounds__(kThreads) k_scan(const int* in, int* out, cons
 }
 }  // namespace
 
-void exclusive_scan(const int* in, int* out, const int* d_n, int n_add, int* d_total, int* scratch, cudaStream_t s,
-                    int* err, long long n_bound) {
+void exclusive_scans(const ScanJob* jobs, int count, cudaStream_t s, int* err, long long n_bound) {
+    if (count < 1 || count > kMaxScanJobs) return;
+    ScanJobs all{};
+    int n_add = 0;
+    for (int k = 0; k < count; ++k) {
+        all.j[k] = jobs[k];
+        n_add = std::max(n_add, jobs[k].n_add);
+    }
     int tiles = kScanTiles;
     if (n_bound >= 0 && n_bound < (1 << 19)) {  // callers cap their bounds at 2^19 (every grid full from there)
         const long long want = (n_bound + n_add + kPass - 1) / kPass;
         tiles = (int)(want < 1 ? 1 : (want > kScanTiles ? kScanTiles : want));
     }
-    k_scan<<<tiles, kThreads, 0, s>>>(in, out, d_n, n_add, d_total, scratch, err); note_launch();
+    k_scan<<<dim3(tiles, count), kThreads, 0, s>>>(all, err); note_launch();
+}
+
+void exclusive_scan(const int* in, int* out, const int* d_n, int n_add, int* d_total, int* scratch, cudaStream_t s,
+                    int* err, long long n_bound) {
+    const ScanJob job{in, out, d_n, n_add, d_total, scratch};
+    exclusive_scans(&job, 1, s, err, n_bound);
 }
 
 int scan_scratch_clear(int* scratch) {

@@ -19,6 +19,19 @@ inline size_t scan_scratch_ints() { return 8 + 2 * (size_t)kScanTiles; }
 void exclusive_scan(const int* in, int* out, const int* d_n, int n_add, int* d_total, int* scratch,
                     cudaStream_t s, int* err = nullptr, long long n_bound = -1);
 
+// Independent scans launched together (one launch instead of `count`): each job has the meaning of
+// exclusive_scan's arguments and its own scratch; n_bound bounds every job's element count.
+constexpr int kMaxScanJobs = 3;
+struct ScanJob {
+    const int* in;
+    int* out;
+    const int* d_n;
+    int n_add;
+    int* d_total;
+    int* scratch;
+};
+void exclusive_scans(const ScanJob* jobs, int count, cudaStream_t s, int* err = nullptr, long long n_bound = -1);
+
 // Zeroes a freshly allocated scan scratch (synchronous); returns nonzero on a CUDA error.
 int scan_scratch_clear(int* scratch);
 
