@@ -484,11 +484,8 @@ struct pamo_ctx {
             launch_round_begin(rc, d_ls, d_ls + 1, s);
             launch_undo_bookkeeping_dev(undo_in.p, d_ls, list_cap, tmp_undo.p, undo_list.p, pts_map.p, (int)pts_map.n,
                                         invalid.p, (int)invalid.n, s);
-            launch_copy_map_dev(d_ls, pts_map.p, pts_map_prev.p, nPb, s);
-            launch_load_points4_dev(pos_in.p, rc, nPb, pos.p, orig_pos.p, occ.p, s);
-            launch_copy_tris_dev(tri_in.p, tri.p, rc, nTb, s);
-            launch_copy_tris_dev(tri.p, orig_tri.p, rc, nTb, s);
-            launch_zero_vertex_counts_dev(rc, nPb, valence.p, cursor.p, vedges.p, vcursor.p, s);
+            launch_round_prologue_dev(d_ls, rc, nPb, nTb, pts_map.p, pts_map_prev.p, pos_in.p, pos.p, orig_pos.p, occ.p,
+                                      tri_in.p, tri.p, orig_tri.p, valence.p, cursor.p, vedges.p, vcursor.p, qflag.p, s);
             launch_face_counts(tri.p, rc, nTb, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
             scan_adjacency_counts(s, std::max(nPb, nTb));
             launch_fill_adjacency(tri.p, rc, nTb, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p,
@@ -509,7 +506,6 @@ struct pamo_ctx {
             launch_remove_invalid(rc, nTb, tri.p, s);
             launch_line_edges(rc, eb, edges.p, nt_off, nt.p, tri.p, pos.p, occ.p, nullptr, (int)collapsed.n,
                               collapsed.p, s);
-            launch_zero_face_ints_dev(rc, nTb, qflag.p, s);
             launch_mark_query(rc, eb, collapsed.p, edges.p, nt_off, nt.p, qflag.p, s);
             exclusive_scan(qflag.p, qflag.p, &rc->n_tris, 1, &rc->n_query, scan_scratch, s, &rc->status, nTb);
             launch_compact_flags(qflag.p, nTb, &rc->n_tris, qlist.p, s);

@@ -957,37 +957,36 @@ __global__ void k_undo_book_dev(const int* __restrict__ verts_undo, const LoopSt
     }
 }
 
-__global__ void k_load_points4_dev(const float4* __restrict__ pts, const RoundCounters* rc, float4* pos, float4* orig,
-                                   int* occ) {
-    const int n = rc->n_pts;
-    for (int v = gtid(); v < n; v += gstride()) {
-        const float4 p = pts[v];
-        pos[v] = p;
-        orig[v] = p;
-        occ[v] = 1;
+// the start of a device round (launch_round_prologue_dev)
+__global__ void k_round_prologue_dev(const LoopState* ls, const RoundCounters* rc, const int* __restrict__ pts_map,
+                                     int* pts_map_prev, const float4* __restrict__ pts_in, float4* pos, float4* orig_pos,
+                                     int* occ, const int4* __restrict__ tri_in, int4* tri, int4* orig_tri, int* valence,
+                                     int* cursor, int* vedges, int* vcursor, int* qflag) {
+    const int nm = ls->np, np = rc->n_pts, nf = rc->n_tris;
+    const int n = max(max(nm, np + 1), nf + 1);
+    for (int i = gtid(); i < n; i += gstride()) {
+        if (i < nm) pts_map_prev[i] = pts_map[i];
+        if (i < np) {
+            const float4 p = pts_in[i];
+            pos[i] = p;
+            orig_pos[i] = p;
+            occ[i] = 1;
+        } else if (i == np) {
+            occ[np] = 0;
+        }
+        if (i <= np) valence[i] = cursor[i] = vedges[i] = vcursor[i] = 0;
+        if (i < nf) {
+            const int4 t = tri_in[i];
+            tri[i] = t;
+            orig_tri[i] = t;
+        }
+        if (i <= nf) qflag[i] = 0;
     }
-    if (gtid() == 0) occ[n] = 0;
-}
-
-__global__ void k_copy_tris_dev(const int4* __restrict__ src, int4* dst, const RoundCounters* rc) {
-    const int n = rc->n_tris;
-    for (int f = gtid(); f < n; f += gstride()) dst[f] = src[f];
-}
-
-// valence, cursor, vedges, vcursor = 0 over n_pts + 1 entries
-__global__ void k_zero_vertex_counts_dev(const RoundCounters* rc, int* a, int* b, int* c, int* d) {
-    const int n = rc->n_pts + 1;
-    for (int i = gtid(); i < n; i += gstride()) a[i] = b[i] = c[i] = d[i] = 0;
 }
 
 __global__ void k_fill_u64_dev(const RoundCounters* rc, unsigned long long* p, unsigned long long v) {
     const int n = rc->n_pts + 1;
     for (int i = gtid(); i < n; i += gstride()) p[i] = v;
-}
-
-__global__ void k_zero_face_ints_dev(const RoundCounters* rc, int* p) {
-    const int n = rc->n_tris + 1;
-    for (int i = gtid(); i < n; i += gstride()) p[i] = 0;
 }
 
 __global__ void k_zero_face_bytes_dev(const RoundCounters* rc, unsigned char* p) {
@@ -1016,11 +1015,6 @@ __global__ void k_round_end(const RoundCounters* rc, const LoopState* ls, LoopSt
 
 // the previous round's compaction map, kept for the undo passes of this round (the round's own compaction
 // overwrites pts_map before an undo pass may follow); undo entries index it with this round's vertex ids (< np)
-__global__ void k_copy_map_dev(const LoopState* ls, const int* __restrict__ src, int* dst) {
-    const int n = ls->np;
-    for (int i = gtid(); i < n; i += gstride()) dst[i] = src[i];
-}
-
 // undo vertices carried to the next round (the host loop's copy of the previous undo list)
 __global__ void k_copy_undo_dev(const RoundCounters* rc, const int* __restrict__ src, int* dst, int cap) {
     const int n = min(rc->n_vertices_undo, cap);
@@ -1169,9 +1163,6 @@ void launch_undo_check(RoundCounters* rc, int n_edges_bound, const int* collapse
                        const int* nt, const unsigned char* hit, int* uflag, cudaStream_t s) {
     k_undo_check<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, collapsed, edges, nt_off, nt, hit, uflag); note_launch();
 }
-void launch_copy_map_dev(const LoopState* ls, const int* pts_map, int* pts_map_prev, int n_pts_bound, cudaStream_t s) {
-    k_copy_map_dev<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(ls, pts_map, pts_map_prev); note_launch();
-}
 void launch_undo_apply(RoundCounters* rc, int n_edges_bound, const int* collapsed, const int* uscan, const int2* edges,
                        const int* nt_off, const int* nt, int4* tri, const int4* orig_tri, float4* pos,
                        const float4* orig_pos, int* occ, int* tmp_undo, int* undo_list, const int* pts_map,
@@ -1234,23 +1225,18 @@ void launch_undo_bookkeeping_dev(const int* verts_undo, const LoopState* ls, int
     k_undo_book_dev<<<grid_for(n_undo_bound, kT), kT, 0, s>>>(verts_undo, ls, tmp_undo, undo_list, pts_map, pts_map_len,
                                                              invalid, invalid_len); note_launch();
 }
-void launch_load_points4_dev(const float4* pts, const RoundCounters* rc, int n_pts_bound, float4* pos, float4* orig_pos,
-                             int* occ, cudaStream_t s) {
-    k_load_points4_dev<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(pts, rc, pos, orig_pos, occ); note_launch();
-}
-void launch_copy_tris_dev(const int4* src, int4* dst, const RoundCounters* rc, int n_tris_bound, cudaStream_t s) {
-    k_copy_tris_dev<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(src, dst, rc); note_launch();
-}
-void launch_zero_vertex_counts_dev(const RoundCounters* rc, int n_pts_bound, int* a, int* b, int* c, int* d,
-                                   cudaStream_t s) {
-    k_zero_vertex_counts_dev<<<grid_for(n_pts_bound + 1, kT), kT, 0, s>>>(rc, a, b, c, d); note_launch();
+void launch_round_prologue_dev(const LoopState* ls, const RoundCounters* rc, int n_pts_bound, int n_tris_bound,
+                               const int* pts_map, int* pts_map_prev, const float4* pts_in, float4* pos,
+                               float4* orig_pos, int* occ, const int4* tri_in, int4* tri, int4* orig_tri, int* valence,
+                               int* cursor, int* vedges, int* vcursor, int* qflag, cudaStream_t s) {
+    const int n = (n_pts_bound > n_tris_bound ? n_pts_bound : n_tris_bound) + 1;
+    k_round_prologue_dev<<<grid_for(n, kT), kT, 0, s>>>(ls, rc, pts_map, pts_map_prev, pts_in, pos, orig_pos, occ, tri_in,
+                                                        tri, orig_tri, valence, cursor, vedges, vcursor, qflag);
+    note_launch();
 }
 void launch_fill_u64_dev(const RoundCounters* rc, int n_pts_bound, unsigned long long* p, unsigned long long v,
                          cudaStream_t s) {
     k_fill_u64_dev<<<grid_for(n_pts_bound + 1, kT), kT, 0, s>>>(rc, p, v); note_launch();
-}
-void launch_zero_face_ints_dev(const RoundCounters* rc, int n_tris_bound, int* p, cudaStream_t s) {
-    k_zero_face_ints_dev<<<grid_for(n_tris_bound + 1, kT), kT, 0, s>>>(rc, p); note_launch();
 }
 void launch_zero_face_bytes_dev(const RoundCounters* rc, int n_tris_bound, unsigned char* p, cudaStream_t s) {
     k_zero_face_bytes_dev<<<grid_for(n_tris_bound + 1, kT), kT, 0, s>>>(rc, p); note_launch();

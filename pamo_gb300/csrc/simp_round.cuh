@@ -86,19 +86,19 @@ void launch_after_check(RoundCounters* rc, cudaStream_t s);
 
 // ---- device-driven rounds: sizes from LoopState / RoundCounters, host values only bound the grids ----
 void launch_round_begin(RoundCounters* rc, LoopState* ls, const LoopState* next, cudaStream_t s);
-// pts_map_prev[0, ls->np) = pts_map: the previous round's map, read by this round's undo passes
-void launch_copy_map_dev(const LoopState* ls, const int* pts_map, int* pts_map_prev, int n_pts_bound, cudaStream_t s);
 void launch_undo_bookkeeping_dev(const int* verts_undo, const LoopState* ls, int n_undo_bound, int* tmp_undo,
                                  int* undo_list, const int* pts_map, int pts_map_len, unsigned char* invalid,
                                  int invalid_len, cudaStream_t s);
-void launch_load_points4_dev(const float4* pts, const RoundCounters* rc, int n_pts_bound, float4* pos, float4* orig_pos,
-                             int* occ, cudaStream_t s);
-void launch_copy_tris_dev(const int4* src, int4* dst, const RoundCounters* rc, int n_tris_bound, cudaStream_t s);
-void launch_zero_vertex_counts_dev(const RoundCounters* rc, int n_pts_bound, int* a, int* b, int* c, int* d,
-                                   cudaStream_t s);
+// Start of a device round, after the undo bookkeeping, in one launch: pts_map_prev[0, ls->np) = pts_map (the
+// previous round's map, read by this round's undo passes); pos = orig_pos = the round's points, occ = 1 and
+// occ[n_pts] = 0; tri = orig_tri = the round's faces; valence, cursor, vedges, vcursor = 0 over n_pts + 1 entries;
+// qflag = 0 over n_tris + 1 entries.
+void launch_round_prologue_dev(const LoopState* ls, const RoundCounters* rc, int n_pts_bound, int n_tris_bound,
+                               const int* pts_map, int* pts_map_prev, const float4* pts_in, float4* pos,
+                               float4* orig_pos, int* occ, const int4* tri_in, int4* tri, int4* orig_tri, int* valence,
+                               int* cursor, int* vedges, int* vcursor, int* qflag, cudaStream_t s);
 void launch_fill_u64_dev(const RoundCounters* rc, int n_pts_bound, unsigned long long* p, unsigned long long v,
                          cudaStream_t s);
-void launch_zero_face_ints_dev(const RoundCounters* rc, int n_tris_bound, int* p, cudaStream_t s);
 void launch_zero_face_bytes_dev(const RoundCounters* rc, int n_tris_bound, unsigned char* p, cudaStream_t s);
 void launch_round_end(const RoundCounters* rc, const LoopState* ls, LoopState* next, const int* undo_list, int* undo_in,
                       int undo_cap, int n_undo_bound, cudaStream_t s);
