@@ -178,6 +178,21 @@ def cpu_sample(v, f, ratio, gpu_faces_per_round, budget_s=15.0, threads=None, st
     }
 
 
+def replica_throughput(local_value: float, units: float, world: int, device, per="ms") -> tuple[float, float]:
+    """(slowest rank's time, whole-job throughput) for N independent replicas: the per-rank time (ms per step, or
+    seconds when per="s") is reduced by MAX over the process group, and the throughput is N * units / that time."""
+    t = local_value
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        x = torch.tensor([float(local_value)], dtype=torch.float64, device=device)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        t = float(x.item())
+    seconds = t / 1000.0 if per == "ms" else t
+    return t, world * units / seconds
+
+
 def run_reference(args):
     """CPU reference arm: the oracle restatement of the reference's algorithm on all host cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -487,12 +502,7 @@ def main():
     launches = simp.launch_count() - launches0
     cost_ms, cost_n = ctx.kernel_time(reset=True)
     ctx.set_option("time_edge_cost", 0)
-    ms = float(np.mean(step_ms))
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * F0 / (ms / 1000.0)
+    ms, value = replica_throughput(float(np.mean(step_ms)), F0, world, dev)
 
     # ---- end to end through the public API from pinned host buffers ----
     v_host = torch.from_numpy(v).pin_memory()
@@ -510,11 +520,7 @@ def main():
         if i > 0:
             e2e_s.append(time.perf_counter() - t0)
         d2h = V.nbytes + Fo.nbytes
-    e2e = F0 / float(np.mean(e2e_s))
-    if world > 1:
-        t = torch.tensor([float(np.mean(e2e_s))], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e = world * F0 / float(t.item())
+    _, e2e = replica_throughput(float(np.mean(e2e_s)), F0, world, dev, per="s")
 
     # ---- phase profile of one more job (not part of the timed steps) ----
     ctx.profile(True)
