@@ -37,7 +37,7 @@ def _rank(rank, world, port, out):
 
 def test_replica_throughput_takes_the_slowest_rank():
     world = 2
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank, args=(world, _free_port(), out), nprocs=world, join=True)
         res = dict(out)
