@@ -423,6 +423,7 @@ class PaMO(torch.nn.Module):
         self.R = 256  # vol2mesh resolution (pamo/__init__.py:50-52), lowered for small targets in run()
         self.last_rounds = 0
         self.system = None  # the reference builds its Stage3System here; it is made on the first run's device
+        self._gt_dev = None  # the input mesh on the run's device (float64 points, int32 faces), kept across runs
         if use_stage3:
             from . import safe_project
 
@@ -460,5 +461,9 @@ class PaMO(torch.nn.Module):
             if self.system is None or self.system.device != points.device:
                 self.system = safe_project.Stage3System(self.config, points.device)
             V2, F2 = safe_project.mesh_process(verts_np, faces_np)
-            verts_np, faces_np = safe_project.process(self.gt_mesh[0], self.gt_mesh[1], V2, F2, 5, system=self.system)
+            if self._gt_dev is None or self._gt_dev[0].device != points.device:
+                # the projection's target is fixed at construction: uploaded once, like resident model state
+                self._gt_dev = (torch.as_tensor(self.gt_mesh[0], dtype=torch.float64).to(points.device),
+                                torch.as_tensor(self.gt_mesh[1], dtype=torch.int32).to(points.device))
+            verts_np, faces_np = safe_project.process(self._gt_dev[0], self._gt_dev[1], V2, F2, 5, system=self.system)
         return verts_np, faces_np
