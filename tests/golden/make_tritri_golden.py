@@ -1,8 +1,8 @@
 """Generates tests/golden/tritri_cases.npz: triangle pairs with the reference's own per-pair
 self-intersection decision.
 
-The decisions come from oracle/_ref/ref_tritri, the reference's tri-tri code (simp_cuda/src/bvh under
-/root/reference) compiled for the host by oracle/build_ref.py. The script also checks that the oracle's
+The decisions come from oracle/_ref/ref_tritri, the reference's tri-tri code (simp_cuda/src/bvh of the reference
+checkout named by $PAMO_REFERENCE_ROOT) compiled for the host by oracle/build_ref.py. The script also checks that the oracle's
 restatement agrees on every generated case before writing the fixture (all positive cases and a sample of
 negatives are stored).
 
