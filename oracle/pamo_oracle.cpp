@@ -531,8 +531,11 @@ struct Oracle {
     }
 
     // normal-flip test and skinny term over the ring of w, with w moved to vm, skipping faces that
-    // contain `other` (cusimp_free.cu:497-575). Returns false when a normal flips.
-    inline bool ring_skinny(int w, int other, P3 vm, float& qa, int& ntri) const {
+    // contain `other` (cusimp_free.cu:497-575). Returns false when a normal flips. The reference squares the
+    // lengths with the device's pow(float, int); this restatement multiplies (the device function differs from
+    // x * x by one ulp for a few floats in a million, which the GPU tests find to change no result). legacy: the
+    // legacy round's sum runs in double (cusimp.cu:423,463: `4.0f * sqrt(3)` takes the integer overload).
+    inline bool ring_skinny(int w, int other, P3 vm, float& qa, int& ntri, bool legacy = false) const {
         const float k4s3 = 4.0f * std::sqrt(3.0f);
         for (int s = nt_off[w]; s < nt_off[w + 1]; ++s) {
             const F3& t = tris[nt[s]];
@@ -549,7 +552,12 @@ struct Oracle {
             if (vdot(on, nn) < 0) return false;
             float l01 = vnorm(vsub(n0, n1)), l12 = vnorm(vsub(n1, n2)), l20 = vnorm(vsub(n2, n0));
             // operator precedence of the reference (Q4): only the first squared length divides
-            float e = k4s3 * tri_area(n0, n1, n2) / (l01 * l01) + l12 * l12 + l20 * l20 + 0.0000001f;
+            float e;
+            if (legacy)
+                e = (float)((double)4.0f * std::sqrt(3.0) * (double)tri_area(n0, n1, n2) / (double)(l01 * l01) +
+                            (double)(l12 * l12) + (double)(l20 * l20) + (double)0.0000001f);
+            else
+                e = k4s3 * tri_area(n0, n1, n2) / (l01 * l01) + l12 * l12 + l20 * l20 + 0.0000001f;
             qa += 1.0f - rclamp(e, 0.0f, 1.0f);
             ntri++;
         }
@@ -618,8 +626,8 @@ struct Oracle {
         P3 vm = vdiv(vadd(v0, v1), 2.0f);
         float qa = 0.0f;
         int ntri = 0;
-        if (!ring_skinny(u, v, vm, qa, ntri)) return 0xFFFFFFFFu;
-        if (!ring_skinny(v, u, vm, qa, ntri)) return 0xFFFFFFFFu;
+        if (!ring_skinny(u, v, vm, qa, ntri, true)) return 0xFFFFFFFFu;
+        if (!ring_skinny(v, u, vm, qa, ntri, true)) return 0xFFFFFFFFu;
         Q44 Q;
         for (int a = 0; a < 16; ++a) Q.m[a] = vq[u].m[a] + vq[v].m[a];
         float v4[4] = {vm.x, vm.y, vm.z, 1.0f};

@@ -58,6 +58,22 @@ def cases():
     return out
 
 
+def legacy_cases():
+    """name -> (points, triangles, threshold, max rounds) for the legacy round and PaSP.run."""
+    from pamo_gb300 import synth
+    from tests import meshes
+
+    c1v, c1f = synth.star_mesh(32, 6, lambda l: 0.03, 0)
+    return {
+        "legacy_plain_small": (c1v, c1f, 1e-3, 1000),
+        "legacy_sphere8": (*meshes.sphere(8, L=5, sigma=0.05, seed=3), 1e-3, 1000),
+        "legacy_sphere12_rough": (*meshes.sphere(12, L=8, sigma=0.08, seed=21), 1e-3, 1000),
+        "legacy_open_patch": (*meshes.open_patch(), 1e-3, 1000),
+        "legacy_tangled": (*meshes.tangled(10, seed=9, amp=0.25), 1e-3, 1000),
+        "legacy_high_threshold": (*meshes.sphere(10, L=6, sigma=0.06, seed=7), 5e-2, 1000),
+    }
+
+
 def digest(a: np.ndarray) -> np.ndarray:
     return np.frombuffer(hashlib.sha256(np.ascontiguousarray(a).tobytes()).digest(), dtype=np.uint8)
 
@@ -111,6 +127,78 @@ class RefRound:
 
     def n_collapsed(self):
         return int(self.counts()[3])
+
+
+class RefLegacy:
+    """ctypes view of the legacy round in oracle/_ref/libref_round_emu.so (one reference CUSimp)."""
+
+    def __init__(self, path: str):
+        L = ctypes.CDLL(path)
+        P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        L.ref_legacy_create.restype = P
+        L.ref_legacy_destroy.argtypes = [P]
+        L.ref_legacy_forward.argtypes = [P, P, P, I, I, F, F, I]
+        L.ref_legacy_counts.argtypes = [P, P]
+        L.ref_legacy_outputs.argtypes = [P, P, P, P, P]
+        self.L = L
+        self.h = ctypes.c_void_p(L.ref_legacy_create())
+
+    def __del__(self):
+        try:
+            self.L.ref_legacy_destroy(self.h)
+        except Exception:
+            pass
+
+    def forward_legacy(self, points, triangles, scale, threshold, init):
+        p = RefRound._p
+        pts = np.ascontiguousarray(points, np.float32)
+        tri = np.ascontiguousarray(triangles, np.int32)
+        self.L.ref_legacy_forward(self.h, p(pts), p(tri), len(pts), len(tri), float(scale), float(threshold),
+                                  int(bool(init)))
+        c = np.zeros(2, np.int64)
+        self.L.ref_legacy_counts(self.h, p(c))
+        nP, nT = int(c[0]), int(c[1])
+        verts = np.zeros((nP, 3), np.float32)
+        tris = np.zeros((nT, 3), np.int32)
+        occ = np.zeros((nP, 1), np.int32)
+        vmap = np.zeros((nP, 1), np.int32)
+        self.L.ref_legacy_outputs(self.h, p(verts), p(tris), p(occ), p(vmap))
+        return verts, tris, occ, vmap
+
+
+def legacy_loop(op, points, triangles, threshold=1e-3, iters=1000, on_round=None):
+    """PaSP.run (pamo/__init__.py:197-227) over an operator with CUDSP.forward's contract: no centring, stop at the
+    first round without progress. on_round(r, outputs, faces_after_compaction). Returns (verts, faces)."""
+    verts, faces = points, triangles
+    ext = verts.max(0) - verts.min(0)
+    scale = max(max(ext[0], ext[1]), ext[2])
+    init = True
+    for it in range(iters):
+        n_prev = faces.shape[0]
+        res = op.forward_legacy(verts, faces, scale, threshold, init)
+        v_out, t_out, occ, vmap = res
+        verts = v_out[occ.reshape(-1).astype(bool)]
+        faces = t_out[t_out[:, 0] >= 0].copy()
+        faces[:, 0] = vmap.reshape(-1)[faces[:, 0]]
+        faces[:, 1] = vmap.reshape(-1)[faces[:, 1]]
+        faces[:, 2] = vmap.reshape(-1)[faces[:, 2]]
+        init = False
+        if on_round is not None:
+            on_round(it, res, faces)
+        if faces.shape[0] == n_prev:
+            break
+    return verts, faces
+
+
+def record_legacy(op, v, f, thr, iters):
+    rows = []
+
+    def on_round(r, res, faces):
+        verts, tris, occ, vmap = res
+        rows.append(([len(verts), len(tris), len(faces)], [digest(a) for a in res]))
+
+    V, F = legacy_loop(op, v, f, thr, iters, on_round)
+    return (np.array([c for c, _ in rows], np.int64), np.stack([np.stack(d) for _, d in rows]), V, F)
 
 
 def centre(points: np.ndarray, triangles: np.ndarray):
@@ -210,6 +298,30 @@ def main():
                 print(f"  oracle differs: first at round {r}: ref {counts[r] if r is not None else counts.shape} "
                       f"oracle {oc[r] if r is not None else oc.shape}; outputs differing: "
                       f"{[OUTPUT_NAMES[k] for k in range(5) if r is not None and not np.array_equal(od[r, k], digests[r, k])]}")
+            else:
+                print("  oracle identical")
+    for name, (v, f, thr, iters) in legacy_cases().items():
+        if sel and name not in sel:
+            continue
+        counts, digests, V, F = record_legacy(RefLegacy(lib), v, f, thr, iters)
+        out[f"{name}.input"] = np.concatenate([digest(np.ascontiguousarray(v, np.float32)),
+                                               digest(np.ascontiguousarray(f, np.int32))])
+        out[f"{name}.params"] = np.array([thr, iters], np.float64)
+        out[f"{name}.counts"] = counts
+        out[f"{name}.digests"] = digests
+        out[f"{name}.final_verts"] = V
+        out[f"{name}.final_faces"] = F
+        print(f"{name}: {len(f)} -> {len(F)} faces in {len(counts)} rounds")
+        if args.check:
+            from oracle import oracle as orc
+
+            oc, od, OV, OF = record_legacy(orc.Oracle(), v, f, thr, iters)
+            same = oc.shape == counts.shape and np.array_equal(oc, counts) and np.array_equal(od, digests)
+            if not same:
+                r = next((i for i in range(min(len(oc), len(counts)))
+                          if not (np.array_equal(oc[i], counts[i]) and np.array_equal(od[i], digests[i]))), None)
+                print(f"  oracle differs: first at round {r} of {len(counts)}: ref {counts[r] if r is not None else counts.shape} "
+                      f"oracle {oc[r] if r is not None else oc.shape}")
             else:
                 print("  oracle identical")
     if not args.only:

@@ -5,7 +5,8 @@ with its LBVH, compiled for the host by oracle/build_ref.py) driven through PaMO
 the level-5 icosphere workload (20480 faces, 84 rounds), small spheres, an open patch, an index-degenerate face, a
 zero-length edge, folded meshes whose rounds take undo passes, and stuck rounds (quirks Q1-Q3). Every round's
 five operator outputs must have the same digests from the oracle, and the oracle's own whole loop (oracle_run, the
-loop the CUDA path follows) must end on the reference loop's final mesh bit for bit.
+loop the CUDA path follows) must end on the reference loop's final mesh bit for bit. The same holds for the legacy
+round without rollback (simp_cuda/src/cusimp.cu) driven through PaSP.run on 6 meshes.
 """
 
 import os
@@ -29,8 +30,9 @@ def _names(g):
 
 
 def test_fixture_covers_the_cases(golden):
-    names = _names(golden)
+    names = [n for n in _names(golden) if not n.startswith("legacy_")]
     assert set(names) == set(gen.cases())
+    assert {n for n in _names(golden) if n.startswith("legacy_")} == set(gen.legacy_cases())
     counts = np.concatenate([golden[f"{n}.counts"] for n in names])
     assert counts[:, 5].sum() >= 6, "stuck rounds are covered"
     assert (counts[:, 2] > 0).sum() >= 50, "rounds that carry undo vertices are covered"
@@ -61,3 +63,16 @@ def test_oracle_loop_equals_reference_loop(golden, name):
     assert np.array_equal(fpr, golden[f"{name}.counts"][:, 4])
     assert np.array_equal(F, golden[f"{name}.final_faces"])
     assert np.array_equal(V, golden[f"{name}.final_verts"])
+
+
+@pytest.mark.parametrize("name", sorted(gen.legacy_cases()))
+def test_oracle_legacy_rounds_equal_reference_rounds(golden, name):
+    v, f, thr, iters = gen.legacy_cases()[name]
+    counts, digests, V, F = gen.record_legacy(orc.Oracle(), v, f, thr, iters)
+    assert np.array_equal(counts, golden[f"{name}.counts"])
+    assert np.array_equal(digests, golden[f"{name}.digests"])
+    assert np.array_equal(V, golden[f"{name}.final_verts"])
+    assert np.array_equal(F, golden[f"{name}.final_faces"])
+    Vr, Fr, rounds = orc.Oracle().run_legacy(v, f, thr, iters)
+    assert rounds == len(counts)
+    assert np.array_equal(Fr, golden[f"{name}.final_faces"]) and np.array_equal(Vr, golden[f"{name}.final_verts"])
