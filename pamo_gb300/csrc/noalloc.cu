@@ -11,12 +11,20 @@
 // scratch, the query list, the flags, the counters) lives in one file-scope __device__ array of
 // kNoAllocBytes, carved the same way for every call. Every GPU that loads this library holds that array
 // until the process exits. In host code the array's name is only a host-side stand-in, so its device
-// address is looked up with cudaGetSymbolAddress once per device (with that device current), on the first
-// call made on that device, and passed to the kernels. That first call should therefore come before any
-// stream capture. All calls share the one array: everything that must start at zero is cleared at the
-// start of each call, and calls that overlap on the GPU (concurrent streams, other host threads) race on
-// it. Limits: at most kNoAllocMaxPoints points and kNoAllocMaxTriangles triangles per call; larger meshes
-// are rejected with PAMO_ERR_CAPACITY before any GPU work. The call synchronises its stream.
+// address is looked up with cudaGetSymbolAddress, with the device current, on the first call made in each
+// CUDA context, and passed to the kernels. A __device__ array has its own address in every context, so the
+// address is cached per context, keyed on the context's process-unique id (cuCtxGetId): a host that runs its
+// own context, or one that resets the device (cudaDeviceReset) and so gets a new primary context, gets a
+// fresh lookup. Where the driver cannot report that id, the address is looked up on every call. The first
+// call in a context should therefore come before any stream capture. All calls share the one array:
+// everything that must start at zero is cleared at the start of each call, and calls that overlap on the GPU
+// (concurrent streams, other host threads) race on it. Limits: at most kNoAllocMaxPoints points and
+// kNoAllocMaxTriangles triangles per call; larger meshes are rejected with PAMO_ERR_CAPACITY before any GPU
+// work. A CUDA error left pending by the caller's earlier work is reported as PAMO_ERR_CUDA before any GPU work
+// and is not cleared. Once work is queued, every return synchronises the stream first, so no kernel of the
+// call is still running on the shared array when it returns.
+#include <cuda.h>  // CUcontext and the types of the two driver entry points (no link to the driver library)
+
 #include <cstdint>
 #include <mutex>
 
@@ -33,12 +41,18 @@ constexpr int kNoAllocMaxTriangles = 65536;
 constexpr size_t kNoAllocBytes = 24u << 20;  // 24 MiB
 constexpr int kExactCap = 8 * kNoAllocMaxTriangles;
 constexpr float kTriEps = 1e-3f;  // cusimp_free.cu:893
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
+constexpr int kCachedContexts = 64;
+
 std::mutex g_setup_mutex;
-unsigned char* g_scratch_ptr[kMaxDevices] = {};
+struct CachedAddress {
+    unsigned long long ctx_id;  // 0 = empty slot
+    unsigned char* ptr;
+};
+CachedAddress g_scratch_cache[kCachedContexts] = {};
+int g_scratch_next = 0;
 
 size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -80,17 +94,54 @@ Layout carve(unsigned char* base) {
     return L;
 }
 
-// Device address of the scratch array on the current device; looked up once per device.
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+// The process-unique id of the current context (cuCtxGetId), or 0 where no context is current yet or the
+// driver cannot report it. The driver entry points are resolved through the runtime once.
+unsigned long long current_context_id() {
+    static PfnCtxGetCurrent get_current = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (PfnCtxGetCurrent)p;
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (PfnCtxGetId)p;
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return 0;
+    unsigned long long id = 0;
+    return get_id(ctx, &id) == CUDA_SUCCESS ? id : 0;
+}
+
+// Device address of the scratch array in the current context: looked up once per context and cached by the
+// context's id; looked up on every call where the id is unknown.
 int scratch_on_current_device(unsigned char** out) {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return PAMO_ERR_CUDA;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return PAMO_ERR_CUDA;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return PAMO_ERR_CUDA;
-        g_scratch_ptr[dev] = (unsigned char*)p;
+    unsigned long long id = current_context_id();
+    if (id != 0)
+        for (const CachedAddress& c : g_scratch_cache)
+            if (c.ctx_id == id) {
+                *out = c.ptr;
+                return PAMO_OK;
+            }
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return PAMO_ERR_CUDA;
+    id = current_context_id();  // the lookup made the device's primary context current if none was
+    if (id != 0) {
+        g_scratch_cache[g_scratch_next] = CachedAddress{id, (unsigned char*)p};
+        g_scratch_next = (g_scratch_next + 1) % kCachedContexts;
     }
-    *out = g_scratch_ptr[dev];
+    *out = (unsigned char*)p;
     return PAMO_OK;
 }
 
@@ -111,6 +162,7 @@ extern "C" int pamo_self_intersect_noalloc(const float* points, const int32_t* t
                                            int32_t n_triangles, uint8_t* face_hit, pamo_stream stream) {
     if (!points || !triangles || !face_hit || n_points < 1 || n_triangles < 1) return PAMO_ERR_INVALID_ARG;
     if (n_points > kNoAllocMaxPoints || n_triangles > kNoAllocMaxTriangles) return PAMO_ERR_CAPACITY;
+    if (cudaPeekAtLastError() != cudaSuccess) return PAMO_ERR_CUDA;  // the caller's pending error, left as is
     unsigned char* base = nullptr;
     int r = scratch_on_current_device(&base);
     if (r) return r;
@@ -133,11 +185,13 @@ extern "C" int pamo_self_intersect_noalloc(const float* points, const int32_t* t
     pamo::bvh_build(bvh, L.tri, L.pos, L.rc, n_triangles, s, false, L.qflag, false);
     pamo::bvh_query(bvh, L.tri, L.pos, L.qlist, L.qflag, L.hit, L.exact, kExactCap, L.rc, n_triangles, kTriEps, s);
     cudaMemcpyAsync(face_hit, L.hit, n_triangles, cudaMemcpyDeviceToDevice, s);
-
-    if (cudaGetLastError() != cudaSuccess) return PAMO_ERR_CUDA;
-    if (cudaStreamSynchronize(s) != cudaSuccess) return PAMO_ERR_CUDA;
     int status = 0;
-    if (cudaMemcpy(&status, &L.rc->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return PAMO_ERR_CUDA;
+    cudaMemcpyAsync(&status, &L.rc->status, sizeof(int), cudaMemcpyDeviceToHost, s);
+
+    // whatever happened, nothing of this call may still run on the shared array when it returns
+    const cudaError_t launched = cudaGetLastError();
+    const cudaError_t finished = cudaStreamSynchronize(s);
+    if (launched != cudaSuccess || finished != cudaSuccess) return PAMO_ERR_CUDA;
     if (status & pamo::kErrBadIndex) return PAMO_ERR_INVALID_ARG;
     if (status & (pamo::kErrStackOverflow | pamo::kErrIterLimit)) return PAMO_ERR_ITER_LIMIT;
     if (status & pamo::kErrCapacity) return PAMO_ERR_CAPACITY;
