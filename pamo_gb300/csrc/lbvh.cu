@@ -84,8 +84,11 @@ __global__ void __launch_bounds__(256) k_boxes(const int4* __restrict__ tri, con
 }
 
 // ---------------------------------------------------------------- Morton codes of live faces
+// fmesh (many meshes in one numbering): the key's top mesh_bits hold the face's mesh and the rest the top bits of its
+// Morton code, so that the sort groups each mesh's faces and every Karras node under a mesh boundary covers one mesh
 __global__ void __launch_bounds__(256) k_morton(const RoundCounters* rc, const int* live_scan, const float4* box_lo,
-                                                 const float4* box_hi, const unsigned* scene, unsigned* keys, int* vals) {
+                                                 const float4* box_hi, const unsigned* scene, unsigned* keys, int* vals,
+                                                 const int* __restrict__ fmesh, int mesh_bits) {
     const int n = rc->n_tris;
     float lo[3], ext[3];
 #pragma unroll
@@ -106,7 +109,12 @@ __global__ void __launch_bounds__(256) k_morton(const RoundCounters* rc, const i
             t = fminf(fmaxf(t * 1024.0f, 0.0f), 1023.0f);
             q[d] = (unsigned)t;
         }
-        keys[i] = expand10(q[0]) * 4u + expand10(q[1]) * 2u + expand10(q[2]);
+        unsigned key = expand10(q[0]) * 4u + expand10(q[1]) * 2u + expand10(q[2]);
+        if (fmesh) {
+            const unsigned m = (unsigned)fmesh[f];
+            key = mesh_bits <= 2 ? ((m << 30) | key) : ((m << (32 - mesh_bits)) | (key >> (mesh_bits - 2)));
+        }
+        keys[i] = key;
         vals[i] = f;
     }
 }
@@ -412,11 +420,18 @@ __device__ __forceinline__ bool box_overlap4(float4 qlo, float4 qhi, float4 lo, 
 // next query in the same iteration in which the other lanes of its warp take their next node, so the lanes
 // stay busy until the warp runs out of queries. A query whose pair does not fit the list, or whose deferred
 // siblings do not fit the short stack, stops and is marked in redo[qi] (and counted in rc->pad[3]).
+// With fmesh, a query walks only the subtree of its own mesh (mesh_root; < 0: the mesh has one leaf, no pair).
+__device__ __forceinline__ int query_root(int f, const int* __restrict__ fmesh, const int* __restrict__ mesh_root) {
+    return fmesh ? mesh_root[fmesh[f]] : 0;
+}
+
 __global__ void __launch_bounds__(kQueryThreads) k_traverse_list(const float4* __restrict__ packed,
                                                                   const float4* __restrict__ box_lo,
                                                                   const float4* __restrict__ box_hi,
                                                                   const int* __restrict__ qsorted, int2* pairs_out,
-                                                                  int pair_cap, RoundCounters* rc, int* redo) {
+                                                                  int pair_cap, RoundCounters* rc, int* redo,
+                                                                  const int* __restrict__ fmesh,
+                                                                  const int* __restrict__ mesh_root) {
     __shared__ int stack[kShortStack][kQueryThreads];
     int* n_list = &rc->pad[1];
     const int nq = rc->pad[2];
@@ -436,9 +451,10 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse_list(const float4* _
             redo[qi] = 0;
             if (empty) continue;
             f = qsorted[qi];
+            node = query_root(f, fmesh, mesh_root);
+            if (node < 0) continue;
             qlo = box_lo[f];
             qhi = box_hi[f];
-            node = 0;
             sp = 0;
             guard = 0;
         }
@@ -516,7 +532,9 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse_redo(const float4* _
                                                                   const int4* __restrict__ tri,
                                                                   const float4* __restrict__ pos,
                                                                   const int* __restrict__ qsorted, unsigned char* hit,
-                                                                  RoundCounters* rc, float eps, const int* redo) {
+                                                                  RoundCounters* rc, float eps, const int* redo,
+                                                                  const int* __restrict__ fmesh,
+                                                                  const int* __restrict__ mesh_root) {
     __shared__ int stack[kStackDepth][kQueryThreads];
     if (rc->pad[3] == 0) return;
     const int nq = rc->pad[2];
@@ -524,9 +542,10 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse_redo(const float4* _
     for (int qi = gtid(); qi < nq; qi += gstride()) {
         if (redo[qi] == 0) continue;
         const int f = qsorted[qi];
+        int node = query_root(f, fmesh, mesh_root);
+        if (node < 0) continue;
         const float4 qlo = box_lo[f], qhi = box_hi[f];
         int sp = 0;
-        int node = 0;
         int guard = 0;
         while (true) {
             if (++guard > (1 << 22)) {
@@ -591,6 +610,25 @@ __global__ void __launch_bounds__(128, 6) k_pairs(const int4* __restrict__ tri, 
     if ((threadIdx.x & 31) == 0 && exact) atomicAdd(&rc->n_exact, (unsigned long long)exact);
 }
 
+// The subtree root of each mesh: its live faces are the leaves [live_scan[f0], live_scan[f0 + nf]) of a tree built
+// with mesh keys; a Karras node has one end of its range at its own index, so the node covering exactly that range
+// is internal node lo or hi. -1 for a mesh with fewer than two leaves.
+__global__ void k_mesh_roots(const RoundCounters* rc, const int* __restrict__ live_scan, const int2* __restrict__ range,
+                             const int* __restrict__ mesh_f0, const int* __restrict__ mesh_nf, const int* d_count,
+                             int* root) {
+    const int n = *d_count;
+    const int n_live = rc->n_live;
+    for (int m = gtid(); m < n; m += gstride()) {
+        const int lo = live_scan[mesh_f0[m]], hi = live_scan[mesh_f0[m] + mesh_nf[m]] - 1;
+        int r = -1;
+        if (hi > lo && n_live >= 2) {
+            const int2 a = range[lo];
+            r = (a.x == lo && a.y == hi) ? lo : hi;
+        }
+        root[m] = r;
+    }
+}
+
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 }  // namespace
@@ -649,13 +687,14 @@ void bvh_carve(BvhBuffers& b, int cap, char* base, bool clear_scan_scratch) {
 }
 
 void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s,
-               bool all_faces, const int* qscan, bool nodes) {
+               bool all_faces, const int* qscan, bool nodes, const BvhMeshes* meshes) {
     cudaMemsetAsync(b.scene, 0xFF, 3 * sizeof(unsigned), s);
     cudaMemsetAsync(b.scene + 3, 0x00, 3 * sizeof(unsigned), s);
     const int gF = grid_for(n_tris_bound, 256);
     k_boxes<<<gF, 256, 0, s>>>(tri, pos, rc, b.box_lo, b.box_hi, b.live_scan, b.scene, all_faces ? 1 : 0); note_launch();
     exclusive_scan(b.live_scan, b.live_scan, &rc->n_tris, 1, &rc->n_live, b.scan_scratch, s, &rc->status, n_tris_bound);
-    k_morton<<<gF, 256, 0, s>>>(rc, b.live_scan, b.box_lo, b.box_hi, b.scene, b.keys[0], b.vals[0]); note_launch();
+    k_morton<<<gF, 256, 0, s>>>(rc, b.live_scan, b.box_lo, b.box_hi, b.scene, b.keys[0], b.vals[0],
+                                meshes ? meshes->fmesh : nullptr, meshes ? meshes->bits : 0); note_launch();
     // sort tiles from the launch's bound (about 2048 keys per tile; all kSortTiles from 2^19 on, where callers
     // cap their bounds); the histogram is
     // digit-major over the tiles, so its scan gives each tile's output offset per digit
@@ -670,6 +709,11 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
     }
     k_leaves<<<gF, 256, 0, s>>>(rc, b.vals[0], b.box_lo, b.box_hi, b.llo, b.lhi, b.visit, b.lparent); note_launch();
     k_karras<<<gF, 256, 0, s>>>(rc, b.keys[0], b.child, b.iparent, b.lparent, b.range); note_launch();
+    if (meshes) {
+        k_mesh_roots<<<grid_for(meshes->count_bound, 256), 256, 0, s>>>(rc, b.live_scan, b.range, meshes->f0, meshes->nf,
+                                                                          meshes->d_count, meshes->root);
+        note_launch();
+    }
     const int gT = tile_grid(n_tris_bound);
     if (nodes)
         k_bottom_up_tiles<true, true><<<gT, kTileThreads, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.range,
@@ -761,7 +805,7 @@ void bvh_remap(BvhBuffers& b, const int* fscan, int n_tris_bound, cudaStream_t s
 
 void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, const int* qscan,
                unsigned char* hit, int2* pair_list, int pair_cap, RoundCounters* rc, int n_query_bound, float eps,
-               cudaStream_t s) {
+               cudaStream_t s, const int* fmesh, const int* mesh_root) {
     (void)qlist;
     cudaMemsetAsync(&rc->pad[1], 0, 3 * sizeof(int), s);  // list length, query count, redo count
     // query faces in leaf order (uses the sort's second buffers, free after the build)
@@ -773,20 +817,20 @@ void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const in
     k_query_gather<<<gF, 256, 0, s>>>(rc, b.vals[0], b.live_scan, b.vals[1]);
     note_launch();
     // b.visit (free between a tree's bottom-up passes) holds the per-query redo marks
-    static int blocks_per_sm = 0;
-    if (blocks_per_sm == 0) {
+    // a function-local static initialiser runs once even when worker threads query concurrently
+    static const int blocks_per_sm = [] {
         int nb = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_traverse_list, kQueryThreads, 0) != cudaSuccess || nb < 1)
             nb = 4;
-        blocks_per_sm = nb;
-    }
+        return nb;
+    }();
     k_traverse_list<<<grid_for(n_query_bound, kQueryThreads, blocks_per_sm), kQueryThreads, 0, s>>>(
-        b.packed, b.box_lo, b.box_hi, b.vals[1], pair_list, pair_cap, rc, b.visit);
+        b.packed, b.box_lo, b.box_hi, b.vals[1], pair_list, pair_cap, rc, b.visit, fmesh, mesh_root);
     note_launch();
     k_pairs<<<grid_for((long long)pair_cap, 128, 16), 128, 0, s>>>(tri, pos, pair_list, pair_cap, hit, rc, eps);
     note_launch();
     k_traverse_redo<<<grid_for(n_query_bound, kQueryThreads, 4), kQueryThreads, 0, s>>>(
-        b.packed, b.box_lo, b.box_hi, tri, pos, b.vals[1], hit, rc, eps, b.visit);
+        b.packed, b.box_lo, b.box_hi, tri, pos, b.vals[1], hit, rc, eps, b.visit, fmesh, mesh_root);
     note_launch();
 }
 
