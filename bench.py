@@ -38,6 +38,9 @@ CONFIGS = {
                     "tolerance 4, min_verts 0; stage 3 off"),
 }
 STAGE3_STEPS = 5  # PaMO.run's process(..., 5) (simp_cuda/pamo/__init__.py:168-176)
+# DRAM bytes (read + write) per launch of the roofline kernel, from one ncu capture of the same workload
+# (dram__bytes_read.sum + dram__bytes_write.sum averaged over its launches); null where none was taken
+NCU_DRAM_BYTES_PER_LAUNCH = {"plain_large": {"edge_cost": 253243523.8}}
 THRESHOLD, TOLERANCE = 1e-3, 4
 L2_FLUSH_BYTES = 512 << 20
 
@@ -127,10 +130,19 @@ def compulsory_bytes(phase: str, t: dict) -> tuple[float, str]:
     return 32.0 * V + 32.0 * F, "32 B/vertex + 32 B/face"
 
 
-def cpu_sample(v, f, ratio, gpu_faces_per_round, budget_s=15.0, threads=None, stage3_input=None):
+def _digests(outs):
+    import hashlib
+
+    return [[hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest() for a in o] for o in outs]
+
+
+def cpu_sample(v, f, ratio, faces_per_round, budget_s=15.0, threads=None, stage3_input=None, stage3_s=None,
+               keep_rounds=0):
     """Times the oracle (OpenMP) on the first rounds of the same job until budget_s, then projects stage 2 with
-    the face counts per round of the GPU run (time per face-round is taken as constant). With stage3_input
-    (V, F, description) the float64 stage-3 oracle runs whole on that mesh and its time is added."""
+    the face counts per round of the whole job (time per face-round is taken as constant). With stage3_input
+    (V, F, description) the float64 stage-3 oracle runs whole on that mesh and its time is added; stage3_s
+    (seconds, description) adds an already measured stage-3 time instead. keep_rounds > 0 keeps the digests of
+    the five outputs of that many first rounds (for the parity check with the GPU's rounds)."""
     from oracle import oracle as orc
 
     threads = threads or os.cpu_count() or 1
@@ -143,10 +155,13 @@ def cpu_sample(v, f, ratio, gpu_faces_per_round, budget_s=15.0, threads=None, st
     t0 = time.perf_counter()
     face_rounds = 0
     rounds = 0
+    kept = []
     while True:
         out = o.forward(verts, faces, undo, len(undo), scale, THRESHOLD, False, rounds == 0)
         face_rounds += len(faces)
         rounds += 1
+        if len(kept) < keep_rounds:
+            kept.append(out)
         vv, tt, occ, vmap, undo = out
         verts = vv[occ[:, 0].astype(bool)]
         faces = vmap[:, 0][tt[tt[:, 0] >= 0]].astype(np.int32)
@@ -154,11 +169,10 @@ def cpu_sample(v, f, ratio, gpu_faces_per_round, budget_s=15.0, threads=None, st
             break
     dt = time.perf_counter() - t0
     rate = face_rounds / dt
-    total_face_rounds = int(len(f) + sum(gpu_faces_per_round[:-1])) if gpu_faces_per_round else face_rounds
+    total_face_rounds = int(len(f) + sum(faces_per_round[:-1])) if faces_per_round else face_rounds
     projected = total_face_rounds / rate
     sample = (f"oracle (OpenMP, {threads} threads) ran the first {rounds} rounds ({face_rounds} face-rounds) in "
-              f"{dt:.1f} s; stage 2 projected from the per-round face counts of the GPU run ({total_face_rounds} "
-              f"face-rounds)")
+              f"{dt:.1f} s; stage 2 projected to the job's {total_face_rounds} face-rounds")
     s3_out = None
     if stage3_input is not None:
         V2, F2, what = stage3_input
@@ -167,6 +181,9 @@ def cpu_sample(v, f, ratio, gpu_faces_per_round, budget_s=15.0, threads=None, st
         t3 = time.perf_counter() - t1
         projected += t3
         sample += f"; stage 3 (float64 oracle) run whole on {what} ({len(F2)} faces) in {t3:.1f} s"
+    elif stage3_s is not None:
+        projected += stage3_s[0]
+        sample += f"; stage 3: {stage3_s[1]}"
     return {
         "value": len(f) / projected,
         "unit": "input faces/s",
@@ -175,7 +192,31 @@ def cpu_sample(v, f, ratio, gpu_faces_per_round, budget_s=15.0, threads=None, st
         "sample": sample,
         "projected_job_s": projected,
         "stage3_out": s3_out,
+        "kept_digests": _digests(kept),
+        "mean": mean,
+        "scale": scale,
     }
+
+
+def gpu_round_digests(v_centred, f, scale, rounds, dev):
+    """Digests of the five outputs of the first `rounds` rounds of CUDSP_Free.forward (the GPU round entry) with
+    the same chaining as cpu_sample (not stuck, shuffle on the first round)."""
+    import torch
+
+    import pamo_gb300
+
+    op = pamo_gb300.CUDSP_Free()
+    verts = torch.from_numpy(np.ascontiguousarray(v_centred, np.float32)).to(dev)
+    faces = torch.from_numpy(np.ascontiguousarray(f, np.int32)).to(dev)
+    undo = torch.zeros(0, dtype=torch.int32, device=dev)
+    outs = []
+    for r in range(rounds):
+        res = op.forward(verts, faces, undo, undo.shape[0], scale, THRESHOLD, False, r == 0)
+        outs.append([t.cpu().numpy() for t in res])
+        vv, tt, occ, vmap, undo = res
+        verts = vv[occ[:, 0].bool()]
+        faces = vmap[:, 0][tt[tt[:, 0] >= 0].long()].to(torch.int32).contiguous()
+    return _digests(outs)
 
 
 def replica_throughput(local_value: float, units: float, world: int, device, per="ms") -> tuple[float, float]:
@@ -193,41 +234,78 @@ def replica_throughput(local_value: float, units: float, world: int, device, per
     return t, world * units / seconds
 
 
+def reference_config(args, out_faces, rounds, merge_identity):
+    """The `config` object both arms print for a plain configuration (the same keys and values)."""
+    mesh, ratio, stage3, desc = CONFIGS[args.config]
+    return {"workload": f"{args.config}: {desc}", "stage3": stage3, "parallelism": f"replicas{args.gpus}",
+            "l2": "GPU arm: 512 MiB buffer written between timed steps; CPU arm: inputs larger than the host caches",
+            "output_faces": int(out_faces), "rounds": int(rounds), "stage3_merge_identity": bool(merge_identity)}
+
+
 def run_reference(args):
-    """CPU reference arm: the oracle restatement of the reference's algorithm on all host cores."""
+    """CPU reference arm: the oracle restatement of the reference's algorithm on all host cores.
+
+    The whole job (stage-2 loop, then stage 3 on its own output) runs once, measured, with the time of each of its
+    rounds. Each step is a bounded sample: the job's first stage-2 rounds again, timed, and scaled by the measured
+    job's ratio of its whole stage-2 time to the time of those same rounds, plus the measured stage-3 time; the
+    projection error of the steps against the measured job is reported."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    from oracle import oracle as orc
     from pamo_gb300 import synth
 
     mesh, ratio, stage3, desc = CONFIGS[args.config]
     v, f = synth.config_mesh(mesh, seed=0)
     threads = os.cpu_count() or 1
-    s3_in = None
+    # the whole job, once
+    o = orc.Oracle(threads=threads)
+    t0 = time.perf_counter()
+    V2, F2, fpr = o.run(v, f, ratio, tolerance=TOLERANCE, threshold=THRESHOLD, min_verts=0)
+    t2 = time.perf_counter() - t0
+    per_round = o.round_seconds()
+    fpr = [int(x) for x in fpr]
+    t3, merge_identity = 0.0, True
     if stage3:
-        # stand-in for the stage-2 output (not available without running the whole stage-2 job): the same
-        # surface at icosphere frequency 16 (5120 faces, the size the job's 0.1 % output has)
-        V2, F2 = synth.star_mesh(16, 16, lambda l: 0.05 / l, 0)
-        s3_in = (V2.astype(np.float64), F2, "a 5120-face mesh of the same surface standing in for the stage-2 output")
-    budget = 8.0 if args.config == "plain_large" else 2.0
-    # face counts per round of the whole job (identical on the GPU path and the oracle), for the projection
-    fpr = []
-    rec = os.path.join(ROOT, "profiles", f"faces_per_round_{args.config}.json")
-    if os.path.exists(rec):
-        fpr = json.load(open(rec))["faces_per_round"]
-    vals = []
+        from pamo_gb300 import safe_project
+
+        Vm, Fm = safe_project.mesh_process(V2, F2)
+        merge_identity = len(Vm) == len(V2) and np.array_equal(Fm, F2)
+        t1 = time.perf_counter()
+        orc.stage3_run(v.astype(np.float64), f, Vm.astype(np.float64), Fm, STAGE3_STEPS)
+        t3 = time.perf_counter() - t1
+    measured_s = t2 + t3
+    k = 2 if args.config == "plain_large" else max(1, len(fpr) // 4)  # rounds per step sample
+    scale_k = t2 / float(per_round[:k].sum())  # whole stage 2 / its first k rounds, in the measured job
+    vals, samples = [], []
     for i in range(args.warmup + args.steps):
-        s = cpu_sample(v, f, ratio, fpr, budget_s=budget, threads=threads, stage3_input=s3_in)
+        ts = time.perf_counter()
+        orc.Oracle(threads=threads).run(v, f, ratio, tolerance=TOLERANCE, threshold=THRESHOLD, iters=k, min_verts=0)
+        dt = time.perf_counter() - ts
         if i >= args.warmup:
-            vals.append(s)
-    value = float(np.median([s["value"] for s in vals]))
+            projected = dt * scale_k + t3
+            vals.append(len(f) / projected)
+            samples.append(projected)
+    value = float(np.median(vals))
+    projected_s = len(f) / value
+    sample = (f"oracle (OpenMP, {threads} threads): each step runs the job's first {k} stage-2 rounds "
+              f"({len(f) + sum(fpr[:k - 1])} face-rounds), scaled by the measured job's whole stage-2 time over "
+              f"those rounds' time ({scale_k:.2f}x)")
+    if stage3:
+        sample += (f", plus the measured stage-3 time ({t3:.1f} s, float64 oracle on the oracle's own "
+                   f"{len(F2)}-face stage-2 output)")
     line = {
         "impl": "reference", "metric": "input faces/s to 0.1% ratio", "value": value, "unit": "input faces/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * len(f) / value,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * projected_s,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{args.config}: {desc}", "stage3": stage3},
-        "cpu_baseline": {k: vals[-1][k] for k in ("unit", "cores", "kind", "sample")} | {"value": value},
+        "config": reference_config(args, len(F2), len(fpr), merge_identity),
+        "cpu_baseline": {"value": value, "unit": "input faces/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "input faces/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "measured_job": {"seconds": measured_s, "value": len(f) / measured_s, "stage2_s": t2, "stage3_s": t3,
+                         "rounds": len(fpr), "output_faces": int(len(F2)),
+                         "how": "the oracle's whole job once, before the steps: its stage-2 loop, then stage 3 on "
+                                "its own stage-2 output; ms_per_step is the steps' projection of this job"},
+        "projection_error": abs(projected_s - measured_s) / measured_s,
     }
     print(json.dumps(line))
     return 0
@@ -530,8 +608,8 @@ def main():
     s3_stats = s3.stats() if s3 is not None else None
     totals = ctx.run_totals()
     fpr = simp.round_faces(ctx, rounds)
-    # roofline kernel: k_edge_cost, the largest single kernel of the job's launch list
-    # (profiles/launches_plain_large.md); its launches are timed by events on the round stream in the timed region
+    # roofline kernel: k_edge_cost, the largest single kernel of the job's launch list; its launches are timed by
+    # events on the round stream in the timed region
     dom = "edge_cost"
     peak, peak_kind = load_peaks()
     run_bytes, unit_desc = compulsory_bytes(dom, totals)
@@ -539,13 +617,7 @@ def main():
     dom_n = int(cost_n)
     avg_launch_ms = cost_ms / max(1, cost_n)
     achieved = per_launch_bytes / (avg_launch_ms / 1000.0) / 1e9 if cost_n else None
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tfile):
-        try:
-            traffic = json.load(open(tfile)).get(args.config, {}).get(dom)
-        except Exception:
-            traffic = None
+    traffic = NCU_DRAM_BYTES_PER_LAUNCH.get(args.config, {}).get(dom)
     # the same arithmetic for every phase of the profiled job (host-sized rounds with per-phase events)
     phase_roofline = {}
     for ph, (pms, pn) in prof.items():
@@ -563,6 +635,7 @@ def main():
     cpu_qem = None
     precision = None
     quality = None
+    parity = None
     if not args.no_cpu_baseline:
         from oracle import oracle as orc
 
@@ -573,9 +646,27 @@ def main():
             return orc.hausdorff(Va, Fa, Vb, Fb)[0]
 
         s3_in = (stage2_out[0], stage2_out[1], "the stage-2 output of the GPU run") if s3 is not None else None
-        cpu = cpu_sample(v, f, ratio, fpr, budget_s=12.0 if args.config == "plain_large" else 3.0, stage3_input=s3_in)
+        cpu = cpu_sample(v, f, ratio, fpr, budget_s=12.0 if args.config == "plain_large" else 3.0, stage3_input=s3_in,
+                         keep_rounds=3)
         cpu.pop("projected_job_s", None)
         ref3 = cpu.pop("stage3_out", None)
+        # stage-2 parity on this workload: the oracle rounds just timed against the GPU's rounds on the same input
+        kept = cpu.pop("kept_digests")
+        mean, scale = cpu.pop("mean"), cpu.pop("scale")
+        got = gpu_round_digests((v - mean).astype(np.float32), f, scale, len(kept), dev)
+        # the whole job with the skinny term squared by multiplication (the oracle's form) instead of the device's
+        # pow(float, int) that the reference and this path call
+        ctx2 = pamo_gb300.Context(dev)
+        ctx2.set_option("skinny_pow", 0)
+        alt = pamo_gb300.simplify(pts, tri, ratio, TOLERANCE, THRESHOLD, 1000000, 0, ctx=ctx2)
+        ref2 = pamo_gb300.simplify(pts, tri, ratio, TOLERANCE, THRESHOLD, 1000000, 0, ctx=ctx)
+        same_sq = bool(torch.equal(alt[0], ref2[0]) and torch.equal(alt[1], ref2[1]) and alt[2] == ref2[2])
+        del ctx2
+        parity = {"config": args.config, "rounds_checked": len(kept), "identical": got == kept,
+                  "whole_job_same_with_multiplied_squares": same_sq,
+                  "what": "SHA-256 of the five outputs (positions, faces, occupancy, map, undo list) of each of the "
+                          "first rounds: the oracle rounds timed for cpu_baseline against CUDSP_Free.forward on "
+                          "the GPU, same centred input, same chaining"}
         if ref3 is not None:
             got = prof_out[0].cpu().numpy()
             diag = float(np.linalg.norm(stage2_out[0].max(0) - stage2_out[0].min(0)))
@@ -611,9 +702,7 @@ def main():
         "metric": "input faces/s to 0.1% ratio", "value": value, "unit": "input faces/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{args.config}: {desc}", "stage3": stage3, "parallelism": f"replicas{world}",
-                   "l2": "512 MiB buffer written between timed steps", "output_faces": out_faces, "rounds": rounds,
-                   "stage3_merge_identity": merge_identity},
+        "config": reference_config(args, out_faces, rounds, merge_identity),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic, "kernel": "k_edge_cost",
                      "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_launch_bytes, "launches": dom_n,
@@ -625,6 +714,7 @@ def main():
         "stage3": s3_stats,
         "precision": precision,
         "quality": quality,
+        "parity": parity,
         "cpu_baseline": cpu,
         "cpu_qem": cpu_qem,
         "e2e": {"value": e2e, "unit": "input faces/s", "h2d_bytes_per_step": int(v.nbytes + f.nbytes),

@@ -35,6 +35,8 @@ def lib():
         L.oracle_tris_mean.argtypes = [P, P, I, P]
         L.oracle_run.argtypes = [P, P, P, I, I, D, I, F, I, LL, P, P]
         L.oracle_run_result.argtypes = [P, P, P, P]
+        L.oracle_run_round_seconds.argtypes = [P, P, I]
+        L.oracle_run_round_seconds.restype = I
         L.oracle_run_blender.argtypes = [P, P, P, I, I, F, P, P]
         L.oracle_self_intersect.argtypes = [P, P, P, I, I, P]
         L.oracle_self_intersect.restype = LL
@@ -190,6 +192,13 @@ class Oracle:
         fpr = np.zeros(max(rounds, 1), np.int32)
         lib().oracle_run_result(self._h, _p(V), _p(F), _p(fpr))
         return V, F, fpr[:rounds]
+
+    def round_seconds(self) -> np.ndarray:
+        """Wall time of each round of the last run()/run_blender() (seconds)."""
+        n = lib().oracle_run_round_seconds(self._h, None, 0)
+        out = np.zeros(max(n, 1), np.float64)
+        lib().oracle_run_round_seconds(self._h, _p(out), n)
+        return out[:n]
 
     def run_blender(self, points, triangles, threshold=1e-3):
         """The Blender add-on's pamo_simplify loop: returns (verts, faces, faces_per_round)."""

@@ -26,6 +26,7 @@
 // Memory the reference reads before writing (fresh cudaMalloc blocks) is modelled as zero-filled.
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -972,6 +973,7 @@ struct RunState {
     std::vector<int> faces;
     int rounds = 0;
     std::vector<int> faces_per_round;
+    std::vector<double> round_seconds;  // wall time of each round (the forward call and the compaction)
 };
 
 }  // namespace
@@ -1087,8 +1089,10 @@ static int run_loop(void* h, const float* pts, const int* tris, int nP, int nT, 
     int count = 0;
     bool stuck = false, init = true;
     R.faces_per_round.clear();
+    R.round_seconds.clear();
     int rounds = 0;
     for (int it = 0; it < iters; ++it) {
+        const auto t0 = std::chrono::steady_clock::now();
         const int nf_prev = (int)(faces.size() / 3);
         const int np = (int)(verts.size() / 3);
         o.forward(verts.data(), faces.data(), undo.data(), (int)undo.size(), np, nf_prev, scale, threshold, stuck, init);
@@ -1111,6 +1115,7 @@ static int run_loop(void* h, const float* pts, const int* tris, int nP, int nT, 
         faces.swap(nf);
         const int nf_cur = (int)(faces.size() / 3);
         R.faces_per_round.push_back(nf_cur);
+        R.round_seconds.push_back(std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
         if (!blender && (nf_cur <= target || nf_cur <= 10)) break;
         if (nf_cur == nf_prev) {
             count++;
@@ -1136,6 +1141,14 @@ int oracle_run(void* h, const float* pts, const int* tris, int nP, int nT, doubl
                int iters, long long min_verts, int* out_nP, int* out_nT) {
     const long long target = std::max((long long)(ratio * (double)nT), min_verts);
     return run_loop(h, pts, tris, nP, nT, target, tolerance, threshold, iters, false, out_nP, out_nT);
+}
+
+// wall time of each round of the last run (seconds); returns the number of rounds
+int oracle_run_round_seconds(void* h, double* out, int cap) {
+    const RunState& R = ((pamo_oracle_handle*)h)->run;
+    const int n = (int)R.round_seconds.size();
+    for (int i = 0; i < n && i < cap; ++i) out[i] = R.round_seconds[i];
+    return n;
 }
 
 // pamo_simplify of the Blender add-on: scale from the host bounding box of the raw vertices
