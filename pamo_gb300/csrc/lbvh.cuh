@@ -31,6 +31,19 @@ struct BvhBuffers {
     int* meta = nullptr;               // [0]: leaves of the current tree (kept across refits)
 };
 
+// Many meshes in one face numbering (faces of mesh m: [f0[m], f0[m] + nf[m]), meshes in face order): the tree keeps
+// each mesh in its own subtree (its mesh index in the top `bits` key bits, 1 <= bits <= 16) and writes each mesh's
+// subtree root to root[m] (-1 below two live faces); d_count meshes, at most count_bound.
+struct BvhMeshes {
+    const int* fmesh = nullptr;  // mesh of each face
+    int bits = 0;
+    const int* f0 = nullptr;
+    const int* nf = nullptr;
+    const int* d_count = nullptr;
+    int count_bound = 0;
+    int* root = nullptr;
+};
+
 size_t bvh_bytes(int cap);
 // Lays the buffers out from base; clear_scan_scratch zeroes the tree's scan scratch (synchronous), which
 // memory that is not zero-initialised needs before its first build.
@@ -43,7 +56,8 @@ void bvh_carve(BvhBuffers& b, int cap, char* base, bool clear_scan_scratch = tru
 // nodes: also keep the internal node boxes nlo/nhi for every node (the traversals of the projection stage read
 // them); the packed records that bvh_query reads are always written.
 void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters* rc, int n_tris_bound, cudaStream_t s,
-               bool all_faces = false, const int* qscan = nullptr, bool nodes = true);
+               bool all_faces = false, const int* qscan = nullptr, bool nodes = true,
+               const BvhMeshes* meshes = nullptr);
 
 // New boxes for the leaves of a tree built with all_faces (a removed face, or a leaf whose face is gone, gets an
 // empty box that overlaps nothing); sets rc->n_live to the tree's leaf count. next_round: first take the leaf
@@ -67,8 +81,10 @@ void bvh_refit(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
 // order. The tree must have been built or refitted with the same qscan (face ids below 2^30). Candidate pairs
 // go through pair_list (capacity pair_cap; queries beyond it decide their pairs in place).
 // qlist is unused (kept for callers that hold one).
+// With fmesh and mesh_root (from a bvh_build with BvhMeshes), each query walks only its own mesh's subtree, so
+// pairs never join two meshes.
 void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const int* qlist, const int* qscan,
                unsigned char* hit, int2* pair_list, int pair_cap, RoundCounters* rc, int n_query_bound, float eps,
-               cudaStream_t s);
+               cudaStream_t s, const int* fmesh = nullptr, const int* mesh_root = nullptr);
 
 }  // namespace pamo

@@ -103,6 +103,19 @@ __device__ __forceinline__ long long spread_first() {
 }
 __device__ __forceinline__ long long spread_stride() { return (long long)gridDim.x * blockDim.x; }
 
+// The quantised collapse threshold of forward() (cusimp_free.cu:923): clamp(threshold, 0, 10) / 10 * 2^32 as
+// uint32, saturating (the reference's host conversion is undefined beyond the range; NaN clamps to the upper bound).
+inline uint32_t collapse_threshold(float threshold) {
+    constexpr float kRange = 10.0f;
+    float t = threshold > 0.0f ? threshold : 0.0f;
+    t = (t < kRange) ? t : kRange;
+    if (threshold != threshold) t = kRange;
+    const float f = t / kRange * 4294967296.0f;
+    if (!(f > 0.0f)) return 0u;
+    if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)f;
+}
+
 // Host-side count of kernels this library has launched (for launch accounting in benchmarks).
 void note_launch();
 void note_launches(long long n);  // kernels run by a CUDA graph launch

@@ -37,15 +37,6 @@ struct DevBuf {
     size_t bytes() const { return p ? n * sizeof(T) : 0; }
 };
 
-inline uint32_t collapse_threshold(float threshold) {  // cusimp_free.cu:923, saturating
-    float t = threshold > 0.0f ? threshold : 0.0f;  // clamp of cusimp_free.cu:34 (NaN -> upper bound)
-    t = (t < kCostRange) ? t : kCostRange;
-    if (threshold != threshold) t = kCostRange;
-    const float f = t / kCostRange * 4294967296.0f;
-    if (!(f > 0.0f)) return 0u;
-    if (f >= 4294967296.0f) return 0xFFFFFFFFu;
-    return (uint32_t)f;
-}
 
 }  // namespace
 
@@ -165,6 +156,7 @@ struct pamo_ctx {
     bool use_graphs = true;     // device rounds as cached graphs
     bool device_rounds = true;  // rounds after the first from device-resident sizes (pamo_simplify_device)
     bool bvh_reuse = true;      // device rounds refit the LBVH carried from the previous round
+    bool skinny_pow = true;     // the skinny term squares with the device's pow(float, int), as the reference does
     long long pair_cap_limit = 0;  // > 0: at most this many listed candidate pairs per check (tests the overflow path)
 
     int pair_cap() const {
@@ -445,7 +437,7 @@ struct pamo_ctx {
         launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
         cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
         launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p, vmin.p,
-                         d_scale, threshold, 0, s, nullptr, true);
+                         d_scale, threshold, 0, s, nullptr, true, skinny_pow);
         launch_face_keys(rc, nT, tri.p, vmin.p, fkey.p, s);
         launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p,
                         orig_pos.p, occ.p, win.p, s, false);
@@ -496,7 +488,7 @@ struct pamo_ctx {
             launch_fill_u64_dev(rc, nPb, vmin.p, ~0ull, s);
             cost_begin(s);
             launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p,
-                             vmin.p, d_scale, threshold, 0, s, &d_ls->is_stuck);
+                             vmin.p, d_scale, threshold, 0, s, &d_ls->is_stuck, false, skinny_pow);
             cost_end(s);
             launch_face_keys(rc, nTb, tri.p, vmin.p, fkey.p, s);
             launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p,
@@ -672,7 +664,7 @@ struct pamo_ctx {
         prof.begin(kPhCost, s);
         cost_begin(s);
         launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p, vmin.p,
-                         d_scale, threshold, is_stuck, s);
+                         d_scale, threshold, is_stuck, s, nullptr, false, skinny_pow);
         cost_end(s);
         prof.end(kPhCost, s);
         prof.begin(kPhCollapse, s);
@@ -790,6 +782,10 @@ int pamo_ctx_set_option(pamo_ctx* ctx, const char* name, int64_t value) {
     if (n == "graphs") ctx->use_graphs = value != 0;
     else if (n == "device_rounds") ctx->device_rounds = value != 0;
     else if (n == "bvh_reuse") ctx->bvh_reuse = value != 0;
+    else if (n == "skinny_pow") {
+        ctx->skinny_pow = value != 0;
+        ctx->drop_graphs();
+    }
     else if (n == "time_rounds") ctx->time_rounds = value != 0;
     else if (n == "time_edge_cost") {
         ctx->time_cost = value != 0;
@@ -813,7 +809,9 @@ int pamo_forward_round(pamo_ctx* ctx, const float* points, const int32_t* triang
                        int32_t is_stuck, int32_t init, pamo_stream stream) {
     if (!ctx) return PAMO_ERR_INVALID_ARG;
     ctx->err.clear();
-    if (n_points < 1 || n_triangles < 1 || !points || !triangles || n_verts_undo < 0 || (n_verts_undo > 0 && !verts_undo))
+    // a round on zero faces is valid (the reference's loop makes one after a mesh has lost all its faces)
+    if (n_points < 1 || n_triangles < 0 || !points || (n_triangles > 0 && !triangles) || n_verts_undo < 0 ||
+        (n_verts_undo > 0 && !verts_undo))
         return ctx->fail(PAMO_ERR_INVALID_ARG, "invalid sizes or null pointers");
     cudaSetDevice(ctx->device);
     ctx->stream = (cudaStream_t)stream;
@@ -834,7 +832,7 @@ int pamo_legacy_round(pamo_ctx* ctx, const float* points, const int32_t* triangl
                       int32_t n_triangles, float scale, float threshold, int32_t init, pamo_stream stream) {
     if (!ctx) return PAMO_ERR_INVALID_ARG;
     ctx->err.clear();
-    if (n_points < 1 || n_triangles < 1 || !points || !triangles)
+    if (n_points < 1 || n_triangles < 0 || !points || (n_triangles > 0 && !triangles))
         return ctx->fail(PAMO_ERR_INVALID_ARG, "invalid sizes or null pointers");
     cudaSetDevice(ctx->device);
     ctx->stream = (cudaStream_t)stream;
@@ -863,7 +861,7 @@ int pamo_round_outputs(pamo_ctx* ctx, float* verts, int32_t* tris, int32_t* vert
                        int32_t* verts_undo, pamo_stream stream) {
     if (!ctx) return PAMO_ERR_INVALID_ARG;
     if (!ctx->have_round) return ctx->fail(PAMO_ERR_STATE, "no round has run");
-    if (!verts || !tris) return ctx->fail(PAMO_ERR_INVALID_ARG, "verts and tris are required");
+    if (!verts || (!tris && ctx->out_nt > 0)) return ctx->fail(PAMO_ERR_INVALID_ARG, "verts and tris are required");
     cudaSetDevice(ctx->device);
     cudaStream_t s = (cudaStream_t)stream;
     launch_export_round(ctx->rc, ctx->out_np, ctx->out_nt, ctx->pos.p, ctx->tri.p, ctx->occ.p, ctx->pts_map.p,
@@ -1127,7 +1125,7 @@ int pamo_simplify(float* in_verts, int* in_tris, float* out_verts, int* out_tris
 int pamo_simplify_result(pamo_ctx* ctx, float* verts, int32_t* tris, pamo_stream stream) {
     if (!ctx) return PAMO_ERR_INVALID_ARG;
     if (!ctx->have_run) return ctx->fail(PAMO_ERR_STATE, "no simplification has run");
-    if (!verts || !tris) return ctx->fail(PAMO_ERR_INVALID_ARG, "verts and tris are required");
+    if (!verts || (!tris && ctx->out_nt > 0)) return ctx->fail(PAMO_ERR_INVALID_ARG, "verts and tris are required");
     cudaSetDevice(ctx->device);
     launch_export_mesh(ctx->run_np, ctx->run_nt, ctx->pos_in.p, ctx->tri_in.p, ctx->d_center, verts, tris,
                        (cudaStream_t)stream);

@@ -13,6 +13,7 @@
 #include <cstdint>
 #include "scan.cuh"
 #include "simp_round.cuh"
+#include "round_ops.cuh"
 
 namespace pamo {
 
@@ -251,6 +252,44 @@ __device__ __forceinline__ void ring_len(int w, const int* __restrict__ nt_off, 
 // The flip test dot(n_old/|n_old|, n_new/|n_new|) < 0 takes its sign from the unnormalised normals when a
 // float bound proves it (|dot| > 1e-5 |n_old|_1 |n_new|_1, far above the ~1e-6 relative rounding of the
 // normalised form); otherwise the normalised form is evaluated exactly as the reference does.
+// The squared lengths of the skinny term: the reference squares with the device's pow(float, int)
+// (cusimp_free.cu:533,573, cusimp.cu:423,463), which on the GPU differs from x * x by one ulp for a few floats in
+// a million and costs far more; kPow = false squares by multiplication (the oracle's form).
+template <bool kPow>
+__device__ __forceinline__ float sq_len(float x) {
+    if constexpr (kPow) return pow(x, 2);
+    else return x * x;
+}
+
+// The skinny sum 4*sqrt(3)*A/l01^2 + l12^2 + l20^2 + 1e-7 (only the first square divides: the reference's
+// precedence), in float, or in double for the legacy round (cusimp.cu:423,463: `4.0f * sqrt(3)` takes the
+// integer overload of sqrt).
+template <bool kLegacy>
+__device__ __forceinline__ float skinny_sum(float k4s3, float area, float p01, float p12, float p20) {
+    if constexpr (kLegacy)
+        return (float)((double)4.0f * sqrt(3.0) * (double)area / (double)p01 + (double)p12 + (double)p20 +
+                       (double)0.0000001f);
+    else
+        return k4s3 * area / p01 + p12 + p20 + 0.0000001f;
+}
+
+// The term 1 - clamp(sum, 0, 1) with the reference's squares. The sum is first taken with x * x: the device's
+// pow(float, int) is within 2 ulp of it (CUDA's documented powf bound) for squares in the normal range, the sum is
+// monotone in each square (area >= 0) and rounding is monotone, so a sum of at least 1 + 1e-5 with x * x is at
+// least 1 with the device's squares too, and the term is 0 either way. Only other sums (below the margin, tiny
+// squares, NaN) are evaluated again with the device's pow.
+template <bool kLegacy, bool kPow>
+__device__ __forceinline__ float skinny_term(float k4s3, float area, float l01, float l12, float l20) {
+    const float q01 = l01 * l01, q12 = l12 * l12, q20 = l20 * l20;
+    float e = skinny_sum<kLegacy>(k4s3, area, q01, q12, q20);
+    if constexpr (kPow) {
+        const bool saturated = e >= 1.00001f && q01 >= 1e-30f && q12 >= 1e-30f && q20 >= 1e-30f;
+        if (!saturated) e = skinny_sum<kLegacy>(k4s3, area, sq_len<true>(l01), sq_len<true>(l12), sq_len<true>(l20));
+    }
+    return 1.0f - rclamp(e, 0.0f, 1.0f);
+}
+
+template <bool kLegacy, bool kPow>
 __device__ __forceinline__ bool ring_skinny(int w, int other, V3 vm, const int* __restrict__ nt_off,
                                             const int* __restrict__ nt, const int4* __restrict__ tri,
                                             const float4* __restrict__ pos, const float4* __restrict__ fgeo, float& qa,
@@ -281,9 +320,7 @@ __device__ __forceinline__ bool ring_skinny(int w, int other, V3 vm, const int* 
         const float l20 = (wz || wx) ? vnorm(vsub(n2, n0)) : lg.z;
         const float sh = (l01 + l12 + l20) / 2;  // triangle_area (Heron), :368-375
         const float area = sqrtf(sh * (sh - l01) * (sh - l12) * (sh - l20));
-        // the reference's operator precedence: only the first squared length divides (pow(x, 2) == x * x)
-        const float e = k4s3 * area / (l01 * l01) + l12 * l12 + l20 * l20 + 0.0000001f;
-        qa += 1.0f - rclamp(e, 0.0f, 1.0f);
+        qa += skinny_term<kLegacy, kPow>(k4s3, area, l01, l12, l20);
         ntri++;
     }
     return true;
@@ -296,7 +333,7 @@ __device__ __forceinline__ uint32_t f2u_sat(float f) {
 // returns false when the reference leaves the stale cost in place. kLegacy: the cost of CUSimp
 // (cusimp.cu:270-471): the mean ring length is counted twice (`edge_len += edge_len + |e|`) and the skinny term
 // has no penalty factor.
-template <bool kLegacy>
+template <bool kLegacy, bool kPow>
 __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restrict__ nt_off, const int* __restrict__ nt,
                                                 const int4* __restrict__ tri, const float4* __restrict__ pos,
                                                 const Quadric* __restrict__ q, const float4* __restrict__ fgeo,
@@ -327,8 +364,8 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
     const V3 vm = vdiv(vadd(v0, v1), 2.0f);
     float qa = 0.0f;
     int ntri = 0;
-    if (!ring_skinny(u, v, vm, nt_off, nt, tri, pos, fgeo, qa, ntri) ||
-        !ring_skinny(v, u, vm, nt_off, nt, tri, pos, fgeo, qa, ntri)) {
+    if (!ring_skinny<kLegacy, kPow>(u, v, vm, nt_off, nt, tri, pos, fgeo, qa, ntri) ||
+        !ring_skinny<kLegacy, kPow>(v, u, vm, nt_off, nt, tri, pos, fgeo, qa, ntri)) {
         out = 0xFFFFFFFFu;
         return true;
     }
@@ -350,7 +387,9 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
     return true;
 }
 
-template <bool kLegacy>
+// kBatch: many meshes in one vertex numbering; the scale and is_stuck of an edge's mesh come from per-mesh arrays
+// (mesh of the lower vertex from vmesh) instead of d_scale and the single flag.
+template <bool kLegacy, bool kPow, bool kBatch>
 __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const int* __restrict__ eorder,
                                                   const int2* __restrict__ edges,
                                                   const int* __restrict__ nt_off, const int* __restrict__ nt,
@@ -358,14 +397,24 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
                                                   const Quadric* __restrict__ q, const float4* __restrict__ fgeo,
                                                   const int* __restrict__ nxt, const unsigned char* __restrict__ invalid,
                                                   uint32_t* cost, unsigned long long* vmin, const float* d_scale,
-                                                  float tres, int is_stuck_host, const int* is_stuck_dev) {
-    const int is_stuck = is_stuck_dev ? *is_stuck_dev : is_stuck_host;
+                                                  float tres, int is_stuck_host, const int* is_stuck_dev,
+                                                  const int* __restrict__ vmesh, const int* __restrict__ mesh_stuck) {
+    int is_stuck = 0;
+    float scale = 0.0f;
+    if constexpr (!kBatch) {
+        is_stuck = is_stuck_dev ? *is_stuck_dev : is_stuck_host;
+        scale = *d_scale;
+    }
     const int n = rc->n_edges;
-    const float scale = *d_scale;
     for (int i = gtid(); i < n; i += gstride()) {
         const int e = eorder[i];  // edges grouped by their lower vertex: neighbouring threads share rings
         const int2 ed = edges[e];
         const int u = ed.x, v = ed.y;
+        if constexpr (kBatch) {
+            const int m = vmesh[u];
+            scale = d_scale[m];
+            is_stuck = mesh_stuck[m];
+        }
         uint32_t c = 0;
         bool write;
         if (!kLegacy && invalid[u] && invalid[v]) {
@@ -374,7 +423,7 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
         } else if (!kLegacy && is_stuck) {
             write = false;
         } else {
-            write = edge_cost_value<kLegacy>(u, v, nt_off, nt, tri, pos, q, fgeo, nxt, scale, tres, c);
+            write = edge_cost_value<kLegacy, kPow>(u, v, nt_off, nt, tri, pos, q, fgeo, nxt, scale, tres, c);
         }
         if (write) cost[e] = c;
         else c = cost[e];  // stale value of an earlier round
@@ -423,22 +472,6 @@ __device__ __forceinline__ bool is_skinny(V3 p, V3 q, V3 r) {  // :617-637
     return area < thr;
 }
 
-__device__ __forceinline__ void rewire(int u, int v, const int* __restrict__ nt_off, const int* __restrict__ nt, int4* tri) {
-    for (int s = nt_off[u]; s < nt_off[u + 1]; ++s) {
-        const int f = nt[s];
-        const int4 t = tri[f];
-        if (t.x == v || t.y == v || t.z == v) tri[f] = make_int4(-1, -1, -1, 0);
-    }
-    for (int s = nt_off[v]; s < nt_off[v + 1]; ++s) {
-        const int f = nt[s];
-        int4 t = tri[f];
-        if (t.x == u || t.y == u || t.z == u) t = make_int4(-1, -1, -1, 0);
-        else if (t.x == v) t.x = u;
-        else if (t.y == v) t.y = u;
-        else if (t.z == v) t.z = u;
-        tri[f] = t;
-    }
-}
 
 __device__ __forceinline__ bool ring_has_skinny(int w, const int* __restrict__ nt_off, const int* __restrict__ nt,
                                                 const int4* tri, const float4* pos) {
@@ -450,13 +483,6 @@ __device__ __forceinline__ bool ring_has_skinny(int w, const int* __restrict__ n
     return false;
 }
 
-__device__ __forceinline__ void restore_ring(int w, const int* __restrict__ nt_off, const int* __restrict__ nt, int4* tri,
-                                             const int4* __restrict__ orig_tri) {
-    for (int s = nt_off[w]; s < nt_off[w + 1]; ++s) {
-        const int f = nt[s];
-        tri[f] = orig_tri[f];
-    }
-}
 
 // kRestore = false: CUSimp's collapse (cusimp.cu:512-585), without the skinny-ring restore
 template <bool kRestore>
@@ -1113,14 +1139,39 @@ void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cos
 void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
                       const int* nt, const int4* tri, const float4* pos, const Quadric* q, const float4* fgeo,
                       const int* nxt, const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin,
-                      const float* d_scale, float tres, int is_stuck, cudaStream_t s, const int* is_stuck_dev, bool legacy) {
-    if (legacy)
-        k_edge_cost<true><<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt,
-                                                                     invalid, cost, vmin, d_scale, tres, 0, nullptr);
+                      const float* d_scale, float tres, int is_stuck, cudaStream_t s, const int* is_stuck_dev, bool legacy,
+                      bool device_pow) {
+    const int g = grid_for(n_edges_bound, kT);
+    if (legacy) {
+        if (device_pow)
+            k_edge_cost<true, true, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
+                                                            cost, vmin, d_scale, tres, 0, nullptr, nullptr, nullptr);
+        else
+            k_edge_cost<true, false, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
+                                                             cost, vmin, d_scale, tres, 0, nullptr, nullptr, nullptr);
+    } else if (device_pow) {
+        k_edge_cost<false, true, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
+                                                         cost, vmin, d_scale, tres, is_stuck, is_stuck_dev, nullptr,
+                                                         nullptr);
+    } else {
+        k_edge_cost<false, false, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
+                                                          cost, vmin, d_scale, tres, is_stuck, is_stuck_dev, nullptr,
+                                                          nullptr);
+    }
+    note_launch();
+}
+void launch_edge_cost_batch(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges,
+                            const int* nt_off, const int* nt, const int4* tri, const float4* pos, const Quadric* q,
+                            const float4* fgeo, const int* nxt, const unsigned char* invalid, uint32_t* cost,
+                            unsigned long long* vmin, const float* mesh_scale, const int* mesh_stuck, const int* vmesh,
+                            float tres, cudaStream_t s, bool device_pow) {
+    const int g = grid_for(n_edges_bound, kT);
+    if (device_pow)
+        k_edge_cost<false, true, true><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
+                                                        cost, vmin, mesh_scale, tres, 0, nullptr, vmesh, mesh_stuck);
     else
-        k_edge_cost<false><<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt,
-                                                                      invalid,
-                                                                      cost, vmin, d_scale, tres, is_stuck, is_stuck_dev);
+        k_edge_cost<false, false, true><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
+                                                         cost, vmin, mesh_scale, tres, 0, nullptr, vmesh, mesh_stuck);
     note_launch();
 }
 void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
@@ -1151,6 +1202,9 @@ void launch_line_edges(RoundCounters* rc, int n_edges_bound, const int2* edges, 
     (void)line_buf;
     k_line_detect<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, edges, pos); note_launch();
     k_line_apply<<<1, 32, 0, s>>>(rc, edges, nt_off, nt, tri, pos, occ, collapsed, line_cap); note_launch();
+}
+void launch_line_detect(RoundCounters* rc, int n_edges_bound, const int2* edges, const float4* pos, cudaStream_t s) {
+    k_line_detect<<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, edges, pos); note_launch();
 }
 void launch_mark_query(const RoundCounters* rc, int n_edges_bound, const int* collapsed, const int2* edges,
                        const int* nt_off, const int* nt, int* qflag, cudaStream_t s) {

@@ -43,7 +43,14 @@ void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eor
                       const int* nt, const int4* tri, const float4* pos, const Quadric* q, const float4* fgeo,
                       const int* nxt, const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin,
                       const float* d_scale, float tres, int is_stuck, cudaStream_t s, const int* is_stuck_dev = nullptr,
-                      bool legacy = false);
+                      bool legacy = false, bool device_pow = true);
+// The edge cost of many meshes in one vertex numbering: the scale and is_stuck of each edge's mesh (vmesh of its
+// lower vertex) come from mesh_scale and mesh_stuck.
+void launch_edge_cost_batch(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges,
+                            const int* nt_off, const int* nt, const int4* tri, const float4* pos, const Quadric* q,
+                            const float4* fgeo, const int* nxt, const unsigned char* invalid, uint32_t* cost,
+                            unsigned long long* vmin, const float* mesh_scale, const int* mesh_stuck, const int* vmesh,
+                            float tres, cudaStream_t s, bool device_pow = true);
 void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
                       unsigned long long* fkey, cudaStream_t s);
 void launch_collapse(RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const uint32_t* cost,
@@ -57,6 +64,8 @@ void launch_line_edges(RoundCounters* rc, int n_edges_bound, const int2* edges, 
                        int4* tri, float4* pos, int* occ, int* line_buf, int line_cap, int* collapsed, cudaStream_t s);
 
 // ---- self-intersection rollback ----
+// counts coincident-endpoint edges into rc->n_line (the first half of launch_line_edges)
+void launch_line_detect(RoundCounters* rc, int n_edges_bound, const int2* edges, const float4* pos, cudaStream_t s);
 void launch_mark_query(const RoundCounters* rc, int n_edges_bound, const int* collapsed, const int2* edges,
                        const int* nt_off, const int* nt, int* qflag, cudaStream_t s);
 void launch_compact_flags(const int* scan, int n_bound, const int* d_n, int* out_list, cudaStream_t s);
