@@ -20,3 +20,16 @@ def native_lib():
     import pamo_gb300._native as n
 
     return n.load()
+
+
+@pytest.fixture(scope="session")
+def torch_ext():
+    """The extension module pamo_gb300._C (built with the library)."""
+    import pamo_gb300._build as b
+
+    b.build()
+    import torch  # noqa: F401  (loads the torch libraries the module links)
+
+    import pamo_gb300._C as C
+
+    return C
