@@ -158,10 +158,12 @@ int pamo_self_intersect(pamo_ctx* ctx, const float* points, const int32_t* trian
  * (hosts that own a fixed memory budget and forbid cudaMalloc/cudaFree by plug-ins, or code that cannot
  * afford the device synchronisation an allocation may cause). No counterpart in the reference.
  * Same result as pamo_self_intersect; needs no context. Scratch is a 24 MiB array in device memory that
- * the library holds on every GPU that loads it; its address is looked up on the first call made on each
- * device, so make that first call before any stream capture. Limits: n_points <= 65536 and
- * n_triangles <= 65536, else PAMO_ERR_CAPACITY. All calls share the scratch: calls that overlap on the
- * GPU race. Uses the current device; synchronises `stream`.
+ * the library holds on every GPU that loads it; its address is looked up on the first call made in each CUDA
+ * context (a new context, e.g. after cudaDeviceReset, gets a new lookup), so make that first call before any
+ * stream capture. Limits: n_points <= 65536 and n_triangles <= 65536, else PAMO_ERR_CAPACITY. All calls
+ * share the scratch: calls that overlap on the GPU race. A CUDA error already pending from earlier work
+ * returns PAMO_ERR_CUDA before any GPU work (and stays pending). Uses the current device and context; every
+ * return after work was queued synchronises `stream` first.
  */
 int pamo_self_intersect_noalloc(const float* points, const int32_t* triangles, int32_t n_points,
                                 int32_t n_triangles, uint8_t* face_hit, pamo_stream stream);
@@ -211,6 +213,27 @@ int pamo_batch_simplify(pamo_batch* b, const float* points, const int32_t* trian
 
 /* Rounds each mesh of the last batch ran (host array); returns the number written. */
 int pamo_batch_rounds(const pamo_batch* b, int32_t* rounds, int32_t capacity);
+
+/* ------------------------------------------------------------------------------------------------------
+ * Batched rounds (no reference counterpart): many meshes concatenated in CSR form run the PaMO.run loop together
+ * on one stream, every round being one pass of the round's kernels over all live meshes (CUSimp_Free::forward,
+ * cusimp_free.cu:891-1048, once per mesh). The state the reference carries between rounds lives in fixed regions
+ * per mesh, each mesh gets its own LBVH subtree, loop control is per mesh, and a finished mesh leaves the next
+ * round: each result equals the mesh's result alone.
+ * ------------------------------------------------------------------------------------------------------ */
+typedef struct pamo_csr pamo_csr;
+int pamo_csr_create(pamo_csr** out, int device);
+int pamo_csr_destroy(pamo_csr* b);
+const char* pamo_csr_last_error(const pamo_csr* b);
+/* "skinny_pow" (default 1): the skinny term squares with the device's pow(float, int), as the reference does. */
+int pamo_csr_set_option(pamo_csr* b, const char* name, int64_t value);
+/* Same contract as pamo_batch_simplify (at most 65,536 meshes and 2^29 faces per call); synchronises `stream`. */
+int pamo_csr_simplify(pamo_csr* b, const float* points, const int32_t* triangles, const int64_t* vert_offsets,
+                      const int64_t* face_offsets, int32_t n_meshes, const double* ratios, int32_t tolerance,
+                      float threshold, int32_t iter, int64_t min_verts, float* out_points, int32_t* out_triangles,
+                      int64_t* out_vert_offsets, int64_t* out_face_offsets, pamo_stream stream);
+/* Rounds each mesh of the last call ran (host array); returns the number written. */
+int pamo_csr_rounds(const pamo_csr* b, int32_t* rounds, int32_t capacity);
 
 /* A request loop: n_workers workers; requests queue in arrival order and are admitted while the device bytes
  * they are estimated to need (pamo_server_job_bytes) fit hbm_budget_bytes (a request larger than the budget

@@ -66,6 +66,12 @@ SIGNATURES = {
     "pamo_simplify_round_gpu_ms": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _I32]),
     "pamo_self_intersect": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _P, _P]),
     "pamo_self_intersect_noalloc": (ctypes.c_int, [_P, _P, _I32, _I32, _P, _P]),
+    "pamo_csr_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int]),
+    "pamo_csr_destroy": (ctypes.c_int, [_P]),
+    "pamo_csr_last_error": (ctypes.c_char_p, [_P]),
+    "pamo_csr_set_option": (ctypes.c_int, [_P, ctypes.c_char_p, _I64]),
+    "pamo_csr_simplify": (ctypes.c_int, [_P, _P, _P, _P, _P, _I32, _P, _I32, _F32, _I32, _I64, _P, _P, _P, _P, _P]),
+    "pamo_csr_rounds": (ctypes.c_int, [_P, _PI32, _I32]),
     "pamo_run_totals": (ctypes.c_int, [_P, _PI64, _I32]),
     "pamo_launch_count": (ctypes.c_int64, []),
     "pamo_profile_enable": (ctypes.c_int, [_P, _I32]),

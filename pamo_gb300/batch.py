@@ -1,8 +1,9 @@
 """Many meshes on one GPU: batched simplification and a request server over the C ABI.
 
-Both run the whole PaMO.run stage-2 loop per mesh on a pool of worker contexts (one CUDA stream and host
-thread each, in ``libpamo_gb300.so``); every job starts from the state of a new context, so a mesh's result is
-the same alone, in a batch, or among other requests.
+``CsrBatch`` runs all meshes of a CSR batch through the PaMO.run stage-2 loop together, every round one pass of the
+round's kernels over all live meshes (``pamo_csr_*``). ``Batch`` and ``Server`` run the whole loop per mesh on a pool
+of worker contexts (one CUDA stream and host thread each). Every mesh starts from the state of a new context, so a
+mesh's result is the same alone, in a batch, or among other requests.
 """
 
 from __future__ import annotations
@@ -74,6 +75,61 @@ class Batch:
         return out[:k]
 
 
+class CsrBatch:
+    """Batched rounds (``pamo_csr_*``): all meshes of a CSR batch run the PaMO.run loop together on one stream,
+    every round one pass of the round's kernels over all live meshes; each result equals the mesh's result alone."""
+
+    def __init__(self, device=None):
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        lib = _native.load()
+        h = ctypes.c_void_p()
+        st = lib.pamo_csr_create(ctypes.byref(h), self.device.index or 0)
+        if st != _native.PAMO_OK:
+            raise _native.PamoError(st, "pamo_csr_create")
+        self._lib, self._h = lib, h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._lib.pamo_csr_destroy(h)
+            except Exception:  # interpreter shutdown
+                pass
+            self._h = None
+
+    def set_option(self, name: str, value: int):
+        st = self._lib.pamo_csr_set_option(self._h, name.encode(), int(value))
+        if st != _native.PAMO_OK:
+            raise _native.PamoError(st, _err(self._lib.pamo_csr_last_error, self._h))
+
+    def simplify_csr(self, points: torch.Tensor, triangles: torch.Tensor, vert_offsets, face_offsets, ratios,
+                     tolerance: int = 4, threshold: float = 1e-3, iter: int = 1000000, min_verts: int = 0):
+        """The contract of Batch.simplify_csr."""
+        n = len(vert_offsets) - 1
+        voff = np.ascontiguousarray(vert_offsets, dtype=np.int64)
+        foff = np.ascontiguousarray(face_offsets, dtype=np.int64)
+        rat = np.ascontiguousarray(np.broadcast_to(np.asarray(ratios, dtype=np.float64), (n,)))
+        pts = points.to(self.device, torch.float32).contiguous()
+        tri = triangles.to(self.device, torch.int32).contiguous()
+        out_p = torch.empty_like(pts)
+        out_t = torch.empty_like(tri)
+        ovoff = np.zeros(n + 1, np.int64)
+        ofoff = np.zeros(n + 1, np.int64)
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        st = self._lib.pamo_csr_simplify(self._h, pts.data_ptr(), tri.data_ptr(), voff.ctypes.data, foff.ctypes.data,
+                                         n, rat.ctypes.data, int(tolerance), ctypes.c_float(threshold), int(iter),
+                                         int(min_verts), out_p.data_ptr(), out_t.data_ptr(), ovoff.ctypes.data,
+                                         ofoff.ctypes.data, ctypes.c_void_p(stream))
+        if st != _native.PAMO_OK:
+            raise _native.PamoError(st, _err(self._lib.pamo_csr_last_error, self._h))
+        return out_p[: ovoff[-1]], out_t[: ofoff[-1]], ovoff, ofoff
+
+    def rounds(self, n: int) -> np.ndarray:
+        out = np.zeros(n, np.int32)
+        k = self._lib.pamo_csr_rounds(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), n)
+        return out[:k]
+
+
 def pack(meshes):
     """[(V [n,3], F [m,3]), ...] -> (points, triangles, vert_offsets, face_offsets) NumPy CSR form."""
     voff = np.zeros(len(meshes) + 1, np.int64)
@@ -93,9 +149,10 @@ def unpack(points, triangles, voff, foff):
 
 
 def simplify_batch(meshes, ratios, tolerance: int = 4, threshold: float = 1e-3, iter: int = 1000000,
-                   min_verts: int = 0, workers: int | None = None, batch: Batch | None = None):
-    """Simplify a list of (V, F) meshes; returns a list of (V float32, F int32) NumPy results."""
-    batch = batch or Batch(workers=workers)
+                   min_verts: int = 0, workers: int | None = None, batch=None):
+    """Simplify a list of (V, F) meshes; returns a list of (V float32, F int32) NumPy results. Batched rounds
+    (CsrBatch) unless a worker count or a Batch is given."""
+    batch = batch or (Batch(workers=workers) if workers is not None else CsrBatch())
     P, T, voff, foff = pack(meshes)
     out = batch.simplify_csr(torch.from_numpy(P).to(batch.device), torch.from_numpy(T).to(batch.device), voff, foff,
                              ratios, tolerance, threshold, iter, min_verts)
