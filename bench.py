@@ -324,6 +324,206 @@ def synth_batch(n_meshes, f_lo, f_hi, seed):
     return meshes, ratios
 
 
+def precision_stage2(v, f, pts, tri, ratio, dev):
+    """Stage-2 precision figures on this workload's input: each edge's cost before quantisation from one round of
+    the CUDA path (pamo_cost_probe) in the reference's float order (mode 0), with compensated sums (1), and with the
+    placement at the quadric's minimiser (2), against the float64 oracle of the cost (oracle/cost_fp64.cpp) on the
+    edges the GPU found valid; and the whole job in modes 1 and 2 (faces, self-intersections, Hausdorff)."""
+    import torch
+
+    import pamo_gb300
+    from oracle import oracle as orc
+
+    vc = (v - orc.tris_mean(v, f)).astype(np.float32)  # the centred input the first round sees
+    scale = float(np.max(vc.max(0) - vc.min(0)))
+    diag = float(np.linalg.norm(v.max(0) - v.min(0)))
+    vcd = torch.from_numpy(vc).to(dev)
+    out = {"what": "relative error of each valid edge's float32 cost (before clamp and quantisation) against float64, "
+                   "first round of the input; placement error over the bounding-box diagonal"}
+    c64 = {}
+    for mode in (0, 1, 2):
+        e, c, p = (t.cpu().numpy() for t in pamo_gb300.cost_probe(vcd, tri, scale, THRESHOLD, mode))
+        ok = np.isfinite(c)
+        optimal = mode == 2
+        if optimal not in c64:
+            c64[optimal] = orc.cost_fp64(vc, f, e[ok], scale, THRESHOLD, optimal)
+        ref, ref_p = c64[optimal]
+        rel = np.abs(c[ok].astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-30)
+        rec = {"edges": int(ok.sum()), "median": float(np.median(rel)), "p99": float(np.percentile(rel, 99)),
+               "max": float(rel.max())}
+        if optimal:
+            perr = np.abs(p[ok].astype(np.float64) - ref_p).max(1) / diag
+            rec["placement_over_diag"] = {"p99": float(np.percentile(perr, 99)), "max": float(perr.max())}
+        out[["reference_order", "compensated", "compensated_optimal_placement"][mode]] = rec
+    jobs = {}
+    diag_in = float(np.linalg.norm(v.max(0) - v.min(0)))
+    for mode in (1, 2):
+        ctx = pamo_gb300.Context(dev)
+        ctx.set_option("precision", mode)
+        V, F, rounds = pamo_gb300.simplify(pts, tri, ratio, TOLERANCE, THRESHOLD, 1000000, 0, ctx=ctx)
+        Vn, Fn = V.cpu().numpy().astype(np.float64), F.cpu().numpy()
+        jobs[["", "compensated", "compensated_optimal_placement"][mode]] = {
+            "output_faces": int(len(Fn)), "rounds": int(rounds),
+            "self_intersecting_pairs": orc.self_intersections(Vn, Fn)[0],
+            "hausdorff_over_bbox_diag": orc.hausdorff(Vn, Fn, v, f)[0] / diag_in}
+    out["whole_job_stage2"] = jobs
+    return out
+
+
+def batch_record(dev, steps=2):
+    """C4 inside the default run, after its timed region: 256 star meshes (faces log-uniform 5k-200k, ratios
+    U[0.001, 0.01]) as one CSR batch through the batched rounds (every round one pass over all live meshes), against
+    the plain path (one context, one mesh after the other, each on a new context's state); results compared mesh by
+    mesh, and each result's two-sided vertex Hausdorff distance to its input over the input's bounding-box diagonal."""
+    import torch
+
+    import pamo_gb300
+    from oracle import oracle as orc
+    from pamo_gb300.batch import CsrBatch, pack, unpack
+
+    meshes, ratios = synth_batch(256, 5e3, 2e5, 7)
+    P, T, voff, foff = pack(meshes)
+    F0 = int(foff[-1])
+    Pd, Td = torch.from_numpy(P).to(dev), torch.from_numpy(T).to(dev)
+    ctx = pamo_gb300.Context(dev)
+    plain_out = []
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for i in range(len(meshes)):
+        ctx.reset()
+        V, Fo, _ = pamo_gb300.simplify(Pd[voff[i]:voff[i + 1]], Td[foff[i]:foff[i + 1]], float(ratios[i]), TOLERANCE,
+                                      THRESHOLD, 1000000, 0, ctx=ctx)
+        plain_out.append((V, Fo))
+    torch.cuda.synchronize(dev)
+    plain_s = time.perf_counter() - t0
+    b = CsrBatch(dev)
+    out = b.simplify_csr(Pd, Td, voff, foff, ratios)  # warm-up
+    stream = torch.cuda.current_stream(dev)
+    ms = []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = b.simplify_csr(Pd, Td, voff, foff, ratios)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    res = unpack(*out)
+    identical = all(np.array_equal(res[i][1], plain_out[i][1].cpu().numpy()) and
+                    np.array_equal(res[i][0], plain_out[i][0].cpu().numpy()) for i in range(len(meshes)))
+    hd = []
+    for (v, f), (V, Fo) in zip(meshes, res):
+        diag = float(np.linalg.norm(v.max(0) - v.min(0)))
+        hd.append(orc.hausdorff(V, Fo, v, f)[0] / diag)
+    hd = np.array(hd)
+    value = F0 / (float(np.mean(ms)) / 1000.0)
+    return {
+        "workload": f"256 star meshes, faces log-uniform 5k-200k ({F0} faces), SH l<=6 sigma 0.03, seed 7; ratios "
+                    "U[0.001,0.01], threshold 1e-3, tolerance 4, min_verts 0",
+        "value": value, "unit": "input faces/s", "ms": float(np.mean(ms)),
+        "timing": f"CUDA events around pamo_csr_simplify, inputs resident, mean of {steps} after 1 warm-up",
+        "plain": {"value": F0 / plain_s, "seconds": plain_s,
+                  "how": "one context, one mesh after the other (pamo_simplify_device on a reset context)"},
+        "vs_plain": value / (F0 / plain_s),
+        "identical_to_plain": bool(identical),
+        "rounds_max": int(b.rounds(len(meshes)).max()),
+        "hausdorff_over_bbox_diag": {"max": float(hd.max()), "median": float(np.median(hd)),
+                                     "over_1e-3": int((hd > 1e-3).sum()), "meshes": len(hd)},
+    }
+
+
+def serve_record(dev, n_req=2000, workers=16, stage3=True, sample_every=10):
+    """C5 inside the default run, after its timed region: a Poisson stream of n_req requests (mean 50/s) of star
+    meshes with faces log-uniform in [10k, 2M] (drawn from 48 distinct meshes), ratios U[0.001, 0.01], admitted by
+    an 80 GB device-memory budget into a pool of worker contexts; each request is a whole PaMO.run job (with
+    stage 3 onto its own input when stage3). Latency = arrival to result on the host. Plain path: sequential PaMO.run
+    (one job after the other, the same stages) on every sample_every-th request, measured; its latency under the
+    same arrivals is that of a single first-in-first-out server whose service times follow the measured jobs
+    (a line fitted to time against faces). Hausdorff: the two-sided vertex distance of each result to its input,
+    over the input's bounding-box diagonal (GPU point-to-mesh distances)."""
+    import torch
+
+    import pamo_gb300
+    from pamo_gb300 import metrics
+    from pamo_gb300.batch import Server
+
+    pool, _ = synth_batch(48, 1e4, 2e6, 11)
+    rng = np.random.default_rng(12)
+    pick = rng.integers(0, len(pool), n_req)
+    ratios = rng.uniform(0.001, 0.01, n_req)
+    arrivals = np.cumsum(rng.exponential(1.0 / 50.0, n_req))
+    faces = np.array([len(pool[k][1]) for k in pick], np.int64)
+    srv = Server(dev, workers=workers, hbm_budget_bytes=80 << 30)
+    lat = np.zeros(n_req)
+    results = [None] * n_req
+    ids = {}
+    t0 = time.perf_counter()
+    done = i = 0
+    while done < n_req:
+        now = time.perf_counter() - t0
+        while i < n_req and arrivals[i] <= now:
+            v, f = pool[pick[i]]
+            ids[srv.submit(v, f, float(ratios[i]), TOLERANCE, THRESHOLD, stage3=stage3)] = i
+            i += 1
+        w = srv.wait(1 if i < n_req else 1000)
+        while w is not None:
+            rid, st, npt, ntr, _ = w
+            k = ids[rid]
+            results[k] = srv.fetch(rid, npt, ntr, float64=stage3)  # raises with the server's message on a failure
+            lat[k] = (time.perf_counter() - t0) - arrivals[k]
+            done += 1
+            w = srv.wait(0)
+    wall = time.perf_counter() - t0
+    stats = srv.stats()
+    srv.close()
+    # plain: sequential PaMO.run on a sample of the requests
+    samp = np.arange(0, n_req, sample_every)
+    svc = []
+    for k in samp:
+        v, f = pool[pick[k]]
+        pm = pamo_gb300.PaMO((v.astype(np.float64), f), use_stage1=False, use_stage3=stage3)
+        pv, pf = torch.from_numpy(v).to(dev), torch.from_numpy(f).to(dev)
+        torch.cuda.synchronize(dev)
+        ts = time.perf_counter()
+        pm.run(pv, pf, ratio=float(ratios[k]), tolerance=TOLERANCE, threshold=THRESHOLD, min_verts=0)
+        torch.cuda.synchronize(dev)
+        svc.append(time.perf_counter() - ts)
+    svc = np.array(svc)
+    b, a = np.polyfit(faces[samp].astype(np.float64), svc, 1)
+    t_model = np.maximum(a + b * faces, 0.0)
+    finish = 0.0
+    lat_plain = np.zeros(n_req)
+    for k in range(n_req):  # one server, first in first out
+        finish = max(finish, arrivals[k]) + t_model[k]
+        lat_plain[k] = finish - arrivals[k]
+    # per-request Hausdorff distance to the input
+    hd = np.zeros(n_req)
+    for k in range(n_req):
+        v, f = pool[pick[k]]
+        V, F = results[k]
+        diag = float(np.linalg.norm(v.max(0) - v.min(0)))
+        hd[k] = metrics.hausdorff_vertices(V, F, v, f) / diag
+    plain_value = float(faces[samp].sum() / svc.sum())
+    value = float(faces.sum() / wall)
+    return {
+        "workload": f"{n_req} requests, Poisson arrivals mean 50/s, faces log-uniform 10k-2M drawn from 48 distinct "
+                    f"star meshes ({int(faces.sum())} faces), ratios U[0.001,0.01], 80 GB budget, "
+                    f"stage 3 {'on' if stage3 else 'off'}, {workers} workers",
+        "value": value, "unit": "input faces/s", "wall_s": wall,
+        "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3)},
+        "plain": {"value": plain_value, "measured_requests": int(len(samp)), "seconds": float(svc.sum()),
+                  "latency_ms": {"p50": float(np.percentile(lat_plain, 50) * 1e3),
+                                 "p99": float(np.percentile(lat_plain, 99) * 1e3)},
+                  "how": f"sequential PaMO.run on every {sample_every}th request (measured); latency of a single "
+                         "first-in-first-out server under the same arrivals with service time a + b * faces "
+                         f"fitted to them (a = {a * 1e3:.2f} ms, b = {b * 1e9:.2f} ns per face)"},
+        "vs_plain": value / plain_value,
+        "hausdorff_over_bbox_diag": {"max": float(hd.max()), "median": float(np.median(hd)),
+                                     "p99": float(np.percentile(hd, 99)), "over_1e-3": int((hd > 1e-3).sum()),
+                                     "requests": n_req},
+        "server": stats,
+    }
+
+
 def run_batch(args):
     """Batching: 256 meshes (5k-200k faces) per step through the worker pool, against the plain path (one
     context, one mesh after the other) on the same meshes."""
@@ -475,6 +675,8 @@ def main():
     ap.add_argument("--config", default="plain_large", choices=sorted(CONFIGS) + ["batch256", "serve"])
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-rounds record of the default run")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving record of the default run")
     ap.add_argument("--workers", type=int, default=16,
                     help="worker contexts for --config batch256 / serve (0: tuned on a sample first)")
     ap.add_argument("--requests", type=int, default=2000, help="requests for --config serve")
@@ -654,16 +856,16 @@ def main():
         kept = cpu.pop("kept_digests")
         mean, scale = cpu.pop("mean"), cpu.pop("scale")
         got = gpu_round_digests((v - mean).astype(np.float32), f, scale, len(kept), dev)
-        # the whole job with the skinny term squared by multiplication (the oracle's form) instead of the device's
-        # pow(float, int) that the reference and this path call
+        # the whole job with the skinny term squared by the device's pow(float, int), the reference's call, instead of
+        # the multiplication this path and the oracle use
         ctx2 = pamo_gb300.Context(dev)
-        ctx2.set_option("skinny_pow", 0)
+        ctx2.set_option("skinny_pow", 1)
         alt = pamo_gb300.simplify(pts, tri, ratio, TOLERANCE, THRESHOLD, 1000000, 0, ctx=ctx2)
         ref2 = pamo_gb300.simplify(pts, tri, ratio, TOLERANCE, THRESHOLD, 1000000, 0, ctx=ctx)
         same_sq = bool(torch.equal(alt[0], ref2[0]) and torch.equal(alt[1], ref2[1]) and alt[2] == ref2[2])
         del ctx2
         parity = {"config": args.config, "rounds_checked": len(kept), "identical": got == kept,
-                  "whole_job_same_with_multiplied_squares": same_sq,
+                  "whole_job_same_with_device_pow": same_sq,
                   "what": "SHA-256 of the five outputs (positions, faces, occupancy, map, undo list) of each of the "
                           "first rounds: the oracle rounds timed for cpu_baseline against CUDSP_Free.forward on "
                           "the GPU, same centred input, same chaining"}
@@ -686,6 +888,8 @@ def main():
                    "kind": "sequential priority-queue QEM (Garland-Heckbert, midpoint placement, link and flip checks)",
                    "sample": f"{n_col} collapses in {dt_q:.1f} s including set-up; projected to the {need} collapses "
                              f"of the job"}
+        if args.config == "plain_large" and precision is not None:
+            precision = {"stage3": precision, "stage2": precision_stage2(v, f, pts, tri, ratio, dev)}
         # output checks: exact-predicate self-intersection count and Hausdorff distance to the input
         fin = (prof_out[0].double().cpu().numpy(), prof_out[1].cpu().numpy())
         diag_in = float(np.linalg.norm(v.max(0) - v.min(0)))
@@ -697,6 +901,12 @@ def main():
         if s3 is not None:
             quality["stage2_self_intersecting_pairs"] = orc_si(*stage2_out)
             quality["stage2_hausdorff_over_bbox_diag"] = orc_hd(stage2_out[0], stage2_out[1], v, f) / diag_in
+
+    batch = serve = None
+    if args.config == "plain_large" and not args.no_batch:
+        batch = batch_record(dev)
+    if args.config == "plain_large" and not args.no_serve:
+        serve = serve_record(dev, n_req=args.requests)
 
     line = {
         "metric": "input faces/s to 0.1% ratio", "value": value, "unit": "input faces/s", "n_gpus": world,
@@ -715,6 +925,8 @@ def main():
         "precision": precision,
         "quality": quality,
         "parity": parity,
+        "batch": batch,
+        "serve": serve,
         "cpu_baseline": cpu,
         "cpu_qem": cpu_qem,
         "e2e": {"value": e2e, "unit": "input faces/s", "h2d_bytes_per_step": int(v.nbytes + f.nbytes),

@@ -50,12 +50,21 @@ int pamo_ctx_reset(pamo_ctx* ctx, pamo_stream stream);
 /* Device memory the context currently holds, in bytes (no reference counterpart; used for admission). */
 int64_t pamo_ctx_device_bytes(const pamo_ctx* ctx);
 
-/* Execution options of pamo_simplify_device (results are the same with any setting):
+/* Options of the stage-2 rounds (the execution options give the same results with any setting):
  *   "device_rounds" (default 1): rounds after the first read their sizes and loop state from device memory
  *                                and synchronise once per round (plus once per extra undo pass);
  *   "graphs"        (default 1): those rounds run as CUDA graphs cached per size class;
  *   "bvh_reuse"     (default 1): those rounds refit the LBVH carried from the previous round (rebuilt when a
- *                                quarter of its leaves lost their faces) instead of building it each round.
+ *                                quarter of its leaves lost their faces) instead of building it each round;
+ *   "precision"     (default 0): 0 the reference's float arithmetic; 1 (precision mode) quadric, ring-length,
+ *                                skinny and cost sums compensated (TwoSum/TwoProd, rounded once); 2 as 1 with each
+ *                                collapse placed at the edge quadric's minimiser instead of the reference's midpoint
+ *                                (float solve, double for near-singular quadrics, midpoint for singular ones);
+ *                                modes 1 and 2 change results and are not the reference's arithmetic;
+ *   "skinny_pow"    (default 0): 1 squares the skinny term's lengths with the device's pow(float, int), the
+ *                                reference's call (cusimp_free.cu:533,573), where 0 multiplies; the device function
+ *                                differs from the product by one ulp on a few floats in a million and costs the
+ *                                edge-cost kernel about 12x; every job measured so far is bit-identical either way.
  * The phase timers (pamo_profile_enable) use the host-sized path. */
 int pamo_ctx_set_option(pamo_ctx* ctx, const char* name, int64_t value);
 
@@ -83,6 +92,17 @@ int pamo_legacy_round(pamo_ctx* ctx, const float* points, const int32_t* triangl
 
 /* Shapes of the five outputs of the last round: verts [n_points,3], tris [n_triangles,3],
  * verts_occ [n_points,1], verts_map [n_points,1], verts_undo [n_verts_undo] (simp_cuda/src/pybind.cpp:74-102). */
+/* Precision probe (no reference counterpart): one round up to the edge costs (no shuffle, no collapse, fresh state)
+ * on device arrays, with precision mode 0 (the reference's float arithmetic), 1 (quadric, length, skinny and cost sums
+ * compensated by TwoSum/TwoProd) or 2 (as 1, placement at the edge quadric's minimiser: a float solve when well
+ * conditioned, a double solve when near-singular, the midpoint when singular). Writes n_edges and, when capacity
+ * allows, out_edges [n,2] (the reference's edge numbering), out_cost [n] (cost before clamp and quantisation, NaN
+ * where the edge is invalid) and out_place [n,3] (device arrays; any may be NULL). Overwrites the context's round
+ * state: use a context of its own. Synchronises `stream`. */
+int pamo_cost_probe(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                    int32_t n_triangles, float scale, float threshold, int32_t precision, int32_t* out_edges,
+                    float* out_cost, float* out_place, int32_t capacity, int32_t* n_edges, pamo_stream stream);
+
 int pamo_round_sizes(const pamo_ctx* ctx, int32_t* n_points, int32_t* n_triangles, int32_t* n_verts_undo);
 
 /* Copy the last round's outputs into caller-owned device buffers (any may be NULL to skip it). Removed
@@ -225,7 +245,7 @@ typedef struct pamo_csr pamo_csr;
 int pamo_csr_create(pamo_csr** out, int device);
 int pamo_csr_destroy(pamo_csr* b);
 const char* pamo_csr_last_error(const pamo_csr* b);
-/* "skinny_pow" (default 1): the skinny term squares with the device's pow(float, int), as the reference does. */
+/* "skinny_pow" (default 0): as pamo_ctx_set_option's option of the same name. */
 int pamo_csr_set_option(pamo_csr* b, const char* name, int64_t value);
 /* Same contract as pamo_batch_simplify (at most 65,536 meshes and 2^29 faces per call); synchronises `stream`. */
 int pamo_csr_simplify(pamo_csr* b, const float* points, const int32_t* triangles, const int64_t* vert_offsets,
@@ -246,6 +266,13 @@ const char* pamo_server_last_error(const pamo_server* s);
 int pamo_server_submit(pamo_server* s, const float* points, const int32_t* triangles, int32_t n_points,
                        int32_t n_triangles, double ratio, int32_t tolerance, float threshold, int64_t* request_id);
 
+/* pamo_server_submit with use_stage3 != 0: after stage 2 the job runs PaMO.run's stage 3 (trimesh's processing of
+ * the stage-2 mesh, then pamo_safe_project onto the request's own input mesh, 5 steps, default parameters), and its
+ * result has float64 positions (pamo_server_fetch_f64). */
+int pamo_server_submit_ex(pamo_server* s, const float* points, const int32_t* triangles, int32_t n_points,
+                          int32_t n_triangles, double ratio, int32_t tolerance, float threshold, int32_t use_stage3,
+                          int64_t* request_id);
+
 /* Wait up to timeout_ms for a finished request: returns 1 with its id, status, output sizes and times_ms[3]
  * (queued until admitted, admitted until finished, submitted until finished), or 0 on time-out. */
 int pamo_server_wait(pamo_server* s, int32_t timeout_ms, int64_t* request_id, int32_t* status, int32_t* out_n_points,
@@ -253,6 +280,8 @@ int pamo_server_wait(pamo_server* s, int32_t timeout_ms, int64_t* request_id, in
 
 /* Copy a finished request's result into host arrays (sizes from pamo_server_wait) and release it. */
 int pamo_server_fetch(pamo_server* s, int64_t request_id, float* points, int32_t* triangles);
+/* The same with float64 positions (a stage-3 result's own precision). */
+int pamo_server_fetch_f64(pamo_server* s, int64_t request_id, double* points, int32_t* triangles);
 
 /* Counters, out[0..n): bytes in use, most bytes in use so far, requests admitted, finished, queued, budget.
  * Returns 6. */

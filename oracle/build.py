@@ -1,6 +1,6 @@
 """Builds the CPU oracle (oracle/pamo_oracle.cpp: stage 2, oracle/stage3_oracle.cpp: stage 3,
 oracle/mesh_check.cpp: exact self-intersection check and Hausdorff distance, oracle/cpu_qem.cpp: the sequential
-QEM baseline) into oracle/build/libpamo_oracle.so.
+QEM baseline, oracle/cost_fp64.cpp: the float64 edge cost of the precision figures) into oracle/build/libpamo_oracle.so.
 
 Test infrastructure: the oracle is the checker of the CUDA path, loaded only by tests/, the smoke check of
 __graft_entry__ and the CPU-baseline leg of bench.py. -ffp-contract=off keeps every float product and sum
@@ -11,7 +11,8 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRCS = [os.path.join(HERE, n) for n in ("pamo_oracle.cpp", "stage3_oracle.cpp", "mesh_check.cpp", "cpu_qem.cpp")]
+SRCS = [os.path.join(HERE, n) for n in ("pamo_oracle.cpp", "stage3_oracle.cpp", "mesh_check.cpp", "cpu_qem.cpp",
+                                        "cost_fp64.cpp")]
 OUT = os.path.join(HERE, "build", "libpamo_oracle.so")
 
 

@@ -47,6 +47,8 @@ def lib():
         L.hausdorff.argtypes = [P, I, P, I, P, I, P, I, P]
         L.hausdorff.restype = D
         L.cpu_qem_simplify.argtypes = [P, I, P, I, LL, D, P]
+        L.oracle_cost_fp64.argtypes = [P, P, I, I, P, I, D, D, I, I, P, P]
+        L.oracle_cost_fp64.restype = I
         L.cpu_qem_simplify.restype = LL
         L.exact_orient3d.argtypes = [P]
         L.exact_orient3d.restype = I
@@ -317,6 +319,23 @@ def hausdorff(va, fa, vb, fb):
     out = np.zeros(2, np.float64)
     h = lib().hausdorff(_p(A), len(A), _p(FA), len(FA), _p(B), len(B), _p(FB), len(FB), _p(out))
     return float(h), float(out[0]), float(out[1])
+
+
+def cost_fp64(points, tris, edges, scale: float, threshold: float, optimal: bool = False, threads: int = 0):
+    """The reference's edge cost of each edge (u, v) in float64, before clamp and quantisation, with its placement
+    (the midpoint, or the quadric's minimiser with optimal): (cost [E], place [E,3])."""
+    import os
+
+    P = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    T = np.ascontiguousarray(tris, np.int32).reshape(-1, 3)
+    E = np.ascontiguousarray(edges, np.int32).reshape(-1, 2)
+    cost = np.zeros(len(E), np.float64)
+    place = np.zeros((len(E), 3), np.float64)
+    rc = lib().oracle_cost_fp64(_p(P), _p(T), len(P), len(T), _p(E), len(E), float(scale), float(threshold),
+                                int(bool(optimal)), int(threads or os.cpu_count() or 1), _p(cost), _p(place))
+    if rc:
+        raise ValueError("triangle index out of range")
+    return cost, place
 
 
 def cpu_qem(points, tris, target_faces: int, time_budget_s: float = 0.0):

@@ -154,8 +154,8 @@ inline int __clzll(long long x) { return x == 0 ? 64 : __builtin_clzll(static_ca
 // device overloads the reference's code relies on: min/max of floats are fminf/fmaxf, and pow(float, int)
 // stays in float (only squares occur: cusimp_free.cu:533,573, cusimp.cu:423,463). The device's pow(x, 2) is not
 // restated here: the square is taken by multiplication, which on the GPU differs from the device function by one
-// ulp for a few floats in a million (tests/test_gpu_device_pins.py measures it; the CUDA path calls the device
-// function and its GPU tests find the same results as with the multiplication)
+// ulp for a few floats in a million (tests/test_gpu_device_pins.py measures it, and finds the CUDA path's rounds the
+// same with the device function as with the multiplication)
 inline float min(float a, float b) { return fminf(a, b); }
 inline float max(float a, float b) { return fmaxf(a, b); }
 inline double min(double a, double b) { return fmin(a, b); }

@@ -14,6 +14,7 @@ from .api import (  # noqa: F401
     PaMO,
     PaSP,
     Remesher,
+    cost_probe,
     launch_count,
     pamo_simplify,
     round_faces,

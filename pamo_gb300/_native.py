@@ -51,6 +51,7 @@ SIGNATURES = {
                                                    ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
                                                    ctypes.POINTER(ctypes.c_int32), _P]),
     "pamo_tris_mean": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _P, _P]),
+    "pamo_cost_probe": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _F32, _F32, _I32, _P, _P, _P, _I32, _PI32, _P]),
     "pamo_round_sizes": (ctypes.c_int, [_P, _PI32, _PI32, _PI32]),
     "pamo_round_outputs": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "pamo_round_stats": (ctypes.c_int, [_P, _PI64, _I32]),
@@ -66,6 +67,8 @@ SIGNATURES = {
     "pamo_simplify_round_gpu_ms": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_double), _I32]),
     "pamo_self_intersect": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _P, _P]),
     "pamo_self_intersect_noalloc": (ctypes.c_int, [_P, _P, _I32, _I32, _P, _P]),
+    "pamo_server_submit_ex": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _F64, _I32, _F32, _I32, _PI64]),
+    "pamo_server_fetch_f64": (ctypes.c_int, [_P, _I64, _P, _P]),
     "pamo_csr_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int]),
     "pamo_csr_destroy": (ctypes.c_int, [_P]),
     "pamo_csr_last_error": (ctypes.c_char_p, [_P]),

@@ -389,6 +389,31 @@ def tris_mean(points: torch.Tensor, triangles: torch.Tensor, ctx: Context | None
     return out
 
 
+def cost_probe(points: torch.Tensor, triangles: torch.Tensor, scale: float, threshold: float = 1e-3,
+               precision: int = 0):
+    """One round up to the edge costs (pamo_cost_probe) in precision mode 0, 1 or 2 on a context of its own:
+    (edges int32 [E,2], cost float32 [E] before clamp and quantisation, NaN where invalid, placement float32 [E,3]),
+    CUDA tensors."""
+    _check_input(points, "points", torch.float32)
+    _check_input(triangles, "triangles", torch.int32)
+    dev = points.device
+    ctx = Context(dev)
+    lib = _native.load()
+    ne = ctypes.c_int32()
+    with torch.cuda.device(dev):
+        st = _stream(dev)
+        args = (ctx.handle, _ptr(points), _ptr(triangles), int(points.shape[0]), int(triangles.shape[0]), float(scale),
+                float(threshold), int(precision))
+        _native.check(lib.pamo_cost_probe(*args, None, None, None, 0, ctypes.byref(ne), st), ctx.handle)
+        n = ne.value
+        edges = torch.empty((n, 2), dtype=torch.int32, device=dev)
+        cost = torch.empty(n, dtype=torch.float32, device=dev)
+        place = torch.empty((n, 3), dtype=torch.float32, device=dev)
+        _native.check(lib.pamo_cost_probe(*args, _ptr(edges), _ptr(cost), _ptr(place), n, ctypes.byref(ne), st),
+                      ctx.handle)
+    return edges, cost, place
+
+
 def launch_count() -> int:
     """Kernels launched by the CUDA library since it was loaded."""
     return int(_native.load().pamo_launch_count())
@@ -465,5 +490,9 @@ class PaMO(torch.nn.Module):
                 # the projection's target is fixed at construction: uploaded once, like resident model state
                 self._gt_dev = (torch.as_tensor(self.gt_mesh[0], dtype=torch.float64).to(points.device),
                                 torch.as_tensor(self.gt_mesh[1], dtype=torch.int32).to(points.device))
-            verts_np, faces_np = safe_project.process(self._gt_dev[0], self._gt_dev[1], V2, F2, 5, system=self.system)
+            if len(V2) >= 3 and len(F2) >= 1:
+                verts_np, faces_np = safe_project.process(self._gt_dev[0], self._gt_dev[1], V2, F2, 5,
+                                                          system=self.system)
+            else:  # nothing to project (the reference's stage 3 has no behaviour for an empty mesh)
+                verts_np, faces_np = V2, F2
         return verts_np, faces_np

@@ -187,12 +187,16 @@ class Server:
         except Exception:  # interpreter shutdown
             pass
 
-    def submit(self, verts, tris, ratio: float, tolerance: int = 4, threshold: float = 1e-3) -> int:
+    def submit(self, verts, tris, ratio: float, tolerance: int = 4, threshold: float = 1e-3,
+               stage3: bool = False) -> int:
+        """Queue one PaMO.run job; with stage3 the result is also projected onto the request's own input mesh
+        (PaMO(use_stage3=True)), with float64 positions."""
         v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
         t = np.ascontiguousarray(tris, np.int32).reshape(-1, 3)
         rid = ctypes.c_int64()
-        st = self._lib.pamo_server_submit(self._h, v.ctypes.data, t.ctypes.data, len(v), len(t), float(ratio),
-                                          int(tolerance), ctypes.c_float(threshold), ctypes.byref(rid))
+        st = self._lib.pamo_server_submit_ex(self._h, v.ctypes.data, t.ctypes.data, len(v), len(t), float(ratio),
+                                             int(tolerance), ctypes.c_float(threshold), int(bool(stage3)),
+                                             ctypes.byref(rid))
         if st != _native.PAMO_OK:
             raise _native.PamoError(st, _err(self._lib.pamo_server_last_error, self._h))
         return rid.value
@@ -207,10 +211,11 @@ class Server:
             return None
         return rid.value, st.value, npt.value, ntr.value, tuple(times)
 
-    def fetch(self, request_id: int, n_points: int, n_triangles: int):
-        v = np.zeros((n_points, 3), np.float32)
+    def fetch(self, request_id: int, n_points: int, n_triangles: int, float64: bool = False):
+        v = np.zeros((n_points, 3), np.float64 if float64 else np.float32)
         t = np.zeros((n_triangles, 3), np.int32)
-        st = self._lib.pamo_server_fetch(self._h, int(request_id), v.ctypes.data, t.ctypes.data)
+        fn = self._lib.pamo_server_fetch_f64 if float64 else self._lib.pamo_server_fetch
+        st = fn(self._h, int(request_id), v.ctypes.data, t.ctypes.data)
         if st != _native.PAMO_OK:
             raise _native.PamoError(st, _err(self._lib.pamo_server_last_error, self._h))
         return v, t

@@ -14,7 +14,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
+#include <cmath>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -241,6 +243,10 @@ namespace {
 // rounded up to 680 and 330), its input and output copies, and 16 MiB of fixed-size scratch.
 int64_t job_bytes(int64_t nv, int64_t nf) { return 680 * nf + 330 * nv + 2 * (12 * nv + 12 * nf) + (16ll << 20); }
 
+// What stage 3 adds while it runs: the input as the float64 projection target and the stage-3 handle's buffers over
+// it (its LBVH and per-face records, about 240 B per target face), plus 64 MiB for the small projected mesh.
+int64_t stage3_bytes(int64_t nv, int64_t nf) { return 24 * nv + 240 * nf + (64ll << 20); }
+
 struct Request {
     int64_t id = 0;
     std::vector<float> points;
@@ -248,14 +254,60 @@ struct Request {
     double ratio = 0.001;
     int32_t tolerance = 4;
     float threshold = 1e-3f;
+    bool stage3 = false;
     int64_t bytes = 0;
     Clock::time_point t_submit, t_admit, t_done;
     int status = PAMO_OK;
     std::string err;
     std::vector<float> out_points;
+    std::vector<double> out_points64;  // stage 3: the projection's float64 positions
     std::vector<int32_t> out_tris;
     int32_t rounds = 0;
 };
+
+// What trimesh.Trimesh(V, F) does to the stage-2 output before the reference's stage 3 (simp_cuda/pamo/__init__.py:
+// 166-172, trimesh 4.4.0 as pinned in env.yaml): faces touching a non-finite vertex are dropped, then referenced
+// vertices whose coordinates agree after rounding to 8 decimals (round half to even, like numpy) are merged, keeping
+// the first occurrence's coordinates, in order of first occurrence; unreferenced vertices are dropped.
+void mesh_process(const std::vector<double>& V, const std::vector<int32_t>& F, std::vector<double>& Vo,
+                  std::vector<int32_t>& Fo) {
+    const size_t nv = V.size() / 3, nf = F.size() / 3;
+    std::vector<int64_t> remap(nv, -1);
+    size_t k = 0;
+    for (size_t v = 0; v < nv; ++v)
+        if (std::isfinite(V[3 * v]) && std::isfinite(V[3 * v + 1]) && std::isfinite(V[3 * v + 2])) remap[v] = (int64_t)k++;
+    std::vector<int32_t> faces;
+    faces.reserve(F.size());
+    for (size_t f = 0; f < nf; ++f) {
+        const int32_t a = F[3 * f], b = F[3 * f + 1], c = F[3 * f + 2];
+        if (remap[a] < 0 || remap[b] < 0 || remap[c] < 0) continue;
+        faces.push_back((int32_t)remap[a]);
+        faces.push_back((int32_t)remap[b]);
+        faces.push_back((int32_t)remap[c]);
+    }
+    std::vector<double> verts;
+    verts.reserve(3 * k);
+    for (size_t v = 0; v < nv; ++v)
+        if (remap[v] >= 0) verts.insert(verts.end(), V.begin() + 3 * v, V.begin() + 3 * v + 3);
+    std::vector<char> referenced(k, 0);
+    for (int32_t x : faces) referenced[x] = 1;
+    std::map<std::array<int64_t, 3>, int32_t> ids;
+    std::vector<int32_t> inv(k, 0);
+    Vo.clear();
+    for (size_t v = 0; v < k; ++v) {
+        if (!referenced[v]) continue;
+        std::array<int64_t, 3> key;
+        for (int d = 0; d < 3; ++d) key[d] = (int64_t)std::nearbyint(verts[3 * v + d] * 100000000.0);
+        auto it = ids.find(key);
+        if (it == ids.end()) {
+            it = ids.emplace(key, (int32_t)(Vo.size() / 3)).first;
+            Vo.insert(Vo.end(), verts.begin() + 3 * v, verts.begin() + 3 * v + 3);
+        }
+        inv[v] = it->second;
+    }
+    Fo.resize(faces.size());
+    for (size_t i = 0; i < faces.size(); ++i) Fo[i] = inv[faces[i]];
+}
 
 }  // namespace
 
@@ -291,12 +343,75 @@ struct pamo_server {
         }
     }
 
+    // grows a device buffer (elements of T) to at least n
+    template <typename T>
+    static int ensure_dev(T*& p, size_t& cap, size_t n) {
+        if (n <= cap && p) return PAMO_OK;
+        cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        if (cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return PAMO_ERR_OOM;
+        cap = std::max<size_t>(n, 1);
+        return PAMO_OK;
+    }
+
+    // stage 3 of a finished stage-2 job (simp_cuda/pamo/__init__.py:165-176): the stage-2 mesh through trimesh's
+    // processing, then the projection onto the request's own input mesh; float64 positions
+    int stage3_job(Worker& w, pamo_stage3*& s3, Request& q, const int32_t* d_gt_tris, const float* d_res_p,
+                   const int32_t* d_res_t, int32_t onp, int32_t ont, double*& gp, size_t& cgp, double*& sp,
+                   size_t& csp, int32_t*& st, size_t& cst) {
+        int r;
+        if (!s3 && (r = pamo_stage3_create(&s3, device))) return r;
+        std::vector<float> v2((size_t)onp * 3);
+        std::vector<int32_t> f2((size_t)ont * 3);
+        cudaMemcpyAsync(v2.data(), d_res_p, v2.size() * sizeof(float), cudaMemcpyDeviceToHost, w.stream);
+        cudaMemcpyAsync(f2.data(), d_res_t, f2.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, w.stream);
+        if (cudaStreamSynchronize(w.stream) != cudaSuccess) return PAMO_ERR_CUDA;
+        std::vector<double> vd(v2.begin(), v2.end()), vm;
+        std::vector<int32_t> fm;
+        mesh_process(vd, f2, vm, fm);
+        const size_t ngp = q.points.size() / 3, ngt = q.tris.size() / 3, nm = vm.size() / 3, nfm = fm.size() / 3;
+        if (nm < 3 || nfm < 1) {  // nothing to project (the reference's stage 3 has no behaviour for an empty mesh)
+            q.out_points64 = vm;
+            q.out_tris = fm;
+            q.out_points.assign(vm.begin(), vm.end());
+            return PAMO_OK;
+        }
+        std::vector<double> gt(q.points.begin(), q.points.end());
+        if ((r = ensure_dev(gp, cgp, 3 * ngp)) || (r = ensure_dev(sp, csp, 6 * std::max<size_t>(nm, 1))) ||
+            (r = ensure_dev(st, cst, 3 * std::max<size_t>(nfm, 1))))
+            return r;
+        cudaMemcpyAsync(gp, gt.data(), gt.size() * sizeof(double), cudaMemcpyHostToDevice, w.stream);
+        cudaMemcpyAsync(sp, vm.data(), vm.size() * sizeof(double), cudaMemcpyHostToDevice, w.stream);
+        cudaMemcpyAsync(st, fm.data(), fm.size() * sizeof(int32_t), cudaMemcpyHostToDevice, w.stream);
+        double* out = sp + 3 * nm;
+        if ((r = pamo_safe_project(s3, gp, d_gt_tris, (int32_t)ngp, (int32_t)ngt, sp, st, (int32_t)nm, (int32_t)nfm, 5,
+                                   out, w.stream))) {
+            q.err = pamo_stage3_last_error(s3);
+            return r;
+        }
+        q.out_points64.resize(3 * nm);
+        q.out_tris = fm;
+        cudaMemcpyAsync(q.out_points64.data(), out, 3 * nm * sizeof(double), cudaMemcpyDeviceToHost, w.stream);
+        if (cudaStreamSynchronize(w.stream) != cudaSuccess) return PAMO_ERR_CUDA;
+        q.out_points.assign(q.out_points64.begin(), q.out_points64.end());
+        return PAMO_OK;
+    }
+
     void worker_loop(int i) {
         Worker& w = workers[i];
         cudaSetDevice(device);
         float* dp = nullptr;
         int32_t* dt = nullptr;
         size_t cp = 0, ct = 0;
+        float* rp = nullptr;  // stage-2 result (the input copies stay the stage-3 target)
+        int32_t* rt = nullptr;
+        size_t crp = 0, crt = 0;
+        double* gp = nullptr;
+        double* sp = nullptr;
+        int32_t* st = nullptr;
+        size_t cgp = 0, csp = 0, cst = 0;
+        pamo_stage3* s3 = nullptr;
         for (;;) {
             std::shared_ptr<Request> q;
             {
@@ -323,14 +438,20 @@ struct pamo_server {
                 else ct = nt * 3;
             }
             int32_t onp = 0, ont = 0;
+            if (!r && q->stage3) {
+                r = ensure_dev(rp, crp, np * 3);
+                if (!r) r = ensure_dev(rt, crt, nt * 3);
+            }
             if (!r) {
                 cudaMemcpyAsync(dp, q->points.data(), np * 3 * sizeof(float), cudaMemcpyHostToDevice, w.stream);
                 cudaMemcpyAsync(dt, q->tris.data(), nt * 3 * sizeof(int32_t), cudaMemcpyHostToDevice, w.stream);
-                // the result is exported over the input copies (both at least as large)
-                r = run_job(w, dp, dt, (int32_t)np, (int32_t)nt, q->ratio, q->tolerance, q->threshold, 1000000, 0, dp,
-                            dt, &onp, &ont, &q->rounds, q->err);
+                // without stage 3 the result is exported over the input copies (both at least as large)
+                r = run_job(w, dp, dt, (int32_t)np, (int32_t)nt, q->ratio, q->tolerance, q->threshold, 1000000, 0,
+                            q->stage3 ? rp : dp, q->stage3 ? rt : dt, &onp, &ont, &q->rounds, q->err);
             }
-            if (!r) {
+            if (!r && q->stage3) {
+                r = stage3_job(w, s3, *q, dt, rp, rt, onp, ont, gp, cgp, sp, csp, st, cst);
+            } else if (!r) {
                 q->out_points.resize((size_t)onp * 3);
                 q->out_tris.resize((size_t)ont * 3);
                 cudaMemcpyAsync(q->out_points.data(), dp, (size_t)onp * 3 * sizeof(float), cudaMemcpyDeviceToHost,
@@ -357,6 +478,12 @@ struct pamo_server {
         }
         cudaFree(dp);
         cudaFree(dt);
+        cudaFree(rp);
+        cudaFree(rt);
+        cudaFree(gp);
+        cudaFree(sp);
+        cudaFree(st);
+        if (s3) pamo_stage3_destroy(s3);
     }
 };
 
@@ -395,14 +522,22 @@ int pamo_server_destroy(pamo_server* s) {
 
 int pamo_server_submit(pamo_server* s, const float* points, const int32_t* triangles, int32_t n_points,
                        int32_t n_triangles, double ratio, int32_t tolerance, float threshold, int64_t* request_id) {
+    return pamo_server_submit_ex(s, points, triangles, n_points, n_triangles, ratio, tolerance, threshold, 0,
+                                 request_id);
+}
+
+int pamo_server_submit_ex(pamo_server* s, const float* points, const int32_t* triangles, int32_t n_points,
+                          int32_t n_triangles, double ratio, int32_t tolerance, float threshold, int32_t use_stage3,
+                          int64_t* request_id) {
     if (!s || !points || !triangles || n_points < 1 || n_triangles < 1 || !request_id) return PAMO_ERR_INVALID_ARG;
     auto q = std::make_shared<Request>();
+    q->stage3 = use_stage3 != 0;
     q->points.assign(points, points + 3 * (size_t)n_points);
     q->tris.assign(triangles, triangles + 3 * (size_t)n_triangles);
     q->ratio = ratio;
     q->tolerance = tolerance;
     q->threshold = threshold;
-    q->bytes = job_bytes(n_points, n_triangles);
+    q->bytes = job_bytes(n_points, n_triangles) + (q->stage3 ? stage3_bytes(n_points, n_triangles) : 0);
     q->t_submit = Clock::now();
     {
         std::lock_guard<std::mutex> lock(s->mu);
@@ -454,6 +589,30 @@ int pamo_server_fetch(pamo_server* s, int64_t request_id, float* points, int32_t
         return q->status;
     }
     if (points) std::memcpy(points, q->out_points.data(), q->out_points.size() * sizeof(float));
+    if (triangles) std::memcpy(triangles, q->out_tris.data(), q->out_tris.size() * sizeof(int32_t));
+    return PAMO_OK;
+}
+
+int pamo_server_fetch_f64(pamo_server* s, int64_t request_id, double* points, int32_t* triangles) {
+    if (!s) return PAMO_ERR_INVALID_ARG;
+    std::shared_ptr<Request> q;
+    {
+        std::lock_guard<std::mutex> lock(s->mu);
+        auto it = s->finished.find(request_id);
+        if (it == s->finished.end()) return PAMO_ERR_STATE;
+        q = it->second;
+        s->finished.erase(it);
+    }
+    if (q->status != PAMO_OK) {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->err = q->err;
+        return q->status;
+    }
+    if (points) {
+        if (!q->out_points64.empty()) std::memcpy(points, q->out_points64.data(), q->out_points64.size() * sizeof(double));
+        else
+            for (size_t i = 0; i < q->out_points.size(); ++i) points[i] = q->out_points[i];
+    }
     if (triangles) std::memcpy(triangles, q->out_tris.data(), q->out_tris.size() * sizeof(int32_t));
     return PAMO_OK;
 }

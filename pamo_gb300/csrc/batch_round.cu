@@ -510,7 +510,7 @@ struct pamo_csr {
     int device = 0;
     std::string err;
     cudaStream_t stream = nullptr;
-    bool skinny_pow = true;
+    bool skinny_pow = false;  // as pamo_ctx's option of the same name
 
     // per vertex / face / edge of a round
     Buf<float4> pos, orig_pos, pos_in, pos_next, res_pos;

@@ -156,7 +156,13 @@ struct pamo_ctx {
     bool use_graphs = true;     // device rounds as cached graphs
     bool device_rounds = true;  // rounds after the first from device-resident sizes (pamo_simplify_device)
     bool bvh_reuse = true;      // device rounds refit the LBVH carried from the previous round
-    bool skinny_pow = true;     // the skinny term squares with the device's pow(float, int), as the reference does
+    bool skinny_pow = false;    // 1: the skinny term squares with the device's pow(float, int), as the reference does
+                                // (12x slower edge cost; every measured job is bit-identical with either form)
+    int precision = 0;          // 0 the reference's arithmetic; 1 compensated sums; 2 compensated, optimal placement
+    DevBuf<float4> place;       // precision 2: each edge's placement
+    DevBuf<float> probe_raw;    // pamo_cost_probe: each edge's cost before quantisation
+    int ensure_place(size_t n_edges) { return precision == 2 ? grow(place, n_edges) : PAMO_OK; }
+    float4* place_ptr() { return precision == 2 ? place.p : nullptr; }
     long long pair_cap_limit = 0;  // > 0: at most this many listed candidate pairs per check (tests the overflow path)
 
     int pair_cap() const {
@@ -278,7 +284,7 @@ struct pamo_ctx {
         fr(edge_cost); fr(invalid); fr(pts_map); fr(pts_map_prev); fr(undo_list); fr(tmp_undo);
         fr(pos); fr(orig_pos); fr(pos_in); fr(pos_out); fr(occ); fr(valence); fr(cursor); fr(quad); fr(vmin); fr(undo_in);
         fr(nxt); fr(fgeo); fr(tri); fr(orig_tri); fr(tri_in); fr(tri_out); fr(ecount); fr(qflag); fr(qlist); fr(fflags); fr(nt);
-        fr(shuffle_flags); fr(fkey); fr(eorder); fr(vedges); fr(vcursor); fr(hit); fr(edges); fr(win); fr(collapsed); fr(uflag); fr(face_mean); fr(exact_list);
+        fr(shuffle_flags); fr(fkey); fr(eorder); fr(vedges); fr(vcursor); fr(hit); fr(edges); fr(win); fr(collapsed); fr(uflag); fr(face_mean); fr(exact_list); fr(place); fr(probe_raw);
         if (bvh_mem) cudaFree(bvh_mem);
         bvh_mem = nullptr;
         prof.destroy();
@@ -388,6 +394,7 @@ struct pamo_ctx {
             return r;
         // edge costs keep their stale contents when the physical buffer grows
         if ((r = grow(edge_cost, 2 * nc + 2 * nc / 5 + 2, true, true))) return r;
+        if ((r = ensure_place(2 * nc))) return r;
         if (bvh_cap < nc) {
             drop_graphs();
             if (bvh_mem) {
@@ -449,6 +456,44 @@ struct pamo_ctx {
         return PAMO_OK;
     }
 
+    // pamo_cost_probe: one round up to the edge costs (no shuffle, no collapse) with the given precision mode; the
+    // edges, their costs before quantisation and their placements stay in edges / probe_raw / place.
+    int probe(const float* pts3, const int* tris3, int nP, int nT, float threshold, int mode) {
+        cudaStream_t s = stream;
+        const int keep = precision;
+        precision = mode;
+        int r;
+        if ((r = ensure_vertex_buffers(nP)) || (r = ensure_face_buffers(nT)) || (r = ensure_pts_state(nP)) ||
+            (r = grow(probe_raw, 2 * cap_f)) || (r = grow(place, 2 * cap_f))) {
+            precision = keep;
+            return r;
+        }
+        std::memset(h_rc, 0, sizeof(RoundCounters));
+        h_rc->n_pts = nP;
+        h_rc->n_tris = nT;
+        cudaMemcpyAsync(rc, h_rc, sizeof(RoundCounters), cudaMemcpyHostToDevice, s);
+        launch_load_points(pts3, nP, pos.p, orig_pos.p, occ.p, s);
+        launch_load_tris(tris3, nT, nP, tri.p, rc, s);
+        cudaMemsetAsync(valence.p, 0, (nP + 1) * sizeof(int), s);
+        cudaMemsetAsync(cursor.p, 0, (nP + 1) * sizeof(int), s);
+        cudaMemsetAsync(vedges.p, 0, (nP + 1) * sizeof(int), s);
+        cudaMemsetAsync(vcursor.p, 0, (nP + 1) * sizeof(int), s);
+        cudaMemsetAsync(invalid.p, 0, invalid.n, s);
+        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
+        scan_adjacency_counts(s, std::max(nP, nT));
+        launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p, eorder.p, s);
+        launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
+        launch_quadrics(rc, nP, valence.p, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s, mode > 0);
+        cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
+        cudaMemsetAsync(probe_raw.p, 0xFF, probe_raw.n * sizeof(float), s);  // NaN where no cost is computed
+        launch_edge_cost(rc, 2 * nT, eorder.p, edges.p, valence.p, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p,
+                         edge_cost.p, vmin.p, d_scale, threshold, 0, s, nullptr, false, skinny_pow, mode, probe_raw.p,
+                         place.p);
+        precision = keep;
+        if ((r = read_counters())) return r;
+        return status_to_error(h_rc->status);
+    }
+
     // Host copy of the counters (synchronises the stream).
     int read_counters() {
         int r;
@@ -483,16 +528,17 @@ struct pamo_ctx {
             launch_fill_adjacency(tri.p, rc, nTb, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p,
                                   eorder.p, s);
             launch_sort_adjacency(rc, nPb, valence.p, nt.p, s);
-            launch_quadrics(rc, nPb, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s);
+            launch_quadrics(rc, nPb, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s, precision > 0);
             launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
             launch_fill_u64_dev(rc, nPb, vmin.p, ~0ull, s);
             cost_begin(s);
             launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p,
-                             vmin.p, d_scale, threshold, 0, s, &d_ls->is_stuck, false, skinny_pow);
+                             vmin.p, d_scale, threshold, 0, s, &d_ls->is_stuck, false, skinny_pow, precision, nullptr,
+                             place_ptr());
             cost_end(s);
             launch_face_keys(rc, nTb, tri.p, vmin.p, fkey.p, s);
             launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p,
-                            pos.p, orig_pos.p, occ.p, win.p, s);
+                            pos.p, orig_pos.p, occ.p, win.p, s, true, place_ptr());
             exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s, &rc->status, eb);
             launch_compact_winners(rc, eb, win.p, collapsed.p, s);
             launch_remove_invalid(rc, nTb, tri.p, s);
@@ -657,20 +703,20 @@ struct pamo_ctx {
 
         // cost and selection
         prof.begin(kPhQuad, s);
-        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s);
+        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s, precision > 0);
         prof.end(kPhQuad, s);
         launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
         cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
         prof.begin(kPhCost, s);
         cost_begin(s);
         launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p, vmin.p,
-                         d_scale, threshold, is_stuck, s, nullptr, false, skinny_pow);
+                         d_scale, threshold, is_stuck, s, nullptr, false, skinny_pow, precision, nullptr, place_ptr());
         cost_end(s);
         prof.end(kPhCost, s);
         prof.begin(kPhCollapse, s);
         launch_face_keys(rc, nT, tri.p, vmin.p, fkey.p, s);
         launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p,
-                        orig_pos.p, occ.p, win.p, s);
+                        orig_pos.p, occ.p, win.p, s, true, place_ptr());
         exclusive_scan(win.p, win.p, &rc->n_edges, 1, &rc->n_win, scan_scratch, s, &rc->status, eb);
         launch_compact_winners(rc, eb, win.p, collapsed.p, s);
         prof.end(kPhCollapse, s);
@@ -785,6 +831,14 @@ int pamo_ctx_set_option(pamo_ctx* ctx, const char* name, int64_t value) {
     else if (n == "skinny_pow") {
         ctx->skinny_pow = value != 0;
         ctx->drop_graphs();
+    } else if (n == "precision") {
+        if (value < 0 || value > 2) return ctx->fail(PAMO_ERR_INVALID_ARG, "precision is 0, 1 or 2");
+        ctx->precision = (int)value;
+        ctx->drop_graphs();
+        if (ctx->cap_f) {
+            const int r = ctx->ensure_place(2 * ctx->cap_f);
+            if (r) return r;
+        }
     }
     else if (n == "time_rounds") ctx->time_rounds = value != 0;
     else if (n == "time_edge_cost") {
@@ -846,6 +900,32 @@ int pamo_legacy_round(pamo_ctx* ctx, const float* points, const int32_t* triangl
     ctx->out_nt = n_triangles;
     ctx->out_nu = 0;
     return PAMO_OK;
+}
+
+int pamo_cost_probe(pamo_ctx* ctx, const float* points, const int32_t* triangles, int32_t n_points,
+                    int32_t n_triangles, float scale, float threshold, int32_t precision, int32_t* out_edges,
+                    float* out_cost, float* out_place, int32_t capacity, int32_t* n_edges, pamo_stream stream) {
+    if (!ctx) return PAMO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (n_points < 1 || n_triangles < 1 || !points || !triangles || !n_edges || precision < 0 || precision > 2)
+        return ctx->fail(PAMO_ERR_INVALID_ARG, "invalid sizes, mode or null pointers");
+    cudaSetDevice(ctx->device);
+    ctx->stream = (cudaStream_t)stream;
+    ctx->have_round = false;
+    ctx->h_pinned_f[0] = scale;
+    cudaMemcpyAsync(ctx->d_scale, ctx->h_pinned_f, sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    int r = ctx->probe(points, triangles, n_points, n_triangles, threshold, precision);
+    if (r) return r;
+    const int ne = ctx->h_rc->n_edges;
+    *n_edges = ne;
+    if (capacity < ne) return capacity == 0 ? PAMO_OK : ctx->fail(PAMO_ERR_CAPACITY, "room for %d edges needed", ne);
+    cudaStream_t s = ctx->stream;
+    if (out_edges) cudaMemcpy2DAsync(out_edges, 2 * sizeof(int32_t), ctx->edges.p, sizeof(int2), 2 * sizeof(int32_t), ne,
+                                     cudaMemcpyDeviceToDevice, s);
+    if (out_cost) cudaMemcpyAsync(out_cost, ctx->probe_raw.p, ne * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    if (out_place) cudaMemcpy2DAsync(out_place, 3 * sizeof(float), ctx->place.p, sizeof(float4), 3 * sizeof(float), ne,
+                                     cudaMemcpyDeviceToDevice, s);
+    return ctx->check(cudaStreamSynchronize(s), "cost probe");
 }
 
 int pamo_round_sizes(const pamo_ctx* ctx, int32_t* n_points, int32_t* n_triangles, int32_t* n_verts_undo) {

@@ -11,6 +11,7 @@
 //   * the undo check marks intersecting faces in a flag array and tests ring membership in O(ring) instead
 //     of scanning the whole intersection list per collapsed edge (:776-827).
 #include <cstdint>
+#include <type_traits>
 #include "scan.cuh"
 #include "simp_round.cuh"
 #include "round_ops.cuh"
@@ -111,6 +112,38 @@ __global__ void k_shuffle_gather(Feistel fb, const int* __restrict__ scan, const
 //   fgeo[3f + 2] = the face plane of tri2plane (:337-346).
 __device__ __forceinline__ void face_plane(const float4* __restrict__ pos, int4 t, float p[4]);
 
+// ---- precision mode: error-free transforms (Knuth's TwoSum; TwoProd with an explicit fused multiply-add, which
+// --fmad=false leaves alone) and a compensated float accumulator (Ogita, Rump and Oishi's Sum2/Dot2)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+    p = a * b;
+    e = __fmaf_rn(a, b, -p);
+}
+struct CSum {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        float t, e;
+        two_sum(s, x, t, e);
+        s = t;
+        c += e;
+    }
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        float p, pe;
+        two_prod(a, b, p, pe);
+        add(p);
+        c += pe;
+    }
+    __device__ __forceinline__ float value() const { return s + c; }
+};
+__device__ __forceinline__ void acc_add(float& a, float x) { a += x; }
+__device__ __forceinline__ void acc_add(CSum& a, float x) { a.add(x); }
+__device__ __forceinline__ float acc_value(float a) { return a; }
+__device__ __forceinline__ float acc_value(const CSum& a) { return a.value(); }
+
 __global__ void __launch_bounds__(kT) k_face_counts(const int4* __restrict__ tri, const RoundCounters* rc, int* valence,
                                                     int* ecount, int* vedges, const float4* __restrict__ pos,
                                                     float4* fgeo) {
@@ -202,22 +235,36 @@ __device__ __forceinline__ int next_after(int4 t, int v);
 
 // Quadrics from the face planes of fgeo; also nxt[s] = the vertex after v in ring face s (the link condition's
 // per-slot value).
+// kComp (precision mode): every entry summed with compensation (products by TwoProd, sums by TwoSum), rounded once
+template <bool kComp>
 __global__ void __launch_bounds__(kT) k_quadrics(const RoundCounters* rc, const int* __restrict__ nt_off,
                                                  const int* __restrict__ nt, const int4* __restrict__ tri,
                                                  const float4* __restrict__ fgeo, Quadric* q, int* nxt) {
     const int n = rc->n_pts;
     for (int v = gtid(); v < n; v += gstride()) {
         float m00 = 0.f, m01 = 0.f, m02 = 0.f, m03 = 0.f, m11 = 0.f, m12 = 0.f, m13 = 0.f, m22 = 0.f, m23 = 0.f, m33 = 0.f;
+        CSum c[10];
         const int b = nt_off[v + 1];
         for (int s = nt_off[v]; s < b; ++s) {
             const int f = nt[s];
             nxt[s] = next_after(tri[f], v);
             const float4 pl = fgeo[3 * (size_t)f + 2];
             const float p[4] = {pl.x, pl.y, pl.z, pl.w};
-            m00 += p[0] * p[0]; m01 += p[0] * p[1]; m02 += p[0] * p[2]; m03 += p[0] * p[3];
-            m11 += p[1] * p[1]; m12 += p[1] * p[2]; m13 += p[1] * p[3];
-            m22 += p[2] * p[2]; m23 += p[2] * p[3];
-            m33 += p[3] * p[3];
+            if constexpr (kComp) {
+                c[0].add_prod(p[0], p[0]); c[1].add_prod(p[0], p[1]); c[2].add_prod(p[0], p[2]);
+                c[3].add_prod(p[0], p[3]); c[4].add_prod(p[1], p[1]); c[5].add_prod(p[1], p[2]);
+                c[6].add_prod(p[1], p[3]); c[7].add_prod(p[2], p[2]); c[8].add_prod(p[2], p[3]);
+                c[9].add_prod(p[3], p[3]);
+            } else {
+                m00 += p[0] * p[0]; m01 += p[0] * p[1]; m02 += p[0] * p[2]; m03 += p[0] * p[3];
+                m11 += p[1] * p[1]; m12 += p[1] * p[2]; m13 += p[1] * p[3];
+                m22 += p[2] * p[2]; m23 += p[2] * p[3];
+                m33 += p[3] * p[3];
+            }
+        }
+        if constexpr (kComp) {
+            m00 = c[0].value(); m01 = c[1].value(); m02 = c[2].value(); m03 = c[3].value(); m11 = c[4].value();
+            m12 = c[5].value(); m13 = c[6].value(); m22 = c[7].value(); m23 = c[8].value(); m33 = c[9].value();
         }
         Quadric Q;
         Q.a = make_float4(m00, m01, m02, m03);
@@ -236,15 +283,16 @@ __device__ __forceinline__ int next_after(int4 t, int v) {
 }
 
 
+template <class Acc>
 __device__ __forceinline__ void ring_len(int w, const int* __restrict__ nt_off, const int* __restrict__ nt,
-                                         const float4* __restrict__ fgeo, float& len, int& cnt) {
+                                         const float4* __restrict__ fgeo, Acc& len, int& cnt) {
     const int b = nt_off[w + 1];
     for (int s = nt_off[w]; s < b; ++s) {
         const float4 g = fgeo[3 * (size_t)nt[s]];
         const int mask = __float_as_int(g.w);
-        if (mask & 1) { len += g.x; cnt++; }
-        if (mask & 2) { len += g.y; cnt++; }
-        if (mask & 4) { len += g.z; cnt++; }
+        if (mask & 1) { acc_add(len, g.x); cnt++; }
+        if (mask & 2) { acc_add(len, g.y); cnt++; }
+        if (mask & 4) { acc_add(len, g.z); cnt++; }
     }
 }
 
@@ -289,10 +337,10 @@ __device__ __forceinline__ float skinny_term(float k4s3, float area, float l01, 
     return 1.0f - rclamp(e, 0.0f, 1.0f);
 }
 
-template <bool kLegacy, bool kPow>
+template <bool kLegacy, bool kPow, class Acc>
 __device__ __forceinline__ bool ring_skinny(int w, int other, V3 vm, const int* __restrict__ nt_off,
                                             const int* __restrict__ nt, const int4* __restrict__ tri,
-                                            const float4* __restrict__ pos, const float4* __restrict__ fgeo, float& qa,
+                                            const float4* __restrict__ pos, const float4* __restrict__ fgeo, Acc& qa,
                                             int& ntri) {
     const float k4s3 = 4.0f * sqrtf(3.0f);
     const int b = nt_off[w + 1];
@@ -320,7 +368,7 @@ __device__ __forceinline__ bool ring_skinny(int w, int other, V3 vm, const int* 
         const float l20 = (wz || wx) ? vnorm(vsub(n2, n0)) : lg.z;
         const float sh = (l01 + l12 + l20) / 2;  // triangle_area (Heron), :368-375
         const float area = sqrtf(sh * (sh - l01) * (sh - l12) * (sh - l20));
-        qa += skinny_term<kLegacy, kPow>(k4s3, area, l01, l12, l20);
+        acc_add(qa, skinny_term<kLegacy, kPow>(k4s3, area, l01, l12, l20));
         ntri++;
     }
     return true;
@@ -330,14 +378,55 @@ __device__ __forceinline__ uint32_t f2u_sat(float f) {
     return __float2uint_rz(f);  // round toward zero, saturating like the reference's uint32_t(float) on the GPU
 }
 
+// Minimiser of v^T Q v over v = (x, y, z, 1) for the quadric Q of an edge (precision mode 2, optimal placement; the
+// reference places at the midpoint, cusimp_free.cu:491,687): A x = -b with A the upper 3x3 block and b the last
+// column, by the adjugate. A is positive semi-definite, so its largest diagonal entry bounds its entries: a
+// determinant above 1e-2 of its cube (a well-conditioned A) is solved in float, one down to 1e-10 of it (near
+// singular) in double from the compensated entries (hi + lo), and a singular one (flat or cylindrical rings) keeps
+// the midpoint. Returns 0 (midpoint), 1 (float) or 2 (double).
+__device__ __forceinline__ int qem_optimum(const float* m, const float* lo, V3 mid, V3& x) {
+    const float m00 = m[0], m01 = m[1], m02 = m[2], m03 = m[3], m11 = m[4], m12 = m[5], m13 = m[6], m22 = m[7],
+                m23 = m[8];
+    const float nrm = fmaxf(fabsf(m00), fmaxf(fabsf(m11), fabsf(m22)));
+    const float n3 = nrm * nrm * nrm;
+    const float c00 = m11 * m22 - m12 * m12, c01 = m02 * m12 - m01 * m22, c02 = m01 * m12 - m11 * m02;
+    const float det = m00 * c00 + m01 * c01 + m02 * c02;
+    if (nrm > 0.0f && fabsf(det) > 1e-2f * n3) {
+        const float c11 = m00 * m22 - m02 * m02, c12 = m01 * m02 - m00 * m12, c22 = m00 * m11 - m01 * m01;
+        x.x = -(c00 * m03 + c01 * m13 + c02 * m23) / det;
+        x.y = -(c01 * m03 + c11 * m13 + c12 * m23) / det;
+        x.z = -(c02 * m03 + c12 * m13 + c22 * m23) / det;
+        return 1;
+    }
+    double d[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) d[i] = (double)m[i] + (double)lo[i];
+    const double e00 = d[4] * d[7] - d[5] * d[5], e01 = d[2] * d[5] - d[1] * d[7], e02 = d[1] * d[5] - d[4] * d[2];
+    const double det64 = d[0] * e00 + d[1] * e01 + d[2] * e02;
+    if (nrm > 0.0f && fabs(det64) > 1e-10 * (double)n3) {
+        const double e11 = d[0] * d[7] - d[2] * d[2], e12 = d[1] * d[2] - d[0] * d[5], e22 = d[0] * d[4] - d[1] * d[1];
+        x.x = (float)(-(e00 * d[3] + e01 * d[6] + e02 * d[8]) / det64);
+        x.y = (float)(-(e01 * d[3] + e11 * d[6] + e12 * d[8]) / det64);
+        x.z = (float)(-(e02 * d[3] + e12 * d[6] + e22 * d[8]) / det64);
+        return 2;
+    }
+    x = mid;
+    return 0;
+}
+
 // returns false when the reference leaves the stale cost in place. kLegacy: the cost of CUSimp
 // (cusimp.cu:270-471): the mean ring length is counted twice (`edge_len += edge_len + |e|`) and the skinny term
-// has no penalty factor.
-template <bool kLegacy, bool kPow>
+// has no penalty factor. kMode (precision mode, not the reference's arithmetic): 0 the reference's float order;
+// 1 quadric, ring-length, skinny and cost sums compensated (TwoSum/TwoProd, rounded once); 2 as 1 with the
+// placement at the quadric's minimiser (qem_optimum) instead of the midpoint. raw: the cost before its clamp and
+// quantisation; place: the placement.
+template <bool kLegacy, bool kPow, int kMode>
 __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restrict__ nt_off, const int* __restrict__ nt,
                                                 const int4* __restrict__ tri, const float4* __restrict__ pos,
                                                 const Quadric* __restrict__ q, const float4* __restrict__ fgeo,
-                                                const int* __restrict__ nxt, float scale, float tres, uint32_t& out) {
+                                                const int* __restrict__ nxt, float scale, float tres, uint32_t& out,
+                                                float& raw, V3& place) {
+    raw = __int_as_float(0x7fc00000);  // NaN: no finite cost (invalid)
     // link condition
     int dup = 0;
     const int ua = nt_off[u], ub = nt_off[u + 1], va = nt_off[v], vb = nt_off[v + 1];
@@ -353,43 +442,89 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
         }
     }
     if (dup != 2) return false;
-    float len = 0.0f;
+    typedef typename std::conditional<kMode == 0, float, CSum>::type Acc;
+    Acc lacc{};
     int cnt = 0;
-    ring_len(u, nt_off, nt, fgeo, len, cnt);
-    ring_len(v, nt_off, nt, fgeo, len, cnt);
+    ring_len(u, nt_off, nt, fgeo, lacc, cnt);
+    ring_len(v, nt_off, nt, fgeo, lacc, cnt);
+    float len = acc_value(lacc);
     const V3 v0 = v3(pos[u]), v1 = v3(pos[v]);
     len = len / (float)cnt / scale * tres;
     if (kLegacy) len = len + (len + vnorm(vsub(v0, v1)) / scale * tres);
     else len = len + vnorm(vsub(v0, v1)) / scale * tres;
-    const V3 vm = vdiv(vadd(v0, v1), 2.0f);
-    float qa = 0.0f;
+    const Quadric Qu = q[u], Qv = q[v];
+    const float qu[10] = {Qu.a.x, Qu.a.y, Qu.a.z, Qu.a.w, Qu.b.x, Qu.b.y, Qu.b.z, Qu.b.w, Qu.c.x, Qu.c.y};
+    const float qv[10] = {Qv.a.x, Qv.a.y, Qv.a.z, Qv.a.w, Qv.b.x, Qv.b.y, Qv.b.z, Qv.b.w, Qv.c.x, Qv.c.y};
+    float m[10], mlo[10];
+#pragma unroll
+    for (int i = 0; i < 10; ++i) {
+        if constexpr (kMode == 0) {
+            m[i] = qu[i] + qv[i];
+            mlo[i] = 0.0f;
+        } else {
+            two_sum(qu[i], qv[i], m[i], mlo[i]);
+        }
+    }
+    V3 vm = vdiv(vadd(v0, v1), 2.0f);
+    if constexpr (kMode == 2) qem_optimum(m, mlo, vm, vm);
+    place = vm;
+    Acc qacc{};
     int ntri = 0;
-    if (!ring_skinny<kLegacy, kPow>(u, v, vm, nt_off, nt, tri, pos, fgeo, qa, ntri) ||
-        !ring_skinny<kLegacy, kPow>(v, u, vm, nt_off, nt, tri, pos, fgeo, qa, ntri)) {
+    if (!ring_skinny<kLegacy, kPow>(u, v, vm, nt_off, nt, tri, pos, fgeo, qacc, ntri) ||
+        !ring_skinny<kLegacy, kPow>(v, u, vm, nt_off, nt, tri, pos, fgeo, qacc, ntri)) {
         out = 0xFFFFFFFFu;
         return true;
     }
+    float qa = acc_value(qacc);
     if (!kLegacy) qa = 5.0f * qa;  // SKINNY_TRIANGLE_PENALTY
-    const Quadric Qu = q[u], Qv = q[v];
-    const float m00 = Qu.a.x + Qv.a.x, m01 = Qu.a.y + Qv.a.y, m02 = Qu.a.z + Qv.a.z, m03 = Qu.a.w + Qv.a.w;
-    const float m11 = Qu.b.x + Qv.b.x, m12 = Qu.b.y + Qv.b.y, m13 = Qu.b.z + Qv.b.z, m22 = Qu.b.w + Qv.b.w;
-    const float m23 = Qu.c.x + Qv.c.x, m33 = Qu.c.y + Qv.c.y;
     const float x = vm.x, y = vm.y, z = vm.z, w = 1.0f;
-    // Mat4x4::vTMv (cusimp_free.h:145-152) on the symmetric matrix
-    const float c0 = m00 * x + m01 * y + m02 * z + m03 * w;
-    const float c1 = m01 * x + m11 * y + m12 * z + m13 * w;
-    const float c2 = m02 * x + m12 * y + m22 * z + m23 * w;
-    const float c3 = m03 * x + m13 * y + m23 * z + m33 * w;
-    const float qem = c0 * x + c1 * y + c2 * z + c3 * w;
+    float qem;
+    if constexpr (kMode == 0) {
+        const float m00 = m[0], m01 = m[1], m02 = m[2], m03 = m[3], m11 = m[4], m12 = m[5], m13 = m[6], m22 = m[7],
+                    m23 = m[8], m33 = m[9];
+        // Mat4x4::vTMv (cusimp_free.h:145-152) on the symmetric matrix
+        const float c0 = m00 * x + m01 * y + m02 * z + m03 * w;
+        const float c1 = m01 * x + m11 * y + m12 * z + m13 * w;
+        const float c2 = m02 * x + m12 * y + m22 * z + m23 * w;
+        const float c3 = m03 * x + m13 * y + m23 * z + m33 * w;
+        qem = c0 * x + c1 * y + c2 * z + c3 * w;
+    } else {
+        // the same products with the matrix as hi + lo, each dot compensated
+        const int row[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
+        const float vv[4] = {x, y, z, w};
+        CSum outer;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            CSum inner;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                inner.add_prod(m[row[r][c]], vv[c]);
+                inner.add_prod(mlo[row[r][c]], vv[c]);
+            }
+            outer.add_prod(inner.s, vv[r]);
+            outer.add_prod(inner.c, vv[r]);
+        }
+        qem = outer.value();
+    }
     const float cost = qem / (scale * scale);
-    const float tot = cost + len + qa / (float)ntri * tres;
+    float tot;
+    if constexpr (kMode == 0) {
+        tot = cost + len + qa / (float)ntri * tres;
+    } else {
+        CSum t;
+        t.add(cost);
+        t.add(len);
+        t.add(qa / (float)ntri * tres);
+        tot = t.value();
+    }
+    raw = tot;
     out = f2u_sat(rclamp(tot, 0.0f, kCostRange) / kCostRange * kU32MaxF);
     return true;
 }
 
 // kBatch: many meshes in one vertex numbering; the scale and is_stuck of an edge's mesh come from per-mesh arrays
 // (mesh of the lower vertex from vmesh) instead of d_scale and the single flag.
-template <bool kLegacy, bool kPow, bool kBatch>
+template <bool kLegacy, bool kPow, bool kBatch, int kMode = 0>
 __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const int* __restrict__ eorder,
                                                   const int2* __restrict__ edges,
                                                   const int* __restrict__ nt_off, const int* __restrict__ nt,
@@ -398,7 +533,8 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
                                                   const int* __restrict__ nxt, const unsigned char* __restrict__ invalid,
                                                   uint32_t* cost, unsigned long long* vmin, const float* d_scale,
                                                   float tres, int is_stuck_host, const int* is_stuck_dev,
-                                                  const int* __restrict__ vmesh, const int* __restrict__ mesh_stuck) {
+                                                  const int* __restrict__ vmesh, const int* __restrict__ mesh_stuck,
+                                                  float* raw_out = nullptr, float4* place_out = nullptr) {
     int is_stuck = 0;
     float scale = 0.0f;
     if constexpr (!kBatch) {
@@ -423,7 +559,12 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
         } else if (!kLegacy && is_stuck) {
             write = false;
         } else {
-            write = edge_cost_value<kLegacy, kPow>(u, v, nt_off, nt, tri, pos, q, fgeo, nxt, scale, tres, c);
+            float raw;
+            V3 place;
+            write = edge_cost_value<kLegacy, kPow, kMode>(u, v, nt_off, nt, tri, pos, q, fgeo, nxt, scale, tres, c, raw,
+                                                          place);
+            if (raw_out) raw_out[e] = write ? raw : __int_as_float(0x7fc00000);
+            if (place_out) place_out[e] = make_float4(place.x, place.y, place.z, 0.f);
         }
         if (write) cost[e] = c;
         else c = cost[e];  // stale value of an earlier round
@@ -485,13 +626,15 @@ __device__ __forceinline__ bool ring_has_skinny(int w, const int* __restrict__ n
 
 
 // kRestore = false: CUSimp's collapse (cusimp.cu:512-585), without the skinny-ring restore
-template <bool kRestore>
+// kOpt (precision mode 2): the collapse places at the edge's precomputed placement instead of the midpoint
+template <bool kRestore, bool kOpt = false>
 __global__ void __launch_bounds__(kT) k_collapse(RoundCounters* rc, const int* __restrict__ eorder,
                                                  const int2* __restrict__ edges,
                                                  const uint32_t* __restrict__ cost, uint32_t collapse_t,
                                                  const unsigned long long* __restrict__ fkey, const int* __restrict__ nt_off,
                                                  const int* __restrict__ nt, int4* tri, const int4* __restrict__ orig_tri,
-                                                 float4* pos, const float4* __restrict__ orig_pos, int* occ, int* win) {
+                                                 float4* pos, const float4* __restrict__ orig_pos, int* occ, int* win,
+                                                 const float4* __restrict__ place = nullptr) {
     const int n = rc->n_edges;
     if (gtid() == 0) win[n] = 0;
     for (int i = gtid(); i < n; i += gstride()) {
@@ -508,7 +651,8 @@ __global__ void __launch_bounds__(kT) k_collapse(RoundCounters* rc, const int* _
             if (ok) {
                 w = 1;
                 const V3 v0 = v3(pos[u]), v1 = v3(pos[v]);
-                const V3 vm = vdiv(vadd(v0, v1), 2.0f);
+                V3 vm = vdiv(vadd(v0, v1), 2.0f);
+                if constexpr (kOpt) vm = v3(place[e]);
                 pos[u] = make_float4(vm.x, vm.y, vm.z, 0.f);
                 pos[v] = make_float4(0.f, 0.f, 0.f, 0.f);
                 occ[v] = 0;
@@ -1129,8 +1273,10 @@ void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* 
     k_sort_adjacency<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt); note_launch();
 }
 void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
-                     const float4* fgeo, Quadric* q, int* nxt, cudaStream_t s) {
-    k_quadrics<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, fgeo, q, nxt); note_launch();
+                     const float4* fgeo, Quadric* q, int* nxt, cudaStream_t s, bool comp) {
+    if (comp) k_quadrics<true><<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, fgeo, q, nxt);
+    else k_quadrics<false><<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, fgeo, q, nxt);
+    note_launch();
 }
 void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s) {
     k_edge_cost_capacity<<<1, 1, 0, s>>>(rc, d_cap); note_launch();
@@ -1140,8 +1286,36 @@ void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eor
                       const int* nt, const int4* tri, const float4* pos, const Quadric* q, const float4* fgeo,
                       const int* nxt, const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin,
                       const float* d_scale, float tres, int is_stuck, cudaStream_t s, const int* is_stuck_dev, bool legacy,
-                      bool device_pow) {
+                      bool device_pow, int mode, float* raw, float4* place) {
     const int g = grid_for(n_edges_bound, kT);
+    if (!legacy && mode != 0) {
+#define PAMO_COST_MODE(M, P)                                                                                         \
+    k_edge_cost<false, P, false, M><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,  \
+                                                     cost, vmin, d_scale, tres, is_stuck, is_stuck_dev, nullptr,    \
+                                                     nullptr, raw, place)
+        if (mode == 1) {
+            if (device_pow) PAMO_COST_MODE(1, true);
+            else PAMO_COST_MODE(1, false);
+        } else {
+            if (device_pow) PAMO_COST_MODE(2, true);
+            else PAMO_COST_MODE(2, false);
+        }
+#undef PAMO_COST_MODE
+        note_launch();
+        return;
+    }
+    if (raw || place) {  // the reference's arithmetic with the probe outputs
+        if (device_pow)
+            k_edge_cost<false, true, false, 0><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt,
+                                                                invalid, cost, vmin, d_scale, tres, is_stuck,
+                                                                is_stuck_dev, nullptr, nullptr, raw, place);
+        else
+            k_edge_cost<false, false, false, 0><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt,
+                                                                 invalid, cost, vmin, d_scale, tres, is_stuck,
+                                                                 is_stuck_dev, nullptr, nullptr, raw, place);
+        note_launch();
+        return;
+    }
     if (legacy) {
         if (device_pow)
             k_edge_cost<true, true, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
@@ -1181,8 +1355,12 @@ void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri
 void launch_collapse(RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const uint32_t* cost,
                      uint32_t collapse_t, const unsigned long long* fkey, const int* nt_off, const int* nt, int4* tri,
                      const int4* orig_tri, float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s,
-                     bool restore) {
-    if (restore)
+                     bool restore, const float4* place) {
+    if (restore && place)
+        k_collapse<true, true><<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, cost, collapse_t, fkey,
+                                                                          nt_off, nt, tri, orig_tri, pos, orig_pos, occ,
+                                                                          win, place);
+    else if (restore)
         k_collapse<true><<<grid_for(n_edges_bound, kT), kT, 0, s>>>(rc, eorder, edges, cost, collapse_t, fkey, nt_off, nt,
                                                                     tri, orig_tri, pos, orig_pos, occ, win);
     else

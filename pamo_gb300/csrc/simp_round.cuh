@@ -36,27 +36,32 @@ void launch_fill_adjacency(const int4* tri, const RoundCounters* rc, int n_tris_
 void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* nt_off, int* nt, cudaStream_t s);
 
 // ---- cost, selection, collapse ----
+// comp: precision mode, the quadric sums compensated
 void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
-                     const float4* fgeo, Quadric* q, int* nxt, cudaStream_t s);
+                     const float4* fgeo, Quadric* q, int* nxt, cudaStream_t s, bool comp = false);
 void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s);
+// mode: 0 the reference's arithmetic; precision mode 1 (compensated sums) or 2 (compensated, placement at the
+// quadric's minimiser, written to place[e]). raw (optional): each edge's cost before clamp and quantisation (NaN where
+// none is computed); place (optional, required by mode 2): each edge's placement.
 void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
                       const int* nt, const int4* tri, const float4* pos, const Quadric* q, const float4* fgeo,
                       const int* nxt, const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin,
                       const float* d_scale, float tres, int is_stuck, cudaStream_t s, const int* is_stuck_dev = nullptr,
-                      bool legacy = false, bool device_pow = true);
+                      bool legacy = false, bool device_pow = false, int mode = 0, float* raw = nullptr,
+                      float4* place = nullptr);
 // The edge cost of many meshes in one vertex numbering: the scale and is_stuck of each edge's mesh (vmesh of its
 // lower vertex) come from mesh_scale and mesh_stuck.
 void launch_edge_cost_batch(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges,
                             const int* nt_off, const int* nt, const int4* tri, const float4* pos, const Quadric* q,
                             const float4* fgeo, const int* nxt, const unsigned char* invalid, uint32_t* cost,
                             unsigned long long* vmin, const float* mesh_scale, const int* mesh_stuck, const int* vmesh,
-                            float tres, cudaStream_t s, bool device_pow = true);
+                            float tres, cudaStream_t s, bool device_pow = false);
 void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
                       unsigned long long* fkey, cudaStream_t s);
 void launch_collapse(RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const uint32_t* cost,
                      uint32_t collapse_t, const unsigned long long* fkey, const int* nt_off, const int* nt, int4* tri,
                      const int4* orig_tri, float4* pos, const float4* orig_pos, int* occ, int* win, cudaStream_t s,
-                     bool restore = true);
+                     bool restore = true, const float4* place = nullptr);
 void launch_compact_winners(const RoundCounters* rc, int n_edges_bound, const int* win_scan, int* collapsed,
                             cudaStream_t s);
 void launch_remove_invalid(const RoundCounters* rc, int n_tris_bound, int4* tri, cudaStream_t s);

@@ -105,3 +105,32 @@ def test_autotune_picks_a_candidate_and_caches_it(tmp_path, monkeypatch):
     assert res["best"] in (2, 4) and res[2] > 0 and res[4] > 0
     assert autotune.best_workers() == res["best"]
     assert (tmp_path / "tune.json").exists()
+
+
+def test_server_stage3_equals_pamo_run():
+    """Requests with stage 3 (PaMO(use_stage3=True) per request, the projection onto the request's own input): each
+    result has PaMO.run's faces and its positions within 1e-5 of the bounding-box diagonal (stage 3 sums with float
+    atomics), alone and among other requests."""
+    import pamo_gb300
+    from pamo_gb300.batch import Server
+    from pamo_gb300 import synth
+
+    ms = [synth.star_mesh(n, 4, lambda l: 0.04, seed) for n, seed in [(10, 1), (14, 2), (8, 3)]]
+    srv = Server("cuda:0", workers=3, hbm_budget_bytes=8 << 30)
+    ids = {srv.submit(v, f, 0.05, stage3=True): i for i, (v, f) in enumerate(ms)}
+    got = {}
+    while len(got) < len(ms):
+        w = srv.wait(20000)
+        assert w is not None, "server stalled"
+        rid, st, npt, ntr, _ = w
+        assert st == 0
+        got[ids[rid]] = srv.fetch(rid, npt, ntr, float64=True)
+    srv.close()
+    for i, (v, f) in enumerate(ms):
+        pm = pamo_gb300.PaMO((v.astype(np.float64), f), use_stage1=False, use_stage3=True)
+        V, F = pm.run(torch.from_numpy(v).cuda(), torch.from_numpy(f).cuda(), ratio=0.05, min_verts=0)
+        V, F = np.asarray(V), np.asarray(F)
+        assert got[i][0].dtype == np.float64
+        assert np.array_equal(got[i][1], F)
+        diag = float(np.linalg.norm(V.max(0) - V.min(0)))
+        assert np.abs(got[i][0] - V).max() <= 1e-5 * diag

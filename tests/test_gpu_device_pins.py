@@ -4,8 +4,8 @@
   permutations as tests/golden/thrust_shuffle.npz, which was made with Thrust's CPP device system: the generator
   tests/golden/thrust_shuffle_golden.cpp is compiled here as CUDA and run on the GPU.
 * the device's pow(float, 2) (the reference's skinny term, cusimp_free.cu:533,573) differs from x * x only by one
-  ulp, on a few floats in a million (the oracle squares by multiplication); and the CUDA path, which calls the
-  device function like the reference, gives the same rounds with either form on the test meshes and the
+  ulp, on a few floats in a million; the oracle and, by default, the CUDA path square by multiplication, and the
+  CUDA path gives the same rounds with the device function (option skinny_pow) on the test meshes and the
   20,480-face workload.
 
 Both programs are compiled with nvcc for sm_103a at test time.
