@@ -638,7 +638,7 @@ struct pamo_csr {
             (r = grow(res_tri, fc)) || (r = grow(tri_load, fc)) || (r = grow(ecount, fc + 1)) ||
             (r = grow(qflag, fc + 1)) || (r = grow(qlist, fc)) || (r = grow(fflags, fc + 1)) || (r = grow(nt, 3 * fc)) ||
             (r = grow(nxt, 3 * fc)) || (r = grow(fmesh, fc)) || (r = grow(shuffle_flags, 2 * fc + 40)) ||
-            (r = grow(fgeo, 3 * fc)) || (r = grow(face_mean, 3 * fc)) || (r = grow(fkey, fc)) || (r = grow(hit, fc + 1)))
+            (r = grow(fgeo, 4 * fc)) || (r = grow(face_mean, 3 * fc)) || (r = grow(fkey, fc)) || (r = grow(hit, fc + 1)))
             return r;
         if ((r = grow(edges, ec)) || (r = grow(eorder, ec)) || (r = grow(win, ec + 1)) || (r = grow(winners, ec)) ||
             (r = grow(lines, ec)) || (r = grow(considered, ec)) || (r = grow(uflag, ec + 1)) || (r = grow(cost, ec)) ||

@@ -108,6 +108,7 @@ struct pamo_ctx {
     DevBuf<int> occ, valence, cursor;
     DevBuf<int> vedges, vcursor;  // edges per lower endpoint (offsets) and fill cursors
     DevBuf<Quadric> quad;
+    DevBuf<Quadric> quad_lo;  // precision modes: the quadrics' lo parts (q = quad + quad_lo in double-float)
     DevBuf<unsigned long long> vmin;
     DevBuf<int> undo_in;
 
@@ -115,7 +116,7 @@ struct pamo_ctx {
     DevBuf<int4> tri, orig_tri, tri_in, tri_out;
     DevBuf<int> ecount, qflag, qlist, fflags, nt, shuffle_flags;
     DevBuf<int> nxt;        // per CSR slot: the vertex after the ring's vertex in the slot's face
-    DevBuf<float4> fgeo;    // per face: edge lengths, unnormalised normal, plane (three float4)
+    DevBuf<float4> fgeo;    // per face: edge lengths and normal (two float4), then the planes (room for four per face)
     DevBuf<unsigned long long> fkey;
     DevBuf<unsigned char> hit;
     BvhBuffers bvh;
@@ -163,6 +164,8 @@ struct pamo_ctx {
     DevBuf<float> probe_raw;    // pamo_cost_probe: each edge's cost before quantisation
     int ensure_place(size_t n_edges) { return precision == 2 ? grow(place, n_edges) : PAMO_OK; }
     float4* place_ptr() { return precision == 2 ? place.p : nullptr; }
+    int ensure_quad_lo() { return precision > 0 && cap_v ? grow(quad_lo, cap_v) : PAMO_OK; }
+    Quadric* qlo_ptr() { return precision > 0 ? quad_lo.p : nullptr; }
     long long pair_cap_limit = 0;  // > 0: at most this many listed candidate pairs per check (tests the overflow path)
 
     int pair_cap() const {
@@ -282,7 +285,7 @@ struct pamo_ctx {
             b.n = 0;
         };
         fr(edge_cost); fr(invalid); fr(pts_map); fr(pts_map_prev); fr(undo_list); fr(tmp_undo);
-        fr(pos); fr(orig_pos); fr(pos_in); fr(pos_out); fr(occ); fr(valence); fr(cursor); fr(quad); fr(vmin); fr(undo_in);
+        fr(pos); fr(orig_pos); fr(pos_in); fr(pos_out); fr(occ); fr(valence); fr(cursor); fr(quad); fr(quad_lo); fr(vmin); fr(undo_in);
         fr(nxt); fr(fgeo); fr(tri); fr(orig_tri); fr(tri_in); fr(tri_out); fr(ecount); fr(qflag); fr(qlist); fr(fflags); fr(nt);
         fr(shuffle_flags); fr(fkey); fr(eorder); fr(vedges); fr(vcursor); fr(hit); fr(edges); fr(win); fr(collapsed); fr(uflag); fr(face_mean); fr(exact_list); fr(place); fr(probe_raw);
         if (bvh_mem) cudaFree(bvh_mem);
@@ -353,7 +356,8 @@ struct pamo_ctx {
     size_t device_bytes() const {
         size_t b = 0;
         b += pos.bytes() + orig_pos.bytes() + pos_in.bytes() + pos_out.bytes() + occ.bytes() + valence.bytes() +
-             cursor.bytes() + vedges.bytes() + vcursor.bytes() + quad.bytes() + vmin.bytes() + undo_in.bytes();
+             cursor.bytes() + vedges.bytes() + vcursor.bytes() + quad.bytes() + quad_lo.bytes() + vmin.bytes() +
+             undo_in.bytes();
         b += nxt.bytes() + fgeo.bytes();
         b += tri.bytes() + orig_tri.bytes() + tri_in.bytes() + tri_out.bytes() + ecount.bytes() + qflag.bytes() +
              qlist.bytes() + fflags.bytes() + nt.bytes() + shuffle_flags.bytes() + fkey.bytes() + hit.bytes() +
@@ -375,7 +379,7 @@ struct pamo_ctx {
             (r = grow(pos_in, nc)))
             return r;
         cap_v = nc;
-        return PAMO_OK;
+        return ensure_quad_lo();
     }
 
     int ensure_face_buffers(size_t n) {
@@ -386,7 +390,7 @@ struct pamo_ctx {
         int r;
         if ((r = grow(tri, nc)) || (r = grow(orig_tri, nc)) || (r = grow(tri_in, nc)) || (r = grow(tri_out, nc)) ||
             (r = grow(ecount, nc + 1)) || (r = grow(qflag, nc + 1)) || (r = grow(qlist, nc)) || (r = grow(fflags, nc + 1)) ||
-            (r = grow(nt, 3 * nc)) || (r = grow(nxt, 3 * nc)) || (r = grow(fgeo, 3 * nc)) || (r = grow(shuffle_flags, 2 * nc + 40)) || (r = grow(fkey, nc)) || (r = grow(hit, nc)) ||
+            (r = grow(nt, 3 * nc)) || (r = grow(nxt, 3 * nc)) || (r = grow(fgeo, 4 * nc)) || (r = grow(shuffle_flags, 2 * nc + 40)) || (r = grow(fkey, nc)) || (r = grow(hit, nc)) ||
             (r = grow(eorder, 2 * nc)) ||
             (r = grow(edges, 2 * nc)) || (r = grow(win, 2 * nc + 1)) || (r = grow(collapsed, 2 * nc)) ||
             (r = grow(uflag, 2 * nc + 1)) || (r = grow(face_mean, 3 * nc)) ||
@@ -464,7 +468,7 @@ struct pamo_ctx {
         precision = mode;
         int r;
         if ((r = ensure_vertex_buffers(nP)) || (r = ensure_face_buffers(nT)) || (r = ensure_pts_state(nP)) ||
-            (r = grow(probe_raw, 2 * cap_f)) || (r = grow(place, 2 * cap_f))) {
+            (r = grow(probe_raw, 2 * cap_f)) || (r = grow(place, 2 * cap_f)) || (mode > 0 && (r = grow(quad_lo, cap_v)))) {
             precision = keep;
             return r;
         }
@@ -479,16 +483,17 @@ struct pamo_ctx {
         cudaMemsetAsync(vedges.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(vcursor.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(invalid.p, 0, invalid.n, s);
-        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
+        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p, mode > 0);
         scan_adjacency_counts(s, std::max(nP, nT));
         launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p, eorder.p, s);
         launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
-        launch_quadrics(rc, nP, valence.p, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s, mode > 0);
+        Quadric* qlo = mode > 0 ? quad_lo.p : nullptr;
+        launch_quadrics(rc, nP, valence.p, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s, qlo);
         cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
         cudaMemsetAsync(probe_raw.p, 0xFF, probe_raw.n * sizeof(float), s);  // NaN where no cost is computed
         launch_edge_cost(rc, 2 * nT, eorder.p, edges.p, valence.p, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p,
                          edge_cost.p, vmin.p, d_scale, threshold, 0, s, nullptr, false, skinny_pow, mode, probe_raw.p,
-                         place.p);
+                         place.p, qlo);
         precision = keep;
         if ((r = read_counters())) return r;
         return status_to_error(h_rc->status);
@@ -523,18 +528,18 @@ struct pamo_ctx {
                                         invalid.p, (int)invalid.n, s);
             launch_round_prologue_dev(d_ls, rc, nPb, nTb, pts_map.p, pts_map_prev.p, pos_in.p, pos.p, orig_pos.p, occ.p,
                                       tri_in.p, tri.p, orig_tri.p, valence.p, cursor.p, vedges.p, vcursor.p, qflag.p, s);
-            launch_face_counts(tri.p, rc, nTb, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
+            launch_face_counts(tri.p, rc, nTb, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p, precision > 0);
             scan_adjacency_counts(s, std::max(nPb, nTb));
             launch_fill_adjacency(tri.p, rc, nTb, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p,
                                   eorder.p, s);
             launch_sort_adjacency(rc, nPb, valence.p, nt.p, s);
-            launch_quadrics(rc, nPb, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s, precision > 0);
+            launch_quadrics(rc, nPb, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s, qlo_ptr());
             launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
             launch_fill_u64_dev(rc, nPb, vmin.p, ~0ull, s);
             cost_begin(s);
             launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p,
                              vmin.p, d_scale, threshold, 0, s, &d_ls->is_stuck, false, skinny_pow, precision, nullptr,
-                             place_ptr());
+                             place_ptr(), qlo_ptr());
             cost_end(s);
             launch_face_keys(rc, nTb, tri.p, vmin.p, fkey.p, s);
             launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p,
@@ -693,7 +698,7 @@ struct pamo_ctx {
         cudaMemsetAsync(cursor.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(vedges.p, 0, (nP + 1) * sizeof(int), s);
         cudaMemsetAsync(vcursor.p, 0, (nP + 1) * sizeof(int), s);
-        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p);
+        launch_face_counts(tri.p, rc, nT, valence.p, ecount.p, vedges.p, s, pos.p, fgeo.p, precision > 0);
         scan_adjacency_counts(s, std::max(nP, nT));
         launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p, eorder.p, s);
         launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
@@ -703,14 +708,15 @@ struct pamo_ctx {
 
         // cost and selection
         prof.begin(kPhQuad, s);
-        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s, precision > 0);
+        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s, qlo_ptr());
         prof.end(kPhQuad, s);
         launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
         cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
         prof.begin(kPhCost, s);
         cost_begin(s);
         launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p, vmin.p,
-                         d_scale, threshold, is_stuck, s, nullptr, false, skinny_pow, precision, nullptr, place_ptr());
+                         d_scale, threshold, is_stuck, s, nullptr, false, skinny_pow, precision, nullptr, place_ptr(),
+                         qlo_ptr());
         cost_end(s);
         prof.end(kPhCost, s);
         prof.begin(kPhCollapse, s);
@@ -839,6 +845,8 @@ int pamo_ctx_set_option(pamo_ctx* ctx, const char* name, int64_t value) {
             const int r = ctx->ensure_place(2 * ctx->cap_f);
             if (r) return r;
         }
+        const int r = ctx->ensure_quad_lo();
+        if (r) return r;
     }
     else if (n == "time_rounds") ctx->time_rounds = value != 0;
     else if (n == "time_edge_cost") {

@@ -2310,7 +2310,10 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     // Hinges: hinge_preprocess_slow_kernel (hinge_energy.py:21-57) pairs every directed edge (a, b), a < b,
     // of a face t0 with every face t1 holding the edge as (b, a): hinge (opposite in t0, a, b, opposite in t1).
     std::vector<int> hf((size_t)3 * n_tris);
-    if (cudaMemcpy(hf.data(), tris, hf.size() * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    // on the caller's stream, after the work that produced the triangles there (a non-blocking stream does not
+    // order with a copy on the legacy default stream)
+    if (cudaMemcpyAsync(hf.data(), tris, hf.size() * sizeof(int), cudaMemcpyDeviceToHost, caller) != cudaSuccess ||
+        cudaStreamSynchronize(caller) != cudaSuccess)
         return fail(PAMO_ERR_CUDA, "copy of the triangles");
     std::vector<long long> ukeys;
     std::vector<std::pair<long long, int>> dkeys;  // directed edge (a * n + b) -> face * 3 + corner

@@ -106,10 +106,13 @@ __global__ void k_shuffle_gather(Feistel fb, const int* __restrict__ scan, const
 // ------------------------------------------------------------------ adjacency
 // Per-face values that the vertex rings read many times (every face lies in three rings and every ring is
 // read once per incident edge), each computed by the same operations as where the reference computes it:
-//   fgeo[3f]     = |p_x - p_y|, |p_y - p_z|, |p_z - p_x| and, as int bits, which of t.x > t.y, t.y > t.z,
-//                  t.z > t.x hold (the ring edge-length terms, :449-484);
-//   fgeo[3f + 1] = the unnormalised normal cross(p_y - p_x, p_z - p_x) and its L1 norm (the flip test);
-//   fgeo[3f + 2] = the face plane of tri2plane (:337-346).
+//   fgeo[2f]      = |p_x - p_y|, |p_y - p_z|, |p_z - p_x| and, as int bits, which of t.x > t.y, t.y > t.z,
+//                   t.z > t.x hold (the ring edge-length terms, :449-484);
+//   fgeo[2f + 1]  = the unnormalised normal cross(p_y - p_x, p_z - p_x) and its L1 norm (the flip test);
+//   fgeo[2n + f]  = the face plane of tri2plane (:337-346), n = the round's face count (precision mode: the plane
+//                   as a double-float pair, fgeo[2n + 2f] and fgeo[2n + 2f + 1]).
+// The two records the edge cost reads for a ring face form one aligned 32-byte sector; the planes, which only the
+// quadrics read, follow all of them. The buffer holds 4 float4 per face.
 __device__ __forceinline__ void face_plane(const float4* __restrict__ pos, int4 t, float p[4]);
 
 // ---- precision mode: error-free transforms (Knuth's TwoSum; TwoProd with an explicit fused multiply-add, which
@@ -139,14 +142,70 @@ struct CSum {
     }
     __device__ __forceinline__ float value() const { return s + c; }
 };
+// Double-float numbers (hi + lo, |lo| <= ulp(hi) / 2) from FP32 operations only (Dekker; Hida, Li and Bailey's
+// double-double algorithms), for the precision mode's face planes: about 44 significant bits without FP64.
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ DF df_fast(float a, float b) {  // |a| >= |b|
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e += a.lo + b.lo;
+    return df_fast(s, e);
+}
+__device__ __forceinline__ DF df_neg(DF a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+    float p, e;
+    two_prod(a.hi, b.hi, p, e);
+    e += a.hi * b.lo + a.lo * b.hi;
+    return df_fast(p, e);
+}
+__device__ __forceinline__ DF df_diff(float a, float b) {  // a - b exactly
+    float s, e;
+    two_sum(a, -b, s, e);
+    return {s, e};
+}
+__device__ __forceinline__ DF df_sqrt(DF a) {
+    if (!(a.hi > 0.0f)) return {0.0f, 0.0f};
+    const float r = sqrtf(a.hi);
+    float p, e;
+    two_prod(r, r, p, e);
+    return df_fast(r, ((a.hi - p) - e + a.lo) / (2.0f * r));
+}
+__device__ __forceinline__ DF df_div(DF a, DF b) {
+    const float q1 = a.hi / b.hi;
+    const DF r = df_add(a, df_neg(df_mul(b, DF{q1, 0.0f})));
+    return df_fast(q1, r.hi / b.hi);
+}
+
+// The face plane of tri2plane (unit normal of cross(p_y - p_x, p_z - p_x), offset -n.p_x) in double-float
+__device__ __forceinline__ void face_plane_df(const float4* __restrict__ pos, int4 t, DF p[4]) {
+    const float4 a = pos[t.x], b = pos[t.y], c = pos[t.z];
+    const DF e1[3] = {df_diff(b.x, a.x), df_diff(b.y, a.y), df_diff(b.z, a.z)};
+    const DF e2[3] = {df_diff(c.x, a.x), df_diff(c.y, a.y), df_diff(c.z, a.z)};
+    DF n[3];
+    n[0] = df_add(df_mul(e1[1], e2[2]), df_neg(df_mul(e1[2], e2[1])));
+    n[1] = df_add(df_mul(e1[2], e2[0]), df_neg(df_mul(e1[0], e2[2])));
+    n[2] = df_add(df_mul(e1[0], e2[1]), df_neg(df_mul(e1[1], e2[0])));
+    const DF len = df_sqrt(df_add(df_add(df_mul(n[0], n[0]), df_mul(n[1], n[1])), df_mul(n[2], n[2])));
+    for (int k = 0; k < 3; ++k) p[k] = df_div(n[k], len);
+    const DF d = df_add(df_add(df_mul(p[0], DF{a.x, 0.0f}), df_mul(p[1], DF{a.y, 0.0f})), df_mul(p[2], DF{a.z, 0.0f}));
+    p[3] = df_neg(d);
+}
+
 __device__ __forceinline__ void acc_add(float& a, float x) { a += x; }
 __device__ __forceinline__ void acc_add(CSum& a, float x) { a.add(x); }
 __device__ __forceinline__ float acc_value(float a) { return a; }
 __device__ __forceinline__ float acc_value(const CSum& a) { return a.value(); }
 
+// plane_df (precision mode): the planes as double-float pairs, fgeo[2n + 2f] (hi) and fgeo[2n + 2f + 1] (lo)
 __global__ void __launch_bounds__(kT) k_face_counts(const int4* __restrict__ tri, const RoundCounters* rc, int* valence,
                                                     int* ecount, int* vedges, const float4* __restrict__ pos,
-                                                    float4* fgeo) {
+                                                    float4* fgeo, int plane_df) {
     const int n = rc->n_tris;
     for (int f = gtid(); f < n; f += gstride()) {
         const int4 t = tri[f];
@@ -157,13 +216,20 @@ __global__ void __launch_bounds__(kT) k_face_counts(const int4* __restrict__ tri
         if (fgeo) {
             const V3 o0 = v3(pos[t.x]), o1 = v3(pos[t.y]), o2 = v3(pos[t.z]);
             const int mask = (t.x > t.y ? 1 : 0) | (t.y > t.z ? 2 : 0) | (t.z > t.x ? 4 : 0);
-            fgeo[3 * (size_t)f] = make_float4(vnorm(vsub(o0, o1)), vnorm(vsub(o1, o2)), vnorm(vsub(o2, o0)),
+            fgeo[2 * (size_t)f] = make_float4(vnorm(vsub(o0, o1)), vnorm(vsub(o1, o2)), vnorm(vsub(o2, o0)),
                                               __int_as_float(mask));
             const V3 ou = vcross(vsub(o1, o0), vsub(o2, o0));
-            fgeo[3 * (size_t)f + 1] = make_float4(ou.x, ou.y, ou.z, fabsf(ou.x) + fabsf(ou.y) + fabsf(ou.z));
-            float pl[4];
-            face_plane(pos, t, pl);
-            fgeo[3 * (size_t)f + 2] = make_float4(pl[0], pl[1], pl[2], pl[3]);
+            fgeo[2 * (size_t)f + 1] = make_float4(ou.x, ou.y, ou.z, fabsf(ou.x) + fabsf(ou.y) + fabsf(ou.z));
+            if (plane_df) {
+                DF pd[4];
+                face_plane_df(pos, t, pd);
+                fgeo[2 * (size_t)n + 2 * (size_t)f] = make_float4(pd[0].hi, pd[1].hi, pd[2].hi, pd[3].hi);
+                fgeo[2 * (size_t)n + 2 * (size_t)f + 1] = make_float4(pd[0].lo, pd[1].lo, pd[2].lo, pd[3].lo);
+            } else {
+                float pl[4];
+                face_plane(pos, t, pl);
+                fgeo[2 * (size_t)n + f] = make_float4(pl[0], pl[1], pl[2], pl[3]);
+            }
         }
         atomicAdd(&valence[t.x], 1);
         atomicAdd(&valence[t.y], 1);
@@ -239,8 +305,10 @@ __device__ __forceinline__ int next_after(int4 t, int v);
 template <bool kComp>
 __global__ void __launch_bounds__(kT) k_quadrics(const RoundCounters* rc, const int* __restrict__ nt_off,
                                                  const int* __restrict__ nt, const int4* __restrict__ tri,
-                                                 const float4* __restrict__ fgeo, Quadric* q, int* nxt) {
+                                                 const float4* __restrict__ fgeo, Quadric* q, int* nxt,
+                                                 Quadric* qlo) {
     const int n = rc->n_pts;
+    const size_t planes = 2 * (size_t)rc->n_tris;
     for (int v = gtid(); v < n; v += gstride()) {
         float m00 = 0.f, m01 = 0.f, m02 = 0.f, m03 = 0.f, m11 = 0.f, m12 = 0.f, m13 = 0.f, m22 = 0.f, m23 = 0.f, m33 = 0.f;
         CSum c[10];
@@ -248,23 +316,40 @@ __global__ void __launch_bounds__(kT) k_quadrics(const RoundCounters* rc, const 
         for (int s = nt_off[v]; s < b; ++s) {
             const int f = nt[s];
             nxt[s] = next_after(tri[f], v);
-            const float4 pl = fgeo[3 * (size_t)f + 2];
-            const float p[4] = {pl.x, pl.y, pl.z, pl.w};
-            if constexpr (kComp) {
-                c[0].add_prod(p[0], p[0]); c[1].add_prod(p[0], p[1]); c[2].add_prod(p[0], p[2]);
-                c[3].add_prod(p[0], p[3]); c[4].add_prod(p[1], p[1]); c[5].add_prod(p[1], p[2]);
-                c[6].add_prod(p[1], p[3]); c[7].add_prod(p[2], p[2]); c[8].add_prod(p[2], p[3]);
-                c[9].add_prod(p[3], p[3]);
+            if constexpr (kComp) {  // double-float planes (face_plane_df), double-float products and sums
+                const float4 ph = fgeo[planes + 2 * (size_t)f], pl = fgeo[planes + 2 * (size_t)f + 1];
+                const DF d[4] = {{ph.x, pl.x}, {ph.y, pl.y}, {ph.z, pl.z}, {ph.w, pl.w}};
+                const int ij[10][2] = {{0, 0}, {0, 1}, {0, 2}, {0, 3}, {1, 1}, {1, 2}, {1, 3}, {2, 2}, {2, 3}, {3, 3}};
+#pragma unroll
+                for (int k = 0; k < 10; ++k) {
+                    const DF pr = df_mul(d[ij[k][0]], d[ij[k][1]]);
+                    c[k].add(pr.hi);
+                    c[k].c += pr.lo;
+                }
             } else {
+                const float4 pl = fgeo[planes + f];
+                const float p[4] = {pl.x, pl.y, pl.z, pl.w};
                 m00 += p[0] * p[0]; m01 += p[0] * p[1]; m02 += p[0] * p[2]; m03 += p[0] * p[3];
                 m11 += p[1] * p[1]; m12 += p[1] * p[2]; m13 += p[1] * p[3];
                 m22 += p[2] * p[2]; m23 += p[2] * p[3];
                 m33 += p[3] * p[3];
             }
         }
-        if constexpr (kComp) {
-            m00 = c[0].value(); m01 = c[1].value(); m02 = c[2].value(); m03 = c[3].value(); m11 = c[4].value();
-            m12 = c[5].value(); m13 = c[6].value(); m22 = c[7].value(); m23 = c[8].value(); m33 = c[9].value();
+        if constexpr (kComp) {  // each entry as hi (q) + lo (qlo)
+            float l[10];
+#pragma unroll
+            for (int k = 0; k < 10; ++k) {
+                const DF e = df_fast(c[k].s, c[k].c);
+                c[k].s = e.hi;
+                l[k] = e.lo;
+            }
+            m00 = c[0].s; m01 = c[1].s; m02 = c[2].s; m03 = c[3].s; m11 = c[4].s;
+            m12 = c[5].s; m13 = c[6].s; m22 = c[7].s; m23 = c[8].s; m33 = c[9].s;
+            Quadric L;
+            L.a = make_float4(l[0], l[1], l[2], l[3]);
+            L.b = make_float4(l[4], l[5], l[6], l[7]);
+            L.c = make_float4(l[8], l[9], 0.f, 0.f);
+            qlo[v] = L;
         }
         Quadric Q;
         Q.a = make_float4(m00, m01, m02, m03);
@@ -288,7 +373,7 @@ __device__ __forceinline__ void ring_len(int w, const int* __restrict__ nt_off, 
                                          const float4* __restrict__ fgeo, Acc& len, int& cnt) {
     const int b = nt_off[w + 1];
     for (int s = nt_off[w]; s < b; ++s) {
-        const float4 g = fgeo[3 * (size_t)nt[s]];
+        const float4 g = fgeo[2 * (size_t)nt[s]];
         const int mask = __float_as_int(g.w);
         if (mask & 1) { acc_add(len, g.x); cnt++; }
         if (mask & 2) { acc_add(len, g.y); cnt++; }
@@ -350,7 +435,7 @@ __device__ __forceinline__ bool ring_skinny(int w, int other, V3 vm, const int* 
         if (t.x == other || t.y == other || t.z == other) continue;
         const bool wx = t.x == w, wy = t.y == w, wz = t.z == w;
         const V3 n0 = wx ? vm : v3(pos[t.x]), n1 = wy ? vm : v3(pos[t.y]), n2 = wz ? vm : v3(pos[t.z]);
-        const float4 og = fgeo[3 * (size_t)f + 1];
+        const float4 og = fgeo[2 * (size_t)f + 1];
         const V3 ou = {og.x, og.y, og.z};
         const V3 nu = vcross(vsub(n1, n0), vsub(n2, n0));
         const float du = vdot(ou, nu);
@@ -362,7 +447,7 @@ __device__ __forceinline__ bool ring_skinny(int w, int other, V3 vm, const int* 
             if (vdot(on, nn) < 0) return false;
         }
         // an edge without w keeps its length (same operations as the per-face value)
-        const float4 lg = fgeo[3 * (size_t)f];
+        const float4 lg = fgeo[2 * (size_t)f];
         const float l01 = (wx || wy) ? vnorm(vsub(n0, n1)) : lg.x;
         const float l12 = (wy || wz) ? vnorm(vsub(n1, n2)) : lg.y;
         const float l20 = (wz || wx) ? vnorm(vsub(n2, n0)) : lg.z;
@@ -425,7 +510,7 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
                                                 const int4* __restrict__ tri, const float4* __restrict__ pos,
                                                 const Quadric* __restrict__ q, const float4* __restrict__ fgeo,
                                                 const int* __restrict__ nxt, float scale, float tres, uint32_t& out,
-                                                float& raw, V3& place) {
+                                                float& raw, V3& place, const Quadric* __restrict__ qlo) {
     raw = __int_as_float(0x7fc00000);  // NaN: no finite cost (invalid)
     // link condition
     int dup = 0;
@@ -464,6 +549,13 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
         } else {
             two_sum(qu[i], qv[i], m[i], mlo[i]);
         }
+    }
+    if constexpr (kMode != 0) {  // the quadrics' lo parts (k_quadrics<true>)
+        const Quadric Lu = qlo[u], Lv = qlo[v];
+        const float lu[10] = {Lu.a.x, Lu.a.y, Lu.a.z, Lu.a.w, Lu.b.x, Lu.b.y, Lu.b.z, Lu.b.w, Lu.c.x, Lu.c.y};
+        const float lv[10] = {Lv.a.x, Lv.a.y, Lv.a.z, Lv.a.w, Lv.b.x, Lv.b.y, Lv.b.z, Lv.b.w, Lv.c.x, Lv.c.y};
+#pragma unroll
+        for (int i = 0; i < 10; ++i) mlo[i] += lu[i] + lv[i];
     }
     V3 vm = vdiv(vadd(v0, v1), 2.0f);
     if constexpr (kMode == 2) qem_optimum(m, mlo, vm, vm);
@@ -523,8 +615,9 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
 }
 
 // kBatch: many meshes in one vertex numbering; the scale and is_stuck of an edge's mesh come from per-mesh arrays
-// (mesh of the lower vertex from vmesh) instead of d_scale and the single flag.
-template <bool kLegacy, bool kPow, bool kBatch, int kMode = 0>
+// (mesh of the lower vertex from vmesh) instead of d_scale and the single flag. kOut: raw_out / place_out are
+// written (probe and precision modes; a compile-time flag so that the default variant keeps its register budget).
+template <bool kLegacy, bool kPow, bool kBatch, int kMode = 0, bool kOut = false>
 __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const int* __restrict__ eorder,
                                                   const int2* __restrict__ edges,
                                                   const int* __restrict__ nt_off, const int* __restrict__ nt,
@@ -534,7 +627,8 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
                                                   uint32_t* cost, unsigned long long* vmin, const float* d_scale,
                                                   float tres, int is_stuck_host, const int* is_stuck_dev,
                                                   const int* __restrict__ vmesh, const int* __restrict__ mesh_stuck,
-                                                  float* raw_out = nullptr, float4* place_out = nullptr) {
+                                                  float* raw_out = nullptr, float4* place_out = nullptr,
+                                                  const Quadric* __restrict__ qlo = nullptr) {
     int is_stuck = 0;
     float scale = 0.0f;
     if constexpr (!kBatch) {
@@ -562,9 +656,11 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
             float raw;
             V3 place;
             write = edge_cost_value<kLegacy, kPow, kMode>(u, v, nt_off, nt, tri, pos, q, fgeo, nxt, scale, tres, c, raw,
-                                                          place);
-            if (raw_out) raw_out[e] = write ? raw : __int_as_float(0x7fc00000);
-            if (place_out) place_out[e] = make_float4(place.x, place.y, place.z, 0.f);
+                                                          place, qlo);
+            if constexpr (kOut) {
+                if (raw_out) raw_out[e] = write ? raw : __int_as_float(0x7fc00000);
+                if (place_out) place_out[e] = make_float4(place.x, place.y, place.z, 0.f);
+            }
         }
         if (write) cost[e] = c;
         else c = cost[e];  // stale value of an earlier round
@@ -1259,8 +1355,10 @@ void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4*
 }
 
 void launch_face_counts(const int4* tri, const RoundCounters* rc, int n_tris_bound, int* valence, int* ecount,
-                        int* vedges, cudaStream_t s, const float4* pos, float4* fgeo) {
-    k_face_counts<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, valence, ecount, vedges, pos, fgeo); note_launch();
+                        int* vedges, cudaStream_t s, const float4* pos, float4* fgeo, bool plane_df) {
+    k_face_counts<<<grid_for(n_tris_bound, kT), kT, 0, s>>>(tri, rc, valence, ecount, vedges, pos, fgeo,
+                                                            plane_df ? 1 : 0);
+    note_launch();
 }
 void launch_fill_adjacency(const int4* tri, const RoundCounters* rc, int n_tris_bound, const int* nt_off, int* cursor,
                            int* nt, const int* edge_off, int2* edges, const int* voff, int* vcursor, int* eorder,
@@ -1273,9 +1371,9 @@ void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* 
     k_sort_adjacency<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt); note_launch();
 }
 void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
-                     const float4* fgeo, Quadric* q, int* nxt, cudaStream_t s, bool comp) {
-    if (comp) k_quadrics<true><<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, fgeo, q, nxt);
-    else k_quadrics<false><<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, fgeo, q, nxt);
+                     const float4* fgeo, Quadric* q, int* nxt, cudaStream_t s, Quadric* qlo) {
+    if (qlo) k_quadrics<true><<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, fgeo, q, nxt, qlo);
+    else k_quadrics<false><<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, fgeo, q, nxt, nullptr);
     note_launch();
 }
 void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s) {
@@ -1286,36 +1384,36 @@ void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eor
                       const int* nt, const int4* tri, const float4* pos, const Quadric* q, const float4* fgeo,
                       const int* nxt, const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin,
                       const float* d_scale, float tres, int is_stuck, cudaStream_t s, const int* is_stuck_dev, bool legacy,
-                      bool device_pow, int mode, float* raw, float4* place) {
+                      bool device_pow, int mode, float* raw, float4* place, const Quadric* qlo) {
     const int g = grid_for(n_edges_bound, kT);
-    if (!legacy && mode != 0) {
-#define PAMO_COST_MODE(M, P)                                                                                         \
-    k_edge_cost<false, P, false, M><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,  \
-                                                     cost, vmin, d_scale, tres, is_stuck, is_stuck_dev, nullptr,    \
-                                                     nullptr, raw, place)
-        if (mode == 1) {
-            if (device_pow) PAMO_COST_MODE(1, true);
-            else PAMO_COST_MODE(1, false);
+#define PAMO_COST_MODE(M, P, O)                                                                                      \
+    k_edge_cost<false, P, false, M, O><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt,       \
+                                                        invalid, cost, vmin, d_scale, tres, is_stuck, is_stuck_dev,  \
+                                                        nullptr, nullptr, raw, place, qlo)
+    if (!legacy && mode == 1) {
+        if (raw || place) {
+            if (device_pow) PAMO_COST_MODE(1, true, true);
+            else PAMO_COST_MODE(1, false, true);
         } else {
-            if (device_pow) PAMO_COST_MODE(2, true);
-            else PAMO_COST_MODE(2, false);
+            if (device_pow) PAMO_COST_MODE(1, true, false);
+            else PAMO_COST_MODE(1, false, false);
         }
-#undef PAMO_COST_MODE
+        note_launch();
+        return;
+    }
+    if (!legacy && mode == 2) {
+        if (device_pow) PAMO_COST_MODE(2, true, true);
+        else PAMO_COST_MODE(2, false, true);
         note_launch();
         return;
     }
     if (raw || place) {  // the reference's arithmetic with the probe outputs
-        if (device_pow)
-            k_edge_cost<false, true, false, 0><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt,
-                                                                invalid, cost, vmin, d_scale, tres, is_stuck,
-                                                                is_stuck_dev, nullptr, nullptr, raw, place);
-        else
-            k_edge_cost<false, false, false, 0><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt,
-                                                                 invalid, cost, vmin, d_scale, tres, is_stuck,
-                                                                 is_stuck_dev, nullptr, nullptr, raw, place);
+        if (device_pow) PAMO_COST_MODE(0, true, true);
+        else PAMO_COST_MODE(0, false, true);
         note_launch();
         return;
     }
+#undef PAMO_COST_MODE
     if (legacy) {
         if (device_pow)
             k_edge_cost<true, true, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,

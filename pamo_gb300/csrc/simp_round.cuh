@@ -27,28 +27,31 @@ void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4*
 void launch_copy_tris(const int4* src, int4* dst, int n, cudaStream_t s);
 
 // ---- adjacency ----
-// with fgeo: also the per-face geometry the rings read (three float4 per face, from pos)
+// with fgeo: also the per-face geometry the rings read (from pos; room for four float4 per face): the ring lengths
+// and normal as two float4 per face (fgeo[2f], fgeo[2f + 1]), then the planes after all n faces' records, one float4
+// per face (fgeo[2n + f]) or, with plane_df (precision mode), a double-float pair (fgeo[2n + 2f], fgeo[2n + 2f + 1])
 void launch_face_counts(const int4* tri, const RoundCounters* rc, int n_tris_bound, int* valence, int* ecount,
-                        int* vedges, cudaStream_t s, const float4* pos = nullptr, float4* fgeo = nullptr);
+                        int* vedges, cudaStream_t s, const float4* pos = nullptr, float4* fgeo = nullptr,
+                        bool plane_df = false);
 void launch_fill_adjacency(const int4* tri, const RoundCounters* rc, int n_tris_bound, const int* nt_off, int* cursor,
                            int* nt, const int* edge_off, int2* edges, const int* voff, int* vcursor, int* eorder,
                            cudaStream_t s);
 void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* nt_off, int* nt, cudaStream_t s);
 
 // ---- cost, selection, collapse ----
-// comp: precision mode, the quadric sums compensated
+// qlo (precision mode; needs the plane_df planes): each quadric as a double-float sum, hi parts to q, lo to qlo
 void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
-                     const float4* fgeo, Quadric* q, int* nxt, cudaStream_t s, bool comp = false);
+                     const float4* fgeo, Quadric* q, int* nxt, cudaStream_t s, Quadric* qlo = nullptr);
 void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s);
-// mode: 0 the reference's arithmetic; precision mode 1 (compensated sums) or 2 (compensated, placement at the
-// quadric's minimiser, written to place[e]). raw (optional): each edge's cost before clamp and quantisation (NaN where
+// mode: 0 the reference's arithmetic; precision mode 1 (double-float quadrics q + qlo, compensated sums) or 2 (as 1,
+// placement at the quadric's minimiser, written to place[e]). raw (optional): each edge's cost before clamp and quantisation (NaN where
 // none is computed); place (optional, required by mode 2): each edge's placement.
 void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
                       const int* nt, const int4* tri, const float4* pos, const Quadric* q, const float4* fgeo,
                       const int* nxt, const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin,
                       const float* d_scale, float tres, int is_stuck, cudaStream_t s, const int* is_stuck_dev = nullptr,
                       bool legacy = false, bool device_pow = false, int mode = 0, float* raw = nullptr,
-                      float4* place = nullptr);
+                      float4* place = nullptr, const Quadric* qlo = nullptr);
 // The edge cost of many meshes in one vertex numbering: the scale and is_stuck of each edge's mesh (vmesh of its
 // lower vertex) come from mesh_scale and mesh_stuck.
 void launch_edge_cost_batch(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges,
