@@ -239,9 +239,10 @@ int pamo_batch_rounds(const pamo_batch* b, int32_t* rounds, int32_t capacity) {
 namespace {
 
 // Device bytes a job is taken to need while it runs: the working buffers a context allocates for its sizes
-// (face and vertex arrays with the context's growth factor 1.2: about 615 B per face and 195 B per vertex,
-// rounded up to 680 and 330), its input and output copies, and 16 MiB of fixed-size scratch.
-int64_t job_bytes(int64_t nv, int64_t nf) { return 680 * nf + 330 * nv + 2 * (12 * nv + 12 * nf) + (16ll << 20); }
+// (face and vertex arrays with the context's growth factor 1.2: about 700 B per face and 195 B per vertex, with
+// the precision modes' arrays 740 and 255, rounded up to 780 and 330), its input and output copies, and 16 MiB of
+// fixed-size scratch.
+int64_t job_bytes(int64_t nv, int64_t nf) { return 780 * nf + 330 * nv + 2 * (12 * nv + 12 * nf) + (16ll << 20); }
 
 // What stage 3 adds while it runs: the input as the float64 projection target and the stage-3 handle's buffers over
 // it (its LBVH and per-face records, about 240 B per target face), plus 64 MiB for the small projected mesh.

@@ -520,6 +520,7 @@ struct pamo_csr {
     Buf<unsigned char> invalid;
     Buf<int4> tri, orig_tri, tri_in, tri_next, res_tri, tri_load;
     Buf<int> ecount, qflag, qlist, fflags, nt, nxt, fmesh, shuffle_flags;
+    Buf<int2> spc;
     Buf<float4> fgeo;
     Buf<float> face_mean;
     Buf<unsigned long long> fkey;
@@ -607,7 +608,7 @@ struct pamo_csr {
         release(occ); release(valence); release(cursor); release(vedges); release(vcursor); release(vmesh);
         release(vscan); release(quad); release(vmin); release(invalid); release(tri); release(orig_tri);
         release(tri_in); release(tri_next); release(res_tri); release(tri_load); release(ecount); release(qflag);
-        release(qlist); release(fflags); release(nt); release(nxt); release(fmesh); release(shuffle_flags);
+        release(qlist); release(fflags); release(nt); release(nxt); release(spc); release(fmesh); release(shuffle_flags);
         release(fgeo); release(face_mean); release(fkey); release(hit); release(edges); release(exact_list);
         release(eorder); release(win); release(winners); release(lines); release(considered); release(uflag);
         release(cost); release(map_reg); release(undo_list_reg); release(tmp_undo_reg); release(undo_in_reg);
@@ -637,8 +638,8 @@ struct pamo_csr {
         if ((r = grow(tri, fc)) || (r = grow(orig_tri, fc)) || (r = grow(tri_in, fc)) || (r = grow(tri_next, fc)) ||
             (r = grow(res_tri, fc)) || (r = grow(tri_load, fc)) || (r = grow(ecount, fc + 1)) ||
             (r = grow(qflag, fc + 1)) || (r = grow(qlist, fc)) || (r = grow(fflags, fc + 1)) || (r = grow(nt, 3 * fc)) ||
-            (r = grow(nxt, 3 * fc)) || (r = grow(fmesh, fc)) || (r = grow(shuffle_flags, 2 * fc + 40)) ||
-            (r = grow(fgeo, 4 * fc)) || (r = grow(face_mean, 3 * fc)) || (r = grow(fkey, fc)) || (r = grow(hit, fc + 1)))
+            (r = grow(nxt, 3 * fc)) || (r = grow(spc, 3 * fc)) || (r = grow(fmesh, fc)) || (r = grow(shuffle_flags, 2 * fc + 40)) ||
+            (r = grow(fgeo, 6 * fc)) || (r = grow(face_mean, 3 * fc)) || (r = grow(fkey, fc)) || (r = grow(hit, fc + 1)))
             return r;
         if ((r = grow(edges, ec)) || (r = grow(eorder, ec)) || (r = grow(win, ec + 1)) || (r = grow(winners, ec)) ||
             (r = grow(lines, ec)) || (r = grow(considered, ec)) || (r = grow(uflag, ec + 1)) || (r = grow(cost, ec)) ||
@@ -724,13 +725,13 @@ struct pamo_csr {
                               eorder.p, s);
         launch_sort_adjacency(rc, Vb, valence.p, nt.p, s);
         const int* nt_off = valence.p;
-        launch_quadrics(rc, Vb, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s);
+        launch_quadrics(rc, Vb, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, spc.p, s);
         // cost with each mesh's stale costs and invalid table, then the costs back to the meshes' regions
         kb_slot_edges<<<gM, kT, 0, s>>>(ctl, slot_mesh.p, mesh.p, ecount.p, rc); note_launch();
         kb_gather<<<grid_for(std::max(Eb, Vb), kT), kT, 0, s>>>(rc, slot_mesh.p, mesh.p, vmesh.p, edges.p, ecost_reg.p,
                                                                invalid_reg.p, cost.p, invalid.p); note_launch();
         launch_fill_u64_dev(rc, Vb, vmin.p, ~0ull, s);
-        launch_edge_cost_batch(rc, Eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p,
+        launch_edge_cost_batch(rc, Eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, spc.p, invalid.p,
                                cost.p, vmin.p, slot_scale.p, slot_stuck.p, vmesh.p, threshold, s, skinny_pow);
         kb_scatter_costs<<<grid_for(Eb, kT), kT, 0, s>>>(rc, slot_mesh.p, mesh.p, vmesh.p, edges.p, cost.p, ecost_reg.p);
         note_launch();

@@ -116,7 +116,8 @@ struct pamo_ctx {
     DevBuf<int4> tri, orig_tri, tri_in, tri_out;
     DevBuf<int> ecount, qflag, qlist, fflags, nt, shuffle_flags;
     DevBuf<int> nxt;        // per CSR slot: the vertex after the ring's vertex in the slot's face
-    DevBuf<float4> fgeo;    // per face: edge lengths and normal (two float4), then the planes (room for four per face)
+    DevBuf<int2> spc;       // per CSR slot: the vertex before it and its corner
+    DevBuf<float4> fgeo;    // per face: a 64-byte ring record, then the planes (room for six float4 per face)
     DevBuf<unsigned long long> fkey;
     DevBuf<unsigned char> hit;
     BvhBuffers bvh;
@@ -286,7 +287,7 @@ struct pamo_ctx {
         };
         fr(edge_cost); fr(invalid); fr(pts_map); fr(pts_map_prev); fr(undo_list); fr(tmp_undo);
         fr(pos); fr(orig_pos); fr(pos_in); fr(pos_out); fr(occ); fr(valence); fr(cursor); fr(quad); fr(quad_lo); fr(vmin); fr(undo_in);
-        fr(nxt); fr(fgeo); fr(tri); fr(orig_tri); fr(tri_in); fr(tri_out); fr(ecount); fr(qflag); fr(qlist); fr(fflags); fr(nt);
+        fr(nxt); fr(spc); fr(fgeo); fr(tri); fr(orig_tri); fr(tri_in); fr(tri_out); fr(ecount); fr(qflag); fr(qlist); fr(fflags); fr(nt);
         fr(shuffle_flags); fr(fkey); fr(eorder); fr(vedges); fr(vcursor); fr(hit); fr(edges); fr(win); fr(collapsed); fr(uflag); fr(face_mean); fr(exact_list); fr(place); fr(probe_raw);
         if (bvh_mem) cudaFree(bvh_mem);
         bvh_mem = nullptr;
@@ -358,7 +359,7 @@ struct pamo_ctx {
         b += pos.bytes() + orig_pos.bytes() + pos_in.bytes() + pos_out.bytes() + occ.bytes() + valence.bytes() +
              cursor.bytes() + vedges.bytes() + vcursor.bytes() + quad.bytes() + quad_lo.bytes() + vmin.bytes() +
              undo_in.bytes();
-        b += nxt.bytes() + fgeo.bytes();
+        b += nxt.bytes() + spc.bytes() + fgeo.bytes();
         b += tri.bytes() + orig_tri.bytes() + tri_in.bytes() + tri_out.bytes() + ecount.bytes() + qflag.bytes() +
              qlist.bytes() + fflags.bytes() + nt.bytes() + shuffle_flags.bytes() + fkey.bytes() + hit.bytes() +
              edges.bytes() + win.bytes() + collapsed.bytes() + uflag.bytes() + eorder.bytes() + exact_list.bytes() +
@@ -390,7 +391,7 @@ struct pamo_ctx {
         int r;
         if ((r = grow(tri, nc)) || (r = grow(orig_tri, nc)) || (r = grow(tri_in, nc)) || (r = grow(tri_out, nc)) ||
             (r = grow(ecount, nc + 1)) || (r = grow(qflag, nc + 1)) || (r = grow(qlist, nc)) || (r = grow(fflags, nc + 1)) ||
-            (r = grow(nt, 3 * nc)) || (r = grow(nxt, 3 * nc)) || (r = grow(fgeo, 4 * nc)) || (r = grow(shuffle_flags, 2 * nc + 40)) || (r = grow(fkey, nc)) || (r = grow(hit, nc)) ||
+            (r = grow(nt, 3 * nc)) || (r = grow(nxt, 3 * nc)) || (r = grow(spc, 3 * nc)) || (r = grow(fgeo, 6 * nc)) || (r = grow(shuffle_flags, 2 * nc + 40)) || (r = grow(fkey, nc)) || (r = grow(hit, nc)) ||
             (r = grow(eorder, 2 * nc)) ||
             (r = grow(edges, 2 * nc)) || (r = grow(win, 2 * nc + 1)) || (r = grow(collapsed, 2 * nc)) ||
             (r = grow(uflag, 2 * nc + 1)) || (r = grow(face_mean, 3 * nc)) ||
@@ -444,10 +445,10 @@ struct pamo_ctx {
         launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
         const int* nt_off = valence.p;
         const int eb = 2 * nT;
-        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s);
+        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, spc.p, s);
         launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
         cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
-        launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p, vmin.p,
+        launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, spc.p, invalid.p, edge_cost.p, vmin.p,
                          d_scale, threshold, 0, s, nullptr, true, skinny_pow);
         launch_face_keys(rc, nT, tri.p, vmin.p, fkey.p, s);
         launch_collapse(rc, eb, eorder.p, edges.p, edge_cost.p, collapse_t, fkey.p, nt_off, nt.p, tri.p, orig_tri.p, pos.p,
@@ -488,10 +489,10 @@ struct pamo_ctx {
         launch_fill_adjacency(tri.p, rc, nT, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p, eorder.p, s);
         launch_sort_adjacency(rc, nP, valence.p, nt.p, s);
         Quadric* qlo = mode > 0 ? quad_lo.p : nullptr;
-        launch_quadrics(rc, nP, valence.p, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s, qlo);
+        launch_quadrics(rc, nP, valence.p, nt.p, tri.p, fgeo.p, quad.p, nxt.p, spc.p, s, qlo);
         cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
         cudaMemsetAsync(probe_raw.p, 0xFF, probe_raw.n * sizeof(float), s);  // NaN where no cost is computed
-        launch_edge_cost(rc, 2 * nT, eorder.p, edges.p, valence.p, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p,
+        launch_edge_cost(rc, 2 * nT, eorder.p, edges.p, valence.p, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, spc.p, invalid.p,
                          edge_cost.p, vmin.p, d_scale, threshold, 0, s, nullptr, false, skinny_pow, mode, probe_raw.p,
                          place.p, qlo);
         precision = keep;
@@ -533,11 +534,11 @@ struct pamo_ctx {
             launch_fill_adjacency(tri.p, rc, nTb, valence.p, cursor.p, nt.p, ecount.p, edges.p, vedges.p, vcursor.p,
                                   eorder.p, s);
             launch_sort_adjacency(rc, nPb, valence.p, nt.p, s);
-            launch_quadrics(rc, nPb, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s, qlo_ptr());
+            launch_quadrics(rc, nPb, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, spc.p, s, qlo_ptr());
             launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
             launch_fill_u64_dev(rc, nPb, vmin.p, ~0ull, s);
             cost_begin(s);
-            launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p,
+            launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, spc.p, invalid.p, edge_cost.p,
                              vmin.p, d_scale, threshold, 0, s, &d_ls->is_stuck, false, skinny_pow, precision, nullptr,
                              place_ptr(), qlo_ptr());
             cost_end(s);
@@ -708,13 +709,13 @@ struct pamo_ctx {
 
         // cost and selection
         prof.begin(kPhQuad, s);
-        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, s, qlo_ptr());
+        launch_quadrics(rc, nP, nt_off, nt.p, tri.p, fgeo.p, quad.p, nxt.p, spc.p, s, qlo_ptr());
         prof.end(kPhQuad, s);
         launch_edge_cost_capacity(rc, d_ecap, edge_cost.p, (int)edge_cost.n, s);
         cudaMemsetAsync(vmin.p, 0xFF, (nP + 1) * sizeof(unsigned long long), s);
         prof.begin(kPhCost, s);
         cost_begin(s);
-        launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, invalid.p, edge_cost.p, vmin.p,
+        launch_edge_cost(rc, eb, eorder.p, edges.p, nt_off, nt.p, tri.p, pos.p, quad.p, fgeo.p, nxt.p, spc.p, invalid.p, edge_cost.p, vmin.p,
                          d_scale, threshold, is_stuck, s, nullptr, false, skinny_pow, precision, nullptr, place_ptr(),
                          qlo_ptr());
         cost_end(s);

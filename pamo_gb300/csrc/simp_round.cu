@@ -105,14 +105,16 @@ __global__ void k_shuffle_gather(Feistel fb, const int* __restrict__ scan, const
 
 // ------------------------------------------------------------------ adjacency
 // Per-face values that the vertex rings read many times (every face lies in three rings and every ring is
-// read once per incident edge), each computed by the same operations as where the reference computes it:
-//   fgeo[2f]      = |p_x - p_y|, |p_y - p_z|, |p_z - p_x| and, as int bits, which of t.x > t.y, t.y > t.z,
-//                   t.z > t.x hold (the ring edge-length terms, :449-484);
-//   fgeo[2f + 1]  = the unnormalised normal cross(p_y - p_x, p_z - p_x) and its L1 norm (the flip test);
-//   fgeo[2n + f]  = the face plane of tri2plane (:337-346), n = the round's face count (precision mode: the plane
-//                   as a double-float pair, fgeo[2n + 2f] and fgeo[2n + 2f + 1]).
-// The two records the edge cost reads for a ring face form one aligned 32-byte sector; the planes, which only the
-// quadrics read, follow all of them. The buffer holds 4 float4 per face.
+// read once per incident edge), each computed by the same operations as where the reference computes it. One
+// aligned 64-byte record per face, fgeo[4f .. 4f + 3]:
+//   (l01, l12, l20, L1)        the edge lengths |p_x - p_y|, |p_y - p_z|, |p_z - p_x| (the ring edge-length
+//                              terms, :449-484) and the L1 norm of the unnormalised normal;
+//   (o.x, o.y, o.z, p_x.x), (p_x.y, p_x.z, p_y.x, p_y.y), (p_y.z, p_z.x, p_z.y, p_z.z)
+//                              the unnormalised normal cross(p_y - p_x, p_z - p_x) (the flip test) and the three
+//                              corner positions, so that a ring face needs no gather of its vertices;
+// then, after all n records (n = the round's face count), the face planes of tri2plane (:337-346), fgeo[4n + f]
+// (precision mode: a double-float pair, fgeo[4n + 2f] and fgeo[4n + 2f + 1]), which only the quadrics read.
+// The buffer holds 6 float4 per face.
 __device__ __forceinline__ void face_plane(const float4* __restrict__ pos, int4 t, float p[4]);
 
 // ---- precision mode: error-free transforms (Knuth's TwoSum; TwoProd with an explicit fused multiply-add, which
@@ -202,7 +204,7 @@ __device__ __forceinline__ void acc_add(CSum& a, float x) { a.add(x); }
 __device__ __forceinline__ float acc_value(float a) { return a; }
 __device__ __forceinline__ float acc_value(const CSum& a) { return a.value(); }
 
-// plane_df (precision mode): the planes as double-float pairs, fgeo[2n + 2f] (hi) and fgeo[2n + 2f + 1] (lo)
+// plane_df (precision mode): the planes as double-float pairs, fgeo[4n + 2f] (hi) and fgeo[4n + 2f + 1] (lo)
 __global__ void __launch_bounds__(kT) k_face_counts(const int4* __restrict__ tri, const RoundCounters* rc, int* valence,
                                                     int* ecount, int* vedges, const float4* __restrict__ pos,
                                                     float4* fgeo, int plane_df) {
@@ -215,20 +217,22 @@ __global__ void __launch_bounds__(kT) k_face_counts(const int4* __restrict__ tri
         }
         if (fgeo) {
             const V3 o0 = v3(pos[t.x]), o1 = v3(pos[t.y]), o2 = v3(pos[t.z]);
-            const int mask = (t.x > t.y ? 1 : 0) | (t.y > t.z ? 2 : 0) | (t.z > t.x ? 4 : 0);
-            fgeo[2 * (size_t)f] = make_float4(vnorm(vsub(o0, o1)), vnorm(vsub(o1, o2)), vnorm(vsub(o2, o0)),
-                                              __int_as_float(mask));
             const V3 ou = vcross(vsub(o1, o0), vsub(o2, o0));
-            fgeo[2 * (size_t)f + 1] = make_float4(ou.x, ou.y, ou.z, fabsf(ou.x) + fabsf(ou.y) + fabsf(ou.z));
+            float4* r = fgeo + 4 * (size_t)f;
+            r[0] = make_float4(vnorm(vsub(o0, o1)), vnorm(vsub(o1, o2)), vnorm(vsub(o2, o0)),
+                               fabsf(ou.x) + fabsf(ou.y) + fabsf(ou.z));
+            r[1] = make_float4(ou.x, ou.y, ou.z, o0.x);
+            r[2] = make_float4(o0.y, o0.z, o1.x, o1.y);
+            r[3] = make_float4(o1.z, o2.x, o2.y, o2.z);
             if (plane_df) {
                 DF pd[4];
                 face_plane_df(pos, t, pd);
-                fgeo[2 * (size_t)n + 2 * (size_t)f] = make_float4(pd[0].hi, pd[1].hi, pd[2].hi, pd[3].hi);
-                fgeo[2 * (size_t)n + 2 * (size_t)f + 1] = make_float4(pd[0].lo, pd[1].lo, pd[2].lo, pd[3].lo);
+                fgeo[4 * (size_t)n + 2 * (size_t)f] = make_float4(pd[0].hi, pd[1].hi, pd[2].hi, pd[3].hi);
+                fgeo[4 * (size_t)n + 2 * (size_t)f + 1] = make_float4(pd[0].lo, pd[1].lo, pd[2].lo, pd[3].lo);
             } else {
                 float pl[4];
                 face_plane(pos, t, pl);
-                fgeo[2 * (size_t)n + f] = make_float4(pl[0], pl[1], pl[2], pl[3]);
+                fgeo[4 * (size_t)n + f] = make_float4(pl[0], pl[1], pl[2], pl[3]);
             }
         }
         atomicAdd(&valence[t.x], 1);
@@ -297,25 +301,27 @@ __device__ __forceinline__ void face_plane(const float4* __restrict__ pos, int4 
     p[3] = -vdot(n, v0);
 }
 
-__device__ __forceinline__ int next_after(int4 t, int v);
-
-// Quadrics from the face planes of fgeo; also nxt[s] = the vertex after v in ring face s (the link condition's
-// per-slot value).
+// Quadrics from the face planes of fgeo; also, per ring slot s of v (face t = tri[nt[s]]), nxt[s] = the vertex
+// after v in t (the link condition's per-slot value) and spc[s] = (the vertex before v, the corner c of v: the
+// first of t.x, t.y, t.z equal to v), from which the ring passes rebuild t without reading it.
 // kComp (precision mode): every entry summed with compensation (products by TwoProd, sums by TwoSum), rounded once
 template <bool kComp>
 __global__ void __launch_bounds__(kT) k_quadrics(const RoundCounters* rc, const int* __restrict__ nt_off,
                                                  const int* __restrict__ nt, const int4* __restrict__ tri,
                                                  const float4* __restrict__ fgeo, Quadric* q, int* nxt,
-                                                 Quadric* qlo) {
+                                                 int2* spc, Quadric* qlo) {
     const int n = rc->n_pts;
-    const size_t planes = 2 * (size_t)rc->n_tris;
+    const size_t planes = 4 * (size_t)rc->n_tris;
     for (int v = gtid(); v < n; v += gstride()) {
         float m00 = 0.f, m01 = 0.f, m02 = 0.f, m03 = 0.f, m11 = 0.f, m12 = 0.f, m13 = 0.f, m22 = 0.f, m23 = 0.f, m33 = 0.f;
         CSum c[10];
         const int b = nt_off[v + 1];
         for (int s = nt_off[v]; s < b; ++s) {
             const int f = nt[s];
-            nxt[s] = next_after(tri[f], v);
+            const int4 t = tri[f];
+            const int corner = t.x == v ? 0 : (t.y == v ? 1 : 2);
+            nxt[s] = corner == 0 ? t.y : (corner == 1 ? t.z : t.x);
+            spc[s] = make_int2(corner == 0 ? t.z : (corner == 1 ? t.x : t.y), corner);
             if constexpr (kComp) {  // double-float planes (face_plane_df), double-float products and sums
                 const float4 ph = fgeo[planes + 2 * (size_t)f], pl = fgeo[planes + 2 * (size_t)f + 1];
                 const DF d[4] = {{ph.x, pl.x}, {ph.y, pl.y}, {ph.z, pl.z}, {ph.w, pl.w}};
@@ -360,31 +366,7 @@ __global__ void __launch_bounds__(kT) k_quadrics(const RoundCounters* rc, const 
 }
 
 // ------------------------------------------------------------------ edge cost (compute_edge_cost_kernel, :382-585)
-__device__ __forceinline__ int next_after(int4 t, int v) {
-    if (t.x == v) return t.y;
-    if (t.y == v) return t.z;
-    if (t.z == v) return t.x;
-    return -1;
-}
 
-
-template <class Acc>
-__device__ __forceinline__ void ring_len(int w, const int* __restrict__ nt_off, const int* __restrict__ nt,
-                                         const float4* __restrict__ fgeo, Acc& len, int& cnt) {
-    const int b = nt_off[w + 1];
-    for (int s = nt_off[w]; s < b; ++s) {
-        const float4 g = fgeo[2 * (size_t)nt[s]];
-        const int mask = __float_as_int(g.w);
-        if (mask & 1) { acc_add(len, g.x); cnt++; }
-        if (mask & 2) { acc_add(len, g.y); cnt++; }
-        if (mask & 4) { acc_add(len, g.z); cnt++; }
-    }
-}
-
-// normal-flip test and skinny term over the ring of w with w moved to vm (faces holding `other` skipped).
-// The flip test dot(n_old/|n_old|, n_new/|n_new|) < 0 takes its sign from the unnormalised normals when a
-// float bound proves it (|dot| > 1e-5 |n_old|_1 |n_new|_1, far above the ~1e-6 relative rounding of the
-// normalised form); otherwise the normalised form is evaluated exactly as the reference does.
 // The squared lengths of the skinny term: the reference squares with the device's pow(float, int)
 // (cusimp_free.cu:533,573, cusimp.cu:423,463), which on the GPU differs from x * x by one ulp for a few floats in
 // a million and costs far more; kPow = false squares by multiplication (the oracle's form).
@@ -422,24 +404,43 @@ __device__ __forceinline__ float skinny_term(float k4s3, float area, float l01, 
     return 1.0f - rclamp(e, 0.0f, 1.0f);
 }
 
+// One pass over the ring of w (slots in face-index order) for both ring sums of the edge (w, other):
+// * the edge-length term (:449-484): every ring face adds the lengths of its edges whose first vertex is the larger
+//   (t.x > t.y, t.y > t.z, t.z > t.x), to len and their count to cnt;
+// * the flip test and the skinny term with w moved to vm, over the ring faces without `other`: false as soon as a
+//   face's normal flips (the edge is invalid), else each face adds its skinny term to qa and 1 to ntri.
+// Called for the ring of u, then of v, each sum runs in the order of the two separate loops of the reference. The face
+// t is rebuilt from w, nxt[s] and spc[s], and its corners come from the face record, so a slot costs two aligned
+// 32-byte sectors of the record and contiguous per-slot words.
+// The flip test dot(n_old/|n_old|, n_new/|n_new|) < 0 takes its sign from the unnormalised normals when a
+// float bound proves it (|dot| > 1e-5 |n_old|_1 |n_new|_1, far above the ~1e-6 relative rounding of the
+// normalised form); otherwise the normalised form is evaluated exactly as the reference does.
 template <bool kLegacy, bool kPow, class Acc>
-__device__ __forceinline__ bool ring_skinny(int w, int other, V3 vm, const int* __restrict__ nt_off,
-                                            const int* __restrict__ nt, const int4* __restrict__ tri,
-                                            const float4* __restrict__ pos, const float4* __restrict__ fgeo, Acc& qa,
-                                            int& ntri) {
+__device__ __forceinline__ bool ring_pass(int w, int other, V3 vm, const int* __restrict__ nt_off,
+                                          const int* __restrict__ nt, const int* __restrict__ nxt,
+                                          const int2* __restrict__ spc, const float4* __restrict__ fgeo, Acc& len,
+                                          int& cnt, Acc& qa, int& ntri) {
     const float k4s3 = 4.0f * sqrtf(3.0f);
     const int b = nt_off[w + 1];
     for (int s = nt_off[w]; s < b; ++s) {
-        const int f = nt[s];
-        const int4 t = tri[f];
+        const float4* r = fgeo + 4 * (size_t)nt[s];
+        const int nx = nxt[s];
+        const int2 pc = spc[s];
+        const int4 t = pc.y == 0 ? make_int4(w, nx, pc.x, 0) : (pc.y == 1 ? make_int4(pc.x, w, nx, 0)
+                                                                          : make_int4(nx, pc.x, w, 0));
+        const float4 g = r[0];
+        if (t.x > t.y) { acc_add(len, g.x); cnt++; }
+        if (t.y > t.z) { acc_add(len, g.y); cnt++; }
+        if (t.z > t.x) { acc_add(len, g.z); cnt++; }
         if (t.x == other || t.y == other || t.z == other) continue;
+        const float4 r1 = r[1], r2 = r[2], r3 = r[3];
         const bool wx = t.x == w, wy = t.y == w, wz = t.z == w;
-        const V3 n0 = wx ? vm : v3(pos[t.x]), n1 = wy ? vm : v3(pos[t.y]), n2 = wz ? vm : v3(pos[t.z]);
-        const float4 og = fgeo[2 * (size_t)f + 1];
-        const V3 ou = {og.x, og.y, og.z};
+        const V3 n0 = wx ? vm : V3{r1.w, r2.x, r2.y}, n1 = wy ? vm : V3{r2.z, r2.w, r3.x},
+                 n2 = wz ? vm : V3{r3.y, r3.z, r3.w};
+        const V3 ou = {r1.x, r1.y, r1.z};
         const V3 nu = vcross(vsub(n1, n0), vsub(n2, n0));
         const float du = vdot(ou, nu);
-        const float bound = 1e-5f * og.w * (fabsf(nu.x) + fabsf(nu.y) + fabsf(nu.z));
+        const float bound = 1e-5f * g.w * (fabsf(nu.x) + fabsf(nu.y) + fabsf(nu.z));
         if (du < -bound) return false;
         if (!(du > bound)) {
             const V3 on = vdiv(ou, vnorm(ou));
@@ -447,10 +448,9 @@ __device__ __forceinline__ bool ring_skinny(int w, int other, V3 vm, const int* 
             if (vdot(on, nn) < 0) return false;
         }
         // an edge without w keeps its length (same operations as the per-face value)
-        const float4 lg = fgeo[2 * (size_t)f];
-        const float l01 = (wx || wy) ? vnorm(vsub(n0, n1)) : lg.x;
-        const float l12 = (wy || wz) ? vnorm(vsub(n1, n2)) : lg.y;
-        const float l20 = (wz || wx) ? vnorm(vsub(n2, n0)) : lg.z;
+        const float l01 = (wx || wy) ? vnorm(vsub(n0, n1)) : g.x;
+        const float l12 = (wy || wz) ? vnorm(vsub(n1, n2)) : g.y;
+        const float l20 = (wz || wx) ? vnorm(vsub(n2, n0)) : g.z;
         const float sh = (l01 + l12 + l20) / 2;  // triangle_area (Heron), :368-375
         const float area = sqrtf(sh * (sh - l01) * (sh - l12) * (sh - l20));
         acc_add(qa, skinny_term<kLegacy, kPow>(k4s3, area, l01, l12, l20));
@@ -499,6 +499,32 @@ __device__ __forceinline__ int qem_optimum(const float* m, const float* lo, V3 m
     return 0;
 }
 
+// The edge's quadric Q_u + Q_v: in float (mode 0), or as hi + lo by two-sum with the quadrics' own lo parts added
+// (precision modes)
+template <int kMode>
+__device__ __forceinline__ void edge_quadric(int u, int v, const Quadric* __restrict__ q,
+                                             const Quadric* __restrict__ qlo, float m[10], float mlo[10]) {
+    const Quadric Qu = q[u], Qv = q[v];
+    const float qu[10] = {Qu.a.x, Qu.a.y, Qu.a.z, Qu.a.w, Qu.b.x, Qu.b.y, Qu.b.z, Qu.b.w, Qu.c.x, Qu.c.y};
+    const float qv[10] = {Qv.a.x, Qv.a.y, Qv.a.z, Qv.a.w, Qv.b.x, Qv.b.y, Qv.b.z, Qv.b.w, Qv.c.x, Qv.c.y};
+#pragma unroll
+    for (int i = 0; i < 10; ++i) {
+        if constexpr (kMode == 0) {
+            m[i] = qu[i] + qv[i];
+            mlo[i] = 0.0f;
+        } else {
+            two_sum(qu[i], qv[i], m[i], mlo[i]);
+        }
+    }
+    if constexpr (kMode != 0) {
+        const Quadric Lu = qlo[u], Lv = qlo[v];
+        const float lu[10] = {Lu.a.x, Lu.a.y, Lu.a.z, Lu.a.w, Lu.b.x, Lu.b.y, Lu.b.z, Lu.b.w, Lu.c.x, Lu.c.y};
+        const float lv[10] = {Lv.a.x, Lv.a.y, Lv.a.z, Lv.a.w, Lv.b.x, Lv.b.y, Lv.b.z, Lv.b.w, Lv.c.x, Lv.c.y};
+#pragma unroll
+        for (int i = 0; i < 10; ++i) mlo[i] += lu[i] + lv[i];
+    }
+}
+
 // returns false when the reference leaves the stale cost in place. kLegacy: the cost of CUSimp
 // (cusimp.cu:270-471): the mean ring length is counted twice (`edge_len += edge_len + |e|`) and the skinny term
 // has no penalty factor. kMode (precision mode, not the reference's arithmetic): 0 the reference's float order;
@@ -509,8 +535,9 @@ template <bool kLegacy, bool kPow, int kMode>
 __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restrict__ nt_off, const int* __restrict__ nt,
                                                 const int4* __restrict__ tri, const float4* __restrict__ pos,
                                                 const Quadric* __restrict__ q, const float4* __restrict__ fgeo,
-                                                const int* __restrict__ nxt, float scale, float tres, uint32_t& out,
-                                                float& raw, V3& place, const Quadric* __restrict__ qlo) {
+                                                const int* __restrict__ nxt, const int2* __restrict__ spc, float scale,
+                                                float tres, uint32_t& out, float& raw, V3& place,
+                                                const Quadric* __restrict__ qlo) {
     raw = __int_as_float(0x7fc00000);  // NaN: no finite cost (invalid)
     // link condition
     int dup = 0;
@@ -528,45 +555,26 @@ __device__ __forceinline__ bool edge_cost_value(int u, int v, const int* __restr
     }
     if (dup != 2) return false;
     typedef typename std::conditional<kMode == 0, float, CSum>::type Acc;
-    Acc lacc{};
-    int cnt = 0;
-    ring_len(u, nt_off, nt, fgeo, lacc, cnt);
-    ring_len(v, nt_off, nt, fgeo, lacc, cnt);
-    float len = acc_value(lacc);
     const V3 v0 = v3(pos[u]), v1 = v3(pos[v]);
-    len = len / (float)cnt / scale * tres;
-    if (kLegacy) len = len + (len + vnorm(vsub(v0, v1)) / scale * tres);
-    else len = len + vnorm(vsub(v0, v1)) / scale * tres;
-    const Quadric Qu = q[u], Qv = q[v];
-    const float qu[10] = {Qu.a.x, Qu.a.y, Qu.a.z, Qu.a.w, Qu.b.x, Qu.b.y, Qu.b.z, Qu.b.w, Qu.c.x, Qu.c.y};
-    const float qv[10] = {Qv.a.x, Qv.a.y, Qv.a.z, Qv.a.w, Qv.b.x, Qv.b.y, Qv.b.z, Qv.b.w, Qv.c.x, Qv.c.y};
     float m[10], mlo[10];
-#pragma unroll
-    for (int i = 0; i < 10; ++i) {
-        if constexpr (kMode == 0) {
-            m[i] = qu[i] + qv[i];
-            mlo[i] = 0.0f;
-        } else {
-            two_sum(qu[i], qv[i], m[i], mlo[i]);
-        }
-    }
-    if constexpr (kMode != 0) {  // the quadrics' lo parts (k_quadrics<true>)
-        const Quadric Lu = qlo[u], Lv = qlo[v];
-        const float lu[10] = {Lu.a.x, Lu.a.y, Lu.a.z, Lu.a.w, Lu.b.x, Lu.b.y, Lu.b.z, Lu.b.w, Lu.c.x, Lu.c.y};
-        const float lv[10] = {Lv.a.x, Lv.a.y, Lv.a.z, Lv.a.w, Lv.b.x, Lv.b.y, Lv.b.z, Lv.b.w, Lv.c.x, Lv.c.y};
-#pragma unroll
-        for (int i = 0; i < 10; ++i) mlo[i] += lu[i] + lv[i];
-    }
     V3 vm = vdiv(vadd(v0, v1), 2.0f);
-    if constexpr (kMode == 2) qem_optimum(m, mlo, vm, vm);
+    if constexpr (kMode == 2) {
+        edge_quadric<kMode>(u, v, q, qlo, m, mlo);
+        qem_optimum(m, mlo, vm, vm);
+    }
     place = vm;
-    Acc qacc{};
-    int ntri = 0;
-    if (!ring_skinny<kLegacy, kPow>(u, v, vm, nt_off, nt, tri, pos, fgeo, qacc, ntri) ||
-        !ring_skinny<kLegacy, kPow>(v, u, vm, nt_off, nt, tri, pos, fgeo, qacc, ntri)) {
+    Acc lacc{}, qacc{};
+    int cnt = 0, ntri = 0;
+    if (!ring_pass<kLegacy, kPow>(u, v, vm, nt_off, nt, nxt, spc, fgeo, lacc, cnt, qacc, ntri) ||
+        !ring_pass<kLegacy, kPow>(v, u, vm, nt_off, nt, nxt, spc, fgeo, lacc, cnt, qacc, ntri)) {
         out = 0xFFFFFFFFu;
         return true;
     }
+    float len = acc_value(lacc);
+    len = len / (float)cnt / scale * tres;
+    if (kLegacy) len = len + (len + vnorm(vsub(v0, v1)) / scale * tres);
+    else len = len + vnorm(vsub(v0, v1)) / scale * tres;
+    edge_quadric<kMode>(u, v, q, qlo, m, mlo);  // after the ring passes: not live across them
     float qa = acc_value(qacc);
     if (!kLegacy) qa = 5.0f * qa;  // SKINNY_TRIANGLE_PENALTY
     const float x = vm.x, y = vm.y, z = vm.z, w = 1.0f;
@@ -623,7 +631,8 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
                                                   const int* __restrict__ nt_off, const int* __restrict__ nt,
                                                   const int4* __restrict__ tri, const float4* __restrict__ pos,
                                                   const Quadric* __restrict__ q, const float4* __restrict__ fgeo,
-                                                  const int* __restrict__ nxt, const unsigned char* __restrict__ invalid,
+                                                  const int* __restrict__ nxt, const int2* __restrict__ spc,
+                                                  const unsigned char* __restrict__ invalid,
                                                   uint32_t* cost, unsigned long long* vmin, const float* d_scale,
                                                   float tres, int is_stuck_host, const int* is_stuck_dev,
                                                   const int* __restrict__ vmesh, const int* __restrict__ mesh_stuck,
@@ -655,8 +664,8 @@ __global__ void __launch_bounds__(kT) k_edge_cost(const RoundCounters* rc, const
         } else {
             float raw;
             V3 place;
-            write = edge_cost_value<kLegacy, kPow, kMode>(u, v, nt_off, nt, tri, pos, q, fgeo, nxt, scale, tres, c, raw,
-                                                          place, qlo);
+            write = edge_cost_value<kLegacy, kPow, kMode>(u, v, nt_off, nt, tri, pos, q, fgeo, nxt, spc, scale, tres, c,
+                                                          raw, place, qlo);
             if constexpr (kOut) {
                 if (raw_out) raw_out[e] = write ? raw : __int_as_float(0x7fc00000);
                 if (place_out) place_out[e] = make_float4(place.x, place.y, place.z, 0.f);
@@ -1371,9 +1380,9 @@ void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* 
     k_sort_adjacency<<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt); note_launch();
 }
 void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
-                     const float4* fgeo, Quadric* q, int* nxt, cudaStream_t s, Quadric* qlo) {
-    if (qlo) k_quadrics<true><<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, fgeo, q, nxt, qlo);
-    else k_quadrics<false><<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, fgeo, q, nxt, nullptr);
+                     const float4* fgeo, Quadric* q, int* nxt, int2* spc, cudaStream_t s, Quadric* qlo) {
+    if (qlo) k_quadrics<true><<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, fgeo, q, nxt, spc, qlo);
+    else k_quadrics<false><<<grid_for(n_pts_bound, kT), kT, 0, s>>>(rc, nt_off, nt, tri, fgeo, q, nxt, spc, nullptr);
     note_launch();
 }
 void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s) {
@@ -1382,13 +1391,14 @@ void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cos
 }
 void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
                       const int* nt, const int4* tri, const float4* pos, const Quadric* q, const float4* fgeo,
-                      const int* nxt, const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin,
+                      const int* nxt, const int2* spc, const unsigned char* invalid, uint32_t* cost,
+                      unsigned long long* vmin,
                       const float* d_scale, float tres, int is_stuck, cudaStream_t s, const int* is_stuck_dev, bool legacy,
                       bool device_pow, int mode, float* raw, float4* place, const Quadric* qlo) {
     const int g = grid_for(n_edges_bound, kT);
 #define PAMO_COST_MODE(M, P, O)                                                                                      \
     k_edge_cost<false, P, false, M, O><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt,       \
-                                                        invalid, cost, vmin, d_scale, tres, is_stuck, is_stuck_dev,  \
+                                                        spc, invalid, cost, vmin, d_scale, tres, is_stuck, is_stuck_dev,  \
                                                         nullptr, nullptr, raw, place, qlo)
     if (!legacy && mode == 1) {
         if (raw || place) {
@@ -1416,17 +1426,17 @@ void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eor
 #undef PAMO_COST_MODE
     if (legacy) {
         if (device_pow)
-            k_edge_cost<true, true, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
+            k_edge_cost<true, true, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, spc, invalid,
                                                             cost, vmin, d_scale, tres, 0, nullptr, nullptr, nullptr);
         else
-            k_edge_cost<true, false, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
+            k_edge_cost<true, false, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, spc, invalid,
                                                              cost, vmin, d_scale, tres, 0, nullptr, nullptr, nullptr);
     } else if (device_pow) {
-        k_edge_cost<false, true, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
+        k_edge_cost<false, true, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, spc, invalid,
                                                          cost, vmin, d_scale, tres, is_stuck, is_stuck_dev, nullptr,
                                                          nullptr);
     } else {
-        k_edge_cost<false, false, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
+        k_edge_cost<false, false, false><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, spc, invalid,
                                                           cost, vmin, d_scale, tres, is_stuck, is_stuck_dev, nullptr,
                                                           nullptr);
     }
@@ -1434,15 +1444,16 @@ void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eor
 }
 void launch_edge_cost_batch(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges,
                             const int* nt_off, const int* nt, const int4* tri, const float4* pos, const Quadric* q,
-                            const float4* fgeo, const int* nxt, const unsigned char* invalid, uint32_t* cost,
+                            const float4* fgeo, const int* nxt, const int2* spc, const unsigned char* invalid,
+                            uint32_t* cost,
                             unsigned long long* vmin, const float* mesh_scale, const int* mesh_stuck, const int* vmesh,
                             float tres, cudaStream_t s, bool device_pow) {
     const int g = grid_for(n_edges_bound, kT);
     if (device_pow)
-        k_edge_cost<false, true, true><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
+        k_edge_cost<false, true, true><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, spc, invalid,
                                                         cost, vmin, mesh_scale, tres, 0, nullptr, vmesh, mesh_stuck);
     else
-        k_edge_cost<false, false, true><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, invalid,
+        k_edge_cost<false, false, true><<<g, kT, 0, s>>>(rc, eorder, edges, nt_off, nt, tri, pos, q, fgeo, nxt, spc, invalid,
                                                          cost, vmin, mesh_scale, tres, 0, nullptr, vmesh, mesh_stuck);
     note_launch();
 }

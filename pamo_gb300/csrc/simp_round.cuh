@@ -27,9 +27,9 @@ void launch_shuffle_tris(const Feistel& fb, int* flags, int* scan_scratch, int4*
 void launch_copy_tris(const int4* src, int4* dst, int n, cudaStream_t s);
 
 // ---- adjacency ----
-// with fgeo: also the per-face geometry the rings read (from pos; room for four float4 per face): the ring lengths
-// and normal as two float4 per face (fgeo[2f], fgeo[2f + 1]), then the planes after all n faces' records, one float4
-// per face (fgeo[2n + f]) or, with plane_df (precision mode), a double-float pair (fgeo[2n + 2f], fgeo[2n + 2f + 1])
+// with fgeo: also the per-face geometry the rings read (from pos; room for six float4 per face): a 64-byte record per
+// face (fgeo[4f .. 4f + 3]: edge lengths, normal, corner positions), then the planes after all n faces' records, one
+// float4 per face (fgeo[4n + f]) or, with plane_df (precision mode), a double-float pair (fgeo[4n + 2f], +1)
 void launch_face_counts(const int4* tri, const RoundCounters* rc, int n_tris_bound, int* valence, int* ecount,
                         int* vedges, cudaStream_t s, const float4* pos = nullptr, float4* fgeo = nullptr,
                         bool plane_df = false);
@@ -40,15 +40,17 @@ void launch_sort_adjacency(const RoundCounters* rc, int n_pts_bound, const int* 
 
 // ---- cost, selection, collapse ----
 // qlo (precision mode; needs the plane_df planes): each quadric as a double-float sum, hi parts to q, lo to qlo
+// nxt, spc: per ring slot, the vertex after the ring's vertex in the slot's face and (the vertex before it, its corner)
 void launch_quadrics(const RoundCounters* rc, int n_pts_bound, const int* nt_off, const int* nt, const int4* tri,
-                     const float4* fgeo, Quadric* q, int* nxt, cudaStream_t s, Quadric* qlo = nullptr);
+                     const float4* fgeo, Quadric* q, int* nxt, int2* spc, cudaStream_t s, Quadric* qlo = nullptr);
 void launch_edge_cost_capacity(RoundCounters* rc, int* d_cap, uint32_t* edge_cost, int phys_len, cudaStream_t s);
 // mode: 0 the reference's arithmetic; precision mode 1 (double-float quadrics q + qlo, compensated sums) or 2 (as 1,
 // placement at the quadric's minimiser, written to place[e]). raw (optional): each edge's cost before clamp and quantisation (NaN where
 // none is computed); place (optional, required by mode 2): each edge's placement.
 void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges, const int* nt_off,
                       const int* nt, const int4* tri, const float4* pos, const Quadric* q, const float4* fgeo,
-                      const int* nxt, const unsigned char* invalid, uint32_t* cost, unsigned long long* vmin,
+                      const int* nxt, const int2* spc, const unsigned char* invalid, uint32_t* cost,
+                      unsigned long long* vmin,
                       const float* d_scale, float tres, int is_stuck, cudaStream_t s, const int* is_stuck_dev = nullptr,
                       bool legacy = false, bool device_pow = false, int mode = 0, float* raw = nullptr,
                       float4* place = nullptr, const Quadric* qlo = nullptr);
@@ -56,7 +58,8 @@ void launch_edge_cost(const RoundCounters* rc, int n_edges_bound, const int* eor
 // lower vertex) come from mesh_scale and mesh_stuck.
 void launch_edge_cost_batch(const RoundCounters* rc, int n_edges_bound, const int* eorder, const int2* edges,
                             const int* nt_off, const int* nt, const int4* tri, const float4* pos, const Quadric* q,
-                            const float4* fgeo, const int* nxt, const unsigned char* invalid, uint32_t* cost,
+                            const float4* fgeo, const int* nxt, const int2* spc, const unsigned char* invalid,
+                            uint32_t* cost,
                             unsigned long long* vmin, const float* mesh_scale, const int* mesh_stuck, const int* vmesh,
                             float tres, cudaStream_t s, bool device_pow = false);
 void launch_face_keys(const RoundCounters* rc, int n_tris_bound, const int4* tri, const unsigned long long* vmin,
