@@ -382,6 +382,11 @@ inline int tile_grid(int n_bound) {
 __device__ __forceinline__ bool decide_pair(int f, int g, const int4* __restrict__ tri, const float4* __restrict__ pos,
                                             float eps, unsigned& exact) {
     const int4 qt = tri[f], gt = tri[g];
+    // two or three shared vertex indices: no intersection in either order (pair_certainly_disjoint), decided
+    // before the positions are loaded (edge-adjacent faces are about a quarter of the candidate pairs)
+    const int shared = (qt.x == gt.x) + (qt.x == gt.y) + (qt.x == gt.z) + (qt.y == gt.x) + (qt.y == gt.y) +
+                       (qt.y == gt.z) + (qt.z == gt.x) + (qt.z == gt.y) + (qt.z == gt.z);
+    if (shared >= 2) return false;
     const float4 q0 = pos[qt.x], q1 = pos[qt.y], q2 = pos[qt.z];
     const float4 g0 = pos[gt.x], g1 = pos[gt.y], g2 = pos[gt.z];
     PairGeom ga, gb;

@@ -12,6 +12,7 @@
 // fixed order with compensated (two-sum) float accumulation, so the solve is deterministic apart from the
 // float atomics of the gradient, Hessian-diagonal and Hessian-vector scatters (same as the reference).
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -64,8 +65,6 @@ __host__ __device__ constexpr int sym9(int i, int j) {
     return i <= j ? i * 9 - i * (i - 1) / 2 + (j - i) : j * 9 - j * (j - 1) / 2 + (i - j);
 }
 
-// one 16-byte vector atomic (sm_90+ global memory) instead of three scalar ones
-__device__ __forceinline__ void atomic_add3(float4* a, int i, F3 v) { atomicAdd(&a[i], make_float4(v.x, v.y, v.z, 0.f)); }
 // Warp's step(x): 1 when x < 0, else 0
 __device__ __forceinline__ float wstep(float x) { return x < 0.f ? 1.f : 0.f; }
 
@@ -510,12 +509,13 @@ __device__ __forceinline__ double dsq(D3 a, D3 b) {
 // igl::massmatrix(V, F, MASSMATRIX_TYPE_VORONOI) evaluates in float64 (system.py:223-225): corner cosines
 // by the law of cosines, circumcentre barycentric weights cos_i * l_i normalised to sum 1, the vertex
 // taking half of the two sub-triangles beside it; an obtuse corner takes half the area, the others a quarter.
-// Accumulated into float64 per vertex, then rounded to float32 (the simulation's weights array).
+// Each corner's part goes to its position in its vertex's range (inv_vs, the hinge positions staying zero);
+// k_weights_f32 sums a vertex's range in float64 in order (deterministic), then rounds to float32 (the
+// simulation's weights array).
 __global__ void k_voronoi(const double* __restrict__ pts, const double* __restrict__ st, const int4* __restrict__ tri,
-                          int nt, double* w) {
+                          int nt, const int* __restrict__ inv_vs, double* wslot) {
     for (int f = gtid(); f < nt; f += gstride()) {
         const int4 t = tri[f];
-        const int id[3] = {t.x, t.y, t.z};
         const D3 p[3] = {norm_pos(pts, t.x, st), norm_pos(pts, t.y, st), norm_pos(pts, t.z, st)};
         double l[3], l2[3];
         for (int k = 0; k < 3; ++k) {  // l[k]: edge opposite corner k
@@ -542,12 +542,16 @@ __global__ void k_voronoi(const double* __restrict__ pts, const double* __restri
         for (int o = 0; o < 3; ++o)
             if (cs[o] < 0)
                 for (int k = 0; k < 3; ++k) quad[k] = (k == o) ? 0.25 * dblA : 0.125 * dblA;
-        for (int k = 0; k < 3; ++k) atomicAdd(&w[id[k]], quad[k]);
+        for (int k = 0; k < 3; ++k) wslot[inv_vs[3 * (size_t)f + k]] = quad[k];
     }
 }
 
-__global__ void k_weights_f32(const double* __restrict__ w64, int n, float* w) {
-    for (int i = gtid(); i < n; i += gstride()) w[i] = (float)w64[i];
+__global__ void k_weights_f32(const double* __restrict__ wslot, const int* __restrict__ vs_off, int n, float* w) {
+    for (int i = gtid(); i < n; i += gstride()) {
+        double acc = 0.0;
+        for (int s = vs_off[i]; s < vs_off[i + 1]; ++s) acc += wslot[s];
+        w[i] = (float)acc;
+    }
 }
 
 // elastic_preprocess_kernel (elastic_energy.py:7-37)
@@ -718,15 +722,6 @@ __global__ void __launch_bounds__(kQT) k_closest_gt(const float4* __restrict__ q
 // candidate list made with the half-width plus a skin, valid while no vertex moved more than half the skin
 // (in any coordinate) since it was built, and re-evaluates the distance filter on it every iteration. The
 // contact set is the reference's; the LBVH traversal runs only when the list is rebuilt.
-__device__ __forceinline__ int warp_append(int* counter) {
-    const unsigned am = __activemask();
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(am) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(counter, __popc(am));
-    base = __shfl_sync(am, base, leader);
-    return base + __popc(am & ((1u << lane) - 1u));
-}
 
 // rebuild when some vertex moved more than half the skin since the lists were built
 __global__ void k_disp_check(const float4* __restrict__ q, const float4* __restrict__ qref, int np, float half_skin,
@@ -740,26 +735,25 @@ __global__ void k_disp_check(const float4* __restrict__ q, const float4* __restr
     if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) sc->rebuild = 1;
 }
 
-__global__ void k_cand_begin(SolverScalars* sc) {
-    if (sc->abort || !sc->rebuild) return;
-    sc->n_cand_pt = 0;
-    sc->n_cand_ee = 0;
-}
-
-// LBVH traversal emitting candidate pairs whose boxes overlap within reach (one thread per query, stack in
-// shared memory, bounded).
+// LBVH traversal over the candidate pairs whose boxes overlap within reach (one thread per query, stack in
+// shared memory, bounded), in two passes so that the list order is fixed: with qoff == nullptr each query's
+// count goes to qcount[qi]; with the exclusive prefix sums of the counts in qoff, each query writes its pairs at
+// qoff[qi], qoff[qi] + 1, ... in traversal order (the same pairs in the same order as the counting pass).
 template <bool kEdges>
 __global__ void __launch_bounds__(kQT) k_candidates(const float4* __restrict__ x, int n_query, const int4* __restrict__ elems,
                                                     const int2* __restrict__ child, const float4* __restrict__ nlo,
                                                     const float4* __restrict__ nhi, const float4* __restrict__ llo,
                                                     const float4* __restrict__ lhi, const int* __restrict__ leaf_id,
                                                     const RoundCounters* brc, float d_hat, float skin, int2* out,
-                                                    int cap, int* counter, SolverScalars* sc) {
+                                                    int cap, int* qcount, const int* __restrict__ qoff,
+                                                    SolverScalars* sc) {
     __shared__ int stack[kStack][kQT];
     if (sc->abort || !sc->rebuild) return;
     const float reach = 2.0f * sc->radius + d_hat + skin;
     const int nl = brc->n_live;
     for (int qi = gtid(); qi < n_query; qi += gstride()) {
+        int cnt = 0;
+        const int base = qoff ? qoff[qi] : 0;
         int i0, i1 = -1;
         F3 lo, hi;
         if (!kEdges) {
@@ -788,14 +782,21 @@ __global__ void __launch_bounds__(kQT) k_candidates(const float4* __restrict__ x
                 if (!(qi < id)) return;
                 if (i0 == t.x || i0 == t.y || i1 == t.x || i1 == t.y) return;
             }
-            const int at = warp_append(counter);
-            if (at < cap) out[at] = make_int2(qi, id);
+            if (qoff) {
+                const int at = base + cnt;
+                if (at < cap) out[at] = make_int2(qi, id);
+            }
+            ++cnt;
         };
         if (nl == 1) {
             if (overlap(llo[0], lhi[0])) leaf(0);
+            if (!qoff) qcount[qi] = cnt;
             continue;
         }
-        if (nl < 1) continue;
+        if (nl < 1) {
+            if (!qoff) qcount[qi] = 0;
+            continue;
+        }
         int sp = 0, node = 0, guard = 0;
         while (true) {
             if (++guard > (1 << 22)) {
@@ -827,6 +828,7 @@ __global__ void __launch_bounds__(kQT) k_candidates(const float4* __restrict__ x
                 node = stack[--sp][threadIdx.x];
             }
         }
+        if (!qoff) qcount[qi] = cnt;
     }
 }
 
@@ -841,14 +843,18 @@ __global__ void k_cand_done(const float4* __restrict__ q, float4* qref, int np, 
     for (int i = gtid(); i < np; i += gstride()) qref[i] = q[i];
 }
 
-// the reference's distance filter on the candidates (detect_pt_contact_bvh_kernel, detect_ee_contact_bvh_kernel)
+// the reference's distance filter on the candidates (detect_pt_contact_bvh_kernel, detect_ee_contact_bvh_kernel):
+// candidate g (point-triangle pairs first, then edge-edge pairs) gets cflag[g] = 1 when it is a contact, with its
+// vertex ids and type in cid[g] / cty[g]. The contacts are then listed in candidate order (k_contacts_scatter at
+// the exclusive prefix sums of the flags), so the list, and every sum over it, is the same run after run.
 __global__ void __launch_bounds__(kT) k_filter(const float4* __restrict__ x, const int2* __restrict__ cpt,
                                                const int2* __restrict__ cee, const int4* __restrict__ tri,
                                                const int4* __restrict__ edge4, float d_hat, float ee_thres,
-                                               int4* c_idx, int2* c_type, int cap, SolverScalars* sc) {
+                                               int* cflag, int4* cid, int2* cty, SolverScalars* sc) {
     if (sc->abort) return;
     const float thr = 2.0f * sc->radius + d_hat;
     const int npt = sc->n_cand_pt, nee = sc->n_cand_ee;
+    if (gtid() == 0) sc->n_cand_all = npt + nee;
     for (int g = gtid(); g < npt + nee; g += gstride()) {
         int4 id;
         int block, ty;
@@ -870,14 +876,149 @@ __global__ void __launch_bounds__(kT) k_filter(const float4* __restrict__ x, con
             d = ee_pair_distance(x0, x1, x2, x3, ty);
             block = BLOCK_EE;
         }
-        if (d <= thr) {
-            const int at = warp_append(&sc->n_contacts_raw);
-            if (at < cap) {
-                c_idx[at] = id;
-                c_type[at] = make_int2(block, ty);
+        const int hit = d <= thr ? 1 : 0;
+        cflag[g] = hit;
+        if (hit) {
+            cid[g] = id;
+            cty[g] = make_int2(block, ty);
+        }
+    }
+}
+
+// Contact b = cpos[g] of candidate g (when it is one and fits), and the contacts of each vertex counted in ccnt
+// (one per corner) for the vertex contact lists.
+__global__ void __launch_bounds__(kT) k_contacts_scatter(const int* __restrict__ cflag, const int* __restrict__ cpos,
+                                                         const int4* __restrict__ cid, const int2* __restrict__ cty,
+                                                         int4* c_idx, int2* c_type, int* ccnt, SolverScalars* sc) {
+    if (sc->abort) return;
+    const int n = sc->n_cand_all;
+    for (int g = gtid(); g < n; g += gstride()) {
+        if (!cflag[g]) continue;
+        const int b = cpos[g];
+        const int4 id = cid[g];
+        c_idx[b] = id;
+        c_type[b] = cty[g];
+        atomicAdd(&ccnt[id.x], 1);
+        atomicAdd(&ccnt[id.y], 1);
+        atomicAdd(&ccnt[id.z], 1);
+        atomicAdd(&ccnt[id.w], 1);
+    }
+}
+
+// The contact corners of each vertex in a fixed order: the codes 4b + k (contact b, corner k) are filled at the
+// vertex offsets coff into ctmp (in the order the atomics come), then ranked within each vertex's range by one
+// warp (ascending codes), which gives each corner its position cinv[4b + k] = coff[v] + rank. The per-corner parts
+// of a contact are written at those positions, so each vertex's contact parts are contiguous and in code order.
+__global__ void __launch_bounds__(kT) k_cvert_fill(const int4* __restrict__ c_idx, const int* __restrict__ coff,
+                                                   int* ccur, int* ctmp, const SolverScalars* sc) {
+    if (sc->abort) return;
+    const int n = 4 * sc->n_contacts;
+    for (int s = gtid(); s < n; s += gstride()) {
+        const int4 id = c_idx[s >> 2];
+        const int k = s & 3;
+        const int v = k == 0 ? id.x : k == 1 ? id.y : k == 2 ? id.z : id.w;
+        ctmp[coff[v] + atomicAdd(&ccur[v], 1)] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kT) k_cvert_rank(const int* __restrict__ coff, const int* __restrict__ ctmp,
+                                                   int* cinv, int np, const SolverScalars* sc) {
+    if (sc->abort) return;
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x / 32);
+    for (long long v = gtid() / 32; v < np; v += warps) {
+        const int a = coff[v], m = coff[v + 1] - a;
+        for (int b0 = 0; b0 < m; b0 += 32) {
+            const int x = b0 + lane < m ? ctmp[a + b0 + lane] : INT_MAX;
+            int rank = 0;
+            for (int c0 = 0; c0 < m; c0 += 32) {
+                const int y = c0 + lane < m ? ctmp[a + c0 + lane] : INT_MAX;
+                for (int j = 0; j < 32; ++j) rank += __shfl_sync(0xffffffffu, y, j) < x ? 1 : 0;
+            }
+            if (b0 + lane < m) cinv[x] = a + rank;  // the codes of a vertex are distinct
+        }
+    }
+}
+
+// Sum over vertex i's parts in src: its static parts (triangle corners and hinge slots, stored contiguously per
+// vertex at [vs_off[i], vs_off[i + 1]) in ascending code order), then its contact parts at
+// cbase + [coff[i], coff[i + 1]). The G lanes of a group (G a power of two, at most kGather) read them strided
+// (lane k: parts k, k + G, ...) and the partial sums meet in a butterfly over the group, which gives every lane
+// the same value (the same additions, each commutative). src_h (optional) is summed the same way into h. Called
+// by whole warps with the same G (the shuffles); valid = false contributes zeros.
+constexpr int kGather = 8;
+struct VertexSlots {
+    const int* vs_off;   // NP + 1 offsets of the static parts
+    const int* coff;     // NP + 1 offsets of the contact parts
+    const int* inv_vs;   // position of static code 3f + c (triangle corner) or 3 NT + 4h + a (hinge slot)
+    const int* cinv;     // position (after cbase) of contact code 4b + k
+    int cbase;           // 3 NT + 4 NH
+};
+// A vertex's two ranges as one sequence of m parts: [a, a + m1) then [ca, ca + m - m1); m = 0 for no vertex.
+struct VRange {
+    int a, m1, ca, m;
+};
+__device__ __forceinline__ VRange vertex_range(const VertexSlots& S, int i, bool valid) {
+    VRange R{0, 0, 0, 0};
+    if (valid) {
+        R.a = S.vs_off[i];
+        R.m1 = S.vs_off[i + 1] - R.a;
+        const int c0 = S.coff[i];
+        R.ca = S.cbase + c0;
+        R.m = R.m1 + S.coff[i + 1] - c0;
+    }
+    return R;
+}
+
+__device__ __forceinline__ F3 gather_range(const float4* __restrict__ src, const float4* __restrict__ src_h, F3& h,
+                                           const VRange& R, int lane, int G) {
+    F3 acc = {0.f, 0.f, 0.f};
+    h = F3{0.f, 0.f, 0.f};
+    {
+        // lane k takes parts k, k + G, ..., kBatch loads in flight at a time, added in sequence order
+        constexpr int kBatch = 8;
+        const int a = R.a, m1 = R.m1, ca = R.ca, m = R.m;
+        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int j0 = lane; j0 < m; j0 += kBatch * G) {
+            float4 t[kBatch], th[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                const int j = j0 + u * G;
+                const int pos = j < m1 ? a + j : ca + (j - m1);
+                t[u] = j < m ? src[pos] : zero;
+                th[u] = (src_h && j < m) ? src_h[pos] : zero;
+            }
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+                acc = acc + f3(t[u]);
+                if (src_h) h = h + f3(th[u]);
             }
         }
     }
+    for (int o = G / 2; o > 0; o >>= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+        if (src_h) {
+            h.x += __shfl_xor_sync(0xffffffffu, h.x, o);
+            h.y += __shfl_xor_sync(0xffffffffu, h.y, o);
+            h.z += __shfl_xor_sync(0xffffffffu, h.z, o);
+        }
+    }
+    return acc;
+}
+
+__device__ __forceinline__ F3 gather_slots(const float4* __restrict__ src, const float4* __restrict__ src_h, F3& h,
+                                           const VertexSlots& S, int i, bool valid, int lane, int G) {
+    return gather_range(src, src_h, h, vertex_range(S, i, valid), lane, G);
+}
+
+// The widest group (a power of two up to kGather) that still gives every vertex a group of its own when the grid
+// has nthreads threads (one lane per vertex when the grid is smaller than the vertex count).
+__host__ __device__ __forceinline__ int gather_width(long long nthreads, int np) {
+    int G = kGather;
+    while (G > 1 && nthreads / G < np) G >>= 1;
+    return G;
 }
 
 // ------------------------------------------------------------------ energies
@@ -998,20 +1139,12 @@ __global__ void __launch_bounds__(kT) k_energy(const float4* __restrict__ x, Ene
 }
 
 // ------------------------------------------------------------------ gradients and Hessian diagonal (coeff = -1)
-__global__ void k_diff_m2gt(const float4* __restrict__ x, const float4* __restrict__ tgt, const float* __restrict__ w,
-                            float stiff, float coeff, int np, float4* grad, float4* hd,
-                            const SolverScalars* sc) {
-    if (sc->abort) return;
-    for (int i = gtid(); i < np; i += gstride()) {
-        const float wi = w[i] * stiff;
-        atomic_add3(grad, i, (f3(x[i]) - f3(tgt[i])) * wi * coeff);
-        atomic_add3(hd, i, F3{wi, wi, wi});
-    }
-}
-
+// Each element writes its part of the gradient (and of the Hessian diagonal) per corner into the slot arrays
+// gslot / hslot, at the corner's position in its vertex's range (inv_vs / cinv); k_gather_grad then sums each
+// vertex's range in a fixed order (no float atomics, so the result is the same run after run).
 __global__ void k_diff_elastic(const float4* __restrict__ x, const int4* __restrict__ tri, const float* __restrict__ area,
-                               const float4* __restrict__ invDm, float mu, float la, float coeff, int nt, float4* grad,
-                               const SolverScalars* sc) {
+                               const float4* __restrict__ invDm, float mu, float la, float coeff, int nt, float4* gslot,
+                               const int* __restrict__ inv_vs, const SolverScalars* sc) {
     if (sc->abort) return;
     for (int f = gtid(); f < nt; f += gstride()) {
         const int4 t = tri[f];
@@ -1023,9 +1156,10 @@ __global__ void k_diff_elastic(const float4* __restrict__ x, const int4* __restr
         const Mat2 H = mmul(mscale(coeff * L.W, P), mtr(L.invDm));  // ((coeff W) P) invDm^T
         const F3 f1 = H.a * L.b1 + H.c * L.b2;
         const F3 f2 = H.b * L.b1 + H.d * L.b2;
-        atomic_add3(grad, t.x, -f1 - f2);
-        atomic_add3(grad, t.y, f1);
-        atomic_add3(grad, t.z, f2);
+        const int* at = inv_vs + 3 * (size_t)f;
+        gslot[at[0]] = f4(-f1 - f2);
+        gslot[at[1]] = f4(f1);
+        gslot[at[2]] = f4(f2);
     }
 }
 
@@ -1064,8 +1198,8 @@ __device__ __forceinline__ M33 sym(M33 a) { return add(a, tr(a)); }
 
 // hinge_diff_kernel (hinge_energy.py:85-238): gradient, Hessian diagonal and the 4x4 blocks of 3x3
 __global__ void k_diff_hinge(const float4* __restrict__ x, const int4* __restrict__ hinge, const float2* __restrict__ rest,
-                             float k, float coeff, int nh, float* blocks, float4* grad, float4* hd,
-                             const SolverScalars* sc) {
+                             float k, float coeff, int nh, float* blocks, float4* gslot, float4* hslot,
+                             const int* __restrict__ inv_h, const SolverScalars* sc) {
     if (sc->abort) return;
     for (int h = gtid(); h < nh; h += gstride()) {
         const int4 id = hinge[h];
@@ -1088,10 +1222,11 @@ __global__ void k_diff_hinge(const float4* __restrict__ x, const int4* __restric
         const F3 g2 = n * (ca1 / h2) + n_ * (ca1_ / h2_);
         const F3 g0 = n * (-1.0f / h0);
         const F3 g3 = n_ * (-1.0f / h0_);
-        atomic_add3(grad, id.x, dE * g0 * coeff);
-        atomic_add3(grad, id.y, dE * g1 * coeff);
-        atomic_add3(grad, id.z, dE * g2 * coeff);
-        atomic_add3(grad, id.w, dE * g3 * coeff);
+        const int* at = inv_h + 4 * (size_t)h;
+        gslot[at[0]] = f4(dE * g0 * coeff);
+        gslot[at[1]] = f4(dE * g1 * coeff);
+        gslot[at[2]] = f4(dE * g2 * coeff);
+        gslot[at[3]] = f4(dE * g3 * coeff);
         const F3 m0 = normalize(cross(e0, n)), m1 = normalize(cross(e1, n)), m2 = normalize(cross(n, e2));
         const F3 m0_ = normalize(cross(n_, e0)), m1_ = normalize(cross(n_, e1_)), m2_ = normalize(cross(e2_, n_));
         const M33 M0 = outer(n, m0), M1 = outer(n, m1), M2 = outer(n, m2);
@@ -1133,8 +1268,7 @@ __global__ void k_diff_hinge(const float4* __restrict__ x, const int4* __restric
 #pragma unroll
                     for (int j = 0; j < 3; ++j)
                         if (b * 3 + j >= a * 3 + i) out[sym9(a * 3 + i, b * 3 + j)] = B[a][b].m[i][j];
-        const int ids[4] = {id.x, id.y, id.z, id.w};
-        for (int a = 0; a < 4; ++a) atomic_add3(hd, ids[a], F3{B[a][a].m[0][0], B[a][a].m[1][1], B[a][a].m[2][2]});
+        for (int a = 0; a < 4; ++a) hslot[at[a]] = f4(F3{B[a][a].m[0][0], B[a][a].m[1][1], B[a][a].m[2][2]});
     }
 }
 
@@ -1216,12 +1350,20 @@ __global__ void __launch_bounds__(32 * kSpdWarps) k_spd_project(float* blocks, i
 // collision_diff_kernel (collision_energy.py:192-254)
 __global__ void k_diff_contact(const float4* __restrict__ x, const int4* __restrict__ cidx, const int2* __restrict__ ctype,
                                const float* __restrict__ cd, const SolverScalars* sc, float kappa, float dh, float coeff,
-                               float4* cdd, float4* grad, float4* hd) {
+                               float4* cdd, float4* gslot, float4* hslot, const int* __restrict__ cinv) {
     if (sc->abort) return;
     const int n = sc->n_contacts;
     for (int b = gtid(); b < n; b += gstride()) {
         const float d = cd[b];
-        if (d >= dh) continue;
+        const int* at = cinv + 4 * (size_t)b;
+        if (d >= dh) {  // no barrier term: zero parts
+            const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int k = 0; k < 4; ++k) {
+                gslot[at[k]] = zero;
+                hslot[at[k]] = zero;
+            }
+            continue;
+        }
         const int4 i = cidx[b];
         const F3 x0 = f3(x[i.x]), x1 = f3(x[i.y]), x2 = f3(x[i.z]), x3 = f3(x[i.w]);
         const int2 t = ctype[b];
@@ -1230,11 +1372,36 @@ __global__ void k_diff_contact(const float4* __restrict__ x, const int4* __restr
         else ee_pair_grad(x0, x1, x2, x3, t.y, g);
         const float ddc = barrier_d1(d, dh) * kappa * coeff;
         const float d2c = barrier_d2(d, dh) * kappa;
-        const int ids[4] = {i.x, i.y, i.z, i.w};
         for (int k = 0; k < 4; ++k) {
             cdd[4 * (size_t)b + k] = f4(g[k]);
-            atomic_add3(grad, ids[k], g[k] * ddc);
-            atomic_add3(hd, ids[k], d2c * F3{g[k].x * g[k].x, g[k].y * g[k].y, g[k].z * g[k].z});
+            gslot[at[k]] = f4(g[k] * ddc);
+            hslot[at[k]] = f4(d2c * F3{g[k].x * g[k].x, g[k].y * g[k].y, g[k].z * g[k].z});
+        }
+    }
+}
+
+// grad = the mesh-to-GT term (mesh2gt_pp_distance diff, distance_energy.py:20-33) plus the vertex's slots, hd
+// the same for the Hessian diagonal; a group of kGather lanes per vertex.
+__global__ void __launch_bounds__(kT) k_gather_grad(const float4* __restrict__ x, const float4* __restrict__ tgt,
+                                                    const float* __restrict__ w, float stiff, float coeff, int np,
+                                                    const float4* __restrict__ gslot, const float4* __restrict__ hslot,
+                                                    VertexSlots S, float4* grad, float4* hd, const SolverScalars* sc) {
+    if (sc->abort) return;
+    const int G = gather_width((long long)gridDim.x * blockDim.x, np);
+    const long long ngroups = (long long)gridDim.x * blockDim.x / G;
+    const long long group = gtid() / G;
+    const int lane = (int)(gtid() % G);
+    const long long rounds = (np + ngroups - 1) / ngroups;
+    for (long long k = 0; k < rounds; ++k) {
+        const long long ii = group + k * ngroups;
+        const bool valid = ii < np;
+        const int i = valid ? (int)ii : 0;
+        F3 h;
+        const F3 g = gather_slots(gslot, hslot, h, S, i, valid, lane, G);
+        if (valid && lane == 0) {
+            const float wi = w[i] * stiff;
+            grad[i] = f4((f3(x[i]) - f3(tgt[i])) * wi * coeff + g);
+            hd[i] = f4(F3{wi, wi, wi} + h);
         }
     }
 }
@@ -1242,12 +1409,14 @@ __global__ void k_diff_contact(const float4* __restrict__ x, const int4* __restr
 // ------------------------------------------------------------------ Jacobi PCG (cg_solver.py:46-158)
 // Per CG iteration two phases, separated by grid barriers inside one cooperative kernel:
 //   Hessian product: the search direction v = z + (z_r / z_r_last) v_prev is formed where it is read
-//     (update_v_kernel, solver_kernels.py:26-35), Av += H v over every element (system.py:348-352: the hess_dx
-//     kernels of distance_energy.py:20-33, elastic_energy.py:151-220, hinge_energy.py:241-274 and the
-//     Gauss-Newton collision_hess_dx_kernel, collision_energy.py:379-409), and v.Av is summed per element
-//     (v_e . H_e v_e, which equals v . Av), so no separate dot-product pass is needed;
-//   p/r/z: p += alpha v, r -= alpha Av when v.Av > 1e-16, z = r / diag, z.r (update_p_r_z_compute_zr_kernel,
-//     solver_kernels.py:4-23); Av is cleared for the next product.
+//     (update_v_kernel, solver_kernels.py:26-35), each element writes its corners' parts of H v into the slot
+//     array aslot (system.py:348-352: the hess_dx kernels of elastic_energy.py:151-220, hinge_energy.py:241-274
+//     and the Gauss-Newton collision_hess_dx_kernel, collision_energy.py:379-409; the vertex term of
+//     distance_energy.py:20-33 is added where Av is formed), and v.Av is summed per element (v_e . H_e v_e, which
+//     equals v . Av), so no separate dot-product pass is needed;
+//   p/r/z: Av_i = the vertex term plus the sum of vertex i's slots (gather_slots, a fixed order: the same result
+//     run after run, where float atomics would add in the order the threads arrive), p += alpha v, r -= alpha Av
+//     when v.Av > 1e-16, z = r / diag, z.r (update_p_r_z_compute_zr_kernel, solver_kernels.py:4-23).
 struct HvpArgs {
     const float* w;
     float m2gt_k;
@@ -1264,6 +1433,8 @@ struct HvpArgs {
     const float* cd;
     const float4* cdd;
     float kappa, d_hat;
+    float4* aslot;  // per-corner parts of H v (triangles, hinges, then contacts at S.cbase)
+    VertexSlots S;
 };
 
 __device__ __forceinline__ F3 cg_dir(const float4* __restrict__ z, const float4* __restrict__ vprev, float s, int j) {
@@ -1280,11 +1451,29 @@ __device__ __forceinline__ int4 element_ids(const HvpArgs& A, int nc, long long 
     return A.cidx[g - e3];
 }
 
-// Av += H v over the elements gtid, gtid + stride, ...; returns this thread's part of v.Av. The direction is
-// v = z + s v_prev, written to vout by the vertex terms. ids0 = element_ids(first).
+// Where the corners' parts of element g go in A.aslot (unused entries zero; the vertex terms have none). Like the
+// ids they are fixed during a solve, so a thread loads those of its first element once.
+__device__ __forceinline__ int4 element_slots(const HvpArgs& A, int nc, long long g) {
+    const long long e1 = A.np, e2 = e1 + A.nt, e3 = e2 + A.nh, total = e3 + nc;
+    if (g < e1 || g >= total) return make_int4(0, 0, 0, 0);
+    if (g < e2) {
+        const int* at = A.S.inv_vs + 3 * (g - e1);
+        return make_int4(at[0], at[1], at[2], 0);
+    }
+    if (g < e3) {
+        const int* at = A.S.inv_vs + 3 * (size_t)A.nt + 4 * (g - e2);
+        return make_int4(at[0], at[1], at[2], at[3]);
+    }
+    const int* at = A.S.cinv + 4 * (g - e3);
+    return make_int4(A.S.cbase + at[0], A.S.cbase + at[1], A.S.cbase + at[2], A.S.cbase + at[3]);
+}
+
+// The corners' parts of H v over the elements gtid, gtid + stride, ... into A.aslot; returns this thread's part of
+// v.Av. The direction is v = z + s v_prev, written to vout by the vertex terms. ids0 = element_ids(first),
+// at0 = element_slots(first).
 __device__ __forceinline__ CSum hvp_elements(const float4* __restrict__ x, const HvpArgs& A, const float4* __restrict__ z,
-                                             const float4* __restrict__ vprev, float4* vout, float4* Av, float s, int nc,
-                                             long long first, long long stride, int4 ids0) {
+                                             const float4* __restrict__ vprev, float4* vout, float s, int nc,
+                                             long long first, long long stride, int4 ids0, int4 at0) {
     const long long e1 = A.np, e2 = e1 + A.nt, e3 = e2 + A.nh, total = e3 + nc;
     CSum acc;
     for (long long g = first; g < total; g += stride) {
@@ -1294,7 +1483,6 @@ __device__ __forceinline__ CSum hvp_elements(const float4* __restrict__ x, const
             const F3 vi = cg_dir(z, vprev, s, i);
             vout[i] = f4(vi);
             const float wi = A.w[i] * A.m2gt_k;
-            atomic_add3(Av, i, vi * wi);
             acc.add(dot(vi, vi * wi));
         } else if (g < e2) {
             const int f = (int)(g - e1);
@@ -1315,9 +1503,10 @@ __device__ __forceinline__ CSum hvp_elements(const float4* __restrict__ x, const
             const F3 df1 = dH.a * L.b1 + dH.c * L.b2;
             const F3 df2 = dH.b * L.b1 + dH.d * L.b2;
             const F3 df0 = -df1 - df2;
-            atomic_add3(Av, t.x, df0);
-            atomic_add3(Av, t.y, df1);
-            atomic_add3(Av, t.z, df2);
+            const int4 at = cached ? at0 : element_slots(A, nc, g);
+            A.aslot[at.x] = f4(df0);
+            A.aslot[at.y] = f4(df1);
+            A.aslot[at.z] = f4(df2);
             acc.add(dot(v0, df0) + dot(v1, df1) + dot(v2, df2));
         } else if (g < e3) {
             const int h = (int)(g - e2);
@@ -1349,19 +1538,28 @@ __device__ __forceinline__ CSum hvp_elements(const float4* __restrict__ x, const
             }
             float vhv = 0.f;
             F3 sum = {0.f, 0.f, 0.f};
+            const int4 at4 = cached ? at0 : element_slots(A, nc, g);
+            const int at[4] = {at4.x, at4.y, at4.z, at4.w};
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 const F3 ua = {u[3 * a], u[3 * a + 1], u[3 * a + 2]};
-                atomic_add3(Av, ids[a], ua);
+                A.aslot[at[a]] = f4(ua);
                 sum = sum + ua;
                 vhv += w[3 * a] * ua.x + w[3 * a + 1] * ua.y + w[3 * a + 2] * ua.z;
             }
-            atomic_add3(Av, ids[3], -sum);
+            A.aslot[at[3]] = f4(-sum);
             acc.add(vhv);
         } else {
             const int b = (int)(g - e3);
             const float dist = A.cd[b];
-            if (dist >= A.d_hat) continue;
+            float4* as = A.aslot;
+            const int4 at4 = cached ? at0 : element_slots(A, nc, g);
+            const int at[4] = {at4.x, at4.y, at4.z, at4.w};
+            if (dist >= A.d_hat) {  // no barrier term: zero parts
+                const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int k = 0; k < 4; ++k) as[at[k]] = zero;
+                continue;
+            }
             const float c = barrier_d2(dist, A.d_hat) * A.kappa;
             const int4 i = cached ? ids0 : A.cidx[b];
             const int ids[4] = {i.x, i.y, i.z, i.w};
@@ -1371,16 +1569,16 @@ __device__ __forceinline__ CSum hvp_elements(const float4* __restrict__ x, const
                 gg[k] = f3(A.cdd[4 * (size_t)b + k]);
                 sd += dot(gg[k], cg_dir(z, vprev, s, ids[k]));
             }
-            for (int k = 0; k < 4; ++k) atomic_add3(Av, ids[k], gg[k] * (sd * c));
+            for (int k = 0; k < 4; ++k) as[at[k]] = f4(gg[k] * (sd * c));
             acc.add(sd * sd * c);
         }
     }
     return acc;
 }
 
-// p = 0, r = grad, z = r / (diag + 1e-6) (compute_block_diag_inv_kernel), v_prev = 0, Av = 0; returns z.r part
+// p = 0, r = grad, z = r / (diag + 1e-6) (compute_block_diag_inv_kernel), v_prev = 0; returns z.r part
 __device__ __forceinline__ CSum cg_init_vertices(const float4* __restrict__ grad, const float4* __restrict__ hd, int np,
-                                                 float4* p, float4* r, float4* z, float4* vprev, float4* Av, int first,
+                                                 float4* p, float4* r, float4* z, float4* vprev, int first,
                                                  int stride) {
     CSum acc;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1391,42 +1589,71 @@ __device__ __forceinline__ CSum cg_init_vertices(const float4* __restrict__ grad
         const float4 zz = make_float4(g.x / (d.x + 1e-6f), g.y / (d.y + 1e-6f), g.z / (d.z + 1e-6f), 0.f);
         z[i] = zz;
         vprev[i] = zero;
-        Av[i] = zero;
         acc.add(zz.x * g.x + zz.y * g.y + zz.z * g.z);
     }
     return acc;
 }
 
-// The vertex values the p/r/z phase reads, loaded for a thread's first vertex before v.Av is known.
-struct PrzVertex {
-    float4 v, av, p, r, d;
+// The p/r/z phase runs on groups of kGather lanes, group k of the grid taking vertices k, k + groups, ... (the same
+// number of rounds in every warp, for the shuffles of gather_slots).
+struct PrzLanes {
+    int group, lane, groups, rounds, G;
 };
-
-__device__ __forceinline__ PrzVertex prz_load(const float4* __restrict__ v, const float4* Av,
-                                              const float4* __restrict__ hd, const float4* p, const float4* r, int i) {
-    return PrzVertex{v[i], Av[i], p[i], r[i], hd[i]};
+__device__ __forceinline__ PrzLanes prz_lanes(int tid, int nthreads, int np) {
+    PrzLanes L;
+    L.G = gather_width(nthreads, np);
+    L.group = tid / L.G;
+    L.lane = tid % L.G;
+    L.groups = nthreads / L.G;
+    L.rounds = (np + L.groups - 1) / L.groups;
+    return L;
 }
 
-// p += alpha v, r -= alpha Av when v.Av > 1e-16, z = r / diag, Av = 0; returns z.r part. `pre` holds the values
-// of vertex `first` (when first < np), loaded before the block partials of v.Av were summed.
-__device__ __forceinline__ CSum cg_prz_vertices(const float4* __restrict__ v, float4* Av, const float4* __restrict__ hd,
-                                                int np, float4* p, float4* r, float4* z, float zr, float vAv, int first,
-                                                int stride, const PrzVertex& pre) {
+// What the p/r/z phase reads for one vertex: v, p, r, diag and Av (the vertex term plus the gathered slots), all
+// independent of v.Av, so that the first round's values are loaded before the block partials are summed.
+struct PrzVertex {
+    float4 v, p, r, d;
+    F3 av;
+};
+
+__device__ __forceinline__ PrzVertex prz_load(const HvpArgs& A, const float4* __restrict__ v,
+                                              const float4* __restrict__ hd, const float4* p, const float4* r,
+                                              int i, bool valid, const PrzLanes& L, const VRange& R) {
+    PrzVertex pv{};
+    F3 unused;
+    const F3 g = gather_range(A.aslot, nullptr, unused, R, L.lane, L.G);
+    if (valid) {
+        pv.v = v[i];
+        pv.p = p[i];
+        pv.r = r[i];
+        pv.d = hd[i];
+        pv.av = f3(pv.v) * (A.w[i] * A.m2gt_k) + g;
+    }
+    return pv;
+}
+
+// p += alpha v, r -= alpha Av when v.Av > 1e-16, z = r / diag; returns z.r part. `pre` holds the values of the
+// group's first vertex, loaded before the block partials of v.Av were summed.
+__device__ __forceinline__ CSum cg_prz_vertices(const HvpArgs& A, const float4* __restrict__ v,
+                                                const float4* __restrict__ hd, float4* p, float4* r, float4* z,
+                                                float zr, float vAv, const PrzLanes& L, const PrzVertex& pre) {
     const float alpha = zr / vAv;
     CSum acc;
-    for (int i = first; i < np; i += stride) {
-        const bool cached = i == first;
-        float4 ri = cached ? pre.r : r[i];
+    for (int k = 0; k < L.rounds; ++k) {
+        const int i = L.group + k * L.groups;
+        const bool valid = i < A.np;
+        const PrzVertex pv = k == 0 ? pre : prz_load(A, v, hd, p, r, valid ? i : 0, valid, L,
+                                                     vertex_range(A.S, valid ? i : 0, valid));
+        if (!valid || L.lane != 0) continue;
+        float4 ri = pv.r;
         if (vAv > 1e-16f) {
-            const float4 vi = cached ? pre.v : v[i], avi = cached ? pre.av : Av[i];
-            float4 pi = cached ? pre.p : p[i];
-            pi.x += alpha * vi.x; pi.y += alpha * vi.y; pi.z += alpha * vi.z;
-            ri.x -= alpha * avi.x; ri.y -= alpha * avi.y; ri.z -= alpha * avi.z;
+            float4 pi = pv.p;
+            pi.x += alpha * pv.v.x; pi.y += alpha * pv.v.y; pi.z += alpha * pv.v.z;
+            ri.x -= alpha * pv.av.x; ri.y -= alpha * pv.av.y; ri.z -= alpha * pv.av.z;
             p[i] = pi;
             r[i] = ri;
         }
-        Av[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 d = cached ? pre.d : hd[i];
+        const float4 d = pv.d;
         const float4 zz = make_float4(ri.x / d.x, ri.y / d.y, ri.z / d.z, 0.f);
         z[i] = zz;
         acc.add(zz.x * ri.x + zz.y * ri.y + zz.z * ri.z);
@@ -1498,15 +1725,18 @@ struct CgState {
 template <int kThreads>
 __global__ void __launch_bounds__(kThreads) k_cg_solve(const float4* __restrict__ x, HvpArgs A, const float4* __restrict__ grad,
                                                  const float4* __restrict__ hd, float4* p, float4* r, float4* z,
-                                                 float4* v0, float4* v1, float4* Av, int n_iters, SolverScalars* sc,
+                                                 float4* v0, float4* v1, int n_iters, SolverScalars* sc,
                                                  float2* partial, CgState* bar) {
     if (sc->abort) return;
     const int nc = sc->n_contacts;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
     float2* part_a = partial;
     float2* part_b = partial + gridDim.x;
-    const int4 ids0 = element_ids(A, nc, tid);  // fixed for the whole solve
-    store_partial(cg_init_vertices(grad, hd, A.np, p, r, z, v0, Av, tid, nthreads), part_a);
+    const int4 ids0 = element_ids(A, nc, tid);
+    const int4 at0 = element_slots(A, nc, tid);  // fixed for the whole solve
+    const PrzLanes L = prz_lanes(tid, nthreads, A.np);
+    const VRange R0 = vertex_range(A.S, L.group < A.np ? L.group : 0, L.group < A.np);  // the group's first vertex
+    store_partial(cg_init_vertices(grad, hd, A.np, p, r, z, v0, tid, nthreads), part_a);
     grid_barrier(&bar->count, &sc->status);
     float zr = grid_partials_sum(part_a), zr_last = zr;
     for (int it = 0; it < n_iters; ++it) {
@@ -1515,13 +1745,13 @@ __global__ void __launch_bounds__(kThreads) k_cg_solve(const float4* __restrict_
         const float s_dir = it == 0 ? 0.f : zr / zr_last;
         // partials alternate between two buffers phase by phase: a buffer is rewritten only after the next
         // barrier, which every block reaches after it has read that buffer
-        store_partial(hvp_elements(x, A, z, vin, vout, Av, s_dir, nc, tid, nthreads, ids0), part_b);
+        store_partial(hvp_elements(x, A, z, vin, vout, s_dir, nc, tid, nthreads, ids0, at0), part_b);
         grid_barrier(&bar->count, &sc->status);
-        // this thread's vertex loads go out before the partials are summed (they do not depend on v.Av)
-        PrzVertex pre{};
-        if (tid < A.np) pre = prz_load(vout, Av, hd, p, r, tid);
+        // the first vertex's loads and slot gather go out before the partials are summed (they do not depend on
+        // v.Av)
+        const PrzVertex pre = prz_load(A, vout, hd, p, r, L.group < A.np ? L.group : 0, L.group < A.np, L, R0);
         const float vAv = grid_partials_sum(part_b);
-        store_partial(cg_prz_vertices(vout, Av, hd, A.np, p, r, z, zr, vAv, tid, nthreads, pre), part_a);
+        store_partial(cg_prz_vertices(A, vout, hd, p, r, z, zr, vAv, L, pre), part_a);
         grid_barrier(&bar->count, &sc->status);
         zr_last = zr;
         zr = grid_partials_sum(part_a);
@@ -1570,7 +1800,7 @@ constexpr int kClusterThreads = 1024;
 __global__ void __launch_bounds__(kClusterThreads) k_cg_cluster(const float4* __restrict__ x, HvpArgs A,
                                                                 const float4* __restrict__ grad,
                                                                 const float4* __restrict__ hd, float4* p, float4* r,
-                                                                float4* z, float4* v0, float4* v1, float4* Av,
+                                                                float4* z, float4* v0, float4* v1,
                                                                 int n_iters, SolverScalars* sc) {
     namespace cgr = cooperative_groups;
     cgr::cluster_group cl = cgr::this_cluster();
@@ -1605,16 +1835,18 @@ __global__ void __launch_bounds__(kClusterThreads) k_cg_cluster(const float4* __
         return v;
     };
     const int4 ids0 = element_ids(A, nc, tid);
-    float zr = cluster_total(cg_init_vertices(grad, hd, A.np, p, r, z, v0, Av, tid, nthreads)), zr_last = zr;
+    const int4 at0 = element_slots(A, nc, tid);
+    const PrzLanes L = prz_lanes(tid, nthreads, A.np);
+    const VRange R0 = vertex_range(A.S, L.group < A.np ? L.group : 0, L.group < A.np);  // the group's first vertex
+    float zr = cluster_total(cg_init_vertices(grad, hd, A.np, p, r, z, v0, tid, nthreads)), zr_last = zr;
     float vAv = 0.f;
     for (int it = 0; it < n_iters; ++it) {
         const float4* vin = (it & 1) ? v1 : v0;
         float4* vout = (it & 1) ? v0 : v1;
         const float s_dir = it == 0 ? 0.f : zr / zr_last;
-        vAv = cluster_total(hvp_elements(x, A, z, vin, vout, Av, s_dir, nc, tid, nthreads, ids0));
-        PrzVertex pre{};
-        if (tid < A.np) pre = prz_load(vout, Av, hd, p, r, tid);
-        const float zr_new = cluster_total(cg_prz_vertices(vout, Av, hd, A.np, p, r, z, zr, vAv, tid, nthreads, pre));
+        vAv = cluster_total(hvp_elements(x, A, z, vin, vout, s_dir, nc, tid, nthreads, ids0, at0));
+        const PrzVertex pre = prz_load(A, vout, hd, p, r, L.group < A.np ? L.group : 0, L.group < A.np, L, R0);
+        const float zr_new = cluster_total(cg_prz_vertices(A, vout, hd, p, r, z, zr, vAv, L, pre));
         zr_last = zr;
         zr = zr_new;
     }
@@ -1627,18 +1859,18 @@ __global__ void __launch_bounds__(kClusterThreads) k_cg_cluster(const float4* __
 }
 
 // ------------------------------------------------------------------ iteration bookkeeping
-// Start of a Newton iteration (system.py:425-432): q_prev_newton = q, gradient and Hessian diagonal cleared,
-// contact counter reset.
-__global__ void k_iter_begin(const float4* __restrict__ q, float4* qpn, float4* grad, float4* hd, int np,
+// Start of a Newton iteration (system.py:425-432): q_prev_newton = q; the per-vertex contact counts and fill
+// cursors cleared.
+__global__ void k_iter_begin(const float4* __restrict__ q, float4* qpn, int* ccnt, int* ccur, int np,
                              SolverScalars* sc) {
     if (sc->abort) return;
-    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int i = gtid(); i < np; i += gstride()) {
-        qpn[i] = q[i];
-        grad[i] = zero;
-        hd[i] = zero;
+    for (int i = gtid(); i <= np; i += gstride()) {
+        if (i < np) {
+            qpn[i] = q[i];
+            ccur[i] = 0;
+        }
+        ccnt[i] = 0;
     }
-    if (gtid() == 0) sc->n_contacts_raw = 0;
 }
 
 // After detection: the contact count, and the abort code when the list overflowed (energy.py:942-948 halves
@@ -1977,7 +2209,10 @@ void Stage3::release() {
         ptr = nullptr;
     };
     f(gt_pos); f(gt_tri); f(gt_bvh_mem); f(gt_rc); f(q); f(q_rest); f(q_prev_newton); f(p); f(target);
-    f(grad); f(hdiag); f(r); f(z); f(v[0]); f(v[1]); f(Av); f(vweight); f(q_ref); f(cand_pt); f(cand_ee); f(tri); f(edge4); f(el_area); f(el_invDm);
+    f(grad); f(hdiag); f(r); f(z); f(v[0]); f(v[1]); f(vweight);
+    f(cand_cnt); f(cand_off); f(cflag); f(cpos); f(cid); f(cty); f(vs_off); f(inv_vs); f(c_cnt); f(c_off); f(c_cur);
+    f(c_tmp); f(c_inv); f(gslot); f(hslot); f(aslot); f(scan_scratch);
+    cap_cf = cap_vs = cap_vso = cap_slot = cap_cq = 0; f(q_ref); f(cand_pt); f(cand_ee); f(tri); f(edge4); f(el_area); f(el_invDm);
     f(hinge); f(hinge_rest); f(hinge_blocks); f(c_idx); f(c_type); f(c_d); f(c_dd); f(partial); f(tri_bvh_mem);
     f(edge_bvh_mem); f(tri_rc); f(edge_rc); f(sc); f(d_norm); f(cg_bar);
     if (h_sc) cudaFreeHost(h_sc);
@@ -2047,7 +2282,7 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
     }
     if (cap_v < (size_t)np + 2) {
         const size_t n = (size_t)np + 2;
-        for (float4** b : {&q, &q_rest, &q_prev_newton, &q_ref, &p, &target, &grad, &hdiag, &r, &z, &Av, &v[0], &v[1]}) {
+        for (float4** b : {&q, &q_rest, &q_prev_newton, &q_ref, &p, &target, &grad, &hdiag, &r, &z, &v[0], &v[1]}) {
             c = cap_v;
             if ((rr = grow(*b, c, n))) return rr;
         }
@@ -2109,8 +2344,65 @@ int Stage3::ensure_contacts(size_t n) {
     if ((rr = grow(c_d, c, n))) return rr;
     c = 0;
     if ((rr = grow(c_dd, c, 4 * n))) return rr;
+    for (int** b : {&c_tmp, &c_inv}) {
+        c = 0;
+        cudaFree(*b);
+        *b = nullptr;
+        if ((rr = grow(*b, c, 4 * n))) return rr;
+    }
     cap_c = n;
     drop_graph();
+    return ensure_slots();
+}
+
+// The slot arrays (3 NT + 4 NH + 4 cap_c corners), the vertex lists' offsets and counts (NP + 2) and the scan
+// scratch, for the current sizes.
+int Stage3::ensure_slots() {
+    int rr;
+    size_t c;
+    const size_t ns = (size_t)3 * NT + (size_t)4 * NH + (size_t)4 * cap_c;
+    if (cap_slot < ns || !gslot) {
+        if (gslot) cudaStreamSynchronize(stream);
+        for (float4** b : {&gslot, &hslot, &aslot}) {
+            cudaFree(*b);
+            *b = nullptr;
+            c = 0;
+            if ((rr = grow(*b, c, ns))) return rr;
+        }
+        cap_slot = ns;
+    }
+    const size_t nv = (size_t)NP + 2;
+    if (cap_vso < nv || !vs_off) {
+        if (vs_off) cudaStreamSynchronize(stream);
+        for (int** b : {&vs_off, &c_cnt, &c_off, &c_cur}) {
+            cudaFree(*b);
+            *b = nullptr;
+            c = 0;
+            if ((rr = grow(*b, c, nv))) return rr;
+        }
+        cap_vso = nv;
+    }
+    const size_t nq = (size_t)NP + NE + 2;
+    if (cap_cq < nq || !cand_cnt) {
+        c = cap_cq;
+        if ((rr = grow(cand_cnt, c, nq))) return rr;
+        c = cap_cq;
+        if ((rr = grow(cand_off, c, nq))) return rr;
+        cap_cq = nq;
+    }
+    const size_t nl = (size_t)3 * NT + (size_t)4 * NH + 1;
+    if (cap_vs < nl || !inv_vs) {
+        c = cap_vs;
+        if ((rr = grow(inv_vs, c, nl))) return rr;
+        cap_vs = nl;
+    }
+    if (!scan_scratch) {
+        c = 0;
+        if ((rr = grow(scan_scratch, c, 2 * scan_scratch_ints()))) return rr;
+        // both scratches start zeroed (a scan's tile counters live there)
+        if (scan_scratch_clear(scan_scratch) || scan_scratch_clear(scan_scratch + scan_scratch_ints()))
+            return fail(PAMO_ERR_CUDA, "scan scratch");
+    }
     return PAMO_OK;
 }
 
@@ -2126,6 +2418,23 @@ int Stage3::ensure_candidates(size_t npt, size_t nee) {
         c = cand_ee ? cap_cee : 0;
         if ((rr = grow(cand_ee, c, nee))) return rr;
         cap_cee = c;
+    }
+    const size_t nf = cap_cpt + cap_cee + 1;
+    if (cap_cf < nf || !cflag) {
+        if (cflag) cudaStreamSynchronize(stream);
+        cudaFree(cflag); cudaFree(cpos); cudaFree(cid); cudaFree(cty);
+        cflag = cpos = nullptr;
+        cid = nullptr;
+        cty = nullptr;
+        c = 0;
+        if ((rr = grow(cflag, c, nf))) return rr;
+        c = 0;
+        if ((rr = grow(cpos, c, nf))) return rr;
+        c = 0;
+        if ((rr = grow(cid, c, nf))) return rr;
+        c = 0;
+        if ((rr = grow(cty, c, nf))) return rr;
+        cap_cf = nf;
     }
     return PAMO_OK;
 }
@@ -2160,46 +2469,86 @@ void Stage3::newton_iteration() {
     const float la = P.elas_young_modulus * P.elas_poisson_ratio / ((1.f + P.elas_poisson_ratio) * (1.f - 2.f * P.elas_poisson_ratio));
     const int gC = grid_for((long long)cap_c, kT);
     // q_prev_newton = q; contacts at q (system.py:425-432, _detect_contact :308-318 with refitted LBVHs)
-    k_iter_begin<<<grid_for(NP, kT), kT, 0, s>>>(q, q_prev_newton, grad, hdiag, NP, sc);
+    k_iter_begin<<<grid_for(NP + 1, kT), kT, 0, s>>>(q, q_prev_newton, c_cnt, c_cur, NP, sc);
     note_launch();
     const float skin = 2.0f * P.contact_detection_radius + P.d_hat;
     k_disp_check<<<grid_for(NP, kT), kT, 0, s>>>(q, q_ref, NP, 0.5f * skin, sc);
     note_launch();
-    k_cand_begin<<<1, 1, 0, s>>>(sc);
-    note_launch();
     bvh_refit(tri_bvh, tri, q, tri_rc, NT, s, &sc->rebuild);
     bvh_refit(edge_bvh, edge4, q, edge_rc, NE, s, &sc->rebuild);
+    // candidate lists in a fixed order: per-query counts, their prefix sums (the totals are the list lengths),
+    // then each query's pairs at its offset (both passes only when the lists are rebuilt; the sums of unchanged
+    // counts give the same offsets)
+    int* cnt_pt = cand_cnt;
+    int* cnt_ee = cand_cnt + NP;
+    int* off_pt = cand_off;
+    int* off_ee = cand_off + NP;
     k_candidates<false><<<grid_for(NP, kQT, 16), kQT, 0, s>>>(q, NP, tri, tri_bvh.child, tri_bvh.nlo, tri_bvh.nhi,
                                                              tri_bvh.llo, tri_bvh.lhi, tri_bvh.vals[0], tri_rc, P.d_hat,
-                                                             skin, cand_pt, (int)cap_cpt, &sc->n_cand_pt, sc);
+                                                             skin, cand_pt, (int)cap_cpt, cnt_pt, nullptr, sc);
     note_launch();
     k_candidates<true><<<grid_for(NE, kQT, 16), kQT, 0, s>>>(q, NE, edge4, edge_bvh.child, edge_bvh.nlo, edge_bvh.nhi,
                                                             edge_bvh.llo, edge_bvh.lhi, edge_bvh.vals[0], edge_rc,
-                                                            P.d_hat, skin, cand_ee, (int)cap_cee, &sc->n_cand_ee, sc);
+                                                            P.d_hat, skin, cand_ee, (int)cap_cee, cnt_ee, nullptr, sc);
+    note_launch();
+    {
+        const size_t si = scan_scratch_ints();
+        ScanJob jobs[2] = {{cnt_pt, off_pt, nullptr, NP, &sc->n_cand_pt, scan_scratch},
+                           {cnt_ee, off_ee, nullptr, NE, &sc->n_cand_ee, scan_scratch + si}};
+        exclusive_scans(jobs, 2, s, &sc->status, std::max(NP, NE));
+        note_launch();
+    }
+    k_candidates<false><<<grid_for(NP, kQT, 16), kQT, 0, s>>>(q, NP, tri, tri_bvh.child, tri_bvh.nlo, tri_bvh.nhi,
+                                                             tri_bvh.llo, tri_bvh.lhi, tri_bvh.vals[0], tri_rc, P.d_hat,
+                                                             skin, cand_pt, (int)cap_cpt, cnt_pt, off_pt, sc);
+    note_launch();
+    k_candidates<true><<<grid_for(NE, kQT, 16), kQT, 0, s>>>(q, NE, edge4, edge_bvh.child, edge_bvh.nlo, edge_bvh.nhi,
+                                                            edge_bvh.llo, edge_bvh.lhi, edge_bvh.vals[0], edge_rc,
+                                                            P.d_hat, skin, cand_ee, (int)cap_cee, cnt_ee, off_ee, sc);
     note_launch();
     k_cand_done<<<grid_for(NP, kT), kT, 0, s>>>(q, q_ref, NP, (int)cap_cpt, (int)cap_cee, sc);
     note_launch();
+    // contacts in candidate order: flags, their prefix sums (the total is the contact count), the list, then each
+    // vertex's contact corners (counted, offsets, filled, sorted)
     const int cap = (int)std::min<size_t>(cap_c, (size_t)P.max_blocks);
     k_filter<<<grid_for((long long)(cap_cpt + cap_cee), kT), kT, 0, s>>>(q, cand_pt, cand_ee, tri, edge4, P.d_hat,
-                                                                        P.ee_classify_thres, c_idx, c_type, cap, sc);
+                                                                        P.ee_classify_thres, cflag, cid, cty, sc);
+    note_launch();
+    exclusive_scan(cflag, cpos, &sc->n_cand_all, 0, &sc->n_contacts_raw, scan_scratch, s, &sc->status,
+                   (long long)(cap_cpt + cap_cee));
     note_launch();
     k_contacts_done<<<1, 1, 0, s>>>(sc, cap, P.max_blocks);
     note_launch();
-    // energy, gradient (coeff -1), Hessian diagonal and hinge blocks (system.py:433-434)
-    launch_energy(q);
-    k_diff_m2gt<<<grid_for(NP, kT), kT, 0, s>>>(q, target, vweight, P.mesh2gt_dist_stiffness, -1.f, NP, grad, hdiag, sc);
+    k_contacts_scatter<<<grid_for((long long)(cap_cpt + cap_cee), kT), kT, 0, s>>>(cflag, cpos, cid, cty, c_idx, c_type,
+                                                                                  c_cnt, sc);
     note_launch();
-    k_diff_elastic<<<grid_for(NT, kT), kT, 0, s>>>(q, tri, el_area, el_invDm, mu, la, -1.f, NT, grad, sc);
+    exclusive_scan(c_cnt, c_off, nullptr, NP + 1, nullptr, scan_scratch, s, &sc->status, NP + 1);
+    note_launch();
+    k_cvert_fill<<<grid_for(4ll * cap_c, kT), kT, 0, s>>>(c_idx, c_off, c_cur, c_tmp, sc);
+    note_launch();
+    k_cvert_rank<<<grid_for(32ll * NP, kT), kT, 0, s>>>(c_off, c_tmp, c_inv, NP, sc);
+    note_launch();
+    // energy, gradient (coeff -1), Hessian diagonal and hinge blocks (system.py:433-434): per-corner parts into
+    // the slot arrays, then summed per vertex
+    launch_energy(q);
+    const size_t nt3 = (size_t)3 * NT, cbase = nt3 + (size_t)4 * NH;
+    k_diff_elastic<<<grid_for(NT, kT), kT, 0, s>>>(q, tri, el_area, el_invDm, mu, la, -1.f, NT, gslot, inv_vs, sc);
     note_launch();
     if (NH) {
         k_diff_hinge<<<grid_for(NH, 128), 128, 0, s>>>(q, hinge, hinge_rest, P.hinge_stiffness, -1.f, NH, hinge_blocks,
-                                                       grad, hdiag, sc);
+                                                       gslot, hslot, inv_vs + nt3, sc);
         note_launch();
         k_spd_project<<<grid_for((NH + 3 * kSpdWarps - 1) / (3 * kSpdWarps), 1, 16), 32 * kSpdWarps, 0, s>>>(
             hinge_blocks, NH, P.spd_max_iters, sc);
         note_launch();
     }
-    k_diff_contact<<<gC, kT, 0, s>>>(q, c_idx, c_type, c_d, sc, P.coll_stiffness, P.d_hat, -1.f, c_dd, grad, hdiag);
+    k_diff_contact<<<gC, kT, 0, s>>>(q, c_idx, c_type, c_d, sc, P.coll_stiffness, P.d_hat, -1.f, c_dd, gslot + cbase,
+                                     hslot + cbase, c_inv);
+    note_launch();
+    VertexSlots S;
+    S.vs_off = vs_off; S.coff = c_off; S.inv_vs = inv_vs; S.cinv = c_inv; S.cbase = (int)cbase;
+    k_gather_grad<<<grid_for((long long)kGather * NP, kT), kT, 0, s>>>(q, target, vweight, P.mesh2gt_dist_stiffness,
+                                                                      -1.f, NP, gslot, hslot, S, grad, hdiag, sc);
     note_launch();
     // Jacobi PCG (cg_solver.py:96-158)
     HvpArgs H;
@@ -2207,6 +2556,7 @@ void Stage3::newton_iteration() {
     H.tri = tri; H.area = el_area; H.invDm = el_invDm; H.mu = mu; H.la = la; H.nt = NT;
     H.hinge = hinge; H.blocks = hinge_blocks; H.nh = NH;
     H.cidx = c_idx; H.cd = c_d; H.cdd = c_dd; H.kappa = P.coll_stiffness; H.d_hat = P.d_hat;
+    H.aslot = aslot; H.S = S;
     const long long elems_all = (long long)NP + NT + NH;
     // the cluster kernel measured slower than the grid-wide one on the 5k-face stage-2 output (fewer threads
     // per element pass), so it runs only when asked for
@@ -2224,7 +2574,7 @@ void Stage3::newton_iteration() {
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         cudaLaunchKernelEx(&cfg, k_cg_cluster, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r, z,
-                           v[0], v[1], Av, P.n_cg_iters, sc);
+                           v[0], v[1], P.n_cg_iters, sc);
         note_launch();
     } else {
         // one cooperative launch: about one thread per element, at most one block per SM (cg_mode 0, 3, 4); or
@@ -2247,16 +2597,16 @@ void Stage3::newton_iteration() {
         CgState* bar = reinterpret_cast<CgState*>(cg_bar);
         if (bt == 64)
             cudaLaunchKernelEx(&cfg, k_cg_solve<64>, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r,
-                               z, v[0], v[1], Av, P.n_cg_iters, sc, partial, bar);
+                               z, v[0], v[1], P.n_cg_iters, sc, partial, bar);
         else if (bt == 512)
             cudaLaunchKernelEx(&cfg, k_cg_solve<512>, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r,
-                               z, v[0], v[1], Av, P.n_cg_iters, sc, partial, bar);
+                               z, v[0], v[1], P.n_cg_iters, sc, partial, bar);
         else if (bt == 256)
             cudaLaunchKernelEx(&cfg, k_cg_solve<256>, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r,
-                               z, v[0], v[1], Av, P.n_cg_iters, sc, partial, bar);
+                               z, v[0], v[1], P.n_cg_iters, sc, partial, bar);
         else
             cudaLaunchKernelEx(&cfg, k_cg_solve<128>, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r,
-                               z, v[0], v[1], Av, P.n_cg_iters, sc, partial, bar);
+                               z, v[0], v[1], P.n_cg_iters, sc, partial, bar);
         note_launch();
     }
     // step clamp, CCD, line search (system.py:441-459)
@@ -2357,6 +2707,25 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     if ((rr = ensure_contacts(std::max<size_t>(std::max<size_t>(1 << 16, cap_c), (size_t)32 * (NP + NE))))) return rr;
     if ((rr = ensure_candidates(std::max<size_t>(1 << 16, (size_t)64 * NP), std::max<size_t>(1 << 16, (size_t)64 * NE))))
         return rr;
+    if ((rr = ensure_slots())) return rr;
+    {
+        // the static parts' positions: each vertex's triangle corners (codes 3f + c) then hinge slots (3 NT + 4h + a)
+        // contiguous at [off[v], off[v + 1]) in ascending code order; list[code] = its position
+        std::vector<int> off((size_t)NP + 1, 0), list((size_t)3 * NT + (size_t)4 * NH);
+        for (int k = 0; k < 3 * NT; ++k) off[hf[k] + 1]++;
+        for (int h = 0; h < NH; ++h) {
+            off[h4[h].x + 1]++; off[h4[h].y + 1]++; off[h4[h].z + 1]++; off[h4[h].w + 1]++;
+        }
+        for (int i = 0; i < NP; ++i) off[i + 1] += off[i];
+        std::vector<int> cur(off.begin(), off.end() - 1);
+        for (int k = 0; k < 3 * NT; ++k) list[k] = cur[hf[k]]++;  // codes visited ascending: each range sorted
+        for (int h = 0; h < NH; ++h) {
+            const int ids[4] = {h4[h].x, h4[h].y, h4[h].z, h4[h].w};
+            for (int a = 0; a < 4; ++a) list[3 * NT + 4 * h + a] = cur[ids[a]]++;
+        }
+        vs_host_off.swap(off);
+        vs_host_list.swap(list);
+    }
     cudaStream_t s = stream;
     cudaMemsetAsync(cg_bar, 0, 64, s);  // the barrier counters of the PCG and of the line search
     cudaEventRecord(ev_in, caller);
@@ -2368,6 +2737,9 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     }
     cudaMemcpyAsync(edge4, e4.data(), NE * sizeof(int4), cudaMemcpyHostToDevice, s);
     if (NH) cudaMemcpyAsync(hinge, h4.data(), NH * sizeof(int4), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(vs_off, vs_host_off.data(), vs_host_off.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    if (!vs_host_list.empty())
+        cudaMemcpyAsync(inv_vs, vs_host_list.data(), vs_host_list.size() * sizeof(int), cudaMemcpyHostToDevice, s);
 
     // normalisation (processing.py:15-21, 57-59)
     k_norm_partial<<<kNormBlocks, kT, 0, s>>>(gt_points, NGP, d_norm + 16);
@@ -2406,11 +2778,14 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     }
     // register_mesh preprocessing (system.py:167-272): Voronoi areas, elastic rest shape, hinge rest state,
     // minimum internal angle
-    double* w64 = reinterpret_cast<double*>(r);  // scratch: r is free until the first solve
-    cudaMemsetAsync(w64, 0, NP * sizeof(double), s);
-    k_voronoi<<<grid_for(NT, kT), kT, 0, s>>>(points, d_norm, tri, NT, w64);
+    // scratch: 3 NT + 4 NH doubles in gslot, free until the first gradient
+    double* wslot = reinterpret_cast<double*>(gslot);
+    cudaMemsetAsync(wslot, 0, ((size_t)3 * NT + (size_t)4 * NH) * sizeof(double), s);
+    // the triangle positions of hslot hold no Hessian part: zero for the whole call
+    cudaMemsetAsync(hslot, 0, ((size_t)3 * NT + (size_t)4 * NH) * sizeof(float4), s);
+    k_voronoi<<<grid_for(NT, kT), kT, 0, s>>>(points, d_norm, tri, NT, inv_vs, wslot);
     note_launch();
-    k_weights_f32<<<grid_for(NP, kT), kT, 0, s>>>(w64, NP, vweight);
+    k_weights_f32<<<grid_for(NP, kT), kT, 0, s>>>(wslot, vs_off, NP, vweight);
     note_launch();
     k_elastic_pre<<<grid_for(NT, kT), kT, 0, s>>>(q_rest, tri, NT, el_area, el_invDm);
     note_launch();

@@ -49,6 +49,7 @@ struct SolverScalars {
     int max_contacts;
     int rebuild;          // candidate lists are rebuilt in this iteration
     int n_cand_pt, n_cand_ee;  // candidate pairs (true counts, may exceed the capacities)
+    int n_cand_all;            // n_cand_pt + n_cand_ee of this iteration's contact filter
     int n_rebuilds;
     long long total_contacts;
 };
@@ -90,6 +91,7 @@ private:
     int ensure(int np, int nt, int ne, int nh, int ngp, int ngt);
     int ensure_contacts(size_t n);
     int ensure_candidates(size_t npt, size_t nee);
+    int ensure_slots();
     void release();
     void drop_graph();
 
@@ -107,7 +109,7 @@ private:
     // simulated mesh
     float4 *q = nullptr, *q_rest = nullptr, *q_prev_newton = nullptr, *p = nullptr;
     float4* q_ref = nullptr;  // positions at the last build of the candidate lists
-    float4 *target = nullptr, *grad = nullptr, *hdiag = nullptr, *r = nullptr, *z = nullptr, *Av = nullptr;
+    float4 *target = nullptr, *grad = nullptr, *hdiag = nullptr, *r = nullptr, *z = nullptr;
     float4* v[2] = {nullptr, nullptr};  // CG search directions, ping-pong
     float* vweight = nullptr;  // Voronoi area
     int4* tri = nullptr;
@@ -127,6 +129,30 @@ private:
     int2* cand_pt = nullptr;
     int2* cand_ee = nullptr;
     size_t cap_cpt = 0, cap_cee = 0;
+    int* cand_cnt = nullptr;  // per query: candidates of the counting pass (points, then edges)
+    int* cand_off = nullptr;  // their exclusive prefix sums (where each query writes)
+    size_t cap_cq = 0;
+    // the contact filter's per-candidate results (flag, prefix sums = contact index, ids, type)
+    int* cflag = nullptr;
+    int* cpos = nullptr;
+    int4* cid = nullptr;
+    int2* cty = nullptr;
+    size_t cap_cf = 0;
+    // per-vertex sums in a fixed order: the per-corner parts (triangle corners 3f + c, hinge slots 3 NT + 4h + a,
+    // contact corners 4b + k) in slot arrays at their positions in their vertex's range (the static ranges first,
+    // the contact ranges after cbase = 3 NT + 4 NH), each range summed in order
+    std::vector<int> vs_host_off, vs_host_list;  // the static ranges as built on the host
+    int* vs_off = nullptr;   // static ranges (triangle corners and hinge slots per vertex), NP + 1 offsets
+    int* inv_vs = nullptr;   // 3 NT + 4 NH: the position of each static code in its vertex's range
+    size_t cap_vs = 0, cap_vso = 0;
+    int* c_cnt = nullptr;    // contact corners per vertex (NP + 1), their offsets and fill cursors
+    int* c_off = nullptr;
+    int* c_cur = nullptr;
+    int* c_tmp = nullptr;    // 4 per contact: the codes filled per vertex, then ranked
+    int* c_inv = nullptr;    // 4 per contact: the position of each contact code in its vertex's range
+    float4 *gslot = nullptr, *hslot = nullptr, *aslot = nullptr;
+    size_t cap_slot = 0;
+    int* scan_scratch = nullptr;  // two scan scratches (exclusive_scans with two jobs)
     float2* partial = nullptr;  // block partials of the grid-wide sums
     void* cg_bar = nullptr;     // grid-barrier state of the cooperative CG kernel
     int coop_max_blocks = 1, n_sm = 1;
