@@ -252,12 +252,50 @@ __global__ void __launch_bounds__(256) k_karras(const RoundCounters* rc, const u
 // Bottom-up boxes over tiles of kTileLeaves consecutive leaves, one thread per leaf. A Karras node covers a
 // contiguous leaf range with its own index at one end, so every node whose range lies inside a tile has its
 // index inside the tile too: those nodes count arrivals and keep their boxes in shared memory (the tile's leaf
-// boxes are staged there as well); a chain that reaches a node whose range leaves the tile continues with
-// global arrival counters (visit[], zeroed by the leaf kernels) and global boxes (nlo/nhi). The second arrival
-// at a node writes its packed record (kPack) and, with kNodes or when the node's parent may lie outside the
-// tile, its box to nlo/nhi. A node's range, children and parent are loaded together before its arrival count.
+// boxes are staged there as well). A chain that reaches a node whose range leaves the tile counts its arrival
+// there in global memory (visit[], zeroed by the leaf kernels), with its own box in nlo/nhi; the second arrival
+// queues the node (upq: count, then nodes) and stops, and k_bottom_up_upper finishes the nodes above the tiles,
+// so a block never waits at its next tile for a chain climbing the upper tree. The second arrival at a node
+// writes its packed record (kPack) and, with kNodes, its box to nlo/nhi. A node's range, children and parent are
+// loaded together before its arrival count.
 constexpr int kTileLeaves = 512;
 constexpr int kTileThreads = kTileLeaves;
+
+// Arrival counts of the bottom-up pass: a release add (the arriving child's box, stored before, becomes visible
+// with the count) and an acquire-release add (the second arrival also sees the first child's box).
+__device__ __forceinline__ int arrive_release(int* p) {
+    int old;
+    asm volatile("atom.release.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+__device__ __forceinline__ int arrive_acq_rel(int* p) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+
+// The packed 64-byte record of node p (both children's boxes, child references, leaf face ids with the query bit).
+__device__ __forceinline__ void write_packed(int p, int2 c, float4 alo, float4 ahi, float4 clo, float4 chi,
+                                             const int* leaf_face, const int* qscan, float4* packed) {
+    int fa = -1, fc = -1;
+    if (c.x < 0) {
+        fa = leaf_face[~c.x];
+        if (qscan && fa >= 0 && qscan[fa + 1] != qscan[fa]) fa |= kQueryBit;
+    }
+    if (c.y < 0) {
+        fc = leaf_face[~c.y];
+        if (qscan && fc >= 0 && qscan[fc + 1] != qscan[fc]) fc |= kQueryBit;
+    }
+    float4* rec = packed + 4 * (size_t)p;
+    alo.w = __int_as_float(c.x);
+    ahi.w = __int_as_float(fa);
+    clo.w = __int_as_float(c.y);
+    chi.w = __int_as_float(fc);
+    rec[0] = alo;
+    rec[1] = ahi;
+    rec[2] = clo;
+    rec[3] = chi;
+}
 
 template <bool kPack, bool kNodes>
 __global__ void __launch_bounds__(kTileThreads, 3) k_bottom_up_tiles(RoundCounters* rc, const int2* child,
@@ -265,7 +303,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_bottom_up_tiles(RoundCounte
                                                                   const int2* range, const float4* llo,
                                                                   const float4* lhi, float4* nlo, float4* nhi, int* visit,
                                                                   const int* leaf_face, const int* qscan, float4* packed,
-                                                                  int* meta_out, const int* active) {
+                                                                  int* meta_out, const int* active, int* upq) {
     __shared__ int svisit[kTileLeaves];
     __shared__ float4 slo[kTileLeaves], shi[kTileLeaves];    // internal nodes a .. b-2
     __shared__ float4 sllo[kTileLeaves], slhi[kTileLeaves];  // leaves a .. b-1
@@ -289,7 +327,6 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_bottom_up_tiles(RoundCounte
         }
         __syncthreads();
         int ref = ~leaf;
-        bool inside = true;  // the chain is still inside the tile
         int guard = 0;
         while (p >= 0) {
             if (++guard > 4096) {
@@ -299,65 +336,72 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_bottom_up_tiles(RoundCounte
             const int2 rg = range[p];
             const int2 c = child[p];
             const int pp = iparent[p];
-            const bool p_in = inside && rg.x >= a && rg.y < b;
-            if (p_in) {
-                __threadfence_block();
-                if (atomicAdd(&svisit[p - a], 1) == 0) break;
-                __threadfence_block();
-            } else {
-                // leaving the tile: the other child's chain reads this child's box from global memory
-                if (ref >= 0 && inside && !kNodes) {
+            if (!(rg.x >= a && rg.y < b)) {
+                // leaving the tile: this child's box goes to global memory for the other child's chain, and the
+                // second arrival queues p for k_bottom_up_upper instead of climbing on, so that no chain through
+                // the upper tree holds this block at the next tile's barrier
+                if (ref >= 0 && !kNodes) {
                     __stcg(&nlo[ref], blo);
                     __stcg(&nhi[ref], bhi);
                 }
-                inside = false;
-                __threadfence();
-                if (atomicAdd(&visit[p], 1) == 0) break;
-                __threadfence();
+                if (arrive_release(&visit[p]) != 0) upq[1 + atomicAdd(upq, 1)] = p;
+                break;
             }
+            __threadfence_block();
+            if (atomicAdd(&svisit[p - a], 1) == 0) break;
+            __threadfence_block();
+            // both children are in this tile
             float4 alo, ahi, clo, chi;
-            if (p_in) {  // both children are in this tile
-                if (c.x < 0) { alo = sllo[~c.x - a]; ahi = slhi[~c.x - a]; }
-                else { alo = slo[c.x - a]; ahi = shi[c.x - a]; }
-                if (c.y < 0) { clo = sllo[~c.y - a]; chi = slhi[~c.y - a]; }
-                else { clo = slo[c.y - a]; chi = shi[c.y - a]; }
-            } else {
-                if (c.x < 0) { alo = __ldcg(&llo[~c.x]); ahi = __ldcg(&lhi[~c.x]); }
-                else { alo = __ldcg(&nlo[c.x]); ahi = __ldcg(&nhi[c.x]); }
-                if (c.y < 0) { clo = __ldcg(&llo[~c.y]); chi = __ldcg(&lhi[~c.y]); }
-                else { clo = __ldcg(&nlo[c.y]); chi = __ldcg(&nhi[c.y]); }
-            }
+            if (c.x < 0) { alo = sllo[~c.x - a]; ahi = slhi[~c.x - a]; }
+            else { alo = slo[c.x - a]; ahi = shi[c.x - a]; }
+            if (c.y < 0) { clo = sllo[~c.y - a]; chi = slhi[~c.y - a]; }
+            else { clo = slo[c.y - a]; chi = shi[c.y - a]; }
             blo = make_float4(fminf(alo.x, clo.x), fminf(alo.y, clo.y), fminf(alo.z, clo.z), 0.f);
             bhi = make_float4(fmaxf(ahi.x, chi.x), fmaxf(ahi.y, chi.y), fmaxf(ahi.z, chi.z), 0.f);
-            if (p_in) {
-                slo[p - a] = blo;
-                shi[p - a] = bhi;
-            }
-            if (kNodes || !p_in) {
+            slo[p - a] = blo;
+            shi[p - a] = bhi;
+            if (kNodes) {
                 __stcg(&nlo[p], blo);
                 __stcg(&nhi[p], bhi);
             }
-            if (kPack) {
-                int fa = -1, fc = -1;
-                if (c.x < 0) {
-                    fa = leaf_face[~c.x];
-                    if (qscan && fa >= 0 && qscan[fa + 1] != qscan[fa]) fa |= kQueryBit;
-                }
-                if (c.y < 0) {
-                    fc = leaf_face[~c.y];
-                    if (qscan && fc >= 0 && qscan[fc + 1] != qscan[fc]) fc |= kQueryBit;
-                }
-                float4* rec = packed + 4 * (size_t)p;
-                alo.w = __int_as_float(c.x);
-                ahi.w = __int_as_float(fa);
-                clo.w = __int_as_float(c.y);
-                chi.w = __int_as_float(fc);
-                rec[0] = alo;
-                rec[1] = ahi;
-                rec[2] = clo;
-                rec[3] = chi;
-            }
+            if (kPack) write_packed(p, c, alo, ahi, clo, chi, leaf_face, qscan, packed);
             ref = p;
+            p = pp;
+        }
+    }
+}
+
+// The nodes above the tiles (their leaf ranges span two tiles or more): each queued node (both children done)
+// takes its box from the children's boxes in global memory, and climbs on as the second arrival at each parent.
+template <bool kPack, bool kNodes>
+__global__ void __launch_bounds__(256) k_bottom_up_upper(RoundCounters* rc, const int2* child, const int* iparent,
+                                                         const float4* llo, const float4* lhi, float4* nlo,
+                                                         float4* nhi, int* visit, const int* leaf_face,
+                                                         const int* qscan, float4* packed, const int* upq,
+                                                         const int* active) {
+    if (active && *active == 0) return;
+    const int nq = upq[0];
+    for (int k = gtid(); k < nq; k += gstride()) {
+        int p = upq[1 + k];
+        int guard = 0;
+        while (p >= 0) {
+            if (++guard > 4096) {
+                atomicOr(&rc->status, kErrIterLimit);
+                break;
+            }
+            const int2 c = child[p];
+            const int pp = iparent[p];
+            float4 alo, ahi, clo, chi;
+            if (c.x < 0) { alo = __ldcg(&llo[~c.x]); ahi = __ldcg(&lhi[~c.x]); }
+            else { alo = __ldcg(&nlo[c.x]); ahi = __ldcg(&nhi[c.x]); }
+            if (c.y < 0) { clo = __ldcg(&llo[~c.y]); chi = __ldcg(&lhi[~c.y]); }
+            else { clo = __ldcg(&nlo[c.y]); chi = __ldcg(&nhi[c.y]); }
+            const float4 blo = make_float4(fminf(alo.x, clo.x), fminf(alo.y, clo.y), fminf(alo.z, clo.z), 0.f);
+            const float4 bhi = make_float4(fmaxf(ahi.x, chi.x), fmaxf(ahi.y, chi.y), fmaxf(ahi.z, chi.z), 0.f);
+            __stcg(&nlo[p], blo);  // the parent's second arrival reads it
+            __stcg(&nhi[p], bhi);
+            if (kPack) write_packed(p, c, alo, ahi, clo, chi, leaf_face, qscan, packed);
+            if (pp < 0 || arrive_acq_rel(&visit[pp]) == 0) break;
             p = pp;
         }
     }
@@ -369,6 +413,22 @@ inline int tile_grid(int n_bound) {
     int g = (n_bound + kTileLeaves - 1) / kTileLeaves;
     if (n_bound >= (1 << 19) && g < 3 * kNumSM) g = 3 * kNumSM;
     return g < 1 ? 1 : g;
+}
+
+// The whole bottom-up pass: the tiles, then the nodes above them.
+template <bool kPack, bool kNodes>
+void bottom_up(BvhBuffers& b, RoundCounters* rc, int n_bound, const int* leaf_face, const int* qscan, int* meta_out,
+               const int* active, cudaStream_t s) {
+    cudaMemsetAsync(b.upq, 0, sizeof(int), s);
+    const int gT = tile_grid(n_bound);
+    k_bottom_up_tiles<kPack, kNodes><<<gT, kTileThreads, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.range, b.llo,
+                                                                 b.lhi, b.nlo, b.nhi, b.visit, leaf_face, qscan,
+                                                                 b.packed, meta_out, active, b.upq);
+    note_launch();
+    const int gU = std::max(1, std::min(gT, 4 * kNumSM));
+    k_bottom_up_upper<kPack, kNodes><<<gU, 256, 0, s>>>(rc, b.child, b.iparent, b.llo, b.lhi, b.nlo, b.nhi, b.visit,
+                                                        leaf_face, qscan, b.packed, b.upq, active);
+    note_launch();
 }
 
 // ---------------------------------------------------------------- localized query
@@ -651,6 +711,7 @@ size_t bvh_bytes(int cap) {
     b += 2 * align256(4 * c);               // iparent, lparent
     b += 4 * align256(16 * c);              // nlo nhi llo lhi
     b += align256(4 * c);                   // visit
+    b += align256(4 * (c + 1));             // upq
     b += align256(4 * 8);                   // scene
     b += align256(4 * scan_scratch_ints());
     b += align256(64 * c);                  // packed internal nodes
@@ -684,6 +745,7 @@ void bvh_carve(BvhBuffers& b, int cap, char* base, bool clear_scan_scratch) {
     b.llo = (float4*)take(16 * c);
     b.lhi = (float4*)take(16 * c);
     b.visit = (int*)take(4 * c);
+    b.upq = (int*)take(4 * (c + 1));
     b.scene = (unsigned*)take(4 * 8);
     b.scan_scratch = (int*)take(4 * scan_scratch_ints());
     b.packed = (float4*)take(64 * c);
@@ -719,16 +781,8 @@ void bvh_build(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
                                                                           meshes->d_count, meshes->root);
         note_launch();
     }
-    const int gT = tile_grid(n_tris_bound);
-    if (nodes)
-        k_bottom_up_tiles<true, true><<<gT, kTileThreads, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.range,
-                                                                  b.llo, b.lhi, b.nlo, b.nhi, b.visit, b.vals[0], qscan,
-                                                                  b.packed, b.meta, nullptr);
-    else
-        k_bottom_up_tiles<true, false><<<gT, kTileThreads, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.range,
-                                                                   b.llo, b.lhi, b.nlo, b.nhi, b.visit, b.vals[0], qscan,
-                                                                   b.packed, b.meta, nullptr);
-    note_launch();
+    if (nodes) bottom_up<true, true>(b, rc, n_tris_bound, b.vals[0], qscan, b.meta, nullptr, s);
+    else bottom_up<true, false>(b, rc, n_tris_bound, b.vals[0], qscan, b.meta, nullptr, s);
 }
 
 __global__ void __launch_bounds__(256) k_refit_leaves(const RoundCounters* rc, const int4* __restrict__ tri,
@@ -749,11 +803,7 @@ void bvh_refit(BvhBuffers& b, const int4* tri, const float4* pos, RoundCounters*
                const int* active) {
     const int gF = grid_for(n_tris_bound, 256);
     k_refit_leaves<<<gF, 256, 0, s>>>(rc, tri, pos, b.vals[0], b.llo, b.lhi, b.visit, active); note_launch();
-    const int gT = tile_grid(n_tris_bound);
-    k_bottom_up_tiles<false, true><<<gT, kTileThreads, 0, s>>>(rc, b.child, b.iparent, b.lparent, b.range, b.llo,
-                                                               b.lhi, b.nlo, b.nhi, b.visit, nullptr, nullptr, nullptr,
-                                                               nullptr, active);
-    note_launch();
+    bottom_up<false, true>(b, rc, n_tris_bound, nullptr, nullptr, nullptr, active, s);
 }
 
 __global__ void __launch_bounds__(256) k_reuse_leaves(RoundCounters* rc, const int4* __restrict__ tri,
@@ -797,10 +847,7 @@ void bvh_refit_faces(BvhBuffers& b, const int4* tri, const float4* pos, RoundCou
     k_boxes<<<gF, 256, 0, s>>>(tri, pos, rc, b.box_lo, b.box_hi, b.live_scan, b.scene, 1); note_launch();
     k_reuse_leaves<<<gF, 256, 0, s>>>(rc, tri, b.box_lo, b.box_hi, next_round ? (const int*)b.keys[1] : nullptr,
                                       b.vals[0], b.llo, b.lhi, b.visit, b.meta); note_launch();
-    k_bottom_up_tiles<true, false><<<tile_grid(n_tris_bound), kTileThreads, 0, s>>>(
-        rc, b.child, b.iparent, b.lparent, b.range, b.llo, b.lhi, b.nlo, b.nhi, b.visit, b.vals[0], qscan,
-        b.packed, b.meta, nullptr);
-    note_launch();
+    bottom_up<true, false>(b, rc, n_tris_bound, b.vals[0], qscan, b.meta, nullptr, s);
 }
 
 void bvh_remap(BvhBuffers& b, const int* fscan, int n_tris_bound, cudaStream_t s) {

@@ -23,6 +23,7 @@ struct BvhBuffers {
     float4* llo = nullptr;             // leaf boxes in sorted order
     float4* lhi = nullptr;
     int* visit = nullptr;              // bottom-up arrival counters
+    int* upq = nullptr;                // [0] count, then the nodes above the tiles queued by the bottom-up pass
     unsigned* scene = nullptr;         // scene bounds as order-preserving uints (6)
     // internal nodes packed for traversal, 64 B each: {lo_a, hi_a, lo_b, hi_b} with the boxes of both children;
     // lo.w = child reference (>= 0 internal node, < 0 leaf ~i), hi.w = the leaf's face id (or -1), as int bits
