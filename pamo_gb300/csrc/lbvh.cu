@@ -16,6 +16,7 @@ namespace pamo {
 namespace {
 
 constexpr int kSortTiles = 4 * kNumSM;
+constexpr size_t kExactQueue = 1 << 20;  // pairs queued for the float64 pass (the rest are decided in place)
 constexpr int kSortThreads = 256;
 constexpr int kQueryThreads = 128;
 constexpr int kStackDepth = 64;  // enough for any tree (depth <= 62 + 1)
@@ -658,21 +659,80 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse_redo(const float4* _
     if ((threadIdx.x & 31) == 0 && exact) atomicAdd(&rc->n_exact, (unsigned long long)exact);
 }
 
-__global__ void __launch_bounds__(128, 6) k_pairs(const int4* __restrict__ tri, const float4* __restrict__ pos,
+// k_pairs decides every listed pair by the float certificates; each order of a pair they cannot decide (the float64
+// path, a few pairs in a thousand) is queued in xq, and k_pairs_exact runs those one per thread spread over every SM
+// (decided where they were listed, they clustered in a few warps and the float64 pipes of a few SMs set the time).
+// An order that finds the queue full is decided in place. Either way it sets the same flags.
+__global__ void __launch_bounds__(128, 8) k_pairs(const int4* __restrict__ tri, const float4* __restrict__ pos,
                                                const int2* __restrict__ pair_list, int pair_cap, unsigned char* hit,
-                                               RoundCounters* rc, float eps) {
+                                               RoundCounters* rc, float eps, int4* xq, int xq_cap, int* xq_count) {
     const int n = min(rc->pad[1], pair_cap);
     unsigned exact = 0;
     for (int i = gtid(); i < n; i += gstride()) {
-        const int2 p = pair_list[i];
-        if (p.x < 0) continue;  // an unused slot of a chunk
-        if (decide_pair(p.x, p.y, tri, pos, eps, exact)) {
-            hit[p.x] = 1;
-            hit[p.y] = 1;
+        const int2 pr = pair_list[i];
+        if (pr.x < 0) continue;  // an unused slot of a chunk
+        const int f = pr.x, g = pr.y;
+        const int4 qt = tri[f], gt = tri[g];
+        // two or three shared vertex indices: no intersection in either order (pair_certainly_disjoint), decided
+        // before the positions are loaded (edge-adjacent faces are about a quarter of the candidate pairs)
+        const int shared = (qt.x == gt.x) + (qt.x == gt.y) + (qt.x == gt.z) + (qt.y == gt.x) + (qt.y == gt.y) +
+                           (qt.y == gt.z) + (qt.z == gt.x) + (qt.z == gt.y) + (qt.z == gt.z);
+        if (shared >= 2) continue;
+        const float4 q0 = pos[qt.x], q1 = pos[qt.y], q2 = pos[qt.z];
+        const float4 g0 = pos[gt.x], g1 = pos[gt.y], g2 = pos[gt.z];
+        PairGeom ga, gb;
+        pair_geom(g0, g1, g2, gt, q0, q1, q2, qt, ga);  // reference order: the hit is "current"
+        pair_geom(q0, q1, q2, qt, g0, g1, g2, gt, gb);  // the order seen from g's own query
+        const bool need_a = !pair_certainly_disjoint(ga);
+        const bool need_b = !pair_certainly_disjoint(gb);
+        if (!need_a && !need_b) continue;
+        exact += (unsigned)need_a + (unsigned)need_b;
+        // one queue slot per order, taken for the whole warp by one atomic
+        const unsigned am = __activemask();
+        const int lane = threadIdx.x & 31, leader = __ffs(am) - 1;
+        const unsigned ma = __ballot_sync(am, need_a), mb = __ballot_sync(am, need_b);
+        int base = 0;
+        if (lane == leader) base = atomicAdd(xq_count, __popc(ma) + __popc(mb));
+        base = __shfl_sync(am, base, leader);
+        const unsigned lower = (1u << lane) - 1u;
+        const int at_a = base + __popc(ma & lower), at_b = base + __popc(ma) + __popc(mb & lower);
+        bool h = false;
+        if (need_a) {
+            if (at_a < xq_cap) xq[at_a] = make_int4(f, g, 1, 0);
+            else h = pair_decide_exact(g0, g1, g2, gt, q0, q1, q2, qt, eps);
+        }
+        if (need_b) {
+            if (at_b < xq_cap) xq[at_b] = make_int4(f, g, 2, 0);
+            else if (!h) h = pair_decide_exact(q0, q1, q2, qt, g0, g1, g2, gt, eps);
+        }
+        if (h) {
+            hit[f] = 1;
+            hit[g] = 1;
         }
     }
     for (int o = 16; o > 0; o >>= 1) exact += __shfl_xor_sync(0xffffffffu, exact, o);
     if ((threadIdx.x & 31) == 0 && exact) atomicAdd(&rc->n_exact, (unsigned long long)exact);
+}
+
+// The queued pairs, one per thread, consecutive pairs on different SMs (block-cyclic: item k goes to block
+// k mod blocks).
+__global__ void __launch_bounds__(64) k_pairs_exact(const int4* __restrict__ tri, const float4* __restrict__ pos,
+                                                    const int4* __restrict__ xq, int xq_cap,
+                                                    const int* __restrict__ xq_count, unsigned char* hit, float eps) {
+    const int n = min(*xq_count, xq_cap);
+    for (long long k = (long long)threadIdx.x * gridDim.x + blockIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const int4 e = xq[k];
+        const int f = e.x, g = e.y;
+        const int4 qt = tri[f], gt = tri[g];
+        const float4 q0 = pos[qt.x], q1 = pos[qt.y], q2 = pos[qt.z];
+        const float4 g0 = pos[gt.x], g1 = pos[gt.y], g2 = pos[gt.z];
+        const bool h = e.z == 1 ? pair_decide_exact(g0, g1, g2, gt, q0, q1, q2, qt, eps)
+                                : pair_decide_exact(q0, q1, q2, qt, g0, g1, g2, gt, eps);
+        if (h) {
+            hit[f] = 1;
+            hit[g] = 1;
+        }
+    }
 }
 
 // The subtree root of each mesh: its live faces are the leaves [live_scan[f0], live_scan[f0 + nf]) of a tree built
@@ -712,6 +772,7 @@ size_t bvh_bytes(int cap) {
     b += 4 * align256(16 * c);              // nlo nhi llo lhi
     b += align256(4 * c);                   // visit
     b += align256(4 * (c + 1));             // upq
+    b += align256(16 * std::min<size_t>(c, kExactQueue) + 16);  // xq and its count
     b += align256(4 * 8);                   // scene
     b += align256(4 * scan_scratch_ints());
     b += align256(64 * c);                  // packed internal nodes
@@ -746,6 +807,9 @@ void bvh_carve(BvhBuffers& b, int cap, char* base, bool clear_scan_scratch) {
     b.lhi = (float4*)take(16 * c);
     b.visit = (int*)take(4 * c);
     b.upq = (int*)take(4 * (c + 1));
+    b.xq_cap = (int)std::min<size_t>(c, kExactQueue);
+    b.xq = (int4*)take(16 * (size_t)b.xq_cap + 16);
+    b.xq_count = reinterpret_cast<int*>(b.xq + b.xq_cap);
     b.scene = (unsigned*)take(4 * 8);
     b.scan_scratch = (int*)take(4 * scan_scratch_ints());
     b.packed = (float4*)take(64 * c);
@@ -879,7 +943,11 @@ void bvh_query(const BvhBuffers& b, const int4* tri, const float4* pos, const in
     k_traverse_list<<<grid_for(n_query_bound, kQueryThreads, blocks_per_sm), kQueryThreads, 0, s>>>(
         b.packed, b.box_lo, b.box_hi, b.vals[1], pair_list, pair_cap, rc, b.visit, fmesh, mesh_root);
     note_launch();
-    k_pairs<<<grid_for((long long)pair_cap, 128, 16), 128, 0, s>>>(tri, pos, pair_list, pair_cap, hit, rc, eps);
+    cudaMemsetAsync(b.xq_count, 0, sizeof(int), s);
+    k_pairs<<<grid_for((long long)pair_cap, 128, 16), 128, 0, s>>>(tri, pos, pair_list, pair_cap, hit, rc, eps, b.xq,
+                                                                   b.xq_cap, b.xq_count);
+    note_launch();
+    k_pairs_exact<<<4 * kNumSM, 64, 0, s>>>(tri, pos, b.xq, b.xq_cap, b.xq_count, hit, eps);
     note_launch();
     k_traverse_redo<<<grid_for(n_query_bound, kQueryThreads, 4), kQueryThreads, 0, s>>>(
         b.packed, b.box_lo, b.box_hi, tri, pos, b.vals[1], hit, rc, eps, b.visit, fmesh, mesh_root);

@@ -24,6 +24,9 @@ struct BvhBuffers {
     float4* lhi = nullptr;
     int* visit = nullptr;              // bottom-up arrival counters
     int* upq = nullptr;                // [0] count, then the nodes above the tiles queued by the bottom-up pass
+    int4* xq = nullptr;                // candidate pairs for the float64 pass (f, g, orders) and their count
+    int* xq_count = nullptr;
+    int xq_cap = 0;
     unsigned* scene = nullptr;         // scene bounds as order-preserving uints (6)
     // internal nodes packed for traversal, 64 B each: {lo_a, hi_a, lo_b, hi_b} with the boxes of both children;
     // lo.w = child reference (>= 0 internal node, < 0 leaf ~i), hi.w = the leaf's face id (or -1), as int bits
