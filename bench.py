@@ -39,8 +39,9 @@ CONFIGS = {
 }
 STAGE3_STEPS = 5  # PaMO.run's process(..., 5) (simp_cuda/pamo/__init__.py:168-176)
 # DRAM bytes (read + write) per launch of the roofline kernel, from one ncu capture of the same workload
-# (dram__bytes_read.sum + dram__bytes_write.sum averaged over its launches); null where none was taken
-NCU_DRAM_BYTES_PER_LAUNCH = {"plain_large": {"edge_cost": 253243523.8}}
+# (dram__bytes_read.sum + dram__bytes_write.sum, a single-pass metric set, over all 101 launches of one job,
+# averaged); null where none was taken
+NCU_DRAM_BYTES_PER_LAUNCH = {"plain_large": {"edge_cost": 205320420.1}}
 THRESHOLD, TOLERANCE = 1e-3, 4
 L2_FLUSH_BYTES = 512 << 20
 
@@ -682,6 +683,8 @@ def main():
     ap.add_argument("--requests", type=int, default=2000, help="requests for --config serve")
     ap.add_argument("--one-job", action="store_true",
                     help="run one job of the configuration and exit (for profiler captures; prints no JSON)")
+    ap.add_argument("--cg-mode", type=int, default=None,
+                    help="stage-3 PCG launch shape (the Stage3System option cg_mode; default: the tuned one)")
     args = ap.parse_args()
     if args.config == "batch256":
         return run_batch(args)
@@ -717,6 +720,8 @@ def main():
         from pamo_gb300 import safe_project
 
         s3 = safe_project.Stage3System(None, dev)
+        if args.cg_mode is not None:
+            s3.set("cg_mode", args.cg_mode)
         gt_v = torch.from_numpy(v.astype(np.float64)).to(dev)  # the input mesh is the projection's GT
 
     def barrier():

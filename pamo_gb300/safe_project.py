@@ -81,6 +81,11 @@ class Stage3System:
     def clear(self):
         """Kept for the reference's API (system.clear()); buffers are reused as they are."""
 
+    def set(self, name: str, value) -> None:
+        """An execution knob of the solver that keeps the method (pamo_stage3_set_param): use_cuda_graph, ccd_fp64,
+        cg_mode (PCG launch shape), ls_mode (line search launch shape)."""
+        self._check(self._lib.pamo_stage3_set_param(self._h, name.encode(), float(value)), f"set {name}")
+
     def _apply_config(self):
         cfg = tuple((f.name, getattr(self.config, f.name)) for f in fields(self.config))
         if cfg == self._applied:
