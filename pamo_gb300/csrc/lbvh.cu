@@ -484,11 +484,20 @@ __device__ __forceinline__ bool box_overlap4(float4 qlo, float4 qhi, float4 lo, 
 
 // First walk: candidate pairs go to the pair list. The loop is flat: a thread whose query is done takes its
 // next query in the same iteration in which the other lanes of its warp take their next node, so the lanes
-// stay busy until the warp runs out of queries. A query whose pair does not fit the list, or whose deferred
-// siblings do not fit the short stack, stops and is marked in redo[qi] (and counted in rc->pad[3]).
+// stay busy until the warp runs out of queries. From then on, a lane without work takes the bottom entry of the
+// pending stack of a lane that has some (the subtree nearest the root, the largest), together with that lane's query
+// face and box, so that a few long walks are shared by the warp instead of setting the launch's time. A walk whose
+// pair does not fit the list, or whose deferred siblings do not fit the short stack, stops and marks its query in
+// redo[] (counted in rc->pad[3]) for the second walk.
 // With fmesh, a query walks only the subtree of its own mesh (mesh_root; < 0: the mesh has one leaf, no pair).
 __device__ __forceinline__ int query_root(int f, const int* __restrict__ fmesh, const int* __restrict__ mesh_root) {
     return fmesh ? mesh_root[fmesh[f]] : 0;
+}
+
+// the lane of the r-th set bit of m (r < popc(m))
+__device__ __forceinline__ int nth_lane(unsigned m, int r) {
+    for (int k = 0; k < r; ++k) m &= m - 1u;
+    return __ffs(m) - 1;
 }
 
 __global__ void __launch_bounds__(kQueryThreads) k_traverse_list(const float4* __restrict__ packed,
@@ -506,24 +515,68 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse_list(const float4* _
     // each lane fills its own chunk of kPairChunk list slots, so that one atomic on the list length serves
     // many pairs (a single counter is an L2 hot spot); unused slots of a lane's last chunk are set to -1
     const int lane = threadIdx.x & 31;
+    const unsigned lower = (1u << lane) - 1u;
     int cbase = -1, cused = kPairChunk;
-    int qi = gtid() - gstride();
-    int f = 0, node = -1, sp = 0, guard = 0;
+    int qi = gtid() - gstride();  // this lane's query iterator
+    int wq = -1;                  // the query of the current walk (the lane's own or a shared one)
+    bool supply = true;           // this lane may still get queries of its own
+    int f = 0, node = -1, sp = 0, bot = 0, guard = 0;  // pending entries: stack[bot .. sp)
     float4 qlo = make_float4(0.f, 0.f, 0.f, 0.f), qhi = qlo;
     while (true) {
-        if (node < 0) {
+        if (node < 0 && supply) {
             qi += gstride();
-            if (qi >= nq) break;
-            redo[qi] = 0;
-            if (empty) continue;
-            f = qsorted[qi];
-            node = query_root(f, fmesh, mesh_root);
-            if (node < 0) continue;
-            qlo = box_lo[f];
-            qhi = box_hi[f];
-            sp = 0;
-            guard = 0;
+            if (qi >= nq) {
+                supply = false;
+            } else {
+                redo[qi] = 0;
+                if (!empty) {
+                    f = qsorted[qi];
+                    node = query_root(f, fmesh, mesh_root);
+                    if (node >= 0) {
+                        wq = qi;
+                        qlo = box_lo[f];
+                        qhi = box_hi[f];
+                        sp = bot = 0;
+                        guard = 0;
+                    }
+                }
+            }
         }
+        // sharing, once lanes are out of queries (every lane takes part: the shuffles need the whole warp)
+        const bool idle = node < 0 && !supply;
+        const unsigned I = __ballot_sync(0xffffffffu, idle);
+        if (I == 0xffffffffu) break;
+        const unsigned D = __ballot_sync(0xffffffffu, node >= 0 && sp > bot);
+        if (I != 0u && D != 0u) {
+            int partner = -1;
+            if (idle) {
+                const int r = __popc(I & lower);
+                if (r < __popc(D)) partner = nth_lane(D, r);
+            } else if ((D >> lane) & 1u) {
+                const int r = __popc(D & lower);
+                if (r < __popc(I)) partner = nth_lane(I, r);
+            }
+            int give = -1;
+            if (!idle && partner >= 0) give = stack[bot++][threadIdx.x];
+            const int src = (idle && partner >= 0) ? partner : lane;
+            const int g_node = __shfl_sync(0xffffffffu, give, src);
+            const int g_f = __shfl_sync(0xffffffffu, f, src);
+            const int g_wq = __shfl_sync(0xffffffffu, wq, src);
+            const float4 g_lo = make_float4(__shfl_sync(0xffffffffu, qlo.x, src), __shfl_sync(0xffffffffu, qlo.y, src),
+                                            __shfl_sync(0xffffffffu, qlo.z, src), 0.f);
+            const float4 g_hi = make_float4(__shfl_sync(0xffffffffu, qhi.x, src), __shfl_sync(0xffffffffu, qhi.y, src),
+                                            __shfl_sync(0xffffffffu, qhi.z, src), 0.f);
+            if (idle && partner >= 0) {
+                node = g_node;
+                f = g_f;
+                wq = g_wq;
+                qlo = g_lo;
+                qhi = g_hi;
+                sp = bot = 0;
+                guard = 0;
+            }
+        }
+        if (node < 0) continue;
         if (++guard > (1 << 22)) {
             atomicOr(&rc->status, kErrIterLimit);
             node = -1;
@@ -550,7 +603,7 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse_list(const float4* _
                     int b = 0;
                     if (lane == leader) b = atomicAdd(n_list, kPairChunk * __popc(am));
                     b = __shfl_sync(am, b, leader);
-                    cbase = b + kPairChunk * __popc(am & ((1u << lane) - 1u));
+                    cbase = b + kPairChunk * __popc(am & lower);
                     cused = 0;
                 }
                 const int at = cbase + cused++;
@@ -565,6 +618,11 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse_list(const float4* _
             }
         }
         if (nn == 2) {
+            if (sp >= kShortStack && bot > 0) {  // entries given away at the bottom: move the rest down
+                for (int k = bot; k < sp; ++k) stack[k - bot][threadIdx.x] = stack[k][threadIdx.x];
+                sp -= bot;
+                bot = 0;
+            }
             if (sp >= kShortStack) {
                 abandon = true;
             } else {
@@ -574,10 +632,10 @@ __global__ void __launch_bounds__(kQueryThreads) k_traverse_list(const float4* _
         } else if (nn == 1) {
             node = next[0];
         } else {
-            node = sp > 0 ? stack[--sp][threadIdx.x] : -1;
+            node = sp > bot ? stack[--sp][threadIdx.x] : -1;
         }
         if (abandon) {
-            redo[qi] = 1;
+            redo[wq] = 1;
             atomicAdd(&rc->pad[3], 1);
             node = -1;
         }
