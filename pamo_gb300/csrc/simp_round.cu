@@ -452,8 +452,20 @@ __device__ __forceinline__ bool ring_pass(int w, int other, V3 vm, const int* __
         const float l12 = (wy || wz) ? vnorm(vsub(n1, n2)) : g.y;
         const float l20 = (wz || wx) ? vnorm(vsub(n2, n0)) : g.z;
         const float sh = (l01 + l12 + l20) / 2;  // triangle_area (Heron), :368-375
-        const float area = sqrtf(sh * (sh - l01) * (sh - l12) * (sh - l20));
-        acc_add(qa, skinny_term<kLegacy, kPow>(k4s3, area, l01, l12, l20));
+        const float heron = sh * (sh - l01) * (sh - l12) * (sh - l20);
+        // A face with area >= l01^2 / (4 sqrt 3) makes the first quotient of the skinny sum at least 1, so the clamped
+        // sum is 1 and the term exactly 0. Most faces are that fat; it is proven here from Heron's product against
+        // (l01^2 / (4 sqrt 3))^2 with a 1e-4 relative margin (far above the few ulps of rounding on either side, the
+        // 2-ulp difference of the device's pow and the double-precision constant of the legacy sum), which skips the
+        // square root and the division. A bound that is not a normal positive number, or a NaN, takes the full path.
+        const float tb = l01 * l01 * 0.144337567f;  // l01^2 / (4 sqrt 3)
+        const float tb2 = tb * tb;
+        if (tb2 > 1e-30f && tb2 < 1e30f && heron >= tb2 * 1.0001f) {
+            acc_add(qa, 0.0f);  // the saturated term
+        } else {
+            const float area = sqrtf(heron);
+            acc_add(qa, skinny_term<kLegacy, kPow>(k4s3, area, l01, l12, l20));
+        }
         ntri++;
     }
     return true;
