@@ -35,6 +35,13 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// float32 -> float64, on the device (the request's input points, already there for stage 2, become the stage-3
+// target without a host round trip)
+__global__ void k_widen(const float* __restrict__ in, long long n, double* out) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
 double ms_between(Clock::time_point a, Clock::time_point b) {
     return std::chrono::duration<double, std::milli>(b - a).count();
 }
@@ -358,7 +365,8 @@ struct pamo_server {
 
     // stage 3 of a finished stage-2 job (simp_cuda/pamo/__init__.py:165-176): the stage-2 mesh through trimesh's
     // processing, then the projection onto the request's own input mesh; float64 positions
-    int stage3_job(Worker& w, pamo_stage3*& s3, Request& q, const int32_t* d_gt_tris, const float* d_res_p,
+    int stage3_job(Worker& w, pamo_stage3*& s3, Request& q, const float* d_gt_points, const int32_t* d_gt_tris,
+                   const float* d_res_p,
                    const int32_t* d_res_t, int32_t onp, int32_t ont, double*& gp, size_t& cgp, double*& sp,
                    size_t& csp, int32_t*& st, size_t& cst) {
         int r;
@@ -378,11 +386,11 @@ struct pamo_server {
             q.out_points.assign(vm.begin(), vm.end());
             return PAMO_OK;
         }
-        std::vector<double> gt(q.points.begin(), q.points.end());
         if ((r = ensure_dev(gp, cgp, 3 * ngp)) || (r = ensure_dev(sp, csp, 6 * std::max<size_t>(nm, 1))) ||
             (r = ensure_dev(st, cst, 3 * std::max<size_t>(nfm, 1))))
             return r;
-        cudaMemcpyAsync(gp, gt.data(), gt.size() * sizeof(double), cudaMemcpyHostToDevice, w.stream);
+        const long long ng = 3 * (long long)ngp;
+        k_widen<<<(unsigned)std::min<long long>((ng + 255) / 256, 1024), 256, 0, w.stream>>>(d_gt_points, ng, gp);
         cudaMemcpyAsync(sp, vm.data(), vm.size() * sizeof(double), cudaMemcpyHostToDevice, w.stream);
         cudaMemcpyAsync(st, fm.data(), fm.size() * sizeof(int32_t), cudaMemcpyHostToDevice, w.stream);
         double* out = sp + 3 * nm;
@@ -451,7 +459,7 @@ struct pamo_server {
                             q->stage3 ? rp : dp, q->stage3 ? rt : dt, &onp, &ont, &q->rounds, q->err);
             }
             if (!r && q->stage3) {
-                r = stage3_job(w, s3, *q, dt, rp, rt, onp, ont, gp, cgp, sp, csp, st, cst);
+                r = stage3_job(w, s3, *q, dp, dt, rp, rt, onp, ont, gp, cgp, sp, csp, st, cst);
             } else if (!r) {
                 q->out_points.resize((size_t)onp * 3);
                 q->out_tris.resize((size_t)ont * 3);
