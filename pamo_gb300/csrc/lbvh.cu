@@ -298,6 +298,37 @@ __device__ __forceinline__ void write_packed(int p, int2 c, float4 alo, float4 a
     rec[3] = chi;
 }
 
+// From node p, both of whose children are done: its box from the children's boxes in global memory (and its
+// packed record), then on to the parent as long as this is the parent's second arrival.
+template <bool kPack>
+__device__ void climb_from(RoundCounters* rc, int p, const int2* child, const int* iparent, const float4* llo,
+                           const float4* lhi, float4* nlo, float4* nhi, int* visit, const int* leaf_face,
+                           const int* qscan, float4* packed) {
+    {
+        int guard = 0;
+        while (p >= 0) {
+            if (++guard > 4096) {
+                atomicOr(&rc->status, kErrIterLimit);
+                break;
+            }
+            const int2 c = child[p];
+            const int pp = iparent[p];
+            float4 alo, ahi, clo, chi;
+            if (c.x < 0) { alo = __ldcg(&llo[~c.x]); ahi = __ldcg(&lhi[~c.x]); }
+            else { alo = __ldcg(&nlo[c.x]); ahi = __ldcg(&nhi[c.x]); }
+            if (c.y < 0) { clo = __ldcg(&llo[~c.y]); chi = __ldcg(&lhi[~c.y]); }
+            else { clo = __ldcg(&nlo[c.y]); chi = __ldcg(&nhi[c.y]); }
+            const float4 blo = make_float4(fminf(alo.x, clo.x), fminf(alo.y, clo.y), fminf(alo.z, clo.z), 0.f);
+            const float4 bhi = make_float4(fmaxf(ahi.x, chi.x), fmaxf(ahi.y, chi.y), fmaxf(ahi.z, chi.z), 0.f);
+            __stcg(&nlo[p], blo);  // the parent's second arrival reads it
+            __stcg(&nhi[p], bhi);
+            if (kPack) write_packed(p, c, alo, ahi, clo, chi, leaf_face, qscan, packed);
+            if (pp < 0 || arrive_acq_rel(&visit[pp]) == 0) break;
+            p = pp;
+        }
+    }
+}
+
 template <bool kPack, bool kNodes>
 __global__ void __launch_bounds__(kTileThreads, 3) k_bottom_up_tiles(RoundCounters* rc, const int2* child,
                                                                   const int* iparent, const int* lparent,
@@ -311,6 +342,9 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_bottom_up_tiles(RoundCounte
     if (active && *active == 0) return;
     const int n = rc->n_live;
     if (kPack && blockIdx.x == 0 && threadIdx.x == 0) meta_out[0] = n;
+    // one tile per block (a single wave): a chain leaving its tile climbs on here, nothing waits for it; several
+    // tiles per block: the nodes above the tiles are queued for k_bottom_up_upper
+    const bool climb = (long long)gridDim.x * kTileLeaves >= n;
     // tiles in a block-stride loop: the leaf count is read on the device and may exceed the launch's bound
     for (int a = blockIdx.x * kTileLeaves; a < n; a += gridDim.x * kTileLeaves) {
         const int b = min(a + kTileLeaves, n);  // leaves [a, b)
@@ -338,14 +372,18 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_bottom_up_tiles(RoundCounte
             const int2 c = child[p];
             const int pp = iparent[p];
             if (!(rg.x >= a && rg.y < b)) {
-                // leaving the tile: this child's box goes to global memory for the other child's chain, and the
-                // second arrival queues p for k_bottom_up_upper instead of climbing on, so that no chain through
-                // the upper tree holds this block at the next tile's barrier
+                // leaving the tile: this child's box goes to global memory for the other child's chain; with
+                // several tiles per block the second arrival queues p for k_bottom_up_upper instead of climbing
+                // on, so that no chain through the upper tree holds this block at the next tile's barrier
                 if (ref >= 0 && !kNodes) {
                     __stcg(&nlo[ref], blo);
                     __stcg(&nhi[ref], bhi);
                 }
-                if (arrive_release(&visit[p]) != 0) upq[1 + atomicAdd(upq, 1)] = p;
+                if (!climb) {
+                    if (arrive_release(&visit[p]) != 0) upq[1 + atomicAdd(upq, 1)] = p;
+                } else if (arrive_acq_rel(&visit[p]) != 0) {
+                    climb_from<kPack>(rc, p, child, iparent, llo, lhi, nlo, nhi, visit, leaf_face, qscan, packed);
+                }
                 break;
             }
             __threadfence_block();
@@ -382,30 +420,8 @@ __global__ void __launch_bounds__(256) k_bottom_up_upper(RoundCounters* rc, cons
                                                          const int* active) {
     if (active && *active == 0) return;
     const int nq = upq[0];
-    for (int k = gtid(); k < nq; k += gstride()) {
-        int p = upq[1 + k];
-        int guard = 0;
-        while (p >= 0) {
-            if (++guard > 4096) {
-                atomicOr(&rc->status, kErrIterLimit);
-                break;
-            }
-            const int2 c = child[p];
-            const int pp = iparent[p];
-            float4 alo, ahi, clo, chi;
-            if (c.x < 0) { alo = __ldcg(&llo[~c.x]); ahi = __ldcg(&lhi[~c.x]); }
-            else { alo = __ldcg(&nlo[c.x]); ahi = __ldcg(&nhi[c.x]); }
-            if (c.y < 0) { clo = __ldcg(&llo[~c.y]); chi = __ldcg(&lhi[~c.y]); }
-            else { clo = __ldcg(&nlo[c.y]); chi = __ldcg(&nhi[c.y]); }
-            const float4 blo = make_float4(fminf(alo.x, clo.x), fminf(alo.y, clo.y), fminf(alo.z, clo.z), 0.f);
-            const float4 bhi = make_float4(fmaxf(ahi.x, chi.x), fmaxf(ahi.y, chi.y), fmaxf(ahi.z, chi.z), 0.f);
-            __stcg(&nlo[p], blo);  // the parent's second arrival reads it
-            __stcg(&nhi[p], bhi);
-            if (kPack) write_packed(p, c, alo, ahi, clo, chi, leaf_face, qscan, packed);
-            if (pp < 0 || arrive_acq_rel(&visit[pp]) == 0) break;
-            p = pp;
-        }
-    }
+    for (int k = gtid(); k < nq; k += gstride())
+        climb_from<kPack>(rc, upq[1 + k], child, iparent, llo, lhi, nlo, nhi, visit, leaf_face, qscan, packed);
 }
 
 // blocks for k_bottom_up_tiles: a tile per block up to the resident count (the bound may be capped below the
