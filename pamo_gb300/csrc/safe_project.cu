@@ -1719,6 +1719,50 @@ struct CgState {
     unsigned count;  // grid_barrier's counter, zeroed before each stage-3 run
 };
 
+// The same solve as two ordinary launches per iteration (cg_mode 7), for when a cooperative launch, which needs its
+// whole grid resident at once, would wait for other streams' work to drain (many solves at a time on one GPU): each
+// kernel is one phase of k_cg_solve with the same grid, threads and elements, and its block partials are summed by the
+// last block in block order (grid_sum_finish) instead of by every block after a grid barrier, so the scalars and the
+// iterates are the same. The scalars live in sc (z_r, z_r_last, v_A_v).
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads) k_cg_start(const float4* __restrict__ grad, const float4* __restrict__ hd,
+                                                       int np, float4* p, float4* r, float4* z, float4* v0,
+                                                       SolverScalars* sc, float2* partial) {
+    if (sc->abort) return;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    grid_sum_finish(cg_init_vertices(grad, hd, np, p, r, z, v0, tid, nthreads), partial, &sc->red_count, &sc->z_r,
+                    nullptr);
+}
+
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads) k_cg_product(const float4* __restrict__ x, HvpArgs A,
+                                                         const float4* __restrict__ z, const float4* __restrict__ vin,
+                                                         float4* vout, int it, SolverScalars* sc, float2* partial) {
+    if (sc->abort) return;
+    const int nc = sc->n_contacts;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    const float s_dir = it == 0 ? 0.f : sc->z_r / sc->z_r_last;
+    const int4 ids0 = element_ids(A, nc, tid);
+    const int4 at0 = element_slots(A, nc, tid);
+    grid_sum_finish(hvp_elements(x, A, z, vin, vout, s_dir, nc, tid, nthreads, ids0, at0), partial, &sc->red_count,
+                    &sc->v_A_v, nullptr);
+}
+
+template <int kThreads>
+__global__ void __launch_bounds__(kThreads) k_cg_update(HvpArgs A, const float4* __restrict__ v,
+                                                        const float4* __restrict__ hd, float4* p, float4* r, float4* z,
+                                                        SolverScalars* sc, float2* partial) {
+    if (sc->abort) return;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+    const PrzLanes L = prz_lanes(tid, nthreads, A.np);
+    const VRange R0 = vertex_range(A.S, L.group < A.np ? L.group : 0, L.group < A.np);
+    const PrzVertex pre = prz_load(A, v, hd, p, r, L.group < A.np ? L.group : 0, L.group < A.np, L, R0);
+    // read before any block can finish (the last block rewrites them after every block has arrived)
+    const float zr = sc->z_r, vAv = sc->v_A_v;
+    grid_sum_finish(cg_prz_vertices(A, v, hd, p, r, z, zr, vAv, L, pre), partial, &sc->red_count, &sc->z_r,
+                    &sc->z_r_last);
+}
+
 // The whole Jacobi PCG solve (cg_solver.py:96-158, n_cg_iters iterations) as one cooperative kernel: each
 // iteration is the Hessian product phase and the p/r/z phase, with a grid barrier after each. Every block
 // forms the same totals (v.Av, z.r) from the block partials in block order.
@@ -2576,6 +2620,21 @@ void Stage3::newton_iteration() {
         cudaLaunchKernelEx(&cfg, k_cg_cluster, (const float4*)q, H, (const float4*)grad, (const float4*)hdiag, p, r, z,
                            v[0], v[1], P.n_cg_iters, sc);
         note_launch();
+    } else if (cg_mode == 7) {
+        // two ordinary launches per iteration (k_cg_solve's grid, 128 threads)
+        const long long elems = (long long)NP + NT + NH;
+        const int g = (int)std::max<long long>(1, std::min<long long>({(elems + 127) / 128, (long long)n_sm,
+                                                                       (long long)kPartials / 2}));
+        k_cg_start<128><<<g, 128, 0, s>>>(grad, hdiag, NP, p, r, z, v[0], sc, partial);
+        note_launch();
+        for (int it = 0; it < P.n_cg_iters; ++it) {
+            float4* vin = (it & 1) ? v[1] : v[0];
+            float4* vout = (it & 1) ? v[0] : v[1];
+            k_cg_product<128><<<g, 128, 0, s>>>(q, H, z, vin, vout, it, sc, partial);
+            note_launch();
+            k_cg_update<128><<<g, 128, 0, s>>>(H, vout, hdiag, p, r, z, sc, partial);
+            note_launch();
+        }
     } else {
         // one cooperative launch: about one thread per element, at most one block per SM (cg_mode 0, 3, 4); or
         // at least one block per SM (5: 128 threads, 6: 64 threads, two blocks per SM)
@@ -2933,7 +2992,7 @@ int pamo_stage3_set_param(pamo_stage3* s, const char* name, double value) {
     else if (n == "use_cuda_graph") s->solver.use_graph = value != 0.0;
     else if (n == "ccd_fp64") P.ccd_fp64 = value != 0.0;
     else if (n == "ls_mode") s->solver.ls_mode = (int)value;  // 1 cooperative line search, 0 launches per trial
-    else if (n == "cg_mode") s->solver.cg_mode = (int)value;  // 0/1 grid-cooperative (128), 2 cluster, 3 (256), 4 (512), 5 (128, >= 1 block per SM), 6 (64, >= 2 blocks per SM)
+    else if (n == "cg_mode") s->solver.cg_mode = (int)value;  // 0/1 grid-cooperative (128), 2 cluster, 3 (256), 4 (512), 5 (128, >= 1 block per SM), 6 (64, >= 2 blocks per SM), 7 two ordinary launches per iteration
     else {
         s->solver.err = "unknown stage-3 parameter: " + n;
         return PAMO_ERR_INVALID_ARG;

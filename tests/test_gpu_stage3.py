@@ -96,7 +96,7 @@ def test_default_steps_match_oracle(case, steps):
     assert abs(st["energy"] - so["energy"]) <= 1e-4 * abs(so["energy"])
 
 
-@pytest.mark.parametrize("cg_mode", [0, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("cg_mode", [0, 2, 3, 4, 5, 6, 7])
 def test_every_pcg_launch_shape_matches_oracle(cg_mode):
     """The cooperative PCG with 128-, 256- and 512-thread blocks (cg_mode 0, 3, 4), with at least one or two
     blocks per SM (5, 6) and the cluster PCG (2)."""
@@ -185,4 +185,18 @@ def test_identical_bits_for_each_pcg_launch_shape(cg_mode):
         s = safe_project.Stage3System(safe_project.Stage3Config(), "cuda:0")
         s._lib.pamo_stage3_set_param(s._h, b"cg_mode", float(cg_mode))
         outs.append(s.project(GV, GF, V, F, 2).cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_two_launch_pcg_equals_cooperative_pcg():
+    """cg_mode 7 runs k_cg_solve's phases as ordinary launches with the same grid and the block partials summed in
+    the same order, so it gives the cooperative solve's bits."""
+    from pamo_gb300 import safe_project
+
+    GV, GF, V, F = _cases()["sheets_push"]
+    outs = []
+    for mode in (0, 7):
+        s = safe_project.Stage3System(safe_project.Stage3Config(), "cuda:0")
+        s.set("cg_mode", mode)
+        outs.append(s.project(GV, GF, V, F, 3).cpu().numpy())
     assert np.array_equal(outs[0], outs[1])
