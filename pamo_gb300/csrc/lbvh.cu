@@ -306,13 +306,13 @@ __device__ void climb_from(RoundCounters* rc, int p, const int2* child, const in
                            const int* qscan, float4* packed) {
     {
         int guard = 0;
+        int2 c = child[p];
+        int pp = iparent[p];
         while (p >= 0) {
             if (++guard > 4096) {
                 atomicOr(&rc->status, kErrIterLimit);
                 break;
             }
-            const int2 c = child[p];
-            const int pp = iparent[p];
             float4 alo, ahi, clo, chi;
             if (c.x < 0) { alo = __ldcg(&llo[~c.x]); ahi = __ldcg(&lhi[~c.x]); }
             else { alo = __ldcg(&nlo[c.x]); ahi = __ldcg(&nhi[c.x]); }
@@ -323,8 +323,14 @@ __device__ void climb_from(RoundCounters* rc, int p, const int2* child, const in
             __stcg(&nlo[p], blo);  // the parent's second arrival reads it
             __stcg(&nhi[p], bhi);
             if (kPack) write_packed(p, c, alo, ahi, clo, chi, leaf_face, qscan, packed);
-            if (pp < 0 || arrive_acq_rel(&visit[pp]) == 0) break;
+            if (pp < 0) break;
+            // the parent's topology is fixed: loaded before its arrival count, not after
+            const int2 cn = child[pp];
+            const int ppn = iparent[pp];
+            if (arrive_acq_rel(&visit[pp]) == 0) break;
             p = pp;
+            c = cn;
+            pp = ppn;
         }
     }
 }
