@@ -2225,16 +2225,29 @@ __global__ void k_iter_end(SolverScalars* sc) {
 // ================================================================== host driver
 Stage3::~Stage3() { release(); }
 
+// The size-dependent buffers come from the solver's own stream-ordered memory pool: freeing one is ordered after the
+// solver's earlier work on its stream and waits for nothing else, where cudaFree would wait for the whole device (many
+// solvers sharing a GPU, as in a server, would stall each other every time one of them grows a buffer).
+int Stage3::dalloc(void** ptr, size_t bytes) {
+    *ptr = nullptr;
+    if (cudaMallocFromPoolAsync(ptr, std::max<size_t>(bytes, 16), pool, stream) != cudaSuccess) {
+        *ptr = nullptr;
+        return fail(PAMO_ERR_OOM, "cudaMallocFromPoolAsync");
+    }
+    return PAMO_OK;
+}
+
+void Stage3::dfree(void* ptr) {
+    if (ptr) cudaFreeAsync(ptr, stream);
+}
+
 template <typename T>
 int Stage3::grow(T*& ptr, size_t& cap, size_t n) {
     if (ptr && cap >= n) return PAMO_OK;
-    if (ptr) {
-        if (stream) cudaStreamSynchronize(stream);
-        cudaFree(ptr);
-        ptr = nullptr;
-    }
     drop_graph();
-    if (cudaMalloc((void**)&ptr, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+    dfree(ptr);
+    ptr = nullptr;
+    if (dalloc((void**)&ptr, std::max<size_t>(n, 1) * sizeof(T))) return PAMO_ERR_OOM;
     cap = n;
     return PAMO_OK;
 }
@@ -2248,17 +2261,26 @@ void Stage3::drop_graph() {
 void Stage3::release() {
     if (stream) cudaStreamSynchronize(stream);
     drop_graph();
-    auto f = [](auto*& ptr) {
+    auto fp = [this](auto*& ptr) {  // pool buffers
+        dfree(ptr);
+        ptr = nullptr;
+    };
+    auto f = [](auto*& ptr) {  // the fixed-size buffers of the first call
         if (ptr) cudaFree(ptr);
         ptr = nullptr;
     };
-    f(gt_pos); f(gt_tri); f(gt_bvh_mem); f(gt_rc); f(q); f(q_rest); f(q_prev_newton); f(p); f(target);
-    f(grad); f(hdiag); f(r); f(z); f(v[0]); f(v[1]); f(vweight);
-    f(cand_cnt); f(cand_off); f(cflag); f(cpos); f(cid); f(cty); f(vs_off); f(inv_vs); f(c_cnt); f(c_off); f(c_cur);
-    f(c_tmp); f(c_inv); f(gslot); f(hslot); f(aslot); f(scan_scratch);
-    cap_cf = cap_vs = cap_vso = cap_slot = cap_cq = 0; f(q_ref); f(cand_pt); f(cand_ee); f(tri); f(edge4); f(el_area); f(el_invDm);
-    f(hinge); f(hinge_rest); f(hinge_blocks); f(c_idx); f(c_type); f(c_d); f(c_dd); f(partial); f(tri_bvh_mem);
-    f(edge_bvh_mem); f(tri_rc); f(edge_rc); f(sc); f(d_norm); f(cg_bar);
+    fp(gt_pos); fp(gt_tri); fp(gt_bvh_mem); fp(q); fp(q_rest); fp(q_prev_newton); fp(p); fp(target);
+    fp(grad); fp(hdiag); fp(r); fp(z); fp(v[0]); fp(v[1]); fp(vweight);
+    fp(cand_cnt); fp(cand_off); fp(cflag); fp(cpos); fp(cid); fp(cty); fp(vs_off); fp(inv_vs); fp(c_cnt); fp(c_off);
+    fp(c_cur); fp(c_tmp); fp(c_inv); fp(gslot); fp(hslot); fp(aslot); fp(scan_scratch);
+    cap_cf = cap_vs = cap_vso = cap_slot = cap_cq = 0;
+    fp(q_ref); fp(cand_pt); fp(cand_ee); fp(tri); fp(edge4); fp(el_area); fp(el_invDm);
+    fp(hinge); fp(hinge_rest); fp(hinge_blocks); fp(c_idx); fp(c_type); fp(c_d); fp(c_dd); fp(tri_bvh_mem);
+    fp(edge_bvh_mem);
+    if (stream) cudaStreamSynchronize(stream);
+    if (pool) cudaMemPoolDestroy(pool);
+    pool = nullptr;
+    f(gt_rc); f(tri_rc); f(edge_rc); f(sc); f(d_norm); f(cg_bar); f(partial);
     if (h_sc) cudaFreeHost(h_sc);
     h_sc = nullptr;
     if (ev_in) cudaEventDestroy(ev_in);
@@ -2272,6 +2294,17 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
     int rr;
     if (!sc) {
         if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return fail(PAMO_ERR_CUDA, "stream");
+        {
+            int dev0 = 0;
+            cudaGetDevice(&dev0);
+            cudaMemPoolProps props = {};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev0;
+            if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) return fail(PAMO_ERR_CUDA, "memory pool");
+            unsigned long long keep = ~0ull;  // freed memory stays in the pool for the next growth
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
         if (cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming) != cudaSuccess)
             return fail(PAMO_ERR_CUDA, "event");
@@ -2318,10 +2351,12 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
         cap_gt = c;
     }
     if (gt_bvh_cap < (size_t)ngt + 2) {
-        if (gt_bvh_mem) cudaFree(gt_bvh_mem);
+        drop_graph();
+        dfree(gt_bvh_mem);
         gt_bvh_mem = nullptr;
-        if (cudaMalloc((void**)&gt_bvh_mem, bvh_bytes(ngt + 2)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
-        bvh_carve(gt_bvh, ngt + 2, gt_bvh_mem);
+        if ((rr = dalloc((void**)&gt_bvh_mem, bvh_bytes(ngt + 2)))) return rr;
+        bvh_carve(gt_bvh, ngt + 2, gt_bvh_mem, false);
+        cudaMemsetAsync(gt_bvh.scan_scratch, 0, scan_scratch_ints() * sizeof(int), stream);
         gt_bvh_cap = (size_t)ngt + 2;
     }
     if (cap_v < (size_t)np + 2) {
@@ -2343,10 +2378,12 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
         c = cap_t;
         if ((rr = grow(el_invDm, c, n))) return rr;
         cap_t = n;
-        if (tri_bvh_mem) cudaFree(tri_bvh_mem);
+        drop_graph();
+        dfree(tri_bvh_mem);
         tri_bvh_mem = nullptr;
-        if (cudaMalloc((void**)&tri_bvh_mem, bvh_bytes((int)n)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
-        bvh_carve(tri_bvh, (int)n, tri_bvh_mem);
+        if ((rr = dalloc((void**)&tri_bvh_mem, bvh_bytes((int)n)))) return rr;
+        bvh_carve(tri_bvh, (int)n, tri_bvh_mem, false);
+        cudaMemsetAsync(tri_bvh.scan_scratch, 0, scan_scratch_ints() * sizeof(int), stream);
         tri_bvh_cap = n;
     }
     if (cap_e < (size_t)ne + 2) {
@@ -2354,10 +2391,12 @@ int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
         c = cap_e;
         if ((rr = grow(edge4, c, n))) return rr;
         cap_e = n;
-        if (edge_bvh_mem) cudaFree(edge_bvh_mem);
+        drop_graph();
+        dfree(edge_bvh_mem);
         edge_bvh_mem = nullptr;
-        if (cudaMalloc((void**)&edge_bvh_mem, bvh_bytes((int)n)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
-        bvh_carve(edge_bvh, (int)n, edge_bvh_mem);
+        if ((rr = dalloc((void**)&edge_bvh_mem, bvh_bytes((int)n)))) return rr;
+        bvh_carve(edge_bvh, (int)n, edge_bvh_mem, false);
+        cudaMemsetAsync(edge_bvh.scan_scratch, 0, scan_scratch_ints() * sizeof(int), stream);
         edge_bvh_cap = n;
     }
     if (cap_h < (size_t)nh + 2) {
@@ -2378,8 +2417,8 @@ int Stage3::ensure_contacts(size_t n) {
     size_t c;
     int rr;
     c = 0;
-    if (c_idx) cudaStreamSynchronize(stream);
-    cudaFree(c_idx); cudaFree(c_type); cudaFree(c_d); cudaFree(c_dd);
+    drop_graph();
+    dfree(c_idx); dfree(c_type); dfree(c_d); dfree(c_dd);
     c_idx = nullptr; c_type = nullptr; c_d = nullptr; c_dd = nullptr;
     if ((rr = grow(c_idx, c, n))) return rr;
     c = 0;
@@ -2390,7 +2429,7 @@ int Stage3::ensure_contacts(size_t n) {
     if ((rr = grow(c_dd, c, 4 * n))) return rr;
     for (int** b : {&c_tmp, &c_inv}) {
         c = 0;
-        cudaFree(*b);
+        dfree(*b);
         *b = nullptr;
         if ((rr = grow(*b, c, 4 * n))) return rr;
     }
@@ -2406,9 +2445,8 @@ int Stage3::ensure_slots() {
     size_t c;
     const size_t ns = (size_t)3 * NT + (size_t)4 * NH + (size_t)4 * cap_c;
     if (cap_slot < ns || !gslot) {
-        if (gslot) cudaStreamSynchronize(stream);
         for (float4** b : {&gslot, &hslot, &aslot}) {
-            cudaFree(*b);
+            dfree(*b);
             *b = nullptr;
             c = 0;
             if ((rr = grow(*b, c, ns))) return rr;
@@ -2417,9 +2455,8 @@ int Stage3::ensure_slots() {
     }
     const size_t nv = (size_t)NP + 2;
     if (cap_vso < nv || !vs_off) {
-        if (vs_off) cudaStreamSynchronize(stream);
         for (int** b : {&vs_off, &c_cnt, &c_off, &c_cur}) {
-            cudaFree(*b);
+            dfree(*b);
             *b = nullptr;
             c = 0;
             if ((rr = grow(*b, c, nv))) return rr;
@@ -2443,9 +2480,8 @@ int Stage3::ensure_slots() {
     if (!scan_scratch) {
         c = 0;
         if ((rr = grow(scan_scratch, c, 2 * scan_scratch_ints()))) return rr;
-        // both scratches start zeroed (a scan's tile counters live there)
-        if (scan_scratch_clear(scan_scratch) || scan_scratch_clear(scan_scratch + scan_scratch_ints()))
-            return fail(PAMO_ERR_CUDA, "scan scratch");
+        // both scratches start zeroed (a scan's tile counters live there), in stream order
+        cudaMemsetAsync(scan_scratch, 0, 2 * scan_scratch_ints() * sizeof(int), stream);
     }
     return PAMO_OK;
 }
@@ -2465,8 +2501,7 @@ int Stage3::ensure_candidates(size_t npt, size_t nee) {
     }
     const size_t nf = cap_cpt + cap_cee + 1;
     if (cap_cf < nf || !cflag) {
-        if (cflag) cudaStreamSynchronize(stream);
-        cudaFree(cflag); cudaFree(cpos); cudaFree(cid); cudaFree(cty);
+        dfree(cflag); dfree(cpos); dfree(cid); dfree(cty);
         cflag = cpos = nullptr;
         cid = nullptr;
         cty = nullptr;

@@ -84,6 +84,9 @@ public:
 private:
     template <typename T>
     int grow(T*& p, size_t& cap, size_t n);
+    int dalloc(void** p, size_t bytes);
+    void dfree(void* p);
+    cudaMemPool_t pool = nullptr;  // the solver's stream-ordered pool for the size-dependent buffers
     int fail(int code, const std::string& m) {
         err = m;
         return code;
