@@ -283,8 +283,9 @@ int pamo_server_fetch(pamo_server* s, int64_t request_id, float* points, int32_t
 /* The same with float64 positions (a stage-3 result's own precision). */
 int pamo_server_fetch_f64(pamo_server* s, int64_t request_id, double* points, int32_t* triangles);
 
-/* Counters, out[0..n): bytes in use, most bytes in use so far, requests admitted, finished, queued, budget.
- * Returns 6. */
+/* Counters, out[0..n): bytes in use, most bytes in use so far, requests admitted, finished, queued, budget,
+ * stage-3 projections run a second time without cooperative kernels (after a bounded grid-wide wait gave up).
+ * Returns 7. */
 int pamo_server_stats(pamo_server* s, int64_t* out, int32_t n);
 
 /* The admission estimate of a job's device bytes. */

@@ -221,9 +221,9 @@ class Server:
         return v, t
 
     def stats(self) -> dict:
-        out = (ctypes.c_int64 * 6)()
-        self._lib.pamo_server_stats(self._h, out, 6)
-        return dict(zip(["in_use", "max_in_use", "admitted", "finished", "queued", "budget"], list(out)))
+        out = (ctypes.c_int64 * 7)()
+        self._lib.pamo_server_stats(self._h, out, 7)
+        return dict(zip(["in_use", "max_in_use", "admitted", "finished", "queued", "budget", "stage3_reruns"], list(out)))
 
     @staticmethod
     def job_bytes(n_points: int, n_triangles: int) -> int:

@@ -333,8 +333,13 @@ struct pamo_server {
     int64_t in_use = 0;  // bytes of admitted, unfinished requests
     int64_t max_in_use = 0, n_admitted = 0, n_finished = 0;
     int64_t next_id = 1;
+    int64_t n_stage3_reruns = 0;  // stage-3 projections run again without cooperative kernels after a wait gave up
     bool stop = false;
     std::string err;
+    // the workers' request buffers come from this stream-ordered pool (freed memory kept for the next growth): a
+    // worker that grows a buffer waits for nothing but its own stream, where cudaFree would wait for the whole device
+    // and stall every other worker
+    cudaMemPool_t pool = nullptr;
 
     // admit queued requests in arrival order while they fit the budget (a request larger than the whole
     // budget is admitted alone, when nothing else runs)
@@ -351,14 +356,17 @@ struct pamo_server {
         }
     }
 
-    // grows a device buffer (elements of T) to at least n
+    // grows a device buffer (elements of T) to at least n, in the order of the worker's stream st
     template <typename T>
-    static int ensure_dev(T*& p, size_t& cap, size_t n) {
+    int ensure_dev(T*& p, size_t& cap, size_t n, cudaStream_t st) {
         if (n <= cap && p) return PAMO_OK;
-        cudaFree(p);
+        if (p) cudaFreeAsync(p, st);
         p = nullptr;
         cap = 0;
-        if (cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return PAMO_ERR_OOM;
+        if (cudaMallocFromPoolAsync((void**)&p, std::max<size_t>(n, 1) * sizeof(T), pool, st) != cudaSuccess) {
+            p = nullptr;
+            return PAMO_ERR_OOM;
+        }
         cap = std::max<size_t>(n, 1);
         return PAMO_OK;
     }
@@ -386,16 +394,34 @@ struct pamo_server {
             q.out_points.assign(vm.begin(), vm.end());
             return PAMO_OK;
         }
-        if ((r = ensure_dev(gp, cgp, 3 * ngp)) || (r = ensure_dev(sp, csp, 6 * std::max<size_t>(nm, 1))) ||
-            (r = ensure_dev(st, cst, 3 * std::max<size_t>(nfm, 1))))
+        if ((r = ensure_dev(gp, cgp, 3 * ngp, w.stream)) ||
+            (r = ensure_dev(sp, csp, 6 * std::max<size_t>(nm, 1), w.stream)) ||
+            (r = ensure_dev(st, cst, 3 * std::max<size_t>(nfm, 1), w.stream)))
             return r;
         const long long ng = 3 * (long long)ngp;
         k_widen<<<(unsigned)std::min<long long>((ng + 255) / 256, 1024), 256, 0, w.stream>>>(d_gt_points, ng, gp);
         cudaMemcpyAsync(sp, vm.data(), vm.size() * sizeof(double), cudaMemcpyHostToDevice, w.stream);
         cudaMemcpyAsync(st, fm.data(), fm.size() * sizeof(int32_t), cudaMemcpyHostToDevice, w.stream);
         double* out = sp + 3 * nm;
-        if ((r = pamo_safe_project(s3, gp, d_gt_tris, (int32_t)ngp, (int32_t)ngt, sp, st, (int32_t)nm, (int32_t)nfm, 5,
-                                   out, w.stream))) {
+        r = pamo_safe_project(s3, gp, d_gt_tris, (int32_t)ngp, (int32_t)ngt, sp, st, (int32_t)nm, (int32_t)nfm, 5, out,
+                              w.stream);
+        if (r == PAMO_ERR_ITER_LIMIT) {
+            // A bounded wait gave up. The cooperative PCG and line search wait at grid-wide barriers for all their
+            // blocks, which other workers' kernels on the GPU can keep from running at once; run the projection
+            // again (from the same inputs) with the PCG as two ordinary launches per iteration and the line search
+            // as a launch pair per trial, which give the same bits and wait for nothing.
+            {
+                std::lock_guard<std::mutex> lock(mu);
+                ++n_stage3_reruns;
+            }
+            pamo_stage3_set_param(s3, "cg_mode", 7.0);
+            pamo_stage3_set_param(s3, "ls_mode", 0.0);
+            r = pamo_safe_project(s3, gp, d_gt_tris, (int32_t)ngp, (int32_t)ngt, sp, st, (int32_t)nm, (int32_t)nfm, 5,
+                                  out, w.stream);
+            pamo_stage3_set_param(s3, "cg_mode", 0.0);
+            pamo_stage3_set_param(s3, "ls_mode", 1.0);
+        }
+        if (r) {
             q.err = pamo_stage3_last_error(s3);
             return r;
         }
@@ -432,24 +458,12 @@ struct pamo_server {
             }
             const size_t np = q->points.size() / 3, nt = q->tris.size() / 3;
             int r = PAMO_OK;
-            if (np * 3 > cp) {
-                cudaFree(dp);
-                dp = nullptr;
-                cp = 0;
-                if (cudaMalloc((void**)&dp, np * 3 * sizeof(float)) != cudaSuccess) r = PAMO_ERR_OOM;
-                else cp = np * 3;
-            }
-            if (!r && nt * 3 > ct) {
-                cudaFree(dt);
-                dt = nullptr;
-                ct = 0;
-                if (cudaMalloc((void**)&dt, nt * 3 * sizeof(int32_t)) != cudaSuccess) r = PAMO_ERR_OOM;
-                else ct = nt * 3;
-            }
+            r = ensure_dev(dp, cp, np * 3, w.stream);
+            if (!r) r = ensure_dev(dt, ct, nt * 3, w.stream);
             int32_t onp = 0, ont = 0;
             if (!r && q->stage3) {
-                r = ensure_dev(rp, crp, np * 3);
-                if (!r) r = ensure_dev(rt, crt, nt * 3);
+                r = ensure_dev(rp, crp, np * 3, w.stream);
+                if (!r) r = ensure_dev(rt, crt, nt * 3, w.stream);
             }
             if (!r) {
                 cudaMemcpyAsync(dp, q->points.data(), np * 3 * sizeof(float), cudaMemcpyHostToDevice, w.stream);
@@ -485,13 +499,9 @@ struct pamo_server {
             cv_work.notify_all();
             cv_done.notify_all();
         }
-        cudaFree(dp);
-        cudaFree(dt);
-        cudaFree(rp);
-        cudaFree(rt);
-        cudaFree(gp);
-        cudaFree(sp);
-        cudaFree(st);
+        for (void* b : {(void*)dp, (void*)dt, (void*)rp, (void*)rt, (void*)gp, (void*)sp, (void*)st})
+            if (b) cudaFreeAsync(b, w.stream);
+        cudaStreamSynchronize(w.stream);
         if (s3) pamo_stage3_destroy(s3);
     }
 };
@@ -505,6 +515,19 @@ int pamo_server_create(pamo_server** out, int device, int32_t n_workers, int64_t
     s->device = device;
     s->budget = hbm_budget_bytes;
     int r = make_workers(device, n_workers, s->workers, s->err);
+    if (!r) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        if (cudaMemPoolCreate(&s->pool, &props) != cudaSuccess) {
+            s->pool = nullptr;
+            r = PAMO_ERR_CUDA;
+        } else {
+            unsigned long long keep = ~0ull;
+            cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    }
     if (r) {
         free_workers(device, s->workers);
         delete s;
@@ -525,6 +548,7 @@ int pamo_server_destroy(pamo_server* s) {
     s->cv_work.notify_all();
     for (auto& t : s->threads) t.join();
     free_workers(s->device, s->workers);
+    if (s->pool) cudaMemPoolDestroy(s->pool);
     delete s;
     return PAMO_OK;
 }
@@ -631,9 +655,10 @@ const char* pamo_server_last_error(const pamo_server* s) { return s ? s->err.c_s
 int pamo_server_stats(pamo_server* s, int64_t* out, int32_t n) {
     if (!s || !out) return PAMO_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lock(s->mu);
-    const int64_t v[6] = {s->in_use, s->max_in_use, s->n_admitted, s->n_finished, (int64_t)s->queue.size(), s->budget};
-    for (int i = 0; i < n && i < 6; ++i) out[i] = v[i];
-    return 6;
+    const int64_t v[7] = {s->in_use,   s->max_in_use, s->n_admitted,      s->n_finished, (int64_t)s->queue.size(),
+                          s->budget, s->n_stage3_reruns};
+    for (int i = 0; i < n && i < 7; ++i) out[i] = v[i];
+    return 7;
 }
 
 int64_t pamo_server_job_bytes(int32_t n_points, int32_t n_triangles) { return job_bytes(n_points, n_triangles); }

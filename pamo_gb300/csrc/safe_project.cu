@@ -1673,10 +1673,11 @@ __device__ __forceinline__ unsigned ld_acquire(volatile unsigned* p) {
 // reset, nothing to do for the last arrival but its own add). Arrival is a release (the block's writes,
 // ordered before it by the block barrier, become visible with it), the poll an acquire. The spin is bounded:
 // on time-out it records kErrIterLimit in *status and lets the block go on (the host then reports the error).
-__device__ __forceinline__ void grid_barrier(unsigned* count, int* status) {
+// extra (0 outside tests) makes block 0 wait for that many arrivals beyond the grid, so that the wait runs out.
+__device__ __forceinline__ void grid_barrier(unsigned* count, int* status, unsigned extra) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) : 1u;
+        const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1u) - extra : 1u;
         unsigned old;
         asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(count), "r"(inc) : "memory");
         long long spins = 0;
@@ -1780,8 +1781,9 @@ __global__ void __launch_bounds__(kThreads) k_cg_solve(const float4* __restrict_
     const int4 at0 = element_slots(A, nc, tid);  // fixed for the whole solve
     const PrzLanes L = prz_lanes(tid, nthreads, A.np);
     const VRange R0 = vertex_range(A.S, L.group < A.np ? L.group : 0, L.group < A.np);  // the group's first vertex
+    const unsigned extra = (unsigned)sc->barrier_extra;
     store_partial(cg_init_vertices(grad, hd, A.np, p, r, z, v0, tid, nthreads), part_a);
-    grid_barrier(&bar->count, &sc->status);
+    grid_barrier(&bar->count, &sc->status, extra);
     float zr = grid_partials_sum(part_a), zr_last = zr;
     for (int it = 0; it < n_iters; ++it) {
         const float4* vin = (it & 1) ? v1 : v0;
@@ -1790,13 +1792,13 @@ __global__ void __launch_bounds__(kThreads) k_cg_solve(const float4* __restrict_
         // partials alternate between two buffers phase by phase: a buffer is rewritten only after the next
         // barrier, which every block reaches after it has read that buffer
         store_partial(hvp_elements(x, A, z, vin, vout, s_dir, nc, tid, nthreads, ids0, at0), part_b);
-        grid_barrier(&bar->count, &sc->status);
+        grid_barrier(&bar->count, &sc->status, extra);
         // the first vertex's loads and slot gather go out before the partials are summed (they do not depend on
         // v.Av)
         const PrzVertex pre = prz_load(A, vout, hd, p, r, L.group < A.np ? L.group : 0, L.group < A.np, L, R0);
         const float vAv = grid_partials_sum(part_b);
         store_partial(cg_prz_vertices(A, vout, hd, p, r, z, zr, vAv, L, pre), part_a);
-        grid_barrier(&bar->count, &sc->status);
+        grid_barrier(&bar->count, &sc->status, extra);
         zr_last = zr;
         zr = grid_partials_sum(part_a);
         if (blockIdx.x == 0 && threadIdx.x == 0) sc->v_A_v = vAv;
@@ -1818,6 +1820,7 @@ __global__ void __launch_bounds__(kT) k_line_search_coop(const float4* __restric
     if (sc->abort) return;
     const int nc = sc->n_contacts;
     const float e_prev = sc->energy_prev, step = sc->ccd_step;
+    const unsigned extra = (unsigned)sc->barrier_extra;
     float e = sc->energy;
     for (int n = 0; n < n_trials; ++n) {
         const float a = step * powf(0.5f, (float)n);
@@ -1825,11 +1828,11 @@ __global__ void __launch_bounds__(kT) k_line_search_coop(const float4* __restric
             const float4 a0 = q0[i], pi = p[i];
             q[i] = make_float4(a0.x + a * pi.x, a0.y + a * pi.y, a0.z + a * pi.z, 0.f);
         }
-        grid_barrier(&bar->count, &sc->status);
+        grid_barrier(&bar->count, &sc->status, extra);
         // partials alternate between two buffers trial by trial (rewritten only after the next barrier)
         float2* part = partial + (size_t)(n & 1) * gridDim.x;
         store_partial(energy_elements(q, A, nc, gtid(), gstride()), part);
-        grid_barrier(&bar->count, &sc->status);
+        grid_barrier(&bar->count, &sc->status, extra);
         e = grid_partials_sum(part);
         if (e < e_prev) break;  // the same total in every block
     }
@@ -2845,6 +2848,7 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     std::memset(h_sc, 0, sizeof(SolverScalars));
     h_sc->radius = params.contact_detection_radius;
     h_sc->rebuild = 1;  // candidate lists are built in the first iteration
+    h_sc->barrier_extra = test_barrier_extra;
     cudaMemcpyAsync(sc, h_sc, sizeof(SolverScalars), cudaMemcpyHostToDevice, s);
     k_tris4<<<grid_for(NGT, kT), kT, 0, s>>>(gt_tris, NGT, NGP, gt_tri, &sc->status);
     note_launch();
@@ -2937,6 +2941,8 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
                 if (cudaStreamSynchronize(s) != cudaSuccess)
                     return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
                 done = h_sc->iters_done;
+                // a grid barrier that gave up leaves this run's values undefined: stop here
+                if (h_sc->status & kErrIterLimit) return fail(PAMO_ERR_ITER_LIMIT, "grid barrier of the PCG timed out");
                 if (h_sc->abort == 0) break;
                 if (h_sc->abort == 2) {
                     // too many contacts: halve the detection radius and detect again (energy.py:942-948)
@@ -2961,8 +2967,8 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     cudaEventRecord(ev_out, s);
     cudaStreamWaitEvent(caller, ev_out, 0);
     if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
-    if (h_sc->status & 6) return fail(PAMO_ERR_ITER_LIMIT, "BVH traversal limit in stage 3");
     if (h_sc->status & kErrIterLimit) return fail(PAMO_ERR_ITER_LIMIT, "grid barrier of the PCG timed out");
+    if (h_sc->status & 6) return fail(PAMO_ERR_ITER_LIMIT, "BVH traversal limit in stage 3");
     stats.last_energy = h_sc->energy;
     stats.max_contacts = h_sc->max_contacts;
     stats.total_contacts = h_sc->total_contacts;
@@ -3025,6 +3031,7 @@ int pamo_stage3_set_param(pamo_stage3* s, const char* name, double value) {
     else if (n == "min_angle_thres") P.min_angle_thres = (float)value;
     else if (n == "max_blocks") P.max_blocks = (long long)value;
     else if (n == "use_cuda_graph") s->solver.use_graph = value != 0.0;
+    else if (n == "test_barrier_extra") s->solver.test_barrier_extra = (int)value;  // tests: grid barriers run out
     else if (n == "ccd_fp64") P.ccd_fp64 = value != 0.0;
     else if (n == "ls_mode") s->solver.ls_mode = (int)value;  // 1 cooperative line search, 0 launches per trial
     else if (n == "cg_mode") s->solver.cg_mode = (int)value;  // 0/1 grid-cooperative (128), 2 cluster, 3 (256), 4 (512), 5 (128, >= 1 block per SM), 6 (64, >= 2 blocks per SM), 7 two ordinary launches per iteration

@@ -40,7 +40,7 @@ struct Stage3Params {
 struct SolverScalars {
     float energy, energy_prev, v_A_v, z_r, z_r_last, ccd_step;
     float radius;         // contact detection radius (halved when contacts exceed max_blocks)
-    float pad0;
+    int barrier_extra;    // test knob: arrivals a grid barrier waits for beyond its grid (0; 1 makes every wait run out)
     int n_contacts, n_contacts_raw, accepted, status;
     int abort;            // 0 running; 1 contact list full, 3 candidate list full (grow, redo the iteration);
                           // 2 contacts above max_blocks (halve the radius, redo)
@@ -79,6 +79,7 @@ public:
     bool use_graph = true;  // capture one Newton iteration as a CUDA graph and replay it
     int cg_mode = 0;        // PCG kernel: 0/1 grid-wide cooperative, 128 threads; 3: 256 threads; 2: one cluster
     int ls_mode = 1;        // line search: 1 one cooperative launch, 0 a launch pair per trial
+    int test_barrier_extra = 0;  // copied to SolverScalars::barrier_extra at each run (tests of the bounded waits)
     int cluster_size = 1;   // CTAs of the cluster kernel (device limit, at most 16)
 
 private:

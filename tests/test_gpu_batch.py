@@ -109,8 +109,8 @@ def test_autotune_picks_a_candidate_and_caches_it(tmp_path, monkeypatch):
 
 def test_server_stage3_equals_pamo_run():
     """Requests with stage 3 (PaMO(use_stage3=True) per request, the projection onto the request's own input): each
-    result has PaMO.run's faces and its positions within 1e-5 of the bounding-box diagonal (stage 3 sums with float
-    atomics), alone and among other requests."""
+    result has PaMO.run's faces and positions, bit for bit (stage 3 sums in a fixed order, and the server's second
+    attempt after a grid barrier time-out uses launch shapes with the same bits), among other requests."""
     import pamo_gb300
     from pamo_gb300.batch import Server
     from pamo_gb300 import synth
@@ -125,6 +125,7 @@ def test_server_stage3_equals_pamo_run():
         rid, st, npt, ntr, _ = w
         assert st == 0
         got[ids[rid]] = srv.fetch(rid, npt, ntr, float64=True)
+    assert srv.stats()["stage3_reruns"] >= 0
     srv.close()
     for i, (v, f) in enumerate(ms):
         pm = pamo_gb300.PaMO((v.astype(np.float64), f), use_stage1=False, use_stage3=True)
@@ -132,5 +133,4 @@ def test_server_stage3_equals_pamo_run():
         V, F = np.asarray(V), np.asarray(F)
         assert got[i][0].dtype == np.float64
         assert np.array_equal(got[i][1], F)
-        diag = float(np.linalg.norm(V.max(0) - V.min(0)))
-        assert np.abs(got[i][0] - V).max() <= 1e-5 * diag
+        assert np.array_equal(got[i][0], V)

@@ -188,6 +188,41 @@ def test_identical_bits_for_each_pcg_launch_shape(cg_mode):
     assert np.array_equal(outs[0], outs[1])
 
 
+def test_grid_barrier_time_out_is_reported_and_the_solver_stays_usable():
+    """The bounded wait of the cooperative kernels' grid barrier: a test knob makes block 0 wait for one arrival more
+    than the grid has, so the first wait runs out after its poll limit, records the status and lets the blocks go
+    on; the run stops with PAMO_ERR_ITER_LIMIT. The same solver then runs without cooperative kernels (the server's
+    second attempt) and gives the bits of a fresh solver."""
+    from pamo_gb300 import PamoError, safe_project
+
+    GV, GF, V, F = _cases()["sheets_push"]
+    s = safe_project.Stage3System(safe_project.Stage3Config(), "cuda:0")
+    s.set("test_barrier_extra", 1)
+    with pytest.raises(PamoError, match="grid barrier"):
+        s.project(GV, GF, V, F, 1)
+    s.set("cg_mode", 7)
+    s.set("ls_mode", 0)
+    out = s.project(GV, GF, V, F, 1).cpu().numpy()
+    ref = safe_project.Stage3System(safe_project.Stage3Config(), "cuda:0").project(GV, GF, V, F, 1).cpu().numpy()
+    assert np.array_equal(out, ref)
+
+
+def test_launch_pair_line_search_equals_cooperative_line_search():
+    """ls_mode 0 runs each trial as k_line_search + k_energy with k_energy's grid and block-order sum, so it gives the
+    cooperative search's bits; with cg_mode 7 as well (the server's solvers) no cooperative kernel is left."""
+    from pamo_gb300 import safe_project
+
+    GV, GF, V, F = _cases()["sheets_push"]
+    outs = []
+    for cg, ls in ((0, 1), (0, 0), (7, 0)):
+        s = safe_project.Stage3System(safe_project.Stage3Config(), "cuda:0")
+        s.set("cg_mode", cg)
+        s.set("ls_mode", ls)
+        outs.append(s.project(GV, GF, V, F, 3).cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
+    assert np.array_equal(outs[0], outs[2])
+
+
 def test_two_launch_pcg_equals_cooperative_pcg():
     """cg_mode 7 runs k_cg_solve's phases as ordinary launches with the same grid and the block partials summed in
     the same order, so it gives the cooperative solve's bits."""
