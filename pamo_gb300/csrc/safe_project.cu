@@ -9,8 +9,9 @@
 // implementation of the same mathematical operation (stated at each place).
 //
 // All simulation arrays are float32 as in the reference. Energies and the CG dot products are reduced in a
-// fixed order with compensated (two-sum) float accumulation, so the solve is deterministic apart from the
-// float atomics of the gradient, Hessian-diagonal and Hessian-vector scatters (same as the reference).
+// fixed order with compensated (two-sum) float accumulation, and the gradient, Hessian-diagonal and
+// Hessian-vector scatters (float atomics in the reference) are per-corner slots summed per vertex in a fixed
+// order, so the solve gives the same bits run after run.
 #include <algorithm>
 #include <climits>
 #include <cmath>
