@@ -331,7 +331,8 @@ int pamo_safe_project(pamo_stage3* s, const double* gt_points, const int32_t* gt
 
 /* Diagnostics of the last pamo_safe_project call, out[0..n): particles, triangles, edges, hinges, steps,
  * Newton iterations, most contacts in one detection, detection-radius halvings, do-nothing flag, final
- * energy, contacts summed over detections, rebuilds of the contact candidate lists. Returns 12. No reference
+ * energy, contacts summed over detections, rebuilds of the contact candidate lists, 1 when a grid barrier of a
+ * cooperative kernel gave up and the run was made again without cooperative kernels (same bits). Returns 13. No reference
  * counterpart (the reference logs these). */
 int pamo_stage3_stats(const pamo_stage3* s, double* out, int32_t n);
 

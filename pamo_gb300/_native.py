@@ -101,7 +101,7 @@ SIGNATURES = {
 }
 
 STAGE3_STATS = ["particles", "triangles", "edges", "hinges", "steps", "newton_iters", "max_contacts",
-                "radius_halvings", "do_nothing", "energy", "total_contacts", "candidate_rebuilds"]
+                "radius_halvings", "do_nothing", "energy", "total_contacts", "candidate_rebuilds", "barrier_reruns"]
 
 RUN_TOTALS = ["vertices", "faces", "edges", "winners", "query_tests", "pairs", "exact_pairs", "checks", "live_indexed",
               "collapsed"]

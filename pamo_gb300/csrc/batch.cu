@@ -405,21 +405,12 @@ struct pamo_server {
         double* out = sp + 3 * nm;
         r = pamo_safe_project(s3, gp, d_gt_tris, (int32_t)ngp, (int32_t)ngt, sp, st, (int32_t)nm, (int32_t)nfm, 5, out,
                               w.stream);
-        if (r == PAMO_ERR_ITER_LIMIT) {
-            // A bounded wait gave up. The cooperative PCG and line search wait at grid-wide barriers for all their
-            // blocks, which other workers' kernels on the GPU can keep from running at once; run the projection
-            // again (from the same inputs) with the PCG as two ordinary launches per iteration and the line search
-            // as a launch pair per trial, which give the same bits and wait for nothing.
-            {
-                std::lock_guard<std::mutex> lock(mu);
-                ++n_stage3_reruns;
-            }
-            pamo_stage3_set_param(s3, "cg_mode", 7.0);
-            pamo_stage3_set_param(s3, "ls_mode", 0.0);
-            r = pamo_safe_project(s3, gp, d_gt_tris, (int32_t)ngp, (int32_t)ngt, sp, st, (int32_t)nm, (int32_t)nfm, 5,
-                                  out, w.stream);
-            pamo_stage3_set_param(s3, "cg_mode", 0.0);
-            pamo_stage3_set_param(s3, "ls_mode", 1.0);
+        // the solver runs a projection again without cooperative kernels when a grid barrier gave up (other
+        // workers' kernels on the GPU can keep a cooperative kernel's blocks from running at once)
+        double st3[13] = {};
+        if (pamo_stage3_stats(s3, st3, 13) >= 13 && st3[12] > 0.0) {
+            std::lock_guard<std::mutex> lock(mu);
+            ++n_stage3_reruns;
         }
         if (r) {
             q.err = pamo_stage3_last_error(s3);

@@ -2748,8 +2748,25 @@ void Stage3::newton_iteration() {
 
 int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, int n_gt_tris, const double* points,
                 const int* tris, int n_points, int n_tris, int n_iters, double* out_points, cudaStream_t caller) {
+    int r = run_once(gt_points, gt_tris, n_gt_points, n_gt_tris, points, tris, n_points, n_tris, n_iters, out_points,
+                     caller);
+    if (r != PAMO_ERR_ITER_LIMIT || !barrier_gave_up) return r;
+    const int cg = cg_mode, ls = ls_mode;
+    cg_mode = 7;
+    ls_mode = 0;
+    r = run_once(gt_points, gt_tris, n_gt_points, n_gt_tris, points, tris, n_points, n_tris, n_iters, out_points, caller);
+    cg_mode = cg;
+    ls_mode = ls;
+    stats.barrier_reruns = 1;
+    return r;
+}
+
+int Stage3::run_once(const double* gt_points, const int* gt_tris, int n_gt_points, int n_gt_tris,
+                     const double* points, const int* tris, int n_points, int n_tris, int n_iters, double* out_points,
+                     cudaStream_t caller) {
     err.clear();
     stats = Stage3Stats{};
+    barrier_gave_up = false;
     if (n_points < 3 || n_tris < 1 || n_gt_points < 3 || n_gt_tris < 1) return fail(PAMO_ERR_INVALID_ARG, "empty mesh");
     // Topology on the host, once per call.
     // Edges: trimesh's edges_unique (the face edges with sorted endpoints, unique rows). For two int32
@@ -2943,7 +2960,10 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
                     return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
                 done = h_sc->iters_done;
                 // a grid barrier that gave up leaves this run's values undefined: stop here
-                if (h_sc->status & kErrIterLimit) return fail(PAMO_ERR_ITER_LIMIT, "grid barrier of the PCG timed out");
+                if (h_sc->status & kErrIterLimit) {
+                    barrier_gave_up = true;
+                    return fail(PAMO_ERR_ITER_LIMIT, "grid barrier of the PCG timed out");
+                }
                 if (h_sc->abort == 0) break;
                 if (h_sc->abort == 2) {
                     // too many contacts: halve the detection radius and detect again (energy.py:942-948)
@@ -2968,7 +2988,10 @@ int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, in
     cudaEventRecord(ev_out, s);
     cudaStreamWaitEvent(caller, ev_out, 0);
     if (cudaStreamSynchronize(s) != cudaSuccess) return fail(PAMO_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
-    if (h_sc->status & kErrIterLimit) return fail(PAMO_ERR_ITER_LIMIT, "grid barrier of the PCG timed out");
+    if (h_sc->status & kErrIterLimit) {
+        barrier_gave_up = true;
+        return fail(PAMO_ERR_ITER_LIMIT, "grid barrier of the PCG timed out");
+    }
     if (h_sc->status & 6) return fail(PAMO_ERR_ITER_LIMIT, "BVH traversal limit in stage 3");
     stats.last_energy = h_sc->energy;
     stats.max_contacts = h_sc->max_contacts;
@@ -3063,11 +3086,12 @@ int pamo_safe_project(pamo_stage3* s, const double* gt_points, const int32_t* gt
 int pamo_stage3_stats(const pamo_stage3* s, double* out, int32_t n) {
     if (!s || !out) return PAMO_ERR_INVALID_ARG;
     const pamo::Stage3Stats& t = s->solver.stats;
-    const double v[12] = {(double)t.n_particles, (double)t.n_triangles, (double)t.n_edges, (double)t.n_hinges,
+    const double v[13] = {(double)t.n_particles, (double)t.n_triangles, (double)t.n_edges, (double)t.n_hinges,
                           (double)t.steps, (double)t.newton_iters, (double)t.max_contacts, (double)t.radius_halvings,
-                          (double)t.do_nothing, t.last_energy, (double)t.total_contacts, (double)t.candidate_rebuilds};
-    for (int i = 0; i < n && i < 12; ++i) out[i] = v[i];
-    return 12;
+                          (double)t.do_nothing, t.last_energy, (double)t.total_contacts, (double)t.candidate_rebuilds,
+                          (double)t.barrier_reruns};
+    for (int i = 0; i < n && i < 13; ++i) out[i] = v[i];
+    return 13;
 }
 
 }  // extern "C"

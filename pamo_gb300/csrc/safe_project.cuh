@@ -61,6 +61,7 @@ struct Stage3Stats {
     double last_energy = 0.0;
     long long total_contacts = 0;  // summed over Newton iterations
     int candidate_rebuilds = 0;    // Newton iterations that rebuilt the contact candidate lists
+    int barrier_reruns = 0;        // 1: a grid barrier gave up and the run was made again without cooperative kernels
 };
 
 struct EnergyArgs;  // arguments of the energy kernels (safe_project.cu)
@@ -70,7 +71,10 @@ public:
     Stage3() = default;
     ~Stage3();
     // Runs process(gt_V, gt_F, V, F, n_iters) on device buffers; out_points receives float64 positions in
-    // the input frame. Returns a pamo_status code; err holds the message.
+    // the input frame. Returns a pamo_status code; err holds the message. A cooperative kernel's grid barrier
+    // needs all the kernel's blocks running at once, which other work sharing the GPU from other streams can
+    // prevent; when one gives up (its wait is bounded), the run is made again with the PCG as two ordinary launches
+    // per iteration and the line search as a launch pair per trial, which give the bits of cg_mode 0 / ls_mode 1.
     int run(const double* gt_points, const int* gt_tris, int n_gt_points, int n_gt_tris, const double* points,
             const int* tris, int n_points, int n_tris, int n_iters, double* out_points, cudaStream_t s);
     Stage3Params params;
@@ -83,6 +87,9 @@ public:
     int cluster_size = 1;   // CTAs of the cluster kernel (device limit, at most 16)
 
 private:
+    int run_once(const double* gt_points, const int* gt_tris, int n_gt_points, int n_gt_tris, const double* points,
+                 const int* tris, int n_points, int n_tris, int n_iters, double* out_points, cudaStream_t s);
+    bool barrier_gave_up = false;  // the last run_once failed because a grid barrier's bounded wait ran out
     template <typename T>
     int grow(T*& p, size_t& cap, size_t n);
     int dalloc(void** p, size_t bytes);
