@@ -2007,95 +2007,222 @@ __global__ void k_accd(const float4* __restrict__ x, const float4* __restrict__ 
     }
 }
 
-// ------------------------------------------------------------------ CCD in float64
-// The precision mode's "float64 CCD roots": the additive CCD above with positions, step directions, the
-// pair classification, the distances and the advancement in float64 (Warp's kernels run it in float32). The
-// resulting step is rounded down to float, so that it never exceeds the float64 time of impact bound.
-__device__ __forceinline__ D3 d3(float4 a) { return {(double)a.x, (double)a.y, (double)a.z}; }
-__device__ __forceinline__ D3 operator+(D3 a, D3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ D3 operator-(D3 a, D3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ D3 operator*(double s, D3 a) { return {s * a.x, s * a.y, s * a.z}; }
-__device__ __forceinline__ D3 operator/(D3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
-__device__ __forceinline__ double dot(D3 a, D3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ D3 cross(D3 a, D3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
-__device__ __forceinline__ double length_sq(D3 a) { return dot(a, a); }
-__device__ __forceinline__ double length(D3 a) { return sqrt(dot(a, a)); }
-__device__ __forceinline__ D3 normalize(D3 a) {
-    const double l = length(a);
-    return l > 0.0 ? a / l : D3{0.0, 0.0, 0.0};
+// ------------------------------------------------------------------ CCD in a wider precision
+// The precision mode's wide CCD roots: the additive CCD above with positions, step directions, the pair
+// classification, the distances and the advancement in a wider real type R (Warp's kernels run it in float32):
+// R = double (ccd_fp64 = 1), or R = WF, a double-float hi + lo pair built from FP32 operations only
+// (ccd_fp64 = 2, the default): GB300 issues about one FP64 fused multiply-add per SM and clock against 128 in FP32,
+// and the float64 CCD was throughput-bound on the FP64 pipe. The resulting step is rounded down to float, so that
+// it never exceeds the wide time-of-impact bound. The template body performs, for R = double, the operations of the
+// plain float64 code in the same order.
+//
+// WF: Dekker's double-length arithmetic (TwoSum, TwoProd with an explicit fused multiply-add), with the sloppy
+// addition of Hida, Li and Bailey's double-double library: about 44 significant bits.
+struct WF {
+    float hi, lo;
+};
+__device__ __forceinline__ void wf_two_prod(float a, float b, float& p, float& e) {
+    p = a * b;
+    e = __fmaf_rn(a, b, -p);
 }
-__device__ __forceinline__ double wstep(double x) { return x < 0.0 ? 1.0 : 0.0; }
-__device__ __forceinline__ double pt_distance(D3 x0, D3 x1, D3 x2, D3 x3) {
-    return fabs(dot(x0 - x1, normalize(cross(x2 - x1, x3 - x1))));
+__device__ __forceinline__ WF wf_fast(float a, float b) {  // |a| >= |b| or a == 0
+    const float s = a + b;
+    return {s, b - (s - a)};
 }
-__device__ __forceinline__ double ee_distance(D3 x0, D3 x1, D3 x2, D3 x3) {
-    return fabs(dot(x0 - x2, normalize(cross(x1 - x0, x3 - x2))));
+__device__ __forceinline__ WF operator+(WF a, WF b) {
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e += a.lo + b.lo;
+    return wf_fast(s, e);
 }
-__device__ __forceinline__ double pe_distance(D3 x0, D3 x1, D3 x2) { return length(cross(x1 - x0, x2 - x0)) / length(x1 - x2); }
-__device__ __forceinline__ double pp_distance(D3 x0, D3 x1) { return length(x1 - x0); }
+__device__ __forceinline__ WF operator-(WF a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ WF operator-(WF a, WF b) { return a + (-b); }
+__device__ __forceinline__ WF operator*(WF a, WF b) {
+    float p, e;
+    wf_two_prod(a.hi, b.hi, p, e);
+    e += a.hi * b.lo + a.lo * b.hi;
+    return wf_fast(p, e);
+}
+__device__ __forceinline__ WF operator/(WF a, WF b) {
+    const float q1 = a.hi / b.hi;
+    float p, e;
+    wf_two_prod(q1, b.hi, p, e);  // a - q1 b, to first order
+    const float r = ((a.hi - p) - e + a.lo - q1 * b.lo);
+    return wf_fast(q1, r / b.hi);
+}
+// comparisons of normalised pairs, false with a NaN as for double
+__device__ __forceinline__ bool operator<(WF a, WF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool operator>(WF a, WF b) { return b < a; }
+__device__ __forceinline__ bool operator<=(WF a, WF b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
+__device__ __forceinline__ bool operator>=(WF a, WF b) { return b <= a; }
+__device__ __forceinline__ bool operator==(WF a, WF b) { return a.hi == b.hi && a.lo == b.lo; }
 
-__device__ int pt_classify(D3 x0, D3 x1, D3 x2, D3 x3) {
-    D3 x10 = x0 - x1;
-    const D3 x12 = x2 - x1, x13 = x3 - x1;
-    const double area_sq = length_sq(cross(x12, x13));
-    if (area_sq <= 1e-6 * (length_sq(x12) * length_sq(x13)) || area_sq <= 1e-16) {
-        const double e1 = length(x10), e2 = length(x0 - x2), e3 = length(x0 - x3);
+// the real-type operations the template body uses, for double and for WF
+template <class R> struct Real;
+template <> struct Real<double> {
+    __device__ static __forceinline__ double c(double v) { return v; }
+    __device__ static __forceinline__ double of(float v) { return (double)v; }
+    __device__ static __forceinline__ double sqrt_(double a) { return sqrt(a); }
+    __device__ static __forceinline__ double abs_(double a) { return fabs(a); }
+    __device__ static __forceinline__ double max_(double a, double b) { return fmax(a, b); }
+    __device__ static __forceinline__ float floor_float(double a) { return __double2float_rd(a); }
+};
+template <> struct Real<WF> {
+    // constants: hi = v rounded to float, lo = the rest (both folded at compile time for literal v)
+    __device__ static __forceinline__ WF c(double v) { return {(float)v, (float)(v - (double)(float)v)}; }
+    __device__ static __forceinline__ WF of(float v) { return {v, 0.0f}; }
+    __device__ static __forceinline__ WF sqrt_(WF a) {
+        if (!(a.hi > 0.0f)) return {0.0f, 0.0f};
+        const float r = sqrtf(a.hi);
+        float p, e;
+        wf_two_prod(r, r, p, e);
+        return wf_fast(r, ((a.hi - p) - e + a.lo) / (2.0f * r));
+    }
+    __device__ static __forceinline__ WF abs_(WF a) { return a.hi < 0.0f ? -a : a; }
+    __device__ static __forceinline__ WF max_(WF a, WF b) {  // fmax: a NaN operand gives the other
+        if (a.hi != a.hi) return b;
+        if (b.hi != b.hi) return a;
+        return a < b ? b : a;
+    }
+    // the largest float not above hi + lo (|lo| <= ulp(hi) / 2)
+    __device__ static __forceinline__ float floor_float(WF a) {
+        return a.lo < 0.0f ? nextafterf(a.hi, -INFINITY) : a.hi;
+    }
+};
+
+template <class R>
+struct T3 {
+    R x, y, z;
+};
+template <class R>
+__device__ __forceinline__ T3<R> t3(float4 a) {
+    return {Real<R>::of(a.x), Real<R>::of(a.y), Real<R>::of(a.z)};
+}
+template <class R>
+__device__ __forceinline__ T3<R> operator+(T3<R> a, T3<R> b) {
+    return {a.x + b.x, a.y + b.y, a.z + b.z};
+}
+template <class R>
+__device__ __forceinline__ T3<R> operator-(T3<R> a, T3<R> b) {
+    return {a.x - b.x, a.y - b.y, a.z - b.z};
+}
+template <class R>
+__device__ __forceinline__ T3<R> operator*(R s, T3<R> a) {
+    return {s * a.x, s * a.y, s * a.z};
+}
+template <class R>
+__device__ __forceinline__ T3<R> operator/(T3<R> a, R s) {
+    return {a.x / s, a.y / s, a.z / s};
+}
+template <class R>
+__device__ __forceinline__ R dot(T3<R> a, T3<R> b) {
+    return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+template <class R>
+__device__ __forceinline__ T3<R> cross(T3<R> a, T3<R> b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+template <class R>
+__device__ __forceinline__ R length_sq(T3<R> a) {
+    return dot(a, a);
+}
+template <class R>
+__device__ __forceinline__ R length(T3<R> a) {
+    return Real<R>::sqrt_(dot(a, a));
+}
+template <class R>
+__device__ __forceinline__ T3<R> normalize(T3<R> a) {
+    const R l = length(a);
+    const R zero = Real<R>::c(0.0);
+    return l > zero ? a / l : T3<R>{zero, zero, zero};
+}
+template <class R>
+__device__ __forceinline__ R wstep(R x) {
+    return x < Real<R>::c(0.0) ? Real<R>::c(1.0) : Real<R>::c(0.0);
+}
+template <class R>
+__device__ __forceinline__ R pt_distance(T3<R> x0, T3<R> x1, T3<R> x2, T3<R> x3) {
+    return Real<R>::abs_(dot(x0 - x1, normalize(cross(x2 - x1, x3 - x1))));
+}
+template <class R>
+__device__ __forceinline__ R ee_distance(T3<R> x0, T3<R> x1, T3<R> x2, T3<R> x3) {
+    return Real<R>::abs_(dot(x0 - x2, normalize(cross(x1 - x0, x3 - x2))));
+}
+template <class R>
+__device__ __forceinline__ R pe_distance(T3<R> x0, T3<R> x1, T3<R> x2) {
+    return length(cross(x1 - x0, x2 - x0)) / length(x1 - x2);
+}
+template <class R>
+__device__ __forceinline__ R pp_distance(T3<R> x0, T3<R> x1) {
+    return length(x1 - x0);
+}
+
+template <class R>
+__device__ int pt_classify(T3<R> x0, T3<R> x1, T3<R> x2, T3<R> x3) {
+    typedef Real<R> K;
+    const R zero = K::c(0.0);
+    T3<R> x10 = x0 - x1;
+    const T3<R> x12 = x2 - x1, x13 = x3 - x1;
+    const R area_sq = length_sq(cross(x12, x13));
+    if (area_sq <= K::c(1e-6) * (length_sq(x12) * length_sq(x13)) || area_sq <= K::c(1e-16)) {
+        const R e1 = length(x10), e2 = length(x0 - x2), e3 = length(x0 - x3);
         if (e1 < e2) return e1 < e3 ? PT_PP01 : PT_PP03;
         return e2 < e3 ? PT_PP02 : PT_PP03;
     }
-    const D3 n = normalize(cross(x12, x13));
-    const D3 xp = x0 - dot(n, x10) * n;
+    const T3<R> n = normalize(cross(x12, x13));
+    const T3<R> xp = x0 - dot(n, x10) * n;
     x10 = xp - x1;
-    const D3 x20 = xp - x2, x30 = xp - x3;
-    const double a00 = dot(x12, x12), a01 = dot(x12, x13), a11 = dot(x13, x13);
-    const double b0 = dot(x10, x12), b1 = dot(x10, x13);
-    const double det = a00 * a11 - a01 * a01;
-    const double beta = b0 * a11 - b1 * a01;
-    const double gamma = a00 * b1 - b0 * a01;
-    const double alpha = det - beta - gamma;
-    const double nneg = wstep(alpha) + wstep(beta) + wstep(gamma);
-    if (nneg == 0.0) return PT_PT;
-    if (nneg == 1.0) {
-        if (alpha < 0.0) {
-            const D3 x23 = x3 - x2, x20b = x0 - x2;
-            const double dr = dot(x23, x20b);
-            if (dr < 0.0) return PT_PP02;
+    const T3<R> x20 = xp - x2, x30 = xp - x3;
+    const R a00 = dot(x12, x12), a01 = dot(x12, x13), a11 = dot(x13, x13);
+    const R b0 = dot(x10, x12), b1 = dot(x10, x13);
+    const R det = a00 * a11 - a01 * a01;
+    const R beta = b0 * a11 - b1 * a01;
+    const R gamma = a00 * b1 - b0 * a01;
+    const R alpha = det - beta - gamma;
+    const R nneg = wstep(alpha) + wstep(beta) + wstep(gamma);
+    if (nneg == zero) return PT_PT;
+    if (nneg == K::c(1.0)) {
+        if (alpha < zero) {
+            const T3<R> x23 = x3 - x2, x20b = x0 - x2;
+            const R dr = dot(x23, x20b);
+            if (dr < zero) return PT_PP02;
             if (dr > dot(x23, x23)) return PT_PP03;
             return PT_PE023;
-        } else if (beta < 0.0) {
-            const D3 x31 = x1 - x3, x30b = x0 - x3;
-            const double dr = dot(x31, x30b);
-            if (dr < 0.0) return PT_PP03;
+        } else if (beta < zero) {
+            const T3<R> x31 = x1 - x3, x30b = x0 - x3;
+            const R dr = dot(x31, x30b);
+            if (dr < zero) return PT_PP03;
             if (dr > dot(x31, x31)) return PT_PP01;
             return PT_PE031;
-        } else if (gamma < 0.0) {
-            const double dr = dot(x12, x10);
-            if (dr < 0.0) return PT_PP01;
+        } else if (gamma < zero) {
+            const R dr = dot(x12, x10);
+            if (dr < zero) return PT_PP01;
             if (dr > dot(x12, x12)) return PT_PP02;
             return PT_PE012;
         }
         return -1;
     }
-    if (alpha >= 0.0) {
-        const double d12 = dot(x12, x10), d13 = dot(x13, x10);
-        if (d12 > 0.0 && d13 <= 0.0) return dot(x12, x20) > 0.0 ? PT_PP02 : PT_PE012;
-        if (d13 > 0.0 && d12 <= 0.0) return dot(x13, x30) > 0.0 ? PT_PP03 : PT_PE031;
+    if (alpha >= zero) {
+        const R d12 = dot(x12, x10), d13 = dot(x13, x10);
+        if (d12 > zero && d13 <= zero) return dot(x12, x20) > zero ? PT_PP02 : PT_PE012;
+        if (d13 > zero && d12 <= zero) return dot(x13, x30) > zero ? PT_PP03 : PT_PE031;
         return PT_PP01;
-    } else if (beta >= 0.0) {
-        const D3 x23 = x3 - x2, x21 = x1 - x2;
-        const double d23 = dot(x23, x20), d21 = dot(x21, x20);
-        if (d23 > 0.0 && d21 <= 0.0) return dot(x23, x30) > 0.0 ? PT_PP03 : PT_PE023;
-        if (d21 > 0.0 && d23 <= 0.0) return dot(x21, x10) > 0.0 ? PT_PP01 : PT_PE012;
+    } else if (beta >= zero) {
+        const T3<R> x23 = x3 - x2, x21 = x1 - x2;
+        const R d23 = dot(x23, x20), d21 = dot(x21, x20);
+        if (d23 > zero && d21 <= zero) return dot(x23, x30) > zero ? PT_PP03 : PT_PE023;
+        if (d21 > zero && d23 <= zero) return dot(x21, x10) > zero ? PT_PP01 : PT_PE012;
         return PT_PP02;
     }
-    const D3 x31 = x1 - x3, x32 = x2 - x3;
-    const double d31 = dot(x31, x30), d32 = dot(x32, x30);
-    if (d31 > 0.0 && d32 <= 0.0) return dot(x31, x10) > 0.0 ? PT_PP01 : PT_PE031;
-    if (d32 > 0.0 && d31 <= 0.0) return dot(x32, x20) > 0.0 ? PT_PP02 : PT_PE023;
+    const T3<R> x31 = x1 - x3, x32 = x2 - x3;
+    const R d31 = dot(x31, x30), d32 = dot(x32, x30);
+    if (d31 > zero && d32 <= zero) return dot(x31, x10) > zero ? PT_PP01 : PT_PE031;
+    if (d32 > zero && d31 <= zero) return dot(x32, x20) > zero ? PT_PP02 : PT_PE023;
     return PT_PP03;
 }
 
-__device__ double pt_pair_distance(D3 x0, D3 x1, D3 x2, D3 x3, int t) {
+template <class R>
+__device__ R pt_pair_distance(T3<R> x0, T3<R> x1, T3<R> x2, T3<R> x3, int t) {
     switch (t) {
         case PT_PT: return pt_distance(x0, x1, x2, x3);
         case PT_PP01: return pp_distance(x0, x1);
@@ -2105,48 +2232,53 @@ __device__ double pt_pair_distance(D3 x0, D3 x1, D3 x2, D3 x3, int t) {
         case PT_PE031: return pe_distance(x0, x3, x1);
         case PT_PE023: return pe_distance(x0, x2, x3);
     }
-    return 1e9;
+    return Real<R>::c(1e9);
 }
 
-__device__ int ee_classify(D3 x0, D3 x1, D3 x2, D3 x3, double sin_thres) {
-    const D3 e0 = x0 - x1, e1 = x2 - x3;
-    const double e0_sq = dot(e0, e0), e1_sq = dot(e1, e1);
-    const double a00 = e0_sq, a01 = -dot(e0, e1), a10 = dot(e0, e1), a11 = -e1_sq;
-    const double b0 = dot(x3 - x1, e0), b1 = dot(x3 - x1, e1);
-    const double mu0 = -(b0 * a11 - b1 * a01);
-    const double mu1 = -(a00 * b1 - a10 * b0);
-    const double detA = -(a00 * a11 - a01 * a10);
-    const double edge_sin = length(cross(normalize(e0), normalize(e1)));
-    if (mu0 >= 0.0 && mu0 <= detA && mu1 >= 0.0 && mu1 <= detA && edge_sin >= sin_thres && e0_sq > 1e-15 && e1_sq > 1e-15)
+template <class R>
+__device__ int ee_classify(T3<R> x0, T3<R> x1, T3<R> x2, T3<R> x3, R sin_thres) {
+    typedef Real<R> K;
+    const R zero = K::c(0.0);
+    const T3<R> e0 = x0 - x1, e1 = x2 - x3;
+    const R e0_sq = dot(e0, e0), e1_sq = dot(e1, e1);
+    const R a00 = e0_sq, a01 = -dot(e0, e1), a10 = dot(e0, e1), a11 = -e1_sq;
+    const R b0 = dot(x3 - x1, e0), b1 = dot(x3 - x1, e1);
+    const R mu0 = -(b0 * a11 - b1 * a01);
+    const R mu1 = -(a00 * b1 - a10 * b0);
+    const R detA = -(a00 * a11 - a01 * a10);
+    const R edge_sin = length(cross(normalize(e0), normalize(e1)));
+    if (mu0 >= zero && mu0 <= detA && mu1 >= zero && mu1 <= detA && edge_sin >= sin_thres && e0_sq > K::c(1e-15) &&
+        e1_sq > K::c(1e-15))
         return EE_EE;
-    double best = 1e9;
+    R best = K::c(1e9);
     int type = -1;
-    auto consider = [&](double d, int t) {
+    auto consider = [&](R d, int t) {
         if (d < best) {
             best = d;
             type = t;
         }
     };
-    const double t0 = dot(x0 - x3, e1);
+    const R t0 = dot(x0 - x3, e1);
     if (t0 >= e1_sq) consider(pp_distance(x0, x2), EE_PP02);
-    else if (t0 <= 0.0) consider(pp_distance(x0, x3), EE_PP03);
+    else if (t0 <= zero) consider(pp_distance(x0, x3), EE_PP03);
     else consider(pe_distance(x0, x2, x3), EE_PE023);
-    const double t1 = dot(x1 - x3, e1);
+    const R t1 = dot(x1 - x3, e1);
     if (t1 >= e1_sq) consider(pp_distance(x1, x2), EE_PP12);
-    else if (t1 <= 0.0) consider(pp_distance(x1, x3), EE_PP13);
+    else if (t1 <= zero) consider(pp_distance(x1, x3), EE_PP13);
     else consider(pe_distance(x1, x2, x3), EE_PE123);
-    const double t2 = dot(x2 - x1, e0);
+    const R t2 = dot(x2 - x1, e0);
     if (t2 >= e0_sq) consider(pp_distance(x2, x0), EE_PP02);
-    else if (t2 <= 0.0) consider(pp_distance(x2, x1), EE_PP12);
+    else if (t2 <= zero) consider(pp_distance(x2, x1), EE_PP12);
     else consider(pe_distance(x2, x0, x1), EE_PE201);
-    const double t3 = dot(x3 - x1, e0);
+    const R t3 = dot(x3 - x1, e0);
     if (t3 >= e0_sq) consider(pp_distance(x3, x0), EE_PP03);
-    else if (t3 <= 0.0) consider(pp_distance(x3, x1), EE_PP13);
+    else if (t3 <= zero) consider(pp_distance(x3, x1), EE_PP13);
     else consider(pe_distance(x3, x0, x1), EE_PE301);
     return type;
 }
 
-__device__ double ee_pair_distance(D3 x0, D3 x1, D3 x2, D3 x3, int t) {
+template <class R>
+__device__ R ee_pair_distance(T3<R> x0, T3<R> x1, T3<R> x2, T3<R> x3, int t) {
     switch (t) {
         case EE_PP02: return pp_distance(x0, x2);
         case EE_PP03: return pp_distance(x0, x3);
@@ -2158,49 +2290,54 @@ __device__ double ee_pair_distance(D3 x0, D3 x1, D3 x2, D3 x3, int t) {
         case EE_PE301: return pe_distance(x3, x0, x1);
         case EE_EE: return ee_distance(x0, x1, x2, x3);
     }
-    return 1e9;
+    return Real<R>::c(1e9);
 }
 
-__global__ void k_accd_fp64(const float4* __restrict__ x, const float4* __restrict__ vel, const int4* __restrict__ cidx,
-                            const int2* __restrict__ ctype, SolverScalars* sc, double slackness, double thickness,
-                            int max_iters, double ee_thres) {
+// slackness, thickness and ee_thres as R (the host passes their float values, widened)
+template <class R>
+__global__ void k_accd_wide(const float4* __restrict__ x, const float4* __restrict__ vel, const int4* __restrict__ cidx,
+                            const int2* __restrict__ ctype, SolverScalars* sc, float slackness_f, float thickness_f,
+                            int max_iters, float ee_thres_f) {
+    typedef Real<R> K;
     if (sc->abort) return;
+    const R slackness = K::of(slackness_f), thickness = K::of(thickness_f), ee_thres = K::of(ee_thres_f);
+    const R zero = K::c(0.0), one = K::c(1.0);
     const int n = sc->n_contacts;
     for (long long bb = spread_first(); bb < n; bb += spread_stride()) {
         const int b = (int)bb;
         const int4 id = cidx[b];
-        D3 x0 = d3(x[id.x]), x1 = d3(x[id.y]), x2 = d3(x[id.z]), x3 = d3(x[id.w]);
-        D3 v0 = d3(vel[id.x]), v1 = d3(vel[id.y]), v2 = d3(vel[id.z]), v3 = d3(vel[id.w]);
+        T3<R> x0 = t3<R>(x[id.x]), x1 = t3<R>(x[id.y]), x2 = t3<R>(x[id.z]), x3 = t3<R>(x[id.w]);
+        T3<R> v0 = t3<R>(vel[id.x]), v1 = t3<R>(vel[id.y]), v2 = t3<R>(vel[id.z]), v3 = t3<R>(vel[id.w]);
         const int type1 = ctype[b].x;
-        const D3 va = (v0 + v1 + v2 + v3) / 4.0;
+        const T3<R> va = (v0 + v1 + v2 + v3) / K::c(4.0);
         v0 = v0 - va; v1 = v1 - va; v2 = v2 - va; v3 = v3 - va;
-        double lv;
-        if (type1 == BLOCK_PT) lv = length(v0) + fmax(length(v1), fmax(length(v2), length(v3)));
-        else lv = fmax(length(v0), length(v1)) + fmax(length(v2), length(v3));
-        if (lv < 1e-12) continue;
+        R lv;
+        if (type1 == BLOCK_PT) lv = length(v0) + K::max_(length(v1), K::max_(length(v2), length(v3)));
+        else lv = K::max_(length(v0), length(v1)) + K::max_(length(v2), length(v3));
+        if (lv < K::c(1e-12)) continue;
         auto dist = [&]() {
             if (type1 == BLOCK_PT) return pt_pair_distance(x0, x1, x2, x3, pt_classify(x0, x1, x2, x3));
             return ee_pair_distance(x0, x1, x2, x3, ee_classify(x0, x1, x2, x3, ee_thres));
         };
-        double d = dist();
-        double dsq = d * d;
-        double dmt = fmax((dsq - thickness * thickness) / (sqrt(dsq) + thickness), 0.0);
-        const double gap = (1.0 - slackness) * dmt;
-        double t = 0.0;
-        double tl = slackness * dmt / lv;
+        R d = dist();
+        R dsq = d * d;
+        R dmt = K::max_((dsq - thickness * thickness) / (K::sqrt_(dsq) + thickness), zero);
+        const R gap = (one - slackness) * dmt;
+        R t = zero;
+        R tl = slackness * dmt / lv;
         int it = 0;
         while (true) {
             x0 = x0 + tl * v0; x1 = x1 + tl * v1; x2 = x2 + tl * v2; x3 = x3 + tl * v3;
             d = dist();
             dsq = d * d;
-            dmt = fmax((dsq - thickness * thickness) / (sqrt(dsq) + thickness), 0.0);
+            dmt = K::max_((dsq - thickness * thickness) / (K::sqrt_(dsq) + thickness), zero);
             if ((it > 0 && dmt <= gap) || it >= max_iters) {
-                atomicMin((int*)&sc->ccd_step, __float_as_int(__double2float_rd(t)));  // t >= 0: int order = float order
+                atomicMin((int*)&sc->ccd_step, __float_as_int(K::floor_float(t)));  // t >= 0: int order = float order
                 break;
             }
             t = t + tl;
-            if (t > 1.0) break;
-            tl = 0.8 * dmt / lv;
+            if (t > one) break;
+            tl = K::c(0.8) * dmt / lv;
             ++it;
         }
     }
@@ -2712,9 +2849,12 @@ void Stage3::newton_iteration() {
     note_launch();
     k_before_ccd<<<1, 1, 0, s>>>(sc);
     note_launch();
-    if (P.ccd_fp64)
-        k_accd_fp64<<<gC, kT, 0, s>>>(q, p, c_idx, c_type, sc, (double)P.ccd_slackness, (double)P.ccd_thickness,
-                                      P.ccd_max_iters, (double)P.ee_classify_thres);
+    if (P.ccd_fp64 == 2)
+        k_accd_wide<WF><<<gC, kT, 0, s>>>(q, p, c_idx, c_type, sc, P.ccd_slackness, P.ccd_thickness, P.ccd_max_iters,
+                                          P.ee_classify_thres);
+    else if (P.ccd_fp64)
+        k_accd_wide<double><<<gC, kT, 0, s>>>(q, p, c_idx, c_type, sc, P.ccd_slackness, P.ccd_thickness,
+                                              P.ccd_max_iters, P.ee_classify_thres);
     else
         k_accd<<<gC, kT, 0, s>>>(q, p, c_idx, c_type, sc, P.ccd_slackness, P.ccd_thickness, P.ccd_max_iters,
                                 P.ee_classify_thres);
@@ -3056,7 +3196,13 @@ int pamo_stage3_set_param(pamo_stage3* s, const char* name, double value) {
     else if (n == "max_blocks") P.max_blocks = (long long)value;
     else if (n == "use_cuda_graph") s->solver.use_graph = value != 0.0;
     else if (n == "test_barrier_extra") s->solver.test_barrier_extra = (int)value;  // tests: grid barriers run out
-    else if (n == "ccd_fp64") P.ccd_fp64 = value != 0.0;
+    else if (n == "ccd_fp64") {  // 0 float32 (Warp's kernels), 1 float64, 2 double-float (default)
+        if (value != 0.0 && value != 1.0 && value != 2.0) {
+            s->solver.err = "ccd_fp64 is 0, 1 or 2";
+            return PAMO_ERR_INVALID_ARG;
+        }
+        P.ccd_fp64 = (int)value;
+    }
     else if (n == "ls_mode") s->solver.ls_mode = (int)value;  // 1 cooperative line search, 0 launches per trial
     else if (n == "cg_mode") s->solver.cg_mode = (int)value;  // 0/1 grid-cooperative (128), 2 cluster, 3 (256), 4 (512), 5 (128, >= 1 block per SM), 6 (64, >= 2 blocks per SM), 7 two ordinary launches per iteration
     else {

@@ -25,7 +25,7 @@ struct Stage3Params {
     float ccd_slackness = 0.7f;
     float ccd_thickness = 1e-6f;
     int ccd_max_iters = 100;
-    bool ccd_fp64 = true;  // the precision mode: CCD in float64 (false: float32 as Warp's kernels)
+    int ccd_fp64 = 2;  // the precision mode's CCD: 2 double-float (FP32 pipes), 1 float64; 0 float32 as Warp's kernels
     int spd_max_iters = 3;
     float elas_young_modulus = 0.1f;
     float elas_poisson_ratio = 0.0f;

@@ -44,8 +44,9 @@ class Stage3Config:
     mesh2gt_dist_stiffness: float = 1e3
     min_angle_thres: float = 0.0
     max_blocks: int = 1 << 25
-    # this build's precision mode: the CCD step in float64 (False: float32, as Warp's kernels compute it)
-    ccd_fp64: bool = True
+    # this build's precision mode for the CCD step: 2 double-float (hi + lo float pairs, the default), 1 (or True)
+    # float64, 0 (or False) float32 as Warp's kernels compute it
+    ccd_fp64: int = 2
 
 
 class Stage3System:

@@ -188,6 +188,20 @@ def test_identical_bits_for_each_pcg_launch_shape(cg_mode):
     assert np.array_equal(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("case", ["star", "sheets_push"])
+def test_double_float_ccd_matches_float64_ccd(case):
+    """The CCD step's precision modes: double-float pairs (2, the default) against float64 (1); both round the step
+    down to float, so their results agree far below the oracle's 1e-5 of the diagonal, and each matches the
+    oracle."""
+    GV, GF, V, F = _cases()[case]
+    wide, _ = _gpu(GV, GF, V, F, 2, ccd_fp64=2)
+    dbl, _ = _gpu(GV, GF, V, F, 2, ccd_fp64=1)
+    diag = _diag(V)
+    assert np.abs(wide - dbl).max() <= 1e-6 * diag
+    ref, _ = orc.stage3_run(GV, GF, V, F, 2)
+    assert np.abs(wide - ref).max() <= TOL * diag
+
+
 def test_grid_barrier_time_out_reruns_without_cooperative_kernels():
     """The bounded wait of the cooperative kernels' grid barrier: a test knob makes block 0 wait for one arrival more
     than the grid has, so the first wait runs out after its poll limit, records the status and lets the blocks go
