@@ -291,6 +291,14 @@ int pamo_server_stats(pamo_server* s, int64_t* out, int32_t n);
 /* The admission estimate of a job's device bytes. */
 int64_t pamo_server_job_bytes(int32_t n_points, int32_t n_triangles);
 
+/* The processing a stage-3 request's stage-2 mesh goes through before the projection (host code, no GPU):
+ * trimesh.Trimesh(V, F)'s default processing as PaMO.run applies it (simp_cuda/pamo/__init__.py:165-176):
+ * faces on non-finite vertices dropped, vertices equal after rounding to 8 decimals merged (first occurrence
+ * kept), unreferenced vertices dropped, first-occurrence order. Outputs have room for the input sizes; returns
+ * PAMO_ERR_INVALID_ARG for an index outside [0, n_points). */
+int pamo_mesh_process(const double* points, int32_t n_points, const int32_t* triangles, int32_t n_triangles,
+                      double* out_points, int32_t* out_n_points, int32_t* out_triangles, int32_t* out_n_triangles);
+
 /* ------------------------------------------------------------------------------------------------------
  * Stage 3: safe projection of the simplified mesh onto the input ("GT") mesh.
  * A pamo_stage3 handle replaces the reference's Stage3System (simp_cuda/safe_project/src/pamo_safe_project/

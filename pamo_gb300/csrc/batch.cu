@@ -654,4 +654,21 @@ int pamo_server_stats(pamo_server* s, int64_t* out, int32_t n) {
 
 int64_t pamo_server_job_bytes(int32_t n_points, int32_t n_triangles) { return job_bytes(n_points, n_triangles); }
 
+int pamo_mesh_process(const double* points, int32_t n_points, const int32_t* triangles, int32_t n_triangles,
+                      double* out_points, int32_t* out_n_points, int32_t* out_triangles, int32_t* out_n_triangles) {
+    if (n_points < 0 || n_triangles < 0 || (n_points && !points) || (n_triangles && !triangles) || !out_n_points ||
+        !out_n_triangles || (n_points && !out_points) || (n_triangles && !out_triangles))
+        return PAMO_ERR_INVALID_ARG;
+    for (int64_t i = 0; i < 3 * (int64_t)n_triangles; ++i)
+        if (triangles[i] < 0 || triangles[i] >= n_points) return PAMO_ERR_INVALID_ARG;
+    std::vector<double> V(points, points + 3 * (size_t)n_points), Vo;
+    std::vector<int32_t> F(triangles, triangles + 3 * (size_t)n_triangles), Fo;
+    mesh_process(V, F, Vo, Fo);
+    std::copy(Vo.begin(), Vo.end(), out_points);
+    std::copy(Fo.begin(), Fo.end(), out_triangles);
+    *out_n_points = (int32_t)(Vo.size() / 3);
+    *out_n_triangles = (int32_t)(Fo.size() / 3);
+    return PAMO_OK;
+}
+
 }  // extern "C"

@@ -42,3 +42,48 @@ def test_empty_inputs_pass_through():
 
     V2, F2 = mesh_process(np.zeros((0, 3)), np.zeros((0, 3), np.int64))
     assert V2.shape == (0, 3) and F2.shape == (0, 3)
+
+
+def _native_process(lib, V, F):
+    import ctypes
+
+    V = np.ascontiguousarray(V, np.float64)
+    F = np.ascontiguousarray(F, np.int32)
+    Vo = np.zeros_like(V)
+    Fo = np.zeros_like(F)
+    nv, nf = ctypes.c_int32(0), ctypes.c_int32(0)
+    st = lib.pamo_mesh_process(V.ctypes.data, len(V), F.ctypes.data, len(F), Vo.ctypes.data, ctypes.byref(nv),
+                               Fo.ctypes.data, ctypes.byref(nf))
+    return st, Vo[: nv.value], Fo[: nf.value]
+
+
+def test_server_processing_equals_the_python_restatement(native_lib):
+    """pamo_mesh_process (the C++ processing the server applies to each stage-2 result before stage 3) gives
+    safe_project.mesh_process's vertices and faces, bit for bit, on meshes with near-duplicate vertices (inside and
+    just outside the 1e-8 rounding), unreferenced and non-finite vertices."""
+    from pamo_gb300.safe_project import mesh_process
+
+    rng = np.random.default_rng(5)
+    for trial in range(40):
+        n = int(rng.integers(4, 300))
+        V = rng.normal(size=(n, 3))
+        dup = rng.integers(0, n, n // 3)
+        V = np.concatenate([V, V[dup] + rng.choice([0.0, 2e-9, -4e-9, 3e-8], size=(len(dup), 1))])
+        if trial % 3 == 0:
+            V[rng.integers(0, len(V), 2)] = np.nan
+        if trial % 5 == 0:
+            V[rng.integers(0, len(V))] = np.inf
+        F = rng.integers(0, len(V), size=(int(rng.integers(1, 2 * n)), 3)).astype(np.int32)
+        st, Vn, Fn = _native_process(native_lib, V, F)
+        assert st == 0
+        Vp, Fp = mesh_process(V, F)
+        assert np.array_equal(Vn, Vp), trial
+        assert np.array_equal(Fn, Fp), trial
+
+
+def test_server_processing_rejects_bad_indices(native_lib):
+    V, F = meshes.octahedron()
+    F = F.copy()
+    F[0, 0] = len(V)
+    st, _, _ = _native_process(native_lib, V, F)
+    assert st != 0
