@@ -344,6 +344,14 @@ int pamo_safe_project(pamo_stage3* s, const double* gt_points, const int32_t* gt
  * counterpart (the reference logs these). */
 int pamo_stage3_stats(const pamo_stage3* s, double* out, int32_t n);
 
+/* The topology a stage-3 call builds on the host (no GPU): the unique edges in trimesh's edges_unique order
+ * (2 ints per edge, smaller endpoint first, ordered by (larger, smaller); room for 3 n_triangles edges) and the
+ * hinges of hinge_preprocess_slow_kernel (safe_project/.../hinge_energy.py:21-57; 4 ints per hinge: opposite
+ * vertex in t0, a, b, opposite vertex in t1, for every directed edge (a, b), a < b, of a face t0 and every face t1
+ * holding (b, a)). *n_hinges is the full count; PAMO_ERR_CAPACITY when it exceeds hinge_capacity. */
+int pamo_stage3_topology(const int32_t* triangles, int32_t n_points, int32_t n_triangles, int32_t* edges,
+                         int32_t* n_edges, int32_t* hinges, int32_t hinge_capacity, int32_t* n_hinges);
+
 /* ---------------------------------------------------------------- evaluation (metrics.py:7-107)
  * Squared distances from points to a triangle mesh, as igl.point_mesh_squared_distance and
  * trimesh.proximity.closest_point compute them for the reference's Chamfer and Hausdorff distances

@@ -93,6 +93,7 @@ SIGNATURES = {
     "pamo_server_stats": (ctypes.c_int, [_P, _PI64, _I32]),
     "pamo_server_job_bytes": (ctypes.c_int64, [_I32, _I32]),
     "pamo_mesh_process": (ctypes.c_int, [_P, _I32, _P, _I32, _P, _PI32, _P, _PI32]),
+    "pamo_stage3_topology": (ctypes.c_int, [_P, _I32, _I32, _P, _PI32, _P, _I32, _PI32]),
     "pamo_stage3_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int]),
     "pamo_stage3_destroy": (ctypes.c_int, [_P]),
     "pamo_stage3_last_error": (ctypes.c_char_p, [_P]),

@@ -2886,6 +2886,45 @@ void Stage3::newton_iteration() {
     note_launch();
 }
 
+// Topology of one call, on the host.
+// Edges: trimesh's edges_unique (the face edges with sorted endpoints, unique rows). For two int32 columns
+// trimesh hashes a row (u, v) as u ^ (v << 32) and np.unique sorts the hashes, so the edges come ordered by
+// (v, u); the same order is used here (it fixes which edge of an edge-edge pair is "first"). ukeys holds
+// v * n_points + u per edge, ascending.
+// Hinges: hinge_preprocess_slow_kernel (hinge_energy.py:21-57) pairs every directed edge (a, b), a < b, of a face
+// t0 with every face t1 holding the edge as (b, a): hinge (opposite in t0, a, b, opposite in t1), in the order of
+// t0's faces and corners, then of t1's faces and corners. Returns PAMO_ERR_INVALID_ARG for an index outside
+// [0, n_points).
+int stage3_topology(const int* hf, int n_points, int n_tris, std::vector<long long>& ukeys, std::vector<int4>& h4) {
+    std::vector<std::pair<long long, int>> dkeys;  // directed edge (a * n + b) -> face * 3 + corner
+    ukeys.clear();
+    h4.clear();
+    ukeys.reserve((size_t)3 * n_tris);
+    dkeys.reserve((size_t)3 * n_tris);
+    for (int f = 0; f < n_tris; ++f)
+        for (int k = 0; k < 3; ++k) {
+            const long long a = hf[3 * f + k], b = hf[3 * f + (k + 1) % 3];
+            if (a < 0 || b < 0 || a >= n_points || b >= n_points) return PAMO_ERR_INVALID_ARG;
+            ukeys.push_back(std::max(a, b) * n_points + std::min(a, b));
+            dkeys.push_back({a * n_points + b, 3 * f + k});
+        }
+    std::sort(ukeys.begin(), ukeys.end());
+    ukeys.erase(std::unique(ukeys.begin(), ukeys.end()), ukeys.end());
+    std::sort(dkeys.begin(), dkeys.end());
+    for (int f = 0; f < n_tris; ++f)
+        for (int k = 0; k < 3; ++k) {
+            const int a = hf[3 * f + k], b = hf[3 * f + (k + 1) % 3], c = hf[3 * f + (k + 2) % 3];
+            if (!(a < b)) continue;
+            const long long key = (long long)b * n_points + a;
+            auto it = std::lower_bound(dkeys.begin(), dkeys.end(), std::make_pair(key, -1));
+            for (; it != dkeys.end() && it->first == key; ++it) {
+                const int f1 = it->second / 3, k1 = it->second % 3;
+                h4.push_back(make_int4(c, a, b, hf[3 * f1 + (k1 + 2) % 3]));
+            }
+        }
+    return PAMO_OK;
+}
+
 int Stage3::run(const double* gt_points, const int* gt_tris, int n_gt_points, int n_gt_tris, const double* points,
                 const int* tris, int n_points, int n_tris, int n_iters, double* out_points, cudaStream_t caller) {
     int r = run_once(gt_points, gt_tris, n_gt_points, n_gt_tris, points, tris, n_points, n_tris, n_iters, out_points,
@@ -2908,12 +2947,7 @@ int Stage3::run_once(const double* gt_points, const int* gt_tris, int n_gt_point
     stats = Stage3Stats{};
     barrier_gave_up = false;
     if (n_points < 3 || n_tris < 1 || n_gt_points < 3 || n_gt_tris < 1) return fail(PAMO_ERR_INVALID_ARG, "empty mesh");
-    // Topology on the host, once per call.
-    // Edges: trimesh's edges_unique (the face edges with sorted endpoints, unique rows). For two int32
-    // columns trimesh hashes a row (u, v) as u ^ (v << 32) and np.unique sorts the hashes, so the edges come
-    // ordered by (v, u); the same order is used here (it fixes which edge of an edge-edge pair is "first").
-    // Hinges: hinge_preprocess_slow_kernel (hinge_energy.py:21-57) pairs every directed edge (a, b), a < b,
-    // of a face t0 with every face t1 holding the edge as (b, a): hinge (opposite in t0, a, b, opposite in t1).
+    // topology on the host, once per call (stage3_topology)
     std::vector<int> hf((size_t)3 * n_tris);
     // on the caller's stream, after the work that produced the triangles there (a non-blocking stream does not
     // order with a copy on the legacy default stream)
@@ -2921,31 +2955,8 @@ int Stage3::run_once(const double* gt_points, const int* gt_tris, int n_gt_point
         cudaStreamSynchronize(caller) != cudaSuccess)
         return fail(PAMO_ERR_CUDA, "copy of the triangles");
     std::vector<long long> ukeys;
-    std::vector<std::pair<long long, int>> dkeys;  // directed edge (a * n + b) -> face * 3 + corner
-    ukeys.reserve(hf.size());
-    dkeys.reserve(hf.size());
-    for (int f = 0; f < n_tris; ++f)
-        for (int k = 0; k < 3; ++k) {
-            const long long a = hf[3 * f + k], b = hf[3 * f + (k + 1) % 3];
-            if (a < 0 || b < 0 || a >= n_points || b >= n_points) return fail(PAMO_ERR_INVALID_ARG, "bad triangle index");
-            ukeys.push_back(std::max(a, b) * n_points + std::min(a, b));
-            dkeys.push_back({a * n_points + b, 3 * f + k});
-        }
-    std::sort(ukeys.begin(), ukeys.end());
-    ukeys.erase(std::unique(ukeys.begin(), ukeys.end()), ukeys.end());
-    std::sort(dkeys.begin(), dkeys.end());
     std::vector<int4> h4;
-    for (int f = 0; f < n_tris; ++f)
-        for (int k = 0; k < 3; ++k) {
-            const int a = hf[3 * f + k], b = hf[3 * f + (k + 1) % 3], c = hf[3 * f + (k + 2) % 3];
-            if (!(a < b)) continue;
-            const long long key = (long long)b * n_points + a;
-            auto it = std::lower_bound(dkeys.begin(), dkeys.end(), std::make_pair(key, -1));
-            for (; it != dkeys.end() && it->first == key; ++it) {
-                const int f1 = it->second / 3, k1 = it->second % 3;
-                h4.push_back(make_int4(c, a, b, hf[3 * f1 + (k1 + 2) % 3]));
-            }
-        }
+    if (stage3_topology(hf.data(), n_points, n_tris, ukeys, h4)) return fail(PAMO_ERR_INVALID_ARG, "bad triangle index");
     NP = n_points;
     NT = n_tris;
     NE = (int)ukeys.size();
@@ -3227,6 +3238,31 @@ int pamo_safe_project(pamo_stage3* s, const double* gt_points, const int32_t* gt
                                 n_triangles, n_iters, out_points, (cudaStream_t)stream);
     cudaSetDevice(prev);
     return r;
+}
+
+int pamo_stage3_topology(const int32_t* triangles, int32_t n_points, int32_t n_triangles, int32_t* edges,
+                         int32_t* n_edges, int32_t* hinges, int32_t hinge_capacity, int32_t* n_hinges) {
+    if (!triangles || n_points < 1 || n_triangles < 1 || !edges || !n_edges || !n_hinges || hinge_capacity < 0 ||
+        (hinge_capacity > 0 && !hinges))
+        return PAMO_ERR_INVALID_ARG;
+    std::vector<long long> ukeys;
+    std::vector<int4> h4;
+    const int r = pamo::stage3_topology(triangles, n_points, n_triangles, ukeys, h4);
+    if (r) return r;
+    for (size_t e = 0; e < ukeys.size(); ++e) {
+        edges[2 * e] = (int32_t)(ukeys[e] % n_points);
+        edges[2 * e + 1] = (int32_t)(ukeys[e] / n_points);
+    }
+    *n_edges = (int32_t)ukeys.size();
+    *n_hinges = (int32_t)h4.size();
+    if ((int64_t)h4.size() > hinge_capacity) return PAMO_ERR_CAPACITY;
+    for (size_t h = 0; h < h4.size(); ++h) {
+        hinges[4 * h] = h4[h].x;
+        hinges[4 * h + 1] = h4[h].y;
+        hinges[4 * h + 2] = h4[h].z;
+        hinges[4 * h + 3] = h4[h].w;
+    }
+    return PAMO_OK;
 }
 
 int pamo_stage3_stats(const pamo_stage3* s, double* out, int32_t n) {

@@ -64,6 +64,10 @@ struct Stage3Stats {
     int barrier_reruns = 0;        // 1: a grid barrier gave up and the run was made again without cooperative kernels
 };
 
+// The call's unique edges (v * n_points + u, ascending: trimesh's edges_unique order) and hinges, on the host
+int stage3_topology(const int* triangles, int n_points, int n_tris, std::vector<long long>& ukeys,
+                    std::vector<int4>& hinges);
+
 struct EnergyArgs;  // arguments of the energy kernels (safe_project.cu)
 
 class Stage3 {
