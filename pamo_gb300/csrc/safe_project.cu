@@ -2433,52 +2433,61 @@ void Stage3::release() {
 
 int Stage3::ensure(int np, int nt, int ne, int nh, int ngp, int ngt) {
     int rr;
+    // first call: stream, pool, events and the fixed-size buffers; a failure part-way releases what was made, so
+    // that the next call starts over
     if (!sc) {
-        if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return fail(PAMO_ERR_CUDA, "stream");
-        {
-            int dev0 = 0;
-            cudaGetDevice(&dev0);
-            cudaMemPoolProps props = {};
-            props.allocType = cudaMemAllocationTypePinned;
-            props.location.type = cudaMemLocationTypeDevice;
-            props.location.id = dev0;
-            if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) return fail(PAMO_ERR_CUDA, "memory pool");
-            unsigned long long keep = ~0ull;  // freed memory stays in the pool for the next growth
-            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        const int r0 = [&]() -> int {
+            if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return fail(PAMO_ERR_CUDA, "stream");
+            {
+                int dev0 = 0;
+                cudaGetDevice(&dev0);
+                cudaMemPoolProps props = {};
+                props.allocType = cudaMemAllocationTypePinned;
+                props.location.type = cudaMemLocationTypeDevice;
+                props.location.id = dev0;
+                if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) return fail(PAMO_ERR_CUDA, "memory pool");
+                unsigned long long keep = ~0ull;  // freed memory stays in the pool for the next growth
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            }
+            if (cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming) != cudaSuccess)
+                return fail(PAMO_ERR_CUDA, "event");
+            if (cudaMalloc((void**)&sc, sizeof(SolverScalars)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+            if (cudaMallocHost((void**)&h_sc, sizeof(SolverScalars)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMallocHost");
+            if (cudaMalloc((void**)&d_norm, (16 + 9 * kNormBlocks) * sizeof(double)) != cudaSuccess)
+                return fail(PAMO_ERR_OOM, "cudaMalloc");
+            if (cudaMalloc((void**)&partial, kPartials * sizeof(float2)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+            if (cudaMalloc((void**)&cg_bar, 64) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+            cudaMemset(cg_bar, 0, 64);
+            int dev = 0, nsm = 0, occ = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_solve<128>, 128, 0);
+            coop_max_blocks = std::max(1, nsm * std::max(occ, 0));
+            int occ_ls = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ls, k_line_search_coop, kT, 0);
+            ls_coop_max_blocks = nsm * std::max(occ_ls, 0);
+            n_sm = std::max(1, nsm);
+            // largest cluster the device runs k_cg_cluster with (16 needs the non-portable opt-in)
+            cluster_size = 1;
+            if (cudaFuncSetAttribute(k_cg_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(16);
+                cfg.blockDim = dim3(kClusterThreads);
+                int cs = 0;
+                if (cudaOccupancyMaxPotentialClusterSize(&cs, k_cg_cluster, &cfg) == cudaSuccess) cluster_size = std::min(cs, 16);
+            }
+            cudaGetLastError();  // a refused attribute leaves the cooperative path in use
+            if (cluster_size < 2) cluster_size = 1;
+            if (cudaMalloc((void**)&gt_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+            if (cudaMalloc((void**)&tri_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+            if (cudaMalloc((void**)&edge_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
+            return PAMO_OK;
+        }();
+        if (r0) {
+            release();
+            return r0;
         }
-        if (cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming) != cudaSuccess)
-            return fail(PAMO_ERR_CUDA, "event");
-        if (cudaMalloc((void**)&sc, sizeof(SolverScalars)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
-        if (cudaMallocHost((void**)&h_sc, sizeof(SolverScalars)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMallocHost");
-        if (cudaMalloc((void**)&d_norm, (16 + 9 * kNormBlocks) * sizeof(double)) != cudaSuccess)
-            return fail(PAMO_ERR_OOM, "cudaMalloc");
-        if (cudaMalloc((void**)&partial, kPartials * sizeof(float2)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
-        if (cudaMalloc((void**)&cg_bar, 64) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
-        cudaMemset(cg_bar, 0, 64);
-        int dev = 0, nsm = 0, occ = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_cg_solve<128>, 128, 0);
-        coop_max_blocks = std::max(1, nsm * std::max(occ, 0));
-        int occ_ls = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_ls, k_line_search_coop, kT, 0);
-        ls_coop_max_blocks = nsm * std::max(occ_ls, 0);
-        n_sm = std::max(1, nsm);
-        // largest cluster the device runs k_cg_cluster with (16 needs the non-portable opt-in)
-        cluster_size = 1;
-        if (cudaFuncSetAttribute(k_cg_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3(16);
-            cfg.blockDim = dim3(kClusterThreads);
-            int cs = 0;
-            if (cudaOccupancyMaxPotentialClusterSize(&cs, k_cg_cluster, &cfg) == cudaSuccess) cluster_size = std::min(cs, 16);
-        }
-        cudaGetLastError();  // a refused attribute leaves the cooperative path in use
-        if (cluster_size < 2) cluster_size = 1;
-        if (cudaMalloc((void**)&gt_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
-        if (cudaMalloc((void**)&tri_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
-        if (cudaMalloc((void**)&edge_rc, sizeof(RoundCounters)) != cudaSuccess) return fail(PAMO_ERR_OOM, "cudaMalloc");
     }
     size_t c;
     if (cap_gp < (size_t)ngp + 2) {
