@@ -880,8 +880,9 @@ def main():
             precision = {"stage3_max_abs_err": float(np.abs(got - ref3).max()),
                          "stage3_max_err_over_bbox_diag": float(np.abs(got - ref3).max() / diag),
                          "against": "float64 oracle run of stage 3 on the same stage-2 output",
-                         "arithmetic": "float32 with compensated (two-sum) energy and CG sums; float64 for the "
-                                       "CCD step, the normalisation, Voronoi weights and angle test"}
+                         "arithmetic": "float32 with compensated (two-sum) energy and CG sums; double-float "
+                                       "(hi + lo float pairs) for the CCD step; float64 for the normalisation, "
+                                       "Voronoi weights and angle test"}
         # conventional CPU baseline: sequential priority-queue QEM (one host thread) on a time budget, projected to
         # the collapses the job needs (each removes two faces)
         t_q = time.perf_counter()
