@@ -883,6 +883,18 @@ def main():
                          "arithmetic": "float32 with compensated (two-sum) energy and CG sums; double-float "
                                        "(hi + lo float pairs) for the CCD step; float64 for the normalisation, "
                                        "Voronoi weights and angle test"}
+            # the same projection with the CCD roots in float64 (ccd_fp64=1), beside the double-float default
+            try:
+                from pamo_gb300 import safe_project as sp3
+
+                s3_64 = sp3.Stage3System(sp3.Stage3Config(ccd_fp64=1), dev)
+                got64 = s3_64.project(gt_v, tri, v2[0], v2[1], STAGE3_STEPS).cpu().numpy()
+                del s3_64
+                precision["fp64_ccd_roots"] = {
+                    "stage3_max_err_over_bbox_diag": float(np.abs(got64 - ref3).max() / diag),
+                    "identical_to_default": bool(np.array_equal(got64, got))}
+            except Exception as e:  # an auxiliary figure: the bench line stands without it
+                precision["fp64_ccd_roots"] = {"unavailable": f"{type(e).__name__}: {e}"}
         # conventional CPU baseline: sequential priority-queue QEM (one host thread) on a time budget, projected to
         # the collapses the job needs (each removes two faces)
         t_q = time.perf_counter()
